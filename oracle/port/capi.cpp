@@ -1,0 +1,284 @@
+// capi.cpp -- TEST INFRASTRUCTURE (CPU restatement, see port.h).
+// extern "C" entry points of the restatement, with the same argument conventions as the
+// reference shim (oracle/ref_shim.cpp) so that tests can call either through ctypes.
+#include <cstring>
+#include <string>
+
+#include "mg.h"
+#include "port.h"
+#include "twophase.h"
+
+using namespace port;
+
+extern "C" {
+
+int port_bc_fill(int ndim, const int *n, const double *lo, const double *hi, int location, const int *types,
+                 const double *values, double *f) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    bc_fill(g, location, types, values, f);
+    return 0;
+}
+
+int port_flux_extrapolate(int ndim, const int *n, int location, const double *data, double *flux) {
+    double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    Grid g = make_grid(ndim, n, lo, hi);
+    flux_extrapolate(g, location, data, flux);
+    return 0;
+}
+
+int port_zero_order_extrapolation(int ndim, const int *n, double *f) {
+    double lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    Grid g = make_grid(ndim, n, lo, hi);
+    zero_order_extrapolation(g, f);
+    return 0;
+}
+
+int port_uccd(int ndim, const int *n, const double *lo, const double *hi, const double *flux, const double *u,
+              const double *v, const double *w, double *out) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const size_t N = g.size();
+    std::memset(out, 0, 6 * N * sizeof(double));
+    Compact c(g);
+    const double *vel[3] = {u, v, w};
+    for (int a = 0; a < ndim; ++a) c.uccd_axis(a, flux, vel[a], out + a * N, out + (3 + a) * N);
+    return 0;
+}
+
+int port_ccd(int ndim, const int *n, const double *lo, const double *hi, int mixed, const double *flux, double *out) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const size_t N = g.size();
+    std::memset(out, 0, 9 * N * sizeof(double));
+    Compact c(g);
+    for (int a = 0; a < ndim; ++a) c.ccd_axis(a, flux, out + a * N, out + (3 + a) * N);
+    if (mixed) {
+        if (ndim > 1) c.ccd_mixed(1, out + 0 * N, out + 6 * N);
+        if (ndim > 2) {
+            c.ccd_mixed(2, out + 1 * N, out + 7 * N);
+            c.ccd_mixed(0, out + 2 * N, out + 8 * N);
+        }
+    }
+    return 0;
+}
+
+int port_weno5(int ndim, const int *n, const double *lo, const double *hi, const double *flux, const double *u,
+               const double *v, const double *w, double *out) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const size_t N = g.size();
+    std::memset(out, 0, 3 * N * sizeof(double));
+    Field fh(N, 0.0);
+    const double *vel[3] = {u, v, w};
+    for (int a = 0; a < ndim; ++a) weno5_axis(g, a, flux, vel[a], out + a * N, fh.data());
+    return 0;
+}
+
+int port_godunov(int ndim, const int *n, const double *lo, const double *hi, const double *phi, const double *sign,
+                 double *grad) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    godunov_gradient(g, phi, sign, grad);
+    return 0;
+}
+
+int port_lsf_fields(int ndim, const int *n, const double *lo, const double *hi, const double *prm, const double *phi,
+                    double *out) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const size_t N = g.size();
+    const double w = prm[0], dr = prm[1], vr = prm[2];
+    const bool pos = prm[3] != 0.0;
+    for (size_t q = 0; q < N; ++q) {
+        const double h = heaviside(phi[q], w);
+        out[q] = h;
+        out[N + q] = delta(phi[q], w);
+        out[2 * N + q] = sign_fn(phi[q], w);
+        out[3 * N + q] = pos ? h + (1.0 - h) * dr : (1.0 - h) + h * dr;
+        out[4 * N + q] = pos ? h + (1.0 - h) * vr : (1.0 - h) + h * vr;
+    }
+    Field flux(N), d[9];
+    for (auto &f : d) f.assign(N, 0.0);
+    flux_extrapolate(g, LOC_NODE, phi, flux.data());
+    Compact c(g);
+    for (int a = 0; a < ndim; ++a) c.ccd_axis(a, flux.data(), d[a].data(), d[3 + a].data());
+    if (ndim > 1) c.ccd_mixed(1, d[0].data(), d[6].data());
+    if (ndim > 2) {
+        c.ccd_mixed(2, d[1].data(), d[7].data());
+        c.ccd_mixed(0, d[2].data(), d[8].data());
+    }
+    find_curvature(g, phi, d[0].data(), d[1].data(), d[2].data(), d[3].data(), d[4].data(), d[5].data(), d[6].data(),
+                   d[7].data(), d[8].data(), out + 5 * N);
+    return 0;
+}
+
+int port_lsf_integrals(int ndim, const int *n, const double *lo, const double *hi, const double *prm,
+                       const double *phi, double *out) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    Params p;
+    p.ls_width = prm[0];
+    p.density_ratio = prm[1];
+    p.viscosity_ratio = prm[2];
+    p.positive_ref = prm[3] != 0.0;
+    Field H(g.size()), rho(g.size());
+    out[0] = lsf_mass(g, p, phi, H.data(), rho.data());
+    out[1] = lsf_volume(g, p, phi, H.data());
+    return 0;
+}
+
+int port_mg_levels(int ndim, const int *n, int *level_n, int max_levels) {
+    return ref_mg_levels(ndim, n, level_n, max_levels);
+}
+
+// The reference multigrid to a relative residual (see ref_mg_poisson in the shim).
+int port_mg_poisson(int ndim, const int *n, const double *lo, const double *hi, int dirichlet, int full,
+                    const double *rhs, double *sol, double rel_tol, int max_cycles, int *cycles, double *hist) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    RefMG mg;
+    double d[3] = {g.d[0], g.d[1], ndim == 3 ? g.d[2] : 1.0};
+    mg.build(ndim, g.n, d, dirichlet != 0);
+    MGLevel &L0 = mg.at[0];
+    for (int q = 0; q < L0.n; ++q) L0.rhs[q] = rhs[q];
+    double bn = 0.0;
+    for (int q = 0; q < L0.n; ++q) bn += rhs[q] * rhs[q];
+    bn = std::sqrt(bn);
+    int it = 0;
+    double rel = L0.residual() / bn;
+    if (hist) hist[0] = rel;
+    while (rel > rel_tol && it < max_cycles) {
+        if (full) mg.full_cycle();
+        else mg.v_cycle();
+        ++it;
+        rel = L0.residual() / bn;
+        if (hist) hist[it] = rel;
+    }
+    for (int q = 0; q < L0.n; ++q) sol[q] = L0.sol[q];
+    *cycles = it;
+    return 0;
+}
+
+// Variable-coefficient pressure equation of projection() on a given density field: the
+// coefficients of init_ppe_proj_coefficients, rhs on interior cells, exact CG solve.
+// rho, rhs, p are ghosted fields; p carries the initial guess and receives the solution.
+int port_coef_solve(int ndim, const int *n, const double *lo, const double *hi, const double *rho,
+                    const double *rhs, double *p, double rel_tol, int max_iter, double *relres) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    int vb[6] = {2, 2, 2, 2, 2, 2}, sb[6] = {1, 1, 1, 1, 1, 1}, opt[5] = {0, 0, 0, 2, 1};
+    Params prm;
+    TwoPhase tp(g, vb, sb, prm, opt);
+    tp.rho.assign(rho, rho + g.size());
+    tp.ppe_coefficients(false);
+    return coef_cg_solve(g, tp.CC.data(), tp.CR.data(), tp.CL.data(), tp.CU.data(), tp.CD.data(), tp.CF.data(),
+                         tp.CB.data(), rhs, p, rel_tol, max_iter, relres);
+}
+
+// ---------------------------------------------------------------- two-phase state
+void *port_tp_create(int ndim, const int *n, const double *lo, const double *hi, const int *vel_bc,
+                     const int *scalar_bc, const double *prm, const int *opt) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    Params p;
+    p.density_ratio = prm[0];
+    p.viscosity_ratio = prm[1];
+    p.Re = prm[2];
+    p.Fr = prm[3];
+    p.We = prm[4];
+    p.ls_width = prm[5];
+    p.rdt = prm[6];
+    p.max_CFL = prm[7];
+    p.min_CFL = prm[8];
+    p.positive_ref = prm[9] != 0.0;
+    p.ppe_tol = prm[10];
+    p.ppe_tol2 = prm[11];
+    p.ppe_max_iter = int(prm[12]);
+    p.ppe_omega = prm[13];
+    p.ppe_initer = int(prm[14]);
+    p.dt = prm[15];
+    return new TwoPhase(g, vel_bc, scalar_bc, p, opt);
+}
+
+void port_tp_destroy(void *h) { delete static_cast<TwoPhase *>(h); }
+
+int port_tp_set(void *h, const char *name, const double *src) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    Field *f = tp->field(name);
+    if (!f) return -1;
+    std::memcpy(f->data(), src, f->size() * sizeof(double));
+    return 0;
+}
+
+int port_tp_get(void *h, const char *name, double *dst) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    Field *f = tp->field(name);
+    if (!f) return -1;
+    std::memcpy(dst, f->data(), f->size() * sizeof(double));
+    return 0;
+}
+
+int port_tp_scalars(void *h, double *out) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    out[0] = tp->p.t;
+    out[1] = tp->p.dt;
+    out[2] = tp->p.dt_old;
+    out[3] = tp->p.dt_old2;
+    out[4] = tp->p.iter;
+    out[5] = tp->p.stable_CFL;
+    out[6] = tp->p.lsf_mass0;
+    return 0;
+}
+
+int port_tp_set_scalars(void *h, const double *in) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    tp->p.t = in[0];
+    tp->p.dt = in[1];
+    tp->p.dt_old = in[2];
+    tp->p.dt_old2 = in[3];
+    tp->p.iter = int(in[4]);
+    tp->p.stable_CFL = in[5];
+    tp->p.lsf_mass0 = in[6];
+    return 0;
+}
+
+int port_tp_set_exact_tol(void *h, double tol) {
+    static_cast<TwoPhase *>(h)->exact_tol = tol;
+    return 0;
+}
+
+int port_tp_init(void *h) {
+    static_cast<TwoPhase *>(h)->init();
+    return 0;
+}
+int port_tp_find_dt(void *h) {
+    static_cast<TwoPhase *>(h)->find_dt();
+    return 0;
+}
+int port_tp_advect(void *h) {
+    static_cast<TwoPhase *>(h)->advect();
+    return 0;
+}
+int port_tp_mpls(void *h, int count) {
+    static_cast<TwoPhase *>(h)->mpls(count);
+    return 0;
+}
+int port_tp_reinit(void *h) { return static_cast<TwoPhase *>(h)->reinit(); }
+int port_tp_find_source(void *h) {
+    static_cast<TwoPhase *>(h)->find_source();
+    return 0;
+}
+int port_tp_ab_solve(void *h) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    tp->ab_solve();
+    return tp->last_ppe_iters;
+}
+int port_tp_projection(void *h) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    tp->ppe_coefficients(false);
+    return tp->projection(tp->ppe_mode == 2);
+}
+int port_tp_step(void *h, int nsteps) {
+    static_cast<TwoPhase *>(h)->step(nsteps);
+    return 0;
+}
+int port_tp_diagnostics(void *h, double *out) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    out[0] = tp->mass();
+    out[1] = tp->volume();
+    out[2] = tp->divergence();
+    return 0;
+}
+
+}  // extern "C"
