@@ -1,0 +1,204 @@
+/*
+ * scihpc_gpu.h -- C ABI of the GB300 (sm_103a) two-phase projection-step library.
+ *
+ * The reference (luisleo526/SciHPC) has no FFI: its boundary is the C++ class API of
+ * scihpc/*.h.  Each entry point below replaces one reference function or method on that
+ * path and cites it.  Conventions:
+ *
+ *   - Every function returns an int status (SCIHPC_OK = 0).  scihpc_last_error() gives a
+ *     message for the last failure on the calling thread.
+ *   - Field arguments are DEVICE pointers to FP64 arrays laid out like the reference's
+ *     scalar_data arrays: [Nx][Ny][Nz], k fastest, ghost width 3 on every active axis
+ *     (Nx = nx + 6; Ny = ny + 6 when ndim >= 2, else 1; Nz = nz + 6 when ndim == 3, else 1).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).  Calls are
+ *     asynchronous unless their comment says they return a host value.
+ *   - Boundary codes: 0 periodic, 1 neumann, 2 no_slip, 3 slip, 4 dirichlet
+ *     (bc_factory.h:18-22).  Face order in 6-arrays: xl, xr, yl, yr, zl, zr
+ *     (argument order of the bc_factory / wrapper constructors, bc_factory.h:42-48).
+ *   - Locations: 0 cell-centred ("node"), 1/2/3 staggered in x/y/z ("face"), as in
+ *     bc_factory::apply_node_centered / apply_node_staggered_{x,y,z} (bc_factory.h:53-56).
+ */
+#ifndef SCIHPC_GPU_H
+#define SCIHPC_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCIHPC_OK 0
+#define SCIHPC_ERR_ARG 1
+#define SCIHPC_ERR_CUDA 2
+#define SCIHPC_ERR_NONFINITE 3
+#define SCIHPC_ERR_MAXITER 4
+#define SCIHPC_ERR_UNSUPPORTED 5
+#define SCIHPC_ERR_NOMEM 6
+
+/* Uniform cell-centred grid (structured_grid.h:10-30): n interior cells on [lo, hi] per axis. */
+typedef struct scihpc_grid {
+    int ndim;       /* 1, 2 or 3 */
+    int n[3];       /* interior cells per axis (ignored beyond ndim) */
+    double lo[3];   /* axis start (axis::start, global.h:20-23) */
+    double hi[3];   /* axis end   (axis::end) */
+} scihpc_grid;
+
+/* Message of the last failure on this thread (empty string when none). */
+const char *scihpc_last_error(void);
+
+/* Library version string. */
+const char *scihpc_version(void);
+
+/* ------------------------------------------------------------------ context
+ * Per-grid device state shared by the kernel-level calls: factored compact-scheme line
+ * operators for every axis (uccd_base.cpp:7-118, ccd_base.cpp:7-105), scratch fields and
+ * reduction buffers.  Replaces the per-grid solver objects that SharedSolvers_alloc builds
+ * (shared_solvers.cpp:7-15).  Allocates device memory; must not be called during capture. */
+typedef struct scihpc_ctx scihpc_ctx;
+int scihpc_ctx_create(const scihpc_grid *grid, scihpc_ctx **out);
+int scihpc_ctx_destroy(scihpc_ctx *ctx);
+
+/* ------------------------------------------------------------------ boundary fills
+ * Ghost fill of one field: bc_factory::apply_node_centered (location 0) and
+ * apply_node_staggered_{x,y,z} (locations 1..3) with the per-face kernels of periodic.cpp,
+ * neumann.cpp, no_slip.cpp, slip.cpp and dirichlet.cpp (bc_factory.cpp:123-437).
+ * values[f] is bc_info::value of face f (bc_factory.h:24-27). */
+int scihpc_bc_fill(scihpc_ctx *ctx, int location, const int types[6], const double values[6], double *f,
+                   void *stream);
+
+/* flux <- data with zero-order ghost extrapolation: identity_with_extrapolation (location 0)
+ * and identity_with_extrapolation_face_{x,y,z} (locations 1..3) (flux.cpp:98-330). */
+int scihpc_flux_extrapolate(scihpc_ctx *ctx, int location, const double *data, double *flux, void *stream);
+
+/* zero_order_extrapolation of a raw ghosted array, in place (simple_bc.cpp:7-43). */
+int scihpc_zero_order_extrapolation(scihpc_ctx *ctx, double *f, void *stream);
+
+/* ------------------------------------------------------------------ compact schemes
+ * UCCD first/second derivative along `axis` (0..2) of every grid line, upwinded by the
+ * sign of vel_axis: uccd_solver::find_fx / find_fy / find_fz (uccd_solver.cpp:14-209).
+ * f1 receives f_axis, f2 receives f_axis,axis. */
+int scihpc_uccd(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *f1, double *f2,
+                void *stream);
+
+/* Central CCD first/second derivative along `axis`: ccd_solver::find_fx / find_fy /
+ * find_fz (ccd_solver.cpp:14-141). */
+int scihpc_ccd(scihpc_ctx *ctx, int axis, const double *flux, double *f1, double *f2, void *stream);
+
+/* Mixed derivative: src (a first derivative) is zero-order extrapolated along `axis` in
+ * place, then out = its CCD derivative along `axis`.  axis 1 with src = f_x gives f_xy
+ * (ccd_solver::mixed_xy), axis 2 with f_y gives f_yz (mixed_yz), axis 0 with f_z gives
+ * f_zx (mixed_zx) (ccd_solver.cpp:143-282). */
+int scihpc_ccd_mixed(scihpc_ctx *ctx, int axis, double *src, double *out, void *stream);
+
+/* WENO5 (WENO-Z weights) derivative along `axis` on interior cells, faces upwinded by the
+ * sign of vel_i + vel_{i+1}: weno_solver::weno5_find_fx / fy / fz
+ * (weno_solver.cpp:68-268).  Ghost cells of fa are not written. */
+int scihpc_weno5(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *fa, void *stream);
+
+/* ------------------------------------------------------------------ level-set helpers
+ * Godunov |grad phi| on interior cells, 0 on ghosts (godunov_gradient.cpp:7-157). */
+int scihpc_godunov_gradient(scihpc_ctx *ctx, const double *phi, const double *sign, double *grad, void *stream);
+
+/* Smoothed Heaviside, delta, sign, density and viscosity of phi on every cell
+ * (lsm.cpp:8-43; wrapper_func.cpp:9-40,387-418).  prm = {ls_width, density_ratio,
+ * viscosity_ratio, positive_ref}.  Any output may be NULL. */
+int scihpc_lsf_fields(scihpc_ctx *ctx, const double prm[4], const double *phi, double *heaviside, double *delta,
+                      double *sign, double *density, double *viscosity, void *stream);
+
+/* Curvature from phi and its CCD derivatives d[9] = {fx, fy, fz, fxx, fyy, fzz, fxy, fyz,
+ * fzx} with the reference's correction (wrapper_func.cpp:115-174). */
+int scihpc_curvature(scihpc_ctx *ctx, const double *phi, const double *const d[9], double *curv, void *stream);
+
+/* lsf_mass and lsf_volume of phi (wrapper_func.cpp:450-572); returns both on the host
+ * (synchronises `stream`).  out[0] = mass, out[1] = volume. */
+int scihpc_lsf_integrals(scihpc_ctx *ctx, const double prm[4], const double *phi, double out[2], void *stream);
+
+/* ------------------------------------------------------------------ pressure Poisson
+ * Multigrid solver of the pressure equation of projection_method::projection
+ * (projection_method.cpp:404-465,544-627):
+ *     sum_faces C_f (p_nb - p_c) = rhs   on interior cells,
+ * C_f = 1 / (0.5 (rho_c + rho_nb)) / d^2 (density mode) or 1 / d^2 (constant mode).
+ * Walls: bc = 0 Neumann (C_f = 0 at the wall, solution normalised to zero mean, as the
+ * reference's SOR does every sweep); bc = 1 the reference multigrid's Dirichlet operator,
+ * which keeps the wall term with a zero ghost-centre value (multigrid_base.cpp:293-345).
+ * precision = 0: V-cycles in FP64; 1: V-cycles in FP32 inside the FP64 outer iteration
+ * (the residual, the correction sum and the solution stay FP64).
+ * Red-black Gauss-Seidel V(2,2) cycles, cell-average restriction, (bi/tri)linear
+ * prolongation, FP64 dense direct solve on the coarsest level (levels coarsened by the
+ * rule of multigrid.cpp:8-41), used as the preconditioner of an FP64 conjugate-gradient
+ * outer iteration.  Replaces the reference's SOR sweep loop and multigrid::v_cycle /
+ * full_cycle (multigrid.cpp:43-79).  Allocates device memory at creation. */
+typedef struct scihpc_poisson scihpc_poisson;
+int scihpc_poisson_create(const scihpc_grid *grid, int bc, int density_mode, int precision, scihpc_poisson **out);
+int scihpc_poisson_destroy(scihpc_poisson *ps);
+/* Coefficients from a ghosted density field (dummy_data::density); call again whenever it
+ * changes (init_ppe_proj_coefficients, projection_method.cpp:404-465). */
+int scihpc_poisson_set_density(scihpc_poisson *ps, const double *rho, void *stream);
+/* Solve to ||rhs - A p|| <= rel_tol ||rhs|| (2-norms over interior cells) or max_iter
+ * outer iterations.  rhs and p are ghosted fields; p holds the initial guess (use_guess = 1)
+ * or is zeroed first (use_guess = 0); only interior cells of p are written.  Returns the
+ * iterations and the final relative residual on the host (synchronises `stream`). */
+int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int use_guess, double rel_tol,
+                         int max_iter, int *iters, double *relres, void *stream);
+/* Level sizes of the hierarchy (3 ints per level); returns the level count. */
+int scihpc_poisson_levels(scihpc_poisson *ps, int *level_n, int max_levels);
+
+/* ------------------------------------------------------------------ two-phase time step
+ * One complete two-phase problem resident on the GPU, assembled like the reference drivers
+ * (benchmarks_2d_bubble_rising.cpp:19-89): phi and pressure scalars, staggered velocity and
+ * node velocity vectors, dummy scratch, projection sources and Runge-Kutta stages.
+ * prm[16] = {density_ratio, viscosity_ratio, Re, Fr, We, ls_width, rdt, max_CFL, min_CFL,
+ *            positive_ref, ppe_tol, ppe_tol2, ppe_max_iter, ppe_omega, ppe_initer, dt0}
+ *            (problem_parameters, global.h:25-54; ppe_tol is the relative residual of the
+ *            multigrid pressure solve, ppe_max_iter its outer-iteration cap).
+ * opt[5]  = {convection scheme (0 UCCD, 1 WENO5), mass-correction Euler steps per step,
+ *            reinitialise every k steps (0 never), pressure precision (0 FP64 V-cycles,
+ *            1 FP32 V-cycles with FP64 refinement), reinit with lambda correction (1/0)}. */
+typedef struct scihpc_twophase scihpc_twophase;
+int scihpc_twophase_create(const scihpc_grid *grid, const int vel_bc[6], const int scalar_bc[6], const double prm[16],
+                           const int opt[5], scihpc_twophase **out);
+int scihpc_twophase_destroy(scihpc_twophase *tp);
+/* Copy one named field between HOST memory and the device state (synchronous).  Names:
+ * phi, p, p_old, p_old2, u, v, w (staggered velocity), nu, nv, nw (node velocity), rho,
+ * mu, delta, heaviside, curvature, sign, grad, u_src, v_src, w_src, u_src_old, v_src_old,
+ * w_src_old, rhs. */
+int scihpc_twophase_upload(scihpc_twophase *tp, const char *name, const double *host);
+int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host);
+/* Device pointer of a named field (for zero-copy use by callers). */
+int scihpc_twophase_field(scihpc_twophase *tp, const char *name, double **dev);
+/* Scalars {t, dt, dt_old, dt_old2, iter, stable_CFL, lsf_mass0}. */
+int scihpc_twophase_get_scalars(scihpc_twophase *tp, double out[7]);
+int scihpc_twophase_set_scalars(scihpc_twophase *tp, const double in[7]);
+/* Start-up of the drivers: scalar BC, find_source, lsf_mass0
+ * (benchmarks_2d_bubble_rising.cpp:51,88-89). */
+int scihpc_twophase_init(scihpc_twophase *tp);
+/* Pieces of the step, for parity checks of each stage:
+ * find_dt (wrapper_func.cpp:335-385); tvd_rk3 with convection (runge_kutta.cpp:13-49,
+ * source.cpp:8-40); `count` Euler steps with mpls (runge_kutta.cpp:51-63, source.cpp:109-154);
+ * the reinitialisation loop with lsf_redistance_lambda (benchmarks_2d_bubble_rising.cpp:
+ * 122-129, source.cpp:156-241), returning its RK3 step count in *steps; find_source
+ * (projection_method.cpp:244-312); ab_solve with the multigrid pressure solve
+ * (projection_method.cpp:755-777), returning the solver's iterations and relative
+ * residual. */
+int scihpc_twophase_find_dt(scihpc_twophase *tp);
+int scihpc_twophase_advect(scihpc_twophase *tp);
+int scihpc_twophase_mpls(scihpc_twophase *tp, int count);
+int scihpc_twophase_reinit(scihpc_twophase *tp, int *steps);
+int scihpc_twophase_find_source(scihpc_twophase *tp);
+int scihpc_twophase_ab_solve(scihpc_twophase *tp, int *iters, double *relres);
+/* nsteps time steps of the drivers' loop (benchmarks_2d_bubble_rising.cpp:100-130):
+ * find_dt, advection, mass correction, ab_solve, reinitialisation.  use_graph = 1 replays
+ * a captured CUDA graph per step (the pressure solve iterates inside it under a device-side
+ * convergence test).  Asynchronous on the problem's own stream unless `sync`. */
+int scihpc_twophase_step(scihpc_twophase *tp, int nsteps, int use_graph, int sync);
+/* lsf_mass, lsf_volume and the maximum |div u| (wrapper_func.cpp:295-333,450-572),
+ * on the host (synchronises). */
+int scihpc_twophase_diagnostics(scihpc_twophase *tp, double out[3]);
+/* The problem's CUDA stream (cudaStream_t as void*). */
+int scihpc_twophase_stream(scihpc_twophase *tp, void **stream);
+/* Statistics of the last pressure solve: {iterations, relative residual, ms}. */
+int scihpc_twophase_ppe_stats(scihpc_twophase *tp, double out[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCIHPC_GPU_H */

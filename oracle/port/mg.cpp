@@ -324,20 +324,30 @@ int coef_cg_solve(const Grid &g, const double *CC, const double *CR, const doubl
     if (bnorm == 0.0) bnorm = 1.0;
     applyM(x, Md);
     for (size_t t = 0; t < n; ++t) r[t] = b[t] - Md[t];
+    // Jacobi preconditioner.  z is not projected: D^-1 stays symmetric, the constant
+    // component it adds to x is removed once at the end.
     auto precond = [&]() {
         for (size_t t = 0; t < n; ++t) z[t] = r[t] / (-CC[idx[t]]);
-        remove_mean(z);
     };
     precond();
     d = z;
     double rz = 0.0;
     for (size_t t = 0; t < n; ++t) rz += r[t] * z[t];
     int it = 0;
-    double rel = 0.0;
+    double rel = 0.0, best = 1e300;
+    int since_best = 0;
+    std::vector<double> xbest = x;
     for (; it < max_iter; ++it) {
         double rn = 0.0;
         for (double e : r) rn += e * e;
         rel = std::sqrt(rn) / bnorm;
+        if (rel < best) {
+            best = rel;
+            xbest = x;
+            since_best = 0;
+        } else if (++since_best > 2000) {
+            break;   // stagnated at the attainable accuracy
+        }
         if (rel <= rel_tol) break;
         applyM(d, Md);
         double dMd = 0.0;
@@ -358,9 +368,10 @@ int coef_cg_solve(const Grid &g, const double *CC, const double *CR, const doubl
         rz = rz2;
         for (size_t t = 0; t < n; ++t) d[t] = z[t] + beta * d[t];
     }
+    x = xbest;
     remove_mean(x);
     for (size_t t = 0; t < n; ++t) p[idx[t]] = x[t];
-    if (relres) *relres = rel;
+    if (relres) *relres = best;
     return it;
 }
 

@@ -1,0 +1,434 @@
+// capi.cu -- the extern "C" entry points declared in include/scihpc_gpu.h.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "common.cuh"
+#include "compact.cuh"
+#include "levelset.cuh"
+#include "poisson.cuh"
+#include "reduce.cuh"
+#include "twophase.cuh"
+
+namespace scihpc {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_last_error = buf;
+    return e == cudaErrorMemoryAllocation ? SCIHPC_ERR_NOMEM : SCIHPC_ERR_CUDA;
+}
+
+// structured_grid.cpp:7-134 -- d = (end - start) / n, h = min d, dv = prod d.
+Dims make_dims(const scihpc_grid *g) {
+    Dims D{};
+    D.ndim = g->ndim;
+    for (int a = 0; a < 3; ++a) {
+        const bool act = a < g->ndim;
+        D.n[a] = act ? g->n[a] : 1;
+        D.N[a] = act ? g->n[a] + 2 * GHC : 1;
+        D.d[a] = act ? (g->hi[a] - g->lo[a]) / static_cast<double>(g->n[a]) : 0.0;
+        D.lo[a] = act ? g->lo[a] : 0.0;
+    }
+    D.s[2] = 1;
+    D.s[1] = D.N[2];
+    D.s[0] = (long long)D.N[1] * D.N[2];
+    if (D.ndim == 1) {
+        D.h = D.d[0];
+        D.dv = D.d[0];
+    } else if (D.ndim == 2) {
+        D.h = D.d[0] < D.d[1] ? D.d[0] : D.d[1];
+        D.dv = D.d[0] * D.d[1];
+    } else {
+        D.h = D.d[0] < D.d[1] ? D.d[0] : D.d[1];
+        D.h = D.h < D.d[2] ? D.h : D.d[2];
+        D.dv = D.d[0] * D.d[1] * D.d[2];
+    }
+    return D;
+}
+
+static int check_grid(const scihpc_grid *g) {
+    if (!g || g->ndim < 1 || g->ndim > 3) {
+        set_last_error("grid: ndim must be 1, 2 or 3");
+        return SCIHPC_ERR_ARG;
+    }
+    for (int a = 0; a < g->ndim; ++a) {
+        if (g->n[a] < 3 || !(g->hi[a] > g->lo[a])) {
+            set_last_error("grid: every active axis needs n >= 3 and hi > lo");
+            return SCIHPC_ERR_ARG;
+        }
+    }
+    return SCIHPC_OK;
+}
+
+}  // namespace scihpc
+
+using namespace scihpc;
+
+struct scihpc_ctx {
+    Dims D;
+    CompactOps ops;
+    double *t1 = nullptr, *t2 = nullptr, *work = nullptr, *partial = nullptr, *red = nullptr;
+};
+
+struct scihpc_poisson {
+    Poisson ps;
+};
+
+struct scihpc_twophase {
+    TwoPhaseGpu tp;
+};
+
+static inline cudaStream_t S(void *s) { return static_cast<cudaStream_t>(s); }
+
+#define CHECK_LAUNCH()                                             \
+    do {                                                           \
+        cudaError_t e_ = cudaGetLastError();                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, "kernel launch", __FILE__, __LINE__); \
+    } while (0)
+
+#define REQUIRE(cond, msg)           \
+    do {                             \
+        if (!(cond)) {               \
+            set_last_error(msg);     \
+            return SCIHPC_ERR_ARG;   \
+        }                            \
+    } while (0)
+
+extern "C" {
+
+const char *scihpc_last_error(void) { return g_last_error.c_str(); }
+
+const char *scihpc_version(void) { return "scihpc_gb300 0.1 (sm_103a)"; }
+
+int scihpc_ctx_create(const scihpc_grid *grid, scihpc_ctx **out) {
+    REQUIRE(out, "ctx_create: out is NULL");
+    int rc = check_grid(grid);
+    if (rc) return rc;
+    auto *c = new (std::nothrow) scihpc_ctx;
+    if (!c) return SCIHPC_ERR_NOMEM;
+    c->D = make_dims(grid);
+    rc = c->ops.build(c->D);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    const size_t bytes = size_t(c->D.size()) * sizeof(double);
+    SCIHPC_CUDA(cudaMalloc(&c->t1, 3 * bytes));
+    c->t2 = c->t1 + c->D.size();
+    c->work = c->t2 + c->D.size();
+    SCIHPC_CUDA(cudaMalloc(&c->partial, (RED_MAX_BLOCKS + 8) * sizeof(double)));
+    c->red = c->partial + RED_MAX_BLOCKS;
+    *out = c;
+    return SCIHPC_OK;
+}
+
+int scihpc_ctx_destroy(scihpc_ctx *ctx) {
+    if (!ctx) return SCIHPC_OK;
+    ctx->ops.release();
+    cudaFree(ctx->t1);
+    cudaFree(ctx->partial);
+    delete ctx;
+    return SCIHPC_OK;
+}
+
+int scihpc_bc_fill(scihpc_ctx *ctx, int location, const int types[6], const double values[6], double *f,
+                   void *stream) {
+    REQUIRE(ctx && f && types && values, "bc_fill: NULL argument");
+    REQUIRE(location >= 0 && location <= ctx->D.ndim, "bc_fill: location out of range");
+    for (int a = 0; a < ctx->D.ndim; ++a) {
+        REQUIRE(types[2 * a] >= 0 && types[2 * a] <= 4 && types[2 * a + 1] >= 0 && types[2 * a + 1] <= 4,
+                "bc_fill: boundary type out of range");
+        // bc_factory::check_bc (bc_factory.cpp:8-21): periodic on both faces or neither
+        REQUIRE((types[2 * a] == 0) == (types[2 * a + 1] == 0), "bc_fill: periodic must be set on both faces");
+    }
+    launch_bc_fill(ctx->D, location, types, values, f, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_flux_extrapolate(scihpc_ctx *ctx, int location, const double *data, double *flux, void *stream) {
+    REQUIRE(ctx && data && flux, "flux_extrapolate: NULL argument");
+    REQUIRE(location >= 0 && location <= ctx->D.ndim, "flux_extrapolate: location out of range");
+    launch_extrapolate(ctx->D, location, data, flux, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_zero_order_extrapolation(scihpc_ctx *ctx, double *f, void *stream) {
+    REQUIRE(ctx && f, "zero_order_extrapolation: NULL argument");
+    launch_zero_order(ctx->D, f, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_uccd(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *f1, double *f2,
+                void *stream) {
+    REQUIRE(ctx && flux && vel_axis && f1 && f2, "uccd: NULL argument");
+    REQUIRE(axis >= 0 && axis < ctx->D.ndim, "uccd: axis out of range");
+    launch_uccd(ctx->D, ctx->ops, axis, flux, vel_axis, f1, f2, ctx->t1, ctx->t2, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_ccd(scihpc_ctx *ctx, int axis, const double *flux, double *f1, double *f2, void *stream) {
+    REQUIRE(ctx && flux && f1 && f2, "ccd: NULL argument");
+    REQUIRE(axis >= 0 && axis < ctx->D.ndim, "ccd: axis out of range");
+    launch_ccd(ctx->D, ctx->ops, axis, flux, f1, f2, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_ccd_mixed(scihpc_ctx *ctx, int axis, double *src, double *out, void *stream) {
+    REQUIRE(ctx && src && out, "ccd_mixed: NULL argument");
+    REQUIRE(axis >= 0 && axis < ctx->D.ndim, "ccd_mixed: axis out of range");
+    launch_ccd_mixed(ctx->D, ctx->ops, axis, src, out, ctx->work, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_weno5(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *fa, void *stream) {
+    REQUIRE(ctx && flux && vel_axis && fa, "weno5: NULL argument");
+    REQUIRE(axis >= 0 && axis < ctx->D.ndim, "weno5: axis out of range");
+    launch_weno5(ctx->D, axis, flux, vel_axis, fa, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_godunov_gradient(scihpc_ctx *ctx, const double *phi, const double *sign, double *grad, void *stream) {
+    REQUIRE(ctx && phi && sign && grad, "godunov_gradient: NULL argument");
+    launch_godunov(ctx->D, phi, sign, grad, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_lsf_fields(scihpc_ctx *ctx, const double prm[4], const double *phi, double *heaviside, double *delta,
+                      double *sign, double *density, double *viscosity, void *stream) {
+    REQUIRE(ctx && prm && phi, "lsf_fields: NULL argument");
+    launch_lsf_fields(ctx->D, prm, phi, heaviside, delta, sign, density, viscosity, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_curvature(scihpc_ctx *ctx, const double *phi, const double *const d[9], double *curv, void *stream) {
+    REQUIRE(ctx && phi && d && curv, "curvature: NULL argument");
+    REQUIRE(ctx->D.ndim >= 2, "curvature: ndim must be 2 or 3");
+    launch_curvature(ctx->D, phi, d, curv, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_lsf_integrals(scihpc_ctx *ctx, const double prm[4], const double *phi, double out[2], void *stream) {
+    REQUIRE(ctx && prm && phi && out, "lsf_integrals: NULL argument");
+    REQUIRE(ctx->D.ndim >= 2, "lsf_integrals: ndim must be 2 or 3");
+    launch_lsf_integral(ctx->D, prm, phi, 0, ctx->work, ctx->partial, ctx->red, S(stream));
+    launch_lsf_integral(ctx->D, prm, phi, 1, ctx->work, ctx->partial, ctx->red + 1, S(stream));
+    CHECK_LAUNCH();
+    double h[2];
+    SCIHPC_CUDA(cudaMemcpyAsync(h, ctx->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, S(stream)));
+    SCIHPC_CUDA(cudaStreamSynchronize(S(stream)));
+    out[0] = h[0] * ctx->D.dv;   // wrapper_func.cpp:510
+    out[1] = h[1] * ctx->D.dv;   // wrapper_func.cpp:571
+    return SCIHPC_OK;
+}
+
+// ------------------------------------------------------------------ pressure Poisson
+int scihpc_poisson_create(const scihpc_grid *grid, int bc, int density_mode, int precision, scihpc_poisson **out) {
+    REQUIRE(out, "poisson_create: out is NULL");
+    int rc = check_grid(grid);
+    if (rc) return rc;
+    REQUIRE(grid->ndim >= 2, "poisson_create: ndim must be 2 or 3");
+    REQUIRE(bc == 0 || bc == 1, "poisson_create: bc must be 0 (Neumann) or 1 (Dirichlet)");
+    REQUIRE(precision == 0 || precision == 1, "poisson_create: precision must be 0 (FP64) or 1 (FP32 inner)");
+    REQUIRE(!(density_mode && bc == 1), "poisson_create: density coefficients are supported with Neumann walls");
+    auto *p = new (std::nothrow) scihpc_poisson;
+    if (!p) return SCIHPC_ERR_NOMEM;
+    rc = p->ps.create(grid, bc, density_mode ? 1 : 0, precision);
+    if (rc) {
+        p->ps.destroy();
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return SCIHPC_OK;
+}
+
+int scihpc_poisson_destroy(scihpc_poisson *ps) {
+    if (!ps) return SCIHPC_OK;
+    ps->ps.destroy();
+    delete ps;
+    return SCIHPC_OK;
+}
+
+int scihpc_poisson_set_density(scihpc_poisson *ps, const double *rho, void *stream) {
+    REQUIRE(ps && rho, "poisson_set_density: NULL argument");
+    return ps->ps.set_density(rho, S(stream));
+}
+
+int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int use_guess, double rel_tol, int max_iter,
+                         int *iters, double *relres, void *stream) {
+    REQUIRE(ps && rhs && p, "poisson_solve: NULL argument");
+    REQUIRE(rel_tol > 0.0 && max_iter > 0, "poisson_solve: rel_tol and max_iter must be positive");
+    return ps->ps.solve(rhs, p, use_guess, rel_tol, max_iter, iters, relres, S(stream));
+}
+
+int scihpc_poisson_levels(scihpc_poisson *ps, int *level_n, int max_levels) {
+    if (!ps || !level_n) return -SCIHPC_ERR_ARG;
+    return ps->ps.levels(level_n, max_levels);
+}
+
+// ------------------------------------------------------------------ two-phase step
+int scihpc_twophase_create(const scihpc_grid *grid, const int vel_bc[6], const int scalar_bc[6], const double prm[16],
+                           const int opt[5], scihpc_twophase **out) {
+    REQUIRE(out && vel_bc && scalar_bc && prm && opt, "twophase_create: NULL argument");
+    int rc = check_grid(grid);
+    if (rc) return rc;
+    REQUIRE(grid->ndim >= 2, "twophase_create: ndim must be 2 or 3");
+    REQUIRE(opt[0] == 0 || opt[0] == 1, "twophase_create: scheme must be 0 (UCCD) or 1 (WENO5)");
+    REQUIRE(opt[3] == 0 || opt[3] == 1, "twophase_create: pressure precision must be 0 or 1");
+    for (int f = 0; f < 2 * grid->ndim; ++f)
+        REQUIRE(vel_bc[f] >= 0 && vel_bc[f] <= 4 && scalar_bc[f] >= 0 && scalar_bc[f] <= 4,
+                "twophase_create: boundary type out of range");
+    for (int f = 0; f < 2 * grid->ndim; ++f)
+        REQUIRE(scalar_bc[f] == 1 && (vel_bc[f] == 2 || vel_bc[f] == 3),
+                "twophase_create: the multigrid pressure solve supports walls (no_slip/slip velocity, neumann scalars)");
+    auto *t = new (std::nothrow) scihpc_twophase;
+    if (!t) return SCIHPC_ERR_NOMEM;
+    rc = t->tp.create(grid, vel_bc, scalar_bc, prm, opt);
+    if (rc) {
+        t->tp.destroy();
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_destroy(scihpc_twophase *tp) {
+    if (!tp) return SCIHPC_OK;
+    tp->tp.destroy();
+    delete tp;
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_upload(scihpc_twophase *tp, const char *name, const double *host) {
+    REQUIRE(tp && name && host, "twophase_upload: NULL argument");
+    double *d = tp->tp.field(name);
+    REQUIRE(d, "twophase_upload: unknown field name");
+    SCIHPC_CUDA(cudaMemcpyAsync(d, host, size_t(tp->tp.D.size()) * sizeof(double), cudaMemcpyHostToDevice, tp->tp.stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(tp->tp.stream));
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host) {
+    REQUIRE(tp && name && host, "twophase_download: NULL argument");
+    double *d = tp->tp.field(name);
+    REQUIRE(d, "twophase_download: unknown field name");
+    SCIHPC_CUDA(cudaMemcpyAsync(host, d, size_t(tp->tp.D.size()) * sizeof(double), cudaMemcpyDeviceToHost, tp->tp.stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(tp->tp.stream));
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_field(scihpc_twophase *tp, const char *name, double **dev) {
+    REQUIRE(tp && name && dev, "twophase_field: NULL argument");
+    double *d = tp->tp.field(name);
+    REQUIRE(d, "twophase_field: unknown field name");
+    *dev = d;
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_get_scalars(scihpc_twophase *tp, double out[7]) {
+    REQUIRE(tp && out, "twophase_get_scalars: NULL argument");
+    return tp->tp.get_scalars(out);
+}
+
+int scihpc_twophase_set_scalars(scihpc_twophase *tp, const double in[7]) {
+    REQUIRE(tp && in, "twophase_set_scalars: NULL argument");
+    return tp->tp.set_scalars(in);
+}
+
+int scihpc_twophase_init(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_init: NULL argument");
+    return tp->tp.init();
+}
+
+#define TP_SYNC(tp)                                                 \
+    do {                                                            \
+        CHECK_LAUNCH();                                             \
+        SCIHPC_CUDA(cudaStreamSynchronize((tp)->tp.stream));        \
+    } while (0)
+
+int scihpc_twophase_find_dt(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_find_dt: NULL argument");
+    tp->tp.find_dt();
+    TP_SYNC(tp);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_advect(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_advect: NULL argument");
+    tp->tp.advect();
+    TP_SYNC(tp);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_mpls(scihpc_twophase *tp, int count) {
+    REQUIRE(tp && count >= 0, "twophase_mpls: bad argument");
+    tp->tp.mpls(count);
+    TP_SYNC(tp);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_reinit(scihpc_twophase *tp, int *steps) {
+    REQUIRE(tp, "twophase_reinit: NULL argument");
+    const int n = tp->tp.reinit();
+    TP_SYNC(tp);
+    if (steps) *steps = n;
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_find_source(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_find_source: NULL argument");
+    tp->tp.find_source();
+    TP_SYNC(tp);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_ab_solve(scihpc_twophase *tp, int *iters, double *relres) {
+    REQUIRE(tp, "twophase_ab_solve: NULL argument");
+    return tp->tp.ab_solve(iters, relres);
+}
+
+int scihpc_twophase_step(scihpc_twophase *tp, int nsteps, int use_graph, int sync) {
+    REQUIRE(tp && nsteps >= 0, "twophase_step: bad argument");
+    int rc = tp->tp.step(nsteps, use_graph != 0);
+    if (rc) return rc;
+    if (sync) SCIHPC_CUDA(cudaStreamSynchronize(tp->tp.stream));
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_diagnostics(scihpc_twophase *tp, double out[3]) {
+    REQUIRE(tp && out, "twophase_diagnostics: NULL argument");
+    return tp->tp.diagnostics(out);
+}
+
+int scihpc_twophase_stream(scihpc_twophase *tp, void **stream) {
+    REQUIRE(tp && stream, "twophase_stream: NULL argument");
+    *stream = tp->tp.stream;
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_ppe_stats(scihpc_twophase *tp, double out[3]) {
+    REQUIRE(tp && out, "twophase_ppe_stats: NULL argument");
+    out[0] = tp->tp.last_iters;
+    out[1] = tp->tp.last_relres;
+    out[2] = tp->tp.last_ms;
+    return SCIHPC_OK;
+}
+
+}  // extern "C"

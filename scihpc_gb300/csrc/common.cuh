@@ -1,0 +1,81 @@
+// common.cuh -- grid description, index helpers and error plumbing shared by all kernels.
+//
+// Device fields use the reference's logical layout: one contiguous FP64 array per field,
+// [Nx][Ny][Nz] with k fastest and ghost width 3 in every active dimension
+// (scalar_data.h:12-17, global.cpp:7-19).  Keeping that order makes host<->device copies
+// plain memcpys of the reference's data and keeps every boundary fill, line solve and
+// stencil expressible in the reference's own indices.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "scihpc_gpu.h"
+
+namespace scihpc {
+
+constexpr int GHC = 3;
+
+struct Dims {
+    int ndim;
+    int n[3];         // interior cells (1 on inactive axes)
+    int N[3];         // with ghosts (1 on inactive axes)
+    long long s[3];   // element strides
+    double d[3];      // spacing (0 on inactive axes)
+    double h, dv;     // min spacing, cell volume (structured_grid.cpp:7-134)
+    double lo[3];
+
+    __host__ __device__ long long size() const { return (long long)N[0] * N[1] * N[2]; }
+    __host__ __device__ long long at(int i, int j, int k) const { return i * s[0] + j * s[1] + k; }
+    // array index of interior cell I along axis a (scalar_data.cpp:95-123)
+    __host__ __device__ int ix(int a, int I) const { return a < ndim ? I + GHC : I; }
+    __host__ __device__ long long interior() const { return (long long)n[0] * n[1] * n[2]; }
+};
+
+Dims make_dims(const scihpc_grid *g);
+
+// Problem parameters that change from step to step live in device memory so that a
+// captured CUDA graph replays correctly (problem_parameters, global.h:25-54).
+struct StepScalars {
+    double t, dt, dt_old, dt_old2;
+    double stable_CFL;
+    double lsf_mass0;
+    double iter;
+    double eta;          // mass-correction coefficient of the last mpls stage
+    double mass;         // last lsf_mass
+    double red[16];      // reduction results (maxima, sums)
+};
+
+#define SCIHPC_CUDA(call)                                                              \
+    do {                                                                               \
+        cudaError_t err__ = (call);                                                    \
+        if (err__ != cudaSuccess) return ::scihpc::cuda_fail(err__, #call, __FILE__, __LINE__); \
+    } while (0)
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+void set_last_error(const char *msg);
+
+inline unsigned blocks_for(long long n, int threads) { return unsigned((n + threads - 1) / threads); }
+
+// Interior linear index q -> (I, J, K) with K fastest, matching the reference loop nests.
+__host__ __device__ inline void split3(long long q, const Dims &D, int &I, int &J, int &K) {
+    K = int(q % D.n[2]);
+    long long r = q / D.n[2];
+    J = int(r % D.n[1]);
+    I = int(r / D.n[1]);
+}
+
+__host__ __device__ inline void split3_full(long long q, const Dims &D, int &i, int &j, int &k) {
+    k = int(q % D.N[2]);
+    long long r = q / D.N[2];
+    j = int(r % D.N[1]);
+    i = int(r / D.N[1]);
+}
+
+// ---------------------------------------------------------------- kernels used across files
+void launch_bc_fill(const Dims &D, int location, const int *types, const double *values, double *f, cudaStream_t s);
+void launch_extrapolate(const Dims &D, int location, const double *data, double *flux, cudaStream_t s);
+void launch_zero_order(const Dims &D, double *f, cudaStream_t s);
+
+}  // namespace scihpc

@@ -1,0 +1,199 @@
+// levelset.cu -- WENO5 derivatives, Godunov gradient, smoothed level-set fields, curvature
+// and the enclosed mass / volume integrals.  All FP64 (level-set transport and
+// reinitialisation keep the reference's precision).
+#include "common.cuh"
+#include "levelset.cuh"
+#include "lsm_device.cuh"
+#include "reduce.cuh"
+
+namespace scihpc {
+
+namespace {
+
+// WENO-Z face value from five cell values (weno_solver.cpp:16-66): `left` selects the
+// left-biased reconstruction (indicators_m / interpolation_m), else the right-biased one.
+__device__ __forceinline__ double weno_face(double a, double b, double c, double d, double e, bool left) {
+    double b0, b1, b2, q0, q1, q2;
+    const double sixth = 1.0 / 6.0;
+    const double t1 = b - 2.0 * c + d;
+    b1 = 13.0 * t1 * t1 + 3.0 * (b - d) * (b - d);
+    if (left) {
+        const double ta = a - 2.0 * b + c, tb = a - 4.0 * b + 3.0 * c;
+        const double tc = c - 2.0 * d + e, td = 3.0 * c - 4.0 * d + e;
+        b0 = 13.0 * ta * ta + 3.0 * tb * tb;
+        b2 = 13.0 * tc * tc + 3.0 * td * td;
+        q0 = (11.0 * c - 7.0 * b + 2.0 * a) * sixth;
+        q1 = (2.0 * d + 5.0 * c - b) * sixth;
+        q2 = (-e + 5.0 * d + 2.0 * c) * sixth;
+    } else {
+        const double ta = c - 2.0 * d + e, tb = 3.0 * c - 4.0 * d + e;
+        const double tc = a - 2.0 * b + c, td = a - 4.0 * b + 3.0 * c;
+        b0 = 13.0 * ta * ta + 3.0 * tb * tb;
+        b2 = 13.0 * tc * tc + 3.0 * td * td;
+        q0 = (11.0 * c - 7.0 * d + 2.0 * e) * sixth;
+        q1 = (2.0 * b + 5.0 * c - d) * sixth;
+        q2 = (-a + 5.0 * b + 2.0 * c) * sixth;
+    }
+    const double tau = fabs(b0 - b2);
+    const double a0 = 1.0 + tau / (WENO_EPS + b0);
+    const double a1 = 6.0 * (1.0 + tau / (WENO_EPS + b1));
+    const double a2 = 3.0 * (1.0 + tau / (WENO_EPS + b2));
+    const double inv = 1.0 / (a0 + a1 + a2);
+    return (a0 * q0 + a1 * q1 + a2 * q2) * inv;
+}
+
+// Upwinded face value between cells i and i+1 (weno_solver.cpp:185-199).
+__device__ __forceinline__ double weno_upwind_face(const double *f, long long o, long long st, const double *vel) {
+    const double fm = weno_face(f[o - 2 * st], f[o - st], f[o], f[o + st], f[o + 2 * st], true);
+    const double fp = weno_face(f[o - st], f[o], f[o + st], f[o + 2 * st], f[o + 3 * st], false);
+    return vel[o] + vel[o + st] > 0.0 ? fm : fp;
+}
+
+__global__ void weno_kernel(const double *__restrict__ f, const double *__restrict__ vel, double *__restrict__ out,
+                            Dims D, int a) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.interior()) return;
+    int I, J, K;
+    split3(q, D, I, J, K);
+    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+    const long long st = D.s[a];
+    const double hr = weno_upwind_face(f, o, st, vel);
+    const double hl = weno_upwind_face(f, o - st, st, vel);
+    out[o] = (hr - hl) / D.d[a];
+}
+
+}  // namespace
+
+namespace {
+
+__global__ void godunov_kernel(const double *__restrict__ phi, const double *__restrict__ sign,
+                               double *__restrict__ grad, Dims D) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.size()) return;
+    int i, j, k;
+    split3_full(q, D, i, j, k);
+    const bool inside = (i >= GHC && i < D.N[0] - GHC) && (D.ndim < 2 || (j >= GHC && j < D.N[1] - GHC)) &&
+                        (D.ndim < 3 || (k >= GHC && k < D.N[2] - GHC));
+    grad[q] = inside ? godunov_at(phi, q, sign[q], D) : 0.0;
+}
+
+__global__ void fields_kernel(const double *__restrict__ phi, double *H, double *De, double *Sg, double *Rho,
+                              double *Mu, long long n, double w, double dr, double vr, int pos) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double x = phi[q];
+    const double h = heaviside_d(x, w);
+    if (H) H[q] = h;
+    if (De) De[q] = delta_d(x, w);
+    if (Sg) Sg[q] = sign_d(x, w);
+    if (Rho) Rho[q] = pos ? h + (1.0 - h) * dr : (1.0 - h) + h * dr;   // wrapper_func.cpp:387-402
+    if (Mu) Mu[q] = pos ? h + (1.0 - h) * vr : (1.0 - h) + h * vr;     // wrapper_func.cpp:404-418
+}
+
+__global__ void curvature_kernel(const double *__restrict__ phi, const double *fx, const double *fy,
+                                 const double *fz, const double *fxx, const double *fyy, const double *fzz,
+                                 const double *fxy, const double *fyz, const double *fzx, double *curv, long long n,
+                                 int ndim) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    double k;
+    if (ndim == 2) {
+        const double x = fx[q], y = fy[q];
+        k = (fxx[q] * y * y + fyy[q] * x * x - 2.0 * fxy[q] * x * y) / pow(x * x + y * y, 1.5);
+        k = k > 0.0 ? 1.0 / (1.0 / k + phi[q]) : -1.0 / (-1.0 / k + phi[q]);
+    } else {
+        const double x = fx[q], y = fy[q], z = fz[q];
+        k = (x * x * (fyy[q] + fzz[q]) + y * y * (fxx[q] + fzz[q]) + z * z * (fxx[q] + fyy[q]) -
+             2.0 * (x * y * fxy[q] + x * z * fzx[q] + y * z * fyz[q])) /
+            pow(x * x + y * y + z * z, 1.5);
+        k = k > 0.0 ? 1.0 / (2.0 / k + phi[q]) : -1.0 / (-2.0 / k + phi[q]);
+    }
+    curv[q] = k;
+}
+
+// Per-cell contribution of lsf_mass (which = 0) or lsf_volume (which = 1) from the
+// product field w (rho * H for mass, H for volume) (wrapper_func.cpp:450-572).
+__device__ double integral_cell(const double *w, long long q, const Dims &D, int which) {
+    int I, J, K;
+    split3(q, D, I, J, K);
+    const int i = D.ix(0, I), j = D.ix(1, J), k = D.ix(2, K);
+    const long long o = D.at(i, j, k);
+    if (D.ndim == 2) {
+        const bool inner = I != 0 && I != D.n[0] - 1 && J != 0 && J != D.n[1] - 1;
+        if (!inner) return w[o];
+        double s = 15.0 * w[o];
+        for (int a = -1; a < 2; ++a)
+            for (int b = -1; b < 2; ++b) s += w[o + a * D.s[0] + b * D.s[1]];
+        return s / 24.0;
+    }
+    const bool inner = I != 0 && I != D.n[0] - 1 && J != 0 && J != D.n[1] - 1 && K != 0 && K != D.n[2] - 1;
+    double s = 50.0 * w[o];
+    if (inner)
+        for (int a = -1; a < 2; ++a)
+            for (int b = -1; b < 2; ++b)
+                for (int c = -1; c < 2; ++c) s += w[o + a * D.s[0] + b * D.s[1] + c];
+    if (which == 0) return inner ? s * D.dv / 77.0 : w[o] * D.dv;
+    return (inner ? s / 77.0 : w[o]) + s / 77.0;
+}
+
+__global__ void product_kernel(const double *__restrict__ phi, double *__restrict__ w, long long n, double lw,
+                               double dr, int pos, int which) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double h = heaviside_d(phi[q], lw);
+    if (which == 1) {
+        w[q] = h;
+    } else {
+        const double rho = pos ? h + (1.0 - h) * dr : (1.0 - h) + h * dr;
+        w[q] = rho * h;
+    }
+}
+
+__global__ void integral_kernel(const double *__restrict__ w, Dims D, int which, double *__restrict__ partial) {
+    __shared__ double sh[RED_THREADS];
+    const long long n = D.interior();
+    const long long per_block = (n + gridDim.x - 1) / gridDim.x;
+    const long long b0 = blockIdx.x * per_block;
+    const long long b1 = b0 + per_block < n ? b0 + per_block : n;
+    const long long per = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    const long long t0 = b0 + threadIdx.x * per;
+    double s = 0.0;
+    for (long long q = t0; q < t0 + per && q < b1; ++q) s += integral_cell(w, q, D, which);
+    s = block_reduce<SumOp>(s, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+}  // namespace
+
+void launch_weno5(const Dims &D, int a, const double *flux, const double *vel, double *out, cudaStream_t s) {
+    weno_kernel<<<blocks_for(D.interior(), 128), 128, 0, s>>>(flux, vel, out, D, a);
+}
+
+void launch_godunov(const Dims &D, const double *phi, const double *sign, double *grad, cudaStream_t s) {
+    godunov_kernel<<<blocks_for(D.size(), 128), 128, 0, s>>>(phi, sign, grad, D);
+}
+
+void launch_lsf_fields(const Dims &D, const double *prm, const double *phi, double *H, double *De, double *Sg,
+                       double *Rho, double *Mu, cudaStream_t s) {
+    fields_kernel<<<blocks_for(D.size(), 256), 256, 0, s>>>(phi, H, De, Sg, Rho, Mu, D.size(), prm[0], prm[1], prm[2],
+                                                             prm[3] != 0.0);
+}
+
+void launch_curvature(const Dims &D, const double *phi, const double *const d[9], double *curv, cudaStream_t s) {
+    curvature_kernel<<<blocks_for(D.size(), 256), 256, 0, s>>>(phi, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7],
+                                                                d[8], curv, D.size(), D.ndim);
+}
+
+// lsf_mass (which 0) or lsf_volume (which 1) into *out (device), using `work` (one field)
+// and `partial` (RED_MAX_BLOCKS doubles) as scratch.  The result still needs the final dv
+// factor, applied by the caller (wrapper_func.cpp:510,571).
+void launch_lsf_integral(const Dims &D, const double *prm, const double *phi, int which, double *work,
+                         double *partial, double *out, cudaStream_t s) {
+    product_kernel<<<blocks_for(D.size(), 256), 256, 0, s>>>(phi, work, D.size(), prm[0], prm[1], prm[3] != 0.0,
+                                                             which);
+    const int nb = red_blocks(D.interior());
+    integral_kernel<<<nb, RED_THREADS, 0, s>>>(work, D, which, partial);
+    finish_reduce<SumOp><<<1, 1024, 0, s>>>(partial, nb, out);
+}
+
+}  // namespace scihpc

@@ -1,0 +1,60 @@
+// lsm_device.cuh -- inline device helpers of the level-set method shared by kernels in
+// several files: smoothed Heaviside / delta / sign and the Godunov gradient.
+#pragma once
+
+#include "common.cuh"
+
+namespace scihpc {
+
+constexpr double WENO_EPS = 1e-8;   // global.h:14
+
+__device__ __forceinline__ double heaviside_d(double x, double w) {
+    if (x < -w) return 0.0;
+    if (x > w) return 1.0;
+    return 0.5 * (1.0 + x / w + sin(M_PI * x / w) / M_PI);   // lsm.cpp:8-18
+}
+__device__ __forceinline__ double delta_d(double x, double w) {
+    if (x < -w) return 0.0;
+    if (x > w) return 0.0;
+    return 0.5 * (1.0 + cos(M_PI * x / w)) / w;   // lsm.cpp:20-30
+}
+__device__ __forceinline__ double sign_d(double x, double w) {
+    if (x < -w) return -1.0;
+    if (x > w) return 1.0;
+    return x / sqrt(x * x + w * w);   // lsm.cpp:33-43
+}
+
+// WENO-JS correction of the fourth-order central gradient (godunov_gradient.cpp:183-198).
+__device__ __forceinline__ double weno_godunov(double a, double b, double c, double d) {
+    const double is0 = 13.0 * (a - b) * (a - b) + 3.0 * (a - 3.0 * b) * (a - 3.0 * b);
+    const double is1 = 13.0 * (b - c) * (b - c) + 3.0 * (b + c) * (b + c);
+    const double is2 = 13.0 * (c - d) * (c - d) + 3.0 * (3.0 * c - d) * (3.0 * c - d);
+    const double e0 = WENO_EPS + is0, e1 = WENO_EPS + is1, e2 = WENO_EPS + is2;
+    const double al0 = 1.0 / (e0 * e0), al1 = 6.0 / (e1 * e1), al2 = 3.0 / (e2 * e2);
+    const double inv = 1.0 / (al0 + al1 + al2);
+    const double w0 = al0 * inv, w2 = al2 * inv;
+    return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
+}
+
+// Godunov |grad phi| at one interior cell (godunov_gradient.cpp:19-153).
+__device__ __forceinline__ double godunov_at(const double *__restrict__ phi, long long o, double sgn, const Dims &D) {
+    double g2 = 0.0;
+    for (int a = 0; a < D.ndim; ++a) {
+        const long long st = D.s[a];
+        const double ih = 1.0 / D.d[a];
+        const double m3 = phi[o - 3 * st], m2 = phi[o - 2 * st], m1 = phi[o - st], c0 = phi[o];
+        const double p1 = phi[o + st], p2 = phi[o + 2 * st], p3 = phi[o + 3 * st];
+        const double v = ih * (1.0 / 12.0) * (-(m1 - m2) + 7.0 * (c0 - m1) + 7.0 * (p1 - c0) - (p2 - p1));
+        const double dp = v + ih * weno_godunov(p3 - 2.0 * p2 + p1, p2 - 2.0 * p1 + c0, p1 - 2.0 * c0 + m1,
+                                                c0 - 2.0 * m1 + m2);
+        const double dm = v - ih * weno_godunov(m3 - 2.0 * m2 + m1, m2 - 2.0 * m1 + c0, m1 - 2.0 * c0 + p1,
+                                                c0 - 2.0 * p1 + p2);
+        double g;
+        if (sgn > 0.0) g = fmax(-fmin(dp, 0.0), fmax(dm, 0.0));
+        else g = fmax(fmax(dp, 0.0), -fmin(dm, 0.0));
+        g2 += g * g;
+    }
+    return sqrt(g2);
+}
+
+}  // namespace scihpc

@@ -1,0 +1,972 @@
+// poisson.cu -- multigrid-preconditioned conjugate gradients for the pressure equation of
+// projection_method::projection (projection_method.cpp:404-465,544-627).
+//
+// Outer iteration (always FP64): flexible preconditioned CG on L p = g with
+//   L p |_c = sum_f C_f (p_c - p_nb),  C_f = 1 / (0.5 (rho_c + rho_nb)) / d^2  (or 1/d^2),
+// g = -rhs (projected to zero mean for Neumann walls).  The residual, the search direction,
+// the solution update and the convergence test stay in FP64.
+// Preconditioner: one V(2,2) cycle in precision T (double, or float for the
+// FP32-inner / FP64-outer mode):
+//   - red-black Gauss-Seidel smoothing, red then black before, black then red after
+//     (symmetric), coefficients of level 0 derived on the fly from the cell density;
+//   - residual + cell-average restriction fused into one kernel;
+//   - face coefficients of coarse levels: mean of the fine faces covering a coarse face,
+//     divided by the square of the coarsening ratio;
+//   - (bi/tri)linear prolongation for ratio 2, piecewise constant for ratio 3, fused with
+//     the correction;
+//   - FP64 dense direct solve on the coarsest level (explicit inverse, built once per
+//     density update, applied as a matrix-vector product).
+// Level hierarchy: the reference's coarsening rule (multigrid.cpp:8-41), so level counts
+// match the reference's multigrid.
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "poisson.cuh"
+#include "reduce.cuh"
+
+namespace scihpc {
+
+namespace {
+
+constexpr int TPB = 256;
+
+// ---------------------------------------------------------------- grid-wide deterministic reductions
+// Each block reduces its values in a fixed tree, writes a partial, and the last block to
+// arrive sums the partials in a fixed order.  Results do not depend on block scheduling.
+struct RedSlot {
+    double *partial;        // gridDim.x entries
+    unsigned *counter;      // zero-initialised, reset by the last block
+};
+
+template <int NV>
+__device__ void grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
+    __shared__ double sh[NV][TPB];
+    __shared__ bool last;
+    const int t = threadIdx.x;
+    for (int m = 0; m < NV; ++m) sh[m][t] = v[m];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (t < w)
+            for (int m = 0; m < NV; ++m) sh[m][t] += sh[m][t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        for (int m = 0; m < NV; ++m) slot.partial[m * RED_MAX_BLOCKS + blockIdx.x] = sh[m][0];
+        __threadfence();
+        const unsigned ticket = atomicAdd(slot.counter, 1u);
+        last = ticket == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int nb = gridDim.x;
+    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    for (int m = 0; m < NV; ++m) {
+        double a = 0.0;
+        for (int q = t * per; q < (t + 1) * per && q < nb; ++q) a += __ldcg(&slot.partial[m * RED_MAX_BLOCKS + q]);
+        sh[m][t] = a;
+    }
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (t < w)
+            for (int m = 0; m < NV; ++m) sh[m][t] += sh[m][t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        for (int m = 0; m < NV; ++m) *out[m] = sh[m][0];
+        *slot.counter = 0u;
+    }
+}
+
+inline int grid_blocks(long long n) {
+    long long b = (n + TPB - 1) / TPB;
+    if (b > RED_MAX_BLOCKS) b = RED_MAX_BLOCKS;
+    if (b < 1) b = 1;
+    return int(b);
+}
+
+// ---------------------------------------------------------------- FP64 outer operator
+struct Outer {
+    Dims D;           // ghosted field geometry
+    int nint[3];      // interior extents
+    long long cs[3];  // compact strides (K fastest)
+    double id2[3];
+    int density;      // 1: coefficients from rho64
+    int dirichlet;    // 1: wall term against a zero ghost-centre value
+};
+
+// (L v)_c for a compact vector v (or a ghosted field when `ghosted`).
+template <bool GHOSTED>
+__device__ __forceinline__ double apply_L(const double *__restrict__ v, const double *__restrict__ rho, const Outer &O,
+                                          int I, int J, int K) {
+    const int II[3] = {I, J, K};
+    const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
+    const long long co = I * O.cs[0] + J * O.cs[1] + K;
+    const long long c = GHOSTED ? go : co;
+    const double vc = v[c];
+    const double rc = O.density ? rho[go] : 1.0;
+    double s = 0.0;
+    for (int a = 0; a < O.D.ndim; ++a) {
+        const long long st = GHOSTED ? O.D.s[a] : O.cs[a];
+        const long long gs = O.D.s[a];
+        for (int side = -1; side <= 1; side += 2) {
+            const bool wall = side < 0 ? II[a] == 0 : II[a] == O.nint[a] - 1;
+            double C, vn;
+            if (wall) {
+                if (!O.dirichlet) continue;
+                C = O.id2[a];
+                vn = 0.0;
+            } else {
+                if (O.density) {
+                    const double R = 0.5 * (rc + rho[go + side * gs]);
+                    C = 1.0 / R * O.id2[a];   // 1.0 / R / d / d (projection_method.cpp:416-424)
+                } else {
+                    C = O.id2[a];
+                }
+                vn = v[c + side * st];
+            }
+            s += C * (vc - vn);
+        }
+    }
+    return s;
+}
+
+__device__ __forceinline__ void split_int(long long q, const Outer &O, int &I, int &J, int &K) {
+    K = int(q % O.nint[2]);
+    const long long r = q / O.nint[2];
+    J = int(r % O.nint[1]);
+    I = int(r / O.nint[1]);
+}
+
+// sum of rhs over interior cells (for the Neumann projection of the right-hand side)
+__global__ void k_rhs_sum(const double *__restrict__ rhs, Outer O, long long n, RedSlot slot, double *out) {
+    double v[1] = {0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        v[0] += rhs[O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K))];
+    }
+    double *o[1] = {out};
+    grid_sum<1>(v, slot, o);
+}
+
+// r = g - L p, g = -(rhs - mean); ||g||^2, ||r||^2; level-0 V-cycle input b0 = r.
+template <class T>
+__global__ void k_init(const double *__restrict__ rhs, double *__restrict__ p, const double *__restrict__ rho,
+                       Outer O, long long n, int use_guess, double *__restrict__ r, T *__restrict__ b0, Level<T> L0,
+                       RedSlot slot, PcgScalars *st) {
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(n);
+    double v[2] = {0.0, 0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
+        const double g = -(rhs[go] - mean);
+        double rv = g;
+        if (use_guess) rv -= apply_L<true>(p, rho, O, I, J, K);
+        else p[go] = 0.0;
+        r[q] = rv;
+        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
+        b0[P0] = T(rv);
+        v[0] += g * g;
+        v[1] += rv * rv;
+    }
+    double *o[2] = {&st->bb, &st->rr};
+    grid_sum<2>(v, slot, o);
+}
+
+// rz = <r, z>, r_zold = <r, z_old> (flexible CG)
+template <class T>
+__global__ void k_dot_rz(const double *__restrict__ r, const T *__restrict__ z, const T *__restrict__ zold, Outer O,
+                         Level<T> L0, long long n, RedSlot slot, PcgScalars *st) {
+    if (st->done) return;
+    double v[2] = {0.0, 0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
+        v[0] += r[q] * double(z[P0]);
+        v[1] += r[q] * double(zold[P0]);
+    }
+    double *o[2] = {&st->rz, &st->r_zold};
+    grid_sum<2>(v, slot, o);
+}
+
+// d = z + beta d (beta = (rz - r.zold) / rz_prev; 0 on the first iteration), z_old = z,
+// then q = L d and <d, q>.  Two passes: d must be complete before L d reads neighbours.
+template <class T>
+__global__ void k_update_d(const T *__restrict__ z, T *__restrict__ zold, double *__restrict__ d, Outer O,
+                           Level<T> L0, long long n, const PcgScalars *st) {
+    if (st->done) return;
+    const double beta = st->it == 0 ? 0.0 : (st->rz - st->r_zold) / st->rz_prev;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
+        const T zz = z[P0];
+        d[q] = double(zz) + beta * d[q];
+        zold[P0] = zz;
+    }
+}
+
+__global__ void k_apply_dq(const double *__restrict__ d, double *__restrict__ qv, const double *__restrict__ rho,
+                           Outer O, long long n, RedSlot slot, PcgScalars *st) {
+    if (st->done) return;
+    double v[1] = {0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const double lq = apply_L<false>(d, rho, O, I, J, K);
+        qv[q] = lq;
+        v[0] += d[q] * lq;
+    }
+    double *o[1] = {&st->dq};
+    grid_sum<1>(v, slot, o);
+}
+
+// p += alpha d, r -= alpha q, ||r||^2, b0 = r
+template <class T>
+__global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const double *__restrict__ d,
+                       const double *__restrict__ qv, T *__restrict__ b0, Outer O, Level<T> L0, long long n,
+                       RedSlot slot, PcgScalars *st) {
+    if (st->done) return;
+    const double alpha = st->rz / st->dq;
+    double v[1] = {0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
+        p[go] += alpha * d[q];
+        const double rv = r[q] - alpha * qv[q];
+        r[q] = rv;
+        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
+        b0[P0] = T(rv);
+        v[0] += rv * rv;
+    }
+    double *o[1] = {&st->rr};
+    grid_sum<1>(v, slot, o);
+}
+
+// Convergence test; in graph mode it also drives the conditional while-node.
+__global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
+                        int use_handle) {
+    if (advance) {
+        if (st->done) {
+#if defined(__CUDA_ARCH__)
+            if (use_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, 0u);
+#endif
+            return;
+        }
+        st->rz_prev = st->rz;
+        st->it += 1;
+    }
+    const double rel = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0;
+    st->relres = rel;
+    if (!(rel == rel) || isinf(rel)) st->diverged = 1;
+    st->done = (rel <= tol || st->it >= max_iter || st->diverged) ? 1 : 0;
+#if defined(__CUDA_ARCH__)
+    if (use_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, st->done ? 0u : 1u);
+#endif
+}
+
+// final: mean removal (Neumann) and the true relative residual
+__global__ void k_p_sum(const double *__restrict__ p, Outer O, long long n, RedSlot slot, double *out) {
+    double v[1] = {0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        v[0] += p[O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K))];
+    }
+    double *o[1] = {out};
+    grid_sum<1>(v, slot, o);
+}
+
+__global__ void k_p_shift(double *__restrict__ p, Outer O, long long n, const double *sum) {
+    const double m = *sum / double(n);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        p[O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K))] -= m;
+    }
+}
+
+__global__ void k_true_res(const double *__restrict__ rhs, const double *__restrict__ p, const double *__restrict__ rho,
+                           Outer O, long long n, RedSlot slot, PcgScalars *st) {
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(n);
+    double v[1] = {0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
+        const double rv = -(rhs[go] - mean) - apply_L<true>(p, rho, O, I, J, K);
+        v[0] += rv * rv;
+    }
+    double *o[1] = {&st->rr};
+    grid_sum<1>(v, slot, o);
+}
+
+__global__ void k_relres(PcgScalars *st) { st->relres = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0; }
+
+// ---------------------------------------------------------------- V-cycle kernels (precision T)
+// MODE 0: stored face coefficients; 1: level 0 from the padded density (+inf halo gives
+// zero wall coefficients); 2: level 0 constant 1/d^2 with the zero halo as ghost value.
+template <class T, int MODE>
+__device__ __forceinline__ void faces(const Level<T> &L, const T *__restrict__ rho, const T *id2, long long P, int ndim,
+                                      T C[6]) {
+    if (MODE == 0) {
+        C[0] = L.cx[P - L.s[0]], C[1] = L.cx[P];
+        C[2] = L.cy[P - L.s[1]], C[3] = L.cy[P];
+        if (ndim == 3) C[4] = L.cz[P - L.s[2]], C[5] = L.cz[P];
+    } else if (MODE == 1) {
+        const T rc = rho[P];
+        for (int a = 0; a < ndim; ++a) {
+            C[2 * a] = T(2) / (rc + rho[P - L.s[a]]) * id2[a];
+            C[2 * a + 1] = T(2) / (rc + rho[P + L.s[a]]) * id2[a];
+        }
+    } else {
+        for (int a = 0; a < ndim; ++a) C[2 * a] = C[2 * a + 1] = id2[a];
+    }
+}
+
+template <class T>
+struct Id2 {
+    T v[3];
+};
+
+template <class T, int MODE, int DIM>
+__global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int color) {
+    const int nf = L.n[DIM - 1];
+    const int nh = (nf + 1) / 2;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long rows = DIM == 3 ? (long long)L.n[0] * L.n[1] : L.n[0];
+    if (t >= rows * nh) return;
+    const int kh = int(t % nh);
+    const long long row = t / nh;
+    int I, J, K;
+    long long P;
+    if (DIM == 3) {
+        J = int(row % L.n[1]);
+        I = int(row / L.n[1]);
+        K = 2 * kh + ((I + J + color) & 1);
+        if (K >= L.n[2]) return;
+        P = (I + 1) * L.s[0] + (J + 1) * L.s[1] + (K + 1);
+    } else {
+        I = int(row);
+        J = 2 * kh + ((I + color) & 1);
+        if (J >= L.n[1]) return;
+        P = (I + 1) * L.s[0] + (J + 1);
+    }
+    T C[6];
+    faces<T, MODE>(L, rho, id2.v, P, DIM, C);
+    T sc = C[0] + C[1] + C[2] + C[3];
+    T sx = C[0] * L.x[P - L.s[0]] + C[1] * L.x[P + L.s[0]] + C[2] * L.x[P - L.s[1]] + C[3] * L.x[P + L.s[1]];
+    if (DIM == 3) {
+        sc += C[4] + C[5];
+        sx += C[4] * L.x[P - 1] + C[5] * L.x[P + 1];
+    }
+    L.x[P] = (L.b[P] + sx) / sc;
+}
+
+template <class T, int MODE, int DIM>
+__device__ __forceinline__ T residual_at(const Level<T> &L, const T *__restrict__ rho, const T *id2, long long P) {
+    T C[6];
+    faces<T, MODE>(L, rho, id2, P, DIM, C);
+    const T xc = L.x[P];
+    T s = C[0] * (xc - L.x[P - L.s[0]]) + C[1] * (xc - L.x[P + L.s[0]]) + C[2] * (xc - L.x[P - L.s[1]]) +
+          C[3] * (xc - L.x[P + L.s[1]]);
+    if (DIM == 3) s += C[4] * (xc - L.x[P - 1]) + C[5] * (xc - L.x[P + 1]);
+    return L.b[P] - s;
+}
+
+// coarse b = mean of the fine residuals of its r^d children; coarse x = 0
+template <class T, int MODE, int DIM>
+__global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
+    if (t >= nc) return;
+    int I, J, K = 0;
+    if (DIM == 3) {
+        K = int(t % Cl.n[2]);
+        const long long rr = t / Cl.n[2];
+        J = int(rr % Cl.n[1]);
+        I = int(rr / Cl.n[1]);
+    } else {
+        J = int(t % Cl.n[1]);
+        I = int(t / Cl.n[1]);
+    }
+    const int r = F.ratio;
+    T s = 0;
+    for (int a = 0; a < r; ++a)
+        for (int b = 0; b < r; ++b)
+            for (int c = 0; c < (DIM == 3 ? r : 1); ++c) {
+                const long long P = (r * I + a + 1) * F.s[0] + (r * J + b + 1) * F.s[1] + (DIM == 3 ? r * K + c + 1 : 0);
+                s += residual_at<T, MODE, DIM>(F, rho, id2.v, P);
+            }
+    const long long Pc = (I + 1) * Cl.s[0] + (J + 1) * Cl.s[1] + (DIM == 3 ? K + 1 : 0);
+    Cl.b[Pc] = s / T(DIM == 3 ? r * r * r : r * r);
+    Cl.x[Pc] = 0;
+}
+
+// fine x += interpolation of coarse x: (bi/tri)linear for ratio 2 (weights 3/4, 1/4 per
+// axis; Neumann walls clamp to the wall cell, Dirichlet walls read the zero halo),
+// piecewise constant for ratio 3.
+template <class T, int DIM>
+__global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nf = (long long)F.n[0] * F.n[1] * (DIM == 3 ? F.n[2] : 1);
+    if (t >= nf) return;
+    int ii[3] = {0, 0, 0};
+    if (DIM == 3) {
+        ii[2] = int(t % F.n[2]);
+        const long long rr = t / F.n[2];
+        ii[1] = int(rr % F.n[1]);
+        ii[0] = int(rr / F.n[1]);
+    } else {
+        ii[1] = int(t % F.n[1]);
+        ii[0] = int(t / F.n[1]);
+    }
+    const int r = F.ratio;
+    const long long Pf = (ii[0] + 1) * F.s[0] + (ii[1] + 1) * F.s[1] + (DIM == 3 ? ii[2] + 1 : 0);
+    int par[3], nb[3];
+    for (int a = 0; a < DIM; ++a) {
+        par[a] = ii[a] / r;
+        const int off = ii[a] - par[a] * r;
+        int dn = off == 0 ? par[a] - 1 : par[a] + 1;
+        if (neumann && (dn < 0 || dn >= Cl.n[a])) dn = par[a];
+        nb[a] = dn;
+    }
+    auto CX = [&](int a0, int a1, int a2) {
+        return Cl.x[(a0 + 1) * Cl.s[0] + (a1 + 1) * Cl.s[1] + (DIM == 3 ? a2 + 1 : 0)];
+    };
+    T v;
+    if (r != 2) {
+        v = CX(par[0], par[1], DIM == 3 ? par[2] : 0);
+    } else if (DIM == 2) {
+        v = T(0.5625) * CX(par[0], par[1], 0) + T(0.1875) * (CX(nb[0], par[1], 0) + CX(par[0], nb[1], 0)) +
+            T(0.0625) * CX(nb[0], nb[1], 0);
+    } else {
+        v = T(27.0 / 64.0) * CX(par[0], par[1], par[2]) +
+            T(9.0 / 64.0) * (CX(nb[0], par[1], par[2]) + CX(par[0], nb[1], par[2]) + CX(par[0], par[1], nb[2])) +
+            T(3.0 / 64.0) * (CX(nb[0], nb[1], par[2]) + CX(nb[0], par[1], nb[2]) + CX(par[0], nb[1], nb[2])) +
+            T(1.0 / 64.0) * CX(nb[0], nb[1], nb[2]);
+    }
+    F.x[Pf] += v;
+}
+
+// coarse face coefficients from the fine level (mean over the fine faces of a coarse face,
+// divided by ratio^2).  Faces at padded index 0 .. n along the face axis (walls included).
+template <class T, int MODE, int DIM>
+__global__ void k_coarse_coef(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2, int axis) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int E[3] = {Cl.n[0], Cl.n[1], DIM == 3 ? Cl.n[2] : 1};
+    E[axis] += 1;   // faces 0..n
+    const long long total = (long long)E[0] * E[1] * E[2];
+    if (t >= total) return;
+    int c[3];
+    c[2] = int(t % E[2]);
+    const long long rr = t / E[2];
+    c[1] = int(rr % E[1]);
+    c[0] = int(rr / E[1]);
+    const int r = F.ratio;
+    // padded coarse index of the cell on the low side of the face: axis coordinate c[axis]
+    // (0 = halo), others +1
+    long long Pc = 0;
+    for (int a = 0; a < DIM; ++a) Pc += (a == axis ? c[a] : c[a] + 1) * Cl.s[a];
+    T sum = 0;
+    int cnt = 0;
+    const int ra = DIM == 3 ? r : 1;
+    for (int u = 0; u < r; ++u)
+        for (int w = 0; w < ra; ++w) {
+            int f[3];
+            int tr = 0;
+            for (int a = 0; a < DIM; ++a) {
+                if (a == axis) {
+                    f[a] = r * c[a];   // padded fine index of the low-side cell of the face
+                } else {
+                    f[a] = r * c[a] + (tr == 0 ? u : w) + 1;
+                    ++tr;
+                }
+            }
+            const long long Pf = f[0] * F.s[0] + f[1] * F.s[1] + (DIM == 3 ? f[2] * F.s[2] : 0);
+            T C;
+            if (MODE == 0) {
+                C = axis == 0 ? F.cx[Pf] : (axis == 1 ? F.cy[Pf] : F.cz[Pf]);
+            } else if (MODE == 1) {
+                C = T(2) / (rho[Pf] + rho[Pf + F.s[axis]]) * id2.v[axis];
+            } else {
+                C = id2.v[axis];
+            }
+            sum += C;
+            ++cnt;
+        }
+    T *dst = axis == 0 ? Cl.cx : (axis == 1 ? Cl.cy : Cl.cz);
+    dst[Pc] = sum / T(cnt) / T(r * r);
+}
+
+// ---------------------------------------------------------------- coarsest level: dense FP64 inverse
+template <class T, int DIM>
+__global__ void k_dense_build(Level<T> L, double *__restrict__ M, int n, int neumann) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    int I, J, K = 0;
+    if (DIM == 3) {
+        K = c % L.n[2];
+        J = (c / L.n[2]) % L.n[1];
+        I = c / (L.n[2] * L.n[1]);
+    } else {
+        J = c % L.n[1];
+        I = c / L.n[1];
+    }
+    double *row = M + (size_t)c * n;
+    for (int q = 0; q < n; ++q) row[q] = 0.0;
+    const long long P = (I + 1) * L.s[0] + (J + 1) * L.s[1] + (DIM == 3 ? K + 1 : 0);
+    const T C[6] = {L.cx[P - L.s[0]], L.cx[P], L.cy[P - L.s[1]], L.cy[P], DIM == 3 ? L.cz[P - 1] : T(0),
+                    DIM == 3 ? L.cz[P] : T(0)};
+    const int nbI[6] = {I - 1, I + 1, I, I, I, I}, nbJ[6] = {J, J, J - 1, J + 1, J, J}, nbK[6] = {K, K, K, K, K - 1, K + 1};
+    double diag = 0.0;
+    for (int f = 0; f < 2 * DIM; ++f) {
+        diag += double(C[f]);
+        const bool in = nbI[f] >= 0 && nbI[f] < L.n[0] && nbJ[f] >= 0 && nbJ[f] < L.n[1] &&
+                        (DIM == 2 || (nbK[f] >= 0 && nbK[f] < L.n[2]));
+        if (in) {
+            const int cn = DIM == 3 ? (nbI[f] * L.n[1] + nbJ[f]) * L.n[2] + nbK[f] : nbI[f] * L.n[1] + nbJ[f];
+            row[cn] -= double(C[f]);
+        }
+    }
+    row[c] += diag;
+    if (neumann) {
+        // pin the constant null space: + (mean diagonal / n) 1 1^T, applied after a sync below
+        row[c] += 0.0;
+    }
+}
+
+__global__ void k_dense_pin_and_invert(double *__restrict__ M, double *__restrict__ W, int n, int neumann) {
+    // W: n x 2n work matrix [M | I]; result inverse written back into M.
+    __shared__ double piv, scale;
+    __shared__ double fac[1024];
+    const int t = threadIdx.x, nt = blockDim.x;
+    if (neumann) {
+        if (t == 0) {
+            double s = 0.0;
+            for (int c = 0; c < n; ++c) s += M[(size_t)c * n + c];
+            scale = s / n / n;
+        }
+        __syncthreads();
+        for (int e = t; e < n * n; e += nt) M[e] += scale;
+        __syncthreads();
+    }
+    const int w = 2 * n;
+    for (int e = t; e < n * w; e += nt) {
+        const int rr = e / w, cc = e % w;
+        W[e] = cc < n ? M[(size_t)rr * n + cc] : (cc - n == rr ? 1.0 : 0.0);
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        if (t == 0) piv = 1.0 / W[(size_t)k * w + k];
+        __syncthreads();
+        for (int cc = t; cc < w; cc += nt) W[(size_t)k * w + cc] *= piv;
+        __syncthreads();
+        for (int rr = t; rr < n; rr += nt) fac[rr] = W[(size_t)rr * w + k];
+        __syncthreads();
+        for (int e = t; e < n * w; e += nt) {
+            const int rr = e / w, cc = e % w;
+            if (rr != k) W[e] -= fac[rr] * W[(size_t)k * w + cc];
+        }
+        __syncthreads();
+    }
+    for (int e = t; e < n * n; e += nt) M[e] = W[(size_t)(e / n) * w + n + e % n];
+}
+
+template <class T, int DIM>
+__global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n, int neumann) {
+    __shared__ double b[1024];
+    __shared__ double mean;
+    const int t = threadIdx.x;
+    auto pidx = [&](int c) {
+        int I, J, K = 0;
+        if (DIM == 3) {
+            K = c % L.n[2];
+            J = (c / L.n[2]) % L.n[1];
+            I = c / (L.n[2] * L.n[1]);
+        } else {
+            J = c % L.n[1];
+            I = c / L.n[1];
+        }
+        return (I + 1) * L.s[0] + (J + 1) * L.s[1] + (DIM == 3 ? K + 1 : 0);
+    };
+    for (int c = t; c < n; c += blockDim.x) b[c] = double(L.b[pidx(c)]);
+    __syncthreads();
+    if (t == 0) {
+        double s = 0.0;
+        if (neumann)
+            for (int c = 0; c < n; ++c) s += b[c];
+        mean = s / n;
+    }
+    __syncthreads();
+    for (int c = t; c < n; c += blockDim.x) {
+        const double *row = Minv + (size_t)c * n;
+        double s = 0.0;
+        for (int q = 0; q < n; ++q) s += row[q] * (b[q] - mean);
+        L.x[pidx(c)] = T(s);
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+static void coarsen_sizes(int ndim, const int *n, std::vector<std::array<int, 3>> &sizes, std::vector<int> &ratio) {
+    // multigrid::check2d / check3d (multigrid.cpp:10-41): halve while every halved extent
+    // stays above 3, else divide by 3, else stop.
+    const int min_grid = 3;
+    sizes.push_back({n[0], n[1], ndim == 3 ? n[2] : 1});
+    while (true) {
+        const auto &c = sizes.back();
+        auto ok = [&](int q) {
+            bool all = c[0] % q == 0 && c[1] % q == 0 && c[0] / q > min_grid && c[1] / q > min_grid;
+            if (ndim == 3) all = all && c[2] % q == 0 && c[2] / q > min_grid;
+            return all;
+        };
+        int r = ok(2) ? 2 : (ok(3) ? 3 : 1);
+        if (r == 1) break;
+        ratio.push_back(r);
+        sizes.push_back({c[0] / r, c[1] / r, ndim == 3 ? c[2] / r : 1});
+    }
+    ratio.push_back(1);
+}
+
+template <class T>
+int Poisson::alloc_levels() {
+    std::vector<std::array<int, 3>> sizes;
+    std::vector<int> ratio;
+    coarsen_sizes(D.ndim, D.n, sizes, ratio);
+    nlev = int(sizes.size());
+    std::vector<Level<T>> &Ls = levs<T>();
+    Ls.resize(nlev);
+    double dd[3] = {D.d[0], D.d[1], D.d[2]};
+    for (int l = 0; l < nlev; ++l) {
+        Level<T> &L = Ls[l];
+        for (int a = 0; a < 3; ++a) {
+            L.n[a] = sizes[l][a];
+            L.P[a] = a < D.ndim ? L.n[a] + 2 : 1;
+            L.d[a] = dd[a];
+        }
+        L.s[2] = 1;
+        L.s[1] = L.P[2];
+        L.s[0] = (long long)L.P[1] * L.P[2];
+        if (D.ndim == 2) L.s[2] = 0;
+        L.cells = (long long)L.P[0] * L.P[1] * L.P[2];
+        L.ratio = ratio[l];
+        const size_t bytes = size_t(L.cells) * sizeof(T);
+        SCIHPC_CUDA(cudaMalloc(&L.x, bytes));
+        SCIHPC_CUDA(cudaMalloc(&L.b, bytes));
+        SCIHPC_CUDA(cudaMemset(L.x, 0, bytes));
+        SCIHPC_CUDA(cudaMemset(L.b, 0, bytes));
+        if (l > 0) {
+            SCIHPC_CUDA(cudaMalloc(&L.cx, 3 * bytes));
+            SCIHPC_CUDA(cudaMemset(L.cx, 0, 3 * bytes));
+            L.cy = L.cx + L.cells;
+            L.cz = L.cy + L.cells;
+        }
+        for (int a = 0; a < 3; ++a) dd[a] *= ratio[l];
+    }
+    // coarsest dense solve
+    const Level<T> &C = Ls[nlev - 1];
+    ncoarse = C.n[0] * C.n[1] * C.n[2];
+    if (ncoarse > 1024) {
+        set_last_error("coarsest multigrid level exceeds 1024 cells (grid sizes need more factors of 2 or 3)");
+        return SCIHPC_ERR_UNSUPPORTED;
+    }
+    SCIHPC_CUDA(cudaMalloc(&dense, size_t(ncoarse) * ncoarse * sizeof(double) * 3));
+    const size_t zbytes = size_t(Ls[0].cells) * sizeof(T);
+    SCIHPC_CUDA(cudaMalloc(&zold, zbytes));
+    SCIHPC_CUDA(cudaMemset(zold, 0, zbytes));
+    SCIHPC_CUDA(cudaMalloc(&rho_pad, zbytes));
+    return SCIHPC_OK;
+}
+
+int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
+    D = make_dims(g);
+    if (D.ndim < 2) {
+        set_last_error("the pressure solver needs ndim 2 or 3");
+        return SCIHPC_ERR_UNSUPPORTED;
+    }
+    bc_ = bc;
+    density_ = density;
+    fp32_ = fp32;
+    const long long n = D.interior();
+    SCIHPC_CUDA(cudaMalloc(&r, 3 * n * sizeof(double)));
+    dvec = r + n;
+    q = dvec + n;
+    SCIHPC_CUDA(cudaMemset(r, 0, 3 * n * sizeof(double)));
+    SCIHPC_CUDA(cudaMalloc(&partial, 2 * RED_MAX_BLOCKS * sizeof(double) + 64));
+    SCIHPC_CUDA(cudaMemset(partial, 0, 2 * RED_MAX_BLOCKS * sizeof(double) + 64));
+    SCIHPC_CUDA(cudaMalloc(&dev_state, sizeof(PcgScalars)));
+    SCIHPC_CUDA(cudaMemset(dev_state, 0, sizeof(PcgScalars)));
+    SCIHPC_CUDA(cudaMallocHost(&host_state, sizeof(PcgScalars)));
+    int rc = fp32 ? alloc_levels<float>() : alloc_levels<double>();
+    if (rc) return rc;
+    if (!density) {
+        // constant coefficients: build the hierarchy once (rho unused)
+        cudaStream_t s = 0;
+        if (fp32) build_coarse<float>(s);
+        else build_coarse<double>(s);
+        SCIHPC_CUDA(cudaStreamSynchronize(s));
+    }
+    return SCIHPC_OK;
+}
+
+void Poisson::destroy() {
+    auto rel = [](void *p) {
+        if (p) cudaFree(p);
+    };
+    for (auto &L : Lf) rel(L.x), rel(L.b), rel(L.cx);
+    for (auto &L : Ld) rel(L.x), rel(L.b), rel(L.cx);
+    Lf.clear();
+    Ld.clear();
+    rel(r);
+    rel(partial);
+    rel(dev_state);
+    rel(dense);
+    rel(zold);
+    rel(rho_pad);
+    if (host_state) cudaFreeHost(host_state);
+    r = nullptr;
+}
+
+namespace {
+template <class T>
+__global__ void k_pad_rho(const double *__restrict__ rho, T *__restrict__ out, Dims D, Level<T> L0, int have_rho) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L0.cells) return;
+    int pi[3] = {0, 0, 0};
+    long long r = t;
+    if (D.ndim == 3) {
+        pi[2] = int(r % L0.P[2]);
+        r /= L0.P[2];
+    }
+    pi[1] = int(r % L0.P[1]);
+    pi[0] = int(r / L0.P[1]);
+    bool halo = false;
+    for (int a = 0; a < D.ndim; ++a) halo = halo || pi[a] == 0 || pi[a] == L0.P[a] - 1;
+    if (halo) {
+        out[t] = T(INFINITY);
+        return;
+    }
+    if (!have_rho) {
+        out[t] = T(1);
+        return;
+    }
+    const long long go = D.at(pi[0] - 1 + GHC, pi[1] - 1 + GHC, D.ndim == 3 ? pi[2] - 1 + GHC : 0);
+    out[t] = T(rho[go]);
+}
+}  // namespace
+
+template <class T>
+void Poisson::build_coarse(cudaStream_t s) {
+    std::vector<Level<T>> &Ls = levs<T>();
+    const bool neumann = bc_ == 0;
+    const int mode0 = (density_ || neumann) ? 1 : 2;
+    if (mode0 == 1) {
+        k_pad_rho<T><<<blocks_for(Ls[0].cells, TPB), TPB, 0, s>>>(rho64, (T *)rho_pad, D, Ls[0], density_ && rho64 != nullptr);
+    }
+    Id2<T> id2{};
+    for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? T(1.0 / (D.d[a] * D.d[a])) : T(0);
+    for (int l = 0; l + 1 < nlev; ++l) {
+        Level<T> &F = Ls[l], &Cl = Ls[l + 1];
+        for (int axis = 0; axis < D.ndim; ++axis) {
+            int E[3] = {Cl.n[0], Cl.n[1], D.ndim == 3 ? Cl.n[2] : 1};
+            E[axis] += 1;
+            const long long total = (long long)E[0] * E[1] * E[2];
+            const unsigned nb = blocks_for(total, TPB);
+            const T *rp = (const T *)rho_pad;
+            if (D.ndim == 2) {
+                if (l > 0) k_coarse_coef<T, 0, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+                else if (mode0 == 1) k_coarse_coef<T, 1, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+                else k_coarse_coef<T, 2, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+            } else {
+                if (l > 0) k_coarse_coef<T, 0, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+                else if (mode0 == 1) k_coarse_coef<T, 1, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+                else k_coarse_coef<T, 2, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+            }
+        }
+    }
+    Level<T> &C = Ls[nlev - 1];
+    double *M = dense, *W = dense + size_t(ncoarse) * ncoarse;
+    if (D.ndim == 2) k_dense_build<T, 2><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, M, ncoarse, neumann);
+    else k_dense_build<T, 3><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, M, ncoarse, neumann);
+    k_dense_pin_and_invert<<<1, 1024, 0, s>>>(M, W, ncoarse, neumann);
+}
+
+int Poisson::set_density(const double *rho, cudaStream_t s) {
+    rho64 = rho;
+    if (fp32_) build_coarse<float>(s);
+    else build_coarse<double>(s);
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+template <class T>
+void Poisson::vcycle(cudaStream_t s) {
+    std::vector<Level<T>> &Ls = levs<T>();
+    const bool neumann = bc_ == 0;
+    const int mode0 = (density_ || neumann) ? 1 : 2;
+    const T *rp = (const T *)rho_pad;
+    Id2<T> id2{};
+    for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? T(1.0 / (D.d[a] * D.d[a])) : T(0);
+    const int nu = 2;
+    auto smooth = [&](int l, int color) {
+        Level<T> &L = Ls[l];
+        const long long rows = D.ndim == 3 ? (long long)L.n[0] * L.n[1] : L.n[0];
+        const long long nh = (L.n[D.ndim - 1] + 1) / 2;
+        const unsigned nb = blocks_for(rows * nh, TPB);
+        const int m = l == 0 ? mode0 : 0;
+        if (D.ndim == 2) {
+            if (m == 0) k_smooth<T, 0, 2><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+            else if (m == 1) k_smooth<T, 1, 2><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+            else k_smooth<T, 2, 2><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+        } else {
+            if (m == 0) k_smooth<T, 0, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+            else if (m == 1) k_smooth<T, 1, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+            else k_smooth<T, 2, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+        }
+    };
+    cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
+    for (int l = 0; l + 1 < nlev; ++l) {
+        for (int k = 0; k < nu; ++k) {
+            smooth(l, 0);
+            smooth(l, 1);
+        }
+        Level<T> &F = Ls[l], &Cl = Ls[l + 1];
+        const long long nc = (long long)Cl.n[0] * Cl.n[1] * Cl.n[2];
+        const unsigned nb = blocks_for(nc, TPB);
+        const int m = l == 0 ? mode0 : 0;
+        if (D.ndim == 2) {
+            if (m == 0) k_restrict<T, 0, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+            else if (m == 1) k_restrict<T, 1, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+            else k_restrict<T, 2, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+        } else {
+            if (m == 0) k_restrict<T, 0, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+            else if (m == 1) k_restrict<T, 1, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+            else k_restrict<T, 2, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+        }
+    }
+    {
+        Level<T> &C = Ls[nlev - 1];
+        if (D.ndim == 2) k_dense_solve<T, 2><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
+        else k_dense_solve<T, 3><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
+    }
+    for (int l = nlev - 2; l >= 0; --l) {
+        Level<T> &F = Ls[l], &Cl = Ls[l + 1];
+        const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
+        if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann);
+        else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann);
+        for (int k = 0; k < nu; ++k) {
+            smooth(l, 1);
+            smooth(l, 0);
+        }
+    }
+}
+
+static Outer make_outer(const Dims &D, int density, int dirichlet) {
+    Outer O;
+    O.D = D;
+    for (int a = 0; a < 3; ++a) {
+        O.nint[a] = D.n[a];
+        O.id2[a] = a < D.ndim ? 1.0 / D.d[a] / D.d[a] : 0.0;
+    }
+    O.cs[2] = 1;
+    O.cs[1] = D.n[2];
+    O.cs[0] = (long long)D.n[1] * D.n[2];
+    O.density = density;
+    O.dirichlet = dirichlet;
+    return O;
+}
+
+void Poisson::begin(const double *rhs, double *p, int use_guess, cudaStream_t s) {
+    rhs_ = rhs;
+    p_ = p;
+    const long long n = D.interior();
+    const Outer O = make_outer(D, density_, bc_ == 1);
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
+    const int nb = grid_blocks(n);
+    cudaMemsetAsync(dev_state, 0, sizeof(PcgScalars), s);
+    if (bc_ == 0) k_rhs_sum<<<nb, TPB, 0, s>>>(rhs, O, n, slot, &dev_state->mean);
+    if (fp32_) k_init<float><<<nb, TPB, 0, s>>>(rhs, p, rho64, O, n, use_guess, r, Lf[0].b, Lf[0], slot, dev_state);
+    else k_init<double><<<nb, TPB, 0, s>>>(rhs, p, rho64, O, n, use_guess, r, Ld[0].b, Ld[0], slot, dev_state);
+    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 0, conditional, 0);
+}
+
+void Poisson::iterate(cudaStream_t s) {
+    const long long n = D.interior();
+    const Outer O = make_outer(D, density_, bc_ == 1);
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
+    const int nb = grid_blocks(n);
+    if (fp32_) {
+        vcycle<float>(s);
+        k_dot_rz<float><<<nb, TPB, 0, s>>>(r, Lf[0].x, (const float *)zold, O, Lf[0], n, slot, dev_state);
+        k_update_d<float><<<nb, TPB, 0, s>>>(Lf[0].x, (float *)zold, dvec, O, Lf[0], n, dev_state);
+    } else {
+        vcycle<double>(s);
+        k_dot_rz<double><<<nb, TPB, 0, s>>>(r, Ld[0].x, (const double *)zold, O, Ld[0], n, slot, dev_state);
+        k_update_d<double><<<nb, TPB, 0, s>>>(Ld[0].x, (double *)zold, dvec, O, Ld[0], n, dev_state);
+    }
+    k_apply_dq<<<nb, TPB, 0, s>>>(dvec, q, rho64, O, n, slot, dev_state);
+    if (fp32_) k_axpy<float><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Lf[0].b, O, Lf[0], n, slot, dev_state);
+    else k_axpy<double><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Ld[0].b, O, Ld[0], n, slot, dev_state);
+    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 1, conditional, use_conditional ? 1 : 0);
+}
+
+void Poisson::finish(double *p, cudaStream_t s) {
+    const long long n = D.interior();
+    const Outer O = make_outer(D, density_, bc_ == 1);
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
+    const int nb = grid_blocks(n);
+    if (bc_ == 0) {
+        k_p_sum<<<nb, TPB, 0, s>>>(p, O, n, slot, &dev_state->dq);
+        k_p_shift<<<nb, TPB, 0, s>>>(p, O, n, &dev_state->dq);
+    }
+    k_true_res<<<nb, TPB, 0, s>>>(rhs_, p, rho64, O, n, slot, dev_state);
+    k_relres<<<1, 1, 0, s>>>(dev_state);
+}
+
+int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int maxit, int *iters, double *relres,
+                   cudaStream_t s) {
+    rel_tol = tol;
+    max_iter = maxit;
+    use_conditional = false;
+    begin(rhs, p, use_guess, s);
+    SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    SCIHPC_CUDA(cudaStreamSynchronize(s));
+    while (!host_state->done) {
+        iterate(s);
+        SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        SCIHPC_CUDA(cudaStreamSynchronize(s));
+    }
+    const int it = host_state->it;
+    const bool div = host_state->diverged;
+    finish(p, s);
+    SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    SCIHPC_CUDA(cudaStreamSynchronize(s));
+    SCIHPC_CUDA(cudaGetLastError());
+    if (iters) *iters = it;
+    if (relres) *relres = host_state->relres;
+    if (div) {
+        set_last_error("pressure solve produced a non-finite residual");
+        return SCIHPC_ERR_NONFINITE;
+    }
+    if (host_state->relres > tol && it >= maxit) return SCIHPC_ERR_MAXITER;
+    return SCIHPC_OK;
+}
+
+int Poisson::levels(int *out, int max_levels) const {
+    for (int l = 0; l < nlev && l < max_levels; ++l) {
+        const int *n = fp32_ ? Lf[l].n : Ld[l].n;
+        out[3 * l] = n[0], out[3 * l + 1] = n[1], out[3 * l + 2] = n[2];
+    }
+    return nlev;
+}
+
+}  // namespace scihpc

@@ -1,0 +1,91 @@
+// poisson.cuh -- multigrid-preconditioned solver of the pressure equation.
+#pragma once
+
+#include <type_traits>
+#include <vector>
+
+#include "common.cuh"
+
+namespace scihpc {
+
+// One multigrid level in a padded layout with a one-cell halo that is kept at zero:
+// (nx+2) x (ny+2) [x (nz+2)], k fastest.  `coef` holds, for levels >= 1, the face
+// coefficients C = k / d^2 of the +x, +y, +z faces of every padded cell (three arrays).
+template <class T>
+struct Level {
+    int n[3] = {1, 1, 1};   // interior cells
+    int P[3] = {1, 1, 1};   // padded extents
+    long long s[3] = {0, 0, 0};
+    long long cells = 0;    // padded size
+    int ratio = 2;          // coarsening factor to the next level
+    double d[3] = {0, 0, 0};
+    T *x = nullptr, *b = nullptr;
+    T *cx = nullptr, *cy = nullptr, *cz = nullptr;
+};
+
+struct PcgScalars {
+    double bb;        // ||g||^2 of the projected right-hand side
+    double rr;        // ||r||^2
+    double rz, rz_prev, r_zold;
+    double dq;
+    double relres;
+    double mean;
+    int it, done, diverged, pad;
+};
+
+class Poisson {
+public:
+    // bc: 0 Neumann walls, 1 Dirichlet walls with zero ghost-centre value.
+    // density: 1 coefficients from a density field, 0 constant 1/d^2.
+    // fp32: V-cycles in single precision.
+    int create(const scihpc_grid *g, int bc, int density, int fp32);
+    void destroy();
+    int set_density(const double *rho, cudaStream_t s);
+    // Device-side pieces of one solve (no host synchronisation; usable in graph capture).
+    void begin(const double *rhs, double *p, int use_guess, cudaStream_t s);
+    void iterate(cudaStream_t s);   // one outer iteration incl. convergence test
+    void finish(double *p, cudaStream_t s);
+    // Host-driven solve: iterates until converged or max_iter (synchronising once per iteration).
+    int solve(const double *rhs, double *p, int use_guess, double rel_tol, int max_iter, int *iters, double *relres,
+              cudaStream_t s);
+    int levels(int *out, int max_levels) const;
+
+    double rel_tol = 1e-10;
+    int max_iter = 200;
+    PcgScalars *dev_state = nullptr;    // device
+    PcgScalars *host_state = nullptr;   // pinned mirror
+    unsigned long long *cond_handle = nullptr;   // graph conditional handle slot (device), 0 when unused
+    bool use_conditional = false;
+    unsigned long long conditional = 0;
+
+private:
+    template <class T>
+    std::vector<Level<T>> &levs() {
+        if constexpr (std::is_same_v<T, float>) return Lf;
+        else return Ld;
+    }
+    template <class T>
+    void vcycle(cudaStream_t s);
+    template <class T>
+    int alloc_levels();
+    template <class T>
+    void build_coarse(cudaStream_t s);
+
+    Dims D{};
+    int bc_ = 0, density_ = 1, fp32_ = 0;
+    int nlev = 0;
+    std::vector<Level<float>> Lf;
+    std::vector<Level<double>> Ld;
+    // FP64 outer iteration vectors (interior, compact, K fastest)
+    double *r = nullptr, *dvec = nullptr, *q = nullptr;
+    void *zold = nullptr;       // previous preconditioned residual, level-0 padded, T
+    void *rho_pad = nullptr;    // level-0 density, padded, T, +inf halo
+    const double *rho64 = nullptr;   // caller's ghosted density (FP64 operator)
+    double *partial = nullptr;       // reduction scratch (2 x RED_MAX_BLOCKS)
+    double *dense = nullptr;         // coarsest-level inverse (n x n, FP64)
+    int ncoarse = 0;
+    const double *rhs_ = nullptr;
+    double *p_ = nullptr;
+};
+
+}  // namespace scihpc

@@ -1,0 +1,941 @@
+// twophase.cu -- the two-phase projection time step on one GPU.
+//
+// The step is the reference drivers' loop (benchmarks_2d_bubble_rising.cpp:100-130):
+// find_dt, TVD-RK3 level-set advection, mass-preserving correction, ab_solve (sources,
+// Adams-Bashforth predictor, pressure Poisson solve, velocity correction) and Godunov
+// reinitialisation.  Everything stays resident in HBM; values that change from step to step
+// (dt, t, the mass-correction coefficient, reduction results) live in device memory so the
+// whole step can be captured once as a CUDA graph and replayed, with the pressure solve's
+// convergence loop as a conditional while-node inside the graph.
+//
+// Cells whose values the reference computes but never reads again (ghost cells that the
+// next boundary fill overwrites, and the corner ghosts no stencil reaches) are not
+// computed: stage updates, sources and corrections run on interior cells, followed by the
+// boundary fill, which reproduces every value that later work reads.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "levelset.cuh"
+#include "lsm_device.cuh"
+#include "reduce.cuh"
+#include "twophase.cuh"
+
+namespace scihpc {
+
+namespace {
+
+constexpr int TPB = 256;
+
+__device__ __forceinline__ bool interior_cell(long long q, const Dims &D, long long &o) {
+    if (q >= D.interior()) return false;
+    int I, J, K;
+    split3(q, D, I, J, K);
+    o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+    return true;
+}
+
+// ---------------------------------------------------------------- Runge-Kutta stages (runge_kutta.cpp:13-63)
+// stage 1: f += dt s1; stage 2: f += dt (s2 - 3 s1) / 4; stage 3: f += dt (-s1 - s2 + 8 s3) / 12;
+// stage 0: forward Euler f += dt s1.
+__global__ void k_stage(double *__restrict__ f, const double *__restrict__ s1, const double *__restrict__ s2,
+                        const double *__restrict__ s3, Dims D, int stage, const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const double dt = sc->dt;
+    if (stage <= 1) f[o] += dt * s1[o];
+    else if (stage == 2) f[o] += dt * (s2[o] - 3.0 * s1[o]) / 4.0;
+    else f[o] += dt * (-s1[o] - s2[o] + 8.0 * s3[o]) / 12.0;
+}
+
+// s = -u phi_x - v phi_y - w phi_z (source.cpp:8-40), interior cells
+__global__ void k_convection_s(double *__restrict__ s, const double *__restrict__ u, const double *__restrict__ v,
+                               const double *__restrict__ w, const double *__restrict__ fx,
+                               const double *__restrict__ fy, const double *__restrict__ fz, Dims D) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    double r = -u[o] * fx[o];
+    if (D.ndim > 1) r -= v[o] * fy[o];
+    if (D.ndim > 2) r -= w[o] * fz[o];
+    s[o] = r;
+}
+
+// ---------------------------------------------------------------- mass-preserving correction (source.cpp:109-154)
+// pass 1 (every cell): rho*H for lsf_mass, delta, |grad phi| from the CCD derivatives.
+__global__ void k_mpls_fields(const double *__restrict__ phi, const double *__restrict__ fx,
+                              const double *__restrict__ fy, const double *__restrict__ fz, double *__restrict__ w,
+                              double *__restrict__ H, double *__restrict__ De, double *__restrict__ G,
+                              double *__restrict__ Rho, Dims D, double lw, double dr, int pos) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.size()) return;
+    const double x = phi[q];
+    const double h = heaviside_d(x, lw);
+    const double rho = pos ? h + (1.0 - h) * dr : (1.0 - h) + h * dr;
+    w[q] = rho * h;
+    H[q] = h;
+    Rho[q] = rho;
+    De[q] = delta_d(x, lw);
+    double g = fx[q] * fx[q];
+    if (D.ndim > 1) g += fy[q] * fy[q];
+    if (D.ndim > 2) g += fz[q] * fz[q];
+    G[q] = sqrt(g);
+}
+
+// pass 2: sums of the lsf_mass contributions and of g delta |grad phi| over interior cells
+__global__ void k_mpls_sums(const double *__restrict__ w, const double *__restrict__ H, const double *__restrict__ De,
+                            const double *__restrict__ G, Dims D, double dr, int pos, double *__restrict__ partial) {
+    __shared__ double sh[RED_THREADS];
+    const long long n = D.interior();
+    const long long per_block = (n + gridDim.x - 1) / gridDim.x;
+    const long long b0 = blockIdx.x * per_block;
+    const long long b1 = b0 + per_block < n ? b0 + per_block : n;
+    const long long per = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    const long long t0 = b0 + threadIdx.x * per;
+    double sm = 0.0, se = 0.0;
+    for (long long q = t0; q < t0 + per && q < b1; ++q) {
+        int I, J, K;
+        split3(q, D, I, J, K);
+        const int i = D.ix(0, I), j = D.ix(1, J), k = D.ix(2, K);
+        const long long o = D.at(i, j, k);
+        // lsf_mass (wrapper_func.cpp:456-507)
+        if (D.ndim == 2) {
+            if (I != 0 && I != D.n[0] - 1 && J != 0 && J != D.n[1] - 1) {
+                double s = 15.0 * w[o];
+                for (int a = -1; a < 2; ++a)
+                    for (int b = -1; b < 2; ++b) s += w[o + a * D.s[0] + b * D.s[1]];
+                sm += s / 24.0;
+            } else {
+                sm += w[o];
+            }
+        } else {
+            if (I != 0 && I != D.n[0] - 1 && J != 0 && J != D.n[1] - 1 && K != 0 && K != D.n[2] - 1) {
+                double s = 50.0 * w[o];
+                for (int a = -1; a < 2; ++a)
+                    for (int b = -1; b < 2; ++b)
+                        for (int c = -1; c < 2; ++c) s += w[o + a * D.s[0] + b * D.s[1] + c];
+                sm += s * D.dv / 77.0;
+            } else {
+                sm += w[o] * D.dv;
+            }
+        }
+        const double de = De[o], hv = H[o];
+        const double g = pos ? de * (2.0 * (1.0 - dr) * hv + dr) : de * (2.0 * (dr - 1.0) * hv + 1.0);
+        se += g * de * G[o];
+    }
+    const double a = block_reduce<SumOp>(sm, sh);
+    __syncthreads();
+    const double b = block_reduce<SumOp>(se, sh);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = a;
+        partial[RED_MAX_BLOCKS + blockIdx.x] = b;
+    }
+}
+
+__global__ void k_mpls_finish(const double *__restrict__ partial, int nb, StepScalars *sc, double dv) {
+    __shared__ double sh[1024];
+    double v[2];
+    for (int m = 0; m < 2; ++m) {
+        const int per = (nb + blockDim.x - 1) / blockDim.x;
+        double a = 0.0;
+        for (int q = threadIdx.x * per; q < (threadIdx.x + 1) * per && q < nb; ++q) a += partial[m * RED_MAX_BLOCKS + q];
+        v[m] = block_reduce<SumOp>(a, sh);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double mass = v[0] * dv;
+        sc->mass = mass;
+        sc->eta = (sc->lsf_mass0 - mass) / (v[1] * dv * sc->dt);
+    }
+}
+
+// s = eta delta |grad phi|, then the Euler update (runge_kutta.cpp:51-63), interior cells
+__global__ void k_mpls_update(double *__restrict__ phi, const double *__restrict__ De, const double *__restrict__ G,
+                              Dims D, const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const double s = sc->eta * De[o] * G[o];
+    phi[o] += sc->dt * s;
+}
+
+// ---------------------------------------------------------------- reinitialisation (source.cpp:156-241)
+__global__ void k_sign(const double *__restrict__ phi, double *__restrict__ sg, long long n, double lw) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) sg[q] = sign_d(phi[q], lw);
+}
+
+// Godunov gradient, the redistance source and the lambda-correction fields a, b.
+__global__ void k_reinit_a(const double *__restrict__ phi, const double *__restrict__ sg,
+                           const double *__restrict__ De, double *__restrict__ G, double *__restrict__ s,
+                           double *__restrict__ A, double *__restrict__ B, Dims D, double rdt, const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const double g = godunov_at(phi, o, sg[o], D);
+    G[o] = g;
+    s[o] = -sg[o] * (g - 1.0) * rdt / sc->dt;
+    A[o] = sg[o] * De[o] * (g - 1.0);
+    B[o] = g * De[o] * De[o];
+}
+
+// lambda correction with the zero-order-extrapolated a, b (a ghost reads the nearest
+// interior cell) and the stage update (the update reads only per-cell fields, so it can
+// run in place on phi).
+__global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ De, const double *__restrict__ G,
+                           double *__restrict__ sk, const double *__restrict__ s1, const double *__restrict__ s2,
+                           const double *__restrict__ A, const double *__restrict__ B, Dims D, double rdt,
+                           int lambda, int stage, const StepScalars *sc) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.interior()) return;
+    int I, J, K;
+    split3(q, D, I, J, K);
+    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+    const double dt = sc->dt;
+    double s = sk[o];
+    if (lambda) {
+        auto cl = [&](int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); };
+        double a, b;
+        if (D.ndim == 2) {
+            a = 16.0 * A[o];
+            b = 16.0 * B[o];
+            for (int ii = -1; ii < 2; ii += 2)
+                for (int jj = -1; jj < 2; jj += 2) {
+                    const long long p = D.at(D.ix(0, cl(I + ii, D.n[0])), D.ix(1, cl(J + jj, D.n[1])), 0);
+                    a += A[p];
+                    b += B[p];
+                }
+        } else {
+            a = 51.0 * A[o];
+            b = 51.0 * B[o];
+            for (int ii = -1; ii < 2; ii += 2)
+                for (int jj = -1; jj < 2; jj += 2)
+                    for (int kk = -1; kk < 2; kk += 2) {
+                        const long long p = D.at(D.ix(0, cl(I + ii, D.n[0])), D.ix(1, cl(J + jj, D.n[1])),
+                                                 D.ix(2, cl(K + kk, D.n[2])));
+                        a += A[p];
+                        b += B[p];
+                    }
+        }
+        if (fabs(b) > 1e-8) s += a / b * De[o] * G[o] * rdt / dt;
+        sk[o] = s;
+    }
+    double &f = phi[o];
+    if (stage == 1) f += dt * s;
+    else if (stage == 2) f += dt * (s - 3.0 * s1[o]) / 4.0;
+    else f += dt * (-s1[o] - s2[o] + 8.0 * s) / 12.0;
+}
+
+// ---------------------------------------------------------------- projection method (projection_method.cpp)
+__global__ void k_props(const double *__restrict__ phi, double *H, double *De, double *Rho, double *Mu, long long n,
+                        double lw, double dr, double vr, int pos) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double x = phi[q];
+    const double h = heaviside_d(x, lw);
+    H[q] = h;
+    De[q] = delta_d(x, lw);
+    Rho[q] = pos ? h + (1.0 - h) * dr : (1.0 - h) + h * dr;
+    Mu[q] = pos ? h + (1.0 - h) * vr : (1.0 - h) + h * vr;
+}
+
+__global__ void k_copy(double *__restrict__ dst, const double *__restrict__ src, long long n) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) dst[q] = src[q];
+}
+
+// all_to_face_{x,y,z} (wrapper_func.cpp:177-265) on i in [1, Nx-2], j in [1, Ny-2] and, in
+// 3D, k in [1, Nz-2].
+__global__ void k_to_face(double *__restrict__ n0, double *__restrict__ n1, double *__restrict__ n2,
+                          const double *__restrict__ v0, const double *__restrict__ v1, const double *__restrict__ v2,
+                          Dims D, int a) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int e0 = D.N[0] - 2, e1 = D.N[1] - 2, e2 = D.ndim == 3 ? D.N[2] - 2 : D.N[2];
+    if (q >= (long long)e0 * e1 * e2) return;
+    const int k = int(q % e2) + (D.ndim == 3 ? 1 : 0);
+    const long long r = q / e2;
+    const int j = int(r % e1) + 1;
+    const int i = int(r / e1) + 1;
+    const long long o = D.at(i, j, k);
+    const long long s0 = D.s[0], s1 = D.s[1], s2 = D.ndim == 3 ? 1 : 0;
+    double *nv[3] = {n0, n1, n2};
+    const double *vv[3] = {v0, v1, v2};
+    nv[a][o] = vv[a][o];
+    for (int c = 0; c < D.ndim; ++c) {
+        if (c == a) continue;
+        const double *v = vv[c];
+        double r4;
+        if (a == 0) r4 = v[o] + v[o + s0] + v[o - (c == 1 ? s1 : s2)] + v[o + s0 - (c == 1 ? s1 : s2)];
+        else if (a == 1) r4 = c == 0 ? v[o] + v[o + s1] + v[o - s0] + v[o - s0 + s1] : v[o] + v[o + s1] + v[o - s2] + v[o + s1 - s2];
+        else r4 = c == 0 ? v[o] + v[o + s2] + v[o - s0] + v[o - s0 + s2] : v[o] + v[o + s2] + v[o - s1] + v[o - s1 + s2];
+        nv[c][o] = 0.25 * r4;
+    }
+}
+
+// add_stress_{x,y,z} (projection_method.cpp:31-182), added to src (which holds the
+// convection term), interior cells.
+struct StressArgs {
+    const double *delta, *mu, *rho, *pfx, *pfy, *pfz;
+    const double *Ufx, *Ufy, *Ufz, *Ufxx, *Ufyy, *Ufzz;   // derivatives of the component itself
+    const double *c1, *c2;   // cross terms: a=0: nv.fx, nw.fx; a=1: nu.fy, nw.fy; a=2: nu.fz, nv.fz
+    double *src;
+    double ref, vr, Re;
+};
+
+__global__ void k_stress(StressArgs S, Dims D, int a) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const long long sa = D.s[a];
+    auto avg = [&](const double *f) { return 0.5 * (f[o] + f[o + sa]); };
+    const double de = avg(S.delta), m = avg(S.mu), r = avg(S.rho);
+    const double px = avg(S.pfx), py = avg(S.pfy);
+    double p1, p2;
+    if (a == 0) {
+        p1 = S.Ufxx[o] + S.Ufyy[o];
+        p2 = 2.0 * px * S.Ufx[o] + py * (S.Ufy[o] + S.c1[o]);
+        if (D.ndim > 2) {
+            p1 += S.Ufzz[o];
+            p2 += avg(S.pfz) * (S.Ufz[o] + S.c2[o]);
+        }
+    } else if (a == 1) {
+        p1 = S.Ufxx[o] + S.Ufyy[o];
+        p2 = 2.0 * py * S.Ufy[o] + px * (S.Ufx[o] + S.c1[o]);
+        if (D.ndim > 2) {
+            p1 += S.Ufzz[o];
+            p2 += avg(S.pfz) * (S.Ufz[o] + S.c2[o]);
+        }
+    } else {
+        const double pz = avg(S.pfz);
+        p1 = S.Ufxx[o] + S.Ufyy[o];   // the reference has no w_zz term here (projection_method.cpp:171)
+        p2 = 2.0 * pz * S.Ufz[o] + px * (S.Ufx[o] + S.c1[o]) + py * (S.Ufy[o] + S.c2[o]);
+    }
+    p1 *= m;
+    p2 *= S.ref * de * (1.0 - S.vr);
+    S.src[o] += (p1 + p2) / S.Re / r;
+}
+
+// add_body_force + add_surface_force (projection_method.cpp:184-242) on interior cells.
+__global__ void k_forces(double *__restrict__ su, double *__restrict__ sv, double *__restrict__ sw,
+                         const double *__restrict__ curv, const double *__restrict__ De, const double *__restrict__ Rho,
+                         const double *__restrict__ fx, const double *__restrict__ fy, const double *__restrict__ fz,
+                         Dims D, double Fr, double We) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    if (Fr > 0.0) {
+        if (D.ndim == 2) sv[o] += -1.0 / Fr;
+        else if (D.ndim == 3) sw[o] += -1.0 / Fr;
+    }
+    if (We > 0.0) {
+        double *dst[3] = {su, sv, sw};
+        const double *pf[3] = {fx, fy, fz};
+        for (int a = 0; a < D.ndim; ++a) {
+            const long long st = D.s[a];
+            const double c = 0.5 * (curv[o] + curv[o + st]);
+            const double de = 0.5 * (De[o] + De[o + st]);
+            const double pp = 0.5 * (pf[a][o] + pf[a][o + st]);
+            const double r = 0.5 * (Rho[o] + Rho[o + st]);
+            dst[a][o] -= c * de * pp / (We * r);
+        }
+    }
+}
+
+// find_intermediate_velocity (projection_method.cpp:384-402), interior cells
+__global__ void k_ab2(double *__restrict__ u, double *__restrict__ v, double *__restrict__ w,
+                      const double *__restrict__ su, const double *__restrict__ sv, const double *__restrict__ sw,
+                      const double *__restrict__ ou, const double *__restrict__ ov, const double *__restrict__ ow, Dims D,
+                      const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const double dt = sc->dt;
+    u[o] += dt * (1.5 * su[o] - 0.5 * ou[o]);
+    v[o] += dt * (1.5 * sv[o] - 0.5 * ov[o]);
+    if (D.ndim == 3) w[o] += dt * (1.5 * sw[o] - 0.5 * ow[o]);
+}
+
+// divergence / dt into RHS (projection_method.cpp:546-568)
+__global__ void k_div_rhs(double *__restrict__ rhs, const double *__restrict__ u, const double *__restrict__ v,
+                          const double *__restrict__ w, Dims D, const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    double d = (u[o] - u[o - D.s[0]]) / D.d[0] + (v[o] - v[o - D.s[1]]) / D.d[1];
+    if (D.ndim > 2) d += (w[o] - w[o - 1]) / D.d[2];
+    rhs[o] = d / sc->dt;
+}
+
+// velocity correction of projection() (projection_method.cpp:630-654), interior cells
+__global__ void k_correct(double *__restrict__ u, double *__restrict__ v, double *__restrict__ w,
+                          const double *__restrict__ p, const double *__restrict__ Rho, Dims D, const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const double dt = sc->dt;
+    double r = 0.5 * (Rho[o] + Rho[o + D.s[0]]);
+    u[o] -= dt / D.d[0] / r * (p[o + D.s[0]] - p[o]);
+    r = 0.5 * (Rho[o] + Rho[o + D.s[1]]);
+    v[o] -= dt / D.d[1] / r * (p[o + D.s[1]] - p[o]);
+    if (D.ndim > 2) {
+        r = 0.5 * (Rho[o] + Rho[o + 1]);
+        w[o] -= dt / D.d[2] / r * (p[o + 1] - p[o]);
+    }
+}
+
+// node_from_face (wrapper_func.cpp:267-293), interior cells (the node BC fills the rest)
+__global__ void k_node_from_face(double *__restrict__ n0, double *__restrict__ n1, double *__restrict__ n2,
+                                 const double *__restrict__ u, const double *__restrict__ v,
+                                 const double *__restrict__ w, Dims D) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    n0[o] = 0.5 * (u[o] + u[o - D.s[0]]);
+    n1[o] = 0.5 * (v[o] + v[o - D.s[1]]);
+    if (D.ndim > 2) n2[o] = 0.5 * (w[o] + w[o - 1]);
+}
+
+// ---------------------------------------------------------------- find_dt (wrapper_func.cpp:335-385)
+// Maxima of |u|, |v|, |w| and the reference's running curvature bound m <- max(delta m, |kappa|)
+// in loop order.  The bound is a composition of maps m -> max(a m, b) with a >= 0, which is
+// associative: (a2, b2) o (a1, b1) = (a2 a1, max(a2 b1, b2)), so it reduces in a fixed tree.
+struct DtPart {
+    double mu, mv, mw, a, b;
+};
+
+__device__ __forceinline__ DtPart dt_combine(const DtPart &l, const DtPart &r) {
+    DtPart o;
+    o.mu = fmax(l.mu, r.mu);
+    o.mv = fmax(l.mv, r.mv);
+    o.mw = fmax(l.mw, r.mw);
+    o.a = r.a * l.a;
+    o.b = fmax(r.a * l.b, r.b);
+    return o;
+}
+
+__global__ void k_dt_part(const double *__restrict__ u, const double *__restrict__ v, const double *__restrict__ w,
+                          const double *__restrict__ De, const double *__restrict__ curv, Dims D,
+                          double *__restrict__ partial) {
+    __shared__ DtPart sh[RED_THREADS];
+    const long long n = D.interior();
+    const long long per_block = (n + gridDim.x - 1) / gridDim.x;
+    const long long b0 = blockIdx.x * per_block;
+    const long long b1 = b0 + per_block < n ? b0 + per_block : n;
+    const long long per = (b1 - b0 + blockDim.x - 1) / blockDim.x;
+    const long long t0 = b0 + threadIdx.x * per;
+    DtPart acc{0.0, 0.0, 0.0, 1.0, 0.0};
+    for (long long q = t0; q < t0 + per && q < b1; ++q) {
+        int I, J, K;
+        split3(q, D, I, J, K);
+        const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+        DtPart e{fabs(u[o]), fabs(v[o]), fabs(w[o]), De[o], fabs(curv[o])};
+        acc = dt_combine(acc, e);
+    }
+    const int t = threadIdx.x;
+    sh[t] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (t < s) sh[t] = dt_combine(sh[t], sh[t + s]);
+        __syncthreads();
+    }
+    if (t == 0) {
+        DtPart *pp = reinterpret_cast<DtPart *>(partial);
+        pp[blockIdx.x] = sh[0];
+    }
+}
+
+__global__ void k_dt_finish(const double *__restrict__ partial, int nb, StepScalars *sc, Dims D, HostParams P,
+                            int advance_time) {
+    if (threadIdx.x != 0) return;
+    const DtPart *pp = reinterpret_cast<const DtPart *>(partial);
+    DtPart acc{0.0, 0.0, 0.0, 1.0, 0.0};
+    for (int q = 0; q < nb; ++q) acc = dt_combine(acc, pp[q]);
+    const double mc = fmax(acc.a * 0.0, acc.b);
+    const double dx = D.d[0], dy = D.d[1], dz = D.d[2];
+    double conv = acc.mu / dx + acc.mv / dy;
+    if (D.ndim == 3) conv += acc.mw / dz;
+    double diff = 2.0 / (dx * dx) + 2.0 / (dy * dy);
+    if (D.ndim == 3) diff += 2.0 / (dz * dz);
+    diff *= P.viscosity_ratio / P.density_ratio / P.Re;
+    double grav = 0.0, surf = 0.0;
+    if (P.Fr > 0.0) grav = sqrt(fabs(1.0 - P.density_ratio) / (2 * P.density_ratio) / D.h / P.Fr);
+    if (P.We > 0.0) surf = sqrt(mc / (D.h * D.h) / P.We / P.density_ratio);
+    const double cfl = conv + diff + sqrt((conv + diff) * (conv + diff) + 4 * grav * grav + 4 * surf * surf);
+    sc->stable_CFL = 1.0 / cfl / D.h;
+    sc->dt_old2 = sc->dt_old;
+    sc->dt_old = sc->dt;
+    sc->dt = fmax(fmin(sc->stable_CFL, P.max_CFL), P.min_CFL) * D.h;
+    if (advance_time) {
+        sc->t += sc->dt;
+        sc->iter += 1.0;
+    }
+}
+
+__global__ void k_div_part(const double *__restrict__ u, const double *__restrict__ v, const double *__restrict__ w,
+                           Dims D, double *__restrict__ partial) {
+    __shared__ double sh[RED_THREADS];
+    double m = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < D.interior();
+         q += (long long)gridDim.x * blockDim.x) {
+        long long o;
+        interior_cell(q, D, o);
+        double d = (u[o] - u[o - D.s[0]]) / D.d[0] + (v[o] - v[o - D.s[1]]) / D.d[1];
+        if (D.ndim == 3) d += (w[o] - w[o - 1]) / D.d[2];
+        m = fmax(m, fabs(d));
+    }
+    m = block_reduce<MaxOp>(m, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+}
+
+}  // namespace
+
+// ================================================================= host side
+int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scalar_bc, const double *prm,
+                        const int *opt) {
+    D = make_dims(g);
+    if (D.ndim < 2) {
+        set_last_error("the two-phase step needs ndim 2 or 3");
+        return SCIHPC_ERR_UNSUPPORTED;
+    }
+    P.density_ratio = prm[0];
+    P.viscosity_ratio = prm[1];
+    P.Re = prm[2];
+    P.Fr = prm[3];
+    P.We = prm[4];
+    P.ls_width = prm[5];
+    P.rdt = prm[6];
+    P.max_CFL = prm[7];
+    P.min_CFL = prm[8];
+    P.positive_ref = prm[9] != 0.0;
+    P.ppe_tol = prm[10];
+    P.ppe_max_iter = int(prm[12]);
+    scheme = opt[0];
+    n_mpls = opt[1];
+    reinit_every = opt[2];
+    fp32 = opt[3];
+    reinit_lambda = opt[4];
+    // The wrapper turns a SLIP wall into NO_SLIP for the velocity component normal to it
+    // (wrapper.cpp:240-345).
+    for (int c = 0; c < 3; ++c)
+        for (int f = 0; f < 6; ++f) {
+            vel_types[c][f] = vel_bc[f];
+            if (f / 2 == c && vel_bc[f] == 3) vel_types[c][f] = 2;
+        }
+    for (int f = 0; f < 6; ++f) scalar_types[f] = scalar_bc[f];
+    int rc = ops.build(D);
+    if (rc) return rc;
+    SCIHPC_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    const size_t bytes = size_t(D.size()) * sizeof(double);
+    auto A = [&](double *&p) -> int {
+        SCIHPC_CUDA(cudaMalloc(&p, bytes));
+        SCIHPC_CUDA(cudaMemset(p, 0, bytes));
+        allocs.push_back(p);
+        return SCIHPC_OK;
+    };
+#define ALLOC(p)          \
+    do {                  \
+        int e_ = A(p);    \
+        if (e_) return e_; \
+    } while (0)
+    ALLOC(phi.data);
+    ALLOC(phi.flux);
+    for (int a = 0; a < 3; ++a) {
+        ALLOC(phi.d1[a]);
+        ALLOC(phi.d2[a]);
+        ALLOC(phi.mixed[a]);
+    }
+    ALLOC(pres.data);
+    ALLOC(pres.flux);
+    ALLOC(pres.old);
+    ALLOC(pres.old2);
+    for (int c = 0; c < 3; ++c) {
+        for (DevScalar *s : {&vel[c], &nvel[c]}) {
+            ALLOC(s->data);
+            ALLOC(s->flux);
+            for (int a = 0; a < 3; ++a) {
+                ALLOC(s->d1[a]);
+                ALLOC(s->d2[a]);
+            }
+        }
+        ALLOC(src[c]);
+        ALLOC(src_old[c]);
+    }
+    for (double **p : {&H, &delta, &sign, &grad, &curv, &a_f, &b_f, &rho, &mu, &RHS, &s1, &s2, &s3, &t1, &t2, &work})
+        ALLOC(*p);
+#undef ALLOC
+    SCIHPC_CUDA(cudaMalloc(&partial, 8 * RED_MAX_BLOCKS * sizeof(double)));
+    allocs.push_back(partial);
+    SCIHPC_CUDA(cudaMalloc(&sc, sizeof(StepScalars)));
+    allocs.push_back(sc);
+    SCIHPC_CUDA(cudaMallocHost(&sc_host, sizeof(StepScalars)));
+    std::memset(sc_host, 0, sizeof(StepScalars));
+    sc_host->dt = prm[15];
+    SCIHPC_CUDA(cudaMemcpy(sc, sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice));
+    scihpc_grid gg = *g;
+    rc = ppe.create(&gg, 0, 1, fp32);
+    if (rc) return rc;
+    // the reinitialisation loop length (benchmarks_2d_bubble_rising.cpp:122-129) depends only on
+    // rdt and ls_width
+    reinit_steps = 0;
+    while (reinit_steps * P.rdt < 2.0 * P.ls_width) ++reinit_steps;
+    return SCIHPC_OK;
+}
+
+void TwoPhaseGpu::destroy() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+    ppe.destroy();
+    ops.release();
+    for (void *p : allocs) cudaFree(p);
+    allocs.clear();
+    if (sc_host) cudaFreeHost(sc_host);
+    sc_host = nullptr;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+}
+
+double *TwoPhaseGpu::field(const std::string &s) {
+    if (s == "phi") return phi.data;
+    if (s == "p") return pres.data;
+    if (s == "p_old") return pres.old;
+    if (s == "p_old2") return pres.old2;
+    if (s == "u") return vel[0].data;
+    if (s == "v") return vel[1].data;
+    if (s == "w") return vel[2].data;
+    if (s == "nu") return nvel[0].data;
+    if (s == "nv") return nvel[1].data;
+    if (s == "nw") return nvel[2].data;
+    if (s == "rho") return rho;
+    if (s == "mu") return mu;
+    if (s == "delta") return delta;
+    if (s == "heaviside") return H;
+    if (s == "curvature") return curv;
+    if (s == "sign") return sign;
+    if (s == "grad") return grad;
+    if (s == "u_src") return src[0];
+    if (s == "v_src") return src[1];
+    if (s == "w_src") return src[2];
+    if (s == "u_src_old") return src_old[0];
+    if (s == "v_src_old") return src_old[1];
+    if (s == "w_src_old") return src_old[2];
+    if (s == "rhs") return RHS;
+    return nullptr;
+}
+
+int TwoPhaseGpu::get_scalars(double *out) {
+    SCIHPC_CUDA(cudaMemcpyAsync(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    out[0] = sc_host->t;
+    out[1] = sc_host->dt;
+    out[2] = sc_host->dt_old;
+    out[3] = sc_host->dt_old2;
+    out[4] = sc_host->iter;
+    out[5] = sc_host->stable_CFL;
+    out[6] = sc_host->lsf_mass0;
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::set_scalars(const double *in) {
+    SCIHPC_CUDA(cudaMemcpyAsync(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    sc_host->t = in[0];
+    sc_host->dt = in[1];
+    sc_host->dt_old = in[2];
+    sc_host->dt_old2 = in[3];
+    sc_host->iter = in[4];
+    sc_host->stable_CFL = in[5];
+    sc_host->lsf_mass0 = in[6];
+    SCIHPC_CUDA(cudaMemcpyAsync(sc, sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    return SCIHPC_OK;
+}
+
+void TwoPhaseGpu::scalar_bc(double *f) {
+    static const double zero[6] = {0, 0, 0, 0, 0, 0};
+    launch_bc_fill(D, 0, scalar_types, zero, f, stream);
+}
+
+void TwoPhaseGpu::vel_bc(DevScalar *v, int location_for_all) {
+    static const double zero[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < D.ndim; ++c) {
+        const int loc = location_for_all >= 0 ? location_for_all : 1 + c;
+        launch_bc_fill(D, loc, vel_types[c], zero, v[c].data, stream);
+    }
+}
+
+void TwoPhaseGpu::find_dt() {
+    const int nb = red_blocks(D.interior());
+    k_dt_part<<<nb, RED_THREADS, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, delta, curv, D, partial);
+    k_dt_finish<<<1, 32, 0, stream>>>(partial, nb, sc, D, P, 0);
+}
+
+void TwoPhaseGpu::convection_rhs(double *s) {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    if (scheme == 1) {
+        // identity_flux: flux = data; WENO reads data directly
+        for (int a = 0; a < D.ndim; ++a) launch_weno5(D, a, phi.data, nvel[a].data, phi.d1[a], stream);
+    } else {
+        for (int a = 0; a < D.ndim; ++a)
+            launch_uccd(D, ops, a, phi.data, nvel[a].data, phi.d1[a], phi.d2[a], t1, t2, stream);
+    }
+    k_convection_s<<<nbi, TPB, 0, stream>>>(s, nvel[0].data, nvel[1].data, nvel[2].data, phi.d1[0], phi.d1[1],
+                                            phi.d1[2], D);
+}
+
+void TwoPhaseGpu::advect() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    double *S[3] = {s1, s2, s3};
+    for (int st = 1; st <= 3; ++st) {
+        convection_rhs(S[st - 1]);
+        k_stage<<<nbi, TPB, 0, stream>>>(phi.data, s1, s2, s3, D, st, sc);
+        scalar_bc(phi.data);
+    }
+}
+
+void TwoPhaseGpu::mpls(int count) {
+    const unsigned nbf = blocks_for(D.size(), TPB), nbi = blocks_for(D.interior(), TPB);
+    const int nb = red_blocks(D.interior());
+    for (int c = 0; c < count; ++c) {
+        launch_extrapolate(D, 0, phi.data, phi.flux, stream);
+        for (int a = 0; a < D.ndim; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], stream);
+        k_mpls_fields<<<nbf, TPB, 0, stream>>>(phi.data, phi.d1[0], phi.d1[1], phi.d1[2], work, H, delta, grad, rho, D,
+                                               P.ls_width, P.density_ratio, P.positive_ref);
+        k_mpls_sums<<<nb, RED_THREADS, 0, stream>>>(work, H, delta, grad, D, P.density_ratio, P.positive_ref, partial);
+        k_mpls_finish<<<1, 1024, 0, stream>>>(partial, nb, sc, D.dv);
+        k_mpls_update<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, D, sc);
+        scalar_bc(phi.data);
+    }
+}
+
+void TwoPhaseGpu::reinit_stage(int stage) {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    double *S[3] = {s1, s2, s3};
+    k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
+    k_reinit_b<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, S[stage - 1], s1, s2, a_f, b_f, D, P.rdt, reinit_lambda,
+                                        stage, sc);
+    scalar_bc(phi.data);
+}
+
+int TwoPhaseGpu::reinit() {
+    k_sign<<<blocks_for(D.size(), TPB), TPB, 0, stream>>>(phi.data, sign, D.size(), P.ls_width);
+    for (int k = 0; k < reinit_steps; ++k)
+        for (int st = 1; st <= 3; ++st) reinit_stage(st);
+    return reinit_steps;
+}
+
+void TwoPhaseGpu::find_source() {
+    const long long N = D.size();
+    const unsigned nbf = blocks_for(N, TPB), nbi = blocks_for(D.interior(), TPB);
+    for (int c = 0; c < D.ndim; ++c) k_copy<<<nbf, TPB, 0, stream>>>(src_old[c], src[c], N);
+    k_props<<<nbf, TPB, 0, stream>>>(phi.data, H, delta, rho, mu, N, P.ls_width, P.density_ratio, P.viscosity_ratio,
+                                     P.positive_ref);
+    launch_extrapolate(D, 0, phi.data, phi.flux, stream);
+    for (int a = 0; a < D.ndim; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], stream);
+    launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, stream);
+    if (D.ndim > 2) {
+        launch_ccd_mixed(D, ops, 2, phi.d1[1], phi.mixed[1], work, stream);
+        launch_ccd_mixed(D, ops, 0, phi.d1[2], phi.mixed[2], work, stream);
+    }
+    const double ref = P.positive_ref ? 1.0 : -1.0;
+    const long long e2 = D.ndim == 3 ? D.N[2] - 2 : D.N[2];
+    const long long nface = (long long)(D.N[0] - 2) * (D.N[1] - 2) * e2;
+    for (int a = 0; a < D.ndim; ++a) {
+        k_to_face<<<blocks_for(nface, TPB), TPB, 0, stream>>>(nvel[0].data, nvel[1].data, nvel[2].data, vel[0].data,
+                                                              vel[1].data, vel[2].data, D, a);
+        vel_bc(nvel, 1 + a);
+        // convection of the a-component by the face-averaged velocity (source.cpp:8-40 with
+        // identity_with_extrapolation_face_*)
+        DevScalar &U = vel[a];
+        launch_extrapolate(D, 1 + a, U.data, U.flux, stream);
+        for (int b = 0; b < D.ndim; ++b) launch_uccd(D, ops, b, U.flux, nvel[b].data, U.d1[b], U.d2[b], t1, t2, stream);
+        k_convection_s<<<nbi, TPB, 0, stream>>>(src[a], nvel[0].data, nvel[1].data, nvel[2].data, U.d1[0], U.d1[1],
+                                                U.d1[2], D);
+        // cross derivatives of the other face-averaged components along a
+        for (int c = 0; c < D.ndim; ++c) {
+            if (c == a) continue;
+            launch_extrapolate(D, 1 + a, nvel[c].data, nvel[c].flux, stream);
+            launch_uccd(D, ops, a, nvel[c].flux, nvel[a].data, nvel[c].d1[a], nvel[c].d2[a], t1, t2, stream);
+        }
+        StressArgs S;
+        S.delta = delta, S.mu = mu, S.rho = rho;
+        S.pfx = phi.d1[0], S.pfy = phi.d1[1], S.pfz = phi.d1[2];
+        S.Ufx = U.d1[0], S.Ufy = U.d1[1], S.Ufz = U.d1[2];
+        S.Ufxx = U.d2[0], S.Ufyy = U.d2[1], S.Ufzz = U.d2[2];
+        if (a == 0) S.c1 = nvel[1].d1[0], S.c2 = nvel[2].d1[0];
+        else if (a == 1) S.c1 = nvel[0].d1[1], S.c2 = nvel[2].d1[1];
+        else S.c1 = nvel[0].d1[2], S.c2 = nvel[1].d1[2];
+        S.src = src[a];
+        S.ref = ref, S.vr = P.viscosity_ratio, S.Re = P.Re;
+        k_stress<<<nbi, TPB, 0, stream>>>(S, D, a);
+    }
+    if (P.We > 0.0) {
+        const double *d[9] = {phi.d1[0], phi.d1[1], phi.d1[2], phi.d2[0], phi.d2[1], phi.d2[2],
+                              phi.mixed[0], phi.mixed[1], phi.mixed[2]};
+        launch_curvature(D, phi.data, d, curv, stream);
+    }
+    k_forces<<<nbi, TPB, 0, stream>>>(src[0], src[1], src[2], curv, delta, rho, phi.d1[0], phi.d1[1], phi.d1[2], D,
+                                      P.Fr, P.We);
+}
+
+void TwoPhaseGpu::ab_solve_pre() {
+    const long long N = D.size();
+    const unsigned nbf = blocks_for(N, TPB), nbi = blocks_for(D.interior(), TPB);
+    // scalar_data::store (scalar_data.cpp:125-135)
+    k_copy<<<nbf, TPB, 0, stream>>>(pres.old2, pres.old, N);
+    k_copy<<<nbf, TPB, 0, stream>>>(pres.old, pres.data, N);
+    find_source();
+    k_ab2<<<nbi, TPB, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, src[0], src[1], src[2], src_old[0],
+                                   src_old[1], src_old[2], D, sc);
+    vel_bc(vel, -1);
+    k_div_rhs<<<nbi, TPB, 0, stream>>>(RHS, vel[0].data, vel[1].data, vel[2].data, D, sc);
+    ppe.set_density(rho, stream);
+    ppe.rel_tol = P.ppe_tol;
+    ppe.max_iter = P.ppe_max_iter;
+    ppe.begin(RHS, pres.data, 1, stream);
+}
+
+void TwoPhaseGpu::ab_solve_post() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    ppe.finish(pres.data, stream);
+    scalar_bc(pres.data);
+    k_correct<<<nbi, TPB, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, pres.data, rho, D, sc);
+    vel_bc(vel, -1);
+    k_node_from_face<<<nbi, TPB, 0, stream>>>(nvel[0].data, nvel[1].data, nvel[2].data, vel[0].data, vel[1].data,
+                                              vel[2].data, D);
+    vel_bc(nvel, 0);
+}
+
+int TwoPhaseGpu::ab_solve(int *iters, double *relres) {
+    ppe.use_conditional = false;
+    ab_solve_pre();
+    SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    while (!ppe.host_state->done) {
+        ppe.iterate(stream);
+        SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
+        SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    }
+    const int it = ppe.host_state->it;
+    ab_solve_post();
+    SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    last_iters = it;
+    last_relres = ppe.host_state->relres;
+    if (iters) *iters = it;
+    if (relres) *relres = ppe.host_state->relres;
+    if (ppe.host_state->diverged) {
+        set_last_error("pressure solve produced a non-finite residual");
+        return SCIHPC_ERR_NONFINITE;
+    }
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::init() {
+    scalar_bc(phi.data);
+    find_source();
+    const double prm[4] = {P.ls_width, P.density_ratio, P.viscosity_ratio, double(P.positive_ref)};
+    launch_lsf_integral(D, prm, phi.data, 0, work, partial, &sc->lsf_mass0, stream);
+    // lsf_mass multiplies the sum by dv once more at the end (wrapper_func.cpp:510)
+    SCIHPC_CUDA(cudaMemcpyAsync(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    sc_host->lsf_mass0 *= D.dv;
+    SCIHPC_CUDA(cudaMemcpyAsync(sc, sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+namespace {
+__global__ void k_advance_time(StepScalars *sc) {
+    sc->t += sc->dt;
+    sc->iter += 1.0;
+}
+}  // namespace
+
+int TwoPhaseGpu::capture_step() {
+    // Graph of one time step: [pre-solve kernels] -> while(not converged){ one pressure
+    // iteration } -> [post-solve kernels, reinitialisation].
+    cudaGraph_t g;
+    SCIHPC_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle handle;
+    SCIHPC_CUDA(cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault));
+    ppe.use_conditional = true;
+    ppe.conditional = (unsigned long long)handle;
+
+    cudaGraph_t pre_g, body_g_dummy, post_g;
+    (void)body_g_dummy;
+    SCIHPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    find_dt();
+    k_advance_time<<<1, 1, 0, stream>>>(sc);
+    advect();
+    mpls(n_mpls);
+    ab_solve_pre();
+    SCIHPC_CUDA(cudaStreamEndCapture(stream, &pre_g));
+
+    cudaGraphNode_t pre_node, cond_node, post_node;
+    SCIHPC_CUDA(cudaGraphAddChildGraphNode(&pre_node, g, nullptr, 0, pre_g));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    SCIHPC_CUDA(cudaGraphAddNode(&cond_node, g, &pre_node, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    SCIHPC_CUDA(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    ppe.iterate(stream);
+    SCIHPC_CUDA(cudaStreamEndCapture(stream, &body));
+
+    SCIHPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    ab_solve_post();
+    // step counter handled on the host: reinit runs every `reinit_every` steps; the graph
+    // is captured for the common case reinit_every == 1 (otherwise the host calls reinit)
+    if (reinit_every == 1) reinit();
+    SCIHPC_CUDA(cudaStreamEndCapture(stream, &post_g));
+    SCIHPC_CUDA(cudaGraphAddChildGraphNode(&post_node, g, &cond_node, 1, post_g));
+    SCIHPC_CUDA(cudaGraphInstantiate(&graph_exec, g, 0));
+    graph = g;
+    cudaGraphDestroy(pre_g);
+    cudaGraphDestroy(post_g);
+    ppe.use_conditional = false;
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::step(int nsteps, bool use_graph) {
+    if (use_graph && !graph_exec) {
+        int rc = capture_step();
+        if (rc) return rc;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        if (use_graph) {
+            SCIHPC_CUDA(cudaGraphLaunch(graph_exec, stream));
+            ++step_count;
+            if (reinit_every > 1 && step_count % reinit_every == 0) reinit();
+        } else {
+            find_dt();
+            k_advance_time<<<1, 1, 0, stream>>>(sc);
+            advect();
+            mpls(n_mpls);
+            int it;
+            double rr;
+            int rc = ab_solve(&it, &rr);
+            if (rc) return rc;
+            ++step_count;
+            if (reinit_every > 0 && step_count % reinit_every == 0) reinit();
+        }
+    }
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::diagnostics(double *out) {
+    const double prm[4] = {P.ls_width, P.density_ratio, P.viscosity_ratio, double(P.positive_ref)};
+    launch_lsf_integral(D, prm, phi.data, 0, work, partial, &sc->red[0], stream);
+    launch_lsf_integral(D, prm, phi.data, 1, work, partial, &sc->red[1], stream);
+    const int nb = red_blocks(D.interior());
+    k_div_part<<<nb, RED_THREADS, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, D, partial);
+    finish_reduce<MaxOp><<<1, 1024, 0, stream>>>(partial, nb, &sc->red[2]);
+    SCIHPC_CUDA(cudaMemcpyAsync(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    out[0] = sc_host->red[0] * D.dv;
+    out[1] = sc_host->red[1] * D.dv;
+    out[2] = sc_host->red[2];
+    last_iters = ppe.host_state ? ppe.host_state->it : 0;
+    return SCIHPC_OK;
+}
+
+}  // namespace scihpc

@@ -1,0 +1,82 @@
+// twophase.cuh -- one two-phase problem resident on the GPU.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "compact.cuh"
+#include "poisson.cuh"
+
+namespace scihpc {
+
+// The arrays of one scalar_data that the step uses (scalar_data.h:14-17).
+struct DevScalar {
+    double *data = nullptr, *flux = nullptr, *old = nullptr, *old2 = nullptr;
+    double *d1[3] = {nullptr, nullptr, nullptr};   // fx, fy, fz
+    double *d2[3] = {nullptr, nullptr, nullptr};   // fxx, fyy, fzz
+    double *mixed[3] = {nullptr, nullptr, nullptr};   // fxy, fyz, fzx
+};
+
+struct HostParams {
+    double density_ratio, viscosity_ratio, Re, Fr, We, ls_width, rdt, max_CFL, min_CFL;
+    int positive_ref;
+    double ppe_tol;
+    int ppe_max_iter;
+};
+
+class TwoPhaseGpu {
+public:
+    int create(const scihpc_grid *g, const int *vel_bc, const int *scalar_bc, const double *prm, const int *opt);
+    void destroy();
+    double *field(const std::string &name);
+    int get_scalars(double *out);
+    int set_scalars(const double *in);
+
+    // stages (asynchronous on `stream`)
+    void find_dt();
+    void advect();
+    void mpls(int count);
+    int reinit();            // returns RK3 steps
+    void find_source();
+    void ab_solve_pre();     // store, find_source, AB2, PPE right-hand side, solver begin
+    void ab_solve_post();    // solver finish, pressure BC, velocity correction, node velocity
+    int ab_solve(int *iters, double *relres);   // host-driven pressure iteration
+    int init();
+    int step(int nsteps, bool graph);
+    int diagnostics(double *out);
+
+    cudaStream_t stream = nullptr;
+    Dims D{};
+    double last_iters = 0, last_relres = 0, last_ms = 0;
+
+private:
+    void scalar_bc(double *f);
+    void vel_bc(DevScalar *v, int location_for_all);
+    void rk_stage_update(int stage);
+    void convection_rhs(double *s);
+    void reinit_stage(int stage);
+    int capture_step();
+
+    HostParams P{};
+    int scheme = 1, n_mpls = 5, reinit_every = 1, fp32 = 0, reinit_lambda = 1;
+    int step_count = 0;
+    int vel_types[3][6];
+    int scalar_types[6];
+    CompactOps ops;
+    Poisson ppe;
+    DevScalar phi, pres, vel[3], nvel[3];
+    double *H = nullptr, *delta = nullptr, *sign = nullptr, *grad = nullptr, *curv = nullptr, *a_f = nullptr,
+           *b_f = nullptr, *rho = nullptr, *mu = nullptr;
+    double *src[3] = {nullptr, nullptr, nullptr}, *src_old[3] = {nullptr, nullptr, nullptr};
+    double *RHS = nullptr, *s1 = nullptr, *s2 = nullptr, *s3 = nullptr, *t1 = nullptr, *t2 = nullptr, *work = nullptr;
+    double *partial = nullptr;
+    StepScalars *sc = nullptr;        // device
+    StepScalars *sc_host = nullptr;   // pinned
+    std::vector<void *> allocs;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    int reinit_steps = 0;
+};
+
+}  // namespace scihpc

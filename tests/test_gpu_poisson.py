@@ -1,0 +1,121 @@
+"""Pressure Poisson solver (scihpc_poisson_*) against the CPU checkers.
+
+Converged fields are compared (the iterates differ: red-black Gauss-Seidel multigrid with
+CG acceleration here, steepest-descent multigrid / SOR / CG in the checkers).  Both sides
+solve to a relative residual far below the parity tolerance, so the difference is the
+solution's own round-off: pressure within 1e-9 relative L2."""
+import numpy as np
+import pytest
+
+import oracle as O
+from tests.helpers import bubble_phi, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+PARITY = 1e-9
+
+
+@pytest.fixture(scope="module")
+def port():
+    return O.Checker("port")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def native(g):
+    from scihpc_gb300 import Grid
+    return Grid(g.ndim, tuple(g.n), tuple(g.lo), tuple(g.hi))
+
+
+def ghosted_from_mg(g, v):
+    """x-fastest multigrid vector -> ghosted [Nx][Ny][Nz] field (interior cells)."""
+    out = np.zeros(g.shape)
+    if g.ndim == 2:
+        out[3:-3, 3:-3, 0] = v.reshape(g.n[1], g.n[0]).T
+    else:
+        out[3:-3, 3:-3, 3:-3] = v.reshape(g.n[2], g.n[1], g.n[0]).transpose(2, 1, 0)
+    return out
+
+
+@pytest.mark.parametrize("n", [32, 64])
+@pytest.mark.parametrize("fp32", [False, True])
+def test_dirichlet_constant_matches_reference_multigrid(port, n, fp32):
+    """cfg-1 problem (-lap p = 2 pi^2 sin sin, the reference's Dirichlet operator with the
+    zero at the ghost-cell centre, multigrid_base.cpp:293-345) at a reduced size."""
+    from scihpc_gb300 import Poisson
+    g = O.Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    h = 1.0 / n
+    xc = (np.arange(n) + 0.5) * h
+    X, Y = np.meshgrid(xc, xc, indexing="ij")
+    f = 2 * np.pi ** 2 * np.sin(np.pi * X) * np.sin(np.pi * Y)
+    rhs_mg = (-f).T.ravel()                       # A p = -f, x-fastest
+    ref, cyc, hist = port.mg_poisson(g, rhs_mg, True, 1e-14, 400)
+    ref = ghosted_from_mg(g, ref)
+    rhs = np.zeros(g.shape)
+    rhs[3:-3, 3:-3, 0] = -f
+    ps = Poisson(native(g), bc=1, density=False, fp32=fp32)
+    p = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-13, max_iter=100)
+    out = p.cpu().numpy()
+    I = g.interior()
+    assert rr <= 1e-13, rr
+    assert rel_l2(out[I], ref[I]) <= PARITY, rel_l2(out[I], ref[I])
+
+
+def _density_case(g, seed):
+    rng = np.random.default_rng(seed)
+    if g.ndim == 2:
+        phi = bubble_phi(g, (0.5, 0.5 * g.hi[1] / 2 + 0.25), 0.2)
+    else:
+        c = g.spacing()
+        xs = [g.lo[a] + (np.arange(g.n[a]) + 0.5) * c[a] for a in range(3)]
+        X, Y, Z = np.meshgrid(*xs, indexing="ij")
+        phi = np.zeros(g.shape)
+        d = np.full(X.shape, -1e9)
+        for s in range(3):
+            r = rng.uniform(0.1, 0.2)
+            cen = rng.uniform(r, 1 - r, size=3)
+            d = np.maximum(d, r - np.sqrt((X - cen[0]) ** 2 + (Y - cen[1]) ** 2 + (Z - cen[2]) ** 2))
+        phi[3:-3, 3:-3, 3:-3] = d
+    phi = O.Checker("port").bc_fill(g, 0, [1] * 6, [0.0] * 6, phi)
+    h = min(g.spacing())
+    H = np.where(phi < -1.5 * h, 0.0, np.where(phi > 1.5 * h, 1.0,
+                 0.5 * (1 + phi / (1.5 * h) + np.sin(np.pi * phi / (1.5 * h)) / np.pi)))
+    rho = (1.0 - H) + H * 0.001
+    rhs = np.zeros(g.shape)
+    I = g.interior()
+    rhs[I] = rng.standard_normal(rhs[I].shape)
+    rhs[I] -= rhs[I].mean()
+    return rho, rhs
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+@pytest.mark.parametrize("case", ["2d", "3d"])
+def test_variable_density_matches_exact_solve(port, fp32, case):
+    """Density ratio 1000 pressure equation of projection() (coefficients of
+    init_ppe_proj_coefficients, projection_method.cpp:404-465, Neumann walls, zero mean)."""
+    from scihpc_gb300 import Poisson
+    g = O.Grid(2, (32, 64), (0.0, 0.0), (1.0, 2.0)) if case == "2d" else O.Grid(3, (16, 16, 16), (0, 0, 0), (1, 1, 1))
+    rho, rhs = _density_case(g, 5)
+    ref, it_ref, rel_ref = port.coef_solve(g, rho, rhs, rel_tol=1e-14, max_iter=200000)
+    ps = Poisson(native(g), bc=0, density=True, fp32=fp32)
+    ps.set_density(dev(rho))
+    p = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-13, max_iter=200)
+    out = p.cpu().numpy()
+    I = g.interior()
+    assert rr <= 1e-13, (rr, it)
+    assert abs(out[I].mean()) <= 1e-12 * np.abs(out[I]).max()
+    assert rel_l2(out[I], ref[I]) <= PARITY, rel_l2(out[I], ref[I])
+
+
+def test_levels_follow_reference_rule(port):
+    from scihpc_gb300 import Poisson
+    for nd, n in [(2, (128, 256)), (2, (256, 256)), (3, (128, 64, 64)), (3, (64, 64, 64))]:
+        g = O.Grid(nd, n, (0,) * nd, (1,) * nd)
+        ps = Poisson(native(g), bc=0, density=True, fp32=False)
+        assert [tuple(l[:nd]) for l in ps.levels()] == [tuple(l[:nd]) for l in port.mg_levels(nd, n)]
