@@ -24,6 +24,11 @@ FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path
          "--expt-relaxed-constexpr"]
 
 
+# Per-file flags: the boundary fills must round exactly like the reference's separate
+# multiply and add, so contraction into fused multiply-adds is off there.
+FILE_FLAGS = {"bc.cu": ["-fmad=false"]}
+
+
 def nvcc() -> str:
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -49,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(OBJ, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([cc, *ARCH, *FLAGS, "-c", s, "-o", o])
+            jobs.append([cc, *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(s), []), "-c", s, "-o", o])
 
     def run(cmd):
         if verbose:

@@ -250,6 +250,30 @@ __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const dou
     grid_sum<1>(v, slot, o);
 }
 
+// Residual replacement: once the recursively updated residual meets the tolerance, replace it
+// by the true residual g - L p (the recursion drifts by round-off), so that convergence is
+// declared on the true residual.
+template <class T>
+__global__ void k_replace(const double *__restrict__ rhs, const double *__restrict__ p, const double *__restrict__ rho,
+                          Outer O, long long n, double *__restrict__ r, T *__restrict__ b0, Level<T> L0, double tol,
+                          RedSlot slot, PcgScalars *st) {
+    if (st->done || !(st->rr <= tol * tol * st->bb)) return;
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(n);
+    double v[1] = {0.0};
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        split_int(q, O, I, J, K);
+        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
+        const double rv = -(rhs[go] - mean) - apply_L<true>(p, rho, O, I, J, K);
+        r[q] = rv;
+        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
+        b0[P0] = T(rv);
+        v[0] += rv * rv;
+    }
+    double *o[1] = {&st->rr};
+    grid_sum<1>(v, slot, o);
+}
+
 // Convergence test; in graph mode it also drives the conditional while-node.
 __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
                         int use_handle) {
@@ -914,8 +938,13 @@ void Poisson::iterate(cudaStream_t s) {
         k_update_d<double><<<nb, TPB, 0, s>>>(Ld[0].x, (double *)zold, dvec, O, Ld[0], n, dev_state);
     }
     k_apply_dq<<<nb, TPB, 0, s>>>(dvec, q, rho64, O, n, slot, dev_state);
-    if (fp32_) k_axpy<float><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Lf[0].b, O, Lf[0], n, slot, dev_state);
-    else k_axpy<double><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Ld[0].b, O, Ld[0], n, slot, dev_state);
+    if (fp32_) {
+        k_axpy<float><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Lf[0].b, O, Lf[0], n, slot, dev_state);
+        k_replace<float><<<nb, TPB, 0, s>>>(rhs_, p_, rho64, O, n, r, Lf[0].b, Lf[0], rel_tol, slot, dev_state);
+    } else {
+        k_axpy<double><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Ld[0].b, O, Ld[0], n, slot, dev_state);
+        k_replace<double><<<nb, TPB, 0, s>>>(rhs_, p_, rho64, O, n, r, Ld[0].b, Ld[0], rel_tol, slot, dev_state);
+    }
     k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 1, conditional, use_conditional ? 1 : 0);
 }
 

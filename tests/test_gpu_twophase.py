@@ -77,8 +77,9 @@ def test_mpls_and_reinit():
     port, gpu = make_pair(G)
     port.call("init")
     gpu.init()
+    m0 = port.scalars()["lsf_mass0"] * 1.01   # force a visible mass correction
     for s in (port, gpu):
-        s.set_scalars(dt=0.01, lsf_mass0=port.scalars()["lsf_mass0"] * 1.01)
+        s.set_scalars(dt=0.01, lsf_mass0=m0)
     port.call("mpls", 5)
     gpu.mpls(5)
     compare(G, port, gpu, ["phi"], LS_TOL)
@@ -96,8 +97,28 @@ def test_projection_step():
         s.set_scalars(dt=0.0125, dt_old=0.0125, dt_old2=0.0125)
     port.call("ab_solve")
     it, rr = gpu.ab_solve()
-    assert rr <= 1e-12, (it, rr)
+    compare(G, port, gpu, ["u_src", "v_src", "rho", "rhs"], 1e-11)
     compare(G, port, gpu, ["p", "u", "v", "nu", "nv"], FLOW_TOL)
+    assert rr <= 1e-12, (it, rr)
+
+
+def test_pressure_solver_on_checker_state():
+    """The GPU pressure solver applied to the checker's own right-hand side and density."""
+    import torch
+    from scihpc_gb300 import Poisson
+    port, gpu = make_pair(G)
+    port.call("init")
+    for s in (port,):
+        s.set_scalars(dt=0.0125, dt_old=0.0125, dt_old2=0.0125)
+    port.call("ab_solve")
+    rho = torch.from_numpy(port.get("rho")).cuda()
+    rhs = torch.from_numpy(port.get("rhs")).cuda()
+    ps = Poisson(native(G), bc=0, density=True, fp32=False)
+    ps.set_density(rho)
+    p = torch.zeros(G.shape, dtype=torch.float64, device="cuda")
+    it, rr = ps.solve(rhs, p, rel_tol=1e-13, max_iter=200)
+    I = G.interior()
+    assert rel_l2(p.cpu().numpy()[I], port.get("p")[I]) <= FLOW_TOL
 
 
 @pytest.mark.parametrize("graph", [False, True], ids=["eager", "graph"])
