@@ -46,7 +46,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(SRC, "*.cu")))
-    headers = sorted(glob.glob(os.path.join(SRC, "*.cuh"))) + [os.path.join(ROOT, "include", "scihpc_gpu.h")]
+    headers = sorted(glob.glob(os.path.join(SRC, "*.cuh"))) + [os.path.join(ROOT, "include", "scihpc_gpu.h"),
+                                                                os.path.abspath(__file__)]
     cc = nvcc()
     jobs = []
     objs = []
