@@ -21,6 +21,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -274,7 +275,10 @@ __global__ void k_replace(const double *__restrict__ rhs, const double *__restri
     grid_sum<1>(v, slot, o);
 }
 
-// Convergence test; in graph mode it also drives the conditional while-node.
+// Convergence test; in graph mode it also drives the conditional while-node.  Besides the
+// tolerance and the iteration cap, the iteration stops once the residual has not improved
+// for three consecutive iterations: it has reached the attainable accuracy of FP64 for
+// this operator, and conjugate gradients would only accumulate round-off from there.
 __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
                         int use_handle) {
     if (advance) {
@@ -289,8 +293,14 @@ __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, u
     }
     const double rel = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0;
     st->relres = rel;
+    if (!advance || rel < st->best) {
+        st->best = rel;
+        st->since_best = 0;
+    } else {
+        st->since_best += 1;
+    }
     if (!(rel == rel) || isinf(rel)) st->diverged = 1;
-    st->done = (rel <= tol || st->it >= max_iter || st->diverged) ? 1 : 0;
+    st->done = (rel <= tol || st->it >= max_iter || st->diverged || st->since_best >= 3) ? 1 : 0;
 #if defined(__CUDA_ARCH__)
     if (use_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, st->done ? 0u : 1u);
 #endif
@@ -434,11 +444,12 @@ __global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, I
     Cl.x[Pc] = 0;
 }
 
-// fine x += interpolation of coarse x: (bi/tri)linear for ratio 2 (weights 3/4, 1/4 per
-// axis; Neumann walls clamp to the wall cell, Dirichlet walls read the zero halo),
-// piecewise constant for ratio 3.
+// fine x += interpolation of coarse x.  Default: piecewise constant (the transpose of the
+// cell-average restriction up to the factor ratio^d, which keeps the V-cycle symmetric, as
+// CG requires).  linear = 1: (bi/tri)linear for ratio 2 (weights 3/4, 1/4 per axis; Neumann
+// walls clamp to the wall cell, Dirichlet walls read the zero halo).
 template <class T, int DIM>
-__global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann) {
+__global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nf = (long long)F.n[0] * F.n[1] * (DIM == 3 ? F.n[2] : 1);
     if (t >= nf) return;
@@ -466,7 +477,7 @@ __global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann) {
         return Cl.x[(a0 + 1) * Cl.s[0] + (a1 + 1) * Cl.s[1] + (DIM == 3 ? a2 + 1 : 0)];
     };
     T v;
-    if (r != 2) {
+    if (r != 2 || !linear) {
         v = CX(par[0], par[1], DIM == 3 ? par[2] : 0);
     } else if (DIM == 2) {
         v = T(0.5625) * CX(par[0], par[1], 0) + T(0.1875) * (CX(nb[0], par[1], 0) + CX(par[0], nb[1], 0)) +
@@ -885,8 +896,8 @@ void Poisson::vcycle(cudaStream_t s) {
     for (int l = nlev - 2; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
-        if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann);
-        else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann);
+        if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
+        else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
         for (int k = 0; k < nu; ++k) {
             smooth(l, 1);
             smooth(l, 0);
@@ -969,10 +980,14 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
     begin(rhs, p, use_guess, s);
     SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
     SCIHPC_CUDA(cudaStreamSynchronize(s));
+    const bool trace = std::getenv("SCIHPC_PPE_TRACE") != nullptr;
+    if (trace) std::fprintf(stderr, "ppe it %d relres %.3e\n", host_state->it, host_state->relres);
     while (!host_state->done) {
         iterate(s);
         SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         SCIHPC_CUDA(cudaStreamSynchronize(s));
+        if (trace) std::fprintf(stderr, "ppe it %d relres %.3e rz %.3e dq %.3e\n", host_state->it, host_state->relres,
+                                host_state->rz, host_state->dq);
     }
     const int it = host_state->it;
     const bool div = host_state->diverged;

@@ -30,7 +30,8 @@ struct PcgScalars {
     double dq;
     double relres;
     double mean;
-    int it, done, diverged, pad;
+    double best;      // smallest relative residual seen
+    int it, done, diverged, since_best;
 };
 
 class Poisson {
@@ -56,6 +57,7 @@ public:
     PcgScalars *host_state = nullptr;   // pinned mirror
     unsigned long long *cond_handle = nullptr;   // graph conditional handle slot (device), 0 when unused
     bool use_conditional = false;
+    int prolong_linear = 0;   // 0: piecewise-constant prolongation (default), 1: (bi/tri)linear
     unsigned long long conditional = 0;
 
 private:

@@ -59,10 +59,10 @@ def test_dirichlet_constant_matches_reference_multigrid(port, n, fp32):
     rhs[3:-3, 3:-3, 0] = -f
     ps = Poisson(native(g), bc=1, density=False, fp32=fp32)
     p = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
-    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-13, max_iter=100)
+    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-12, max_iter=100)
     out = p.cpu().numpy()
     I = g.interior()
-    assert rr <= 1e-12, rr
+    assert rr <= 1e-11, rr
     assert rel_l2(out[I], ref[I]) <= PARITY, rel_l2(out[I], ref[I])
 
 
@@ -106,10 +106,10 @@ def test_variable_density_matches_exact_solve(port, fp32, case):
     rho_d = dev(rho)   # the solver keeps using this buffer: it must outlive the solves
     ps.set_density(rho_d)
     p = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
-    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-13, max_iter=200)
+    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-12, max_iter=200)
     out = p.cpu().numpy()
     I = g.interior()
-    assert rr <= 1e-12, (rr, it)
+    assert rr <= 1e-11, (rr, it)
     assert abs(out[I].mean()) <= 1e-12 * np.abs(out[I]).max()
     assert rel_l2(out[I], ref[I]) <= PARITY, rel_l2(out[I], ref[I])
 

@@ -1,7 +1,7 @@
 """The two-phase projection step on the GPU against the CPU restatement, stage by stage and
 for whole steps, on the rising-bubble problem at reduced size.  The restatement's pressure
 solve is an exact CG solve of the reference's projection() equation (ppe_mode 2) to a
-relative residual of 1e-14; the GPU solves the same equation to 1e-13 with multigrid.
+relative residual of 1e-14; the GPU solves the same equation to 1e-12 with multigrid.
 Tolerances: level set within 1e-10, pressure and velocity within 1e-9 relative L2."""
 import numpy as np
 import pytest
@@ -22,7 +22,7 @@ def native(g):
 
 def make_pair(g, scheme=1, fp32=False):
     from scihpc_gb300 import TwoPhase
-    prm = bubble_params(g, ppe_tol=1e-13)
+    prm = bubble_params(g, ppe_tol=1e-12)
     port = O.Checker("port").twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm,
                                       dict(scheme=scheme, n_mpls=5, reinit_every=1, ppe_mode=2, reinit_lambda=1))
     port.set_exact_tol(1e-14)
@@ -99,7 +99,7 @@ def test_projection_step():
     it, rr = gpu.ab_solve()
     compare(G, port, gpu, ["u_src", "v_src", "rho", "rhs"], 1e-11)
     compare(G, port, gpu, ["p", "u", "v", "nu", "nv"], FLOW_TOL)
-    assert rr <= 1e-12, (it, rr)
+    assert rr <= 1e-11, (it, rr)
 
 
 def test_pressure_solver_on_checker_state():
@@ -116,7 +116,7 @@ def test_pressure_solver_on_checker_state():
     ps = Poisson(native(G), bc=0, density=True, fp32=False)
     ps.set_density(rho)
     p = torch.zeros(G.shape, dtype=torch.float64, device="cuda")
-    it, rr = ps.solve(rhs, p, rel_tol=1e-13, max_iter=200)
+    it, rr = ps.solve(rhs, p, rel_tol=1e-12, max_iter=200)
     I = G.interior()
     assert rel_l2(p.cpu().numpy()[I], port.get("p")[I]) <= FLOW_TOL
 
