@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark of the two-phase projection time step (rising bubble, 128 x 256) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-poisson]
+
+One JSON line on stdout (rank 0).  Our arm: the CUDA library through its C ABI, one step =
+one complete time step replayed as a captured CUDA graph (find_dt, WENO5/TVD-RK3 advection,
+5 mass-correction Euler steps, ab_solve with the multigrid pressure solve iterated to a
+relative residual of 1e-10 inside the graph, Godunov reinitialisation).  The reference
+arm (--impl reference) times the reference algorithm's CPU implementation (the CPU
+restatement in oracle/, built from committed sources) on all host cores, on the same
+workload.  With N > 1 (torchrun) every rank runs an independent replica: the step does
+not shard (one 128 x 256 grid), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY = 128, 256
+DOMAIN = ((0.0, 0.0), (1.0, 2.0))
+BUBBLE = ((0.5, 0.5), 0.25)
+PPE_TOL = 1e-10
+
+
+def physics(h: float) -> dict:
+    """Hysing TC1 (rho 1000/100, mu 10/1, sigma 24.5, g 0.98, L = 1), nondimensionalised as
+    set_parameters does (global.cpp:31-52); ls_width 1.5h, rdt 0.25h; dt from the reference's
+    stability estimate (find_dt) capped at CFL 0.2."""
+    import math
+    r1, r2, m1, m2, sig, g = 1000.0, 100.0, 10.0, 1.0, 24.5, 0.98
+    Uc = math.sqrt(g * 1.0)
+    return dict(density_ratio=r2 / r1, viscosity_ratio=m2 / m1, Re=r1 * Uc * 1.0 / m1, Fr=Uc / math.sqrt(g * 1.0),
+                We=r1 * Uc * Uc * 1.0 / sig, ls_width=1.5 * h, rdt=0.25 * h, max_CFL=0.2, min_CFL=1e-4,
+                positive_ref=0.0, ppe_tol=PPE_TOL, ppe_tol2=0.0, ppe_max_iter=200, ppe_omega=1.5, ppe_initer=1,
+                dt0=1.0)
+
+
+def initial_phi(shape):
+    import numpy as np
+    dx, dy = (DOMAIN[1][0] - DOMAIN[0][0]) / NX, (DOMAIN[1][1] - DOMAIN[0][1]) / NY
+    xc = DOMAIN[0][0] + (np.arange(NX) + 0.5) * dx
+    yc = DOMAIN[0][1] + (np.arange(NY) + 0.5) * dy
+    X, Y = np.meshgrid(xc, yc, indexing="ij")
+    phi = np.zeros(shape)
+    (cx, cy), r = BUBBLE
+    phi[3:-3, 3:-3, 0] = r - np.sqrt((X - cx) ** 2 + (Y - cy) ** 2)
+    return phi
+
+
+def config_block(extra=None) -> dict:
+    c = {"workload": "2D rising bubble, one two-phase projection time step",
+         "grid": f"{NX}x{NY} cells on [0,1]x[0,2], ghost width 3",
+         "physics": "Hysing TC1 (rho 1000/100, mu 10/1, sigma 24.5, g 0.98); the stated "
+                    "rho 1000/1, mu 10/0.1 case diverges within 20 steps in the reference scheme",
+         "step": "find_dt + WENO5/TVD-RK3 advection + 5 mpls Euler steps + ab_solve "
+                 f"(multigrid-PCG pressure to rel. residual {PPE_TOL:g}) + 12-stage-triple reinit",
+         "pressure_precision": "fp64 V-cycles",
+         "l2": "working set 24 MB < L2; L2 flushed (256 MiB write) before every timed step"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f".clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}", "--format=csv,noheader",
+                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            os.remove(self.path)
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1].split()[0]) for r in rows if len(r) >= 9 and r[1].strip().split()[0].replace(".", "").isdigit()]
+        mx = [float(r[2].split()[0]) for r in rows if len(r) >= 9 and r[2].strip().split()[0].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v: float, device) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def cpu_reference_rate(steps: int, warmup: int, budget_s: float, threads: int):
+    """The reference algorithm on the host cores: the restatement's stock ab_solve (SOR for
+    the first 5 steps, then fast pressure correction with the reference multigrid), WENO5
+    advection, as the reference drivers run it.  Returns (steps/s, steps timed)."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle as O
+    g = O.Grid(2, (NX, NY), DOMAIN[0], DOMAIN[1])
+    prm = physics(min((DOMAIN[1][0] - DOMAIN[0][0]) / NX, (DOMAIN[1][1] - DOMAIN[0][1]) / NY))
+    # the reference drivers' solver settings (benchmarks_2d_bubble_rising.cpp:78-79, global.h:49-53)
+    prm.update(ppe_tol=1e-8, ppe_tol2=1e-7, ppe_max_iter=100, ppe_initer=1)
+    s = O.Checker("port").twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm,
+                                   dict(scheme=1, n_mpls=5, reinit_every=1, ppe_mode=0, reinit_lambda=1))
+    s.set("phi", initial_phi(g.shape))
+    s.call("init")
+    for _ in range(warmup):
+        s.call("step", 1)
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps:
+        s.call("step", 1)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return n / dt, n
+
+
+def run_reference(args) -> None:
+    ws, rank, local = dist_init()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rate, n = cpu_reference_rate(args.steps, min(args.warmup, 3), budget_s=120.0, threads=threads)
+    line = {"metric": "time steps/s", "value": rate, "unit": "steps/s", "n_gpus": args.gpus, "steps": n,
+            "warmup": min(args.warmup, 3), "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic bubble)",
+            "config": config_block({"parallelism": "host OpenMP", "pressure_solver": "reference schedule: SOR "
+                                    "for 5 steps, then fast pressure correction on the reference multigrid"}),
+            "impl": "reference",
+            "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{n} time steps after warm-up (bounded to 120 s)"},
+            "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU leg
+def vcycle_bytes(levels, ndim: int, w: int) -> float:
+    """Algorithmic bytes of one V(2,2) cycle, summed over levels: per cell of level l, 4 full
+    red-black sweeps reading x, b and the coefficients (level 0: the density; coarser: ndim
+    face arrays) and writing x; the fused residual-restriction reads x, b, coefficients and
+    writes the coarse b and x; the prolongation reads the coarse x and updates x; level 0's
+    x is cleared once."""
+    tot = 0.0
+    for l, n in enumerate(levels):
+        cells = 1
+        for a in range(ndim):
+            cells *= n[a]
+        coef = 1 if l == 0 else ndim
+        sweeps = 4 * (3 + coef) if l < len(levels) - 1 else 0
+        restrict = (2 + coef) if l < len(levels) - 1 else 0
+        coarse_w = 2.0 / (2 ** ndim) if l < len(levels) - 1 else 0.0
+        prolong = (2.0 + 1.0 / (2 ** ndim)) if l < len(levels) - 1 else 0.0
+        clear = 1 if l == 0 else 0
+        last = 2 if l == len(levels) - 1 else 0   # dense solve: read b, write x
+        tot += cells * w * (sweeps + restrict + coarse_w + prolong + clear + last)
+    return tot
+
+
+def poisson_block(torch, Poisson, Grid, hbm):
+    """256^3 variable-density pressure equation (density 1 + 999 H(phi), phi from 12 seeded
+    spheres, Neumann walls, zero-mean right-hand side from a random divergent velocity),
+    solved to relative residual 1e-10 with FP64 V-cycles and with FP32 V-cycles inside the
+    FP64 refinement."""
+    n = 256
+    g = Grid(3, (n, n, n), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    dev = torch.device("cuda")
+    gen = torch.Generator(device="cpu").manual_seed(20261203)
+    h = 1.0 / n
+    c = (torch.arange(n, dtype=torch.float64, device=dev) + 0.5) * h
+    X, Y, Z = torch.meshgrid(c, c, c, indexing="ij")
+    phi = torch.full((n, n, n), -1e9, dtype=torch.float64, device=dev)
+    for _ in range(12):
+        r = 0.05 + 0.15 * torch.rand(1, generator=gen).item()
+        cen = [r + (1 - 2 * r) * torch.rand(1, generator=gen).item() for _ in range(3)]
+        phi = torch.maximum(phi, r - torch.sqrt((X - cen[0]) ** 2 + (Y - cen[1]) ** 2 + (Z - cen[2]) ** 2))
+    del X, Y, Z
+    w = 1.5 * h
+    H = torch.where(phi < -w, torch.zeros_like(phi), torch.where(phi > w, torch.ones_like(phi),
+                    0.5 * (1 + phi / w + torch.sin(torch.pi * phi / w) / torch.pi)))
+    rho = torch.ones(g.shape, dtype=torch.float64, device=dev)
+    rho[3:-3, 3:-3, 3:-3] = 1.0 + 999.0 * H
+    # ghost density: copy the boundary cells (any finite value works: wall faces carry no flux)
+    rho[:3], rho[-3:] = rho[3:4].clone(), rho[-4:-3].clone()
+    rho[:, :3], rho[:, -3:] = rho[:, 3:4].clone(), rho[:, -4:-3].clone()
+    rho[:, :, :3], rho[:, :, -3:] = rho[:, :, 3:4].clone(), rho[:, :, -4:-3].clone()
+    del H, phi
+    # rhs = div u of a random face velocity with zero normal velocity on the walls
+    u = torch.rand((n + 1, n, n), generator=gen, dtype=torch.float64).to(dev) - 0.5
+    u[0], u[-1] = 0, 0
+    div = (u[1:] - u[:-1]) / h
+    del u
+    v = torch.rand((n, n + 1, n), generator=gen, dtype=torch.float64).to(dev) - 0.5
+    v[:, 0], v[:, -1] = 0, 0
+    div += (v[:, 1:] - v[:, :-1]) / h
+    del v
+    wv = torch.rand((n, n, n + 1), generator=gen, dtype=torch.float64).to(dev) - 0.5
+    wv[:, :, 0], wv[:, :, -1] = 0, 0
+    div += (wv[:, :, 1:] - wv[:, :, :-1]) / h
+    del wv
+    rhs = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+    rhs[3:-3, 3:-3, 3:-3] = div - div.mean()
+    del div
+    out = {"grid": "256^3", "density": "1 + 999 H(phi), 12 seeded spheres r in [0.05, 0.2]",
+           "rel_tol": 1e-10}
+    for name, fp32 in (("fp64", False), ("fp32_refined", True)):
+        ps = Poisson(g, bc=0, density=True, fp32=fp32)
+        ps.set_density(rho)
+        p = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+        ps.solve(rhs, p, rel_tol=1e-10, max_iter=100)   # warm
+        times, its = [], []
+        for _ in range(3):
+            p.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            it, rr = ps.solve(rhs, p, rel_tol=1e-10, max_iter=100)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            its.append(it)
+        ncyc = 20
+        ms = ps.time_vcycles(rhs, p, ncyc) / ncyc
+        by = vcycle_bytes(ps.levels(), 3, 4 if fp32 else 8)
+        out[name] = {"ms_to_tol": min(times), "iterations": its[0], "final_relres": rr,
+                     "vcycle_ms": ms, "vcycle_alg_bytes": by, "vcycle_gbs": by / ms / 1e6,
+                     "vcycle_frac_of_hbm": by / ms / 1e6 / hbm["hbm_gbs"]}
+        ps.close()
+        del p
+    out["fp32_speedup"] = out["fp64"]["ms_to_tol"] / out["fp32_refined"]["ms_to_tol"]
+    return out
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    from scihpc_gb300 import Grid, Poisson, TwoPhase, lib
+    lib()   # raises if the CUDA library is missing: there is no CPU path
+    g = Grid(2, (NX, NY), DOMAIN[0], DOMAIN[1])
+    h = min(g.spacing())
+    tp = TwoPhase(g, ["no_slip"] * 6, ["neumann"] * 6, physics(h), scheme=1, n_mpls=5, reinit_every=1, fp32=False)
+    phi0 = initial_phi(g.shape)
+    tp.set("phi", phi0)
+    tp.init()
+    stream = torch.cuda.ExternalStream(tp.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    tp.step(args.warmup, graph=True, sync=True)
+    it0 = tp.graph_stats()["ppe_iters_total"]
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with clocks:
+        t_wall = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.current_stream().synchronize()
+            ev[k][0].record(stream)
+            tp.step(1, graph=True, sync=False)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier(ws)
+    torch.cuda.synchronize()
+    ms_local = sum(a.elapsed_time(b) for a, b in ev)
+    ms_total = max_over_ranks(ws, ms_local, torch.device("cuda"))
+    value = ws * args.steps / (ms_total / 1e3)
+    gs = tp.graph_stats()
+    ppe_iters = gs["ppe_iters_total"] - it0
+    launches = args.steps * (gs["pre"] + gs["post"]) + gs["body"] * ppe_iters
+    diag = tp.diagnostics()
+    if args.lite:
+        if rank == 0:
+            print(json.dumps({"metric": "time steps/s", "value": value, "lite": True, "gpu_launches": launches,
+                              "ppe_iters_per_step": ppe_iters / args.steps, "graph": gs}), flush=True)
+        return
+
+    # end to end through the public API with host buffers: per step, upload the state
+    # (phi, u, v, p) from pinned host memory, one step, download it again
+    names = ["phi", "u", "v", "p"]
+    hb = {nm: torch.empty(g.shape, dtype=torch.float64).pin_memory() for nm in names}
+    for nm in names:
+        tp.download_ptr(nm, hb[nm].data_ptr())
+    nbytes = len(names) * g.size * 8
+    e2e_steps = max(1, min(args.steps, 50))
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for nm in names:
+            tp.upload_ptr(nm, hb[nm].data_ptr())
+        tp.step(1, graph=True, sync=True)
+        for nm in names:
+            tp.download_ptr(nm, hb[nm].data_ptr())
+    e2e_s = max_over_ranks(ws, time.perf_counter() - t0, torch.device("cuda"))
+    e2e = {"value": ws * e2e_steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
+           "api": "scihpc_twophase_upload x4 + scihpc_twophase_step + scihpc_twophase_download x4"}
+
+    # roofline of the dominant kernel group: one V(2,2) pressure V-cycle on this grid
+    hbm = peaks()
+    ps = Poisson(g, bc=0, density=True, fp32=False)
+    ps.set_density(tp.device_ptr("rho"))
+    ptmp = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    ncyc = 200
+    vms = ps.time_vcycles(tp.device_ptr("rhs"), ptmp, ncyc) / ncyc
+    vb = vcycle_bytes(ps.levels(), 2, 8)
+    roof = {"bound": "hbm", "kernel": "pressure V(2,2) cycle, all levels (FP64)", "achieved": vb / vms / 1e6,
+            "peak": hbm["hbm_gbs"], "unit": "GB/s", "frac": vb / vms / 1e6 / hbm["hbm_gbs"],
+            "peak_src": hbm["src"], "traffic": None, "alg_bytes_per_launch": vb, "launch_ms": vms,
+            "note": "128x256 FP64 working set is L2-resident; achieved counts algorithmic bytes"}
+    ps.close()
+
+    line = {"metric": "time steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic bubble)",
+            "config": config_block({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches),
+            "ppe_iters_per_step": ppe_iters / args.steps, "wall_s": t_wall, "roofline": roof,
+            "diagnostics": diag}
+    if rank == 0 and not args.no_poisson:
+        line["poisson_256^3"] = poisson_block(torch, Poisson, Grid, hbm)
+    if rank == 0 and not args.no_cpu:
+        rate, n = cpu_reference_rate(20, 2, budget_s=20.0, threads=os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n} time steps of the same workload (reference algorithm, "
+                                          "restatement in oracle/port, all host cores)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-poisson", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--lite", action="store_true", help="timed steps only (for kernel launch lists)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

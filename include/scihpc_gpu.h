@@ -121,16 +121,18 @@ int scihpc_lsf_integrals(scihpc_ctx *ctx, const double prm[4], const double *phi
  * which keeps the wall term with a zero ghost-centre value (multigrid_base.cpp:293-345).
  * precision = 0: V-cycles in FP64; 1: V-cycles in FP32 inside the FP64 outer iteration
  * (the residual, the correction sum and the solution stay FP64).
- * Red-black Gauss-Seidel V(2,2) cycles, cell-average restriction, (bi/tri)linear
- * prolongation, FP64 dense direct solve on the coarsest level (levels coarsened by the
- * rule of multigrid.cpp:8-41), used as the preconditioner of an FP64 conjugate-gradient
- * outer iteration.  Replaces the reference's SOR sweep loop and multigrid::v_cycle /
+ * Red-black Gauss-Seidel V(2,2) cycles, cell-average restriction, piecewise-constant
+ * prolongation (its transpose, so the cycle is symmetric), FP64 dense direct solve on the
+ * coarsest level (levels coarsened by the rule of multigrid.cpp:8-41), used as the
+ * preconditioner of an FP64 flexible conjugate-gradient outer iteration that stops at the
+ * tolerance, the iteration cap, or when the residual stops improving.  Replaces the reference's SOR sweep loop and multigrid::v_cycle /
  * full_cycle (multigrid.cpp:43-79).  Allocates device memory at creation. */
 typedef struct scihpc_poisson scihpc_poisson;
 int scihpc_poisson_create(const scihpc_grid *grid, int bc, int density_mode, int precision, scihpc_poisson **out);
 int scihpc_poisson_destroy(scihpc_poisson *ps);
 /* Coefficients from a ghosted density field (dummy_data::density); call again whenever it
- * changes (init_ppe_proj_coefficients, projection_method.cpp:404-465). */
+ * changes (init_ppe_proj_coefficients, projection_method.cpp:404-465).  The solver keeps
+ * reading `rho` in every solve: it must stay valid until the next set_density. */
 int scihpc_poisson_set_density(scihpc_poisson *ps, const double *rho, void *stream);
 /* Solve to ||rhs - A p|| <= rel_tol ||rhs|| (2-norms over interior cells) or max_iter
  * outer iterations.  rhs and p are ghosted fields; p holds the initial guess (use_guess = 1)
@@ -138,6 +140,10 @@ int scihpc_poisson_set_density(scihpc_poisson *ps, const double *rho, void *stre
  * iterations and the final relative residual on the host (synchronises `stream`). */
 int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int use_guess, double rel_tol,
                          int max_iter, int *iters, double *relres, void *stream);
+/* Times `ncycles` V-cycles (the preconditioner alone, on the residual of p = 0 for rhs)
+ * with CUDA events on `stream`; *ms receives the total.  p is overwritten with zeros.
+ * Synchronises `stream`.  Measurement hook with no reference counterpart. */
+int scihpc_poisson_time_vcycles(scihpc_poisson *ps, const double *rhs, double *p, int ncycles, float *ms, void *stream);
 /* Level sizes of the hierarchy (3 ints per level); returns the level count. */
 int scihpc_poisson_levels(scihpc_poisson *ps, int *level_n, int max_levels);
 
@@ -194,6 +200,10 @@ int scihpc_twophase_step(scihpc_twophase *tp, int nsteps, int use_graph, int syn
 int scihpc_twophase_diagnostics(scihpc_twophase *tp, double out[3]);
 /* The problem's CUDA stream (cudaStream_t as void*). */
 int scihpc_twophase_stream(scihpc_twophase *tp, void **stream);
+/* Kernel nodes of the captured step graph {before the pressure loop, per pressure
+ * iteration, after it} and the pressure iterations summed over all steps so far
+ * (out[3]).  Measurement hook with no reference counterpart. */
+int scihpc_twophase_graph_stats(scihpc_twophase *tp, long long out[4]);
 /* Statistics of the last pressure solve: {iterations, relative residual, ms}. */
 int scihpc_twophase_ppe_stats(scihpc_twophase *tp, double out[3]);
 

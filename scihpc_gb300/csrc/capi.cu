@@ -277,6 +277,12 @@ int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int u
     return ps->ps.solve(rhs, p, use_guess, rel_tol, max_iter, iters, relres, S(stream));
 }
 
+int scihpc_poisson_time_vcycles(scihpc_poisson *ps, const double *rhs, double *p, int ncycles, float *ms,
+                                void *stream) {
+    REQUIRE(ps && rhs && p && ms && ncycles > 0, "poisson_time_vcycles: bad argument");
+    return ps->ps.time_vcycles(rhs, p, ncycles, ms, S(stream));
+}
+
 int scihpc_poisson_levels(scihpc_poisson *ps, int *level_n, int max_levels) {
     if (!ps || !level_n) return -SCIHPC_ERR_ARG;
     return ps->ps.levels(level_n, max_levels);
@@ -421,6 +427,11 @@ int scihpc_twophase_stream(scihpc_twophase *tp, void **stream) {
     REQUIRE(tp && stream, "twophase_stream: NULL argument");
     *stream = tp->tp.stream;
     return SCIHPC_OK;
+}
+
+int scihpc_twophase_graph_stats(scihpc_twophase *tp, long long out[4]) {
+    REQUIRE(tp && out, "twophase_graph_stats: NULL argument");
+    return tp->tp.graph_stats(out);
 }
 
 int scihpc_twophase_ppe_stats(scihpc_twophase *tp, double out[3]) {

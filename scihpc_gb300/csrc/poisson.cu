@@ -1005,6 +1005,28 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
     return SCIHPC_OK;
 }
 
+int Poisson::time_vcycles(const double *rhs, double *p, int n, float *ms, cudaStream_t s) {
+    use_conditional = false;
+    begin(rhs, p, 0, s);
+    cudaEvent_t e0, e1;
+    SCIHPC_CUDA(cudaEventCreate(&e0));
+    SCIHPC_CUDA(cudaEventCreate(&e1));
+    if (fp32_) vcycle<float>(s);   // warm
+    else vcycle<double>(s);
+    SCIHPC_CUDA(cudaEventRecord(e0, s));
+    for (int k = 0; k < n; ++k) {
+        if (fp32_) vcycle<float>(s);
+        else vcycle<double>(s);
+    }
+    SCIHPC_CUDA(cudaEventRecord(e1, s));
+    SCIHPC_CUDA(cudaEventSynchronize(e1));
+    SCIHPC_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
 int Poisson::levels(int *out, int max_levels) const {
     for (int l = 0; l < nlev && l < max_levels; ++l) {
         const int *n = fp32_ ? Lf[l].n : Ld[l].n;

@@ -50,6 +50,9 @@ public:
     int solve(const double *rhs, double *p, int use_guess, double rel_tol, int max_iter, int *iters, double *relres,
               cudaStream_t s);
     int levels(int *out, int max_levels) const;
+    // Times n V-cycles (the preconditioner alone) on the residual of p = 0 for rhs.
+    int time_vcycles(const double *rhs, double *p, int n, float *ms, cudaStream_t s);
+    int fp32() const { return fp32_; }
 
     double rel_tol = 1e-10;
     int max_iter = 200;

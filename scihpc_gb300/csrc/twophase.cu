@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "levelset.cuh"
 #include "lsm_device.cuh"
@@ -844,6 +845,26 @@ __global__ void k_advance_time(StepScalars *sc) {
     sc->t += sc->dt;
     sc->iter += 1.0;
 }
+// running total of pressure iterations (StepScalars::red[15])
+__global__ void k_count_ppe(StepScalars *sc, const PcgScalars *ps) { sc->red[15] += double(ps->it); }
+
+long long count_kernels(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(g, nodes.data(), &n);
+    long long k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nd, &t);
+        if (t == cudaGraphNodeTypeKernel) ++k;
+        else if (t == cudaGraphNodeTypeGraph) {
+            cudaGraph_t child;
+            if (cudaGraphChildGraphNodeGetGraph(nd, &child) == cudaSuccess) k += count_kernels(child);
+        }
+    }
+    return k;
+}
 }  // namespace
 
 int TwoPhaseGpu::capture_step() {
@@ -879,13 +900,17 @@ int TwoPhaseGpu::capture_step() {
     ppe.iterate(stream);
     SCIHPC_CUDA(cudaStreamEndCapture(stream, &body));
 
+    nodes_body = count_kernels(body);
     SCIHPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    k_count_ppe<<<1, 1, 0, stream>>>(sc, ppe.dev_state);
     ab_solve_post();
     // step counter handled on the host: reinit runs every `reinit_every` steps; the graph
     // is captured for the common case reinit_every == 1 (otherwise the host calls reinit)
     if (reinit_every == 1) reinit();
     SCIHPC_CUDA(cudaStreamEndCapture(stream, &post_g));
     SCIHPC_CUDA(cudaGraphAddChildGraphNode(&post_node, g, &cond_node, 1, post_g));
+    nodes_pre = count_kernels(pre_g);
+    nodes_post = count_kernels(post_g);
     SCIHPC_CUDA(cudaGraphInstantiate(&graph_exec, g, 0));
     graph = g;
     cudaGraphDestroy(pre_g);
@@ -913,11 +938,22 @@ int TwoPhaseGpu::step(int nsteps, bool use_graph) {
             double rr;
             int rc = ab_solve(&it, &rr);
             if (rc) return rc;
+            k_count_ppe<<<1, 1, 0, stream>>>(sc, ppe.dev_state);
             ++step_count;
             if (reinit_every > 0 && step_count % reinit_every == 0) reinit();
         }
     }
     SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::graph_stats(long long *out) {
+    SCIHPC_CUDA(cudaMemcpyAsync(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    out[0] = nodes_pre;
+    out[1] = nodes_body;
+    out[2] = nodes_post;
+    out[3] = (long long)sc_host->red[15];
     return SCIHPC_OK;
 }
 

@@ -45,6 +45,7 @@ public:
     int init();
     int step(int nsteps, bool graph);
     int diagnostics(double *out);
+    int graph_stats(long long *out);   // kernel nodes {pre, body, post}, PPE iterations summed over steps
 
     cudaStream_t stream = nullptr;
     Dims D{};
@@ -77,6 +78,7 @@ private:
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;
     int reinit_steps = 0;
+    long long nodes_pre = 0, nodes_body = 0, nodes_post = 0;
 };
 
 }  // namespace scihpc

@@ -91,6 +91,8 @@ _SIGS = {
     "scihpc_poisson_set_density": ([_vp, _vp, _vp], ctypes.c_int),
     "scihpc_poisson_solve": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _ip, _dp, _vp],
                              ctypes.c_int),
+    "scihpc_poisson_time_vcycles": ([_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float), _vp],
+                                    ctypes.c_int),
     "scihpc_poisson_levels": ([_vp, _ip, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_create": ([ctypes.POINTER(_GridC), _ip, _ip, _dp, _ip, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_destroy": ([_vp], ctypes.c_int),
@@ -110,6 +112,7 @@ _SIGS = {
     "scihpc_twophase_diagnostics": ([_vp, _dp], ctypes.c_int),
     "scihpc_twophase_stream": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_ppe_stats": ([_vp, _dp], ctypes.c_int),
+    "scihpc_twophase_graph_stats": ([_vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
 }
 
 
@@ -242,6 +245,11 @@ class Poisson:
             self.L.check(rc)
         return it.value, rr.value
 
+    def time_vcycles(self, rhs, p, ncycles, stream=0) -> float:
+        ms = ctypes.c_float(0.0)
+        self.L.check(self.L.scihpc_poisson_time_vcycles(self.h, _ptr(rhs), _ptr(p), ncycles, ctypes.byref(ms), stream))
+        return ms.value
+
     def levels(self) -> list:
         buf = (ctypes.c_int * 96)()
         n = self.L.scihpc_poisson_levels(self.h, buf, 32)
@@ -344,6 +352,17 @@ class TwoPhase:
         p = _vp()
         self.L.check(self.L.scihpc_twophase_stream(self.h, ctypes.byref(p)))
         return p.value or 0
+
+    def graph_stats(self) -> dict:
+        out = (ctypes.c_longlong * 4)()
+        self.L.check(self.L.scihpc_twophase_graph_stats(self.h, out))
+        return dict(pre=out[0], body=out[1], post=out[2], ppe_iters_total=out[3])
+
+    def upload_ptr(self, name: str, host_ptr: int) -> None:
+        self.L.check(self.L.scihpc_twophase_upload(self.h, name.encode(), ctypes.cast(host_ptr, _dp)))
+
+    def download_ptr(self, name: str, host_ptr: int) -> None:
+        self.L.check(self.L.scihpc_twophase_download(self.h, name.encode(), ctypes.cast(host_ptr, _dp)))
 
     def ppe_stats(self) -> dict:
         out = (ctypes.c_double * 3)()

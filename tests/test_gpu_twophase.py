@@ -2,7 +2,13 @@
 for whole steps, on the rising-bubble problem at reduced size.  The restatement's pressure
 solve is an exact CG solve of the reference's projection() equation (ppe_mode 2) to a
 relative residual of 1e-14; the GPU solves the same equation to 1e-12 with multigrid.
-Tolerances: level set within 1e-10, pressure and velocity within 1e-9 relative L2."""
+Tolerances: level set within 1e-10, pressure and velocity within 1e-9 relative L2.
+
+The bubble is placed off the domain's symmetry line.  With a mirror-symmetric bubble the
+face velocities on the symmetry line are zero up to round-off, and the WENO upwind choice
+there (sign of u_i + u_i+1, weno_solver.cpp:192) is decided by that round-off: two correct
+implementations -- or the restatement against itself with a 1e-14 perturbation -- then
+differ by 1e-7 in p and 1e-5 in u after the second step."""
 import numpy as np
 import pytest
 
@@ -28,7 +34,7 @@ def make_pair(g, scheme=1, fp32=False):
     port.set_exact_tol(1e-14)
     gpu = TwoPhase(native(g), ["no_slip"] * 6, ["neumann"] * 6, prm, scheme=scheme, n_mpls=5, reinit_every=1,
                    fp32=fp32)
-    phi = bubble_phi(g)
+    phi = bubble_phi(g, (0.43, 0.57), 0.23)
     port.set("phi", phi)
     gpu.set("phi", phi)
     return port, gpu
