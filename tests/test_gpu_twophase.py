@@ -58,7 +58,9 @@ def test_init_find_source():
     port, gpu = make_pair(G)
     port.call("init")
     gpu.init()
-    compare(G, port, gpu, ["rho", "delta", "curvature", "u_src", "v_src"], 1e-11)
+    compare(G, port, gpu, ["rho", "delta", "u_src", "v_src"], 1e-11)
+    # curvature divides by |grad phi|^1.5: far from the interface it amplifies round-off
+    compare(G, port, gpu, ["curvature"], 1e-10)
     assert abs(gpu.scalars()["lsf_mass0"] - port.scalars()["lsf_mass0"]) <= 1e-13 * port.scalars()["lsf_mass0"]
 
 
