@@ -85,6 +85,7 @@ _SIGS = {
     "scihpc_lsf_fields": ([_vp, _dp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_curvature": ([_vp, _vp, ctypes.POINTER(_vp), _vp, _vp], ctypes.c_int),
     "scihpc_lsf_integrals": ([_vp, _dp, _vp, _dp, _vp], ctypes.c_int),
+    "scihpc_lsf_integrals_noalloc": ([ctypes.POINTER(_GridC), _dp, _vp, _dp, _vp], ctypes.c_int),
     "scihpc_poisson_create": ([ctypes.POINTER(_GridC), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_poisson_destroy": ([_vp], ctypes.c_int),
@@ -213,6 +214,16 @@ class Workspace:
         out = (ctypes.c_double * 2)()
         self.L.check(self.L.scihpc_lsf_integrals(self.h, p, _ptr(phi), out, stream))
         return out[0], out[1]
+
+
+def lsf_integrals_noalloc(grid: Grid, prm, phi, stream=0):
+    """lsf_mass and lsf_volume without any device allocation (static scratch; see the header)."""
+    L = lib()
+    g = grid.c()
+    p = (ctypes.c_double * 4)(*prm)
+    out = (ctypes.c_double * 2)()
+    L.check(L.scihpc_lsf_integrals_noalloc(ctypes.byref(g), p, _ptr(phi), out, stream))
+    return out[0], out[1]
 
 
 class Poisson:
