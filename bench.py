@@ -308,7 +308,7 @@ def run_ours(args) -> None:
     tp.init()
     stream = torch.cuda.ExternalStream(tp.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    tp.step(args.warmup, graph=True, sync=True)
+    tp.step(args.warmup, graph=not args.eager, sync=True)
     it0 = tp.graph_stats()["ppe_iters_total"]
     torch.cuda.synchronize()
     barrier(ws)
@@ -321,7 +321,7 @@ def run_ours(args) -> None:
             flush.fill_(float(k))
             torch.cuda.current_stream().synchronize()
             ev[k][0].record(stream)
-            tp.step(1, graph=True, sync=False)
+            tp.step(1, graph=not args.eager, sync=False)
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
@@ -403,6 +403,7 @@ def main():
     ap.add_argument("--no-poisson", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--lite", action="store_true", help="timed steps only (for kernel launch lists)")
+    ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of graph replay")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

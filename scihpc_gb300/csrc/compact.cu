@@ -8,7 +8,8 @@
 // block.  One thread owns one line: a forward sweep builds the right-hand side on the fly
 // and eliminates, storing the partial results in the output arrays (and, for UCCD's second
 // system, a scratch pair), then the backward sweep finishes the line holding only the i+1
-// values in registers.
+// values in registers.  This sequential form serves lines longer than the warp-cooperative
+// solver of linescan.cu handles (more than 512 points).
 #include <cmath>
 #include <vector>
 
@@ -116,6 +117,23 @@ std::vector<double> pack(const HostLineOp &op) {
         const double den = op.P[1][i] * op.S[1][i] - op.R[1][i] * op.Q[1][i];
         r[8] = op.S[1][i] / den, r[9] = -op.Q[1][i] / den;
         r[10] = -op.R[1][i] / den, r[11] = op.P[1][i] / den;
+    }
+    return t;
+}
+
+// Scan form (linescan.cu): {L, K = -Dinv U, Dinv} per line position.
+std::vector<double> pack_scan(const HostLineOp &op) {
+    std::vector<double> t(size_t(op.n) * 12);
+    for (int i = 0; i < op.n; ++i) {
+        double *r = &t[size_t(i) * 12];
+        const double den = op.P[1][i] * op.S[1][i] - op.R[1][i] * op.Q[1][i];
+        const double a = op.S[1][i] / den, b = -op.Q[1][i] / den, c = -op.R[1][i] / den, d = op.P[1][i] / den;
+        r[0] = op.P[0][i], r[1] = op.Q[0][i], r[2] = op.R[0][i], r[3] = op.S[0][i];
+        r[4] = -(a * op.P[2][i] + b * op.R[2][i]);
+        r[5] = -(a * op.Q[2][i] + b * op.S[2][i]);
+        r[6] = -(c * op.P[2][i] + d * op.R[2][i]);
+        r[7] = -(c * op.Q[2][i] + d * op.S[2][i]);
+        r[8] = a, r[9] = b, r[10] = c, r[11] = d;
     }
     return t;
 }
@@ -307,13 +325,20 @@ int CompactOps::build(const Dims &D) {
         HostLineOp c = ccd_op(n, h), u, dn;
         uccd_ops(n, h, u, dn);
         std::vector<double> tc = pack(c), tu = pack(u), td = pack(dn);
+        std::vector<double> sc = pack_scan(c), su = pack_scan(u), sd = pack_scan(dn);
         const size_t bytes = tc.size() * sizeof(double);
-        SCIHPC_CUDA(cudaMalloc(&ccd[a], 3 * bytes));
+        SCIHPC_CUDA(cudaMalloc(&ccd[a], 6 * bytes));
         up[a] = ccd[a] + tc.size();
         down[a] = up[a] + tc.size();
+        scan_ccd[a] = down[a] + tc.size();
+        scan_up[a] = scan_ccd[a] + tc.size();
+        scan_down[a] = scan_up[a] + tc.size();
         SCIHPC_CUDA(cudaMemcpy(ccd[a], tc.data(), bytes, cudaMemcpyHostToDevice));
         SCIHPC_CUDA(cudaMemcpy(up[a], tu.data(), bytes, cudaMemcpyHostToDevice));
         SCIHPC_CUDA(cudaMemcpy(down[a], td.data(), bytes, cudaMemcpyHostToDevice));
+        SCIHPC_CUDA(cudaMemcpy(scan_ccd[a], sc.data(), bytes, cudaMemcpyHostToDevice));
+        SCIHPC_CUDA(cudaMemcpy(scan_up[a], su.data(), bytes, cudaMemcpyHostToDevice));
+        SCIHPC_CUDA(cudaMemcpy(scan_down[a], sd.data(), bytes, cudaMemcpyHostToDevice));
     }
     return SCIHPC_OK;
 }
@@ -322,6 +347,7 @@ void CompactOps::release() {
     for (int a = 0; a < 3; ++a) {
         if (ccd[a]) cudaFree(ccd[a]);
         ccd[a] = up[a] = down[a] = nullptr;
+        scan_ccd[a] = scan_up[a] = scan_down[a] = nullptr;
     }
 }
 
@@ -334,6 +360,7 @@ static void line_layout(const Dims &D, int a, int &fast, int &slow, long long &l
 
 void launch_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
                  double *f2, double *t1, double *t2, cudaStream_t s) {
+    if (scan_uccd(D, ops, a, flux, vel, f1, f2, s)) return;
     int fast, slow;
     long long lines;
     line_layout(D, a, fast, slow, lines);
@@ -343,6 +370,7 @@ void launch_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux
 
 void launch_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux, double *f1, double *f2,
                 cudaStream_t s) {
+    if (scan_ccd(D, ops, a, flux, f1, f2, s)) return;
     int fast, slow;
     long long lines;
     line_layout(D, a, fast, slow, lines);
@@ -352,6 +380,7 @@ void launch_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux,
 
 void launch_ccd_mixed(const Dims &D, const CompactOps &ops, int a, double *src, double *out, double *tmp,
                       cudaStream_t s) {
+    if (scan_mixed(D, ops, a, src, out, s)) return;
     int fast, slow;
     long long lines;
     line_layout(D, a, fast, slow, lines);

@@ -95,24 +95,26 @@ struct Outer {
     int nint[3];      // interior extents
     long long cs[3];  // compact strides (K fastest)
     double id2[3];
-    int density;      // 1: coefficients from rho64
+    int density;      // 1: coefficients oc[a * n + c] of the +a face of compact cell c
     int dirichlet;    // 1: wall term against a zero ghost-centre value
+    const double *oc;
+    long long n;
 };
 
-// (L v)_c for a compact vector v (or a ghosted field when `ghosted`).
+// (L v)_c for a compact vector v (or a ghosted field when `ghosted`).  Density mode reads the
+// precomputed face coefficients (no FP64 division in the iteration).
 template <bool GHOSTED>
 __device__ __forceinline__ double apply_L(const double *__restrict__ v, const double *__restrict__ rho, const Outer &O,
                                           int I, int J, int K) {
+    (void)rho;
     const int II[3] = {I, J, K};
     const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
     const long long co = I * O.cs[0] + J * O.cs[1] + K;
     const long long c = GHOSTED ? go : co;
     const double vc = v[c];
-    const double rc = O.density ? rho[go] : 1.0;
     double s = 0.0;
     for (int a = 0; a < O.D.ndim; ++a) {
         const long long st = GHOSTED ? O.D.s[a] : O.cs[a];
-        const long long gs = O.D.s[a];
         for (int side = -1; side <= 1; side += 2) {
             const bool wall = side < 0 ? II[a] == 0 : II[a] == O.nint[a] - 1;
             double C, vn;
@@ -121,18 +123,35 @@ __device__ __forceinline__ double apply_L(const double *__restrict__ v, const do
                 C = O.id2[a];
                 vn = 0.0;
             } else {
-                if (O.density) {
-                    const double R = 0.5 * (rc + rho[go + side * gs]);
-                    C = 1.0 / R * O.id2[a];   // 1.0 / R / d / d (projection_method.cpp:416-424)
-                } else {
-                    C = O.id2[a];
-                }
+                C = O.density ? O.oc[a * O.n + (side < 0 ? co - O.cs[a] : co)] : O.id2[a];
                 vn = v[c + side * st];
             }
             s += C * (vc - vn);
         }
     }
     return s;
+}
+
+// Face coefficients of the outer operator, exactly as init_ppe_proj_coefficients forms them
+// (projection_method.cpp:416-424): 1.0 / R / d / d with R the mean density of the two cells;
+// zero on the wall faces.
+__global__ void k_outer_coef(const double *__restrict__ rho, double *__restrict__ oc, Dims D, long long n) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int K = int(q % D.n[2]);
+    const long long r = q / D.n[2];
+    int J = int(r % D.n[1]);
+    int I = int(r / D.n[1]);
+    const int II[3] = {I, J, K};
+    const long long go = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+    for (int a = 0; a < 3; ++a) {
+        double C = 0.0;
+        if (a < D.ndim && II[a] < D.n[a] - 1) {
+            const double R = 0.5 * (rho[go] + rho[go + D.s[a]]);
+            C = 1.0 / R / D.d[a] / D.d[a];
+        }
+        oc[a * n + q] = C;
+    }
 }
 
 __device__ __forceinline__ void split_int(long long q, const Outer &O, int &I, int &J, int &K) {
@@ -395,13 +414,15 @@ __global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int 
     }
     T C[6];
     faces<T, MODE>(L, rho, id2.v, P, DIM, C);
-    T sc = C[0] + C[1] + C[2] + C[3];
     T sx = C[0] * L.x[P - L.s[0]] + C[1] * L.x[P + L.s[0]] + C[2] * L.x[P - L.s[1]] + C[3] * L.x[P + L.s[1]];
-    if (DIM == 3) {
-        sc += C[4] + C[5];
-        sx += C[4] * L.x[P - 1] + C[5] * L.x[P + 1];
+    if (DIM == 3) sx += C[4] * L.x[P - 1] + C[5] * L.x[P + 1];
+    if (MODE == 0) {
+        L.x[P] = (L.b[P] + sx) * L.idg[P];
+    } else {
+        T sc = C[0] + C[1] + C[2] + C[3];
+        if (DIM == 3) sc += C[4] + C[5];
+        L.x[P] = (L.b[P] + sx) / sc;
     }
-    L.x[P] = (L.b[P] + sx) / sc;
 }
 
 template <class T, int MODE, int DIM>
@@ -539,6 +560,50 @@ __global__ void k_coarse_coef(Level<T> F, Level<T> Cl, const T *__restrict__ rho
         }
     T *dst = axis == 0 ? Cl.cx : (axis == 1 ? Cl.cy : Cl.cz);
     dst[Pc] = sum / T(cnt) / T(r * r);
+}
+
+// Level-0 face coefficients from the padded density (+inf halo gives zero wall faces), for
+// the FP64 cycle: stored once per density update instead of divided out in every sweep.
+template <class T, int DIM>
+__global__ void k_level0_coef(Level<T> L, const T *__restrict__ rho) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L.cells) return;
+    int pi[3] = {0, 0, 0};
+    long long r = t;
+    if (DIM == 3) {
+        pi[2] = int(r % L.P[2]);
+        r /= L.P[2];
+    }
+    pi[1] = int(r % L.P[1]);
+    pi[0] = int(r / L.P[1]);
+    T *dst[3] = {L.cx, L.cy, L.cz};
+    for (int a = 0; a < DIM; ++a) {
+        T C = 0;
+        if (pi[a] + 1 < L.P[a]) C = T(2) / (rho[t] + rho[t + L.s[a]]) * T(1.0 / (L.d[a] * L.d[a]));
+        dst[a][t] = C;
+    }
+}
+
+// 1 / (sum of the face coefficients) of every interior cell of a stored-coefficient level
+template <class T, int DIM>
+__global__ void k_inv_diag(Level<T> L) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nc = (long long)L.n[0] * L.n[1] * (DIM == 3 ? L.n[2] : 1);
+    if (t >= nc) return;
+    int I, J, K = 0;
+    if (DIM == 3) {
+        K = int(t % L.n[2]);
+        const long long rr = t / L.n[2];
+        J = int(rr % L.n[1]);
+        I = int(rr / L.n[1]);
+    } else {
+        J = int(t % L.n[1]);
+        I = int(t / L.n[1]);
+    }
+    const long long P = (I + 1) * L.s[0] + (J + 1) * L.s[1] + (DIM == 3 ? K + 1 : 0);
+    T sc = L.cx[P - L.s[0]] + L.cx[P] + L.cy[P - L.s[1]] + L.cy[P];
+    if (DIM == 3) sc += L.cz[P - 1] + L.cz[P];
+    L.idg[P] = T(1) / sc;
 }
 
 // ---------------------------------------------------------------- coarsest level: dense FP64 inverse
@@ -699,11 +764,12 @@ int Poisson::alloc_levels() {
         SCIHPC_CUDA(cudaMalloc(&L.b, bytes));
         SCIHPC_CUDA(cudaMemset(L.x, 0, bytes));
         SCIHPC_CUDA(cudaMemset(L.b, 0, bytes));
-        if (l > 0) {
-            SCIHPC_CUDA(cudaMalloc(&L.cx, 3 * bytes));
-            SCIHPC_CUDA(cudaMemset(L.cx, 0, 3 * bytes));
+        if (l > 0 || sizeof(T) == 8) {
+            SCIHPC_CUDA(cudaMalloc(&L.cx, 4 * bytes));
+            SCIHPC_CUDA(cudaMemset(L.cx, 0, 4 * bytes));
             L.cy = L.cx + L.cells;
             L.cz = L.cy + L.cells;
+            L.idg = L.cz + L.cells;
         }
         for (int a = 0; a < 3; ++a) dd[a] *= ratio[l];
     }
@@ -736,6 +802,10 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     dvec = r + n;
     q = dvec + n;
     SCIHPC_CUDA(cudaMemset(r, 0, 3 * n * sizeof(double)));
+    if (density) {
+        SCIHPC_CUDA(cudaMalloc(&oc, 3 * n * sizeof(double)));
+        SCIHPC_CUDA(cudaMemset(oc, 0, 3 * n * sizeof(double)));
+    }
     SCIHPC_CUDA(cudaMalloc(&partial, 2 * RED_MAX_BLOCKS * sizeof(double) + 64));
     SCIHPC_CUDA(cudaMemset(partial, 0, 2 * RED_MAX_BLOCKS * sizeof(double) + 64));
     SCIHPC_CUDA(cudaMalloc(&dev_state, sizeof(PcgScalars)));
@@ -767,6 +837,8 @@ void Poisson::destroy() {
     rel(dense);
     rel(zold);
     rel(rho_pad);
+    rel(oc);
+    oc = nullptr;
     if (host_state) cudaFreeHost(host_state);
     r = nullptr;
 }
@@ -809,6 +881,10 @@ void Poisson::build_coarse(cudaStream_t s) {
     }
     Id2<T> id2{};
     for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? T(1.0 / (D.d[a] * D.d[a])) : T(0);
+    if (sizeof(T) == 8 && mode0 == 1) {
+        if (D.ndim == 2) k_level0_coef<T, 2><<<blocks_for(Ls[0].cells, TPB), TPB, 0, s>>>(Ls[0], (const T *)rho_pad);
+        else k_level0_coef<T, 3><<<blocks_for(Ls[0].cells, TPB), TPB, 0, s>>>(Ls[0], (const T *)rho_pad);
+    }
     for (int l = 0; l + 1 < nlev; ++l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         for (int axis = 0; axis < D.ndim; ++axis) {
@@ -817,16 +893,22 @@ void Poisson::build_coarse(cudaStream_t s) {
             const long long total = (long long)E[0] * E[1] * E[2];
             const unsigned nb = blocks_for(total, TPB);
             const T *rp = (const T *)rho_pad;
+            const bool stored0 = l > 0 || (sizeof(T) == 8 && mode0 == 1);
             if (D.ndim == 2) {
-                if (l > 0) k_coarse_coef<T, 0, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+                if (stored0) k_coarse_coef<T, 0, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
                 else if (mode0 == 1) k_coarse_coef<T, 1, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
                 else k_coarse_coef<T, 2, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
             } else {
-                if (l > 0) k_coarse_coef<T, 0, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
+                if (stored0) k_coarse_coef<T, 0, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
                 else if (mode0 == 1) k_coarse_coef<T, 1, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
                 else k_coarse_coef<T, 2, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2, axis);
             }
         }
+    }
+    for (int l = (sizeof(T) == 8 && mode0 == 1) ? 0 : 1; l < nlev; ++l) {
+        const long long nc = (long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2];
+        if (D.ndim == 2) k_inv_diag<T, 2><<<blocks_for(nc, TPB), TPB, 0, s>>>(Ls[l]);
+        else k_inv_diag<T, 3><<<blocks_for(nc, TPB), TPB, 0, s>>>(Ls[l]);
     }
     Level<T> &C = Ls[nlev - 1];
     double *M = dense, *W = dense + size_t(ncoarse) * ncoarse;
@@ -837,6 +919,7 @@ void Poisson::build_coarse(cudaStream_t s) {
 
 int Poisson::set_density(const double *rho, cudaStream_t s) {
     rho64 = rho;
+    if (density_) k_outer_coef<<<blocks_for(D.interior(), TPB), TPB, 0, s>>>(rho, oc, D, D.interior());
     if (fp32_) build_coarse<float>(s);
     else build_coarse<double>(s);
     SCIHPC_CUDA(cudaGetLastError());
@@ -847,7 +930,7 @@ template <class T>
 void Poisson::vcycle(cudaStream_t s) {
     std::vector<Level<T>> &Ls = levs<T>();
     const bool neumann = bc_ == 0;
-    const int mode0 = (density_ || neumann) ? 1 : 2;
+    const int mode0 = (density_ || neumann) ? (sizeof(T) == 8 ? 0 : 1) : 2;
     const T *rp = (const T *)rho_pad;
     Id2<T> id2{};
     for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? T(1.0 / (D.d[a] * D.d[a])) : T(0);
@@ -905,9 +988,11 @@ void Poisson::vcycle(cudaStream_t s) {
     }
 }
 
-static Outer make_outer(const Dims &D, int density, int dirichlet) {
+static Outer make_outer(const Dims &D, int density, int dirichlet, const double *oc) {
     Outer O;
     O.D = D;
+    O.oc = oc;
+    O.n = D.interior();
     for (int a = 0; a < 3; ++a) {
         O.nint[a] = D.n[a];
         O.id2[a] = a < D.ndim ? 1.0 / D.d[a] / D.d[a] : 0.0;
@@ -924,7 +1009,7 @@ void Poisson::begin(const double *rhs, double *p, int use_guess, cudaStream_t s)
     rhs_ = rhs;
     p_ = p;
     const long long n = D.interior();
-    const Outer O = make_outer(D, density_, bc_ == 1);
+    const Outer O = make_outer(D, density_, bc_ == 1, oc);
     RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     const int nb = grid_blocks(n);
     cudaMemsetAsync(dev_state, 0, sizeof(PcgScalars), s);
@@ -936,7 +1021,7 @@ void Poisson::begin(const double *rhs, double *p, int use_guess, cudaStream_t s)
 
 void Poisson::iterate(cudaStream_t s) {
     const long long n = D.interior();
-    const Outer O = make_outer(D, density_, bc_ == 1);
+    const Outer O = make_outer(D, density_, bc_ == 1, oc);
     RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     const int nb = grid_blocks(n);
     if (fp32_) {
@@ -961,7 +1046,7 @@ void Poisson::iterate(cudaStream_t s) {
 
 void Poisson::finish(double *p, cudaStream_t s) {
     const long long n = D.interior();
-    const Outer O = make_outer(D, density_, bc_ == 1);
+    const Outer O = make_outer(D, density_, bc_ == 1, oc);
     RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     const int nb = grid_blocks(n);
     if (bc_ == 0) {

@@ -21,6 +21,7 @@ struct Level {
     double d[3] = {0, 0, 0};
     T *x = nullptr, *b = nullptr;
     T *cx = nullptr, *cy = nullptr, *cz = nullptr;
+    T *idg = nullptr;   // 1 / sum of the face coefficients (levels with stored coefficients)
 };
 
 struct PcgScalars {
@@ -87,6 +88,7 @@ private:
     void *rho_pad = nullptr;    // level-0 density, padded, T, +inf halo
     const double *rho64 = nullptr;   // caller's ghosted density (FP64 operator)
     double *partial = nullptr;       // reduction scratch (2 x RED_MAX_BLOCKS)
+    double *oc = nullptr;            // FP64 +face coefficients of the outer operator (3 compact arrays)
     double *dense = nullptr;         // coarsest-level inverse (n x n, FP64)
     int ncoarse = 0;
     const double *rhs_ = nullptr;

@@ -44,6 +44,9 @@ def ws(g):
 
 
 GRIDS = [grid2(), grid2(9, 14, (-1.0, 0.5), (2.0, 3.0)), grid3(), grid3(6, 5, 7)]
+# line lengths for every register tier of the warp-cooperative solver (<= 128, 256, 512
+# points) and one longer line for the sequential fallback
+LONG = [grid2(120, 9), grid2(7, 250), grid2(500, 5), grid2(5, 600), grid3(40, 6, 260)]
 
 
 @pytest.mark.parametrize("gi", range(len(GRIDS)))
@@ -100,9 +103,9 @@ def test_extrapolations_bitexact(port, gi):
     assert np.array_equal(host(d), ref)
 
 
-@pytest.mark.parametrize("gi", range(len(GRIDS)))
+@pytest.mark.parametrize("gi", range(len(GRIDS) + len(LONG)))
 def test_uccd(port, gi):
-    g = GRIDS[gi]
+    g = (GRIDS + LONG)[gi]
     w = ws(g)
     rng = np.random.default_rng(500 + gi)
     flux = smooth_field(g, rng)
@@ -117,9 +120,9 @@ def test_uccd(port, gi):
         assert np.abs(o2 - ref[3 + a]).max() <= TOL_UCCD * np.abs(ref[3 + a]).max(), a
 
 
-@pytest.mark.parametrize("gi", range(len(GRIDS)))
+@pytest.mark.parametrize("gi", range(len(GRIDS) + len(LONG)))
 def test_ccd_and_mixed(port, gi):
-    g = GRIDS[gi]
+    g = (GRIDS + LONG)[gi]
     w = ws(g)
     rng = np.random.default_rng(600 + gi)
     flux = smooth_field(g, rng)
