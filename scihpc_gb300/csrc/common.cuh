@@ -16,6 +16,8 @@
 namespace scihpc {
 
 constexpr int GHC = 3;
+// streaming multiprocessors of a GB300 (two dies of 76); used to size small grids
+constexpr int NUM_SMS = 152;
 
 struct Dims {
     int ndim;

@@ -34,12 +34,14 @@ __device__ __forceinline__ double weno_face(double a, double b, double c, double
         q1 = (2.0 * b + 5.0 * c - d) * sixth;
         q2 = (-a + 5.0 * b + 2.0 * c) * sixth;
     }
+    // WENO-Z weights a_k = d_k (1 + tau / g_k), g_k = eps + beta_k, multiplied through by
+    // g0 g1 g2 so that one division remains
     const double tau = fabs(b0 - b2);
-    const double a0 = 1.0 + tau / (WENO_EPS + b0);
-    const double a1 = 6.0 * (1.0 + tau / (WENO_EPS + b1));
-    const double a2 = 3.0 * (1.0 + tau / (WENO_EPS + b2));
-    const double inv = 1.0 / (a0 + a1 + a2);
-    return (a0 * q0 + a1 * q1 + a2 * q2) * inv;
+    const double g0 = WENO_EPS + b0, g1 = WENO_EPS + b1, g2 = WENO_EPS + b2;
+    const double a0 = (g0 + tau) * g1 * g2;
+    const double a1 = 6.0 * (g1 + tau) * g0 * g2;
+    const double a2 = 3.0 * (g2 + tau) * g0 * g1;
+    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
 }
 
 // Upwinded face value between cells i and i+1 (weno_solver.cpp:185-199).

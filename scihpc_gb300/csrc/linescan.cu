@@ -231,11 +231,16 @@ bool launch_scan(const Dims &D, int a, double *io, const double *vel, double *f1
     const int b = (a + 1) % 3, c = (a + 2) % 3;
     const int fast = b > c ? b : c, slow = b > c ? c : b;
     const long long lines = (long long)D.N[b] * D.N[c];
-    const unsigned blocks = unsigned((lines + 7) / 8);
+    // The solve is FP64-pipe bound, so the lines are spread over as many SMs as possible:
+    // one warp per block until there are several lines for every SM, then up to eight.
+    int wpb = 1;
+    while (wpb < 8 && lines >= (long long)wpb * 2 * 4 * NUM_SMS) wpb *= 2;
+    const unsigned blocks = unsigned((lines + wpb - 1) / wpb);
+    const int tpb = 32 * wpb;
     const int C = (D.N[a] + 31) / 32;
-    if (C <= 4) scan_kernel<MODE, 4><<<blocks, 256, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
-    else if (C <= 8) scan_kernel<MODE, 8><<<blocks, 256, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
-    else if (C <= 16) scan_kernel<MODE, 16><<<blocks, 256, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    if (C <= 4) scan_kernel<MODE, 4><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    else if (C <= 8) scan_kernel<MODE, 8><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    else if (C <= 16) scan_kernel<MODE, 16><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
     else return false;
     return true;
 }

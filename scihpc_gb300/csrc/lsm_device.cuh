@@ -30,9 +30,12 @@ __device__ __forceinline__ double weno_godunov(double a, double b, double c, dou
     const double is1 = 13.0 * (b - c) * (b - c) + 3.0 * (b + c) * (b + c);
     const double is2 = 13.0 * (c - d) * (c - d) + 3.0 * (3.0 * c - d) * (3.0 * c - d);
     const double e0 = WENO_EPS + is0, e1 = WENO_EPS + is1, e2 = WENO_EPS + is2;
-    const double al0 = 1.0 / (e0 * e0), al1 = 6.0 / (e1 * e1), al2 = 3.0 / (e2 * e2);
-    const double inv = 1.0 / (al0 + al1 + al2);
-    const double w0 = al0 * inv, w2 = al2 * inv;
+    // weights alpha_k = d_k / e_k^2 normalised; multiplied through by (e0 e1 e2)^2 so that a
+    // single division remains (FP64 division is the costly operation on this GPU)
+    const double q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+    const double p12 = q1 * q2, p02 = q0 * q2, p01 = q0 * q1;
+    const double inv = 1.0 / (p12 + 6.0 * p02 + 3.0 * p01);
+    const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
     return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
 }
 

@@ -33,6 +33,8 @@ namespace scihpc {
 namespace {
 
 constexpr int TPB = 256;
+// levels of at most this many cells run together in one thread block (k_coarse_cycle)
+constexpr long long COARSE_CELLS = 8192;
 
 // ---------------------------------------------------------------- grid-wide deterministic reductions
 // Each block reduces its values in a fixed tree, writes a partial, and the last block to
@@ -366,6 +368,12 @@ __global__ void k_relres(PcgScalars *st) { st->relres = st->bb > 0.0 ? sqrt(st->
 // ---------------------------------------------------------------- V-cycle kernels (precision T)
 // MODE 0: stored face coefficients; 1: level 0 from the padded density (+inf halo gives
 // zero wall coefficients); 2: level 0 constant 1/d^2 with the zero halo as ghost value.
+// Division inside the preconditioner.  The FP32 cycle only has to be the same linear map
+// on every application, not correctly rounded, so it takes the fast approximate divide
+// (+inf denominators from the padded halo still give 0); FP64 divides exactly.
+__device__ __forceinline__ float pdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double pdiv(double a, double b) { return a / b; }
+
 template <class T, int MODE>
 __device__ __forceinline__ void faces(const Level<T> &L, const T *__restrict__ rho, const T *id2, long long P, int ndim,
                                       T C[6]) {
@@ -376,8 +384,8 @@ __device__ __forceinline__ void faces(const Level<T> &L, const T *__restrict__ r
     } else if (MODE == 1) {
         const T rc = rho[P];
         for (int a = 0; a < ndim; ++a) {
-            C[2 * a] = T(2) / (rc + rho[P - L.s[a]]) * id2[a];
-            C[2 * a + 1] = T(2) / (rc + rho[P + L.s[a]]) * id2[a];
+            C[2 * a] = pdiv(T(2), rc + rho[P - L.s[a]]) * id2[a];
+            C[2 * a + 1] = pdiv(T(2), rc + rho[P + L.s[a]]) * id2[a];
         }
     } else {
         for (int a = 0; a < ndim; ++a) C[2 * a] = C[2 * a + 1] = id2[a];
@@ -389,13 +397,18 @@ struct Id2 {
     T v[3];
 };
 
+template <class T, int DIM>
+__device__ __forceinline__ long long smooth_count(const Level<T> &L) {
+    const long long rows = DIM == 3 ? (long long)L.n[0] * L.n[1] : L.n[0];
+    return rows * ((L.n[DIM - 1] + 1) / 2);
+}
+
+// One red-black Gauss-Seidel update; t enumerates the cells of one colour.
 template <class T, int MODE, int DIM>
-__global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int color) {
+__device__ __forceinline__ void smooth_one(const Level<T> &L, const T *__restrict__ rho, const T *id2, long long t,
+                                           int color) {
     const int nf = L.n[DIM - 1];
     const int nh = (nf + 1) / 2;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long rows = DIM == 3 ? (long long)L.n[0] * L.n[1] : L.n[0];
-    if (t >= rows * nh) return;
     const int kh = int(t % nh);
     const long long row = t / nh;
     int I, J, K;
@@ -413,7 +426,7 @@ __global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int 
         P = (I + 1) * L.s[0] + (J + 1);
     }
     T C[6];
-    faces<T, MODE>(L, rho, id2.v, P, DIM, C);
+    faces<T, MODE>(L, rho, id2, P, DIM, C);
     T sx = C[0] * L.x[P - L.s[0]] + C[1] * L.x[P + L.s[0]] + C[2] * L.x[P - L.s[1]] + C[3] * L.x[P + L.s[1]];
     if (DIM == 3) sx += C[4] * L.x[P - 1] + C[5] * L.x[P + 1];
     if (MODE == 0) {
@@ -421,8 +434,15 @@ __global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int 
     } else {
         T sc = C[0] + C[1] + C[2] + C[3];
         if (DIM == 3) sc += C[4] + C[5];
-        L.x[P] = (L.b[P] + sx) / sc;
+        L.x[P] = pdiv(L.b[P] + sx, sc);
     }
+}
+
+template <class T, int MODE, int DIM>
+__global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int color) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= smooth_count<T, DIM>(L)) return;
+    smooth_one<T, MODE, DIM>(L, rho, id2.v, t, color);
 }
 
 template <class T, int MODE, int DIM>
@@ -438,10 +458,8 @@ __device__ __forceinline__ T residual_at(const Level<T> &L, const T *__restrict_
 
 // coarse b = mean of the fine residuals of its r^d children; coarse x = 0
 template <class T, int MODE, int DIM>
-__global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
-    if (t >= nc) return;
+__device__ __forceinline__ void restrict_one(const Level<T> &F, const Level<T> &Cl, const T *__restrict__ rho,
+                                             const T *id2, long long t) {
     int I, J, K = 0;
     if (DIM == 3) {
         K = int(t % Cl.n[2]);
@@ -458,11 +476,19 @@ __global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, I
         for (int b = 0; b < r; ++b)
             for (int c = 0; c < (DIM == 3 ? r : 1); ++c) {
                 const long long P = (r * I + a + 1) * F.s[0] + (r * J + b + 1) * F.s[1] + (DIM == 3 ? r * K + c + 1 : 0);
-                s += residual_at<T, MODE, DIM>(F, rho, id2.v, P);
+                s += residual_at<T, MODE, DIM>(F, rho, id2, P);
             }
     const long long Pc = (I + 1) * Cl.s[0] + (J + 1) * Cl.s[1] + (DIM == 3 ? K + 1 : 0);
-    Cl.b[Pc] = s / T(DIM == 3 ? r * r * r : r * r);
+    Cl.b[Pc] = pdiv(s, T(DIM == 3 ? r * r * r : r * r));
     Cl.x[Pc] = 0;
+}
+
+template <class T, int MODE, int DIM>
+__global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
+    if (t >= nc) return;
+    restrict_one<T, MODE, DIM>(F, Cl, rho, id2.v, t);
 }
 
 // fine x += interpolation of coarse x.  Default: piecewise constant (the transpose of the
@@ -470,10 +496,8 @@ __global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, I
 // CG requires).  linear = 1: (bi/tri)linear for ratio 2 (weights 3/4, 1/4 per axis; Neumann
 // walls clamp to the wall cell, Dirichlet walls read the zero halo).
 template <class T, int DIM>
-__global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nf = (long long)F.n[0] * F.n[1] * (DIM == 3 ? F.n[2] : 1);
-    if (t >= nf) return;
+__device__ __forceinline__ void prolong_one(const Level<T> &F, const Level<T> &Cl, int neumann, int linear,
+                                            long long t) {
     int ii[3] = {0, 0, 0};
     if (DIM == 3) {
         ii[2] = int(t % F.n[2]);
@@ -510,6 +534,14 @@ __global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
             T(1.0 / 64.0) * CX(nb[0], nb[1], nb[2]);
     }
     F.x[Pf] += v;
+}
+
+template <class T, int DIM>
+__global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nf = (long long)F.n[0] * F.n[1] * (DIM == 3 ? F.n[2] : 1);
+    if (t >= nf) return;
+    prolong_one<T, DIM>(F, Cl, neumann, linear, t);
 }
 
 // coarse face coefficients from the fine level (mean over the fine faces of a coarse face,
@@ -711,6 +743,80 @@ __global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n
         double s = 0.0;
         for (int q = 0; q < n; ++q) s += row[q] * (b[q] - mean);
         L.x[pidx(c)] = T(s);
+    }
+}
+
+// The coarse end of the V-cycle in one thread block: levels lc .. nlev-1 (each at most a few
+// thousand cells) are smoothed, restricted, solved and prolongated with __syncthreads()
+// between phases instead of one kernel launch per phase.  Levels >= 1 carry stored
+// coefficients.
+template <class T>
+struct LevelPack {
+    Level<T> L[16];
+};
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, int nlev, const double *__restrict__ Minv,
+                                                        int n, int neumann, int linear) {
+    __shared__ double b[1024];
+    __shared__ double mean;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int nu = 2;
+    for (int l = lc; l < nlev - 1; ++l) {
+        const Level<T> &L = LP.L[l];
+        const long long cnt = smooth_count<T, DIM>(L);
+        for (int k = 0; k < nu; ++k)
+            for (int color = 0; color < 2; ++color) {
+                for (long long t = tid; t < cnt; t += nt) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
+                __syncthreads();
+            }
+        const Level<T> &Cl = LP.L[l + 1];
+        const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
+        for (long long t = tid; t < nc; t += nt) restrict_one<T, 0, DIM>(L, Cl, nullptr, nullptr, t);
+        __syncthreads();
+    }
+    {
+        const Level<T> &L = LP.L[nlev - 1];
+        auto pidx = [&](int c) {
+            int I, J, K = 0;
+            if (DIM == 3) {
+                K = c % L.n[2];
+                J = (c / L.n[2]) % L.n[1];
+                I = c / (L.n[2] * L.n[1]);
+            } else {
+                J = c % L.n[1];
+                I = c / L.n[1];
+            }
+            return (I + 1) * L.s[0] + (J + 1) * L.s[1] + (DIM == 3 ? K + 1 : 0);
+        };
+        for (int c = tid; c < n; c += nt) b[c] = double(L.b[pidx(c)]);
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0.0;
+            if (neumann)
+                for (int c = 0; c < n; ++c) s += b[c];
+            mean = s / n;
+        }
+        __syncthreads();
+        for (int c = tid; c < n; c += nt) {
+            const double *row = Minv + (size_t)c * n;
+            double s = 0.0;
+            for (int q = 0; q < n; ++q) s += row[q] * (b[q] - mean);
+            L.x[pidx(c)] = T(s);
+        }
+        __syncthreads();
+    }
+    for (int l = nlev - 2; l >= lc; --l) {
+        const Level<T> &L = LP.L[l];
+        const long long nf = (long long)L.n[0] * L.n[1] * (DIM == 3 ? L.n[2] : 1);
+        for (long long t = tid; t < nf; t += nt) prolong_one<T, DIM>(L, LP.L[l + 1], neumann, linear, t);
+        __syncthreads();
+        const long long cnt = smooth_count<T, DIM>(L);
+        for (int k = 0; k < nu; ++k)
+            for (int color = 1; color >= 0; --color) {
+                for (long long t = tid; t < cnt; t += nt) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
+                __syncthreads();
+            }
     }
 }
 
@@ -952,7 +1058,17 @@ void Poisson::vcycle(cudaStream_t s) {
         }
     };
     cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
-    for (int l = 0; l + 1 < nlev; ++l) {
+    // levels from lc on (each <= COARSE_CELLS cells) run inside one thread block
+    int lc = nlev - 1;
+    for (int l = 1; l < nlev; ++l) {
+        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= COARSE_CELLS) {
+            lc = l;
+            break;
+        }
+    }
+    const bool fused = nlev <= 16;   // LevelPack capacity
+    if (lc < 1 || !fused) lc = nlev - 1 > 0 ? nlev - 1 : 0;
+    for (int l = 0; l < lc; ++l) {
         for (int k = 0; k < nu; ++k) {
             smooth(l, 0);
             smooth(l, 1);
@@ -971,12 +1087,17 @@ void Poisson::vcycle(cudaStream_t s) {
             else k_restrict<T, 2, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
         }
     }
-    {
+    if (fused && lc >= 1) {
+        LevelPack<T> LP;
+        for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
+        if (D.ndim == 2) k_coarse_cycle<T, 2><<<1, 1024, 0, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear);
+        else k_coarse_cycle<T, 3><<<1, 1024, 0, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear);
+    } else {
         Level<T> &C = Ls[nlev - 1];
         if (D.ndim == 2) k_dense_solve<T, 2><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
         else k_dense_solve<T, 3><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
     }
-    for (int l = nlev - 2; l >= 0; --l) {
+    for (int l = lc - 1; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
         if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);

@@ -36,17 +36,51 @@ __device__ __forceinline__ bool interior_cell(long long q, const Dims &D, long l
     return true;
 }
 
+// Neumann ghost fill of one scalar fused into the kernel that produces its new interior
+// value: with Neumann on every face (the reference drivers' level-set and pressure BC),
+// each ghost of a transverse-interior line depends only on the boundary cell of that line
+// (neumann.cpp:7-83), so the thread that writes the boundary cell writes its three ghosts.
+// Separate multiply and add keep the rounding of the reference's fill.
+__device__ __forceinline__ void neumann_ghosts(double *__restrict__ f, long long o, int I, int J, int K, const Dims &D,
+                                               const GhostFill &G, double val) {
+    const int II[3] = {I, J, K};
+    for (int a = 0; a < D.ndim; ++a) {
+        const long long st = D.s[a];
+        const double dh = D.d[a];
+        if (II[a] == D.n[a] - 1) {
+            double g = val;
+            for (int q = 1; q <= GHC; ++q) {
+                g = __dadd_rn(g, __dmul_rn(G.v[2 * a + 1], dh));
+                f[o + q * st] = g;
+            }
+        }
+        if (II[a] == 0) {
+            double g = val;
+            for (int q = 1; q <= GHC; ++q) {
+                g = __dsub_rn(g, __dmul_rn(G.v[2 * a], dh));
+                f[o - q * st] = g;
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------- Runge-Kutta stages (runge_kutta.cpp:13-63)
 // stage 1: f += dt s1; stage 2: f += dt (s2 - 3 s1) / 4; stage 3: f += dt (-s1 - s2 + 8 s3) / 12;
 // stage 0: forward Euler f += dt s1.
 __global__ void k_stage(double *__restrict__ f, const double *__restrict__ s1, const double *__restrict__ s2,
-                        const double *__restrict__ s3, Dims D, int stage, const StepScalars *sc) {
-    long long o;
-    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+                        const double *__restrict__ s3, Dims D, int stage, const StepScalars *sc, GhostFill G) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.interior()) return;
+    int I, J, K;
+    split3(q, D, I, J, K);
+    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
     const double dt = sc->dt;
-    if (stage <= 1) f[o] += dt * s1[o];
-    else if (stage == 2) f[o] += dt * (s2[o] - 3.0 * s1[o]) / 4.0;
-    else f[o] += dt * (-s1[o] - s2[o] + 8.0 * s3[o]) / 12.0;
+    double v = f[o];
+    if (stage <= 1) v += dt * s1[o];
+    else if (stage == 2) v += dt * (s2[o] - 3.0 * s1[o]) / 4.0;
+    else v += dt * (-s1[o] - s2[o] + 8.0 * s3[o]) / 12.0;
+    f[o] = v;
+    if (G.on) neumann_ghosts(f, o, I, J, K, D, G, v);
 }
 
 // s = -u phi_x - v phi_y - w phi_z (source.cpp:8-40), interior cells
@@ -151,11 +185,16 @@ __global__ void k_mpls_finish(const double *__restrict__ partial, int nb, StepSc
 
 // s = eta delta |grad phi|, then the Euler update (runge_kutta.cpp:51-63), interior cells
 __global__ void k_mpls_update(double *__restrict__ phi, const double *__restrict__ De, const double *__restrict__ G,
-                              Dims D, const StepScalars *sc) {
-    long long o;
-    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+                              Dims D, const StepScalars *sc, GhostFill GF) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.interior()) return;
+    int I, J, K;
+    split3(q, D, I, J, K);
+    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
     const double s = sc->eta * De[o] * G[o];
-    phi[o] += sc->dt * s;
+    const double v = phi[o] + sc->dt * s;
+    phi[o] = v;
+    if (GF.on) neumann_ghosts(phi, o, I, J, K, D, GF, v);
 }
 
 // ---------------------------------------------------------------- reinitialisation (source.cpp:156-241)
@@ -183,7 +222,7 @@ __global__ void k_reinit_a(const double *__restrict__ phi, const double *__restr
 __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ De, const double *__restrict__ G,
                            double *__restrict__ sk, const double *__restrict__ s1, const double *__restrict__ s2,
                            const double *__restrict__ A, const double *__restrict__ B, Dims D, double rdt,
-                           int lambda, int stage, const StepScalars *sc) {
+                           int lambda, int stage, const StepScalars *sc, GhostFill GF) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= D.interior()) return;
     int I, J, K;
@@ -218,10 +257,12 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
         if (fabs(b) > 1e-8) s += a / b * De[o] * G[o] * rdt / dt;
         sk[o] = s;
     }
-    double &f = phi[o];
+    double f = phi[o];
     if (stage == 1) f += dt * s;
     else if (stage == 2) f += dt * (s - 3.0 * s1[o]) / 4.0;
     else f += dt * (-s1[o] - s2[o] + 8.0 * s) / 12.0;
+    phi[o] = f;
+    if (GF.on) neumann_ghosts(phi, o, I, J, K, D, GF, f);
 }
 
 // ---------------------------------------------------------------- projection method (projection_method.cpp)
@@ -514,6 +555,11 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
             if (f / 2 == c && vel_bc[f] == 3) vel_types[c][f] = 2;
         }
     for (int f = 0; f < 6; ++f) scalar_types[f] = scalar_bc[f];
+    phi_fill.on = 1;
+    for (int f = 0; f < 2 * D.ndim; ++f) {
+        if (scalar_types[f] != 1) phi_fill.on = 0;
+        phi_fill.v[f] = 0.0;   // the wrapper's bc_info values are zero (bc_factory.h:24-27)
+    }
     int rc = ops.build(D);
     if (rc) return rc;
     SCIHPC_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -681,8 +727,8 @@ void TwoPhaseGpu::advect() {
     double *S[3] = {s1, s2, s3};
     for (int st = 1; st <= 3; ++st) {
         convection_rhs(S[st - 1]);
-        k_stage<<<nbi, TPB, 0, stream>>>(phi.data, s1, s2, s3, D, st, sc);
-        scalar_bc(phi.data);
+        k_stage<<<nbi, TPB, 0, stream>>>(phi.data, s1, s2, s3, D, st, sc, phi_fill);
+        if (!phi_fill.on) scalar_bc(phi.data);
     }
 }
 
@@ -696,8 +742,8 @@ void TwoPhaseGpu::mpls(int count) {
                                                P.ls_width, P.density_ratio, P.positive_ref);
         k_mpls_sums<<<nb, RED_THREADS, 0, stream>>>(work, H, delta, grad, D, P.density_ratio, P.positive_ref, partial);
         k_mpls_finish<<<1, 1024, 0, stream>>>(partial, nb, sc, D.dv);
-        k_mpls_update<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, D, sc);
-        scalar_bc(phi.data);
+        k_mpls_update<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, D, sc, phi_fill);
+        if (!phi_fill.on) scalar_bc(phi.data);
     }
 }
 
@@ -706,8 +752,8 @@ void TwoPhaseGpu::reinit_stage(int stage) {
     double *S[3] = {s1, s2, s3};
     k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
     k_reinit_b<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, S[stage - 1], s1, s2, a_f, b_f, D, P.rdt, reinit_lambda,
-                                        stage, sc);
-    scalar_bc(phi.data);
+                                        stage, sc, phi_fill);
+    if (!phi_fill.on) scalar_bc(phi.data);
 }
 
 int TwoPhaseGpu::reinit() {

@@ -18,6 +18,12 @@ struct DevScalar {
     double *mixed[3] = {nullptr, nullptr, nullptr};   // fxy, fyz, fzx
 };
 
+// Neumann ghost fill fused into the kernels that write a scalar's interior (twophase.cu).
+struct GhostFill {
+    int on;
+    double v[6];   // bc values xl, xr, yl, yr, zl, zr
+};
+
 struct HostParams {
     double density_ratio, viscosity_ratio, Re, Fr, We, ls_width, rdt, max_CFL, min_CFL;
     int positive_ref;
@@ -78,6 +84,7 @@ private:
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;
     int reinit_steps = 0;
+    GhostFill phi_fill{};
     long long nodes_pre = 0, nodes_body = 0, nodes_post = 0;
 };
 
