@@ -198,33 +198,22 @@ def run_reference(args) -> None:
 
 # ----------------------------------------------------------------------------- GPU leg
 def vcycle_bytes(levels, ndim: int, w: int) -> float:
-    """Algorithmic bytes of one V(2,2) cycle, summed over levels: per cell of level l, 4 full
-    red-black sweeps reading x, b and the coefficients (level 0: the density; coarser: ndim
-    face arrays) and writing x; the fused residual-restriction reads x, b, coefficients and
-    writes the coarse b and x; the prolongation reads the coarse x and updates x; level 0's
-    x is cleared once."""
-    tot = 0.0
-    for l, n in enumerate(levels):
-        cells = 1
-        for a in range(ndim):
-            cells *= n[a]
-        coef = 1 if l == 0 else ndim
-        sweeps = 4 * (3 + coef) if l < len(levels) - 1 else 0
-        restrict = (2 + coef) if l < len(levels) - 1 else 0
-        coarse_w = 2.0 / (2 ** ndim) if l < len(levels) - 1 else 0.0
-        prolong = (2.0 + 1.0 / (2 ** ndim)) if l < len(levels) - 1 else 0.0
-        clear = 1 if l == 0 else 0
-        last = 2 if l == len(levels) - 1 else 0   # dense solve: read b, write x
-        tot += cells * w * (sweeps + restrict + coarse_w + prolong + clear + last)
-    return tot
+    """Algorithmic bytes of one V(2,2) cycle by the fixed model: per interior cell of the
+    finest level, [4w(nu1 + nu2) + 5w + 2w/2^d] * 2^d / (2^d - 1) -- a full red-black sweep
+    reads x, b and the density and writes x (4w); residual + restriction 3w + w/2^d;
+    prolongation + correction 2w + w/2^d; the coarser levels add the geometric factor.
+    V(2,2) gives 24.29w per cell in 3D and 28.33w in 2D."""
+    cells = 1
+    for a in range(ndim):
+        cells *= levels[0][a]
+    c = 2 ** ndim
+    return cells * (4 * w * 4 + 5 * w + 2 * w / c) * c / (c - 1)
 
 
-def poisson_block(torch, Poisson, Grid, hbm):
-    """256^3 variable-density pressure equation (density 1 + 999 H(phi), phi from 12 seeded
-    spheres, Neumann walls, zero-mean right-hand side from a random divergent velocity),
-    solved to relative residual 1e-10 with FP64 V-cycles and with FP32 V-cycles inside the
-    FP64 refinement."""
-    n = 256
+def poisson_problem(torch, Grid, n=256):
+    """The n^3 variable-density pressure equation: density 1 + 999 H(phi), phi from 12 seeded
+    spheres, Neumann walls, zero-mean right-hand side from a random divergent velocity.
+    Returns (grid, rho, rhs) as ghosted FP64 device fields."""
     g = Grid(3, (n, n, n), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
     dev = torch.device("cuda")
     gen = torch.Generator(device="cpu").manual_seed(20261203)
@@ -263,6 +252,15 @@ def poisson_block(torch, Poisson, Grid, hbm):
     rhs = torch.zeros(g.shape, dtype=torch.float64, device=dev)
     rhs[3:-3, 3:-3, 3:-3] = div - div.mean()
     del div
+    return g, rho, rhs
+
+
+def poisson_block(torch, Poisson, Grid, hbm):
+    """256^3 variable-density pressure equation solved to relative residual 1e-10 with FP64
+    V-cycles (FP64 conjugate gradients) and with FP32 V-cycles inside FP32 conjugate
+    gradients inside FP64 iterative refinement."""
+    g, rho, rhs = poisson_problem(torch, Grid)
+    dev = rho.device
     out = {"grid": "256^3", "density": "1 + 999 H(phi), 12 seeded spheres r in [0.05, 0.2]",
            "rel_tol": 1e-10}
     for name, fp32 in (("fp64", False), ("fp32_refined", True)):
@@ -394,6 +392,21 @@ def run_ours(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+def profile_poisson(precision: str) -> None:
+    """One density update and three solver iterations of the 256^3 pressure equation: the
+    small case the profiles of the pressure kernels are captured on."""
+    import torch
+    from scihpc_gb300 import Grid, Poisson, lib
+    lib()
+    g, rho, rhs = poisson_problem(torch, Grid)
+    ps = Poisson(g, bc=0, density=True, fp32=precision == "fp32")
+    ps.set_density(rho)
+    p = torch.zeros(g.shape, dtype=torch.float64, device=rho.device)
+    it, rr = ps.solve(rhs, p, rel_tol=1e-10, max_iter=3)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "poisson 256^3", "precision": precision, "iterations": it, "relres": rr}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,8 +417,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--lite", action="store_true", help="timed steps only (for kernel launch lists)")
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of graph replay")
+    ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
+                    help="only three iterations of the 256^3 pressure solve (profiling case)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_poisson:
+        profile_poisson(args.profile_poisson)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -33,8 +33,13 @@ namespace scihpc {
 namespace {
 
 constexpr int TPB = 256;
-// levels of at most this many cells run together in one thread block (k_coarse_cycle)
-constexpr long long COARSE_CELLS = 8192;
+// Levels of at most this many cells run together in one thread block (k_coarse_cycle).  One
+// SM executes about 4 FP64 flops per clock on GB300, so FP64 cycles hand over to the single
+// block much later than FP32 ones.
+constexpr long long COARSE_CELLS_FP32 = 4096;
+constexpr long long COARSE_CELLS_FP64 = 512;
+// 3D levels of at least this many cells are smoothed by the one-pass sweep (k_sweep3)
+constexpr long long FUSED_MIN_CELLS = 65536;
 
 // ---------------------------------------------------------------- grid-wide deterministic reductions
 // Each block reduces its values in a fixed tree, writes a partial, and the last block to
@@ -44,14 +49,15 @@ struct RedSlot {
     unsigned *counter;      // zero-initialised, reset by the last block
 };
 
+// Blocks of exactly TPB threads (1D, or 2D with blockDim.x * blockDim.y == TPB).
 template <int NV>
 __device__ void grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
     __shared__ double sh[NV][TPB];
     __shared__ bool last;
-    const int t = threadIdx.x;
+    const int t = threadIdx.x + threadIdx.y * blockDim.x;
     for (int m = 0; m < NV; ++m) sh[m][t] = v[m];
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = TPB / 2; w > 0; w >>= 1) {
         if (t < w)
             for (int m = 0; m < NV; ++m) sh[m][t] += sh[m][t + w];
         __syncthreads();
@@ -66,14 +72,14 @@ __device__ void grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
     if (!last) return;
     __threadfence();
     const int nb = gridDim.x;
-    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    const int per = (nb + TPB - 1) / TPB;
     for (int m = 0; m < NV; ++m) {
         double a = 0.0;
         for (int q = t * per; q < (t + 1) * per && q < nb; ++q) a += __ldcg(&slot.partial[m * RED_MAX_BLOCKS + q]);
         sh[m][t] = a;
     }
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = TPB / 2; w > 0; w >>= 1) {
         if (t < w)
             for (int m = 0; m < NV; ++m) sh[m][t] += sh[m][t + w];
         __syncthreads();
@@ -97,39 +103,70 @@ struct Outer {
     int nint[3];      // interior extents
     long long cs[3];  // compact strides (K fastest)
     double id2[3];
-    int density;      // 1: coefficients oc[a * n + c] of the +a face of compact cell c
+    int density;      // 1: oc[a * n + c] = coefficient of the +a face of compact cell c, oc[3n + c] its diagonal
     int dirichlet;    // 1: wall term against a zero ghost-centre value
     const double *oc;
     long long n;
 };
 
-// (L v)_c for a compact vector v (or a ghosted field when `ghosted`).  Density mode reads the
-// precomputed face coefficients (no FP64 division in the iteration).
-template <bool GHOSTED>
-__device__ __forceinline__ double apply_L(const double *__restrict__ v, const double *__restrict__ rho, const Outer &O,
-                                          int I, int J, int K) {
-    (void)rho;
+// Interior cells visited as rows along the fastest axis: blocks take rows (I[, J]) in a
+// grid-stride loop and threads run along the row, so no thread divides a 64-bit index.
+// f(I, J, K, go, co): go = ghosted offset, co = compact offset.
+template <int DIM, class F>
+__device__ __forceinline__ void for_cells(const Outer &O, F &&f) {
+    const int nf = O.nint[DIM - 1];
+    const int r1 = DIM == 3 ? O.nint[1] : 1;
+    const long long nrows = (long long)O.nint[0] * r1;
+    for (long long row = blockIdx.x; row < nrows; row += gridDim.x) {
+        const int I = int(row / r1);
+        const int J = DIM == 3 ? int(row - (long long)I * r1) : 0;
+        const long long go0 = (long long)(I + GHC) * O.D.s[0] + (DIM == 3 ? (long long)(J + GHC) * O.D.s[1] : 0);
+        const long long co0 = (long long)I * O.cs[0] + (DIM == 3 ? (long long)J * O.cs[1] : 0);
+        for (int t = threadIdx.x; t < nf; t += blockDim.x) {
+            if (DIM == 3) f(I, J, t, go0 + t + GHC, co0 + t);
+            else f(I, t, 0, go0 + (long long)(t + GHC) * O.D.s[1], co0 + t);
+        }
+    }
+}
+
+// padded level-0 offset of interior cell (I, J, K)
+template <int DIM, class T>
+__device__ __forceinline__ long long p0_of(const Level<T> &L0, int I, int J, int K) {
+    return (long long)(I + 1) * L0.s[0] + (long long)(J + 1) * L0.s[1] + (DIM == 3 ? K + 1 : 0);
+}
+
+// g - (L v)_c, with (L v)_c = sum over faces C (v_c - v_nb), for a compact vector v (c = co)
+// or a ghosted field (c = go).  Density mode reads the precomputed face coefficients and
+// diagonal, (L v)_c = diag_c v_c - sum C v_nb: seven FP64 multiply-adds per cell and no FP64
+// division in the iteration.
+template <int DIM, bool GHOSTED>
+__device__ __forceinline__ double minus_L(double g, const double *__restrict__ v, const Outer &O, int I, int J,
+                                          int K, long long c, long long co) {
     const int II[3] = {I, J, K};
-    const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
-    const long long co = I * O.cs[0] + J * O.cs[1] + K;
-    const long long c = GHOSTED ? go : co;
+    double t = fma(-O.oc[3 * O.n + co], v[c], g);
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+        const long long st = GHOSTED ? O.D.s[a] : O.cs[a];
+        if (II[a] > 0) t = fma(O.oc[a * O.n + co - O.cs[a]], v[c - st], t);
+        if (II[a] < O.nint[a] - 1) t = fma(O.oc[a * O.n + co], v[c + st], t);
+    }
+    return t;
+}
+
+template <int DIM, bool GHOSTED>
+__device__ __forceinline__ double apply_L(const double *__restrict__ v, const Outer &O, int I, int J, int K,
+                                          long long c, long long co) {
+    if (O.density) return -minus_L<DIM, GHOSTED>(0.0, v, O, I, J, K, c, co);
+    const int II[3] = {I, J, K};
     const double vc = v[c];
     double s = 0.0;
-    for (int a = 0; a < O.D.ndim; ++a) {
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
         const long long st = GHOSTED ? O.D.s[a] : O.cs[a];
-        for (int side = -1; side <= 1; side += 2) {
-            const bool wall = side < 0 ? II[a] == 0 : II[a] == O.nint[a] - 1;
-            double C, vn;
-            if (wall) {
-                if (!O.dirichlet) continue;
-                C = O.id2[a];
-                vn = 0.0;
-            } else {
-                C = O.density ? O.oc[a * O.n + (side < 0 ? co - O.cs[a] : co)] : O.id2[a];
-                vn = v[c + side * st];
-            }
-            s += C * (vc - vn);
-        }
+        if (II[a] > 0) s += O.id2[a] * (vc - v[c - st]);
+        else if (O.dirichlet) s += O.id2[a] * vc;
+        if (II[a] < O.nint[a] - 1) s += O.id2[a] * (vc - v[c + st]);
+        else if (O.dirichlet) s += O.id2[a] * vc;
     }
     return s;
 }
@@ -137,137 +174,125 @@ __device__ __forceinline__ double apply_L(const double *__restrict__ v, const do
 // Face coefficients of the outer operator, exactly as init_ppe_proj_coefficients forms them
 // (projection_method.cpp:416-424): 1.0 / R / d / d with R the mean density of the two cells;
 // zero on the wall faces.
-__global__ void k_outer_coef(const double *__restrict__ rho, double *__restrict__ oc, Dims D, long long n) {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    int K = int(q % D.n[2]);
-    const long long r = q / D.n[2];
-    int J = int(r % D.n[1]);
-    int I = int(r / D.n[1]);
-    const int II[3] = {I, J, K};
-    const long long go = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
-    for (int a = 0; a < 3; ++a) {
-        double C = 0.0;
-        if (a < D.ndim && II[a] < D.n[a] - 1) {
-            const double R = 0.5 * (rho[go] + rho[go + D.s[a]]);
-            C = 1.0 / R / D.d[a] / D.d[a];
+// (C = (1/d^2) / R: one FP64 division instead of three; within an ulp or two of the
+// reference's value.)
+template <int DIM>
+__global__ void k_outer_coef(const double *__restrict__ rho, double *__restrict__ oc, Outer O) {
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
+        const int II[3] = {I, J, K};
+        for (int a = 0; a < 3; ++a) {
+            double C = 0.0;
+            if (a < DIM && II[a] < O.nint[a] - 1) {
+                const double R = 0.5 * (rho[go] + rho[go + O.D.s[a]]);
+                C = O.id2[a] / R;
+            }
+            oc[a * O.n + co] = C;
         }
-        oc[a * n + q] = C;
-    }
+    });
 }
 
-__device__ __forceinline__ void split_int(long long q, const Outer &O, int &I, int &J, int &K) {
-    K = int(q % O.nint[2]);
-    const long long r = q / O.nint[2];
-    J = int(r % O.nint[1]);
-    I = int(r / O.nint[1]);
+// diagonal: sum of the cell's (up to six) face coefficients
+template <int DIM>
+__global__ void k_outer_diag(double *__restrict__ oc, Outer O) {
+    for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
+        const int II[3] = {I, J, K};
+        double dsum = 0.0;
+        for (int a = 0; a < DIM; ++a) {
+            if (II[a] > 0) dsum += oc[a * O.n + co - O.cs[a]];
+            dsum += oc[a * O.n + co];
+        }
+        oc[3 * O.n + co] = dsum;
+    });
 }
 
 // sum of rhs over interior cells (for the Neumann projection of the right-hand side)
-__global__ void k_rhs_sum(const double *__restrict__ rhs, Outer O, long long n, RedSlot slot, double *out) {
+template <int DIM>
+__global__ void k_rhs_sum(const double *__restrict__ rhs, Outer O, RedSlot slot, double *out) {
     double v[1] = {0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        v[0] += rhs[O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K))];
-    }
+    for_cells<DIM>(O, [&](int, int, int, long long go, long long) { v[0] += rhs[go]; });
     double *o[1] = {out};
     grid_sum<1>(v, slot, o);
 }
 
 // r = g - L p, g = -(rhs - mean); ||g||^2, ||r||^2; level-0 V-cycle input b0 = r.
-template <class T>
-__global__ void k_init(const double *__restrict__ rhs, double *__restrict__ p, const double *__restrict__ rho,
-                       Outer O, long long n, int use_guess, double *__restrict__ r, T *__restrict__ b0, Level<T> L0,
-                       RedSlot slot, PcgScalars *st) {
-    const double mean = O.dirichlet ? 0.0 : st->mean / double(n);
+template <int DIM, class T>
+__global__ void k_init(const double *__restrict__ rhs, double *__restrict__ p, Outer O, int use_guess,
+                       double *__restrict__ r, Level<T> L0, RedSlot slot, PcgScalars *st) {
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
     double v[2] = {0.0, 0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
         const double g = -(rhs[go] - mean);
         double rv = g;
-        if (use_guess) rv -= apply_L<true>(p, rho, O, I, J, K);
+        if (use_guess) rv = O.density ? minus_L<DIM, true>(g, p, O, I, J, K, go, co) : g - apply_L<DIM, true>(p, O, I, J, K, go, co);
         else p[go] = 0.0;
-        r[q] = rv;
-        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
-        b0[P0] = T(rv);
+        r[co] = rv;
+        L0.b[p0_of<DIM>(L0, I, J, K)] = T(rv);
         v[0] += g * g;
         v[1] += rv * rv;
-    }
+    });
     double *o[2] = {&st->bb, &st->rr};
     grid_sum<2>(v, slot, o);
 }
 
 // rz = <r, z>, r_zold = <r, z_old> (flexible CG)
-template <class T>
+template <int DIM, class T>
 __global__ void k_dot_rz(const double *__restrict__ r, const T *__restrict__ z, const T *__restrict__ zold, Outer O,
-                         Level<T> L0, long long n, RedSlot slot, PcgScalars *st) {
+                         Level<T> L0, RedSlot slot, PcgScalars *st) {
     if (st->done) return;
     double v[2] = {0.0, 0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
-        v[0] += r[q] * double(z[P0]);
-        v[1] += r[q] * double(zold[P0]);
-    }
+    for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
+        const long long P0 = p0_of<DIM>(L0, I, J, K);
+        v[0] += r[co] * double(z[P0]);
+        v[1] += r[co] * double(zold[P0]);
+    });
     double *o[2] = {&st->rz, &st->r_zold};
     grid_sum<2>(v, slot, o);
 }
 
-// d = z + beta d (beta = (rz - r.zold) / rz_prev; 0 on the first iteration), z_old = z,
-// then q = L d and <d, q>.  Two passes: d must be complete before L d reads neighbours.
-template <class T>
+// d = z + beta d (beta = (rz - r.zold) / rz_prev; 0 on the first iteration), z_old = z.
+// L d is a separate pass: d must be complete before it reads neighbours.
+template <int DIM, class T>
 __global__ void k_update_d(const T *__restrict__ z, T *__restrict__ zold, double *__restrict__ d, Outer O,
-                           Level<T> L0, long long n, const PcgScalars *st) {
+                           Level<T> L0, const PcgScalars *st) {
     if (st->done) return;
     const double beta = st->it == 0 ? 0.0 : (st->rz - st->r_zold) / st->rz_prev;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
+    for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
+        const long long P0 = p0_of<DIM>(L0, I, J, K);
         const T zz = z[P0];
-        d[q] = double(zz) + beta * d[q];
+        d[co] = double(zz) + beta * d[co];
         zold[P0] = zz;
-    }
+    });
 }
 
-__global__ void k_apply_dq(const double *__restrict__ d, double *__restrict__ qv, const double *__restrict__ rho,
-                           Outer O, long long n, RedSlot slot, PcgScalars *st) {
+// q = L d and <d, q>
+template <int DIM>
+__global__ void k_apply_dq(const double *__restrict__ d, double *__restrict__ qv, Outer O, RedSlot slot,
+                           PcgScalars *st) {
     if (st->done) return;
     double v[1] = {0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const double lq = apply_L<false>(d, rho, O, I, J, K);
-        qv[q] = lq;
-        v[0] += d[q] * lq;
-    }
+    for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
+        const double lq = apply_L<DIM, false>(d, O, I, J, K, co, co);
+        qv[co] = lq;
+        v[0] += d[co] * lq;
+    });
     double *o[1] = {&st->dq};
     grid_sum<1>(v, slot, o);
 }
 
 // p += alpha d, r -= alpha q, ||r||^2, b0 = r
-template <class T>
+template <int DIM, class T>
 __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const double *__restrict__ d,
-                       const double *__restrict__ qv, T *__restrict__ b0, Outer O, Level<T> L0, long long n,
-                       RedSlot slot, PcgScalars *st) {
+                       const double *__restrict__ qv, Outer O, Level<T> L0, RedSlot slot, PcgScalars *st) {
     if (st->done) return;
     const double alpha = st->rz / st->dq;
     double v[1] = {0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
-        p[go] += alpha * d[q];
-        const double rv = r[q] - alpha * qv[q];
-        r[q] = rv;
-        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
-        b0[P0] = T(rv);
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
+        p[go] += alpha * d[co];
+        const double rv = r[co] - alpha * qv[co];
+        r[co] = rv;
+        L0.b[p0_of<DIM>(L0, I, J, K)] = T(rv);
         v[0] += rv * rv;
-    }
+    });
     double *o[1] = {&st->rr};
     grid_sum<1>(v, slot, o);
 }
@@ -275,46 +300,38 @@ __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const dou
 // Residual replacement: once the recursively updated residual meets the tolerance, replace it
 // by the true residual g - L p (the recursion drifts by round-off), so that convergence is
 // declared on the true residual.
-template <class T>
-__global__ void k_replace(const double *__restrict__ rhs, const double *__restrict__ p, const double *__restrict__ rho,
-                          Outer O, long long n, double *__restrict__ r, T *__restrict__ b0, Level<T> L0, double tol,
-                          RedSlot slot, PcgScalars *st) {
+template <int DIM, class T>
+__global__ void k_replace(const double *__restrict__ rhs, const double *__restrict__ p, Outer O,
+                          double *__restrict__ r, Level<T> L0, double tol, RedSlot slot, PcgScalars *st) {
     if (st->done || !(st->rr <= tol * tol * st->bb)) return;
-    const double mean = O.dirichlet ? 0.0 : st->mean / double(n);
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
     double v[1] = {0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
-        const double rv = -(rhs[go] - mean) - apply_L<true>(p, rho, O, I, J, K);
-        r[q] = rv;
-        const long long P0 = (I + 1) * L0.s[0] + (J + 1) * L0.s[1] + (O.D.ndim == 3 ? K + 1 : 0);
-        b0[P0] = T(rv);
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
+        const double g = -(rhs[go] - mean);
+        const double rv = O.density ? minus_L<DIM, true>(g, p, O, I, J, K, go, co) : g - apply_L<DIM, true>(p, O, I, J, K, go, co);
+        r[co] = rv;
+        L0.b[p0_of<DIM>(L0, I, J, K)] = T(rv);
         v[0] += rv * rv;
-    }
+    });
     double *o[1] = {&st->rr};
     grid_sum<1>(v, slot, o);
 }
 
-// Convergence test; in graph mode it also drives the conditional while-node.  Besides the
-// tolerance and the iteration cap, the iteration stops once the residual has not improved
-// for three consecutive iterations: it has reached the attainable accuracy of FP64 for
-// this operator, and conjugate gradients would only accumulate round-off from there.
-__global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
-                        int use_handle) {
-    if (advance) {
-        if (st->done) {
+// Convergence test of the FP64 conjugate-gradient loop; in graph mode it also drives the
+// conditional while-node.  Besides the tolerance and the iteration cap, the iteration stops
+// once the residual has not improved for three consecutive iterations: it has reached the
+// attainable accuracy of FP64 for this operator, and conjugate gradients would only
+// accumulate round-off from there.
+__device__ __forceinline__ void set_cond(unsigned long long handle, int use_handle, int go_on) {
 #if defined(__CUDA_ARCH__)
-            if (use_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, 0u);
+    if (use_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, go_on ? 1u : 0u);
 #endif
-            return;
-        }
-        st->rz_prev = st->rz;
-        st->it += 1;
-    }
+}
+
+__device__ __forceinline__ void outer_progress(PcgScalars *st, double tol, int max_iter, int first) {
     const double rel = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0;
     st->relres = rel;
-    if (!advance || rel < st->best) {
+    if (first || rel < st->best) {
         st->best = rel;
         st->since_best = 0;
     } else {
@@ -322,46 +339,54 @@ __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, u
     }
     if (!(rel == rel) || isinf(rel)) st->diverged = 1;
     st->done = (rel <= tol || st->it >= max_iter || st->diverged || st->since_best >= 3) ? 1 : 0;
-#if defined(__CUDA_ARCH__)
-    if (use_handle) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, st->done ? 0u : 1u);
-#endif
+}
+
+__global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
+                        int use_handle) {
+    if (advance) {
+        if (st->done) {
+            set_cond(handle, use_handle, 0);
+            return;
+        }
+        st->rz_prev = st->rz;
+        st->it += 1;
+    }
+    outer_progress(st, tol, max_iter, !advance);
+    st->rr_in0 = st->rr;
+    st->in_target = fmax(st->in_tol, 0.25 * tol / fmax(st->relres, 1e-300));
+    set_cond(handle, use_handle, !st->done);
 }
 
 // final: mean removal (Neumann) and the true relative residual
-__global__ void k_p_sum(const double *__restrict__ p, Outer O, long long n, RedSlot slot, double *out) {
+template <int DIM>
+__global__ void k_p_sum(const double *__restrict__ p, Outer O, RedSlot slot, double *out) {
     double v[1] = {0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        v[0] += p[O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K))];
-    }
+    for_cells<DIM>(O, [&](int, int, int, long long go, long long) { v[0] += p[go]; });
     double *o[1] = {out};
     grid_sum<1>(v, slot, o);
 }
 
-__global__ void k_p_shift(double *__restrict__ p, Outer O, long long n, const double *sum) {
-    const double m = *sum / double(n);
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        p[O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K))] -= m;
-    }
+template <int DIM>
+__global__ void k_p_shift(double *__restrict__ p, Outer O, const double *sum) {
+    const double m = *sum / double(O.n);
+    for_cells<DIM>(O, [&](int, int, int, long long go, long long) { p[go] -= m; });
 }
 
-__global__ void k_true_res(const double *__restrict__ rhs, const double *__restrict__ p, const double *__restrict__ rho,
-                           Outer O, long long n, RedSlot slot, PcgScalars *st) {
-    const double mean = O.dirichlet ? 0.0 : st->mean / double(n);
+template <int DIM>
+__global__ void k_true_res(const double *__restrict__ rhs, const double *__restrict__ p, Outer O, RedSlot slot,
+                           PcgScalars *st) {
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
     double v[1] = {0.0};
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        int I, J, K;
-        split_int(q, O, I, J, K);
-        const long long go = O.D.at(O.D.ix(0, I), O.D.ix(1, J), O.D.ix(2, K));
-        const double rv = -(rhs[go] - mean) - apply_L<true>(p, rho, O, I, J, K);
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
+        const double g = -(rhs[go] - mean);
+        const double rv = O.density ? minus_L<DIM, true>(g, p, O, I, J, K, go, co) : g - apply_L<DIM, true>(p, O, I, J, K, go, co);
         v[0] += rv * rv;
-    }
+    });
     double *o[1] = {&st->rr};
     grid_sum<1>(v, slot, o);
 }
+
+__global__ void k_set_inner(PcgScalars *st, double in_tol) { st->in_tol = in_tol; }
 
 __global__ void k_relres(PcgScalars *st) { st->relres = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0; }
 
@@ -454,6 +479,145 @@ __device__ __forceinline__ T residual_at(const Level<T> &L, const T *__restrict_
           C[3] * (xc - L.x[P + L.s[1]]);
     if (DIM == 3) s += C[4] * (xc - L.x[P - 1]) + C[5] * (xc - L.x[P + 1]);
     return L.b[P] - s;
+}
+
+// ---------------------------------------------------------------- fused red-black sweep (3D)
+// One full Gauss-Seidel sweep (first colour, then second) as a single pass over the level,
+// out of place: xn = sweep(xo).  A block owns a tile of SW_TJ x SW_TK columns (j, k) and
+// marches along i through a chunk of planes.  At step i it updates the first colour of
+// plane i from xo, then the second colour of plane i-1 from first-colour values that are
+// already on chip (registers for the block's own column pair, shared memory for the
+// neighbours).  A ring of one row / one column pair around the tile recomputes the
+// neighbours' first-colour values instead of waiting for them, so blocks never depend on
+// one another, and xo is read only: the result does not depend on block scheduling.
+// Each pass reads xo, b and the coefficients once and writes xn once.
+constexpr int SW_TK = 64;                    // interior k per tile (32 column pairs)
+constexpr int SW_TJ = 16;                    // interior j rows per tile
+constexpr int SW_PAIRS = SW_TK / 2 + 2;      // with the ring
+constexpr int SW_ROWS = SW_TJ + 2;
+constexpr int SW_THREADS = SW_PAIRS * SW_ROWS;   // 612
+
+// Per-level constants of the sweep: MODE 1 w[a] = 2 / d_a^2 (face coefficient
+// w / (rho_c + rho_nb)); MODE 2 w[a] = 1 / d_a^2 and dinv = 1 / (2 sum w).
+template <class T>
+struct SweepCoef {
+    T w[3];
+    T dinv;
+};
+
+__device__ __forceinline__ float prcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double prcp(double x) { return 1.0 / x; }
+
+// Gauss-Seidel value (b + sum_f C_f x_f) / sum_f C_f of the cell at padded offset `off`.
+// nb: neighbour values (-i, +i, -j, +j, -k, +k); rn (MODE 1): densities of the cell and of the
+// same six neighbours.
+template <class T, int MODE>
+__device__ __forceinline__ T gs_update(const Level<T> &L, int off, int s0, int s1, T b, const T nb[6], const T rn[7],
+                                       const SweepCoef<T> &cf) {
+    if constexpr (MODE == 1) {
+        const T C0 = cf.w[0] * prcp(rn[0] + rn[1]), C1 = cf.w[0] * prcp(rn[0] + rn[2]);
+        const T C2 = cf.w[1] * prcp(rn[0] + rn[3]), C3 = cf.w[1] * prcp(rn[0] + rn[4]);
+        const T C4 = cf.w[2] * prcp(rn[0] + rn[5]), C5 = cf.w[2] * prcp(rn[0] + rn[6]);
+        const T sx = C0 * nb[0] + C1 * nb[1] + C2 * nb[2] + C3 * nb[3] + C4 * nb[4] + C5 * nb[5];
+        return (b + sx) * prcp(C0 + C1 + C2 + C3 + C4 + C5);
+    } else if constexpr (MODE == 0) {
+        const T sx = L.cx[off - s0] * nb[0] + L.cx[off] * nb[1] + L.cy[off - s1] * nb[2] + L.cy[off] * nb[3] +
+                     L.cz[off - 1] * nb[4] + L.cz[off] * nb[5];
+        return (b + sx) * L.idg[off];
+    } else {
+        const T sx = cf.w[0] * (nb[0] + nb[1]) + cf.w[1] * (nb[2] + nb[3]) + cf.w[2] * (nb[4] + nb[5]);
+        return (b + sx) * cf.dinv;
+    }
+}
+
+// c0: 0 = red ((I+J+K) even) first, 1 = black first.  zero: xo is identically zero (not read).
+// Offsets are 32-bit (the caller checks that the padded level has fewer than 2^31 cells).
+template <class T, int MODE>
+__global__ void __launch_bounds__(SW_THREADS, 2) k_sweep3(Level<T> L, const T *__restrict__ xo, T *__restrict__ xn,
+                                                          const T *__restrict__ rho, SweepCoef<T> cf, int c0,
+                                                          int zero, int ci) {
+    __shared__ T first[2][SW_ROWS][SW_PAIRS];
+    const int tid = threadIdx.x;
+    const int row = tid / SW_PAIRS, pr = tid - row * SW_PAIRS;
+    const int tiles_k = (L.n[2] + SW_TK - 1) / SW_TK;
+    const int tk = blockIdx.x % tiles_k, tj = blockIdx.x / tiles_k;
+    const int i0 = blockIdx.y * ci;
+    const int i1 = min(i0 + ci, L.n[0]);
+    const int j = tj * SW_TJ + row - 1;
+    const int kbase = tk * SW_TK + 2 * (pr - 1);
+    const bool inner = row >= 1 && row <= SW_TJ && pr >= 1 && pr <= SW_PAIRS - 2;
+    const bool jin = j >= 0 && j < L.n[1];
+    const int s0 = int(L.s[0]), s1 = int(L.s[1]);
+    const int col = (j + 1) * s1 + kbase + 1;   // padded offset of (i = -1, j, kbase)
+    const T *__restrict__ b = L.b;
+    T f1 = 0, f2 = 0;   // this pair's first-colour values at planes i-1 and i-2
+    for (int i = i0 - 1; i <= i1; ++i) {
+        const int par = (i + j + c0) & 1;
+        const int k = kbase + par;   // first colour of plane i and second colour of plane i-1
+        const bool kin = jin && k >= 0 && k < L.n[2];
+        const int off = (i + 1) * s0 + col + par;
+        const bool fvalid = kin && i >= 0 && i < L.n[0];
+        T fi = 0, rc = 0, rim = 0;   // density at (i, j, k) and (i-1, j, k), MODE 1
+        if (fvalid) {
+            T nb[6] = {0, 0, 0, 0, 0, 0};
+            if (!zero) {
+                nb[0] = xo[off - s0], nb[1] = xo[off + s0], nb[2] = xo[off - s1], nb[3] = xo[off + s1];
+                nb[4] = xo[off - 1], nb[5] = xo[off + 1];
+            }
+            T rn[7] = {0, 0, 0, 0, 0, 0, 0};
+            if (MODE == 1) {
+                rn[0] = rho[off], rn[1] = rho[off - s0], rn[2] = rho[off + s0], rn[3] = rho[off - s1];
+                rn[4] = rho[off + s1], rn[5] = rho[off - 1], rn[6] = rho[off + 1];
+                rc = rn[0], rim = rn[1];
+            }
+            fi = gs_update<T, MODE>(L, off, s0, s1, b[off], nb, rn, cf);
+            if (inner && i >= i0 && i < i1) xn[off] = fi;
+        }
+        first[i & 1][row][pr] = fi;
+        const int ib = i - 1;
+        if (inner && kin && ib >= i0 && ib < i1) {
+            const int q = ib & 1;
+            T nb[6];
+            nb[0] = f2;   // plane i-2, same column
+            nb[1] = fi;   // plane i
+            nb[2] = first[q][row - 1][pr];
+            nb[3] = first[q][row + 1][pr];
+            if (par == 0) {
+                nb[4] = first[q][row][pr - 1];
+                nb[5] = f1;
+            } else {
+                nb[4] = f1;
+                nb[5] = first[q][row][pr + 1];
+            }
+            const int ob = off - s0;
+            T rn[7] = {0, 0, 0, 0, 0, 0, 0};
+            if (MODE == 1) {
+                if (!fvalid) rc = rho[off], rim = rho[ob];   // plane i is the halo (i == n0)
+                rn[0] = rim, rn[1] = rho[ob - s0], rn[2] = rc, rn[3] = rho[ob - s1];
+                rn[4] = rho[ob + s1], rn[5] = rho[ob - 1], rn[6] = rho[ob + 1];
+            }
+            xn[ob] = gs_update<T, MODE>(L, ob, s0, s1, b[ob], nb, rn, cf);
+        }
+        f2 = f1;
+        f1 = fi;
+        __syncthreads();
+    }
+}
+
+// Planes per block for k_sweep3: balances whole waves of blocks against the two planes
+// every chunk recomputes.
+inline int sweep_chunk(const int n[3]) {
+    const long long tiles = (long long)((n[2] + SW_TK - 1) / SW_TK) * ((n[1] + SW_TJ - 1) / SW_TJ);
+    const long long slots = 2LL * NUM_SMS;
+    long long best = -1;
+    int best_ci = n[0];
+    for (int nch = 1; nch <= n[0]; ++nch) {
+        const int ci = (n[0] + nch - 1) / nch;
+        const long long ctas = tiles * ((n[0] + ci - 1) / ci);
+        const long long cost = ((ctas + slots - 1) / slots) * (ci + 2);
+        if (best < 0 || cost < best) best = cost, best_ci = ci;
+    }
+    return best_ci;
 }
 
 // coarse b = mean of the fine residuals of its r^d children; coarse x = 0
@@ -746,6 +910,220 @@ __global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n
     }
 }
 
+// ---------------------------------------------------------------- FP32 inner solve (iterative refinement)
+// FP32 mode: the FP64 loop is iterative refinement.  r64 = g - L p in FP64; an FP32
+// conjugate-gradient solve of L e = r64, preconditioned by the FP32 V-cycle, runs until its
+// residual has dropped by inner_tol (or inner_max iterations); then p += e in FP64 and the
+// FP64 residual is formed again.  The inner vectors live in the padded level-0 layout: r in
+// L0.b (the V-cycle input), z in L0.x (its output), d, q and e beside them.  Only the
+// residual and the accumulation of p are FP64.  The symmetric V-cycle (red-black pre-sweeps
+// mirrored by black-red post-sweeps, restriction the transpose of prolongation) lets the
+// inner loop use the plain conjugate-gradient recurrence.
+
+// Interior cells of the padded level 0, IN_RU elements per thread: blocks of IN_BX x IN_BY
+// threads take IN_BY rows at a time (grid-stride over rows), thread x takes elements x,
+// x + IN_BX, ... of its row, so each thread has several independent loads in flight.
+constexpr int IN_BX = 64, IN_BY = TPB / IN_BX, IN_RU = 4;
+
+struct RowIt {
+    long long base;   // padded offset of the row's element k = -1
+    int fs;           // stride along the row
+    int nf;           // row length
+};
+
+template <int DIM, class F>
+__device__ __forceinline__ void for_level0(const Level<float> &L, F &&f) {
+    const int nf = L.n[DIM - 1];
+    const int r1 = DIM == 3 ? L.n[1] : 1;
+    const long long nrows = (long long)L.n[0] * r1;
+    const int fs = DIM == 3 ? 1 : int(L.s[1]);
+    for (long long row = (long long)blockIdx.x * IN_BY + threadIdx.y; row < nrows; row += (long long)gridDim.x * IN_BY) {
+        const int I = int(row / r1);
+        const int J = DIM == 3 ? int(row - (long long)I * r1) : 0;
+        const long long base = (long long)(I + 1) * L.s[0] + (DIM == 3 ? (long long)(J + 1) * L.s[1] : 0) + fs;
+        for (int k0 = threadIdx.x; k0 < nf; k0 += IN_BX * IN_RU) f(base, fs, nf, k0);
+    }
+}
+
+inline int inner_blocks(const Level<float> &L, int ndim) {
+    const long long rows = ndim == 3 ? (long long)L.n[0] * L.n[1] : L.n[0];
+    long long b = (rows + IN_BY - 1) / IN_BY;
+    if (b > RED_MAX_BLOCKS) b = RED_MAX_BLOCKS;
+    return int(b < 1 ? 1 : b);
+}
+
+// rz = <r, z>
+template <int DIM>
+__global__ void __launch_bounds__(TPB) k_in_dot(Level<float> L, RedSlot slot, PcgScalars *st) {
+    if (st->done) return;
+    float acc = 0.0f;   // per-thread partial in FP32 (FP64 arithmetic is 1/64 rate here)
+    for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
+        float r[IN_RU], z[IN_RU];
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) {
+            const int k = k0 + u * IN_BX;
+            const long long P = base + (long long)k * fs;
+            r[u] = k < nf ? L.b[P] : 0.0f;
+            z[u] = k < nf ? L.x[P] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) acc += r[u] * z[u];
+    });
+    double v[1] = {double(acc)};
+    double *o[1] = {&st->rz};
+    grid_sum<1>(v, slot, o);
+}
+
+// d = z + beta d, beta = rz / rz_prev (0 on the first inner iteration)
+template <int DIM>
+__global__ void __launch_bounds__(TPB) k_in_update_d(Level<float> L, float *__restrict__ d, const PcgScalars *st) {
+    if (st->done) return;
+    const float beta = st->in_it == 0 ? 0.0f : float(st->rz / st->rz_prev);
+    for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
+        float z[IN_RU], dv[IN_RU];
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) {
+            const int k = k0 + u * IN_BX;
+            const long long P = base + (long long)k * fs;
+            z[u] = k < nf ? L.x[P] : 0.0f;
+            dv[u] = k < nf ? d[P] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) {
+            const int k = k0 + u * IN_BX;
+            if (k < nf) d[base + (long long)k * fs] = z[u] + beta * dv[u];
+        }
+    });
+}
+
+// q = L d (the level-0 operator of the V-cycle) and <d, q>
+template <int DIM, int MODE>
+__global__ void __launch_bounds__(TPB) k_in_apply(Level<float> L, const float *__restrict__ rho, Id2<float> id2,
+                                                  const float *__restrict__ d, float *__restrict__ q, RedSlot slot,
+                                                  PcgScalars *st) {
+    if (st->done) return;
+    float acc = 0.0f;
+    const int s0 = int(L.s[0]), s1 = int(L.s[1]);   // padded level 0 has fewer than 2^31 cells
+    const float w0 = 2.0f * id2.v[0], w1 = 2.0f * id2.v[1], w2 = 2.0f * id2.v[2];
+    for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) {
+            const int k = k0 + u * IN_BX;
+            if (k >= nf) continue;
+            const int P = int(base) + k * fs;
+            const float dc = d[P];
+            float sq;
+            if (MODE == 1) {
+                const float rc = rho[P];
+                sq = w0 * prcp(rc + rho[P - s0]) * (dc - d[P - s0]) + w0 * prcp(rc + rho[P + s0]) * (dc - d[P + s0]) +
+                     w1 * prcp(rc + rho[P - s1]) * (dc - d[P - s1]) + w1 * prcp(rc + rho[P + s1]) * (dc - d[P + s1]);
+                if (DIM == 3) sq += w2 * prcp(rc + rho[P - 1]) * (dc - d[P - 1]) + w2 * prcp(rc + rho[P + 1]) * (dc - d[P + 1]);
+            } else {
+                sq = id2.v[0] * ((dc - d[P - s0]) + (dc - d[P + s0])) + id2.v[1] * ((dc - d[P - s1]) + (dc - d[P + s1]));
+                if (DIM == 3) sq += id2.v[2] * ((dc - d[P - 1]) + (dc - d[P + 1]));
+            }
+            q[P] = sq;
+            acc += dc * sq;
+        }
+    });
+    double v[1] = {double(acc)};
+    double *o[1] = {&st->dq};
+    grid_sum<1>(v, slot, o);
+}
+
+// e += alpha d, r -= alpha q, ||r||^2
+template <int DIM>
+__global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, const float *__restrict__ d,
+                                                 const float *__restrict__ q, float *__restrict__ e, RedSlot slot,
+                                                 PcgScalars *st) {
+    if (st->done) return;
+    const float alpha = float(st->rz / st->dq);
+    float acc = 0.0f;
+    for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
+        float ev[IN_RU], dv[IN_RU], rv[IN_RU], qv[IN_RU];
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) {
+            const int k = k0 + u * IN_BX;
+            const long long P = base + (long long)k * fs;
+            const bool ok = k < nf;
+            ev[u] = ok ? e[P] : 0.0f;
+            dv[u] = ok ? d[P] : 0.0f;
+            rv[u] = ok ? L.b[P] : 0.0f;
+            qv[u] = ok ? q[P] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < IN_RU; ++u) {
+            const int k = k0 + u * IN_BX;
+            if (k >= nf) continue;
+            const long long P = base + (long long)k * fs;
+            e[P] = ev[u] + alpha * dv[u];
+            const float r = rv[u] - alpha * qv[u];
+            L.b[P] = r;
+            acc += r * r;
+        }
+    });
+    double v[1] = {double(acc)};
+    double *o[1] = {&st->rr_in};
+    grid_sum<1>(v, slot, o);
+}
+
+// inner progress; marks the refinement step as due
+__global__ void k_in_check(PcgScalars *st, int inner_max, int max_iter) {
+    if (st->done) return;
+    st->rz_prev = st->rz;
+    st->it += 1;
+    st->in_it += 1;
+    const double rel = st->rr_in0 > 0.0 ? sqrt(st->rr_in / st->rr_in0) : 0.0;
+    const bool bad = !(rel == rel) || isinf(rel);
+    st->pending = (bad || rel <= st->in_target || st->in_it >= inner_max || st->it >= max_iter) ? 1 : 0;
+}
+
+// refinement, part 1: p += e
+template <int DIM>
+__global__ void k_out_add(double *__restrict__ p, const float *__restrict__ e, Outer O, Level<float> L0,
+                          const PcgScalars *st) {
+    if (st->done || !st->pending) return;
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long) { p[go] += double(e[p0_of<DIM>(L0, I, J, K)]); });
+}
+
+// refinement, part 2: r64 = g - L p in FP64, ||r64||^2; the inner solve restarts from
+// r = r64 (rounded to FP32), e = 0
+template <int DIM>
+__global__ void k_out_res(const double *__restrict__ rhs, const double *__restrict__ p, Outer O, Level<float> L0,
+                          float *__restrict__ e, RedSlot slot, PcgScalars *st) {
+    if (st->done || !st->pending) return;
+    const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
+    double v[1] = {0.0};
+    for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
+        const double g = -(rhs[go] - mean);
+        const double rv = O.density ? minus_L<DIM, true>(g, p, O, I, J, K, go, co) : g - apply_L<DIM, true>(p, O, I, J, K, go, co);
+        const long long P0 = p0_of<DIM>(L0, I, J, K);
+        L0.b[P0] = float(rv);
+        e[P0] = 0.0f;
+        v[0] += rv * rv;
+    });
+    double *o[1] = {&st->rr};
+    grid_sum<1>(v, slot, o);
+}
+
+// refinement, part 3: convergence on the FP64 residual; drives the conditional while-node
+__global__ void k_out_check(PcgScalars *st, double tol, int max_iter, unsigned long long handle, int use_handle) {
+    if (st->done) {
+        set_cond(handle, use_handle, 0);
+        return;
+    }
+    if (st->pending) {
+        outer_progress(st, tol, max_iter, 0);
+        st->in_it = 0;
+        st->rr_in0 = st->rr;
+        st->pending = 0;
+    }
+    // the next inner solve needs to reduce its residual only by what is left to reach tol
+    // (with a factor 4 of margin), but at least by the inner tolerance
+    st->in_target = fmax(st->in_tol, 0.25 * tol / fmax(st->relres, 1e-300));
+    set_cond(handle, use_handle, !st->done);
+}
+
 // The coarse end of the V-cycle in one thread block: levels lc .. nlev-1 (each at most a few
 // thousand cells) are smoothed, restricted, solved and prolongated with __syncthreads()
 // between phases instead of one kernel launch per phase.  Levels >= 1 carry stored
@@ -866,9 +1244,10 @@ int Poisson::alloc_levels() {
         L.cells = (long long)L.P[0] * L.P[1] * L.P[2];
         L.ratio = ratio[l];
         const size_t bytes = size_t(L.cells) * sizeof(T);
-        SCIHPC_CUDA(cudaMalloc(&L.x, bytes));
+        SCIHPC_CUDA(cudaMalloc(&L.x, 2 * bytes));
         SCIHPC_CUDA(cudaMalloc(&L.b, bytes));
-        SCIHPC_CUDA(cudaMemset(L.x, 0, bytes));
+        SCIHPC_CUDA(cudaMemset(L.x, 0, 2 * bytes));
+        L.x2 = L.x + L.cells;
         SCIHPC_CUDA(cudaMemset(L.b, 0, bytes));
         if (l > 0 || sizeof(T) == 8) {
             SCIHPC_CUDA(cudaMalloc(&L.cx, 4 * bytes));
@@ -878,6 +1257,10 @@ int Poisson::alloc_levels() {
             L.idg = L.cz + L.cells;
         }
         for (int a = 0; a < 3; ++a) dd[a] *= ratio[l];
+    }
+    if (Ls[0].cells >= (1LL << 31)) {
+        set_last_error("pressure grid too large: the padded finest level must have fewer than 2^31 cells");
+        return SCIHPC_ERR_UNSUPPORTED;
     }
     // coarsest dense solve
     const Level<T> &C = Ls[nlev - 1];
@@ -890,6 +1273,12 @@ int Poisson::alloc_levels() {
     const size_t zbytes = size_t(Ls[0].cells) * sizeof(T);
     SCIHPC_CUDA(cudaMalloc(&zold, zbytes));
     SCIHPC_CUDA(cudaMemset(zold, 0, zbytes));
+    if (sizeof(T) == 4) {
+        SCIHPC_CUDA(cudaMalloc(&d32, 3 * zbytes));
+        SCIHPC_CUDA(cudaMemset(d32, 0, 3 * zbytes));
+        q32 = d32 + Ls[0].cells;
+        e32 = q32 + Ls[0].cells;
+    }
     SCIHPC_CUDA(cudaMalloc(&rho_pad, zbytes));
     return SCIHPC_OK;
 }
@@ -909,8 +1298,8 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     q = dvec + n;
     SCIHPC_CUDA(cudaMemset(r, 0, 3 * n * sizeof(double)));
     if (density) {
-        SCIHPC_CUDA(cudaMalloc(&oc, 3 * n * sizeof(double)));
-        SCIHPC_CUDA(cudaMemset(oc, 0, 3 * n * sizeof(double)));
+        SCIHPC_CUDA(cudaMalloc(&oc, 4 * n * sizeof(double)));
+        SCIHPC_CUDA(cudaMemset(oc, 0, 4 * n * sizeof(double)));
     }
     SCIHPC_CUDA(cudaMalloc(&partial, 2 * RED_MAX_BLOCKS * sizeof(double) + 64));
     SCIHPC_CUDA(cudaMemset(partial, 0, 2 * RED_MAX_BLOCKS * sizeof(double) + 64));
@@ -942,6 +1331,7 @@ void Poisson::destroy() {
     rel(dev_state);
     rel(dense);
     rel(zold);
+    rel(d32);
     rel(rho_pad);
     rel(oc);
     oc = nullptr;
@@ -1023,9 +1413,36 @@ void Poisson::build_coarse(cudaStream_t s) {
     k_dense_pin_and_invert<<<1, 1024, 0, s>>>(M, W, ncoarse, neumann);
 }
 
+static Outer make_outer(const Dims &D, int density, int dirichlet, const double *oc) {
+    Outer O;
+    O.D = D;
+    O.oc = oc;
+    O.n = D.interior();
+    for (int a = 0; a < 3; ++a) {
+        O.nint[a] = D.n[a];
+        O.id2[a] = a < D.ndim ? 1.0 / D.d[a] / D.d[a] : 0.0;
+    }
+    O.cs[2] = 1;
+    O.cs[1] = D.n[2];
+    O.cs[0] = (long long)D.n[1] * D.n[2];
+    O.density = density;
+    O.dirichlet = dirichlet;
+    return O;
+}
+
 int Poisson::set_density(const double *rho, cudaStream_t s) {
     rho64 = rho;
-    if (density_) k_outer_coef<<<blocks_for(D.interior(), TPB), TPB, 0, s>>>(rho, oc, D, D.interior());
+    if (density_) {
+        const Outer O = make_outer(D, density_, bc_ == 1, oc);
+        const int nb = grid_blocks(D.interior());
+        if (D.ndim == 2) {
+            k_outer_coef<2><<<nb, TPB, 0, s>>>(rho, oc, O);
+            k_outer_diag<2><<<nb, TPB, 0, s>>>(oc, O);
+        } else {
+            k_outer_coef<3><<<nb, TPB, 0, s>>>(rho, oc, O);
+            k_outer_diag<3><<<nb, TPB, 0, s>>>(oc, O);
+        }
+    }
     if (fp32_) build_coarse<float>(s);
     else build_coarse<double>(s);
     SCIHPC_CUDA(cudaGetLastError());
@@ -1057,22 +1474,56 @@ void Poisson::vcycle(cudaStream_t s) {
             else k_smooth<T, 2, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
         }
     };
-    cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
-    // levels from lc on (each <= COARSE_CELLS cells) run inside one thread block
+    // levels from lc on (small enough for one block) run inside one thread block
     int lc = nlev - 1;
     for (int l = 1; l < nlev; ++l) {
-        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= COARSE_CELLS) {
+        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= (sizeof(T) == 4 ? COARSE_CELLS_FP32 : COARSE_CELLS_FP64)) {
             lc = l;
             break;
         }
     }
-    const bool fused = nlev <= 16;   // LevelPack capacity
-    if (lc < 1 || !fused) lc = nlev - 1 > 0 ? nlev - 1 : 0;
-    for (int l = 0; l < lc; ++l) {
-        for (int k = 0; k < nu; ++k) {
-            smooth(l, 0);
-            smooth(l, 1);
+    const bool packed = nlev <= 16;   // LevelPack capacity
+    if (lc < 1 || !packed) lc = nlev - 1 > 0 ? nlev - 1 : 0;
+    // 3D levels of at least FUSED_MIN_CELLS cells use the one-pass out-of-place sweep
+    auto fused = [&](int l) {
+        return D.ndim == 3 && (long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] >= FUSED_MIN_CELLS &&
+               Ls[l].cells < (1LL << 31);
+    };
+    auto sweep = [&](int l, const T *xo, T *xn, int c0, int zero) {
+        Level<T> &L = Ls[l];
+        const int ci = sweep_chunk(L.n);
+        const dim3 grid(unsigned(((L.n[2] + SW_TK - 1) / SW_TK) * ((L.n[1] + SW_TJ - 1) / SW_TJ)),
+                        unsigned((L.n[0] + ci - 1) / ci));
+        const int m = l == 0 ? mode0 : 0;
+        SweepCoef<T> cf{};
+        double dsum = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            cf.w[a] = T((m == 1 ? 2.0 : 1.0) / (D.d[a] * D.d[a]));
+            dsum += 2.0 / (D.d[a] * D.d[a]);
         }
+        cf.dinv = T(1.0 / dsum);
+        if (m == 0) k_sweep3<T, 0><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
+        else if (m == 2) k_sweep3<T, 2><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
+        else if constexpr (sizeof(T) == 4) k_sweep3<T, 1><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
+    };
+    // nu is even, so an even number of out-of-place sweeps leaves the iterate in x
+    auto smooth_level = [&](int l, int c0, bool from_zero) {
+        if (fused(l)) {
+            for (int k = 0; k < nu; ++k) {
+                T *src = (k & 1) ? Ls[l].x2 : Ls[l].x;
+                T *dst = (k & 1) ? Ls[l].x : Ls[l].x2;
+                sweep(l, src, dst, c0, (k == 0 && from_zero) ? 1 : 0);
+            }
+        } else {
+            for (int k = 0; k < nu; ++k) {
+                smooth(l, c0);
+                smooth(l, 1 - c0);
+            }
+        }
+    };
+    if (!fused(0)) cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
+    for (int l = 0; l < lc; ++l) {
+        smooth_level(l, 0, true);   // level 0 starts from zero; coarser levels are zeroed by restriction
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const long long nc = (long long)Cl.n[0] * Cl.n[1] * Cl.n[2];
         const unsigned nb = blocks_for(nc, TPB);
@@ -1087,7 +1538,7 @@ void Poisson::vcycle(cudaStream_t s) {
             else k_restrict<T, 2, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
         }
     }
-    if (fused && lc >= 1) {
+    if (packed && lc >= 1) {
         LevelPack<T> LP;
         for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
         if (D.ndim == 2) k_coarse_cycle<T, 2><<<1, 1024, 0, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear);
@@ -1102,79 +1553,89 @@ void Poisson::vcycle(cudaStream_t s) {
         const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
         if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
         else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
-        for (int k = 0; k < nu; ++k) {
-            smooth(l, 1);
-            smooth(l, 0);
-        }
+        smooth_level(l, 1, false);
     }
-}
-
-static Outer make_outer(const Dims &D, int density, int dirichlet, const double *oc) {
-    Outer O;
-    O.D = D;
-    O.oc = oc;
-    O.n = D.interior();
-    for (int a = 0; a < 3; ++a) {
-        O.nint[a] = D.n[a];
-        O.id2[a] = a < D.ndim ? 1.0 / D.d[a] / D.d[a] : 0.0;
-    }
-    O.cs[2] = 1;
-    O.cs[1] = D.n[2];
-    O.cs[0] = (long long)D.n[1] * D.n[2];
-    O.density = density;
-    O.dirichlet = dirichlet;
-    return O;
 }
 
 void Poisson::begin(const double *rhs, double *p, int use_guess, cudaStream_t s) {
-    rhs_ = rhs;
-    p_ = p;
-    const long long n = D.interior();
-    const Outer O = make_outer(D, density_, bc_ == 1, oc);
-    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
-    const int nb = grid_blocks(n);
-    cudaMemsetAsync(dev_state, 0, sizeof(PcgScalars), s);
-    if (bc_ == 0) k_rhs_sum<<<nb, TPB, 0, s>>>(rhs, O, n, slot, &dev_state->mean);
-    if (fp32_) k_init<float><<<nb, TPB, 0, s>>>(rhs, p, rho64, O, n, use_guess, r, Lf[0].b, Lf[0], slot, dev_state);
-    else k_init<double><<<nb, TPB, 0, s>>>(rhs, p, rho64, O, n, use_guess, r, Ld[0].b, Ld[0], slot, dev_state);
-    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 0, conditional, 0);
+    if (D.ndim == 2) begin_dim<2>(rhs, p, use_guess, s);
+    else begin_dim<3>(rhs, p, use_guess, s);
 }
 
 void Poisson::iterate(cudaStream_t s) {
-    const long long n = D.interior();
-    const Outer O = make_outer(D, density_, bc_ == 1, oc);
-    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
-    const int nb = grid_blocks(n);
-    if (fp32_) {
-        vcycle<float>(s);
-        k_dot_rz<float><<<nb, TPB, 0, s>>>(r, Lf[0].x, (const float *)zold, O, Lf[0], n, slot, dev_state);
-        k_update_d<float><<<nb, TPB, 0, s>>>(Lf[0].x, (float *)zold, dvec, O, Lf[0], n, dev_state);
-    } else {
-        vcycle<double>(s);
-        k_dot_rz<double><<<nb, TPB, 0, s>>>(r, Ld[0].x, (const double *)zold, O, Ld[0], n, slot, dev_state);
-        k_update_d<double><<<nb, TPB, 0, s>>>(Ld[0].x, (double *)zold, dvec, O, Ld[0], n, dev_state);
-    }
-    k_apply_dq<<<nb, TPB, 0, s>>>(dvec, q, rho64, O, n, slot, dev_state);
-    if (fp32_) {
-        k_axpy<float><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Lf[0].b, O, Lf[0], n, slot, dev_state);
-        k_replace<float><<<nb, TPB, 0, s>>>(rhs_, p_, rho64, O, n, r, Lf[0].b, Lf[0], rel_tol, slot, dev_state);
-    } else {
-        k_axpy<double><<<nb, TPB, 0, s>>>(p_, r, dvec, q, Ld[0].b, O, Ld[0], n, slot, dev_state);
-        k_replace<double><<<nb, TPB, 0, s>>>(rhs_, p_, rho64, O, n, r, Ld[0].b, Ld[0], rel_tol, slot, dev_state);
-    }
-    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 1, conditional, use_conditional ? 1 : 0);
+    if (D.ndim == 2) iterate_dim<2>(s);
+    else iterate_dim<3>(s);
 }
 
 void Poisson::finish(double *p, cudaStream_t s) {
-    const long long n = D.interior();
+    if (D.ndim == 2) finish_dim<2>(p, s);
+    else finish_dim<3>(p, s);
+}
+
+template <int DIM>
+void Poisson::begin_dim(const double *rhs, double *p, int use_guess, cudaStream_t s) {
+    rhs_ = rhs;
+    p_ = p;
     const Outer O = make_outer(D, density_, bc_ == 1, oc);
     RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
-    const int nb = grid_blocks(n);
-    if (bc_ == 0) {
-        k_p_sum<<<nb, TPB, 0, s>>>(p, O, n, slot, &dev_state->dq);
-        k_p_shift<<<nb, TPB, 0, s>>>(p, O, n, &dev_state->dq);
+    const int nb = grid_blocks(D.interior());
+    cudaMemsetAsync(dev_state, 0, sizeof(PcgScalars), s);
+    k_set_inner<<<1, 1, 0, s>>>(dev_state, inner_tol);
+    if (bc_ == 0) k_rhs_sum<DIM><<<nb, TPB, 0, s>>>(rhs, O, slot, &dev_state->mean);
+    if (fp32_) {
+        cudaMemsetAsync(e32, 0, size_t(Lf[0].cells) * sizeof(float), s);
+        k_init<DIM, float><<<nb, TPB, 0, s>>>(rhs, p, O, use_guess, r, Lf[0], slot, dev_state);
+    } else {
+        k_init<DIM, double><<<nb, TPB, 0, s>>>(rhs, p, O, use_guess, r, Ld[0], slot, dev_state);
     }
-    k_true_res<<<nb, TPB, 0, s>>>(rhs_, p, rho64, O, n, slot, dev_state);
+    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 0, conditional, 0);
+}
+
+template <int DIM>
+void Poisson::iterate_dim(cudaStream_t s) {
+    const Outer O = make_outer(D, density_, bc_ == 1, oc);
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
+    const int nb = grid_blocks(D.interior());
+    const int uc = use_conditional ? 1 : 0;
+    if (fp32_) {
+        Level<float> &L0 = Lf[0];
+        const int mode0 = (density_ || bc_ == 0) ? 1 : 2;
+        Id2<float> id2{};
+        for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? float(1.0 / (D.d[a] * D.d[a])) : 0.0f;
+        const dim3 ib(IN_BX, IN_BY);
+        const int nbi = inner_blocks(L0, DIM);
+        vcycle<float>(s);
+        k_in_dot<DIM><<<nbi, ib, 0, s>>>(L0, slot, dev_state);
+        k_in_update_d<DIM><<<nbi, ib, 0, s>>>(L0, d32, dev_state);
+        if (mode0 == 1) k_in_apply<DIM, 1><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
+        else k_in_apply<DIM, 2><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
+        k_in_axpy<DIM><<<nbi, ib, 0, s>>>(L0, d32, q32, e32, slot, dev_state);
+        k_in_check<<<1, 1, 0, s>>>(dev_state, inner_max, max_iter);
+        k_out_add<DIM><<<nb, TPB, 0, s>>>(p_, e32, O, L0, dev_state);
+        k_out_res<DIM><<<nb, TPB, 0, s>>>(rhs_, p_, O, L0, e32, slot, dev_state);
+        k_out_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, conditional, uc);
+        return;
+    }
+    Level<double> &L0 = Ld[0];
+    vcycle<double>(s);
+    k_dot_rz<DIM, double><<<nb, TPB, 0, s>>>(r, L0.x, (const double *)zold, O, L0, slot, dev_state);
+    k_update_d<DIM, double><<<nb, TPB, 0, s>>>(L0.x, (double *)zold, dvec, O, L0, dev_state);
+    k_apply_dq<DIM><<<nb, TPB, 0, s>>>(dvec, q, O, slot, dev_state);
+    k_axpy<DIM, double><<<nb, TPB, 0, s>>>(p_, r, dvec, q, O, L0, slot, dev_state);
+    k_replace<DIM, double><<<nb, TPB, 0, s>>>(rhs_, p_, O, r, L0, rel_tol, slot, dev_state);
+    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 1, conditional, uc);
+}
+
+template <int DIM>
+void Poisson::finish_dim(double *p, cudaStream_t s) {
+    const Outer O = make_outer(D, density_, bc_ == 1, oc);
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
+    const int nb = grid_blocks(D.interior());
+    if (bc_ == 0) {
+        k_p_sum<DIM><<<nb, TPB, 0, s>>>(p, O, slot, &dev_state->dq);
+        k_p_shift<DIM><<<nb, TPB, 0, s>>>(p, O, &dev_state->dq);
+    }
+    k_true_res<DIM><<<nb, TPB, 0, s>>>(rhs_, p, O, slot, dev_state);
     k_relres<<<1, 1, 0, s>>>(dev_state);
 }
 

@@ -20,6 +20,7 @@ struct Level {
     int ratio = 2;          // coarsening factor to the next level
     double d[3] = {0, 0, 0};
     T *x = nullptr, *b = nullptr;
+    T *x2 = nullptr;   // second iterate buffer for out-of-place fused sweeps (same allocation as x)
     T *cx = nullptr, *cy = nullptr, *cz = nullptr;
     T *idg = nullptr;   // 1 / sum of the face coefficients (levels with stored coefficients)
 };
@@ -32,7 +33,10 @@ struct PcgScalars {
     double relres;
     double mean;
     double best;      // smallest relative residual seen
+    double rr_in, rr_in0;   // FP32 inner solve: ||r||^2 now and at its start
+    double in_tol, in_target;   // inner relative tolerance: floor and current target
     int it, done, diverged, since_best;
+    int in_it, pending;     // inner iterations since the last refinement; refinement due
 };
 
 class Poisson {
@@ -62,6 +66,9 @@ public:
     unsigned long long *cond_handle = nullptr;   // graph conditional handle slot (device), 0 when unused
     bool use_conditional = false;
     int prolong_linear = 0;   // 0: piecewise-constant prolongation (default), 1: (bi/tri)linear
+    // FP32 mode: each inner solve stops at this relative residual or after inner_max iterations
+    double inner_tol = 1e-4;
+    int inner_max = 12;
     unsigned long long conditional = 0;
 
 private:
@@ -76,6 +83,12 @@ private:
     int alloc_levels();
     template <class T>
     void build_coarse(cudaStream_t s);
+    template <int DIM>
+    void begin_dim(const double *rhs, double *p, int use_guess, cudaStream_t s);
+    template <int DIM>
+    void iterate_dim(cudaStream_t s);
+    template <int DIM>
+    void finish_dim(double *p, cudaStream_t s);
 
     Dims D{};
     int bc_ = 0, density_ = 1, fp32_ = 0;
@@ -85,6 +98,7 @@ private:
     // FP64 outer iteration vectors (interior, compact, K fastest)
     double *r = nullptr, *dvec = nullptr, *q = nullptr;
     void *zold = nullptr;       // previous preconditioned residual, level-0 padded, T
+    float *d32 = nullptr, *q32 = nullptr, *e32 = nullptr;   // FP32 inner solve vectors, level-0 padded
     void *rho_pad = nullptr;    // level-0 density, padded, T, +inf halo
     const double *rho64 = nullptr;   // caller's ghosted density (FP64 operator)
     double *partial = nullptr;       // reduction scratch (2 x RED_MAX_BLOCKS)

@@ -93,13 +93,45 @@ def _density_case(g, seed):
     return rho, rhs
 
 
+def operator_relres(g, rho, rhs, p):
+    """||g - L p|| / ||g|| with g = -(rhs - mean) and L the face-coefficient operator of
+    init_ppe_proj_coefficients (1 / mean density / d^2 on interior faces, none on walls),
+    evaluated here in numpy, independently of both solvers."""
+    I = g.interior()
+    pi, ri = p[I], rho[I]
+    gv = -(rhs[I] - rhs[I].mean())
+    Lp = np.zeros_like(pi)
+    d = g.spacing()
+    for a in range(g.ndim):
+        lo = [slice(None)] * pi.ndim
+        hi = [slice(None)] * pi.ndim
+        lo[a], hi[a] = slice(0, -1), slice(1, None)
+        lo, hi = tuple(lo), tuple(hi)
+        C = 1.0 / (0.5 * (ri[lo] + ri[hi])) / d[a] / d[a]
+        flux = C * (pi[lo] - pi[hi])
+        Lp[lo] += flux
+        Lp[hi] -= flux
+    return np.linalg.norm(gv - Lp) / np.linalg.norm(gv)
+
+
+DENSITY_GRIDS = {
+    "2d": ((32, 64), (1.0, 2.0)),
+    "3d": ((16, 16, 16), (1.0, 1.0, 1.0)),
+    # level 0 of these is smoothed by the one-pass fused sweep (>= 65536 cells); the second
+    # has partial tiles in j and k
+    "3d_fused": ((48, 48, 48), (1.0, 1.0, 1.0)),
+    "3d_ragged": ((48, 40, 80), (1.0, 0.8, 1.6)),
+}
+
+
 @pytest.mark.parametrize("fp32", [False, True])
-@pytest.mark.parametrize("case", ["2d", "3d"])
+@pytest.mark.parametrize("case", list(DENSITY_GRIDS))
 def test_variable_density_matches_exact_solve(port, fp32, case):
     """Density ratio 1000 pressure equation of projection() (coefficients of
     init_ppe_proj_coefficients, projection_method.cpp:404-465, Neumann walls, zero mean)."""
     from scihpc_gb300 import Poisson
-    g = O.Grid(2, (32, 64), (0.0, 0.0), (1.0, 2.0)) if case == "2d" else O.Grid(3, (16, 16, 16), (0, 0, 0), (1, 1, 1))
+    n, hi = DENSITY_GRIDS[case]
+    g = O.Grid(len(n), n, (0.0,) * len(n), hi)
     rho, rhs = _density_case(g, 5)
     ref, it_ref, rel_ref = port.coef_solve(g, rho, rhs, rel_tol=1e-14, max_iter=200000)
     ps = Poisson(native(g), bc=0, density=True, fp32=fp32)
@@ -110,7 +142,31 @@ def test_variable_density_matches_exact_solve(port, fp32, case):
     out = p.cpu().numpy()
     I = g.interior()
     assert rr <= 1e-11, (rr, it)
+    assert operator_relres(g, rho, rhs, out) <= 2e-11
     assert abs(out[I].mean()) <= 1e-12 * np.abs(out[I]).max()
+    assert rel_l2(out[I], ref[I]) <= PARITY, rel_l2(out[I], ref[I])
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_dirichlet_constant_3d_fused(port, fp32):
+    """Constant-coefficient Dirichlet problem in 3D at 48^3 (fused level-0 sweep, constant
+    faces with the zero ghost-centre wall term) against the reference multigrid."""
+    from scihpc_gb300 import Poisson
+    n = 48
+    g = O.Grid(3, (n, n, n), (0.0,) * 3, (1.0,) * 3)
+    xc = (np.arange(n) + 0.5) / n
+    X, Y, Z = np.meshgrid(xc, xc, xc, indexing="ij")
+    f = 3 * np.pi ** 2 * np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(np.pi * Z)
+    ref, cyc, hist = port.mg_poisson(g, (-f).transpose(2, 1, 0).ravel(), True, 1e-13, 400)
+    ref = ghosted_from_mg(g, ref)
+    rhs = np.zeros(g.shape)
+    rhs[3:-3, 3:-3, 3:-3] = -f
+    ps = Poisson(native(g), bc=1, density=False, fp32=fp32)
+    p = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    it, rr = ps.solve(dev(rhs), p, rel_tol=1e-12, max_iter=100)
+    out = p.cpu().numpy()
+    I = g.interior()
+    assert rr <= 1e-11, rr
     assert rel_l2(out[I], ref[I]) <= PARITY, rel_l2(out[I], ref[I])
 
 
