@@ -31,6 +31,11 @@ BUBBLE = ((0.5, 0.5), 0.25)
 PPE_TOL = 1e-10
 
 
+PPE_DESC = {"fp32": "FP32 V-cycles and conjugate gradients inside FP64 iterative refinement "
+                    "(FP64 residual and pressure)",
+            "fp64": "FP64 V-cycles inside FP64 conjugate gradients"}
+
+
 def physics(h: float) -> dict:
     """Hysing TC1 (rho 1000/100, mu 10/1, sigma 24.5, g 0.98, L = 1), nondimensionalised as
     set_parameters does (global.cpp:31-52); ls_width 1.5h, rdt 0.25h; dt from the reference's
@@ -63,7 +68,6 @@ def config_block(extra=None) -> dict:
                     "rho 1000/1, mu 10/0.1 case diverges within 20 steps in the reference scheme",
          "step": "find_dt + WENO5/TVD-RK3 advection + 5 mpls Euler steps + ab_solve "
                  f"(multigrid-PCG pressure to rel. residual {PPE_TOL:g}) + 12-stage-triple reinit",
-         "pressure_precision": "fp64 V-cycles",
          "l2": "working set 24 MB < L2; L2 flushed (256 MiB write) before every timed step"}
     if extra:
         c.update(extra)
@@ -300,7 +304,8 @@ def run_ours(args) -> None:
     lib()   # raises if the CUDA library is missing: there is no CPU path
     g = Grid(2, (NX, NY), DOMAIN[0], DOMAIN[1])
     h = min(g.spacing())
-    tp = TwoPhase(g, ["no_slip"] * 6, ["neumann"] * 6, physics(h), scheme=1, n_mpls=5, reinit_every=1, fp32=False)
+    tp = TwoPhase(g, ["no_slip"] * 6, ["neumann"] * 6, physics(h), scheme=1, n_mpls=5, reinit_every=1,
+                  fp32=args.ppe == "fp32")
     phi0 = initial_phi(g.shape)
     tp.set("phi", phi0)
     tp.init()
@@ -362,22 +367,26 @@ def run_ours(args) -> None:
 
     # roofline of the dominant kernel group: one V(2,2) pressure V-cycle on this grid
     hbm = peaks()
-    ps = Poisson(g, bc=0, density=True, fp32=False)
+    fp32 = args.ppe == "fp32"
+    ps = Poisson(g, bc=0, density=True, fp32=fp32)
     ps.set_density(tp.device_ptr("rho"))
     ptmp = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
     ncyc = 200
     vms = ps.time_vcycles(tp.device_ptr("rhs"), ptmp, ncyc) / ncyc
-    vb = vcycle_bytes(ps.levels(), 2, 8)
-    roof = {"bound": "hbm", "kernel": "pressure V(2,2) cycle, all levels (FP64)", "achieved": vb / vms / 1e6,
+    vb = vcycle_bytes(ps.levels(), 2, 4 if fp32 else 8)
+    roof = {"bound": "hbm", "kernel": f"pressure V(2,2) cycle, all levels ({'FP32' if fp32 else 'FP64'})",
+            "achieved": vb / vms / 1e6,
             "peak": hbm["hbm_gbs"], "unit": "GB/s", "frac": vb / vms / 1e6 / hbm["hbm_gbs"],
             "peak_src": hbm["src"], "traffic": None, "alg_bytes_per_launch": vb, "launch_ms": vms,
-            "note": "128x256 FP64 working set is L2-resident; achieved counts algorithmic bytes"}
+            "note": "128x256 working set is L2-resident and the cycle is latency bound; achieved "
+                    "counts model bytes (the 256^3 block below is the HBM-bound case)"}
     ps.close()
 
     line = {"metric": "time steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic bubble)",
-            "config": config_block({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+            "config": config_block({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                                    "pressure_precision": PPE_DESC[args.ppe]}),
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches),
             "ppe_iters_per_step": ppe_iters / args.steps, "wall_s": t_wall, "roofline": roof,
             "diagnostics": diag}
@@ -417,6 +426,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--lite", action="store_true", help="timed steps only (for kernel launch lists)")
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of graph replay")
+    ap.add_argument("--ppe", default="fp32", choices=["fp32", "fp64"],
+                    help="pressure V-cycles in FP32 inside FP64 refinement (default) or all FP64")
     ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
                     help="only three iterations of the 256^3 pressure solve (profiling case)")
     args = ap.parse_args()

@@ -37,7 +37,7 @@ constexpr int TPB = 256;
 // SM executes about 4 FP64 flops per clock on GB300, so FP64 cycles hand over to the single
 // block much later than FP32 ones.
 constexpr long long COARSE_CELLS_FP32 = 4096;
-constexpr long long COARSE_CELLS_FP64 = 512;
+constexpr long long COARSE_CELLS_FP64 = 128;
 // 3D levels of at least this many cells are smoothed by the one-pass sweep (k_sweep3)
 constexpr long long FUSED_MIN_CELLS = 65536;
 
@@ -924,6 +924,7 @@ __global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n
 // threads take IN_BY rows at a time (grid-stride over rows), thread x takes elements x,
 // x + IN_BX, ... of its row, so each thread has several independent loads in flight.
 constexpr int IN_BX = 64, IN_BY = TPB / IN_BX, IN_RU = 4;
+constexpr double INNER_ALPHA_MAX = 20.0;
 
 struct RowIt {
     long long base;   // padded offset of the row's element k = -1
@@ -978,7 +979,7 @@ __global__ void __launch_bounds__(TPB) k_in_dot(Level<float> L, RedSlot slot, Pc
 template <int DIM>
 __global__ void __launch_bounds__(TPB) k_in_update_d(Level<float> L, float *__restrict__ d, const PcgScalars *st) {
     if (st->done) return;
-    const float beta = st->in_it == 0 ? 0.0f : float(st->rz / st->rz_prev);
+    const float beta = (st->in_it == 0 || !(st->rz_prev > 0.0)) ? 0.0f : float(st->rz / st->rz_prev);
     for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
         float z[IN_RU], dv[IN_RU];
 #pragma unroll
@@ -1037,7 +1038,14 @@ __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, const float *__
                                                  const float *__restrict__ q, float *__restrict__ e, RedSlot slot,
                                                  PcgScalars *st) {
     if (st->done) return;
-    const float alpha = float(st->rz / st->dq);
+    // Breakdown of the FP32 recurrence: once the remaining error is smooth, L d in FP32 is
+    // mostly cancellation noise, <d, L d> collapses and alpha blows up (a V-cycle-
+    // preconditioned step is O(1)).  Such a step is not taken; the check below ends the
+    // inner solve and the FP64 refinement continues from the last good correction.
+    const double a = st->rz / st->dq;
+    const bool ok = a > 0.0 && a <= INNER_ALPHA_MAX;
+    const float alpha = ok ? float(a) : 0.0f;
+    if (!ok && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) st->in_break = 1;
     float acc = 0.0f;
     for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
         float ev[IN_RU], dv[IN_RU], rv[IN_RU], qv[IN_RU];
@@ -1074,7 +1082,9 @@ __global__ void k_in_check(PcgScalars *st, int inner_max, int max_iter) {
     st->it += 1;
     st->in_it += 1;
     const double rel = st->rr_in0 > 0.0 ? sqrt(st->rr_in / st->rr_in0) : 0.0;
-    const bool bad = !(rel == rel) || isinf(rel);
+    // a residual four times above the best one so far also means FP32 round-off has taken over
+    const bool bad = !(rel == rel) || isinf(rel) || st->in_break || (st->in_it > 1 && st->rr_in > 16.0 * st->rr_in_min);
+    if (st->in_it == 1 || st->rr_in < st->rr_in_min) st->rr_in_min = st->rr_in;
     st->pending = (bad || rel <= st->in_target || st->in_it >= inner_max || st->it >= max_iter) ? 1 : 0;
 }
 
@@ -1115,6 +1125,7 @@ __global__ void k_out_check(PcgScalars *st, double tol, int max_iter, unsigned l
     if (st->pending) {
         outer_progress(st, tol, max_iter, 0);
         st->in_it = 0;
+        st->in_break = 0;
         st->rr_in0 = st->rr;
         st->pending = 0;
     }
@@ -1653,8 +1664,10 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
         iterate(s);
         SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         SCIHPC_CUDA(cudaStreamSynchronize(s));
-        if (trace) std::fprintf(stderr, "ppe it %d relres %.3e rz %.3e dq %.3e\n", host_state->it, host_state->relres,
-                                host_state->rz, host_state->dq);
+        if (trace)
+            std::fprintf(stderr, "ppe it %d relres %.3e rz %.3e dq %.3e in_it %d rr_in %.3e rr_in0 %.3e target %.3e\n",
+                         host_state->it, host_state->relres, host_state->rz, host_state->dq, host_state->in_it,
+                         host_state->rr_in, host_state->rr_in0, host_state->in_target);
     }
     const int it = host_state->it;
     const bool div = host_state->diverged;

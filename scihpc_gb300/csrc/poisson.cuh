@@ -35,8 +35,10 @@ struct PcgScalars {
     double best;      // smallest relative residual seen
     double rr_in, rr_in0;   // FP32 inner solve: ||r||^2 now and at its start
     double in_tol, in_target;   // inner relative tolerance: floor and current target
+    double rr_in_min;           // smallest inner ||r||^2 of the current inner solve
     int it, done, diverged, since_best;
     int in_it, pending;     // inner iterations since the last refinement; refinement due
+    int in_break;           // the inner recurrence broke down (FP32 round-off)
 };
 
 class Poisson {

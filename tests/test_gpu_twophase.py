@@ -97,8 +97,9 @@ def test_mpls_and_reinit():
     compare(G, port, gpu, ["phi"], LS_TOL)
 
 
-def test_projection_step():
-    port, gpu = make_pair(G)
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32_refined"])
+def test_projection_step(fp32):
+    port, gpu = make_pair(G, fp32=fp32)
     port.call("init")
     gpu.init()
     for s in (port, gpu):
@@ -131,9 +132,10 @@ def test_pressure_solver_on_checker_state():
     assert rel_l2(p.cpu().numpy()[I], port.get("p")[I]) <= FLOW_TOL
 
 
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32_refined"])
 @pytest.mark.parametrize("graph", [False, True], ids=["eager", "graph"])
-def test_full_steps(graph):
-    port, gpu = make_pair(G)
+def test_full_steps(graph, fp32):
+    port, gpu = make_pair(G, fp32=fp32)
     port.call("init")
     gpu.init()
     for k in range(2):
