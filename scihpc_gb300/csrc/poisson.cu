@@ -38,6 +38,8 @@ constexpr int TPB = 256;
 // block much later than FP32 ones.
 constexpr long long COARSE_CELLS_FP32 = 4096;
 constexpr long long COARSE_CELLS_FP64 = 128;
+// dynamic shared memory the coarse kernel may take for its levels (plus ~10 KB static)
+constexpr size_t COARSE_SMEM_MAX = 200 * 1024;
 // 3D levels of at least this many cells are smoothed by the one-pass sweep (k_sweep3)
 constexpr long long FUSED_MIN_CELLS = 65536;
 
@@ -1138,34 +1140,71 @@ __global__ void k_out_check(PcgScalars *st, double tol, int max_iter, unsigned l
 // The coarse end of the V-cycle in one thread block: levels lc .. nlev-1 (each at most a few
 // thousand cells) are smoothed, restricted, solved and prolongated with __syncthreads()
 // between phases instead of one kernel launch per phase.  Levels >= 1 carry stored
-// coefficients.
+// coefficients.  When they fit (smem_on), the levels' arrays are first copied into shared
+// memory, so every phase runs at shared-memory latency; level lc's iterate is copied back.
 template <class T>
 struct LevelPack {
     Level<T> L[16];
 };
 
+// shared-memory bytes the coarse levels lc.. need: x, b, ndim face arrays and idg per cell
+template <class T>
+inline size_t coarse_smem_bytes(const std::vector<Level<T>> &Ls, int lc, int ndim) {
+    size_t cells = 0;
+    for (size_t l = lc; l < Ls.size(); ++l) cells += size_t(Ls[l].cells);
+    return cells * size_t(3 + ndim) * sizeof(T);
+}
+
 template <class T, int DIM>
 __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, int nlev, const double *__restrict__ Minv,
-                                                        int n, int neumann, int linear) {
+                                                        int n, int neumann, int linear, int smem_on) {
+    extern __shared__ __align__(16) unsigned char coarse_dsm[];
+    __shared__ Level<T> SL[16];
     __shared__ double b[1024];
     __shared__ double mean;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int nu = 2;
+    if (tid == 0)
+        for (int l = lc; l < nlev; ++l) SL[l] = LP.L[l];
+    __syncthreads();
+    if (smem_on) {
+        T *p = reinterpret_cast<T *>(coarse_dsm);
+        for (int l = lc; l < nlev; ++l) {
+            const Level<T> &G = LP.L[l];
+            const long long c = G.cells;
+            T *x = p, *bb = p + c, *cx = p + 2 * c, *cy = p + 3 * c, *cz = DIM == 3 ? p + 4 * c : nullptr;
+            T *idg = p + (DIM == 3 ? 5 : 4) * c;
+            for (long long i = tid; i < c; i += nt) {
+                x[i] = l == lc ? G.x[i] : T(0);
+                bb[i] = l == lc ? G.b[i] : T(0);
+                cx[i] = G.cx[i];
+                cy[i] = G.cy[i];
+                if (DIM == 3) cz[i] = G.cz[i];
+                idg[i] = G.idg[i];
+            }
+            if (tid == 0) {
+                SL[l].x = x, SL[l].b = bb, SL[l].cx = cx, SL[l].cy = cy, SL[l].idg = idg;
+                if (DIM == 3) SL[l].cz = cz;
+            }
+            p += (DIM == 3 ? 6 : 5) * c;
+        }
+        __syncthreads();
+    }
     for (int l = lc; l < nlev - 1; ++l) {
-        const Level<T> &L = LP.L[l];
+        const Level<T> &L = SL[l];
         const long long cnt = smooth_count<T, DIM>(L);
         for (int k = 0; k < nu; ++k)
             for (int color = 0; color < 2; ++color) {
                 for (long long t = tid; t < cnt; t += nt) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
                 __syncthreads();
             }
-        const Level<T> &Cl = LP.L[l + 1];
+        const Level<T> &Cl = SL[l + 1];
         const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
         for (long long t = tid; t < nc; t += nt) restrict_one<T, 0, DIM>(L, Cl, nullptr, nullptr, t);
         __syncthreads();
     }
     {
-        const Level<T> &L = LP.L[nlev - 1];
+        const Level<T> &L = SL[nlev - 1];
         auto pidx = [&](int c) {
             int I, J, K = 0;
             if (DIM == 3) {
@@ -1196,9 +1235,9 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
         __syncthreads();
     }
     for (int l = nlev - 2; l >= lc; --l) {
-        const Level<T> &L = LP.L[l];
+        const Level<T> &L = SL[l];
         const long long nf = (long long)L.n[0] * L.n[1] * (DIM == 3 ? L.n[2] : 1);
-        for (long long t = tid; t < nf; t += nt) prolong_one<T, DIM>(L, LP.L[l + 1], neumann, linear, t);
+        for (long long t = tid; t < nf; t += nt) prolong_one<T, DIM>(L, SL[l + 1], neumann, linear, t);
         __syncthreads();
         const long long cnt = smooth_count<T, DIM>(L);
         for (int k = 0; k < nu; ++k)
@@ -1206,6 +1245,10 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
                 for (long long t = tid; t < cnt; t += nt) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
                 __syncthreads();
             }
+    }
+    if (smem_on) {
+        const long long c = LP.L[lc].cells;
+        for (long long i = tid; i < c; i += nt) LP.L[lc].x[i] = SL[lc].x[i];
     }
 }
 
@@ -1319,6 +1362,10 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaMallocHost(&host_state, sizeof(PcgScalars)));
     int rc = fp32 ? alloc_levels<float>() : alloc_levels<double>();
     if (rc) return rc;
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     if (!density) {
         // constant coefficients: build the hierarchy once (rho unused)
         cudaStream_t s = 0;
@@ -1552,8 +1599,11 @@ void Poisson::vcycle(cudaStream_t s) {
     if (packed && lc >= 1) {
         LevelPack<T> LP;
         for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
-        if (D.ndim == 2) k_coarse_cycle<T, 2><<<1, 1024, 0, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear);
-        else k_coarse_cycle<T, 3><<<1, 1024, 0, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear);
+        const size_t sm = coarse_smem_bytes(Ls, lc, D.ndim);
+        const int on = sm <= COARSE_SMEM_MAX ? 1 : 0;
+        const size_t dyn = on ? sm : 0;
+        if (D.ndim == 2) k_coarse_cycle<T, 2><<<1, 1024, dyn, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear, on);
+        else k_coarse_cycle<T, 3><<<1, 1024, dyn, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear, on);
     } else {
         Level<T> &C = Ls[nlev - 1];
         if (D.ndim == 2) k_dense_solve<T, 2><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
