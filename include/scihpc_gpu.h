@@ -201,6 +201,15 @@ int scihpc_twophase_mpls(scihpc_twophase *tp, int count);
 int scihpc_twophase_reinit(scihpc_twophase *tp, int *steps);
 int scihpc_twophase_find_source(scihpc_twophase *tp);
 int scihpc_twophase_ab_solve(scihpc_twophase *tp, int *iters, double *relres);
+/* Finer-grained stages for callers that drive the reinitialisation loop themselves, as the
+ * reference drivers do (benchmarks_2d_bubble_rising.cpp:122-129): find_sign
+ * (wrapper_func.cpp:387-402); one runge_kutta::tvd_rk3 step (runge_kutta.cpp:13-49) with
+ * lsf_redistance_lambda (lambda = 1) or lsf_redistance_no_lambda (lambda = 0)
+ * (source.cpp:156-241); and the convection scheme advect() uses: 0 = convection with UCCD
+ * (source.cpp:8-40), 1 = WENO5 (weno_solver.cpp:270-278). */
+int scihpc_twophase_find_sign(scihpc_twophase *tp);
+int scihpc_twophase_reinit_step(scihpc_twophase *tp, int lambda);
+int scihpc_twophase_set_scheme(scihpc_twophase *tp, int scheme);
 /* nsteps time steps of the drivers' loop (benchmarks_2d_bubble_rising.cpp:100-130):
  * find_dt, advection, mass correction, ab_solve, reinitialisation.  use_graph = 1 replays
  * a captured CUDA graph per step (the pressure solve iterates inside it under a device-side

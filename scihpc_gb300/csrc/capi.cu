@@ -398,6 +398,26 @@ int scihpc_twophase_reinit(scihpc_twophase *tp, int *steps) {
     return SCIHPC_OK;
 }
 
+int scihpc_twophase_find_sign(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_find_sign: NULL argument");
+    tp->tp.find_sign();
+    TP_SYNC(tp);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_reinit_step(scihpc_twophase *tp, int lambda) {
+    REQUIRE(tp && (lambda == 0 || lambda == 1), "twophase_reinit_step: bad argument");
+    tp->tp.reinit_step(lambda);
+    TP_SYNC(tp);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_set_scheme(scihpc_twophase *tp, int scheme) {
+    REQUIRE(tp && (scheme == 0 || scheme == 1), "twophase_set_scheme: scheme must be 0 (UCCD) or 1 (WENO5)");
+    tp->tp.set_scheme(scheme);
+    return SCIHPC_OK;
+}
+
 int scihpc_twophase_find_source(scihpc_twophase *tp) {
     REQUIRE(tp, "twophase_find_source: NULL argument");
     tp->tp.find_source();

@@ -756,6 +756,27 @@ void TwoPhaseGpu::reinit_stage(int stage) {
     if (!phi_fill.on) scalar_bc(phi.data);
 }
 
+void TwoPhaseGpu::find_sign() {
+    k_sign<<<blocks_for(D.size(), TPB), TPB, 0, stream>>>(phi.data, sign, D.size(), P.ls_width);
+}
+
+void TwoPhaseGpu::reinit_step(int lambda) {
+    const int keep = reinit_lambda;
+    reinit_lambda = lambda;
+    for (int st = 1; st <= 3; ++st) reinit_stage(st);
+    reinit_lambda = keep;
+}
+
+void TwoPhaseGpu::set_scheme(int s) {
+    if (s == scheme) return;
+    scheme = s;
+    // a captured step graph holds the old scheme's kernels
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+}
+
 int TwoPhaseGpu::reinit() {
     k_sign<<<blocks_for(D.size(), TPB), TPB, 0, stream>>>(phi.data, sign, D.size(), P.ls_width);
     for (int k = 0; k < reinit_steps; ++k)

@@ -44,6 +44,9 @@ public:
     void advect();
     void mpls(int count);
     int reinit();            // returns RK3 steps
+    void find_sign();        // find_sign (wrapper_func.cpp:387-402) into the sign field
+    void reinit_step(int lambda);   // one TVD-RK3 step of the redistance equation
+    void set_scheme(int s);  // convection: 0 UCCD (source.cpp:8-40), 1 WENO5
     void find_source();
     void ab_solve_pre();     // store, find_source, AB2, PPE right-hand side, solver begin
     void ab_solve_post();    // solver finish, pressure BC, velocity correction, node velocity

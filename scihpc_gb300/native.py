@@ -108,6 +108,9 @@ _SIGS = {
     "scihpc_twophase_mpls": ([_vp, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_reinit": ([_vp, _ip], ctypes.c_int),
     "scihpc_twophase_find_source": ([_vp], ctypes.c_int),
+    "scihpc_twophase_find_sign": ([_vp], ctypes.c_int),
+    "scihpc_twophase_reinit_step": ([_vp, ctypes.c_int], ctypes.c_int),
+    "scihpc_twophase_set_scheme": ([_vp, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_ab_solve": ([_vp, _ip, _dp], ctypes.c_int),
     "scihpc_twophase_step": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_diagnostics": ([_vp, _dp], ctypes.c_int),
@@ -344,6 +347,15 @@ class TwoPhase:
 
     def find_source(self):
         self.L.check(self.L.scihpc_twophase_find_source(self.h))
+
+    def find_sign(self):
+        self.L.check(self.L.scihpc_twophase_find_sign(self.h))
+
+    def reinit_step(self, lambda_correction=True):
+        self.L.check(self.L.scihpc_twophase_reinit_step(self.h, int(lambda_correction)))
+
+    def set_scheme(self, scheme: int):
+        self.L.check(self.L.scihpc_twophase_set_scheme(self.h, scheme))
 
     def ab_solve(self):
         it = ctypes.c_int(0)
