@@ -33,6 +33,9 @@ namespace scihpc {
 namespace {
 
 constexpr int TPB = 256;
+// A V-cycle-preconditioned conjugate-gradient step length is O(1); far larger ones come
+// from <d, L d> lost in round-off.
+constexpr double CG_ALPHA_MAX = 20.0;
 // Levels of at most this many cells run together in one thread block (k_coarse_cycle).  One
 // SM executes about 4 FP64 flops per clock on GB300, so FP64 cycles hand over to the single
 // block much later than FP32 ones.
@@ -257,7 +260,8 @@ template <int DIM, class T>
 __global__ void k_update_d(const T *__restrict__ z, T *__restrict__ zold, double *__restrict__ d, Outer O,
                            Level<T> L0, const PcgScalars *st) {
     if (st->done) return;
-    const double beta = st->it == 0 ? 0.0 : (st->rz - st->r_zold) / st->rz_prev;
+    // after a residual replacement the old direction no longer matches r: restart
+    const double beta = (st->it == 0 || st->restart) ? 0.0 : (st->rz - st->r_zold) / st->rz_prev;
     for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
         const long long P0 = p0_of<DIM>(L0, I, J, K);
         const T zz = z[P0];
@@ -271,6 +275,7 @@ template <int DIM>
 __global__ void k_apply_dq(const double *__restrict__ d, double *__restrict__ qv, Outer O, RedSlot slot,
                            PcgScalars *st) {
     if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->restart = 0;   // k_update_d has consumed it
     double v[1] = {0.0};
     for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
         const double lq = apply_L<DIM, false>(d, O, I, J, K, co, co);
@@ -286,7 +291,12 @@ template <int DIM, class T>
 __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const double *__restrict__ d,
                        const double *__restrict__ qv, Outer O, Level<T> L0, RedSlot slot, PcgScalars *st) {
     if (st->done) return;
-    const double alpha = st->rz / st->dq;
+    // A step far outside (0, CG_ALPHA_MAX] means <d, L d> is round-off (the iteration has
+    // reached the attainable accuracy): no update, and the check ends the solve.
+    const double a = st->rz / st->dq;
+    const bool ok = a > 0.0 && a <= CG_ALPHA_MAX;
+    const double alpha = ok ? a : 0.0;
+    if (!ok && blockIdx.x == 0 && threadIdx.x == 0) st->in_break = 1;
     double v[1] = {0.0};
     for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
         p[go] += alpha * d[co];
@@ -306,6 +316,7 @@ template <int DIM, class T>
 __global__ void k_replace(const double *__restrict__ rhs, const double *__restrict__ p, Outer O,
                           double *__restrict__ r, Level<T> L0, double tol, RedSlot slot, PcgScalars *st) {
     if (st->done || !(st->rr <= tol * tol * st->bb)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->restart = 1;
     const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
     double v[1] = {0.0};
     for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long co) {
@@ -354,6 +365,7 @@ __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, u
         st->it += 1;
     }
     outer_progress(st, tol, max_iter, !advance);
+    if (advance && st->in_break) st->done = 1;   // breakdown of the FP64 recurrence (k_axpy)
     st->rr_in0 = st->rr;
     st->in_target = fmax(st->in_tol, 0.25 * tol / fmax(st->relres, 1e-300));
     set_cond(handle, use_handle, !st->done);
@@ -926,7 +938,6 @@ __global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n
 // threads take IN_BY rows at a time (grid-stride over rows), thread x takes elements x,
 // x + IN_BX, ... of its row, so each thread has several independent loads in flight.
 constexpr int IN_BX = 64, IN_BY = TPB / IN_BX, IN_RU = 4;
-constexpr double INNER_ALPHA_MAX = 20.0;
 
 struct RowIt {
     long long base;   // padded offset of the row's element k = -1
@@ -1045,7 +1056,7 @@ __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, const float *__
     // preconditioned step is O(1)).  Such a step is not taken; the check below ends the
     // inner solve and the FP64 refinement continues from the last good correction.
     const double a = st->rz / st->dq;
-    const bool ok = a > 0.0 && a <= INNER_ALPHA_MAX;
+    const bool ok = a > 0.0 && a <= CG_ALPHA_MAX;
     const float alpha = ok ? float(a) : 0.0f;
     if (!ok && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) st->in_break = 1;
     float acc = 0.0f;

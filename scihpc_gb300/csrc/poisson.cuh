@@ -39,6 +39,7 @@ struct PcgScalars {
     int it, done, diverged, since_best;
     int in_it, pending;     // inner iterations since the last refinement; refinement due
     int in_break;           // the inner recurrence broke down (FP32 round-off)
+    int restart;            // FP64 CG: the residual was replaced, next direction restarts
 };
 
 class Poisson {
