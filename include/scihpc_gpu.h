@@ -227,6 +227,45 @@ int scihpc_twophase_graph_stats(scihpc_twophase *tp, long long out[4]);
 /* Statistics of the last pressure solve: {iterations, relative residual, ms}. */
 int scihpc_twophase_ppe_stats(scihpc_twophase *tp, double out[3]);
 
+/* ------------------------------------------------------------------ tensor-core convolutions
+ * 3x3 convolution, stride 1, zero padding 1, as implicit GEMM on the tcgen05 tensor cores
+ * (BF16 operands, FP32 accumulation).  No reference counterpart: building blocks of the
+ * learned pressure guess below.  x: BF16 [h*w][ci] (channels fastest), w: BF16 [co][9][ci]
+ * (tap t = 3 (dy+1) + (dx+1)), bias: FP32 [co] or NULL, out: FP32 [h*w][co]; ci, co multiples
+ * of 16, co <= 256.  conv3x3_wgrad: dw[co][9][ci] = sum_p x[p + off(t)][ci] dz[p][co], dz BF16
+ * [h*w][co], partial: splits * 9 * ci * co floats of scratch.  Device pointers; synchronous. */
+int scihpc_conv3x3(const void *x, const void *w, const float *bias, float *out, int h, int w_, int ci, int co, int relu,
+                   void *stream);
+int scihpc_conv3x3_wgrad(const void *x, const void *dz, float *dw, float *partial, int splits, int h, int w_, int ci,
+                         int co, void *stream);
+
+/* ------------------------------------------------------------------ learned pressure guess
+ * A 4-level 2D U-Net (16-32-64-128 channels) predicting the pressure of the variable-density
+ * Poisson equation from (density, right-hand side, previous pressure) on an h x w grid (h, w
+ * multiples of 8); every convolution, forward and backward, runs on the tensor cores.  No
+ * reference counterpart (the reference has no learned component).  Fields are FP64 ghosted
+ * 2D arrays of a grid with n = (h, w) (the pressure solver's layout); pprev may be NULL.
+ * The network runs on its own stream (scihpc_unet_stream): inputs must be complete before
+ * a call.  infer writes guess = pprev + s * net(...); the pressure solve then starts from
+ * guess and iterates to its tolerance as usual.  loss_grad / train_step fit the network to a
+ * solved pressure p (mean-squared error of the normalised correction; train_step adds one
+ * Adam step with learning rate lr).  Weights and gradients move as FP32 host arrays of
+ * scihpc_unet_num_params entries. */
+typedef struct scihpc_unet scihpc_unet;
+int scihpc_unet_create(int h, int w, unsigned seed, scihpc_unet **out);
+int scihpc_unet_destroy(scihpc_unet *u);
+int scihpc_unet_num_params(scihpc_unet *u, long long *n);
+int scihpc_unet_set_weights(scihpc_unet *u, const float *host, long long n);
+int scihpc_unet_get_weights(scihpc_unet *u, float *host, long long n);
+int scihpc_unet_get_gradient(scihpc_unet *u, float *host, long long n);
+int scihpc_unet_infer(scihpc_unet *u, const scihpc_grid *grid, const double *rho, const double *rhs,
+                      const double *pprev, double *guess);
+int scihpc_unet_loss_grad(scihpc_unet *u, const scihpc_grid *grid, const double *rho, const double *rhs,
+                          const double *pprev, const double *p, double *loss);
+int scihpc_unet_train_step(scihpc_unet *u, const scihpc_grid *grid, const double *rho, const double *rhs,
+                           const double *pprev, const double *p, float lr, double *loss);
+int scihpc_unet_stream(scihpc_unet *u, void **stream);
+
 #ifdef __cplusplus
 }
 #endif

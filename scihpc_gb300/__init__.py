@@ -5,4 +5,5 @@ The product is the C-ABI shared library ``_lib/libscihpc_gb300.so`` (declaration
 Python callers (tests, benchmarks); it raises if the library is missing rather than falling
 back to any CPU path.
 """
-from .native import (BC, Grid, Lib, LibraryNotBuilt, Poisson, ScihpcError, TwoPhase, Workspace, lib)  # noqa: F401
+from .native import (BC, Grid, Lib, LibraryNotBuilt, Poisson, ScihpcError, TwoPhase, UNet, Workspace, conv3x3,  # noqa: F401
+                     conv3x3_wgrad, lib)

@@ -1,0 +1,107 @@
+"""Learned initial guess for the pressure solve: snapshot generation with the GPU multigrid
+solver, training of the tensor-core U-Net (scihpc_unet_*), and the comparison of solver
+iterations with and without the guess.
+
+The workload is the Rayleigh-Taylor-type variable-density Poisson equation (density
+1 + 2 H(phi), interface y = 0.5 + sum of 8 seeded sinusoids of amplitude <= 0.02, Neumann walls,
+zero-mean right-hand side).  Consecutive time steps are imitated by pairs of problems whose
+interface phases and right-hand-side modes differ slightly: the solution of the first is the
+"previous pressure" of the second, as in a time loop.  The multigrid solve always iterates to
+the same relative residual; the network only changes where it starts.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .native import Grid, Poisson, UNet
+
+__all__ = ["rt_problem", "make_snapshots", "train", "solve_iterations"]
+
+
+def rt_problem(n: int, seed: int, drift: float, torch, device):
+    """Density and right-hand side (ghosted FP64 fields on an n x n grid of [0,1]^2) of sample
+    `seed`, advanced by `drift` (0 = the previous step, 1 = the current one)."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(0.0, 0.02, 8)
+    m = rng.integers(1, 9, 8)
+    th = rng.uniform(0.0, 2 * math.pi, 8)
+    kx, ky = rng.integers(1, 6, 6), rng.integers(1, 6, 6)
+    amp, ph = rng.standard_normal(6), rng.uniform(0.0, 2 * math.pi, 6)
+    h = 1.0 / n
+    c = (torch.arange(n, dtype=torch.float64, device=device) + 0.5) * h
+    X, Y = torch.meshgrid(c, c, indexing="ij")
+    iface = 0.5 + sum(float(a[k]) * torch.sin(2 * math.pi * float(m[k]) * X + float(th[k]) + 0.05 * drift)
+                      for k in range(8))
+    phi = Y - iface
+    w = 1.5 * h
+    H = torch.where(phi < -w, torch.zeros_like(phi), torch.where(phi > w, torch.ones_like(phi),
+                    0.5 * (1 + phi / w + torch.sin(math.pi * phi / w) / math.pi)))
+    rho = torch.ones((n + 6, n + 6, 1), dtype=torch.float64, device=device)
+    rho[3:-3, 3:-3, 0] = 1.0 + 2.0 * H
+    rho[:3], rho[-3:] = rho[3:4].clone(), rho[-4:-3].clone()
+    rho[:, :3], rho[:, -3:] = rho[:, 3:4].clone(), rho[:, -4:-3].clone()
+    # smooth zero-mean modes (cosines of the Neumann problem), slightly rotated with the drift
+    f = torch.zeros_like(X)
+    for j in range(6):
+        f += float(amp[j]) * (1 + 0.02 * drift) * torch.cos(math.pi * float(kx[j]) * X + 0.03 * drift * j) * \
+             torch.cos(math.pi * float(ky[j]) * Y + float(ph[j]) * 0.0)
+    rhs = torch.zeros_like(rho)
+    rhs[3:-3, 3:-3, 0] = f - f.mean()
+    return rho, rhs
+
+
+def make_snapshots(n: int, seeds, torch, device, rel_tol: float = 1e-10, fp32: bool = True):
+    """[(rho, rhs, pprev, p)] for the given seeds: pprev solves the drift-0 problem, p the
+    drift-1 problem (both to rel_tol)."""
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    out = []
+    for s in seeds:
+        ps = Poisson(g, bc=0, density=True, fp32=fp32)
+        rho0, rhs0 = rt_problem(n, s, 0.0, torch, device)
+        rho1, rhs1 = rt_problem(n, s, 1.0, torch, device)
+        p0 = torch.zeros_like(rho0)
+        ps.set_density(rho0)
+        ps.solve(rhs0, p0, rel_tol=rel_tol, max_iter=200)
+        p1 = p0.clone()
+        ps.set_density(rho1)
+        ps.solve(rhs1, p1, rel_tol=rel_tol, max_iter=200, use_guess=True)
+        torch.cuda.synchronize()
+        ps.close()
+        out.append((rho1, rhs1, p0, p1))
+    return out
+
+
+def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0):
+    """Adam steps over the snapshots in a seeded random order; returns the loss history."""
+    n = snaps[0][0].shape[0] - 6
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    rng = np.random.default_rng(seed)
+    losses = []
+    torch.cuda.synchronize()
+    for k in range(steps):
+        rho, rhs, pprev, p = snaps[int(rng.integers(len(snaps)))]
+        losses.append(net.train_step(g, rho, rhs, pprev, p, lr))
+    return losses
+
+
+def solve_iterations(snaps, torch, net: UNet | None = None, rel_tol: float = 1e-10, fp32: bool = True):
+    """Solver iterations (V-cycles) and final residuals for each snapshot, starting from the
+    previous pressure (net None) or from the network's guess."""
+    n = snaps[0][0].shape[0] - 6
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    its, res = [], []
+    for rho, rhs, pprev, _ in snaps:
+        ps = Poisson(g, bc=0, density=True, fp32=fp32)
+        ps.set_density(rho)
+        p = pprev.clone()
+        if net is not None:
+            torch.cuda.synchronize()
+            net.infer(g, rho, rhs, pprev, p)
+        it, rr = ps.solve(rhs, p, rel_tol=rel_tol, max_iter=200, use_guess=True)
+        torch.cuda.synchronize()
+        ps.close()
+        its.append(it)
+        res.append(rr)
+    return its, res

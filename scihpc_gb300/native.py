@@ -111,6 +111,20 @@ _SIGS = {
     "scihpc_twophase_find_sign": ([_vp], ctypes.c_int),
     "scihpc_twophase_reinit_step": ([_vp, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_set_scheme": ([_vp, ctypes.c_int], ctypes.c_int),
+    "scihpc_conv3x3": ([_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp],
+                       ctypes.c_int),
+    "scihpc_conv3x3_wgrad": ([_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int, _vp], ctypes.c_int),
+    "scihpc_unet_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)], ctypes.c_int),
+    "scihpc_unet_destroy": ([_vp], ctypes.c_int),
+    "scihpc_unet_num_params": ([_vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+    "scihpc_unet_set_weights": ([_vp, _vp, ctypes.c_longlong], ctypes.c_int),
+    "scihpc_unet_get_weights": ([_vp, _vp, ctypes.c_longlong], ctypes.c_int),
+    "scihpc_unet_get_gradient": ([_vp, _vp, ctypes.c_longlong], ctypes.c_int),
+    "scihpc_unet_infer": ([_vp, ctypes.POINTER(_GridC), _vp, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_unet_loss_grad": ([_vp, ctypes.POINTER(_GridC), _vp, _vp, _vp, _vp, _dp], ctypes.c_int),
+    "scihpc_unet_train_step": ([_vp, ctypes.POINTER(_GridC), _vp, _vp, _vp, _vp, ctypes.c_float, _dp], ctypes.c_int),
+    "scihpc_unet_stream": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_ab_solve": ([_vp, _ip, _dp], ctypes.c_int),
     "scihpc_twophase_step": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_diagnostics": ([_vp, _dp], ctypes.c_int),
@@ -391,3 +405,67 @@ class TwoPhase:
         out = (ctypes.c_double * 3)()
         self.L.check(self.L.scihpc_twophase_ppe_stats(self.h, out))
         return dict(iters=out[0], relres=out[1], ms=out[2])
+
+
+def conv3x3(x, w, bias, out, h: int, wd: int, ci: int, co: int, relu: bool = False):
+    """scihpc_conv3x3 on device tensors: x BF16 [h*w][ci], w BF16 [co][9][ci], out FP32."""
+    lib().check(lib().scihpc_conv3x3(_ptr(x), _ptr(w), _ptr(bias), _ptr(out), h, wd, ci, co, int(relu), None))
+
+
+def conv3x3_wgrad(x, dz, dw, partial, splits: int, h: int, wd: int, ci: int, co: int):
+    """scihpc_conv3x3_wgrad on device tensors: dw FP32 [co][9][ci]."""
+    lib().check(lib().scihpc_conv3x3_wgrad(_ptr(x), _ptr(dz), _ptr(dw), _ptr(partial), splits, h, wd, ci, co, None))
+
+
+class UNet:
+    """scihpc_unet: the learned initial guess of the pressure solve (tensor-core U-Net)."""
+
+    def __init__(self, h: int, w: int, seed: int = 0):
+        self.L = lib()
+        self.h = _vp()
+        self.L.check(self.L.scihpc_unet_create(h, w, seed, ctypes.byref(self.h)))
+        n = ctypes.c_longlong(0)
+        self.L.check(self.L.scihpc_unet_num_params(self.h, ctypes.byref(n)))
+        self.nparam = n.value
+
+    def close(self):
+        if self.h:
+            self.L.scihpc_unet_destroy(self.h)
+            self.h = _vp()
+
+    __del__ = close
+
+    def weights(self):
+        import numpy as np
+        a = np.zeros(self.nparam, dtype=np.float32)
+        self.L.check(self.L.scihpc_unet_get_weights(self.h, a.ctypes.data, self.nparam))
+        return a
+
+    def gradient(self):
+        import numpy as np
+        a = np.zeros(self.nparam, dtype=np.float32)
+        self.L.check(self.L.scihpc_unet_get_gradient(self.h, a.ctypes.data, self.nparam))
+        return a
+
+    def set_weights(self, a):
+        import numpy as np
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        self.L.check(self.L.scihpc_unet_set_weights(self.h, a.ctypes.data, self.nparam))
+
+    def infer(self, grid: Grid, rho, rhs, pprev, guess):
+        g = grid.c()
+        self.L.check(self.L.scihpc_unet_infer(self.h, ctypes.byref(g), _ptr(rho), _ptr(rhs), _ptr(pprev), _ptr(guess)))
+
+    def loss_grad(self, grid: Grid, rho, rhs, pprev, p) -> float:
+        g = grid.c()
+        loss = ctypes.c_double(0.0)
+        self.L.check(self.L.scihpc_unet_loss_grad(self.h, ctypes.byref(g), _ptr(rho), _ptr(rhs), _ptr(pprev), _ptr(p),
+                                                  ctypes.byref(loss)))
+        return loss.value
+
+    def train_step(self, grid: Grid, rho, rhs, pprev, p, lr: float) -> float:
+        g = grid.c()
+        loss = ctypes.c_double(0.0)
+        self.L.check(self.L.scihpc_unet_train_step(self.h, ctypes.byref(g), _ptr(rho), _ptr(rhs), _ptr(pprev), _ptr(p),
+                                                   ctypes.c_float(lr), ctypes.byref(loss)))
+        return loss.value

@@ -1,0 +1,149 @@
+"""Tensor-core convolutions and the learned pressure guess against the CPU restatement
+(oracle/unet_ref.py): single convolutions, their data and weight gradients, and the whole
+U-Net's loss and parameter gradient."""
+import numpy as np
+import pytest
+
+from oracle import unet_ref as R
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def bf16_tensor(a):
+    """float64 numpy array of BF16-representable values -> CUDA bfloat16 tensor (exact)."""
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(torch.bfloat16).cuda()
+
+
+def rel(a, b):
+    return np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300)
+
+
+# exact BF16 inputs, FP32 accumulation of up to 9 * 256 products per output (relative error
+# grows like sqrt(K) * 6e-8)
+FP32_SUM = 1e-5
+CONV_CASES = [(16, 24, 16, 16), (8, 40, 32, 64), (13, 11, 48, 192), (20, 20, 192, 16), (5, 7, 16, 256)]
+
+
+@pytest.mark.parametrize("h,w,ci,co", CONV_CASES)
+def test_conv_forward(h, w, ci, co):
+    from scihpc_gb300 import conv3x3
+    rng = np.random.default_rng(h * 100 + co)
+    x = R.bf16(rng.standard_normal((h * w, ci)))
+    wt = R.bf16(rng.standard_normal((co, 9, ci)) * 0.2)
+    b = rng.standard_normal(co).astype(np.float32)
+    out = torch.zeros((h * w, co), dtype=torch.float32, device="cuda")
+    for relu in (False, True):
+        conv3x3(bf16_tensor(x), bf16_tensor(wt), torch.from_numpy(b).cuda(), out, h, w, ci, co, relu)
+        ref = R.conv(x, wt, b.astype(np.float64), h, w, relu)
+        assert rel(out.cpu().numpy(), ref) <= FP32_SUM, (relu, rel(out.cpu().numpy(), ref))
+
+
+@pytest.mark.parametrize("h,w,ci,co", CONV_CASES)
+def test_conv_data_gradient(h, w, ci, co):
+    """Data gradient = the forward kernel on [ci][8 - t][co] weights."""
+    from scihpc_gb300 import conv3x3
+    rng = np.random.default_rng(7 + h + co)
+    dz = R.bf16(rng.standard_normal((h * w, co)))
+    wt = R.bf16(rng.standard_normal((co, 9, ci)) * 0.2)
+    wflip = np.ascontiguousarray(wt[:, ::-1, :].transpose(2, 1, 0))   # [ci][t][co] = w[co][8 - t][ci]
+    out = torch.zeros((h * w, ci), dtype=torch.float32, device="cuda")
+    conv3x3(bf16_tensor(dz), bf16_tensor(wflip), None, out, h, w, co, ci, False)
+    ref = R.conv_dgrad(dz, wt, h, w)
+    assert rel(out.cpu().numpy(), ref) <= FP32_SUM
+
+
+@pytest.mark.parametrize("h,w,ci,co", CONV_CASES)
+@pytest.mark.parametrize("splits", [1, 7])
+def test_conv_weight_gradient(h, w, ci, co, splits):
+    from scihpc_gb300 import conv3x3_wgrad
+    rng = np.random.default_rng(11 + w + ci)
+    x = R.bf16(rng.standard_normal((h * w, ci)))
+    dz = R.bf16(rng.standard_normal((h * w, co)))
+    dw = torch.zeros((co, 9, ci), dtype=torch.float32, device="cuda")
+    part = torch.zeros(splits * 9 * ci * co, dtype=torch.float32, device="cuda")
+    conv3x3_wgrad(bf16_tensor(x), bf16_tensor(dz), dw, part, splits, h, w, ci, co)
+    ref = R.conv_wgrad(x, dz, h, w)
+    assert rel(dw.cpu().numpy(), ref) <= FP32_SUM
+
+
+def _fields(g, rng):
+    """Ghosted 2D fields on g: density 1 + 2 H(interface), rhs, previous and new pressure."""
+    n0, n1 = g.n[0], g.n[1]
+    shape = (n0 + 6, n1 + 6, 1)
+    x = (np.arange(n0) + 0.5) / n0
+    y = (np.arange(n1) + 0.5) / n1
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    iface = 0.5 + 0.05 * np.sin(2 * np.pi * 2 * X + rng.uniform(0, 6.28))
+    rho = np.ones(shape)
+    rho[3:-3, 3:-3, 0] = 1.0 + 2.0 / (1.0 + np.exp(-(Y - iface) * n1 / 2.0))
+    rhs = np.zeros(shape)
+    rhs[3:-3, 3:-3, 0] = rng.standard_normal((n0, n1))
+    pprev = np.zeros(shape)
+    pprev[3:-3, 3:-3, 0] = np.cos(np.pi * X) * np.cos(2 * np.pi * Y) + 0.1 * rng.standard_normal((n0, n1))
+    pnew = pprev.copy()
+    pnew[3:-3, 3:-3, 0] += 0.05 * np.sin(np.pi * X) * rng.standard_normal((n0, n1))
+    return rho, rhs, pprev, pnew
+
+
+def test_unet_loss_and_gradient_match_oracle():
+    from scihpc_gb300 import Grid, UNet
+    import oracle as O
+    g = O.Grid(2, (32, 32), (0.0, 0.0), (1.0, 1.0))
+    rng = np.random.default_rng(3)
+    rho, rhs, pprev, pnew = _fields(g, rng)
+    net = UNet(32, 32, seed=0)
+    params = R.init_params(5)
+    params[-16:] = rng.standard_normal(16).astype(np.float32) * 0.1   # non-zero output bias
+    net.set_weights(params)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    torch.cuda.synchronize()
+    loss = net.loss_grad(Grid(2, (32, 32), (0.0, 0.0), (1.0, 1.0)), d(rho), d(rhs), d(pprev), d(pnew))
+    grad = net.gradient()
+    I = (slice(3, -3), slice(3, -3), 0)
+    x0, target, _ = R.pack(rho[I], rhs[I], pprev[I], pnew[I])
+    ref_loss, ref_grad, _ = R.loss_and_gradient(params.astype(np.float64), x0, target, 32, 32)
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss, (loss, ref_loss)
+    lay, _ = R.param_layout()
+    for k, (wo, bo) in enumerate(lay):
+        co = R.LAYERS[k][3]
+        ew = rel(grad[wo:bo], ref_grad[wo:bo])
+        eb = rel(grad[bo:bo + co], ref_grad[bo:bo + co])
+        # BF16 activations: a rounding that flips between the two accumulation orders moves a
+        # few entries by one BF16 ulp (0.4 %), and that spreads through the later layers
+        assert ew <= 3e-2 and eb <= 3e-2, (k, ew, eb)
+
+
+def test_unet_guess_is_previous_pressure_when_correction_is_zero():
+    """With the last layer's weights and bias at zero the guess is exactly pprev."""
+    from scihpc_gb300 import Grid, UNet
+    import oracle as O
+    g = O.Grid(2, (16, 24), (0.0, 0.0), (1.0, 1.5))
+    rho, rhs, pprev, _ = _fields(g, np.random.default_rng(1))
+    net = UNet(16, 24, seed=2)
+    p = net.weights()
+    lay, _ = R.param_layout()
+    p[lay[-1][0]:] = 0.0
+    net.set_weights(p)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    guess = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    net.infer(Grid(2, (16, 24), (0.0, 0.0), (1.0, 1.5)), d(rho), d(rhs), d(pprev), guess)
+    assert np.array_equal(guess.cpu().numpy(), pprev)
+
+
+def test_learned_guess_trains_and_keeps_the_solve_exact():
+    """Training on solver snapshots lowers the loss, and a solve started from the network's
+    guess still reaches the same tolerance (multigrid stays the judge of the result)."""
+    from scihpc_gb300 import UNet
+    from scihpc_gb300.learned import make_snapshots, solve_iterations, train
+    dev = torch.device("cuda")
+    tr = make_snapshots(64, range(32), torch, dev)
+    te = make_snapshots(64, range(1000, 1006), torch, dev)
+    net = UNet(64, 64, seed=0)
+    losses = train(net, tr, 300, 1e-3, torch)
+    assert np.mean(losses[-30:]) < 0.5 * np.mean(losses[:30]), (np.mean(losses[:30]), np.mean(losses[-30:]))
+    base, _ = solve_iterations(te, torch)
+    its, res = solve_iterations(te, torch, net)
+    assert max(res) <= 1e-10, res
+    assert max(its) <= max(base) + 2, (its, base)
