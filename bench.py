@@ -467,7 +467,7 @@ def learned_block(torch, n: int = 256, ntrain: int = 96, ntest: int = 12, steps:
     net = UNet(n, n, seed=0)
     torch.cuda.synchronize()
     t0 = _t.perf_counter()
-    losses = train(net, tr, steps, 1e-3, torch)
+    losses = train(net, tr, steps, 3e-4, torch)
     torch.cuda.synchronize()
     t_train = _t.perf_counter() - t0
     # inference time and its convolution work (2 * 9 * ci * co * pixels per layer)
