@@ -600,7 +600,19 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
     }
     for (double **p : {&H, &delta, &sign, &grad, &curv, &a_f, &b_f, &rho, &mu, &RHS, &s1, &s2, &s3, &t1, &t2, &work})
         ALLOC(*p);
+    for (int a = 0; a < D.ndim; ++a) {
+        ALLOC(fv_flux[a]);
+        ALLOC(tb1[a]);
+        ALLOC(tb2[a]);
+        if (a < D.ndim - 1)
+            for (int c = 0; c < D.ndim; ++c) ALLOC(fv[a][c]);
+    }
 #undef ALLOC
+    for (int k = 0; k < 3; ++k) {
+        SCIHPC_CUDA(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
+        SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
+    }
+    SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     SCIHPC_CUDA(cudaMalloc(&partial, 8 * RED_MAX_BLOCKS * sizeof(double)));
     allocs.push_back(partial);
     SCIHPC_CUDA(cudaMalloc(&sc, sizeof(StepScalars)));
@@ -630,8 +642,28 @@ void TwoPhaseGpu::destroy() {
     allocs.clear();
     if (sc_host) cudaFreeHost(sc_host);
     sc_host = nullptr;
+    for (int k = 0; k < 3; ++k) {
+        if (side[k]) cudaStreamDestroy(side[k]);
+        if (ev_join[k]) cudaEventDestroy(ev_join[k]);
+        side[k] = nullptr;
+        ev_join[k] = nullptr;
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    ev_fork = nullptr;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
+}
+
+void TwoPhaseGpu::fork(int n) {
+    cudaEventRecord(ev_fork, stream);
+    for (int k = 0; k < n; ++k) cudaStreamWaitEvent(side[k], ev_fork, 0);
+}
+
+void TwoPhaseGpu::join(int n) {
+    for (int k = 0; k < n; ++k) {
+        cudaEventRecord(ev_join[k], side[k]);
+        cudaStreamWaitEvent(stream, ev_join[k], 0);
+    }
 }
 
 double *TwoPhaseGpu::field(const std::string &s) {
@@ -711,13 +743,14 @@ void TwoPhaseGpu::find_dt() {
 
 void TwoPhaseGpu::convection_rhs(double *s) {
     const unsigned nbi = blocks_for(D.interior(), TPB);
-    if (scheme == 1) {
+    fork(D.ndim - 1);
+    for (int a = 0; a < D.ndim; ++a) {
+        cudaStream_t s = a == D.ndim - 1 ? stream : side[a];
         // identity_flux: flux = data; WENO reads data directly
-        for (int a = 0; a < D.ndim; ++a) launch_weno5(D, a, phi.data, nvel[a].data, phi.d1[a], stream);
-    } else {
-        for (int a = 0; a < D.ndim; ++a)
-            launch_uccd(D, ops, a, phi.data, nvel[a].data, phi.d1[a], phi.d2[a], t1, t2, stream);
+        if (scheme == 1) launch_weno5(D, a, phi.data, nvel[a].data, phi.d1[a], s);
+        else launch_uccd(D, ops, a, phi.data, nvel[a].data, phi.d1[a], phi.d2[a], tb1[a], tb2[a], s);
     }
+    join(D.ndim - 1);
     k_convection_s<<<nbi, TPB, 0, stream>>>(s, nvel[0].data, nvel[1].data, nvel[2].data, phi.d1[0], phi.d1[1],
                                             phi.d1[2], D);
 }
@@ -737,7 +770,10 @@ void TwoPhaseGpu::mpls(int count) {
     const int nb = red_blocks(D.interior());
     for (int c = 0; c < count; ++c) {
         launch_extrapolate(D, 0, phi.data, phi.flux, stream);
-        for (int a = 0; a < D.ndim; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], stream);
+        fork(D.ndim - 1);
+        for (int a = 0; a < D.ndim; ++a)
+            launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], a == D.ndim - 1 ? stream : side[a]);
+        join(D.ndim - 1);
         k_mpls_fields<<<nbf, TPB, 0, stream>>>(phi.data, phi.d1[0], phi.d1[1], phi.d1[2], work, H, delta, grad, rho, D,
                                                P.ls_width, P.density_ratio, P.positive_ref);
         k_mpls_sums<<<nb, RED_THREADS, 0, stream>>>(work, H, delta, grad, D, P.density_ratio, P.positive_ref, partial);
@@ -790,33 +826,52 @@ void TwoPhaseGpu::find_source() {
     for (int c = 0; c < D.ndim; ++c) k_copy<<<nbf, TPB, 0, stream>>>(src_old[c], src[c], N);
     k_props<<<nbf, TPB, 0, stream>>>(phi.data, H, delta, rho, mu, N, P.ls_width, P.density_ratio, P.viscosity_ratio,
                                      P.positive_ref);
-    launch_extrapolate(D, 0, phi.data, phi.flux, stream);
-    for (int a = 0; a < D.ndim; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], stream);
-    launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, stream);
-    if (D.ndim > 2) {
-        launch_ccd_mixed(D, ops, 2, phi.d1[1], phi.mixed[1], work, stream);
-        launch_ccd_mixed(D, ops, 0, phi.d1[2], phi.mixed[2], work, stream);
+    // branches: side[0] the level-set derivatives; side[1..] and the main stream one velocity
+    // direction each (the last direction on the main stream, in nvel)
+    const int nd = D.ndim;
+    fork(nd);
+    {
+        cudaStream_t s = side[0];
+        launch_extrapolate(D, 0, phi.data, phi.flux, s);
+        for (int a = 0; a < nd; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], s);
+        launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
+        if (nd > 2) {
+            launch_ccd_mixed(D, ops, 2, phi.d1[1], phi.mixed[1], work, s);
+            launch_ccd_mixed(D, ops, 0, phi.d1[2], phi.mixed[2], work, s);
+        }
+        if (P.We > 0.0) {
+            const double *d[9] = {phi.d1[0], phi.d1[1], phi.d1[2], phi.d2[0], phi.d2[1], phi.d2[2],
+                                  phi.mixed[0], phi.mixed[1], phi.mixed[2]};
+            launch_curvature(D, phi.data, d, curv, s);
+        }
     }
-    const double ref = P.positive_ref ? 1.0 : -1.0;
+    static const double zero[6] = {0, 0, 0, 0, 0, 0};
     const long long e2 = D.ndim == 3 ? D.N[2] - 2 : D.N[2];
     const long long nface = (long long)(D.N[0] - 2) * (D.N[1] - 2) * e2;
-    for (int a = 0; a < D.ndim; ++a) {
-        k_to_face<<<blocks_for(nface, TPB), TPB, 0, stream>>>(nvel[0].data, nvel[1].data, nvel[2].data, vel[0].data,
-                                                              vel[1].data, vel[2].data, D, a);
-        vel_bc(nvel, 1 + a);
+    for (int a = 0; a < nd; ++a) {
+        cudaStream_t s = a == nd - 1 ? stream : side[1 + a];
+        double *nv[3];
+        for (int c = 0; c < 3; ++c) nv[c] = a == nd - 1 || c >= nd ? nvel[c].data : fv[a][c];
+        k_to_face<<<blocks_for(nface, TPB), TPB, 0, s>>>(nv[0], nv[1], nv[2], vel[0].data, vel[1].data, vel[2].data, D,
+                                                         a);
+        for (int c = 0; c < nd; ++c) launch_bc_fill(D, 1 + a, vel_types[c], zero, nv[c], s);
         // convection of the a-component by the face-averaged velocity (source.cpp:8-40 with
         // identity_with_extrapolation_face_*)
         DevScalar &U = vel[a];
-        launch_extrapolate(D, 1 + a, U.data, U.flux, stream);
-        for (int b = 0; b < D.ndim; ++b) launch_uccd(D, ops, b, U.flux, nvel[b].data, U.d1[b], U.d2[b], t1, t2, stream);
-        k_convection_s<<<nbi, TPB, 0, stream>>>(src[a], nvel[0].data, nvel[1].data, nvel[2].data, U.d1[0], U.d1[1],
-                                                U.d1[2], D);
+        launch_extrapolate(D, 1 + a, U.data, U.flux, s);
+        for (int b = 0; b < nd; ++b) launch_uccd(D, ops, b, U.flux, nv[b], U.d1[b], U.d2[b], tb1[a], tb2[a], s);
+        k_convection_s<<<nbi, TPB, 0, s>>>(src[a], nv[0], nv[1], nv[2], U.d1[0], U.d1[1], U.d1[2], D);
         // cross derivatives of the other face-averaged components along a
-        for (int c = 0; c < D.ndim; ++c) {
+        for (int c = 0; c < nd; ++c) {
             if (c == a) continue;
-            launch_extrapolate(D, 1 + a, nvel[c].data, nvel[c].flux, stream);
-            launch_uccd(D, ops, a, nvel[c].flux, nvel[a].data, nvel[c].d1[a], nvel[c].d2[a], t1, t2, stream);
+            launch_extrapolate(D, 1 + a, nv[c], fv_flux[a], s);
+            launch_uccd(D, ops, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], tb1[a], tb2[a], s);
         }
+    }
+    join(nd);
+    const double ref = P.positive_ref ? 1.0 : -1.0;
+    for (int a = 0; a < nd; ++a) {
+        DevScalar &U = vel[a];
         StressArgs S;
         S.delta = delta, S.mu = mu, S.rho = rho;
         S.pfx = phi.d1[0], S.pfy = phi.d1[1], S.pfz = phi.d1[2];
@@ -828,11 +883,6 @@ void TwoPhaseGpu::find_source() {
         S.src = src[a];
         S.ref = ref, S.vr = P.viscosity_ratio, S.Re = P.Re;
         k_stress<<<nbi, TPB, 0, stream>>>(S, D, a);
-    }
-    if (P.We > 0.0) {
-        const double *d[9] = {phi.d1[0], phi.d1[1], phi.d1[2], phi.d2[0], phi.d2[1], phi.d2[2],
-                              phi.mixed[0], phi.mixed[1], phi.mixed[2]};
-        launch_curvature(D, phi.data, d, curv, stream);
     }
     k_forces<<<nbi, TPB, 0, stream>>>(src[0], src[1], src[2], curv, delta, rho, phi.d1[0], phi.d1[1], phi.d1[2], D,
                                       P.Fr, P.We);

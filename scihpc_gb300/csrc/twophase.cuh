@@ -68,6 +68,16 @@ private:
     void reinit_stage(int stage);
     int capture_step();
 
+    // independent work of one stage runs as parallel branches on side streams (fork/join by
+    // events; the branches become parallel nodes when the step is captured as a graph)
+    void fork(int n);
+    void join(int n);
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
+    // per-direction face-averaged velocities of find_source for the directions other than the
+    // last (that one uses nvel, as before), their extrapolation scratch and line-solve scratch
+    double *fv[3][3] = {}, *fv_flux[3] = {}, *tb1[3] = {}, *tb2[3] = {};
+
     HostParams P{};
     int scheme = 1, n_mpls = 5, reinit_every = 1, fp32 = 0, reinit_lambda = 1;
     int step_count = 0;
