@@ -35,6 +35,7 @@ Dims make_dims(const scihpc_grid *g) {
         D.n[a] = act ? g->n[a] : 1;
         D.N[a] = act ? g->n[a] + 2 * GHC : 1;
         D.d[a] = act ? (g->hi[a] - g->lo[a]) / static_cast<double>(g->n[a]) : 0.0;
+        D.rd[a] = act ? 1.0 / D.d[a] : 0.0;
         D.lo[a] = act ? g->lo[a] : 0.0;
     }
     D.s[2] = 1;

@@ -25,6 +25,7 @@ struct Dims {
     int N[3];         // with ghosts (1 on inactive axes)
     long long s[3];   // element strides
     double d[3];      // spacing (0 on inactive axes)
+    double rd[3];     // 1.0 / d, rounded once on the host (0 on inactive axes)
     double h, dv;     // min spacing, cell volume (structured_grid.cpp:7-134)
     double lo[3];
 

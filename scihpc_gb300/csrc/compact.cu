@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(128) line_kernel(const double *__restrict__ in
     const long long base = D.at(idx[0], idx[1], idx[2]);
     const long long st = D.s[a];
     const int n = D.N[a];
-    const double ih = 1.0 / D.d[a];
+    const double ih = D.rd[a];
     const double *f = in + base;
     double s0, ss0, sn, ssn;
     end_rhs(f, st, n, ih, s0, ss0, sn, ssn);
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(128) mixed_kernel(double *__restrict__ src, do
     const long long base = D.at(idx[0], idx[1], idx[2]);
     const long long st = D.s[a];
     const int n = D.N[a];
-    const double ih = 1.0 / D.d[a];
+    const double ih = D.rd[a];
     double *f = src + base;
     const double lo = f[(long long)GHC * st], hi = f[(long long)(n - 1 - GHC) * st];
     for (int q = 0; q < GHC; ++q) {

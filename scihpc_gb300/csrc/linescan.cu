@@ -49,9 +49,9 @@ __device__ __forceinline__ Aff shfl_down(const Aff &a, int d) {
 
 // One system: rhs r[k] (2-vectors) of the lane's points lo .. lo+cnt-1 in, solution out
 // (in place).  tab: per point {L00 L01 L10 L11, K00 K01 K10 K11, D00 D01 D10 D11}.
-template <int CM>
+template <int CM, int WPL>
 __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM], const double *__restrict__ tab,
-                                             int lo, int cnt, int n, int lane) {
+                                             int lo, int cnt, int n, int lane, int warp, Aff *sh) {
     // forward: chunk map, warp inclusive scan, replay
     Aff F = aff_identity();
 #pragma unroll
@@ -72,8 +72,24 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
         const Aff o = shfl_up(F, d);
         if (lane >= d) F = compose(F, o);
     }
+    // with several warps per line, warp w enters with the composition of warps 0 .. w-1
+    Aff Pw = aff_identity();
+    if (WPL > 1) {
+        if (lane == 31) sh[warp] = F;
+        __syncthreads();
+        for (int v = 0; v < warp; ++v) Pw = compose(sh[v], Pw);
+        __syncthreads();
+    }
     const Aff P = shfl_up(F, 1);
-    double v0 = P.c0, v1 = P.c1;   // v at lo-1 (unused by lane 0)
+    double v0 = P.c0, v1 = P.c1;   // v at lo-1 (unused by the lane holding point 0)
+    if (WPL > 1) {
+        if (lane == 0) {
+            v0 = Pw.c0, v1 = Pw.c1;
+        } else {
+            v0 = P.m00 * Pw.c0 + P.m01 * Pw.c1 + P.c0;
+            v1 = P.m10 * Pw.c0 + P.m11 * Pw.c1 + P.c1;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
@@ -110,8 +126,23 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
         const Aff o = shfl_down(G, d);
         if (lane + d < 32) G = compose(G, o);
     }
+    Aff Sw = aff_identity();   // composition of the warps after this one
+    if (WPL > 1) {
+        if (lane == 0) sh[warp] = G;
+        __syncthreads();
+        for (int v = WPL - 1; v > warp; --v) Sw = compose(sh[v], Sw);
+        __syncthreads();
+    }
     const Aff Q = shfl_down(G, 1);
     double x0 = Q.c0, x1 = Q.c1;   // x at lo+cnt (unused by the lane holding n-1)
+    if (WPL > 1) {
+        if (lane == 31) {
+            x0 = Sw.c0, x1 = Sw.c1;
+        } else {
+            x0 = Q.m00 * Sw.c0 + Q.m01 * Sw.c1 + Q.c0;
+            x1 = Q.m10 * Sw.c0 + Q.m11 * Sw.c1 + Q.c1;
+        }
+    }
 #pragma unroll
     for (int k = CM - 1; k >= 0; --k) {
         if (k < cnt) {
@@ -133,15 +164,18 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
 // MODE 0: CCD (f1 = f', f2 = f''); MODE 1: UCCD (f1 = upwind-selected f', f2 = mean f'');
 // MODE 2: mixed derivative -- `io` is first zero-order extrapolated along the line in place,
 // f1 = its CCD first derivative.
-template <int MODE, int CM>
+// WPL == 1: each warp of the block solves its own line.  WPL > 1: the block's WPL warps solve
+// one line together (shorter chunks per lane, and the per-warp maps combined in shared memory).
+template <int MODE, int CM, int WPL>
 __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, const double *__restrict__ vel,
                                                    double *__restrict__ f1, double *__restrict__ f2,
                                                    const double *__restrict__ tabA, const double *__restrict__ tabB,
                                                    Dims D, int a, int fast, int slow) {
-    const int lane = threadIdx.x & 31;
-    const long long line = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    __shared__ Aff sh[WPL > 1 ? WPL : 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long line = WPL > 1 ? (long long)blockIdx.x : (long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const long long nf = D.N[fast], ns = D.N[slow];
-    if (line >= nf * ns) return;   // uniform per warp
+    if (line >= nf * ns) return;   // uniform per warp (per block when WPL > 1)
     int idx[3];
     idx[a] = 0;
     idx[fast] = int(line % nf);
@@ -149,9 +183,9 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
     const long long base = D.at(idx[0], idx[1], idx[2]);
     const long long st = D.s[a];
     const int n = D.N[a];
-    const double ih = 1.0 / D.d[a];
-    const int C = (n + 31) >> 5;
-    const int lo = lane * C;
+    const double ih = D.rd[a];
+    const int C = (n + 32 * WPL - 1) / (32 * WPL);
+    const int lo = (WPL > 1 ? int(threadIdx.x) : lane) * C;
     const int cnt = lo >= n ? 0 : (lo + C <= n ? C : n - lo);
     double *f = io + base;
     auto src = [&](int i) -> int {
@@ -206,8 +240,8 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
             if (k < cnt && (i < GHC || i > n - 1 - GHC)) f[(long long)i * st] = F(i);
         }
     }
-    solve_system<CM>(r0, r1, tabA, lo, cnt, n, lane);
-    if (MODE == 1) solve_system<CM>(q0, q1, tabB, lo, cnt, n, lane);
+    solve_system<CM, WPL>(r0, r1, tabA, lo, cnt, n, lane, warp, sh);
+    if (MODE == 1) solve_system<CM, WPL>(q0, q1, tabB, lo, cnt, n, lane, warp, sh);
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
@@ -231,16 +265,37 @@ bool launch_scan(const Dims &D, int a, double *io, const double *vel, double *f1
     const int b = (a + 1) % 3, c = (a + 2) % 3;
     const int fast = b > c ? b : c, slow = b > c ? c : b;
     const long long lines = (long long)D.N[b] * D.N[c];
-    // The solve is FP64-pipe bound, so the lines are spread over as many SMs as possible:
-    // one warp per block until there are several lines for every SM, then up to eight.
+    const int n = D.N[a];
+    // Each lane's chunk is an FP64 dependency chain.  When there are few lines (fewer than a
+    // few per SM) several warps share a line: shorter chains and more warps in flight.
+    int wpl = 1;
+    if (lines < 4LL * NUM_SMS) wpl = n >= 192 ? 4 : (n >= 96 ? 2 : 1);
+    const int C = (n + 32 * wpl - 1) / (32 * wpl);
+    if (wpl > 1) {
+        const unsigned blocks = unsigned(lines);
+        const int tpb = 32 * wpl;
+#define SCAN_WPL(W)                                                                                              \
+    if (C <= 2) scan_kernel<MODE, 2, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);        \
+    else if (C <= 4) scan_kernel<MODE, 4, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);   \
+    else if (C <= 8) scan_kernel<MODE, 8, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);   \
+    else if (C <= 16) scan_kernel<MODE, 16, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow); \
+    else return false;
+        if (wpl == 2) {
+            SCAN_WPL(2)
+        } else {
+            SCAN_WPL(4)
+        }
+#undef SCAN_WPL
+        return true;
+    }
+    // many lines: one warp per line, up to eight lines per block
     int wpb = 1;
     while (wpb < 8 && lines >= (long long)wpb * 2 * 4 * NUM_SMS) wpb *= 2;
     const unsigned blocks = unsigned((lines + wpb - 1) / wpb);
     const int tpb = 32 * wpb;
-    const int C = (D.N[a] + 31) / 32;
-    if (C <= 4) scan_kernel<MODE, 4><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
-    else if (C <= 8) scan_kernel<MODE, 8><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
-    else if (C <= 16) scan_kernel<MODE, 16><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    if (C <= 4) scan_kernel<MODE, 4, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    else if (C <= 8) scan_kernel<MODE, 8, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    else if (C <= 16) scan_kernel<MODE, 16, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
     else return false;
     return true;
 }

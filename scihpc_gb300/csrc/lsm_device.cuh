@@ -44,7 +44,7 @@ __device__ __forceinline__ double godunov_at(const double *__restrict__ phi, lon
     double g2 = 0.0;
     for (int a = 0; a < D.ndim; ++a) {
         const long long st = D.s[a];
-        const double ih = 1.0 / D.d[a];
+        const double ih = D.rd[a];
         const double m3 = phi[o - 3 * st], m2 = phi[o - 2 * st], m1 = phi[o - st], c0 = phi[o];
         const double p1 = phi[o + st], p2 = phi[o + 2 * st], p3 = phi[o + 3 * st];
         const double v = ih * (1.0 / 12.0) * (-(m1 - m2) + 7.0 * (c0 - m1) + 7.0 * (p1 - c0) - (p2 - p1));
