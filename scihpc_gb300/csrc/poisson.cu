@@ -27,6 +27,9 @@
 
 #include "poisson.cuh"
 #include "reduce.cuh"
+#include "tc.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace scihpc {
 
@@ -350,7 +353,7 @@ __device__ __forceinline__ void outer_progress(PcgScalars *st, double tol, int m
     } else {
         st->since_best += 1;
     }
-    if (!(rel == rel) || isinf(rel)) st->diverged = 1;
+    if (!(rel == rel) || isinf(rel) || st->sweep_err) st->diverged = 1;
     st->done = (rel <= tol || st->it >= max_iter || st->diverged || st->since_best >= 3) ? 1 : 0;
 }
 
@@ -410,7 +413,13 @@ __global__ void k_relres(PcgScalars *st) { st->relres = st->bb > 0.0 ? sqrt(st->
 // Division inside the preconditioner.  The FP32 cycle only has to be the same linear map
 // on every application, not correctly rounded, so it takes the fast approximate divide
 // (+inf denominators from the padded halo still give 0); FP64 divides exactly.
-__device__ __forceinline__ float pdiv(float a, float b) { return __fdividef(a, b); }
+// approximate reciprocal (one special-function-unit instruction; +inf gives 0)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float pdiv(float a, float b) { return a * rcp_approx(b); }
 __device__ __forceinline__ double pdiv(double a, double b) { return a / b; }
 
 template <class T, int MODE>
@@ -519,7 +528,7 @@ struct SweepCoef {
     T dinv;
 };
 
-__device__ __forceinline__ float prcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ float prcp(float x) { return rcp_approx(x); }
 __device__ __forceinline__ double prcp(double x) { return 1.0 / x; }
 
 // Gauss-Seidel value (b + sum_f C_f x_f) / sum_f C_f of the cell at padded offset `off`.
@@ -618,6 +627,246 @@ __global__ void __launch_bounds__(SW_THREADS, 2) k_sweep3(Level<T> L, const T *_
     }
 }
 
+// k_sweep3 for the finest FP32 level with face coefficients from the padded density
+// (MODE 1), with the planes staged in shared memory by TMA.  The block, the thread layout and
+// the order of the updates are those of k_sweep3 (first colour of plane i from the old
+// iterate, second colour of plane i-1 from the first-colour values on chip, a recomputed
+// ring); what changes is where the operands come from.  One thread streams boxes of
+// TS_H x TS_W cells of the old iterate, the density and the right-hand side, plane by plane,
+// into a ring of TS_STAGES stages (each completing on its own mbarrier), three planes ahead
+// of the planes being updated, and every neighbour value is then a shared-memory load at a
+// constant offset.  The box covers the tile, the ring and the ring's neighbours; it starts
+// four columns before the tile so that its first column is 16-byte aligned (the level's row
+// pitch is a multiple of four cells).  Cells of the box outside the padded level read zero,
+// and only cells outside the domain, whose values are discarded, look at them.
+constexpr int TS_W = SW_TK + 8;       // box columns: padded k from tk * SW_TK - 4
+constexpr int TS_H = SW_TJ + 4;       // box rows: padded j from tj * SW_TJ - 1
+constexpr int TS_PLANE = TS_W * TS_H;   // cells of one box
+constexpr int TS_STAGES = 6;
+constexpr size_t TS_SMEM = size_t(TS_STAGES) * 3 * TS_PLANE * sizeof(float) + 128;
+constexpr int TS_WAIT_LIMIT = 1 << 22;
+
+// out-of-place sweep of level 0; ZERO: the old iterate is zero (not loaded).  err: set when
+// a staged plane did not arrive within the wait limit (the sweep's output is then invalid).
+template <bool ZERO>
+__global__ void __launch_bounds__(SW_THREADS, 2)
+    k_sweep3_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_rho,
+                 const __grid_constant__ CUtensorMap map_b, Level<float> L, float *__restrict__ xn,
+                 SweepCoef<float> cf, int c0, int ci, int *err) {
+    extern __shared__ unsigned char ts_raw[];
+    __shared__ uint64_t bar[TS_STAGES];
+    __shared__ float first[2][SW_ROWS][SW_PAIRS];
+    float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
+    const int tid = threadIdx.x;
+    const int row = tid / SW_PAIRS, pr = tid - row * SW_PAIRS;
+    const int tiles_k = (L.n[2] + SW_TK - 1) / SW_TK;
+    const int tk = blockIdx.x % tiles_k, tj = blockIdx.x / tiles_k;
+    const int i0 = blockIdx.y * ci;
+    const int i1 = min(i0 + ci, L.n[0]);
+    const int nq = i1 - i0 + 4;   // staged planes i0 - 2 .. i1 + 1
+    const int j = tj * SW_TJ + row - 1;
+    const int kbase = tk * SW_TK + 2 * (pr - 1);
+    const bool inner = row >= 1 && row <= SW_TJ && pr >= 1 && pr <= SW_PAIRS - 2;
+    const bool jin = j >= 0 && j < L.n[1];
+    const int s0 = int(L.s[0]), s1 = int(L.s[1]);
+    const int col = (j + 1) * s1 + kbase + 1;   // padded offset of (i = -1, j, kbase)
+    const int sc = (row + 1) * TS_W + 2 * pr + 3;   // box offset of (j, kbase)
+    const uint32_t tx_bytes = (ZERO ? 2u : 3u) * uint32_t(TS_PLANE * sizeof(float));
+    auto issue = [&](int q) {
+        const int st = q % TS_STAGES;
+        float *base = tiles + st * 3 * TS_PLANE;
+        const int z = i0 - 1 + q;   // padded i of staged plane q
+        tc::mbar_expect_tx(&bar[st], tx_bytes);
+        if (!ZERO) tc::tma_load_3d(base, &map_x, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+        tc::tma_load_3d(base + TS_PLANE, &map_rho, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+        tc::tma_load_3d(base + 2 * TS_PLANE, &map_b, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+    };
+    auto wait_plane = [&](int q) {
+        return tc::mbar_wait(&bar[q % TS_STAGES], uint32_t((q / TS_STAGES) & 1), TS_WAIT_LIMIT);
+    };
+    // stage offsets of planes q - 2, q - 1, q, q + 1, rotated once per step
+    constexpr int SST = 3 * TS_PLANE;
+    int om2 = (TS_STAGES - 1) * SST, om1 = 0, oc0 = SST, op1 = 2 * SST;
+    // Thread 0 alone waits on the barriers (the others would spend issue slots polling) and
+    // the block barrier that follows passes the arrival on.
+    const int issued_pre = min(TS_STAGES, nq) - 1;
+    int issued = issued_pre;   // planes 0 .. issued have been requested
+    int waited = -1;           // planes 0 .. waited have arrived (thread 0)
+    bool ok = true;
+    if (tid == 0) {
+        for (int st = 0; st < TS_STAGES; ++st) tc::mbar_init(&bar[st], 1);
+        for (int q = 0; q <= issued_pre; ++q) issue(q);
+        for (int q = 0; q <= 2 && ok; ++q)
+            if ((ok = wait_plane(q))) waited = q;
+    }
+    const float w0 = cf.w[0], w1 = cf.w[1], w2 = cf.w[2];
+    float f1 = 0, f2 = 0;   // this pair's first-colour values at planes i-1 and i-2
+    bool fail = __syncthreads_or(!ok);
+    for (int q = 1; q <= nq - 2 && !fail; ++q) {
+        // planes q - 2 .. q + 1 are on chip
+        const int i = i0 - 2 + q;
+        const int par = (i + j + c0) & 1;
+        const int k = kbase + par;
+        const bool kin = jin && k >= 0 && k < L.n[2];
+        const bool fvalid = kin && i >= 0 && i < L.n[0];
+        const int o = sc + par;
+        const float *Xc = tiles + oc0, *Xm = tiles + om1, *Xp = tiles + op1;
+        const float *Rc = Xc + TS_PLANE, *Rm = Xm + TS_PLANE, *Rp = Xp + TS_PLANE;
+        // first colour of plane i from the old iterate
+        const float rc = Rc[o], rim = Rm[o];
+        const float cim = w0 * prcp(rc + rim);   // face (i-1, i), shared with the update below
+        const float C1 = w0 * prcp(rc + Rp[o]);
+        const float C2 = w1 * prcp(rc + Rc[o - TS_W]), C3 = w1 * prcp(rc + Rc[o + TS_W]);
+        const float C4 = w2 * prcp(rc + Rc[o - 1]), C5 = w2 * prcp(rc + Rc[o + 1]);
+        float sx = 0;
+        if (!ZERO)
+            sx = cim * Xm[o] + C1 * Xp[o] + C2 * Xc[o - TS_W] + C3 * Xc[o + TS_W] + C4 * Xc[o - 1] + C5 * Xc[o + 1];
+        const float fa = (Xc[2 * TS_PLANE + o] + sx) * prcp(cim + C1 + C2 + C3 + C4 + C5);
+        const float fi = fvalid ? fa : 0.0f;
+        const int off = (i + 1) * s0 + col + par;
+        if (inner && fvalid && i >= i0 && i < i1) xn[off] = fi;
+        first[q & 1][row][pr] = fi;
+        // second colour of plane i-1 from the first-colour values of planes i-2, i-1, i
+        const int ib = i - 1;
+        if (inner && kin && ib >= i0 && ib < i1) {
+            const int qb = (q - 1) & 1;
+            const float *Rmm = tiles + om2 + TS_PLANE;
+            const float nbm = first[qb][row][pr - 1], nbp = first[qb][row][pr + 1];
+            const float n4 = par == 0 ? nbm : f1, n5 = par == 0 ? f1 : nbp;
+            const float D0 = w0 * prcp(rim + Rmm[o]);
+            const float D2 = w1 * prcp(rim + Rm[o - TS_W]), D3 = w1 * prcp(rim + Rm[o + TS_W]);
+            const float D4 = w2 * prcp(rim + Rm[o - 1]), D5 = w2 * prcp(rim + Rm[o + 1]);
+            const float sb = D0 * f2 + cim * fi + D2 * first[qb][row - 1][pr] + D3 * first[qb][row + 1][pr] + D4 * n4 +
+                             D5 * n5;
+            xn[off - s0] = (Xm[2 * TS_PLANE + o] + sb) * prcp(D0 + cim + D2 + D3 + D4 + D5);
+        }
+        f2 = f1;
+        f1 = fi;
+        om2 = om1, om1 = oc0, oc0 = op1;
+        op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
+        if (tid == 0 && q + 2 <= nq - 1)
+            if ((ok = wait_plane(q + 2))) waited = q + 2;
+        if ((fail = __syncthreads_or(!ok))) break;
+        // plane q - 2 is no longer needed: its stage takes plane q - 2 + TS_STAGES
+        if (q >= 2 && q - 2 + TS_STAGES < nq) {
+            issued = q - 2 + TS_STAGES;
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(q - 2 + TS_STAGES);
+            }
+        }
+    }
+    if (fail) {
+        // a plane never arrived: report, and let the copies still in flight land (each wait
+        // again bounded) before the block exits
+        if (tid == 0) {
+            atomicExch(err, 1);
+            for (int q = waited + 1; q <= issued; ++q) wait_plane(q);
+        }
+        __syncthreads();
+    }
+}
+
+// Residual + restriction of the finest FP32 level (MODE 1, ratio 2) with the planes of x, the
+// density and b staged in shared memory by TMA, in the boxes of k_sweep3_tma (same tensor
+// maps).  A block owns SW_TJ x SW_TK fine columns and a chunk of planes starting at an even
+// plane; a thread owns a 2 x 2 group of fine columns (one coarse column), adds the residuals
+// of its four fine cells plane by plane and, after every second plane, writes the coarse
+// right-hand side (the mean of the eight residuals) and clears the coarse iterate.  The
+// residual arithmetic is that of residual_at.
+constexpr int RT_THREADS = (SW_TJ / 2) * (SW_TK / 2);   // 256
+
+__global__ void __launch_bounds__(RT_THREADS)
+    k_restrict3_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_rho,
+                    const __grid_constant__ CUtensorMap map_b, Level<float> F, Level<float> Cl, Id2<float> id2, int ci,
+                    int *err) {
+    extern __shared__ unsigned char ts_raw[];
+    __shared__ uint64_t bar[TS_STAGES];
+    float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
+    const int tid = threadIdx.x;
+    const int jc = tid / (SW_TK / 2), kc = tid - jc * (SW_TK / 2);   // coarse row / column in the tile
+    const int tiles_k = (F.n[2] + SW_TK - 1) / SW_TK;
+    const int tk = blockIdx.x % tiles_k, tj = blockIdx.x / tiles_k;
+    const int i0 = blockIdx.y * ci;   // ci is even
+    const int i1 = min(i0 + ci, F.n[0]);
+    const int nq = i1 - i0 + 2;   // staged planes i0 - 1 .. i1
+    const int j = tj * SW_TJ + 2 * jc, k = tk * SW_TK + 2 * kc;   // first fine cell of the group
+    const bool live = j < F.n[1] && k < F.n[2];
+    const int sc = (2 * jc + 2) * TS_W + 2 * kc + 5;   // box offset of (j, k)
+    const uint32_t tx_bytes = 3u * uint32_t(TS_PLANE * sizeof(float));
+    auto issue = [&](int q) {
+        const int st = q % TS_STAGES;
+        float *base = tiles + st * 3 * TS_PLANE;
+        const int z = i0 + q;   // padded i of staged plane q (interior i0 - 1 + q)
+        tc::mbar_expect_tx(&bar[st], tx_bytes);
+        tc::tma_load_3d(base, &map_x, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+        tc::tma_load_3d(base + TS_PLANE, &map_rho, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+        tc::tma_load_3d(base + 2 * TS_PLANE, &map_b, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+    };
+    auto wait_plane = [&](int q) {
+        return tc::mbar_wait(&bar[q % TS_STAGES], uint32_t((q / TS_STAGES) & 1), TS_WAIT_LIMIT);
+    };
+    constexpr int SST = 3 * TS_PLANE;
+    int om1 = 0, oc0 = SST, op1 = 2 * SST;   // stage offsets of planes q - 1, q, q + 1
+    const int issued_pre = min(TS_STAGES, nq) - 1;
+    int issued = issued_pre, waited = -1;
+    bool ok = true;
+    if (tid == 0) {   // thread 0 alone waits (see k_sweep3_tma)
+        for (int st = 0; st < TS_STAGES; ++st) tc::mbar_init(&bar[st], 1);
+        for (int q = 0; q <= issued_pre; ++q) issue(q);
+        for (int q = 0; q <= 2 && ok; ++q)
+            if ((ok = wait_plane(q))) waited = q;
+    }
+    const float c0 = id2.v[0], c1 = id2.v[1], c2 = id2.v[2];
+    float acc = 0;
+    bool fail = __syncthreads_or(!ok);
+    for (int q = 1; q <= nq - 2 && !fail; ++q) {
+        // planes q - 1 .. q + 1 are on chip
+        const float *Xc = tiles + oc0, *Xm = tiles + om1, *Xp = tiles + op1;
+        const float *Rc = Xc + TS_PLANE, *Rm = Xm + TS_PLANE, *Rp = Xp + TS_PLANE, *Bc = Xc + 2 * TS_PLANE;
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                const int o = sc + dj * TS_W + dk;
+                const float rc = Rc[o], xc = Xc[o];
+                const float C0 = pdiv(2.0f, rc + Rm[o]) * c0, C1 = pdiv(2.0f, rc + Rp[o]) * c0;
+                const float C2 = pdiv(2.0f, rc + Rc[o - TS_W]) * c1, C3 = pdiv(2.0f, rc + Rc[o + TS_W]) * c1;
+                const float C4 = pdiv(2.0f, rc + Rc[o - 1]) * c2, C5 = pdiv(2.0f, rc + Rc[o + 1]) * c2;
+                float sres = C0 * (xc - Xm[o]) + C1 * (xc - Xp[o]) + C2 * (xc - Xc[o - TS_W]) + C3 * (xc - Xc[o + TS_W]);
+                sres += C4 * (xc - Xc[o - 1]) + C5 * (xc - Xc[o + 1]);
+                acc += Bc[o] - sres;
+            }
+        const int i = i0 - 1 + q;
+        if ((i & 1) && live) {
+            const long long Pc = (long long)((i >> 1) + 1) * Cl.s[0] + (long long)((j >> 1) + 1) * Cl.s[1] + (k >> 1) + 1;
+            Cl.b[Pc] = pdiv(acc, 8.0f);
+            Cl.x[Pc] = 0;
+        }
+        if (i & 1) acc = 0;
+        om1 = oc0, oc0 = op1;
+        op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
+        if (tid == 0 && q + 2 <= nq - 1)
+            if ((ok = wait_plane(q + 2))) waited = q + 2;
+        if ((fail = __syncthreads_or(!ok))) break;
+        // plane q - 1 is no longer needed: its stage takes plane q - 1 + TS_STAGES
+        if (q + TS_STAGES - 1 < nq) {
+            issued = q + TS_STAGES - 1;
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(q + TS_STAGES - 1);
+            }
+        }
+    }
+    if (fail) {
+        if (tid == 0) {
+            atomicExch(err, 1);
+            for (int q = waited + 1; q <= issued; ++q) wait_plane(q);
+        }
+        __syncthreads();
+    }
+}
+
 // Planes per block for k_sweep3: balances whole waves of blocks against the two planes
 // every chunk recomputes.
 inline int sweep_chunk(const int n[3]) {
@@ -627,6 +876,21 @@ inline int sweep_chunk(const int n[3]) {
     int best_ci = n[0];
     for (int nch = 1; nch <= n[0]; ++nch) {
         const int ci = (n[0] + nch - 1) / nch;
+        const long long ctas = tiles * ((n[0] + ci - 1) / ci);
+        const long long cost = ((ctas + slots - 1) / slots) * (ci + 2);
+        if (best < 0 || cost < best) best = cost, best_ci = ci;
+    }
+    return best_ci;
+}
+
+// Planes per block for k_restrict3_tma: an even number (blocks start on a coarse plane),
+// balancing whole waves of blocks against the two halo planes every chunk stages.
+inline int restrict_chunk(const int n[3]) {
+    const long long tiles = (long long)((n[2] + SW_TK - 1) / SW_TK) * ((n[1] + SW_TJ - 1) / SW_TJ);
+    const long long slots = 2LL * NUM_SMS;
+    long long best = -1;
+    int best_ci = n[0] + (n[0] & 1);
+    for (int ci = 2; ci <= n[0] + 1; ci += 2) {
         const long long ctas = tiles * ((n[0] + ci - 1) / ci);
         const long long cost = ((ctas + slots - 1) / slots) * (ci + 2);
         if (best < 0 || cost < best) best = cost, best_ci = ci;
@@ -722,6 +986,19 @@ __global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
     prolong_one<T, DIM>(F, Cl, neumann, linear, t);
 }
 
+// Piecewise-constant prolongation of a 3D level with ratio 2, p_fine += e_coarse(parent):
+// the block grid spans (k, j, i) directly (no index division), so the pass runs at the
+// speed of the fine-level traffic.
+constexpr int PR_BX = 64, PR_BY = 4;
+template <class T>
+__global__ void __launch_bounds__(PR_BX *PR_BY) k_prolong3_pc(Level<T> F, Level<T> Cl) {
+    const int k = blockIdx.x * PR_BX + threadIdx.x, j = blockIdx.y * PR_BY + threadIdx.y, i = blockIdx.z;
+    if (k >= F.n[2] || j >= F.n[1]) return;
+    const long long Pf = (long long)(i + 1) * F.s[0] + (long long)(j + 1) * F.s[1] + k + 1;
+    const long long Pc = (long long)((i >> 1) + 1) * Cl.s[0] + (long long)((j >> 1) + 1) * Cl.s[1] + (k >> 1) + 1;
+    F.x[Pf] += Cl.x[Pc];
+}
+
 // coarse face coefficients from the fine level (mean over the fine faces of a coarse face,
 // divided by ratio^2).  Faces at padded index 0 .. n along the face axis (walls included).
 template <class T, int MODE, int DIM>
@@ -772,6 +1049,23 @@ __global__ void k_coarse_coef(Level<T> F, Level<T> Cl, const T *__restrict__ rho
     dst[Pc] = sum / T(cnt) / T(r * r);
 }
 
+// Padded coordinates of linear offset t of a level; false for the row-pitch cells beyond the
+// padded extent (3D level 0).
+template <int DIM, class T>
+__device__ __forceinline__ bool padded_index(const Level<T> &L, long long t, int pi[3]) {
+    if (DIM == 3) {
+        pi[0] = int(t / L.s[0]);
+        const long long r = t - (long long)pi[0] * L.s[0];
+        pi[1] = int(r / L.s[1]);
+        pi[2] = int(r - (long long)pi[1] * L.s[1]);
+        return pi[2] < L.P[2];
+    }
+    pi[2] = 0;
+    pi[1] = int(t % L.P[1]);
+    pi[0] = int(t / L.P[1]);
+    return true;
+}
+
 // Level-0 face coefficients from the padded density (+inf halo gives zero wall faces), for
 // the FP64 cycle: stored once per density update instead of divided out in every sweep.
 template <class T, int DIM>
@@ -779,17 +1073,11 @@ __global__ void k_level0_coef(Level<T> L, const T *__restrict__ rho) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= L.cells) return;
     int pi[3] = {0, 0, 0};
-    long long r = t;
-    if (DIM == 3) {
-        pi[2] = int(r % L.P[2]);
-        r /= L.P[2];
-    }
-    pi[1] = int(r % L.P[1]);
-    pi[0] = int(r / L.P[1]);
+    const bool real = padded_index<DIM>(L, t, pi);
     T *dst[3] = {L.cx, L.cy, L.cz};
     for (int a = 0; a < DIM; ++a) {
         T C = 0;
-        if (pi[a] + 1 < L.P[a]) C = T(2) / (rho[t] + rho[t + L.s[a]]) * T(1.0 / (L.d[a] * L.d[a]));
+        if (real && pi[a] + 1 < L.P[a]) C = T(2) / (rho[t] + rho[t + L.s[a]]) * T(1.0 / (L.d[a] * L.d[a]));
         dst[a][t] = C;
     }
 }
@@ -1303,10 +1591,13 @@ int Poisson::alloc_levels() {
             L.d[a] = dd[a];
         }
         L.s[2] = 1;
-        L.s[1] = L.P[2];
-        L.s[0] = (long long)L.P[1] * L.P[2];
+        // 3D level 0: rows padded to a multiple of four cells (16-byte aligned rows, as the
+        // tensor-memory-access descriptors of the staged sweep require); the extra cells are
+        // never part of a stencil
+        L.s[1] = (l == 0 && D.ndim == 3) ? (L.P[2] + 3) / 4 * 4 : L.P[2];
+        L.s[0] = (long long)L.P[1] * L.s[1];
         if (D.ndim == 2) L.s[2] = 0;
-        L.cells = (long long)L.P[0] * L.P[1] * L.P[2];
+        L.cells = (long long)L.P[0] * L.s[0];
         L.ratio = ratio[l];
         const size_t bytes = size_t(L.cells) * sizeof(T);
         SCIHPC_CUDA(cudaMalloc(&L.x, 2 * bytes));
@@ -1345,7 +1636,40 @@ int Poisson::alloc_levels() {
         e32 = q32 + Ls[0].cells;
     }
     SCIHPC_CUDA(cudaMalloc(&rho_pad, zbytes));
+    if constexpr (sizeof(T) == 4) {
+        if (D.ndim == 3) tma_ready = make_level0_maps(Ls[0]);
+    }
     return SCIHPC_OK;
+}
+
+// TMA descriptors of the FP32 level 0: boxes of TS_W x TS_H x 1 cells of x, x2, the padded
+// density and b.  Returns false (and the sweeps keep reading global memory directly) when
+// the driver has no tensor-map encoder or a descriptor is refused.
+bool Poisson::make_level0_maps(const Level<float> &L) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return false;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[3] = {cuuint64_t(L.s[1]), cuuint64_t(L.P[1]), cuuint64_t(L.P[0])};
+    const cuuint64_t strides[2] = {cuuint64_t(L.s[1]) * sizeof(float), cuuint64_t(L.s[0]) * sizeof(float)};
+    const cuuint32_t box[3] = {TS_W, TS_H, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    float *ptr[4] = {L.x, L.x2, static_cast<float *>(rho_pad), L.b};
+    for (int m = 0; m < 4; ++m) {
+        const CUresult r = encode(&tmap[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ptr[m], dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+    }
+    return true;
 }
 
 int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
@@ -1377,6 +1701,10 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_restrict3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    if (const char *e = std::getenv("SCIHPC_SWEEP_TMA")) tma_enable = std::atoi(e) != 0;
     if (!density) {
         // constant coefficients: build the hierarchy once (rho unused)
         cudaStream_t s = 0;
@@ -1414,14 +1742,8 @@ __global__ void k_pad_rho(const double *__restrict__ rho, T *__restrict__ out, D
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= L0.cells) return;
     int pi[3] = {0, 0, 0};
-    long long r = t;
-    if (D.ndim == 3) {
-        pi[2] = int(r % L0.P[2]);
-        r /= L0.P[2];
-    }
-    pi[1] = int(r % L0.P[1]);
-    pi[0] = int(r / L0.P[1]);
-    bool halo = false;
+    const bool real = D.ndim == 3 ? padded_index<3>(L0, t, pi) : padded_index<2>(L0, t, pi);
+    bool halo = !real;
     for (int a = 0; a < D.ndim; ++a) halo = halo || pi[a] == 0 || pi[a] == L0.P[a] - 1;
     if (halo) {
         out[t] = T(INFINITY);
@@ -1571,6 +1893,15 @@ void Poisson::vcycle(cudaStream_t s) {
             dsum += 2.0 / (D.d[a] * D.d[a]);
         }
         cf.dinv = T(1.0 / dsum);
+        if constexpr (sizeof(T) == 4) {
+            if (l == 0 && m == 1 && tma_ready && tma_enable) {
+                const CUtensorMap &mx = xo == Ls[0].x ? tmap[0] : tmap[1];
+                int *err = &dev_state->sweep_err;
+                if (zero) k_sweep3_tma<true><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], L, xn, cf, c0, ci, err);
+                else k_sweep3_tma<false><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], L, xn, cf, c0, ci, err);
+                return;
+            }
+        }
         if (m == 0) k_sweep3<T, 0><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
         else if (m == 2) k_sweep3<T, 2><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
         else if constexpr (sizeof(T) == 4) k_sweep3<T, 1><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
@@ -1597,6 +1928,16 @@ void Poisson::vcycle(cudaStream_t s) {
         const long long nc = (long long)Cl.n[0] * Cl.n[1] * Cl.n[2];
         const unsigned nb = blocks_for(nc, TPB);
         const int m = l == 0 ? mode0 : 0;
+        if constexpr (sizeof(T) == 4) {
+            if (l == 0 && m == 1 && tma_ready && tma_enable && F.ratio == 2 && fused(0)) {
+                const int ci = restrict_chunk(F.n);
+                const dim3 grid(unsigned(((F.n[2] + SW_TK - 1) / SW_TK) * ((F.n[1] + SW_TJ - 1) / SW_TJ)),
+                                unsigned((F.n[0] + ci - 1) / ci));
+                k_restrict3_tma<<<grid, RT_THREADS, TS_SMEM, s>>>(tmap[0], tmap[2], tmap[3], F, Cl, id2, ci,
+                                                                  &dev_state->sweep_err);
+                continue;
+            }
+        }
         if (D.ndim == 2) {
             if (m == 0) k_restrict<T, 0, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
             else if (m == 1) k_restrict<T, 1, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
@@ -1624,6 +1965,10 @@ void Poisson::vcycle(cudaStream_t s) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
         if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
+        else if (F.ratio == 2 && !prolong_linear && F.n[0] <= 65535 && F.n[1] <= 65535 * PR_BY)
+            k_prolong3_pc<T><<<dim3(unsigned((F.n[2] + PR_BX - 1) / PR_BX), unsigned((F.n[1] + PR_BY - 1) / PR_BY),
+                                    unsigned(F.n[0])),
+                               dim3(PR_BX, PR_BY), 0, s>>>(F, Cl);
         else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
         smooth_level(l, 1, false);
     }

@@ -4,6 +4,8 @@
 #include <type_traits>
 #include <vector>
 
+#include <cuda.h>
+
 #include "common.cuh"
 
 namespace scihpc {
@@ -40,6 +42,7 @@ struct PcgScalars {
     int in_it, pending;     // inner iterations since the last refinement; refinement due
     int in_break;           // the inner recurrence broke down (FP32 round-off)
     int restart;            // FP64 CG: the residual was replaced, next direction restarts
+    int sweep_err;          // a staged sweep timed out waiting for its planes
 };
 
 class Poisson {
@@ -86,6 +89,7 @@ private:
     int alloc_levels();
     template <class T>
     void build_coarse(cudaStream_t s);
+    bool make_level0_maps(const Level<float> &L);
     template <int DIM>
     void begin_dim(const double *rhs, double *p, int use_guess, cudaStream_t s);
     template <int DIM>
@@ -107,6 +111,10 @@ private:
     double *partial = nullptr;       // reduction scratch (2 x RED_MAX_BLOCKS)
     double *oc = nullptr;            // FP64 +face coefficients of the outer operator (3 compact arrays)
     double *dense = nullptr;         // coarsest-level inverse (n x n, FP64)
+    // TMA descriptors of the FP32 level 0 (3D): x, x2, padded density, b
+    CUtensorMap tmap[4];
+    bool tma_ready = false;
+    int tma_enable = 1;
     int ncoarse = 0;
     const double *rhs_ = nullptr;
     double *p_ = nullptr;

@@ -94,6 +94,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int l
     return false;
 }
 
+// the next phase of the barrier completes after one arrival and `bytes` of transaction data
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// TMA: one box of a 3D tensor map (x innermost) into shared memory, completing on `mbar`.
+// The box may start at negative or out-of-range coordinates (zero fill there); x times the
+// element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_3d(void *smem, const void *tmap, int x, int y, int z, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_u32(smem)),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // 16-byte asynchronous copy global -> shared; src_bytes 0 zero-fills the destination
 __device__ __forceinline__ void cp16(void *smem, const void *gmem, uint32_t src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem), "r"(src_bytes)
