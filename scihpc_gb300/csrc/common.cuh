@@ -62,7 +62,16 @@ void set_last_error(const char *msg);
 inline unsigned blocks_for(long long n, int threads) { return unsigned((n + threads - 1) / threads); }
 
 // Interior linear index q -> (I, J, K) with K fastest, matching the reference loop nests.
+// Linear index -> (I, J, K).  Indices below 2^31 (every grid of practical size) are split
+// in 32-bit arithmetic: a 64-bit division is a long instruction sequence on the GPU.
 __host__ __device__ inline void split3(long long q, const Dims &D, int &I, int &J, int &K) {
+    if (q < (1LL << 31)) {
+        const unsigned u = unsigned(q), r = u / unsigned(D.n[2]);
+        K = int(u - r * unsigned(D.n[2]));
+        J = int(r % unsigned(D.n[1]));
+        I = int(r / unsigned(D.n[1]));
+        return;
+    }
     K = int(q % D.n[2]);
     long long r = q / D.n[2];
     J = int(r % D.n[1]);
@@ -70,6 +79,13 @@ __host__ __device__ inline void split3(long long q, const Dims &D, int &I, int &
 }
 
 __host__ __device__ inline void split3_full(long long q, const Dims &D, int &i, int &j, int &k) {
+    if (q < (1LL << 31)) {
+        const unsigned u = unsigned(q), r = u / unsigned(D.N[2]);
+        k = int(u - r * unsigned(D.N[2]));
+        j = int(r % unsigned(D.N[1]));
+        i = int(r / unsigned(D.N[1]));
+        return;
+    }
     k = int(q % D.N[2]);
     long long r = q / D.N[2];
     j = int(r % D.N[1]);

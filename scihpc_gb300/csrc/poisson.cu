@@ -455,15 +455,17 @@ __device__ __forceinline__ long long smooth_count(const Level<T> &L) {
 template <class T, int MODE, int DIM>
 __device__ __forceinline__ void smooth_one(const Level<T> &L, const T *__restrict__ rho, const T *id2, long long t,
                                            int color) {
-    const int nf = L.n[DIM - 1];
-    const int nh = (nf + 1) / 2;
-    const int kh = int(t % nh);
-    const long long row = t / nh;
+    // every level has fewer than 2^31 cells: the index is decoded in 32-bit arithmetic
+    const unsigned nf = unsigned(L.n[DIM - 1]);
+    const unsigned nh = (nf + 1) / 2;
+    const unsigned u = unsigned(t);
+    const int kh = int(u % nh);
+    const unsigned row = u / nh;
     int I, J, K;
     long long P;
     if (DIM == 3) {
-        J = int(row % L.n[1]);
-        I = int(row / L.n[1]);
+        J = int(row % unsigned(L.n[1]));
+        I = int(row / unsigned(L.n[1]));
         K = 2 * kh + ((I + J + color) & 1);
         if (K >= L.n[2]) return;
         P = (I + 1) * L.s[0] + (J + 1) * L.s[1] + (K + 1);
@@ -646,19 +648,47 @@ constexpr int TS_STAGES = 6;
 constexpr size_t TS_SMEM = size_t(TS_STAGES) * 3 * TS_PLANE * sizeof(float) + 128;
 constexpr int TS_WAIT_LIMIT = 1 << 22;
 
-// out-of-place sweep of level 0; ZERO: the old iterate is zero (not loaded).  err: set when
-// a staged plane did not arrive within the wait limit (the sweep's output is then invalid).
-template <bool ZERO>
+// Coarse boxes for the prolongation fused into a sweep: the level-1 cells under a fine box.
+constexpr int TS_CW = SW_TK / 2 + 8;    // columns: padded K from tk * SW_TK / 2 - 4
+constexpr int TS_CH = SW_TJ / 2 + 2;    // rows: padded J from tj * SW_TJ / 2
+constexpr int TS_CPLANE = TS_CW * TS_CH;
+constexpr int TS_CSLOT = (TS_CPLANE + 31) / 32 * 32;   // the coarse box's slot, whole 128-byte units
+constexpr int TS_STAGES_PRO = 5;        // one stage fewer keeps two blocks per SM
+constexpr size_t TS_SMEM_PRO = size_t(TS_STAGES_PRO) * (3 * TS_PLANE + TS_CSLOT) * sizeof(float) + 128;
+// every TMA destination (stage starts, the boxes inside a stage) must be 128-byte aligned
+static_assert((TS_PLANE * sizeof(float)) % 128 == 0, "fine box size");
+static_assert(((3 * TS_PLANE + TS_CSLOT) * sizeof(float)) % 128 == 0, "stage size with the coarse box");
+
+// out-of-place sweep of level 0; ZERO: the old iterate is zero (not loaded).  PRO: the old
+// iterate is x + P e, with e the level-1 correction (piecewise-constant prolongation, ratio 2)
+// added on the fly from a staged coarse box: the prolongation pass and its write of x are
+// saved, and the values are the same (one FP32 addition per neighbour).  err: set when a
+// staged plane did not arrive within the wait limit (the sweep's output is then invalid).
+template <bool ZERO, bool PRO>
 __global__ void __launch_bounds__(SW_THREADS, 2)
     k_sweep3_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_rho,
-                 const __grid_constant__ CUtensorMap map_b, Level<float> L, float *__restrict__ xn,
-                 SweepCoef<float> cf, int c0, int ci, int *err) {
+                 const __grid_constant__ CUtensorMap map_b, const __grid_constant__ CUtensorMap map_e,
+                 Level<float> L, float *__restrict__ xn, SweepCoef<float> cf, int c0, int ci, int *err) {
+    static_assert(!(ZERO && PRO), "a prolongated iterate is not zero");
+    constexpr int NS = PRO ? TS_STAGES_PRO : TS_STAGES;
+    constexpr int SST = 3 * TS_PLANE + (PRO ? TS_CSLOT : 0);   // floats per stage
     extern __shared__ unsigned char ts_raw[];
-    __shared__ uint64_t bar[TS_STAGES];
+    __shared__ uint64_t bar[NS];
     __shared__ float first[2][SW_ROWS][SW_PAIRS];
     float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
     const int tid = threadIdx.x;
-    const int row = tid / SW_PAIRS, pr = tid - row * SW_PAIRS;
+    // Warps 0 .. SW_TJ-1 each own one interior row of SW_TK/2 column pairs (first and second
+    // colour); the remaining threads own the ring's pairs (first colour only), so the second-
+    // colour update never diverges inside an interior warp.
+    int row, pr;
+    if (tid < SW_TJ * (SW_PAIRS - 2)) {
+        row = tid / (SW_PAIRS - 2) + 1, pr = tid % (SW_PAIRS - 2) + 1;
+    } else {
+        const int r = tid - SW_TJ * (SW_PAIRS - 2);
+        if (r < SW_PAIRS) row = 0, pr = r;
+        else if (r < 2 * SW_PAIRS) row = SW_ROWS - 1, pr = r - SW_PAIRS;
+        else row = (r - 2 * SW_PAIRS) / 2 + 1, pr = ((r - 2 * SW_PAIRS) & 1) ? SW_PAIRS - 1 : 0;
+    }
     const int tiles_k = (L.n[2] + SW_TK - 1) / SW_TK;
     const int tk = blockIdx.x % tiles_k, tj = blockIdx.x / tiles_k;
     const int i0 = blockIdx.y * ci;
@@ -671,36 +701,44 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
     const int s0 = int(L.s[0]), s1 = int(L.s[1]);
     const int col = (j + 1) * s1 + kbase + 1;   // padded offset of (i = -1, j, kbase)
     const int sc = (row + 1) * TS_W + 2 * pr + 3;   // box offset of (j, kbase)
-    const uint32_t tx_bytes = (ZERO ? 2u : 3u) * uint32_t(TS_PLANE * sizeof(float));
+    const uint32_t tx_bytes = uint32_t(((ZERO ? 2 : 3) * TS_PLANE + (PRO ? TS_CPLANE : 0)) * sizeof(float));
     auto issue = [&](int q) {
-        const int st = q % TS_STAGES;
-        float *base = tiles + st * 3 * TS_PLANE;
+        const int st = q % NS;
+        float *base = tiles + st * SST;
         const int z = i0 - 1 + q;   // padded i of staged plane q
         tc::mbar_expect_tx(&bar[st], tx_bytes);
         if (!ZERO) tc::tma_load_3d(base, &map_x, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
         tc::tma_load_3d(base + TS_PLANE, &map_rho, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
         tc::tma_load_3d(base + 2 * TS_PLANE, &map_b, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st]);
+        // the level-1 plane under fine plane z - 1 (planes -2 and -1 map to its halo plane)
+        if (PRO)
+            tc::tma_load_3d(base + 3 * TS_PLANE, &map_e, tk * (SW_TK / 2) - 4, tj * (SW_TJ / 2), ((z - 1) >> 1) + 1,
+                            &bar[st]);
     };
-    auto wait_plane = [&](int q) {
-        return tc::mbar_wait(&bar[q % TS_STAGES], uint32_t((q / TS_STAGES) & 1), TS_WAIT_LIMIT);
-    };
-    // stage offsets of planes q - 2, q - 1, q, q + 1, rotated once per step
-    constexpr int SST = 3 * TS_PLANE;
-    int om2 = (TS_STAGES - 1) * SST, om1 = 0, oc0 = SST, op1 = 2 * SST;
+    auto wait_plane = [&](int q) { return tc::mbar_wait(&bar[q % NS], uint32_t((q / NS) & 1), TS_WAIT_LIMIT); };
+    // stage offsets of planes q - 1, q, q + 1, rotated once per step
+    int om1 = 0, oc0 = SST, op1 = 2 * SST;
+    // coarse-box offsets of the parent of this pair's cells and of their j neighbours'
+    // parents; a k neighbour's parent is the parent or the cell beside it, by the parity
+    const int cpar = ((row + 1) >> 1) * TS_CW + pr + 4;
+    const int cjm = (row >> 1) * TS_CW + pr + 4, cjp = ((row + 2) >> 1) * TS_CW + pr + 4;
     // Thread 0 alone waits on the barriers (the others would spend issue slots polling) and
     // the block barrier that follows passes the arrival on.
-    const int issued_pre = min(TS_STAGES, nq) - 1;
+    const int issued_pre = min(NS, nq) - 1;
     int issued = issued_pre;   // planes 0 .. issued have been requested
     int waited = -1;           // planes 0 .. waited have arrived (thread 0)
     bool ok = true;
     if (tid == 0) {
-        for (int st = 0; st < TS_STAGES; ++st) tc::mbar_init(&bar[st], 1);
+        for (int st = 0; st < NS; ++st) tc::mbar_init(&bar[st], 1);
         for (int q = 0; q <= issued_pre; ++q) issue(q);
         for (int q = 0; q <= 2 && ok; ++q)
             if ((ok = wait_plane(q))) waited = q;
     }
     const float w0 = cf.w[0], w1 = cf.w[1], w2 = cf.w[2];
     float f1 = 0, f2 = 0;   // this pair's first-colour values at planes i-1 and i-2
+    // the (i, i+1) face coefficient of the first-colour update two steps back is the (i-2, i-1)
+    // face of the second-colour update (same column)
+    float c1h1 = 0, c1h2 = 0;
     bool fail = __syncthreads_or(!ok);
     for (int q = 1; q <= nq - 2 && !fail; ++q) {
         // planes q - 2 .. q + 1 are on chip
@@ -719,8 +757,13 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         const float C2 = w1 * prcp(rc + Rc[o - TS_W]), C3 = w1 * prcp(rc + Rc[o + TS_W]);
         const float C4 = w2 * prcp(rc + Rc[o - 1]), C5 = w2 * prcp(rc + Rc[o + 1]);
         float sx = 0;
-        if (!ZERO)
+        if (PRO) {
+            const float *Em = Xm + 3 * TS_PLANE, *Ec = Xc + 3 * TS_PLANE, *Ep = Xp + 3 * TS_PLANE;
+            sx = cim * (Xm[o] + Em[cpar]) + C1 * (Xp[o] + Ep[cpar]) + C2 * (Xc[o - TS_W] + Ec[cjm]) +
+                 C3 * (Xc[o + TS_W] + Ec[cjp]) + C4 * (Xc[o - 1] + Ec[cpar - 1 + par]) + C5 * (Xc[o + 1] + Ec[cpar + par]);
+        } else if (!ZERO) {
             sx = cim * Xm[o] + C1 * Xp[o] + C2 * Xc[o - TS_W] + C3 * Xc[o + TS_W] + C4 * Xc[o - 1] + C5 * Xc[o + 1];
+        }
         const float fa = (Xc[2 * TS_PLANE + o] + sx) * prcp(cim + C1 + C2 + C3 + C4 + C5);
         const float fi = fvalid ? fa : 0.0f;
         const int off = (i + 1) * s0 + col + par;
@@ -730,10 +773,9 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         const int ib = i - 1;
         if (inner && kin && ib >= i0 && ib < i1) {
             const int qb = (q - 1) & 1;
-            const float *Rmm = tiles + om2 + TS_PLANE;
             const float nbm = first[qb][row][pr - 1], nbp = first[qb][row][pr + 1];
             const float n4 = par == 0 ? nbm : f1, n5 = par == 0 ? f1 : nbp;
-            const float D0 = w0 * prcp(rim + Rmm[o]);
+            const float D0 = c1h2;
             const float D2 = w1 * prcp(rim + Rm[o - TS_W]), D3 = w1 * prcp(rim + Rm[o + TS_W]);
             const float D4 = w2 * prcp(rim + Rm[o - 1]), D5 = w2 * prcp(rim + Rm[o + 1]);
             const float sb = D0 * f2 + cim * fi + D2 * first[qb][row - 1][pr] + D3 * first[qb][row + 1][pr] + D4 * n4 +
@@ -742,17 +784,19 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         }
         f2 = f1;
         f1 = fi;
-        om2 = om1, om1 = oc0, oc0 = op1;
-        op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
+        c1h2 = c1h1;
+        c1h1 = C1;
+        om1 = oc0, oc0 = op1;
+        op1 = op1 == (NS - 1) * SST ? 0 : op1 + SST;
         if (tid == 0 && q + 2 <= nq - 1)
             if ((ok = wait_plane(q + 2))) waited = q + 2;
         if ((fail = __syncthreads_or(!ok))) break;
-        // plane q - 2 is no longer needed: its stage takes plane q - 2 + TS_STAGES
-        if (q >= 2 && q - 2 + TS_STAGES < nq) {
-            issued = q - 2 + TS_STAGES;
+        // plane q - 2 is no longer needed: its stage takes plane q - 2 + NS
+        if (q >= 2 && q - 2 + NS < nq) {
+            issued = q - 2 + NS;
             if (tid == 0) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(q - 2 + TS_STAGES);
+                issue(q - 2 + NS);
             }
         }
     }
@@ -770,29 +814,30 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
 // Residual + restriction of the finest FP32 level (MODE 1, ratio 2) with the planes of x, the
 // density and b staged in shared memory by TMA, in the boxes of k_sweep3_tma (same tensor
 // maps).  A block owns SW_TJ x SW_TK fine columns and a chunk of planes starting at an even
-// plane; a thread owns a 2 x 2 group of fine columns (one coarse column), adds the residuals
-// of its four fine cells plane by plane and, after every second plane, writes the coarse
-// right-hand side (the mean of the eight residuals) and clears the coarse iterate.  The
-// residual arithmetic is that of residual_at.
-constexpr int RT_THREADS = (SW_TJ / 2) * (SW_TK / 2);   // 256
+// plane; a thread owns two fine columns (k, k+1) of one row and adds their residuals plane by
+// plane.  After every second plane the odd row hands its sum to the even row through shared
+// memory, and the even row writes the coarse right-hand side (the mean of the eight
+// residuals) and clears the coarse iterate.  The residual arithmetic is that of residual_at.
+constexpr int RT_THREADS = SW_TJ * (SW_TK / 2);   // 512
 
-__global__ void __launch_bounds__(RT_THREADS)
+__global__ void __launch_bounds__(RT_THREADS, 2)
     k_restrict3_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_rho,
                     const __grid_constant__ CUtensorMap map_b, Level<float> F, Level<float> Cl, Id2<float> id2, int ci,
                     int *err) {
     extern __shared__ unsigned char ts_raw[];
     __shared__ uint64_t bar[TS_STAGES];
+    __shared__ float part[SW_TJ / 2][SW_TK / 2];   // sums of the odd rows
     float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
     const int tid = threadIdx.x;
-    const int jc = tid / (SW_TK / 2), kc = tid - jc * (SW_TK / 2);   // coarse row / column in the tile
+    const int jj = tid / (SW_TK / 2), kc = tid - jj * (SW_TK / 2);   // fine row / coarse column in the tile
     const int tiles_k = (F.n[2] + SW_TK - 1) / SW_TK;
     const int tk = blockIdx.x % tiles_k, tj = blockIdx.x / tiles_k;
     const int i0 = blockIdx.y * ci;   // ci is even
     const int i1 = min(i0 + ci, F.n[0]);
     const int nq = i1 - i0 + 2;   // staged planes i0 - 1 .. i1
-    const int j = tj * SW_TJ + 2 * jc, k = tk * SW_TK + 2 * kc;   // first fine cell of the group
+    const int j = tj * SW_TJ + jj, k = tk * SW_TK + 2 * kc;   // first fine cell of the pair
     const bool live = j < F.n[1] && k < F.n[2];
-    const int sc = (2 * jc + 2) * TS_W + 2 * kc + 5;   // box offset of (j, k)
+    const int sc = (jj + 2) * TS_W + 2 * kc + 5;   // box offset of (j, k)
     const uint32_t tx_bytes = 3u * uint32_t(TS_PLANE * sizeof(float));
     auto issue = [&](int q) {
         const int st = q % TS_STAGES;
@@ -825,30 +870,32 @@ __global__ void __launch_bounds__(RT_THREADS)
         const float *Xc = tiles + oc0, *Xm = tiles + om1, *Xp = tiles + op1;
         const float *Rc = Xc + TS_PLANE, *Rm = Xm + TS_PLANE, *Rp = Xp + TS_PLANE, *Bc = Xc + 2 * TS_PLANE;
 #pragma unroll
-        for (int dj = 0; dj < 2; ++dj)
-#pragma unroll
-            for (int dk = 0; dk < 2; ++dk) {
-                const int o = sc + dj * TS_W + dk;
-                const float rc = Rc[o], xc = Xc[o];
-                const float C0 = pdiv(2.0f, rc + Rm[o]) * c0, C1 = pdiv(2.0f, rc + Rp[o]) * c0;
-                const float C2 = pdiv(2.0f, rc + Rc[o - TS_W]) * c1, C3 = pdiv(2.0f, rc + Rc[o + TS_W]) * c1;
-                const float C4 = pdiv(2.0f, rc + Rc[o - 1]) * c2, C5 = pdiv(2.0f, rc + Rc[o + 1]) * c2;
-                float sres = C0 * (xc - Xm[o]) + C1 * (xc - Xp[o]) + C2 * (xc - Xc[o - TS_W]) + C3 * (xc - Xc[o + TS_W]);
-                sres += C4 * (xc - Xc[o - 1]) + C5 * (xc - Xc[o + 1]);
-                acc += Bc[o] - sres;
-            }
-        const int i = i0 - 1 + q;
-        if ((i & 1) && live) {
-            const long long Pc = (long long)((i >> 1) + 1) * Cl.s[0] + (long long)((j >> 1) + 1) * Cl.s[1] + (k >> 1) + 1;
-            Cl.b[Pc] = pdiv(acc, 8.0f);
-            Cl.x[Pc] = 0;
+        for (int dk = 0; dk < 2; ++dk) {
+            const int o = sc + dk;
+            const float rc = Rc[o], xc = Xc[o];
+            const float C0 = pdiv(2.0f, rc + Rm[o]) * c0, C1 = pdiv(2.0f, rc + Rp[o]) * c0;
+            const float C2 = pdiv(2.0f, rc + Rc[o - TS_W]) * c1, C3 = pdiv(2.0f, rc + Rc[o + TS_W]) * c1;
+            const float C4 = pdiv(2.0f, rc + Rc[o - 1]) * c2, C5 = pdiv(2.0f, rc + Rc[o + 1]) * c2;
+            float sres = C0 * (xc - Xm[o]) + C1 * (xc - Xp[o]) + C2 * (xc - Xc[o - TS_W]) + C3 * (xc - Xc[o + TS_W]);
+            sres += C4 * (xc - Xc[o - 1]) + C5 * (xc - Xc[o + 1]);
+            acc += Bc[o] - sres;
         }
-        if (i & 1) acc = 0;
+        const int i = i0 - 1 + q;
+        if ((i & 1) && (jj & 1)) part[jj >> 1][kc] = acc;
         om1 = oc0, oc0 = op1;
         op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
         if (tid == 0 && q + 2 <= nq - 1)
             if ((ok = wait_plane(q + 2))) waited = q + 2;
         if ((fail = __syncthreads_or(!ok))) break;
+        if (i & 1) {
+            if (!(jj & 1) && live) {
+                const long long Pc =
+                    (long long)((i >> 1) + 1) * Cl.s[0] + (long long)((j >> 1) + 1) * Cl.s[1] + (k >> 1) + 1;
+                Cl.b[Pc] = pdiv(acc + part[jj >> 1][kc], 8.0f);
+                Cl.x[Pc] = 0;
+            }
+            acc = 0;
+        }
         // plane q - 1 is no longer needed: its stage takes plane q - 1 + TS_STAGES
         if (q + TS_STAGES - 1 < nq) {
             issued = q + TS_STAGES - 1;
@@ -903,14 +950,15 @@ template <class T, int MODE, int DIM>
 __device__ __forceinline__ void restrict_one(const Level<T> &F, const Level<T> &Cl, const T *__restrict__ rho,
                                              const T *id2, long long t) {
     int I, J, K = 0;
+    const unsigned u = unsigned(t);   // levels have fewer than 2^31 cells
     if (DIM == 3) {
-        K = int(t % Cl.n[2]);
-        const long long rr = t / Cl.n[2];
-        J = int(rr % Cl.n[1]);
-        I = int(rr / Cl.n[1]);
+        K = int(u % unsigned(Cl.n[2]));
+        const unsigned rr = u / unsigned(Cl.n[2]);
+        J = int(rr % unsigned(Cl.n[1]));
+        I = int(rr / unsigned(Cl.n[1]));
     } else {
-        J = int(t % Cl.n[1]);
-        I = int(t / Cl.n[1]);
+        J = int(u % unsigned(Cl.n[1]));
+        I = int(u / unsigned(Cl.n[1]));
     }
     const int r = F.ratio;
     T s = 0;
@@ -941,14 +989,15 @@ template <class T, int DIM>
 __device__ __forceinline__ void prolong_one(const Level<T> &F, const Level<T> &Cl, int neumann, int linear,
                                             long long t) {
     int ii[3] = {0, 0, 0};
+    const unsigned u = unsigned(t);   // levels have fewer than 2^31 cells
     if (DIM == 3) {
-        ii[2] = int(t % F.n[2]);
-        const long long rr = t / F.n[2];
-        ii[1] = int(rr % F.n[1]);
-        ii[0] = int(rr / F.n[1]);
+        ii[2] = int(u % unsigned(F.n[2]));
+        const unsigned rr = u / unsigned(F.n[2]);
+        ii[1] = int(rr % unsigned(F.n[1]));
+        ii[0] = int(rr / unsigned(F.n[1]));
     } else {
-        ii[1] = int(t % F.n[1]);
-        ii[0] = int(t / F.n[1]);
+        ii[1] = int(u % unsigned(F.n[1]));
+        ii[0] = int(u / unsigned(F.n[1]));
     }
     const int r = F.ratio;
     const long long Pf = (ii[0] + 1) * F.s[0] + (ii[1] + 1) * F.s[1] + (DIM == 3 ? ii[2] + 1 : 0);
@@ -1473,7 +1522,7 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
             const long long c = G.cells;
             T *x = p, *bb = p + c, *cx = p + 2 * c, *cy = p + 3 * c, *cz = DIM == 3 ? p + 4 * c : nullptr;
             T *idg = p + (DIM == 3 ? 5 : 4) * c;
-            for (long long i = tid; i < c; i += nt) {
+            for (int i = tid; i < int(c); i += nt) {
                 x[i] = l == lc ? G.x[i] : T(0);
                 bb[i] = l == lc ? G.b[i] : T(0);
                 cx[i] = G.cx[i];
@@ -1591,10 +1640,10 @@ int Poisson::alloc_levels() {
             L.d[a] = dd[a];
         }
         L.s[2] = 1;
-        // 3D level 0: rows padded to a multiple of four cells (16-byte aligned rows, as the
-        // tensor-memory-access descriptors of the staged sweep require); the extra cells are
-        // never part of a stencil
-        L.s[1] = (l == 0 && D.ndim == 3) ? (L.P[2] + 3) / 4 * 4 : L.P[2];
+        // 3D levels 0 and 1: rows padded to a multiple of four cells (16-byte aligned rows, as
+        // the tensor-memory-access descriptors of the staged sweep require); the extra cells
+        // are never part of a stencil
+        L.s[1] = (l <= 1 && D.ndim == 3) ? (L.P[2] + 3) / 4 * 4 : L.P[2];
         L.s[0] = (long long)L.P[1] * L.s[1];
         if (D.ndim == 2) L.s[2] = 0;
         L.cells = (long long)L.P[0] * L.s[0];
@@ -1637,15 +1686,18 @@ int Poisson::alloc_levels() {
     }
     SCIHPC_CUDA(cudaMalloc(&rho_pad, zbytes));
     if constexpr (sizeof(T) == 4) {
-        if (D.ndim == 3) tma_ready = make_level0_maps(Ls[0]);
+        if (D.ndim == 3) tma_ready = make_level0_maps(Ls);
     }
     return SCIHPC_OK;
 }
 
 // TMA descriptors of the FP32 level 0: boxes of TS_W x TS_H x 1 cells of x, x2, the padded
-// density and b.  Returns false (and the sweeps keep reading global memory directly) when
-// the driver has no tensor-map encoder or a descriptor is refused.
-bool Poisson::make_level0_maps(const Level<float> &L) {
+// density and b; and boxes of TS_CW x TS_CH x 1 cells of level 1's x (prolongation fused into
+// the first post-smoothing sweep; tma_pro_ready).  Returns false (and the sweeps keep reading
+// global memory directly) when the driver has no tensor-map encoder or a descriptor is
+// refused.
+bool Poisson::make_level0_maps(const std::vector<Level<float>> &Ls) {
+    const Level<float> &L = Ls[0];
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         void *fn = nullptr;
@@ -1668,6 +1720,16 @@ bool Poisson::make_level0_maps(const Level<float> &L) {
                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return false;
+    }
+    tma_pro_ready = false;
+    if (Ls.size() > 1 && L.ratio == 2) {
+        const Level<float> &C = Ls[1];
+        const cuuint64_t cdims[3] = {cuuint64_t(C.s[1]), cuuint64_t(C.P[1]), cuuint64_t(C.P[0])};
+        const cuuint64_t cstrides[2] = {cuuint64_t(C.s[1]) * sizeof(float), cuuint64_t(C.s[0]) * sizeof(float)};
+        const cuuint32_t cbox[3] = {TS_CW, TS_CH, 1};
+        tma_pro_ready = encode(&tmap[4], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, C.x, cdims, cstrides, cbox, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
     }
     return true;
 }
@@ -1701,8 +1763,9 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM_PRO)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_restrict3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     if (const char *e = std::getenv("SCIHPC_SWEEP_TMA")) tma_enable = std::atoi(e) != 0;
     if (!density) {
@@ -1880,7 +1943,10 @@ void Poisson::vcycle(cudaStream_t s) {
         return D.ndim == 3 && (long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] >= FUSED_MIN_CELLS &&
                Ls[l].cells < (1LL << 31);
     };
-    auto sweep = [&](int l, const T *xo, T *xn, int c0, int zero) {
+    // the first post-smoothing sweep of level 0 can apply the prolongation itself
+    const bool pro0 = sizeof(T) == 4 && mode0 == 1 && tma_ready && tma_pro_ready && tma_enable && fused(0) &&
+                      Ls[0].ratio == 2 && !prolong_linear;
+    auto sweep = [&](int l, const T *xo, T *xn, int c0, int zero, bool pro) {
         Level<T> &L = Ls[l];
         const int ci = sweep_chunk(L.n);
         const dim3 grid(unsigned(((L.n[2] + SW_TK - 1) / SW_TK) * ((L.n[1] + SW_TJ - 1) / SW_TJ)),
@@ -1897,8 +1963,15 @@ void Poisson::vcycle(cudaStream_t s) {
             if (l == 0 && m == 1 && tma_ready && tma_enable) {
                 const CUtensorMap &mx = xo == Ls[0].x ? tmap[0] : tmap[1];
                 int *err = &dev_state->sweep_err;
-                if (zero) k_sweep3_tma<true><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], L, xn, cf, c0, ci, err);
-                else k_sweep3_tma<false><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], L, xn, cf, c0, ci, err);
+                if (zero)
+                    k_sweep3_tma<true, false><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], tmap[4], L, xn, cf,
+                                                                                 c0, ci, err);
+                else if (pro)
+                    k_sweep3_tma<false, true><<<grid, SW_THREADS, TS_SMEM_PRO, s>>>(mx, tmap[2], tmap[3], tmap[4], L, xn,
+                                                                                    cf, c0, ci, err);
+                else
+                    k_sweep3_tma<false, false><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], tmap[4], L, xn,
+                                                                                 cf, c0, ci, err);
                 return;
             }
         }
@@ -1907,12 +1980,12 @@ void Poisson::vcycle(cudaStream_t s) {
         else if constexpr (sizeof(T) == 4) k_sweep3<T, 1><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
     };
     // nu is even, so an even number of out-of-place sweeps leaves the iterate in x
-    auto smooth_level = [&](int l, int c0, bool from_zero) {
+    auto smooth_level = [&](int l, int c0, bool from_zero, bool pro) {
         if (fused(l)) {
             for (int k = 0; k < nu; ++k) {
                 T *src = (k & 1) ? Ls[l].x2 : Ls[l].x;
                 T *dst = (k & 1) ? Ls[l].x : Ls[l].x2;
-                sweep(l, src, dst, c0, (k == 0 && from_zero) ? 1 : 0);
+                sweep(l, src, dst, c0, (k == 0 && from_zero) ? 1 : 0, k == 0 && pro);
             }
         } else {
             for (int k = 0; k < nu; ++k) {
@@ -1923,7 +1996,7 @@ void Poisson::vcycle(cudaStream_t s) {
     };
     if (!fused(0)) cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
     for (int l = 0; l < lc; ++l) {
-        smooth_level(l, 0, true);   // level 0 starts from zero; coarser levels are zeroed by restriction
+        smooth_level(l, 0, true, false);   // level 0 starts from zero; coarser levels are zeroed by restriction
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const long long nc = (long long)Cl.n[0] * Cl.n[1] * Cl.n[2];
         const unsigned nb = blocks_for(nc, TPB);
@@ -1963,6 +2036,10 @@ void Poisson::vcycle(cudaStream_t s) {
     }
     for (int l = lc - 1; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
+        if (l == 0 && pro0) {
+            smooth_level(0, 1, false, true);
+            continue;
+        }
         const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
         if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
         else if (F.ratio == 2 && !prolong_linear && F.n[0] <= 65535 && F.n[1] <= 65535 * PR_BY)
@@ -1970,7 +2047,7 @@ void Poisson::vcycle(cudaStream_t s) {
                                     unsigned(F.n[0])),
                                dim3(PR_BX, PR_BY), 0, s>>>(F, Cl);
         else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
-        smooth_level(l, 1, false);
+        smooth_level(l, 1, false, false);
     }
 }
 

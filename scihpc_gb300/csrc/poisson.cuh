@@ -89,7 +89,7 @@ private:
     int alloc_levels();
     template <class T>
     void build_coarse(cudaStream_t s);
-    bool make_level0_maps(const Level<float> &L);
+    bool make_level0_maps(const std::vector<Level<float>> &Ls);
     template <int DIM>
     void begin_dim(const double *rhs, double *p, int use_guess, cudaStream_t s);
     template <int DIM>
@@ -111,9 +111,9 @@ private:
     double *partial = nullptr;       // reduction scratch (2 x RED_MAX_BLOCKS)
     double *oc = nullptr;            // FP64 +face coefficients of the outer operator (3 compact arrays)
     double *dense = nullptr;         // coarsest-level inverse (n x n, FP64)
-    // TMA descriptors of the FP32 level 0 (3D): x, x2, padded density, b
-    CUtensorMap tmap[4];
-    bool tma_ready = false;
+    // TMA descriptors of the FP32 level 0 (3D): x, x2, padded density, b; and level 1's x
+    CUtensorMap tmap[5];
+    bool tma_ready = false, tma_pro_ready = false;
     int tma_enable = 1;
     int ncoarse = 0;
     const double *rhs_ = nullptr;

@@ -149,9 +149,10 @@ def test_variable_density_matches_exact_solve(port, fp32, case):
 
 @pytest.mark.parametrize("case", ["3d_fused", "3d_ragged"])
 def test_staged_sweep_matches_direct_sweep(case, monkeypatch):
-    """The FP32 level-0 sweep with its planes staged in shared memory by TMA performs the same
-    updates as the sweep that reads global memory directly (SCIHPC_SWEEP_TMA=0): after one
-    iteration the pressures agree to FP32 round-off, and converged solves take the same
+    """The FP32 level-0 kernels with their planes staged in shared memory by TMA (sweeps,
+    residual restriction, prolongation fused into the first post-smoothing sweep) perform the
+    same updates as the kernels that read global memory directly (SCIHPC_SWEEP_TMA=0): after
+    one iteration the pressures agree to FP32 round-off, and converged solves take the same
     number of iterations to the same answer."""
     from scihpc_gb300 import Poisson
     n, hi = DENSITY_GRIDS[case]
