@@ -38,6 +38,30 @@ struct Dims {
 
 Dims make_dims(const scihpc_grid *g);
 
+// Unsigned division by a run-time invariant d >= 1 as a multiply-high, an add and shifts
+// (T. Granlund, P. Montgomery, "Division by invariant integers using multiplication", 1994):
+// with l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1, for every 32-bit u,
+// u / d = (t + ((u - t) >> 1)) >> (l - 1) with t = mulhi(m, u).  A hardware-free integer
+// division is a long instruction sequence; this is four instructions.
+struct FastDiv {
+    uint32_t m = 0;
+    int l = 0;   // 0: d == 1
+    FastDiv() = default;
+    explicit FastDiv(uint32_t d) {
+        while ((1ull << l) < d) ++l;
+        m = uint32_t(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+    __host__ __device__ uint32_t div(uint32_t u) const {
+        if (l == 0) return u;
+#if defined(__CUDA_ARCH__)
+        const uint32_t t = __umulhi(m, u);
+#else
+        const uint32_t t = uint32_t((uint64_t(m) * u) >> 32);
+#endif
+        return (t + ((u - t) >> 1)) >> (l - 1);
+    }
+};
+
 // Problem parameters that change from step to step live in device memory so that a
 // captured CUDA graph replays correctly (problem_parameters, global.h:25-54).
 struct StepScalars {

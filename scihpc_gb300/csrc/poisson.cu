@@ -456,16 +456,15 @@ template <class T, int MODE, int DIM>
 __device__ __forceinline__ void smooth_one(const Level<T> &L, const T *__restrict__ rho, const T *id2, long long t,
                                            int color) {
     // every level has fewer than 2^31 cells: the index is decoded in 32-bit arithmetic
-    const unsigned nf = unsigned(L.n[DIM - 1]);
-    const unsigned nh = (nf + 1) / 2;
+    const unsigned nh = (unsigned(L.n[DIM - 1]) + 1) / 2;
     const unsigned u = unsigned(t);
-    const int kh = int(u % nh);
-    const unsigned row = u / nh;
+    const unsigned row = L.fh.div(u);
+    const int kh = int(u - row * nh);
     int I, J, K;
     long long P;
     if (DIM == 3) {
-        J = int(row % unsigned(L.n[1]));
-        I = int(row / unsigned(L.n[1]));
+        I = int(L.f1.div(row));
+        J = int(row - unsigned(I) * unsigned(L.n[1]));
         K = 2 * kh + ((I + J + color) & 1);
         if (K >= L.n[2]) return;
         P = (I + 1) * L.s[0] + (J + 1) * L.s[1] + (K + 1);
@@ -531,7 +530,6 @@ struct SweepCoef {
 };
 
 __device__ __forceinline__ float prcp(float x) { return rcp_approx(x); }
-__device__ __forceinline__ double prcp(double x) { return 1.0 / x; }
 
 // Gauss-Seidel value (b + sum_f C_f x_f) / sum_f C_f of the cell at padded offset `off`.
 // nb: neighbour values (-i, +i, -j, +j, -k, +k); rn (MODE 1): densities of the cell and of the
@@ -952,13 +950,13 @@ __device__ __forceinline__ void restrict_one(const Level<T> &F, const Level<T> &
     int I, J, K = 0;
     const unsigned u = unsigned(t);   // levels have fewer than 2^31 cells
     if (DIM == 3) {
-        K = int(u % unsigned(Cl.n[2]));
-        const unsigned rr = u / unsigned(Cl.n[2]);
-        J = int(rr % unsigned(Cl.n[1]));
-        I = int(rr / unsigned(Cl.n[1]));
+        const unsigned rr = Cl.f2.div(u);
+        K = int(u - rr * unsigned(Cl.n[2]));
+        I = int(Cl.f1.div(rr));
+        J = int(rr - unsigned(I) * unsigned(Cl.n[1]));
     } else {
-        J = int(u % unsigned(Cl.n[1]));
-        I = int(u / unsigned(Cl.n[1]));
+        I = int(Cl.f1.div(u));
+        J = int(u - unsigned(I) * unsigned(Cl.n[1]));
     }
     const int r = F.ratio;
     T s = 0;
@@ -991,19 +989,19 @@ __device__ __forceinline__ void prolong_one(const Level<T> &F, const Level<T> &C
     int ii[3] = {0, 0, 0};
     const unsigned u = unsigned(t);   // levels have fewer than 2^31 cells
     if (DIM == 3) {
-        ii[2] = int(u % unsigned(F.n[2]));
-        const unsigned rr = u / unsigned(F.n[2]);
-        ii[1] = int(rr % unsigned(F.n[1]));
-        ii[0] = int(rr / unsigned(F.n[1]));
+        const unsigned rr = F.f2.div(u);
+        ii[2] = int(u - rr * unsigned(F.n[2]));
+        ii[0] = int(F.f1.div(rr));
+        ii[1] = int(rr - unsigned(ii[0]) * unsigned(F.n[1]));
     } else {
-        ii[1] = int(u % unsigned(F.n[1]));
-        ii[0] = int(u / unsigned(F.n[1]));
+        ii[0] = int(F.f1.div(u));
+        ii[1] = int(u - unsigned(ii[0]) * unsigned(F.n[1]));
     }
     const int r = F.ratio;
     const long long Pf = (ii[0] + 1) * F.s[0] + (ii[1] + 1) * F.s[1] + (DIM == 3 ? ii[2] + 1 : 0);
     int par[3], nb[3];
     for (int a = 0; a < DIM; ++a) {
-        par[a] = ii[a] / r;
+        par[a] = r == 2 ? ii[a] >> 1 : (r == 3 ? ii[a] / 3 : ii[a] / r);
         const int off = ii[a] - par[a] * r;
         int dn = off == 0 ? par[a] - 1 : par[a] + 1;
         if (neumann && (dn < 0 || dn >= Cl.n[a])) dn = par[a];
@@ -1227,11 +1225,14 @@ __global__ void k_dense_pin_and_invert(double *__restrict__ M, double *__restric
     for (int e = t; e < n * n; e += nt) M[e] = W[(size_t)(e / n) * w + n + e % n];
 }
 
+// Coarsest-level direct solve x = Minv (b - mean b) in FP64 (mean removed for Neumann walls),
+// run by a whole block: b (n <= 1024 cells) is staged in shared memory, warp 0 forms the mean
+// (fixed-order lane sums and shuffle tree), and each warp takes rows of Minv with coalesced
+// loads and a shuffle reduction.
 template <class T, int DIM>
-__global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n, int neumann) {
-    __shared__ double b[1024];
-    __shared__ double mean;
-    const int t = threadIdx.x;
+__device__ __forceinline__ void dense_apply(const Level<T> &L, const double *__restrict__ Minv, int n, int neumann,
+                                            double *b, double *mean) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nw = blockDim.x >> 5;
     auto pidx = [&](int c) {
         int I, J, K = 0;
         if (DIM == 3) {
@@ -1246,19 +1247,29 @@ __global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n
     };
     for (int c = t; c < n; c += blockDim.x) b[c] = double(L.b[pidx(c)]);
     __syncthreads();
-    if (t == 0) {
-        double s = 0.0;
+    if (warp == 0) {
+        double v = 0.0;
         if (neumann)
-            for (int c = 0; c < n; ++c) s += b[c];
-        mean = s / n;
+            for (int c = lane; c < n; c += 32) v += b[c];
+        for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+        if (lane == 0) *mean = v / n;
     }
     __syncthreads();
-    for (int c = t; c < n; c += blockDim.x) {
+    const double mu = *mean;
+    for (int c = warp; c < n; c += nw) {
         const double *row = Minv + (size_t)c * n;
-        double s = 0.0;
-        for (int q = 0; q < n; ++q) s += row[q] * (b[q] - mean);
-        L.x[pidx(c)] = T(s);
+        double v = 0.0;
+        for (int q = lane; q < n; q += 32) v += row[q] * (b[q] - mu);
+        for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+        if (lane == 0) L.x[pidx(c)] = T(v);
     }
+}
+
+template <class T, int DIM>
+__global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n, int neumann) {
+    __shared__ double b[1024];
+    __shared__ double mean;
+    dense_apply<T, DIM>(L, Minv, n, neumann, b, &mean);
 }
 
 // ---------------------------------------------------------------- FP32 inner solve (iterative refinement)
@@ -1551,37 +1562,8 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
         for (long long t = tid; t < nc; t += nt) restrict_one<T, 0, DIM>(L, Cl, nullptr, nullptr, t);
         __syncthreads();
     }
-    {
-        const Level<T> &L = SL[nlev - 1];
-        auto pidx = [&](int c) {
-            int I, J, K = 0;
-            if (DIM == 3) {
-                K = c % L.n[2];
-                J = (c / L.n[2]) % L.n[1];
-                I = c / (L.n[2] * L.n[1]);
-            } else {
-                J = c % L.n[1];
-                I = c / L.n[1];
-            }
-            return (I + 1) * L.s[0] + (J + 1) * L.s[1] + (DIM == 3 ? K + 1 : 0);
-        };
-        for (int c = tid; c < n; c += nt) b[c] = double(L.b[pidx(c)]);
-        __syncthreads();
-        if (tid == 0) {
-            double s = 0.0;
-            if (neumann)
-                for (int c = 0; c < n; ++c) s += b[c];
-            mean = s / n;
-        }
-        __syncthreads();
-        for (int c = tid; c < n; c += nt) {
-            const double *row = Minv + (size_t)c * n;
-            double s = 0.0;
-            for (int q = 0; q < n; ++q) s += row[q] * (b[q] - mean);
-            L.x[pidx(c)] = T(s);
-        }
-        __syncthreads();
-    }
+    dense_apply<T, DIM>(SL[nlev - 1], Minv, n, neumann, b, &mean);
+    __syncthreads();
     for (int l = nlev - 2; l >= lc; --l) {
         const Level<T> &L = SL[l];
         const long long nf = (long long)L.n[0] * L.n[1] * (DIM == 3 ? L.n[2] : 1);
@@ -1648,6 +1630,9 @@ int Poisson::alloc_levels() {
         if (D.ndim == 2) L.s[2] = 0;
         L.cells = (long long)L.P[0] * L.s[0];
         L.ratio = ratio[l];
+        L.f1 = FastDiv(uint32_t(L.n[1]));
+        L.f2 = FastDiv(uint32_t(L.n[2]));
+        L.fh = FastDiv(uint32_t((L.n[D.ndim - 1] + 1) / 2));
         const size_t bytes = size_t(L.cells) * sizeof(T);
         SCIHPC_CUDA(cudaMalloc(&L.x, 2 * bytes));
         SCIHPC_CUDA(cudaMalloc(&L.b, bytes));

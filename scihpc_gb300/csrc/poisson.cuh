@@ -25,6 +25,9 @@ struct Level {
     T *x2 = nullptr;   // second iterate buffer for out-of-place fused sweeps (same allocation as x)
     T *cx = nullptr, *cy = nullptr, *cz = nullptr;
     T *idg = nullptr;   // 1 / sum of the face coefficients (levels with stored coefficients)
+    // divisions by n[1], n[2] and by the cells of one colour along the last axis,
+    // (n[ndim - 1] + 1) / 2, used to decode cell indices
+    FastDiv f1, f2, fh;
 };
 
 struct PcgScalars {
