@@ -216,6 +216,126 @@ __global__ void k_reinit_a(const double *__restrict__ phi, const double *__restr
     B[o] = g * De[o] * De[o];
 }
 
+// k_reinit_a for 2D grids, on tiles of RA_T x RA_T cells in shared memory.  The Godunov
+// gradient needs, per cell and axis, two WENO-JS corrections (forward and backward), each
+// from four second differences D2 and three smoothness indicators.  The indicators of
+// neighbouring cells are the same three functions of consecutive pairs (u, w) = (D2[p],
+// D2[p+1]) under mirroring:
+//   X(p) = 13 (w - u)^2 + 3 (w - 3u)^2,  Y(p) = 13 (w - u)^2 + 3 (3w - u)^2,
+//   B(p) = 13 (w - u)^2 + 3 (w + u)^2,
+// forward at i:  (is0, is1, is2) = (X(i+1), B(i), Y(i-1)),
+// backward at i: (is0, is1, is2) = (Y(i-2), B(i-1), X(i)),
+// so the tile computes every D2 and every (eps + indicator)^2 once per pair instead of four
+// times per cell, and the two normalisations of a cell share one division.  The arithmetic
+// is FP64 throughout (godunov_gradient.cpp:19-198); the rounding differs from godunov_at's
+// only in the order of operations.
+// Tiles of RA_TI (axis 0) x RA_TJ (axis 1) cells: 256 tiles for the 128 x 256 bubble, so
+// that every SM has FP64 work.
+constexpr int RA_TI = 8, RA_TJ = 16;
+constexpr int RA_NT = RA_TI * RA_TJ;
+
+__global__ void __launch_bounds__(RA_NT)
+    k_reinit_a2d(const double *__restrict__ phi, const double *__restrict__ sg, const double *__restrict__ De,
+                 double *__restrict__ G, double *__restrict__ s, double *__restrict__ A, double *__restrict__ B, Dims D,
+                 double rdt, const StepScalars *sc) {
+    constexpr int PI = RA_TI + 6, PJ = RA_TJ + 6;   // phi with three ghost layers
+    constexpr int DI = RA_TI + 4, DJ = RA_TJ + 4;   // second differences at -2 .. T+1
+    constexpr int QI = RA_TI + 3, QJ = RA_TJ + 3;   // pairs at -2 .. T
+    __shared__ double P[PI][PJ];
+    __shared__ double D0[DI][RA_TJ], D1[RA_TI][DJ];            // D2 along axis 0 / axis 1
+    __shared__ double Q0[3][QI][RA_TJ], Q1[3][RA_TI][QJ];      // (eps + X, Y, B)^2 per pair
+    __shared__ double fsrc;                                    // rdt / dt
+    const int tid = threadIdx.x;
+    const int I0 = blockIdx.y * RA_TI, J0 = blockIdx.x * RA_TJ;
+    if (tid == 0) fsrc = rdt / sc->dt;
+    // phi with three layers around the tile (array rows/columns -3 .. n+2 exist)
+    for (int e = tid; e < PI * PJ; e += RA_NT) {
+        const int r = e / PJ, c = e - r * PJ;
+        const int I = I0 - 3 + r, J = J0 - 3 + c;
+        double v = 0.0;
+        if (I >= -GHC && I < D.n[0] + GHC && J >= -GHC && J < D.n[1] + GHC) v = phi[D.at(I + GHC, J + GHC, 0)];
+        P[r][c] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < DI * RA_TJ + RA_TI * DJ; e += RA_NT) {
+        if (e < DI * RA_TJ) {
+            const int a = e / RA_TJ, b = e - a * RA_TJ;   // D0: tile rows -2 .. T+1
+            D0[a][b] = P[a + 2][b + 3] - 2.0 * P[a + 1][b + 3] + P[a][b + 3];
+        } else {
+            const int f = e - DI * RA_TJ, r = f / DJ, c = f - r * DJ;   // D1: columns -2 .. T+1
+            D1[r][c] = P[r + 3][c + 2] - 2.0 * P[r + 3][c + 1] + P[r + 3][c];
+        }
+    }
+    __syncthreads();
+    auto pair_q = [](double u, double w, double &qx, double &qy, double &qb) {
+        const double d = w - u, t = 13.0 * d * d;
+        const double x = w - 3.0 * u, y = 3.0 * w - u, z = w + u;
+        const double ex = WENO_EPS + (t + 3.0 * x * x), ey = WENO_EPS + (t + 3.0 * y * y),
+                     eb = WENO_EPS + (t + 3.0 * z * z);
+        qx = ex * ex, qy = ey * ey, qb = eb * eb;
+    };
+    for (int e = tid; e < QI * RA_TJ + RA_TI * QJ; e += RA_NT) {
+        if (e < QI * RA_TJ) {
+            const int a = e / RA_TJ, b = e - a * RA_TJ;   // pair p = a - 2 along axis 0
+            pair_q(D0[a][b], D0[a + 1][b], Q0[0][a][b], Q0[1][a][b], Q0[2][a][b]);
+        } else {
+            const int f = e - QI * RA_TJ, r = f / QJ, c = f - r * QJ;   // pair p = c - 2 along axis 1
+            pair_q(D1[r][c], D1[r][c + 1], Q1[0][r][c], Q1[1][r][c], Q1[2][r][c]);
+        }
+    }
+    __syncthreads();
+    const int ti = tid / RA_TJ, tj = tid - ti * RA_TJ;
+    const int I = I0 + ti, J = J0 + tj;
+    if (I >= D.n[0] || J >= D.n[1]) return;
+    const long long o = D.at(I + GHC, J + GHC, 0);
+    const double sgn = sg[o];
+    // weights of one correction from its three squared indicator terms and D2 values a..d
+    auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double d) {
+        const double p12 = q1 * q2, p01 = q0 * q1;
+        const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
+        return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
+    };
+    double g2 = 0.0;
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax) {
+        // D2 at i-2 .. i+2 and the pair terms of this cell along axis ax (index i = cell)
+        double d2[5], qX0, qX1, qY0, qY1, qB0, qB1;
+        double m2, m1, c0, p1, p2;
+        if (ax == 0) {
+            for (int k = 0; k < 5; ++k) d2[k] = D0[ti + k][tj];   // D0 row ti+k is D2 at ti-2+k
+            qX0 = Q0[0][ti + 2][tj], qX1 = Q0[0][ti + 3][tj];     // X(i), X(i+1)
+            qY0 = Q0[1][ti][tj], qY1 = Q0[1][ti + 1][tj];         // Y(i-2), Y(i-1)
+            qB0 = Q0[2][ti + 1][tj], qB1 = Q0[2][ti + 2][tj];     // B(i-1), B(i)
+            m2 = P[ti + 1][tj + 3], m1 = P[ti + 2][tj + 3], c0 = P[ti + 3][tj + 3];
+            p1 = P[ti + 4][tj + 3], p2 = P[ti + 5][tj + 3];
+        } else {
+            for (int k = 0; k < 5; ++k) d2[k] = D1[ti][tj + k];
+            qX0 = Q1[0][ti][tj + 2], qX1 = Q1[0][ti][tj + 3];
+            qY0 = Q1[1][ti][tj], qY1 = Q1[1][ti][tj + 1];
+            qB0 = Q1[2][ti][tj + 1], qB1 = Q1[2][ti][tj + 2];
+            m2 = P[ti + 3][tj + 1], m1 = P[ti + 3][tj + 2], c0 = P[ti + 3][tj + 3];
+            p1 = P[ti + 3][tj + 4], p2 = P[ti + 3][tj + 5];
+        }
+        const double ih = D.rd[ax];
+        const double v = ih * (1.0 / 12.0) * (-(m1 - m2) + 7.0 * (c0 - m1) + 7.0 * (p1 - c0) - (p2 - p1));
+        // forward: (q0, q1, q2) = (X(i+1), B(i), Y(i-1)); backward: (Y(i-2), B(i-1), X(i))
+        const double Sp = qB1 * qY1 + 6.0 * qX1 * qY1 + 3.0 * qX1 * qB1;
+        const double Sm = qB0 * qX0 + 6.0 * qY0 * qX0 + 3.0 * qY0 * qB0;
+        const double r = 1.0 / (Sp * Sm);
+        const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
+        const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
+        const double dp = v + ih * wp, dm = v - ih * wm;
+        const double g = sgn > 0.0 ? fmax(-fmin(dp, 0.0), fmax(dm, 0.0)) : fmax(fmax(dp, 0.0), -fmin(dm, 0.0));
+        g2 += g * g;
+    }
+    const double g = sqrt(g2);
+    const double de = De[o];
+    G[o] = g;
+    s[o] = -sgn * (g - 1.0) * fsrc;
+    A[o] = sgn * de * (g - 1.0);
+    B[o] = g * de * de;
+}
+
 // lambda correction with the zero-order-extrapolated a, b (a ghost reads the nearest
 // interior cell) and the stage update (the update reads only per-cell fields, so it can
 // run in place on phi).
@@ -223,6 +343,9 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
                            double *__restrict__ sk, const double *__restrict__ s1, const double *__restrict__ s2,
                            const double *__restrict__ A, const double *__restrict__ B, Dims D, double rdt,
                            int lambda, int stage, const StepScalars *sc, GhostFill GF) {
+    __shared__ double fsrc;   // rdt / dt, one division per block
+    if (threadIdx.x == 0) fsrc = rdt / sc->dt;
+    __syncthreads();
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= D.interior()) return;
     int I, J, K;
@@ -254,13 +377,13 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
                         b += B[p];
                     }
         }
-        if (fabs(b) > 1e-8) s += a / b * De[o] * G[o] * rdt / dt;
+        if (fabs(b) > 1e-8) s += a / b * De[o] * G[o] * fsrc;
         sk[o] = s;
     }
     double f = phi[o];
     if (stage == 1) f += dt * s;
     else if (stage == 2) f += dt * (s - 3.0 * s1[o]) / 4.0;
-    else f += dt * (-s1[o] - s2[o] + 8.0 * s) / 12.0;
+    else f += dt * (-s1[o] - s2[o] + 8.0 * s) * (1.0 / 12.0);
     phi[o] = f;
     if (GF.on) neumann_ghosts(phi, o, I, J, K, D, GF, f);
 }
@@ -786,7 +909,11 @@ void TwoPhaseGpu::mpls(int count) {
 void TwoPhaseGpu::reinit_stage(int stage) {
     const unsigned nbi = blocks_for(D.interior(), TPB);
     double *S[3] = {s1, s2, s3};
-    k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
+    if (D.ndim == 2)
+        k_reinit_a2d<<<dim3(unsigned((D.n[1] + RA_TJ - 1) / RA_TJ), unsigned((D.n[0] + RA_TI - 1) / RA_TI)), RA_NT, 0,
+                       stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
+    else
+        k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
     k_reinit_b<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, S[stage - 1], s1, s2, a_f, b_f, D, P.rdt, reinit_lambda,
                                         stage, sc, phi_fill);
     if (!phi_fill.on) scalar_bc(phi.data);
