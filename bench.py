@@ -465,16 +465,23 @@ def learned_block(torch, n: int = 256, ntrain: int = 96, ntest: int = 12, steps:
     te = make_snapshots(n, range(10 ** 6, 10 ** 6 + ntest), torch, dev)
     t_snap = _t.perf_counter() - t0
     net = UNet(n, n, seed=0)
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+
+    def test_loss():
+        # mean loss on the held-out snapshots (loss_grad leaves the weights unchanged)
+        return float(np.mean([net.loss_grad(g, *s) for s in te]))
+
+    loss_before = test_loss()
     torch.cuda.synchronize()
     t0 = _t.perf_counter()
-    losses = train(net, tr, steps, 3e-4, torch)
+    losses = train(net, tr, steps, 3e-4, torch, cosine=True)
     torch.cuda.synchronize()
     t_train = _t.perf_counter() - t0
+    loss_after = test_loss()
     # inference time and its convolution work (2 * 9 * ci * co * pixels per layer)
     layers = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (64, 128, 3),
               (128, 128, 3), (192, 64, 2), (64, 64, 2), (96, 32, 1), (32, 32, 1), (48, 16, 0), (16, 16, 0), (16, 16, 0)]
     flops = sum(2.0 * 9 * ci * co * (n >> lv) ** 2 for ci, co, lv in layers)
-    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
     rho, rhs, pprev, _ = te[0]
     guess = pprev.clone()
     for _ in range(3):
@@ -498,7 +505,8 @@ def learned_block(torch, n: int = 256, ntrain: int = 96, ntest: int = 12, steps:
     net.close()
     return {"grid": f"{n}x{n}", "train_snapshots": ntrain, "test_snapshots": ntest, "train_steps": steps,
             "snapshot_s": t_snap, "train_ms_per_step": 1e3 * t_train / steps,
-            "loss_first50": float(np.mean(losses[:50])), "loss_last50": float(np.mean(losses[-50:])),
+            "lr": "3e-4, half-cosine decay to 0", "test_loss_before": loss_before, "test_loss_after": loss_after,
+            "train_loss_first150": float(np.mean(losses[:150])), "train_loss_last150": float(np.mean(losses[-150:])),
             "infer_ms": 1e3 * t_inf, "infer_conv_tflops": flops / t_inf / 1e12,
             "vcycles_from_pprev": float(np.mean(base_it)), "vcycles_from_net": float(np.mean(net_it)),
             "ms_to_tol_from_pprev": 1e3 * t_base, "ms_to_tol_from_net_incl_inference": 1e3 * t_net,

@@ -73,8 +73,9 @@ def make_snapshots(n: int, seeds, torch, device, rel_tol: float = 1e-10, fp32: b
     return out
 
 
-def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0):
-    """Adam steps over the snapshots in a seeded random order; returns the loss history."""
+def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0, cosine: bool = False):
+    """Adam steps over the snapshots in a seeded random order; returns the loss history.
+    cosine: the learning rate decays from lr to 0 along a half cosine over the steps."""
     n = snaps[0][0].shape[0] - 6
     g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
     rng = np.random.default_rng(seed)
@@ -82,7 +83,8 @@ def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0):
     torch.cuda.synchronize()
     for k in range(steps):
         rho, rhs, pprev, p = snaps[int(rng.integers(len(snaps)))]
-        losses.append(net.train_step(g, rho, rhs, pprev, p, lr))
+        lr_k = lr * 0.5 * (1.0 + math.cos(math.pi * k / steps)) if cosine else lr
+        losses.append(net.train_step(g, rho, rhs, pprev, p, lr_k))
     return losses
 
 
