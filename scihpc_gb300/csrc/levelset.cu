@@ -157,10 +157,8 @@ __global__ void integral_kernel(const double *__restrict__ w, Dims D, int which,
     const long long per_block = (n + gridDim.x - 1) / gridDim.x;
     const long long b0 = blockIdx.x * per_block;
     const long long b1 = b0 + per_block < n ? b0 + per_block : n;
-    const long long per = (b1 - b0 + blockDim.x - 1) / blockDim.x;
-    const long long t0 = b0 + threadIdx.x * per;
     double s = 0.0;
-    for (long long q = t0; q < t0 + per && q < b1; ++q) s += integral_cell(w, q, D, which);
+    for (long long q = b0 + threadIdx.x; q < b1; q += blockDim.x) s += integral_cell(w, q, D, which);
     s = block_reduce<SumOp>(s, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }

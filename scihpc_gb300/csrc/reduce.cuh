@@ -48,7 +48,7 @@ constexpr int RED_THREADS = 256;
 constexpr int RED_MAX_BLOCKS = 1024;
 
 inline int red_blocks(long long n) {
-    long long b = (n + RED_THREADS * 8 - 1) / (RED_THREADS * 8);
+    long long b = (n + RED_THREADS * 2 - 1) / (RED_THREADS * 2);   // short chains: these grids are small
     if (b < 1) b = 1;
     if (b > RED_MAX_BLOCKS) b = RED_MAX_BLOCKS;
     return int(b);

@@ -124,10 +124,10 @@ __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restri
     const long long per_block = (n + gridDim.x - 1) / gridDim.x;
     const long long b0 = blockIdx.x * per_block;
     const long long b1 = b0 + per_block < n ? b0 + per_block : n;
-    const long long per = (b1 - b0 + blockDim.x - 1) / blockDim.x;
-    const long long t0 = b0 + threadIdx.x * per;
-    double sm = 0.0, se = 0.0;
-    for (long long q = t0; q < t0 + per && q < b1; ++q) {
+    // the block's cells are interleaved over its threads (coalesced); interior-stencil and
+    // boundary contributions are summed apart and scaled once at the end
+    double si = 0.0, sb = 0.0, se = 0.0;
+    for (long long q = b0 + threadIdx.x; q < b1; q += blockDim.x) {
         int I, J, K;
         split3(q, D, I, J, K);
         const int i = D.ix(0, I), j = D.ix(1, J), k = D.ix(2, K);
@@ -138,9 +138,9 @@ __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restri
                 double s = 15.0 * w[o];
                 for (int a = -1; a < 2; ++a)
                     for (int b = -1; b < 2; ++b) s += w[o + a * D.s[0] + b * D.s[1]];
-                sm += s / 24.0;
+                si += s;
             } else {
-                sm += w[o];
+                sb += w[o];
             }
         } else {
             if (I != 0 && I != D.n[0] - 1 && J != 0 && J != D.n[1] - 1 && K != 0 && K != D.n[2] - 1) {
@@ -148,15 +148,16 @@ __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restri
                 for (int a = -1; a < 2; ++a)
                     for (int b = -1; b < 2; ++b)
                         for (int c = -1; c < 2; ++c) s += w[o + a * D.s[0] + b * D.s[1] + c];
-                sm += s * D.dv / 77.0;
+                si += s;
             } else {
-                sm += w[o] * D.dv;
+                sb += w[o];
             }
         }
         const double de = De[o], hv = H[o];
         const double g = pos ? de * (2.0 * (1.0 - dr) * hv + dr) : de * (2.0 * (dr - 1.0) * hv + 1.0);
         se += g * de * G[o];
     }
+    const double sm = D.ndim == 2 ? si * (1.0 / 24.0) + sb : si * (D.dv / 77.0) + sb * D.dv;
     const double a = block_reduce<SumOp>(sm, sh);
     __syncthreads();
     const double b = block_reduce<SumOp>(se, sh);
@@ -577,10 +578,8 @@ __global__ void k_dt_part(const double *__restrict__ u, const double *__restrict
     const long long per_block = (n + gridDim.x - 1) / gridDim.x;
     const long long b0 = blockIdx.x * per_block;
     const long long b1 = b0 + per_block < n ? b0 + per_block : n;
-    const long long per = (b1 - b0 + blockDim.x - 1) / blockDim.x;
-    const long long t0 = b0 + threadIdx.x * per;
     DtPart acc{0.0, 0.0, 0.0, 1.0, 0.0};
-    for (long long q = t0; q < t0 + per && q < b1; ++q) {
+    for (long long q = b0 + threadIdx.x; q < b1; q += blockDim.x) {
         int I, J, K;
         split3(q, D, I, J, K);
         const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
