@@ -233,7 +233,7 @@ __global__ void k_reinit_a(const double *__restrict__ phi, const double *__restr
 // Tiles of RA_TI (axis 0) x RA_TJ (axis 1) cells: 256 tiles for the 128 x 256 bubble, so
 // that every SM has FP64 work.
 constexpr int RA_TI = 8, RA_TJ = 16;
-constexpr int RA_NT = RA_TI * RA_TJ;
+constexpr int RA_NT = 2 * RA_TI * RA_TJ;   // two threads per cell: one per axis
 
 __global__ void __launch_bounds__(RA_NT)
     k_reinit_a2d(const double *__restrict__ phi, const double *__restrict__ sg, const double *__restrict__ De,
@@ -285,10 +285,12 @@ __global__ void __launch_bounds__(RA_NT)
         }
     }
     __syncthreads();
-    const int ti = tid / RA_TJ, tj = tid - ti * RA_TJ;
+    // thread pair (2c, 2c + 1) owns cell c; the even thread takes axis 0, the odd one axis 1
+    const int ax = tid & 1, cell = tid >> 1;
+    const int ti = cell / RA_TJ, tj = cell - ti * RA_TJ;
     const int I = I0 + ti, J = J0 + tj;
-    if (I >= D.n[0] || J >= D.n[1]) return;
-    const long long o = D.at(I + GHC, J + GHC, 0);
+    const bool live = I < D.n[0] && J < D.n[1];
+    const long long o = live ? D.at(I + GHC, J + GHC, 0) : D.at(GHC, GHC, 0);
     const double sgn = sg[o];
     // weights of one correction from its three squared indicator terms and D2 values a..d
     auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double d) {
@@ -296,45 +298,42 @@ __global__ void __launch_bounds__(RA_NT)
         const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
         return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
     };
-    double g2 = 0.0;
-#pragma unroll
-    for (int ax = 0; ax < 2; ++ax) {
-        // D2 at i-2 .. i+2 and the pair terms of this cell along axis ax (index i = cell)
-        double d2[5], qX0, qX1, qY0, qY1, qB0, qB1;
-        double m2, m1, c0, p1, p2;
-        if (ax == 0) {
-            for (int k = 0; k < 5; ++k) d2[k] = D0[ti + k][tj];   // D0 row ti+k is D2 at ti-2+k
-            qX0 = Q0[0][ti + 2][tj], qX1 = Q0[0][ti + 3][tj];     // X(i), X(i+1)
-            qY0 = Q0[1][ti][tj], qY1 = Q0[1][ti + 1][tj];         // Y(i-2), Y(i-1)
-            qB0 = Q0[2][ti + 1][tj], qB1 = Q0[2][ti + 2][tj];     // B(i-1), B(i)
-            m2 = P[ti + 1][tj + 3], m1 = P[ti + 2][tj + 3], c0 = P[ti + 3][tj + 3];
-            p1 = P[ti + 4][tj + 3], p2 = P[ti + 5][tj + 3];
-        } else {
-            for (int k = 0; k < 5; ++k) d2[k] = D1[ti][tj + k];
-            qX0 = Q1[0][ti][tj + 2], qX1 = Q1[0][ti][tj + 3];
-            qY0 = Q1[1][ti][tj], qY1 = Q1[1][ti][tj + 1];
-            qB0 = Q1[2][ti][tj + 1], qB1 = Q1[2][ti][tj + 2];
-            m2 = P[ti + 3][tj + 1], m1 = P[ti + 3][tj + 2], c0 = P[ti + 3][tj + 3];
-            p1 = P[ti + 3][tj + 4], p2 = P[ti + 3][tj + 5];
-        }
-        const double ih = D.rd[ax];
-        const double v = ih * (1.0 / 12.0) * (-(m1 - m2) + 7.0 * (c0 - m1) + 7.0 * (p1 - c0) - (p2 - p1));
-        // forward: (q0, q1, q2) = (X(i+1), B(i), Y(i-1)); backward: (Y(i-2), B(i-1), X(i))
-        const double Sp = qB1 * qY1 + 6.0 * qX1 * qY1 + 3.0 * qX1 * qB1;
-        const double Sm = qB0 * qX0 + 6.0 * qY0 * qX0 + 3.0 * qY0 * qB0;
-        const double r = 1.0 / (Sp * Sm);
-        const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
-        const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
-        const double dp = v + ih * wp, dm = v - ih * wm;
-        const double g = sgn > 0.0 ? fmax(-fmin(dp, 0.0), fmax(dm, 0.0)) : fmax(fmax(dp, 0.0), -fmin(dm, 0.0));
-        g2 += g * g;
-    }
+    // D2 at i-2 .. i+2 and the pair terms of this cell along axis ax (index i = cell)
+    double d2[5];
+    for (int k = 0; k < 5; ++k) d2[k] = ax == 0 ? D0[ti + k][tj] : D1[ti][tj + k];   // D2 at i-2+k
+    const double qX0 = ax == 0 ? Q0[0][ti + 2][tj] : Q1[0][ti][tj + 2];   // X(i)
+    const double qX1 = ax == 0 ? Q0[0][ti + 3][tj] : Q1[0][ti][tj + 3];   // X(i+1)
+    const double qY0 = ax == 0 ? Q0[1][ti][tj] : Q1[1][ti][tj];           // Y(i-2)
+    const double qY1 = ax == 0 ? Q0[1][ti + 1][tj] : Q1[1][ti][tj + 1];   // Y(i-1)
+    const double qB0 = ax == 0 ? Q0[2][ti + 1][tj] : Q1[2][ti][tj + 1];   // B(i-1)
+    const double qB1 = ax == 0 ? Q0[2][ti + 2][tj] : Q1[2][ti][tj + 2];   // B(i)
+    const double m2 = ax == 0 ? P[ti + 1][tj + 3] : P[ti + 3][tj + 1];
+    const double m1 = ax == 0 ? P[ti + 2][tj + 3] : P[ti + 3][tj + 2];
+    const double c0 = P[ti + 3][tj + 3];
+    const double p1 = ax == 0 ? P[ti + 4][tj + 3] : P[ti + 3][tj + 4];
+    const double p2 = ax == 0 ? P[ti + 5][tj + 3] : P[ti + 3][tj + 5];
+    const double ih = D.rd[ax];
+    const double v = ih * (1.0 / 12.0) * (-(m1 - m2) + 7.0 * (c0 - m1) + 7.0 * (p1 - c0) - (p2 - p1));
+    // forward: (q0, q1, q2) = (X(i+1), B(i), Y(i-1)); backward: (Y(i-2), B(i-1), X(i))
+    const double Sp = qB1 * qY1 + 6.0 * qX1 * qY1 + 3.0 * qX1 * qB1;
+    const double Sm = qB0 * qX0 + 6.0 * qY0 * qX0 + 3.0 * qY0 * qB0;
+    const double r = 1.0 / (Sp * Sm);
+    const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
+    const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
+    const double dp = v + ih * wp, dm = v - ih * wm;
+    const double ga = sgn > 0.0 ? fmax(-fmin(dp, 0.0), fmax(dm, 0.0)) : fmax(fmax(dp, 0.0), -fmin(dm, 0.0));
+    const double gg = ga * ga;
+    const double g2 = gg + __shfl_xor_sync(0xffffffffu, gg, 1);   // the same sum in both threads
+    if (!live) return;
     const double g = sqrt(g2);
     const double de = De[o];
-    G[o] = g;
-    s[o] = -sgn * (g - 1.0) * fsrc;
-    A[o] = sgn * de * (g - 1.0);
-    B[o] = g * de * de;
+    if (ax == 0) {
+        G[o] = g;
+        s[o] = -sgn * (g - 1.0) * fsrc;
+    } else {
+        A[o] = sgn * de * (g - 1.0);
+        B[o] = g * de * de;
+    }
 }
 
 // lambda correction with the zero-order-extrapolated a, b (a ghost reads the nearest
