@@ -1338,7 +1338,7 @@ __global__ void k_dense_pin_and_invert(double *__restrict__ M, double *__restric
 // loads and a shuffle reduction.
 template <class T, int DIM>
 __device__ __forceinline__ void dense_apply(const Level<T> &L, const double *__restrict__ Minv, int n, int neumann,
-                                            double *b, double *mean) {
+                                            double *b, double *mean, const double (*pre)[2] = nullptr) {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nw = blockDim.x >> 5;
     auto pidx = [&](int c) {
         int I, J, K = 0;
@@ -1363,6 +1363,18 @@ __device__ __forceinline__ void dense_apply(const Level<T> &L, const double *__r
     }
     __syncthreads();
     const double mu = *mean;
+    if (pre) {   // n <= 64 and 32 warps: rows warp, warp + 32; this lane's entries lane, lane + 32
+        for (int r = 0; r < 2; ++r) {
+            const int c = warp + 32 * r;
+            if (c >= n) break;
+            double v = 0.0;
+            for (int e = 0; e < 2; ++e)
+                if (lane + 32 * e < n) v += pre[r][e] * (b[lane + 32 * e] - mu);
+            for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+            if (lane == 0) L.x[pidx(c)] = T(v);
+        }
+        return;
+    }
     for (int c = warp; c < n; c += nw) {
         const double *row = Minv + (size_t)c * n;
         double v = 0.0;
@@ -1630,10 +1642,20 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
     __shared__ double mean;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int nu = 2;
+    // the coarsest inverse's rows, fetched now so that the dense solve does not wait for them
+    double pre[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    const bool prefetch = n <= 64 && nt == 1024;
+    if (prefetch)
+        for (int r = 0; r < 2; ++r)
+            for (int e = 0; e < 2; ++e) {
+                const int c = (tid >> 5) + 32 * r, q = (tid & 31) + 32 * e;
+                if (c < n && q < n) pre[r][e] = Minv[(size_t)c * n + q];
+            }
     if (tid == 0)
         for (int l = lc; l < nlev; ++l) SL[l] = LP.L[l];
     __syncthreads();
     if (smem_on) {
+        // copied with asynchronous copies, all in flight at once
         T *p = reinterpret_cast<T *>(coarse_dsm);
         for (int l = lc; l < nlev; ++l) {
             const Level<T> &G = LP.L[l];
@@ -1641,18 +1663,36 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
             T *x = p, *bb = p + c, *cx = p + 2 * c, *cy = p + 3 * c, *cz = DIM == 3 ? p + 4 * c : nullptr;
             T *idg = p + (DIM == 3 ? 5 : 4) * c;
             for (int i = tid; i < int(c); i += nt) {
-                x[i] = l == lc ? G.x[i] : T(0);
-                bb[i] = l == lc ? G.b[i] : T(0);
-                cx[i] = G.cx[i];
-                cy[i] = G.cy[i];
-                if (DIM == 3) cz[i] = G.cz[i];
-                idg[i] = G.idg[i];
+                if (sizeof(T) == 4) {
+                    if (l == lc) {
+                        tc::cp4(&x[i], &G.x[i]);
+                        tc::cp4(&bb[i], &G.b[i]);
+                    } else {
+                        x[i] = T(0);
+                        bb[i] = T(0);
+                    }
+                    tc::cp4(&cx[i], &G.cx[i]);
+                    tc::cp4(&cy[i], &G.cy[i]);
+                    if (DIM == 3) tc::cp4(&cz[i], &G.cz[i]);
+                    tc::cp4(&idg[i], &G.idg[i]);
+                } else {
+                    x[i] = l == lc ? G.x[i] : T(0);
+                    bb[i] = l == lc ? G.b[i] : T(0);
+                    cx[i] = G.cx[i];
+                    cy[i] = G.cy[i];
+                    if (DIM == 3) cz[i] = G.cz[i];
+                    idg[i] = G.idg[i];
+                }
             }
             if (tid == 0) {
                 SL[l].x = x, SL[l].b = bb, SL[l].cx = cx, SL[l].cy = cy, SL[l].idg = idg;
                 if (DIM == 3) SL[l].cz = cz;
             }
             p += (DIM == 3 ? 6 : 5) * c;
+        }
+        if (sizeof(T) == 4) {
+            tc::cp_commit();
+            tc::cp_wait_all();
         }
         __syncthreads();
     }
@@ -1669,7 +1709,7 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
         for (long long t = tid; t < nc; t += nt) restrict_one<T, 0, DIM>(L, Cl, nullptr, nullptr, t);
         __syncthreads();
     }
-    dense_apply<T, DIM>(SL[nlev - 1], Minv, n, neumann, b, &mean);
+    dense_apply<T, DIM>(SL[nlev - 1], Minv, n, neumann, b, &mean, prefetch ? pre : nullptr);
     __syncthreads();
     for (int l = nlev - 2; l >= lc; --l) {
         const Level<T> &L = SL[l];

@@ -116,6 +116,10 @@ __device__ __forceinline__ void cp16(void *smem, const void *gmem, uint32_t src_
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem), "r"(src_bytes)
                  : "memory");
 }
+// 4-byte asynchronous copy global -> shared (no alignment beyond the element's)
+__device__ __forceinline__ void cp4(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
