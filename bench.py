@@ -392,6 +392,7 @@ def run_ours(args) -> None:
             "diagnostics": diag}
     if rank == 0 and not args.no_poisson:
         line["poisson_256^3"] = poisson_block(torch, Poisson, Grid, hbm)
+        line["poisson_256^2_dirichlet"] = dirichlet_block(torch, Poisson, Grid, cpu=not args.no_cpu)
         line["dambreak_3d"] = dambreak_block(torch, TwoPhase, Grid)
         line["learned_guess"] = learned_block(torch)
     if rank == 0 and not args.no_cpu:
@@ -401,6 +402,58 @@ def run_ours(args) -> None:
                                           "restatement in oracle/port, all host cores)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def dirichlet_block(torch, Poisson, Grid, cpu: bool) -> dict:
+    """256^2 constant-coefficient Poisson problem with the reference's Dirichlet operator
+    (-lap p = 2 pi^2 sin(pi x) sin(pi y) on [0,1]^2, zero guess) to relative residual 1e-10:
+    FP64 V-cycles in FP64 CG and FP32 V-cycles in FP64 refinement on the GPU; with `cpu`, the
+    reference multigrid (v_cycle, restated in oracle/port) on the host cores beside it."""
+    import numpy as np
+    n = 256
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    h = 1.0 / n
+    xc = (np.arange(n) + 0.5) * h
+    X, Y = np.meshgrid(xc, xc, indexing="ij")
+    f = 2 * np.pi ** 2 * np.sin(np.pi * X) * np.sin(np.pi * Y)
+    rhs_h = np.zeros((n + 6, n + 6, 1))
+    rhs_h[3:-3, 3:-3, 0] = -f   # A p = -f with A the reference's +laplacian
+    rhs = torch.from_numpy(rhs_h).cuda()
+    out = {"grid": "256^2", "problem": "-lap p = 2 pi^2 sin(pi x) sin(pi y), Dirichlet (reference operator)",
+           "rel_tol": 1e-10}
+    for name, fp32 in (("fp64", False), ("fp32_refined", True)):
+        ps = Poisson(g, bc=1, density=False, fp32=fp32)
+        p = torch.zeros(rhs.shape, dtype=torch.float64, device="cuda")
+        ps.solve(rhs, p, rel_tol=1e-10, max_iter=100)   # warm
+        times = []
+        for _ in range(3):
+            p.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            it, rr = ps.solve(rhs, p, rel_tol=1e-10, max_iter=100)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        out[name] = {"ms_to_tol": min(times), "iterations": it, "final_relres": rr}
+        ps.close()
+    out["fp32_speedup"] = out["fp64"]["ms_to_tol"] / out["fp32_refined"]["ms_to_tol"]
+    out["note"] = "host-driven solve (one host synchronisation per iteration) timed by CUDA events"
+    if cpu:
+        import oracle as O
+        gg = O.Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+        port = O.Checker("port")
+        port.mg_poisson(gg, (-f).T.ravel(), True, 1e-10, 400)   # warm
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            _, cyc, hist = port.mg_poisson(gg, (-f).T.ravel(), True, 1e-10, 400)
+            ts.append(time.perf_counter() - t0)
+        out["cpu_baseline"] = {"value": 1e3 * float(np.median(ts)), "unit": "ms to rel. residual 1e-10",
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"reference multigrid v_cycle ({cyc} cycles, final relres "
+                                         f"{float(hist[-1]):.1e}), median of 3"}
+    return out
 
 
 def dambreak_block(torch, TwoPhase, Grid, steps: int = 40, warmup: int = 3) -> dict:
