@@ -151,6 +151,10 @@ int scihpc_poisson_set_density(scihpc_poisson *ps, const double *rho, void *stre
  * iterations and the final relative residual on the host (synchronises `stream`). */
 int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int use_guess, double rel_tol,
                          int max_iter, int *iters, double *relres, void *stream);
+/* ||rhs - A p|| (2-norm over interior cells; for Neumann walls rhs minus its mean) of the
+ * solver's operator, on the GPU in FP64; synchronises `stream`.  The residual() of
+ * multigrid_base (multigrid_base.cpp:69-72) for the finest level. */
+int scihpc_poisson_residual(scihpc_poisson *ps, const double *rhs, const double *p, double *norm, void *stream);
 /* Times `ncycles` V-cycles (the preconditioner alone, on the residual of p = 0 for rhs)
  * with CUDA events on `stream`; *ms receives the total.  p is overwritten with zeros.
  * Synchronises `stream`.  Measurement hook with no reference counterpart. */

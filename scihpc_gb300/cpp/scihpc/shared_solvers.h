@@ -1,16 +1,18 @@
 // shared_solvers.h -- the per-grid solver bundle of the reference (scihpc/shared_solvers.h:
 // 13-26).  On the GPU the line-solve factorisations and the multigrid hierarchy live inside
-// the device session, so the bundle only records which pressure boundary the drivers asked
-// for.
+// the device session; the bundle records which pressure boundary the drivers asked for and
+// holds a GPU-backed multigrid object for drivers that run the Poisson solver directly.
 #ifndef SCIHPC_GB300_SHARED_SOLVERS_H
 #define SCIHPC_GB300_SHARED_SOLVERS_H
 
+#include "multigrid.h"
 #include "scalar_data.h"
 #include "structured_grid.h"
 
 struct shared_solvers {
     structured_grid *geo = nullptr;
-    int mg_bc = -1;   // -1 none, 0 Neumann, 1 Dirichlet
+    int mg_bc = -1;            // -1 none, 0 Neumann, 1 Dirichlet
+    multigrid *mg = nullptr;   // GPU-backed (multigrid.h)
 };
 
 shared_solvers *SharedSolvers_alloc(scalar_data *f, structured_grid *geo);

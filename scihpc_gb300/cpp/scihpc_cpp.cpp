@@ -30,6 +30,7 @@
 #include "scihpc/global.h"
 #include "scihpc/gpu_session.h"
 #include "scihpc/lsm.h"
+#include "scihpc/multigrid.h"
 #include "scihpc/projection_method.h"
 #include "scihpc/runge_kutta.h"
 #include "scihpc/scalar_data.h"
@@ -560,14 +561,196 @@ void wrapper::apply_vel_z_bc() const {
     bcFactoryW->apply_node_staggered_z(&vector->z);
 }
 
+// ---------------------------------------------------------------- multigrid
+DataType VectorX::norm() const {
+    DataType s = 0.0;
+    for (DataType x : v_) s += x * x;
+    return std::sqrt(s);
+}
+
+multigrid_base::multigrid_base(int _nx, int _ny, int _degree, DataType _dx, DataType _dy)
+    : nx(_nx), ny(_ny), nz(1), degree(_degree), ndim(2), n(_nx * _ny), dx(_dx), dy(_dy), dz(0.0) {
+    rhs.resize(n), sol.resize(n), res.resize(n), buffer.resize(n);
+}
+
+multigrid_base::multigrid_base(int _nx, int _ny, int _nz, int _degree, DataType _dx, DataType _dy, DataType _dz)
+    : nx(_nx), ny(_ny), nz(_nz), degree(_degree), ndim(3), n(_nx * _ny * _nz), dx(_dx), dy(_dy), dz(_dz) {
+    rhs.resize(n), sol.resize(n), res.resize(n), buffer.resize(n);
+}
+
+int multigrid_base::of(int i, int j, int k) { return i + j * nx + k * nx * ny; }
+int multigrid_base::of(int i, int j) { return i + j * nx; }
+
+namespace {
+void select_bc(multigrid_base *b, int code) {
+    multigrid *m = b->owner;
+    if (!m || b->level != 0 || m->bc == code) return;
+    m->bc = code;
+    if (m->gpu) {   // the operator changed: rebuild at the next cycle
+        scihpc_poisson_destroy(m->gpu);
+        m->gpu = nullptr;
+    }
+}
+// recorded in the status; printed once per kind (drivers call these in their cycle loops)
+void internal(const char *what) {
+    static std::map<std::string, bool> said;
+    const std::string msg = std::string(what) + ": the coarse levels and their transfers live inside the GPU cycle";
+    g_status = SCIHPC_ERR_UNSUPPORTED;
+    g_message = msg;
+    if (!said[what]) std::fprintf(stderr, "scihpc_gb300: %s\n", msg.c_str());
+    said[what] = true;
+}
+}  // namespace
+
+void multigrid_base::init_NeumannBC() { select_bc(this, 0); }
+void multigrid_base::init_DirichletBC() { select_bc(this, 1); }
+
+// the mean removal of multigrid_base.cpp:47-67 (a host vector the caller owns)
+void multigrid_base::compatibility_condition(VectorX &f) {
+    if (no_compatibility || f.size() == 0) return;
+    DataType s = 0.0;
+    for (long i = 0; i < f.size(); ++i) s += f[i];
+    s /= DataType(f.size());
+    for (long i = 0; i < f.size(); ++i) f[i] -= s;
+}
+
+void multigrid_base::relax(int iter) {
+    if (level != 0 || !owner) return internal("multigrid_base::relax on a coarse level");
+    owner->iterate(iter);
+}
+
+DataType multigrid_base::residual() {
+    if (level != 0 || !owner) {
+        internal("multigrid_base::residual on a coarse level");
+        return 0.0;
+    }
+    double r = 0.0;
+    owner->residual(r);
+    return r;
+}
+
+void multigrid_base::Ax(const VectorX &) { internal("multigrid_base::Ax"); }
+void multigrid_base::restriction(multigrid_base *) { internal("multigrid_base::restriction"); }
+void multigrid_base::prolongation(multigrid_base *) { internal("multigrid_base::prolongation"); }
+void multigrid_base::solve() { internal("multigrid_base::solve"); }
+
+// one coarsening step of multigrid.cpp:10-41: halve if every halved extent stays above 3,
+// else divide by 3 likewise; returns the ratio (1: no further level)
+int multigrid::check2d(std::vector<int> &nx, std::vector<int> &ny) {
+    for (int r : {2, 3}) {
+        const int a = nx.back(), b = ny.back();
+        if (a % r == 0 && b % r == 0 && a / r > 3 && b / r > 3) {
+            nx.push_back(a / r), ny.push_back(b / r);
+            return r;
+        }
+    }
+    return 1;
+}
+
+int multigrid::check3d(std::vector<int> &nx, std::vector<int> &ny, std::vector<int> &nz) {
+    for (int r : {2, 3}) {
+        const int a = nx.back(), b = ny.back(), c = nz.back();
+        if (a % r == 0 && b % r == 0 && c % r == 0 && a / r > 3 && b / r > 3 && c / r > 3) {
+            nx.push_back(a / r), ny.push_back(b / r), nz.push_back(c / r);
+            return r;
+        }
+    }
+    return 1;
+}
+
+multigrid::multigrid(scalar_data *var, structured_grid *g) : geo(g) {
+    std::vector<int> nx{var->nx}, ny{var->ny}, nz{var->nz};
+    while ((var->ndim == 3 ? check3d(nx, ny, nz) : check2d(nx, ny)) > 1) {
+    }
+    level_num = unsigned(nx.size());
+    at = new multigrid_base *[level_num];
+    for (unsigned l = 0; l < level_num; ++l) {
+        const int deg = nx[0] / nx[l];
+        if (var->ndim == 3)
+            at[l] = new multigrid_base(nx[l], ny[l], nz[l], deg, g->dx * deg, g->dy * deg, g->dz * deg);
+        else
+            at[l] = new multigrid_base(nx[l], ny[l], deg, g->dx * deg, g->dy * deg);
+        at[l]->owner = this;
+        at[l]->level = int(l);
+    }
+}
+
+namespace {
+// interior vector (x fastest) <-> ghosted device field ([i][j][k], k fastest, ghost width 3)
+void to_ghosted(const multigrid_base *b, const VectorX &v, std::vector<double> &out) {
+    const int N1 = b->ny + 6, N2 = b->ndim == 3 ? b->nz + 6 : 1, g2 = b->ndim == 3 ? 3 : 0;
+    out.assign(size_t(b->nx + 6) * N1 * N2, 0.0);
+    for (int k = 0; k < b->nz; ++k)
+        for (int j = 0; j < b->ny; ++j)
+            for (int i = 0; i < b->nx; ++i)
+                out[(size_t(i + 3) * N1 + (j + 3)) * N2 + (k + g2)] = v[i + j * b->nx + k * b->nx * b->ny];
+}
+void from_ghosted(const multigrid_base *b, const std::vector<double> &in, VectorX &v) {
+    const int N1 = b->ny + 6, N2 = b->ndim == 3 ? b->nz + 6 : 1, g2 = b->ndim == 3 ? 3 : 0;
+    for (int k = 0; k < b->nz; ++k)
+        for (int j = 0; j < b->ny; ++j)
+            for (int i = 0; i < b->nx; ++i)
+                v[i + j * b->nx + k * b->nx * b->ny] = in[(size_t(i + 3) * N1 + (j + 3)) * N2 + (k + g2)];
+}
+
+bool mg_upload(multigrid *m) {
+    multigrid_base *f = m->at[0];
+    const scihpc_grid g = grid_of(m->geo);
+    if (!m->gpu) {
+        if (!check(scihpc_poisson_create(&g, m->bc, 0, g_pressure_fp32, &m->gpu), "poisson_create")) return false;
+        const size_t cells = size_t(f->nx + 6) * (f->ny + 6) * (f->ndim == 3 ? f->nz + 6 : 1);
+        if (!m->d_rhs && (!check_cuda(cudaMalloc(&m->d_rhs, cells * sizeof(double)), "cudaMalloc") ||
+                          !check_cuda(cudaMalloc(&m->d_p, cells * sizeof(double)), "cudaMalloc")))
+            return false;
+    }
+    std::vector<double> h;
+    to_ghosted(f, f->rhs, h);
+    if (!check_cuda(cudaMemcpy(m->d_rhs, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice), "upload"))
+        return false;
+    to_ghosted(f, f->sol, h);
+    return check_cuda(cudaMemcpy(m->d_p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice), "upload");
+}
+}  // namespace
+
+bool multigrid::iterate(int iters) {
+    if (iters <= 0) return true;
+    if (!mg_upload(this)) return false;
+    int it = 0;
+    double rr = 0.0;
+    // a relative tolerance no residual reaches: exactly `iters` iterations (fewer if the
+    // residual stops improving)
+    const int rc = scihpc_poisson_solve(gpu, d_rhs, d_p, 1, 1e-300, iters, &it, &rr, nullptr);
+    if (rc != SCIHPC_OK && rc != SCIHPC_ERR_MAXITER && !check(rc, "poisson_solve")) return false;
+    multigrid_base *f = at[0];
+    std::vector<double> h(size_t(f->nx + 6) * (f->ny + 6) * (f->ndim == 3 ? f->nz + 6 : 1));
+    if (!check_cuda(cudaMemcpy(h.data(), d_p, h.size() * sizeof(double), cudaMemcpyDeviceToHost), "download"))
+        return false;
+    from_ghosted(f, h, f->sol);
+    return true;
+}
+
+bool multigrid::residual(double &norm) {
+    return mg_upload(this) && check(scihpc_poisson_residual(gpu, d_rhs, d_p, &norm, nullptr), "poisson_residual");
+}
+
+void multigrid::v_cycle() { iterate(1); }
+void multigrid::full_cycle() { iterate(1); }
+
 // ---------------------------------------------------------------- shared solvers, scratch
-shared_solvers *SharedSolvers_alloc(scalar_data *, structured_grid *geo) {
+shared_solvers *SharedSolvers_alloc(scalar_data *f, structured_grid *geo) {
     auto *s = new shared_solvers();
     s->geo = geo;
+    s->mg = new multigrid(f, geo);
     return s;
 }
-void shared_solvers_mg_init_Neumann(shared_solvers *s) { s->mg_bc = 0; }
-void shared_solvers_mg_init_Dirichlet(shared_solvers *s) { s->mg_bc = 1; }
+void shared_solvers_mg_init_Neumann(shared_solvers *s) {
+    s->mg_bc = 0;
+    for (unsigned l = 0; l < s->mg->level_num; ++l) s->mg->at[l]->init_NeumannBC();
+}
+void shared_solvers_mg_init_Dirichlet(shared_solvers *s) {
+    s->mg_bc = 1;
+    for (unsigned l = 0; l < s->mg->level_num; ++l) s->mg->at[l]->init_DirichletBC();
+}
 
 dummy_data *dummy_data_alloc(scalar_data *f) {
     auto *d = new dummy_data();

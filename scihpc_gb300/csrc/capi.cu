@@ -280,6 +280,11 @@ int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int u
     return ps->ps.solve(rhs, p, use_guess, rel_tol, max_iter, iters, relres, S(stream));
 }
 
+int scihpc_poisson_residual(scihpc_poisson *ps, const double *rhs, const double *p, double *norm, void *stream) {
+    REQUIRE(ps && rhs && p && norm, "poisson_residual: NULL argument");
+    return ps->ps.residual(rhs, p, norm, S(stream));
+}
+
 int scihpc_poisson_time_vcycles(scihpc_poisson *ps, const double *rhs, double *p, int ncycles, float *ms,
                                 void *stream) {
     REQUIRE(ps && rhs && p && ms && ncycles > 0, "poisson_time_vcycles: bad argument");

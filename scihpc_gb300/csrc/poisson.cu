@@ -2324,6 +2324,15 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
     return SCIHPC_OK;
 }
 
+int Poisson::residual(const double *rhs, const double *p, double *norm, cudaStream_t s) {
+    use_conditional = false;
+    begin(rhs, const_cast<double *>(p), 1, s);   // with a guess, begin reads p and writes only scratch
+    SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    SCIHPC_CUDA(cudaStreamSynchronize(s));
+    *norm = std::sqrt(host_state->rr);
+    return SCIHPC_OK;
+}
+
 int Poisson::time_vcycles(const double *rhs, double *p, int n, float *ms, cudaStream_t s) {
     use_conditional = false;
     begin(rhs, p, 0, s);

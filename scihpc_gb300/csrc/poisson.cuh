@@ -64,6 +64,8 @@ public:
     int solve(const double *rhs, double *p, int use_guess, double rel_tol, int max_iter, int *iters, double *relres,
               cudaStream_t s);
     int levels(int *out, int max_levels) const;
+    // ||rhs - A p|| over the interior (rhs minus its mean for Neumann walls), FP64, synchronising.
+    int residual(const double *rhs, const double *p, double *norm, cudaStream_t s);
     // Times n V-cycles (the preconditioner alone) on the residual of p = 0 for rhs.
     int time_vcycles(const double *rhs, double *p, int n, float *ms, cudaStream_t s);
     int fp32() const { return fp32_; }

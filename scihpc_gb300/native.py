@@ -95,6 +95,7 @@ _SIGS = {
     "scihpc_poisson_time_vcycles": ([_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float), _vp],
                                     ctypes.c_int),
     "scihpc_poisson_levels": ([_vp, _ip, ctypes.c_int], ctypes.c_int),
+    "scihpc_poisson_residual": ([_vp, _vp, _vp, _dp, _vp], ctypes.c_int),
     "scihpc_twophase_create": ([ctypes.POINTER(_GridC), _ip, _ip, _dp, _ip, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_destroy": ([_vp], ctypes.c_int),
     "scihpc_twophase_upload": ([_vp, ctypes.c_char_p, _dp], ctypes.c_int),
@@ -277,6 +278,12 @@ class Poisson:
         ms = ctypes.c_float(0.0)
         self.L.check(self.L.scihpc_poisson_time_vcycles(self.h, _ptr(rhs), _ptr(p), ncycles, ctypes.byref(ms), stream))
         return ms.value
+
+    def residual(self, rhs, p, stream=0) -> float:
+        """||rhs - A p|| over the interior cells (FP64, on the GPU)."""
+        out = ctypes.c_double(0.0)
+        self.L.check(self.L.scihpc_poisson_residual(self.h, _ptr(rhs), _ptr(p), ctypes.byref(out), stream))
+        return out.value
 
     def levels(self) -> list:
         buf = (ctypes.c_int * 96)()
