@@ -205,6 +205,16 @@ int scihpc_twophase_mpls(scihpc_twophase *tp, int count);
 int scihpc_twophase_reinit(scihpc_twophase *tp, int *steps);
 int scihpc_twophase_find_source(scihpc_twophase *tp);
 int scihpc_twophase_ab_solve(scihpc_twophase *tp, int *iters, double *relres);
+/* The stages of ab_solve one at a time, for callers that compose them as the reference's
+ * projection_method does: find_intermediate_velocity (AB2 predictor and velocity boundary
+ * fill, projection_method.cpp:384-402); projection (right-hand side div(u*)/dt, the
+ * pressure equation of init_ppe_proj_coefficients solved to ppe_tol, pressure boundary fill,
+ * velocity correction, projection_method.cpp:404-465,544-657); node_from_face (node
+ * velocity from the faces and its boundary fill, wrapper_func.cpp:177-293).  Each
+ * synchronises the session's stream. */
+int scihpc_twophase_intermediate_velocity(scihpc_twophase *tp);
+int scihpc_twophase_projection(scihpc_twophase *tp, int *iters, double *relres);
+int scihpc_twophase_node_from_face(scihpc_twophase *tp);
 /* Finer-grained stages for callers that drive the reinitialisation loop themselves, as the
  * reference drivers do (benchmarks_2d_bubble_rising.cpp:122-129): find_sign
  * (wrapper_func.cpp:387-402); one runge_kutta::tvd_rk3 step (runge_kutta.cpp:13-49) with

@@ -5,14 +5,20 @@
 #ifndef SCIHPC_GB300_SHARED_SOLVERS_H
 #define SCIHPC_GB300_SHARED_SOLVERS_H
 
+#include "ccd_solver.h"
 #include "multigrid.h"
 #include "scalar_data.h"
 #include "structured_grid.h"
+#include "uccd_solver.h"
+#include "weno_solver.h"
 
 struct shared_solvers {
+    ccd_solver *ccd = nullptr;     // GPU line solves on host arrays (ccd_solver.h)
+    uccd_solver *uccd = nullptr;
+    weno_solver *weno = nullptr;
+    multigrid *mg = nullptr;       // GPU-backed (multigrid.h)
     structured_grid *geo = nullptr;
-    int mg_bc = -1;            // -1 none, 0 Neumann, 1 Dirichlet
-    multigrid *mg = nullptr;   // GPU-backed (multigrid.h)
+    int mg_bc = -1;                // -1 none, 0 Neumann, 1 Dirichlet
 };
 
 shared_solvers *SharedSolvers_alloc(scalar_data *f, structured_grid *geo);

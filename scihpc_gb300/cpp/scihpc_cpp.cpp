@@ -25,9 +25,11 @@
 #include <vector>
 
 #include "scihpc/bc_factory.h"
+#include "scihpc/ccd_solver.h"
 #include "scihpc/dummy_data.h"
 #include "scihpc/flux.h"
 #include "scihpc/global.h"
+#include "scihpc/godunov_gradient.h"
 #include "scihpc/gpu_session.h"
 #include "scihpc/lsm.h"
 #include "scihpc/multigrid.h"
@@ -37,8 +39,10 @@
 #include "scihpc/shared_solvers.h"
 #include "scihpc/source.h"
 #include "scihpc/structured_grid.h"
+#include "scihpc/uccd_solver.h"
 #include "scihpc/vector_data.h"
 #include "scihpc/vtkWriter.h"
+#include "scihpc/weno_solver.h"
 #include "scihpc/wrapper.h"
 #include "scihpc/wrapper_func.h"
 #include "scihpc_gpu.h"
@@ -740,6 +744,9 @@ void multigrid::full_cycle() { iterate(1); }
 shared_solvers *SharedSolvers_alloc(scalar_data *f, structured_grid *geo) {
     auto *s = new shared_solvers();
     s->geo = geo;
+    s->ccd = new ccd_solver(f, geo);
+    s->uccd = new uccd_solver(f, geo);
+    s->weno = new weno_solver(f, geo);
     s->mg = new multigrid(f, geo);
     return s;
 }
@@ -761,10 +768,226 @@ dummy_data *dummy_data_alloc(scalar_data *f) {
     return d;
 }
 
-// ---------------------------------------------------------------- flux / source markers
-void identity_flux(scalar_data *, vector_data *) {}
-void identity_flux(scalar_data *) {}
-void identity_flux(vector_data *) {}
+// ---------------------------------------------------------------- host-array GPU calls
+namespace {
+scihpc_ctx *ctx_for(const scihpc_grid &g) {
+    std::vector<double> key = {double(g.ndim)};
+    for (int a = 0; a < 3; ++a) key.insert(key.end(), {double(g.n[a]), g.lo[a], g.hi[a]});
+    Scratch &sc = g_scratch[key];
+    if (!sc.ctx && !check(scihpc_ctx_create(&g, &sc.ctx), "ctx_create")) return nullptr;
+    return sc.ctx;
+}
+
+// a grid with the scalar's sizes (unit spacing) for calls that need no geometry
+scihpc_grid grid_of_sizes(const scalar_data *f) {
+    scihpc_grid c{};
+    c.ndim = f->ndim;
+    const int n[3] = {f->nx, f->ny, f->nz};
+    for (int a = 0; a < 3; ++a) {
+        c.n[a] = a < f->ndim ? n[a] : 1;
+        c.lo[a] = 0.0;
+        c.hi[a] = a < f->ndim ? double(n[a]) : 1.0;
+    }
+    return c;
+}
+
+// One GPU call on host arrays: inputs are brought up to date from a GPU session that owns
+// them and uploaded; outputs are uploaded too (so that cells the call does not write keep
+// their values), downloaded at finish() and pushed to the owning session, if any.
+struct HostCall {
+    scihpc_ctx *ctx = nullptr;
+    size_t n = 0;
+    bool ok = true;
+    std::vector<std::pair<DataType ***, double *>> outs;
+    std::vector<double *> bufs;
+
+    HostCall(const scihpc_grid &g, const scalar_data *f) : ctx(ctx_for(g)), n(cells_of(f)) { ok = ctx != nullptr; }
+    ~HostCall() {
+        for (double *p : bufs) cudaFree(p);
+    }
+    double *in(DataType ***a) {
+        if (!ok) return nullptr;
+        sync_array(a);
+        double *p = nullptr;
+        if (!check_cuda(cudaMalloc(&p, n * sizeof(double)), "cudaMalloc")) return ok = false, nullptr;
+        bufs.push_back(p);
+        if (!check_cuda(cudaMemcpy(p, base_of(a), n * sizeof(double), cudaMemcpyHostToDevice), "upload")) ok = false;
+        return p;
+    }
+    double *out(DataType ***a) {
+        double *p = in(a);
+        if (p) outs.emplace_back(a, p);
+        return p;
+    }
+    bool run(int rc, const char *what) { return ok = ok && check(rc, what); }
+    bool finish() {
+        for (auto &o : outs) {
+            if (!ok) break;
+            ok = check_cuda(cudaMemcpy(base_of(o.first), o.second, n * sizeof(double), cudaMemcpyDeviceToHost),
+                            "download");
+            auto it = g_mirrors.find(o.first);
+            if (ok && it != g_mirrors.end()) ok = upload(it->second.s, it->second.name.c_str(), o.first);
+        }
+        return ok;
+    }
+};
+
+void host_copy(DataType ***dst, DataType ***src, const scalar_data *f) {
+    sync_array(src);
+    std::memcpy(base_of(dst), base_of(src), cells_of(f) * sizeof(DataType));
+}
+
+void extrapolate(scalar_data *f, DataType ***src, int location) {
+    HostCall c(grid_of_sizes(f), f);
+    double *s = c.in(src), *d = c.out(f->flux);
+    if (c.ok) c.run(scihpc_flux_extrapolate(c.ctx, location, s, d, nullptr), "flux_extrapolate");
+    c.finish();
+}
+void unsupported(const char *what, const char *why) { fail(SCIHPC_ERR_UNSUPPORTED, std::string(what) + ": " + why); }
+}  // namespace
+
+// ---------------------------------------------------------------- flux
+void identity_flux(scalar_data *f, vector_data *) { host_copy(f->flux, f->data, f); }
+void identity_flux(scalar_data *f) { host_copy(f->flux, f->data, f); }
+void identity_flux(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) host_copy(c->flux, c->data, c);
+}
+void identity_old_flux(scalar_data *f, vector_data *) { host_copy(f->flux, f->old, f); }
+void identity_old_flux(scalar_data *f) { host_copy(f->flux, f->old, f); }
+void identity_old_flux(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) host_copy(c->flux, c->old, c);
+}
+void guess_from_history(scalar_data *) { unsupported("guess_from_history", "no GPU stage (2 old - old2)"); }
+
+void identity_with_extrapolation(scalar_data *f, vector_data *) { extrapolate(f, f->data, 0); }
+void identity_with_extrapolation(scalar_data *f) { extrapolate(f, f->data, 0); }
+void identity_with_extrapolation(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->data, 0);
+}
+void identity_with_extrapolation_face_x(scalar_data *f) { extrapolate(f, f->data, 1); }
+void identity_with_extrapolation_face_y(scalar_data *f) { extrapolate(f, f->data, 2); }
+void identity_with_extrapolation_face_z(scalar_data *f) { extrapolate(f, f->data, 3); }
+void identity_with_extrapolation_face_x(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->data, 1);
+}
+void identity_with_extrapolation_face_y(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->data, 2);
+}
+void identity_with_extrapolation_face_z(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->data, 3);
+}
+void identity_with_extrapolation_face_x(scalar_data *f, vector_data *) { extrapolate(f, f->data, 1); }
+void identity_with_extrapolation_face_y(scalar_data *f, vector_data *) { extrapolate(f, f->data, 2); }
+void identity_with_extrapolation_face_z(scalar_data *f, vector_data *) { extrapolate(f, f->data, 3); }
+
+void identity_old_with_extrapolation(scalar_data *f, vector_data *) { extrapolate(f, f->old, 0); }
+void identity_old_with_extrapolation(scalar_data *f) { extrapolate(f, f->old, 0); }
+void identity_old_with_extrapolation(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->old, 0);
+}
+void identity_old_with_extrapolation_face_x(scalar_data *f) { extrapolate(f, f->old, 1); }
+void identity_old_with_extrapolation_face_y(scalar_data *f) { extrapolate(f, f->old, 2); }
+void identity_old_with_extrapolation_face_z(scalar_data *f) { extrapolate(f, f->old, 3); }
+void identity_old_with_extrapolation_face_x(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->old, 1);
+}
+void identity_old_with_extrapolation_face_y(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->old, 2);
+}
+void identity_old_with_extrapolation_face_z(vector_data *v) {
+    for (scalar_data *c : {&v->x, &v->y, &v->z}) extrapolate(c, c->old, 3);
+}
+void identity_old_with_extrapolation_face_x(scalar_data *f, vector_data *) { extrapolate(f, f->old, 1); }
+void identity_old_with_extrapolation_face_y(scalar_data *f, vector_data *) { extrapolate(f, f->old, 2); }
+void identity_old_with_extrapolation_face_z(scalar_data *f, vector_data *) { extrapolate(f, f->old, 3); }
+
+// ---------------------------------------------------------------- compact / WENO solvers
+namespace {
+scalar_data *component(vector_data *v, int a) { return a == 0 ? &v->x : (a == 1 ? &v->y : &v->z); }
+DataType ***first_of(scalar_data *f, int a) { return a == 0 ? f->fx : (a == 1 ? f->fy : f->fz); }
+DataType ***second_of(scalar_data *f, int a) { return a == 0 ? f->fxx : (a == 1 ? f->fyy : f->fzz); }
+
+void ccd_axis(const structured_grid *geo, scalar_data *f, int a) {
+    HostCall c(grid_of(geo), f);
+    double *fl = c.in(f->flux), *d1 = c.out(first_of(f, a)), *d2 = c.out(second_of(f, a));
+    if (c.ok) c.run(scihpc_ccd(c.ctx, a, fl, d1, d2, nullptr), "ccd");
+    c.finish();
+}
+// mixed derivative: src extrapolated in place along `a`, out = its CCD derivative along `a`
+void ccd_mixed(const structured_grid *geo, scalar_data *f, DataType ***src, DataType ***out, int a) {
+    HostCall c(grid_of(geo), f);
+    double *sv = c.out(src), *ov = c.out(out);
+    if (c.ok) c.run(scihpc_ccd_mixed(c.ctx, a, sv, ov, nullptr), "ccd_mixed");
+    c.finish();
+}
+void uccd_axis(const structured_grid *geo, scalar_data *f, vector_data *vel, int a) {
+    HostCall c(grid_of(geo), f);
+    double *fl = c.in(f->flux), *u = c.in(component(vel, a)->data);
+    double *d1 = c.out(first_of(f, a)), *d2 = c.out(second_of(f, a));
+    if (c.ok) c.run(scihpc_uccd(c.ctx, a, fl, u, d1, d2, nullptr), "uccd");
+    c.finish();
+}
+void weno_axis(const structured_grid *geo, scalar_data *f, vector_data *vel, int a) {
+    HostCall c(grid_of(geo), f);
+    double *fl = c.in(f->flux), *u = c.in(component(vel, a)->data), *d1 = c.out(first_of(f, a));
+    if (c.ok) c.run(scihpc_weno5(c.ctx, a, fl, u, d1, nullptr), "weno5");
+    c.finish();
+}
+}  // namespace
+
+ccd_solver::ccd_solver(scalar_data *, structured_grid *g) : geo(g) {}
+void ccd_solver::find_fx(scalar_data *f) const { ccd_axis(geo, f, 0); }
+void ccd_solver::find_fy(scalar_data *f) const { ccd_axis(geo, f, 1); }
+void ccd_solver::find_fz(scalar_data *f) const { ccd_axis(geo, f, 2); }
+void ccd_solver::mixed_xy(scalar_data *f) const { ccd_mixed(geo, f, f->fx, f->fxy, 1); }
+void ccd_solver::mixed_yz(scalar_data *f) const { ccd_mixed(geo, f, f->fy, f->fyz, 2); }
+void ccd_solver::mixed_zx(scalar_data *f) const { ccd_mixed(geo, f, f->fz, f->fzx, 0); }
+void ccd_solver::find_derivatives(scalar_data *f) const {
+    find_fx(f);
+    if (f->ndim > 1) find_fy(f);
+    if (f->ndim > 2) find_fz(f);
+}
+void ccd_solver::find_derivatives(vector_data *f) const {
+    find_derivatives(&f->x);
+    find_derivatives(&f->y);
+    find_derivatives(&f->z);
+}
+void ccd_solver::find_derivatives_all(scalar_data *f) const {
+    find_derivatives(f);
+    if (f->ndim > 1) mixed_xy(f);
+    if (f->ndim > 2) {
+        mixed_yz(f);
+        mixed_zx(f);
+    }
+}
+void ccd_solver::find_derivatives_all(vector_data *f) const {
+    find_derivatives_all(&f->x);
+    find_derivatives_all(&f->y);
+    find_derivatives_all(&f->z);
+}
+
+uccd_solver::uccd_solver(scalar_data *, structured_grid *g) : geo(g) {}
+void uccd_solver::find_fx(scalar_data *f, vector_data *vel) const { uccd_axis(geo, f, vel, 0); }
+void uccd_solver::find_fy(scalar_data *f, vector_data *vel) const { uccd_axis(geo, f, vel, 1); }
+void uccd_solver::find_fz(scalar_data *f, vector_data *vel) const { uccd_axis(geo, f, vel, 2); }
+void uccd_solver::find_derivatives(scalar_data *f, vector_data *vel) const {
+    find_fx(f, vel);
+    if (f->ndim > 1) find_fy(f, vel);
+    if (f->ndim > 2) find_fz(f, vel);
+}
+
+weno_solver::weno_solver(scalar_data *, structured_grid *g) : dx(g->dx), dy(g->dy), dz(g->dz), geo(g) {}
+void weno_solver::weno5_flux_x(scalar_data *) { unsupported("weno5_flux_x", "face values are internal to the GPU kernel"); }
+void weno_solver::weno5_flux_y(scalar_data *) { unsupported("weno5_flux_y", "face values are internal to the GPU kernel"); }
+void weno_solver::weno5_flux_z(scalar_data *) { unsupported("weno5_flux_z", "face values are internal to the GPU kernel"); }
+void weno_solver::weno5_find_fx(scalar_data *f, vector_data *vel) { weno_axis(geo, f, vel, 0); }
+void weno_solver::weno5_find_fy(scalar_data *f, vector_data *vel) { weno_axis(geo, f, vel, 1); }
+void weno_solver::weno5_find_fz(scalar_data *f, vector_data *vel) { weno_axis(geo, f, vel, 2); }
+void weno_solver::weno5_find_derivatives(scalar_data *f, vector_data *vel) {
+    weno5_find_fx(f, vel);
+    if (f->ndim > 1) weno5_find_fy(f, vel);
+    if (f->ndim > 2) weno5_find_fz(f, vel);
+}
 
 namespace {
 void direct_call(const char *fn) {
@@ -851,7 +1074,147 @@ void projection_method::ab_solve(wrapper *vel, wrapper *nvel, wrapper *pressure,
     pull_scalars(s);
 }
 
+namespace {
+Session *stage_session(wrapper *any, const char *what) {
+    Session *s = session_of(any);
+    if (!s) fail(SCIHPC_ERR_ARG, std::string(what) + ": call find_source first (it starts the GPU session)");
+    return s && push_scalars(s) ? s : nullptr;
+}
+}  // namespace
+
+// the stages of ab_solve one at a time (projection_method.cpp:384-402, 544-657)
+void projection_method::find_intermediate_velocity(wrapper *vel) const {
+    Session *s = stage_session(vel, "find_intermediate_velocity");
+    if (s && check(scihpc_twophase_intermediate_velocity(s->tp), "intermediate_velocity")) pull_scalars(s);
+}
+
+void projection_method::projection(wrapper *pressure, wrapper *lsf, wrapper *) const {
+    Session *s = stage_session(lsf, "projection");
+    if (!s || !attach_pressure(s, pressure)) return;
+    int it = 0;
+    double rr = 0.0;
+    const int rc = scihpc_twophase_projection(s->tp, &it, &rr);
+    if (rc == SCIHPC_ERR_MAXITER) fail(rc, "projection: pressure solve stopped at ppe_max_iter above ppe_tol");
+    else if (!check(rc, "projection")) return;
+    pull_scalars(s);
+}
+
+// The reference's fast pressure correction iterates a constant-coefficient equation; the GPU
+// solves the variable-coefficient equation of projection() to ppe_tol instead.
+void projection_method::fast_pressure_correction(wrapper *pressure, wrapper *lsf, wrapper *vel) {
+    projection(pressure, lsf, vel);
+}
+
+// the GPU builds the coefficients from the density inside projection()
+void projection_method::init_ppe_proj_coefficients(wrapper *) {}
+void projection_method::init_ppe_fpc_coefficients(wrapper *) {}
+
+void projection_method::pressure_guess_solution(wrapper *) {
+    unsupported("pressure_guess_solution", "the GPU pressure solve starts from the previous pressure");
+}
+void projection_method::add_stress_x(wrapper *, wrapper *, wrapper *) const {
+    unsupported("add_stress_x", "a stage inside the GPU find_source");
+}
+void projection_method::add_stress_y(wrapper *, wrapper *, wrapper *) const {
+    unsupported("add_stress_y", "a stage inside the GPU find_source");
+}
+void projection_method::add_stress_z(wrapper *, wrapper *, wrapper *) const {
+    unsupported("add_stress_z", "a stage inside the GPU find_source");
+}
+void projection_method::add_body_force(wrapper *) const {
+    unsupported("add_body_force", "a stage inside the GPU find_source");
+}
+void projection_method::add_surface_force(wrapper *) const {
+    unsupported("add_surface_force", "a stage inside the GPU find_source");
+}
+void projection_method::find_source_sec(wrapper *, wrapper *, wrapper *) const {
+    unsupported("find_source_sec", "the second-order discretisation is not on the GPU path");
+}
+void projection_method::ab_solve_sec(wrapper *, wrapper *, wrapper *, wrapper *) {
+    unsupported("ab_solve_sec", "the second-order discretisation is not on the GPU path");
+}
+
 // ---------------------------------------------------------------- wrapper_func
+void node_from_face(wrapper *ref, wrapper *) {
+    Session *s = stage_session(ref, "node_from_face");
+    if (s && check(scihpc_twophase_node_from_face(s->tp), "node_from_face")) pull_scalars(s);
+}
+void all_to_face_x(wrapper *, wrapper *) { unsupported("all_to_face_x", "a stage inside the GPU find_source"); }
+void all_to_face_y(wrapper *, wrapper *) { unsupported("all_to_face_y", "a stage inside the GPU find_source"); }
+void all_to_face_z(wrapper *, wrapper *) { unsupported("all_to_face_z", "a stage inside the GPU find_source"); }
+void find_gradient(wrapper *) { unsupported("find_gradient", "a stage inside the GPU find_source"); }
+
+namespace {
+// heaviside, delta, density or viscosity of the host level set, on the GPU
+void lsf_field(wrapper *lsf, int which) {
+    const problem_parameters *p = lsf->params;
+    if (!p || !lsf->dummy) {
+        fail(SCIHPC_ERR_ARG, "level-set fields: wrapper not linked to problem_parameters and dummy_data");
+        return;
+    }
+    const double prm[4] = {p->ls_width, p->density_ratio, p->viscosity_ratio, double(p->positive_ref)};
+    DataType ***dst[4] = {lsf->dummy->heaviside, lsf->dummy->delta, lsf->dummy->density, lsf->dummy->viscosity};
+    HostCall c(grid_of(lsf->geo), lsf->scalar);
+    double *phi = c.in(lsf->scalar->data), *out = c.out(dst[which]);
+    if (c.ok)
+        c.run(scihpc_lsf_fields(c.ctx, prm, phi, which == 0 ? out : nullptr, which == 1 ? out : nullptr, nullptr,
+                                which == 2 ? out : nullptr, which == 3 ? out : nullptr, nullptr),
+              "lsf_fields");
+    c.finish();
+}
+}  // namespace
+
+void find_heavyside(wrapper *lsf) { lsf_field(lsf, 0); }
+void find_delta(wrapper *lsf) { lsf_field(lsf, 1); }
+void find_density(wrapper *lsf) { lsf_field(lsf, 2); }
+void find_viscosity(wrapper *lsf) { lsf_field(lsf, 3); }
+
+// curvature from the level set and its CCD derivative arrays (wrapper_func.cpp:115-174)
+void find_curvature(wrapper *lsf) {
+    if (!lsf->dummy) {
+        fail(SCIHPC_ERR_ARG, "find_curvature: wrapper not linked to dummy_data");
+        return;
+    }
+    scalar_data *f = lsf->scalar;
+    HostCall c(grid_of(lsf->geo), f);
+    DataType ***src[9] = {f->fx, f->fy, f->fz, f->fxx, f->fyy, f->fzz, f->fxy, f->fyz, f->fzx};
+    const double *d[9];
+    for (int q = 0; q < 9; ++q) d[q] = c.in(src[q]);
+    double *phi = c.in(f->data), *curv = c.out(lsf->dummy->curvature);
+    if (c.ok) c.run(scihpc_curvature(c.ctx, phi, d, curv, nullptr), "curvature");
+    c.finish();
+}
+
+// ---------------------------------------------------------------- godunov_gradient
+// the scalar WENO-JS correction of godunov_gradient.cpp:183-198 (weights d = 1/10, 6/10,
+// 3/10 on (eps + indicator)^-2)
+DataType weno5_for_godunov(DataType a, DataType b, DataType c, DataType d) {
+    const DataType eps = 1e-8;
+    const DataType is0 = 13.0 * (a - b) * (a - b) + 3.0 * (a - 3.0 * b) * (a - 3.0 * b);
+    const DataType is1 = 13.0 * (b - c) * (b - c) + 3.0 * (b + c) * (b + c);
+    const DataType is2 = 13.0 * (c - d) * (c - d) + 3.0 * (3.0 * c - d) * (3.0 * c - d);
+    const DataType a0 = 1.0 / ((eps + is0) * (eps + is0)), a1 = 6.0 / ((eps + is1) * (eps + is1)),
+                   a2 = 3.0 / ((eps + is2) * (eps + is2));
+    const DataType w0 = a0 / (a0 + a1 + a2), w2 = a2 / (a0 + a1 + a2);
+    return w0 / 3.0 * (a - 2.0 * b + c) + (w2 - 0.5) / 6.0 * (b - 2.0 * c + d);
+}
+
+void godunov_gradient(wrapper *f) {
+    if (!f->dummy) {
+        fail(SCIHPC_ERR_ARG, "godunov_gradient: wrapper not linked to dummy_data");
+        return;
+    }
+    HostCall c(grid_of(f->geo), f->scalar);
+    double *phi = c.in(f->scalar->data), *sg = c.in(f->dummy->sign), *g = c.out(f->dummy->grad);
+    if (c.ok) c.run(scihpc_godunov_gradient(c.ctx, phi, sg, g, nullptr), "godunov_gradient");
+    c.finish();
+}
+
+void stabilized_upon_gradient(wrapper *f) {
+    godunov_gradient(f);
+    unsupported("stabilized_upon_gradient", "the rescale by max |grad phi| has no GPU stage");
+}
+
 void find_sign(wrapper *lsf) {
     Session *s = session_of(lsf);
     if (!s) {

@@ -438,6 +438,21 @@ int scihpc_twophase_ab_solve(scihpc_twophase *tp, int *iters, double *relres) {
     return tp->tp.ab_solve(iters, relres);
 }
 
+int scihpc_twophase_intermediate_velocity(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_intermediate_velocity: NULL argument");
+    return tp->tp.intermediate_velocity();
+}
+
+int scihpc_twophase_projection(scihpc_twophase *tp, int *iters, double *relres) {
+    REQUIRE(tp, "twophase_projection: NULL argument");
+    return tp->tp.projection(iters, relres);
+}
+
+int scihpc_twophase_node_from_face(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_node_from_face: NULL argument");
+    return tp->tp.node_from_face();
+}
+
 int scihpc_twophase_step(scihpc_twophase *tp, int nsteps, int use_graph, int sync) {
     REQUIRE(tp && nsteps >= 0, "twophase_step: bad argument");
     int rc = tp->tp.step(nsteps, use_graph != 0);

@@ -1013,16 +1013,15 @@ void TwoPhaseGpu::find_source() {
                                       P.Fr, P.We);
 }
 
-void TwoPhaseGpu::ab_solve_pre() {
-    const long long N = D.size();
-    const unsigned nbf = blocks_for(N, TPB), nbi = blocks_for(D.interior(), TPB);
-    // scalar_data::store (scalar_data.cpp:125-135)
-    k_copy<<<nbf, TPB, 0, stream>>>(pres.old2, pres.old, N);
-    k_copy<<<nbf, TPB, 0, stream>>>(pres.old, pres.data, N);
-    find_source();
+void TwoPhaseGpu::ab2_part() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
     k_ab2<<<nbi, TPB, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, src[0], src[1], src[2], src_old[0],
                                    src_old[1], src_old[2], D, sc);
     vel_bc(vel, -1);
+}
+
+void TwoPhaseGpu::projection_begin() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
     k_div_rhs<<<nbi, TPB, 0, stream>>>(RHS, vel[0].data, vel[1].data, vel[2].data, D, sc);
     ppe.set_density(rho, stream);
     ppe.rel_tol = P.ppe_tol;
@@ -1030,20 +1029,39 @@ void TwoPhaseGpu::ab_solve_pre() {
     ppe.begin(RHS, pres.data, 1, stream);
 }
 
-void TwoPhaseGpu::ab_solve_post() {
+void TwoPhaseGpu::projection_end() {
     const unsigned nbi = blocks_for(D.interior(), TPB);
     ppe.finish(pres.data, stream);
     scalar_bc(pres.data);
     k_correct<<<nbi, TPB, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, pres.data, rho, D, sc);
     vel_bc(vel, -1);
+}
+
+void TwoPhaseGpu::node_part() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
     k_node_from_face<<<nbi, TPB, 0, stream>>>(nvel[0].data, nvel[1].data, nvel[2].data, vel[0].data, vel[1].data,
                                               vel[2].data, D);
     vel_bc(nvel, 0);
 }
 
-int TwoPhaseGpu::ab_solve(int *iters, double *relres) {
-    ppe.use_conditional = false;
-    ab_solve_pre();
+void TwoPhaseGpu::ab_solve_pre() {
+    const long long N = D.size();
+    const unsigned nbf = blocks_for(N, TPB);
+    // scalar_data::store (scalar_data.cpp:125-135)
+    k_copy<<<nbf, TPB, 0, stream>>>(pres.old2, pres.old, N);
+    k_copy<<<nbf, TPB, 0, stream>>>(pres.old, pres.data, N);
+    find_source();
+    ab2_part();
+    projection_begin();
+}
+
+void TwoPhaseGpu::ab_solve_post() {
+    projection_end();
+    node_part();
+}
+
+// the pressure iteration after projection_begin, one host synchronisation per iteration
+int TwoPhaseGpu::run_ppe(int *iters, double *relres) {
     SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
     SCIHPC_CUDA(cudaStreamSynchronize(stream));
     while (!ppe.host_state->done) {
@@ -1051,19 +1069,58 @@ int TwoPhaseGpu::ab_solve(int *iters, double *relres) {
         SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
         SCIHPC_CUDA(cudaStreamSynchronize(stream));
     }
-    const int it = ppe.host_state->it;
+    last_iters = ppe.host_state->it;
+    if (iters) *iters = last_iters;
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::ab_solve(int *iters, double *relres) {
+    ppe.use_conditional = false;
+    ab_solve_pre();
+    int rc = run_ppe(iters, relres);
+    if (rc) return rc;
     ab_solve_post();
     SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
     SCIHPC_CUDA(cudaStreamSynchronize(stream));
     SCIHPC_CUDA(cudaGetLastError());
-    last_iters = it;
     last_relres = ppe.host_state->relres;
-    if (iters) *iters = it;
     if (relres) *relres = ppe.host_state->relres;
     if (ppe.host_state->diverged) {
         set_last_error("pressure solve produced a non-finite residual");
         return SCIHPC_ERR_NONFINITE;
     }
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::intermediate_velocity() {
+    ab2_part();
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::projection(int *iters, double *relres) {
+    ppe.use_conditional = false;
+    projection_begin();
+    int rc = run_ppe(iters, relres);
+    if (rc) return rc;
+    projection_end();
+    SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    last_relres = ppe.host_state->relres;
+    if (relres) *relres = ppe.host_state->relres;
+    if (ppe.host_state->diverged) {
+        set_last_error("pressure solve produced a non-finite residual");
+        return SCIHPC_ERR_NONFINITE;
+    }
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::node_from_face() {
+    node_part();
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
     return SCIHPC_OK;
 }
 

@@ -51,6 +51,16 @@ public:
     void ab_solve_pre();     // store, find_source, AB2, PPE right-hand side, solver begin
     void ab_solve_post();    // solver finish, pressure BC, velocity correction, node velocity
     int ab_solve(int *iters, double *relres);   // host-driven pressure iteration
+    // the stages of ab_solve one at a time (projection_method.cpp:384-402, 544-657; the
+    // node velocity of wrapper_func.cpp:177-293)
+    int intermediate_velocity();
+    int projection(int *iters, double *relres);
+    int node_from_face();
+    void ab2_part();
+    void projection_begin();
+    void projection_end();
+    void node_part();
+    int run_ppe(int *iters, double *relres);
     int init();
     int step(int nsteps, bool graph);
     int diagnostics(double *out);

@@ -127,6 +127,9 @@ _SIGS = {
     "scihpc_unet_train_step": ([_vp, ctypes.POINTER(_GridC), _vp, _vp, _vp, _vp, ctypes.c_float, _dp], ctypes.c_int),
     "scihpc_unet_stream": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_ab_solve": ([_vp, _ip, _dp], ctypes.c_int),
+    "scihpc_twophase_intermediate_velocity": ([_vp], ctypes.c_int),
+    "scihpc_twophase_projection": ([_vp, _ip, _dp], ctypes.c_int),
+    "scihpc_twophase_node_from_face": ([_vp], ctypes.c_int),
     "scihpc_twophase_step": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_diagnostics": ([_vp, _dp], ctypes.c_int),
     "scihpc_twophase_stream": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
