@@ -187,6 +187,12 @@ int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host
 int scihpc_twophase_field(scihpc_twophase *tp, const char *name, double **dev);
 /* Scalars {t, dt, dt_old, dt_old2, iter, stable_CFL, lsf_mass0}. */
 int scihpc_twophase_get_scalars(scihpc_twophase *tp, double out[7]);
+/* Checkpoint / restart: every device field of the session and its step scalars written to
+ * `path`, or read back into a session created with the same grid (anything else is refused
+ * with SCIHPC_ERR_ARG).  A restored session continues bit for bit.  Synchronise the
+ * session's stream.  New: the reference writes only VTK output. */
+int scihpc_twophase_checkpoint(scihpc_twophase *tp, const char *path);
+int scihpc_twophase_restore(scihpc_twophase *tp, const char *path);
 int scihpc_twophase_set_scalars(scihpc_twophase *tp, const double in[7]);
 /* Start-up of the drivers: scalar BC, find_source, lsf_mass0
  * (benchmarks_2d_bubble_rising.cpp:51,88-89). */

@@ -356,6 +356,16 @@ int scihpc_twophase_field(scihpc_twophase *tp, const char *name, double **dev) {
     return SCIHPC_OK;
 }
 
+int scihpc_twophase_checkpoint(scihpc_twophase *tp, const char *path) {
+    REQUIRE(tp && path, "twophase_checkpoint: NULL argument");
+    return tp->tp.checkpoint(path);
+}
+
+int scihpc_twophase_restore(scihpc_twophase *tp, const char *path) {
+    REQUIRE(tp && path, "twophase_restore: NULL argument");
+    return tp->tp.restore(path);
+}
+
 int scihpc_twophase_get_scalars(scihpc_twophase *tp, double out[7]) {
     REQUIRE(tp && out, "twophase_get_scalars: NULL argument");
     return tp->tp.get_scalars(out);

@@ -13,6 +13,7 @@
 // computed: stage updates, sources and corrections run on interior cells, followed by the
 // boundary fill, which reproduces every value that later work reads.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -729,6 +730,7 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
             for (int c = 0; c < D.ndim; ++c) ALLOC(fv[a][c]);
     }
 #undef ALLOC
+    nfield_allocs = allocs.size();
     for (int k = 0; k < 3; ++k) {
         SCIHPC_CUDA(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
         SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
@@ -813,6 +815,91 @@ double *TwoPhaseGpu::field(const std::string &s) {
     if (s == "w_src_old") return src_old[2];
     if (s == "rhs") return RHS;
     return nullptr;
+}
+
+// Checkpoint file: an 8-byte tag, the grid extents and the field count (so that a restore
+// into a different session is refused), then every ghosted field of the session in
+// allocation order and the step scalars.  Everything the next step reads is in it (the
+// scratch fields too), so a restored session continues bit for bit.
+namespace {
+constexpr char CKPT_TAG[8] = {'S', 'C', 'I', 'H', 'P', 'C', 'K', '1'};
+struct CkptHeader {
+    char tag[8];
+    int32_t ndim, n[3];
+    int64_t nfields, cells, scalar_bytes;
+};
+}  // namespace
+
+int TwoPhaseGpu::checkpoint(const char *path) {
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    std::FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        set_last_error((std::string("checkpoint: cannot open ") + path).c_str());
+        return SCIHPC_ERR_ARG;
+    }
+    CkptHeader h{};
+    std::memcpy(h.tag, CKPT_TAG, 8);
+    h.ndim = D.ndim;
+    for (int a = 0; a < 3; ++a) h.n[a] = D.n[a];
+    h.nfields = int64_t(nfield_allocs);
+    h.cells = D.size();
+    h.scalar_bytes = sizeof(StepScalars);
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+    std::vector<double> buf(size_t(D.size()));
+    for (size_t k = 0; ok && k < nfield_allocs; ++k) {
+        const cudaError_t e = cudaMemcpy(buf.data(), allocs[k], buf.size() * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            std::fclose(f);
+            set_last_error((std::string("checkpoint: ") + cudaGetErrorString(e)).c_str());
+            return SCIHPC_ERR_CUDA;
+        }
+        ok = std::fwrite(buf.data(), sizeof(double), buf.size(), f) == buf.size();
+    }
+    SCIHPC_CUDA(cudaMemcpy(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost));
+    ok = ok && std::fwrite(sc_host, sizeof(StepScalars), 1, f) == 1;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) {
+        set_last_error((std::string("checkpoint: write failed for ") + path).c_str());
+        return SCIHPC_ERR_ARG;
+    }
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::restore(const char *path) {
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    std::FILE *f = std::fopen(path, "rb");
+    if (!f) {
+        set_last_error((std::string("restore: cannot open ") + path).c_str());
+        return SCIHPC_ERR_ARG;
+    }
+    CkptHeader h{};
+    bool ok = std::fread(&h, sizeof h, 1, f) == 1 && std::memcmp(h.tag, CKPT_TAG, 8) == 0 && h.ndim == D.ndim &&
+              h.n[0] == D.n[0] && h.n[1] == D.n[1] && h.n[2] == D.n[2] && h.nfields == int64_t(nfield_allocs) &&
+              h.cells == D.size() && h.scalar_bytes == int64_t(sizeof(StepScalars));
+    if (!ok) {
+        std::fclose(f);
+        set_last_error((std::string("restore: ") + path + " is not a checkpoint of a session of this grid").c_str());
+        return SCIHPC_ERR_ARG;
+    }
+    std::vector<double> buf(size_t(D.size()));
+    for (size_t k = 0; ok && k < nfield_allocs; ++k) {
+        ok = std::fread(buf.data(), sizeof(double), buf.size(), f) == buf.size();
+        const cudaError_t e =
+            ok ? cudaMemcpy(allocs[k], buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice) : cudaSuccess;
+        if (e != cudaSuccess) {
+            std::fclose(f);
+            set_last_error((std::string("restore: ") + cudaGetErrorString(e)).c_str());
+            return SCIHPC_ERR_CUDA;
+        }
+    }
+    ok = ok && std::fread(sc_host, sizeof(StepScalars), 1, f) == 1;
+    std::fclose(f);
+    if (!ok) {
+        set_last_error((std::string("restore: ") + path + " is truncated").c_str());
+        return SCIHPC_ERR_ARG;
+    }
+    SCIHPC_CUDA(cudaMemcpy(sc, sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice));
+    return SCIHPC_OK;
 }
 
 int TwoPhaseGpu::get_scalars(double *out) {

@@ -37,6 +37,9 @@ public:
     void destroy();
     double *field(const std::string &name);
     int get_scalars(double *out);
+    // every field of the session and the step scalars to / from a file (restart)
+    int checkpoint(const char *path);
+    int restore(const char *path);
     int set_scalars(const double *in);
 
     // stages (asynchronous on `stream`)
@@ -104,6 +107,7 @@ private:
     StepScalars *sc = nullptr;        // device
     StepScalars *sc_host = nullptr;   // pinned
     std::vector<void *> allocs;
+    size_t nfield_allocs = 0;   // allocs[0 .. nfield_allocs) are whole ghosted fields
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;
     int reinit_steps = 0;

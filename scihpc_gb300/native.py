@@ -101,6 +101,8 @@ _SIGS = {
     "scihpc_twophase_upload": ([_vp, ctypes.c_char_p, _dp], ctypes.c_int),
     "scihpc_twophase_download": ([_vp, ctypes.c_char_p, _dp], ctypes.c_int),
     "scihpc_twophase_field": ([_vp, ctypes.c_char_p, ctypes.POINTER(_vp)], ctypes.c_int),
+    "scihpc_twophase_checkpoint": ([_vp, ctypes.c_char_p], ctypes.c_int),
+    "scihpc_twophase_restore": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "scihpc_twophase_get_scalars": ([_vp, _dp], ctypes.c_int),
     "scihpc_twophase_set_scalars": ([_vp, _dp], ctypes.c_int),
     "scihpc_twophase_init": ([_vp], ctypes.c_int),
@@ -340,6 +342,12 @@ class TwoPhase:
         p = _vp()
         self.L.check(self.L.scihpc_twophase_field(self.h, name.encode(), ctypes.byref(p)))
         return p.value
+
+    def checkpoint(self, path: str) -> None:
+        self.L.check(self.L.scihpc_twophase_checkpoint(self.h, str(path).encode()))
+
+    def restore(self, path: str) -> None:
+        self.L.check(self.L.scihpc_twophase_restore(self.h, str(path).encode()))
 
     def scalars(self) -> dict:
         out = (ctypes.c_double * 7)()

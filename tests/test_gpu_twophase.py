@@ -149,3 +149,30 @@ def test_full_steps(graph, fp32):
     dp, dg = port.diagnostics(), gpu.diagnostics()
     assert abs(dp["mass"] - dg["mass"]) <= 1e-10 * abs(dp["mass"])
     assert abs(dp["volume"] - dg["volume"]) <= 1e-10 * abs(dp["volume"])
+
+
+def test_checkpoint_restart_continues_bit_for_bit(tmp_path):
+    """A session written to a checkpoint after three steps and restored into a new session
+    continues exactly as the original does; a checkpoint of another grid is refused."""
+    from scihpc_gb300 import ScihpcError, TwoPhase
+    g = O.Grid(2, (16, 32), (0.0, 0.0), (1.0, 2.0))
+    prm = bubble_params(g, ppe_tol=1e-12)
+    mk = lambda gg: TwoPhase(native(gg), ["no_slip"] * 6, ["neumann"] * 6, prm, scheme=1, n_mpls=5, reinit_every=1)
+    a = mk(g)
+    a.set("phi", bubble_phi(g, (0.43, 0.57), 0.23))
+    a.init()
+    a.step(3)
+    ck = tmp_path / "state.ckpt"
+    a.checkpoint(ck)
+    a.step(2)
+    b = mk(g)
+    b.restore(ck)
+    b.step(2)
+    for nm in ("phi", "p", "u", "v", "nu", "nv"):
+        assert np.array_equal(a.get(nm), b.get(nm)), nm
+    assert a.scalars() == b.scalars()
+    other = mk(O.Grid(2, (16, 16), (0.0, 0.0), (1.0, 1.0)))
+    with pytest.raises(ScihpcError):
+        other.restore(ck)
+    for s in (a, b, other):
+        s.close()
