@@ -1019,6 +1019,113 @@ __global__ void __launch_bounds__(V2_THREADS) k_vcycle2(Level<T> F, Level<T> Cl,
     }
 }
 
+// q = L d and <d, q> of the FP32 inner conjugate gradients on the finest level (3D, face
+// coefficients from the density), with the new direction d = z + beta d_old formed on the fly:
+// the planes of z (the V-cycle's output, level-0 x), the old direction and the density are
+// staged by TMA in the boxes of k_sweep3_tma, and every neighbour's d is z + beta d_old read
+// from shared memory.  The new direction itself is stored by k_in_axpy<true>, which reads the
+// same operands cell by cell (a stencil kernel cannot overwrite d in place: neighbouring
+// blocks still read the old values).  The arithmetic is that of k_in_update_d and
+// k_in_apply.  A block owns SW_TJ x SW_TK columns and a chunk of planes; a thread a 2 x 2
+// group of columns.  The grid is one-dimensional (grid_sum indexes blocks by blockIdx.x).
+constexpr int AP_THREADS = (SW_TJ / 2) * (SW_TK / 2);   // 256 == TPB
+
+__global__ void __launch_bounds__(AP_THREADS)
+    k_in_apply3_tma(const __grid_constant__ CUtensorMap map_z, const __grid_constant__ CUtensorMap map_rho,
+                    const __grid_constant__ CUtensorMap map_d, Level<float> L, float *__restrict__ q, Id2<float> id2,
+                    int ci, RedSlot slot, PcgScalars *st, int *err) {
+    static_assert(AP_THREADS == TPB, "grid_sum needs TPB threads");
+    extern __shared__ unsigned char ts_raw[];
+    __shared__ uint64_t bar[TS_STAGES];
+    if (st->done) return;
+    const float beta = (st->in_it == 0 || !(st->rz_prev > 0.0)) ? 0.0f : float(st->rz / st->rz_prev);
+    float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
+    const int tid = threadIdx.x;
+    const int jc = tid / (SW_TK / 2), kc = tid - jc * (SW_TK / 2);   // 2 x 2 group in the tile
+    const int tiles_k = (L.n[2] + SW_TK - 1) / SW_TK, tiles_j = (L.n[1] + SW_TJ - 1) / SW_TJ;
+    const int tile = blockIdx.x % (tiles_k * tiles_j), chunk = blockIdx.x / (tiles_k * tiles_j);
+    const int tk = tile % tiles_k, tj = tile / tiles_k;
+    const int i0 = chunk * ci;
+    const int i1 = min(i0 + ci, L.n[0]);
+    const int nq = i1 - i0 + 2;   // staged planes i0 - 1 .. i1
+    const int j = tj * SW_TJ + 2 * jc, k = tk * SW_TK + 2 * kc;
+    const int sc = (2 * jc + 2) * TS_W + 2 * kc + 5;   // box offset of (j, k)
+    const uint32_t tx_bytes = 3u * uint32_t(TS_PLANE * sizeof(float));
+    auto issue = [&](int qq) {
+        const int st_ = qq % TS_STAGES;
+        float *base = tiles + st_ * 3 * TS_PLANE;
+        const int z = i0 + qq;   // padded i of staged plane qq (interior i0 - 1 + qq)
+        tc::mbar_expect_tx(&bar[st_], tx_bytes);
+        tc::tma_load_3d(base, &map_z, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st_]);
+        tc::tma_load_3d(base + TS_PLANE, &map_rho, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st_]);
+        tc::tma_load_3d(base + 2 * TS_PLANE, &map_d, tk * SW_TK - 4, tj * SW_TJ - 1, z, &bar[st_]);
+    };
+    auto wait_plane = [&](int qq) {
+        return tc::mbar_wait(&bar[qq % TS_STAGES], uint32_t((qq / TS_STAGES) & 1), TS_WAIT_LIMIT);
+    };
+    constexpr int SST = 3 * TS_PLANE;
+    int om1 = 0, oc0 = SST, op1 = 2 * SST;   // stage offsets of planes qq - 1, qq, qq + 1
+    const int issued_pre = min(TS_STAGES, nq) - 1;
+    int issued = issued_pre, waited = -1;
+    bool ok = true;
+    if (tid == 0) {   // thread 0 alone waits (see k_sweep3_tma)
+        for (int s_ = 0; s_ < TS_STAGES; ++s_) tc::mbar_init(&bar[s_], 1);
+        for (int qq = 0; qq <= issued_pre; ++qq) issue(qq);
+        for (int qq = 0; qq <= 2 && ok; ++qq)
+            if ((ok = wait_plane(qq))) waited = qq;
+    }
+    const float w0 = 2.0f * id2.v[0], w1 = 2.0f * id2.v[1], w2 = 2.0f * id2.v[2];
+    const int s0 = int(L.s[0]), s1 = int(L.s[1]);
+    float acc = 0.0f;
+    bool fail = __syncthreads_or(!ok);
+    for (int qq = 1; qq <= nq - 2 && !fail; ++qq) {
+        const float *Zc = tiles + oc0, *Zm = tiles + om1, *Zp = tiles + op1;
+        const float *Rc = Zc + TS_PLANE, *Rm = Zm + TS_PLANE, *Rp = Zp + TS_PLANE;
+        const float *Dc = Zc + 2 * TS_PLANE, *Dm = Zm + 2 * TS_PLANE, *Dp = Zp + 2 * TS_PLANE;
+        const int i = i0 - 1 + qq;
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                const int o = sc + dj * TS_W + dk;
+                const float dc = Zc[o] + beta * Dc[o];
+                const float rc = Rc[o];
+                float sq = w0 * prcp(rc + Rm[o]) * (dc - (Zm[o] + beta * Dm[o])) +
+                           w0 * prcp(rc + Rp[o]) * (dc - (Zp[o] + beta * Dp[o])) +
+                           w1 * prcp(rc + Rc[o - TS_W]) * (dc - (Zc[o - TS_W] + beta * Dc[o - TS_W])) +
+                           w1 * prcp(rc + Rc[o + TS_W]) * (dc - (Zc[o + TS_W] + beta * Dc[o + TS_W]));
+                sq += w2 * prcp(rc + Rc[o - 1]) * (dc - (Zc[o - 1] + beta * Dc[o - 1])) +
+                      w2 * prcp(rc + Rc[o + 1]) * (dc - (Zc[o + 1] + beta * Dc[o + 1]));
+                if (j + dj < L.n[1] && k + dk < L.n[2]) {
+                    q[(i + 1) * s0 + (j + dj + 1) * s1 + k + dk + 1] = sq;
+                    acc += dc * sq;
+                }
+            }
+        om1 = oc0, oc0 = op1;
+        op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
+        if (tid == 0 && qq + 2 <= nq - 1)
+            if ((ok = wait_plane(qq + 2))) waited = qq + 2;
+        if ((fail = __syncthreads_or(!ok))) break;
+        if (qq + TS_STAGES - 1 < nq) {
+            issued = qq + TS_STAGES - 1;
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(qq + TS_STAGES - 1);
+            }
+        }
+    }
+    if (fail) {
+        if (tid == 0) {
+            atomicExch(err, 1);
+            for (int qq = waited + 1; qq <= issued; ++qq) wait_plane(qq);
+        }
+        __syncthreads();
+    }
+    double v[1] = {double(acc)};
+    double *o[1] = {&st->dq};
+    grid_sum<1>(v, slot, o);
+}
+
 // Planes per block for k_sweep3: balances whole waves of blocks against the two planes
 // every chunk recomputes.
 inline int sweep_chunk(const int n[3]) {
@@ -1048,6 +1155,15 @@ inline int restrict_chunk(const int n[3]) {
         if (best < 0 || cost < best) best = cost, best_ci = ci;
     }
     return best_ci;
+}
+
+// Planes per block for k_in_apply3_tma: the fewest planes that keep the one-dimensional grid
+// within RED_MAX_BLOCKS blocks (the partial sums of grid_sum); 0 when no chunking fits.
+inline int apply_chunk(const int n[3]) {
+    const long long tiles = (long long)((n[2] + SW_TK - 1) / SW_TK) * ((n[1] + SW_TJ - 1) / SW_TJ);
+    if (tiles > RED_MAX_BLOCKS) return 0;
+    const long long chunks = RED_MAX_BLOCKS / tiles;
+    return int((n[0] + chunks - 1) / chunks);
 }
 
 // coarse b = mean of the fine residuals of its r^d children; coarse x = 0
@@ -1513,11 +1629,14 @@ __global__ void __launch_bounds__(TPB) k_in_apply(Level<float> L, const float *_
 }
 
 // e += alpha d, r -= alpha q, ||r||^2
-template <int DIM>
-__global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, const float *__restrict__ d,
+template <int DIM, bool UPD>
+__global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, float *__restrict__ d,
                                                  const float *__restrict__ q, float *__restrict__ e, RedSlot slot,
                                                  PcgScalars *st) {
     if (st->done) return;
+    // UPD: the direction of this iteration is d = z + beta d_old (formed, not stored, by the
+    // staged k_in_apply3_tma); it is stored here, where each cell reads only itself
+    const float beta = UPD ? ((st->in_it == 0 || !(st->rz_prev > 0.0)) ? 0.0f : float(st->rz / st->rz_prev)) : 0.0f;
     // Breakdown of the FP32 recurrence: once the remaining error is smooth, L d in FP32 is
     // mostly cancellation noise, <d, L d> collapses and alpha blows up (a V-cycle-
     // preconditioned step is O(1)).  Such a step is not taken; the check below ends the
@@ -1535,7 +1654,7 @@ __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, const float *__
             const long long P = base + (long long)k * fs;
             const bool ok = k < nf;
             ev[u] = ok ? e[P] : 0.0f;
-            dv[u] = ok ? d[P] : 0.0f;
+            dv[u] = ok ? (UPD ? L.x[P] + beta * d[P] : d[P]) : 0.0f;
             rv[u] = ok ? L.b[P] : 0.0f;
             qv[u] = ok ? q[P] : 0.0f;
         }
@@ -1544,6 +1663,7 @@ __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, const float *__
             const int k = k0 + u * IN_BX;
             if (k >= nf) continue;
             const long long P = base + (long long)k * fs;
+            if (UPD) d[P] = dv[u];
             e[P] = ev[u] + alpha * dv[u];
             const float r = rv[u] - alpha * qv[u];
             L.b[P] = r;
@@ -1846,9 +1966,10 @@ bool Poisson::make_level0_maps(const std::vector<Level<float>> &Ls) {
     const cuuint64_t strides[2] = {cuuint64_t(L.s[1]) * sizeof(float), cuuint64_t(L.s[0]) * sizeof(float)};
     const cuuint32_t box[3] = {TS_W, TS_H, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
-    float *ptr[4] = {L.x, L.x2, static_cast<float *>(rho_pad), L.b};
-    for (int m = 0; m < 4; ++m) {
-        const CUresult r = encode(&tmap[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ptr[m], dims, strides, box, estr,
+    float *ptr[5] = {L.x, L.x2, static_cast<float *>(rho_pad), L.b, d32};
+    for (int m = 0; m < 5; ++m) {
+        const int slot = m < 4 ? m : 5;   // tmap[4] is level 1's x (below)
+        const CUresult r = encode(&tmap[slot], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ptr[m], dims, strides, box, estr,
                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return false;
@@ -1899,6 +2020,7 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM_PRO)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_restrict3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_in_apply3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     if (const char *e = std::getenv("SCIHPC_SWEEP_TMA")) tma_enable = std::atoi(e) != 0;
     if (!density) {
         // constant coefficients: build the hierarchy once (rho unused)
@@ -2256,10 +2378,20 @@ void Poisson::iterate_dim(cudaStream_t s) {
         const int nbi = inner_blocks(L0, DIM);
         vcycle<float>(s);
         k_in_dot<DIM><<<nbi, ib, 0, s>>>(L0, slot, dev_state);
-        k_in_update_d<DIM><<<nbi, ib, 0, s>>>(L0, d32, dev_state);
-        if (mode0 == 1) k_in_apply<DIM, 1><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
-        else k_in_apply<DIM, 2><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
-        k_in_axpy<DIM><<<nbi, ib, 0, s>>>(L0, d32, q32, e32, slot, dev_state);
+        const int aci = DIM == 3 ? apply_chunk(L0.n) : 0;
+        if (DIM == 3 && mode0 == 1 && tma_ready && tma_enable && aci > 0) {
+            // direction update fused: staged q = L (z + beta d_old), then axpy stores d
+            const int tiles = ((L0.n[2] + SW_TK - 1) / SW_TK) * ((L0.n[1] + SW_TJ - 1) / SW_TJ);
+            const unsigned blocks = unsigned(tiles * ((L0.n[0] + aci - 1) / aci));
+            k_in_apply3_tma<<<blocks, AP_THREADS, TS_SMEM, s>>>(tmap[0], tmap[2], tmap[5], L0, q32, id2, aci, slot,
+                                                               dev_state, &dev_state->sweep_err);
+            k_in_axpy<DIM, true><<<nbi, ib, 0, s>>>(L0, d32, q32, e32, slot, dev_state);
+        } else {
+            k_in_update_d<DIM><<<nbi, ib, 0, s>>>(L0, d32, dev_state);
+            if (mode0 == 1) k_in_apply<DIM, 1><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
+            else k_in_apply<DIM, 2><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
+            k_in_axpy<DIM, false><<<nbi, ib, 0, s>>>(L0, d32, q32, e32, slot, dev_state);
+        }
         k_in_check<<<1, 1, 0, s>>>(dev_state, inner_max, max_iter);
         k_out_add<DIM><<<nb, TPB, 0, s>>>(p_, e32, O, L0, dev_state);
         k_out_res<DIM><<<nb, TPB, 0, s>>>(rhs_, p_, O, L0, e32, slot, dev_state);

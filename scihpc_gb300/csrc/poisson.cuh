@@ -116,8 +116,9 @@ private:
     double *partial = nullptr;       // reduction scratch (2 x RED_MAX_BLOCKS)
     double *oc = nullptr;            // FP64 +face coefficients of the outer operator (3 compact arrays)
     double *dense = nullptr;         // coarsest-level inverse (n x n, FP64)
-    // TMA descriptors of the FP32 level 0 (3D): x, x2, padded density, b; and level 1's x
-    CUtensorMap tmap[5];
+    // TMA descriptors of the FP32 level 0 (3D): x, x2, padded density, b; level 1's x; the
+    // inner conjugate-gradient direction
+    CUtensorMap tmap[6];
     bool tma_ready = false, tma_pro_ready = false;
     int tma_enable = 1;
     int ncoarse = 0;
