@@ -657,22 +657,61 @@ constexpr size_t TS_SMEM_PRO = size_t(TS_STAGES_PRO) * (3 * TS_PLANE + TS_CSLOT)
 static_assert((TS_PLANE * sizeof(float)) % 128 == 0, "fine box size");
 static_assert(((3 * TS_PLANE + TS_CSLOT) * sizeof(float)) % 128 == 0, "stage size with the coarse box");
 
+// Deterministic grid-wide sum of one value per thread for blocks of any size up to 1024
+// threads, in a 2D grid of at most RED_MAX_BLOCKS blocks: the block's values go through `red`
+// (blockDim doubles of shared memory the caller lends), warp 0 sums them in a fixed order,
+// and the last block to arrive sums the block partials in a fixed order.
+__device__ void block_grid_sum(double v, double *red, RedSlot slot, double *out) {
+    __shared__ bool last;
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int bid = blockIdx.x + blockIdx.y * gridDim.x, nb = gridDim.x * gridDim.y;
+    red[t] = v;
+    __syncthreads();
+    if (t < 32) {
+        double a = 0.0;
+        for (int u = t; u < nt; u += 32) a += red[u];
+        for (int w = 16; w > 0; w >>= 1) a += __shfl_down_sync(0xffffffffu, a, w);
+        if (t == 0) {
+            slot.partial[bid] = a;
+            __threadfence();
+            last = atomicAdd(slot.counter, 1u) == unsigned(nb - 1);
+        }
+    }
+    __syncthreads();
+    if (!last || t >= 32) return;
+    __threadfence();
+    double a = 0.0;
+    for (int q = t; q < nb; q += 32) a += __ldcg(&slot.partial[q]);
+    for (int w = 16; w > 0; w >>= 1) a += __shfl_down_sync(0xffffffffu, a, w);
+    if (t == 0) {
+        *out = a;
+        *slot.counter = 0u;
+    }
+}
+
 // out-of-place sweep of level 0; ZERO: the old iterate is zero (not loaded).  PRO: the old
 // iterate is x + P e, with e the level-1 correction (piecewise-constant prolongation, ratio 2)
 // added on the fly from a staged coarse box: the prolongation pass and its write of x are
-// saved, and the values are the same (one FP32 addition per neighbour).  err: set when a
-// staged plane did not arrive within the wait limit (the sweep's output is then invalid).
-template <bool ZERO, bool PRO>
+// saved, and the values are the same (one FP32 addition per neighbour).  DOT: the sweep is
+// the last of a V-cycle that preconditions the inner conjugate gradients, so its output is z
+// and the staged right-hand side is the inner residual r: <r, z> is reduced into *dot.  err:
+// set when a staged plane did not arrive within the wait limit (the sweep's output is then
+// invalid).
+template <bool ZERO, bool PRO, bool DOT>
 __global__ void __launch_bounds__(SW_THREADS, 2)
     k_sweep3_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_rho,
                  const __grid_constant__ CUtensorMap map_b, const __grid_constant__ CUtensorMap map_e,
-                 Level<float> L, float *__restrict__ xn, SweepCoef<float> cf, int c0, int ci, int *err) {
+                 Level<float> L, float *__restrict__ xn, SweepCoef<float> cf, int c0, int ci, int *err,
+                 RedSlot slot, double *dot) {
     static_assert(!(ZERO && PRO), "a prolongated iterate is not zero");
+    static_assert(!(DOT && (ZERO || PRO)), "the dot product belongs to the last sweep of a cycle");
     constexpr int NS = PRO ? TS_STAGES_PRO : TS_STAGES;
     constexpr int SST = 3 * TS_PLANE + (PRO ? TS_CSLOT : 0);   // floats per stage
     extern __shared__ unsigned char ts_raw[];
     __shared__ uint64_t bar[NS];
-    __shared__ float first[2][SW_ROWS][SW_PAIRS];
+    // after the plane loop, DOT reuses these SW_THREADS * 2 floats as SW_THREADS doubles
+    __shared__ __align__(16) float first[2][SW_ROWS][SW_PAIRS];
+    static_assert(2 * SW_ROWS * SW_PAIRS >= 2 * SW_THREADS, "reduction scratch");
     float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
     const int tid = threadIdx.x;
     // Warps 0 .. SW_TJ-1 each own one interior row of SW_TK/2 column pairs (first and second
@@ -737,6 +776,7 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
     // the (i, i+1) face coefficient of the first-colour update two steps back is the (i-2, i-1)
     // face of the second-colour update (same column)
     float c1h1 = 0, c1h2 = 0;
+    float acc = 0.0f;   // DOT: this thread's part of <r, z> (FP32, as the inner vector kernels)
     bool fail = __syncthreads_or(!ok);
     for (int q = 1; q <= nq - 2 && !fail; ++q) {
         // planes q - 2 .. q + 1 are on chip
@@ -765,7 +805,10 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         const float fa = (Xc[2 * TS_PLANE + o] + sx) * prcp(cim + C1 + C2 + C3 + C4 + C5);
         const float fi = fvalid ? fa : 0.0f;
         const int off = (i + 1) * s0 + col + par;
-        if (inner && fvalid && i >= i0 && i < i1) xn[off] = fi;
+        if (inner && fvalid && i >= i0 && i < i1) {
+            xn[off] = fi;
+            if (DOT) acc = fmaf(Xc[2 * TS_PLANE + o], fi, acc);
+        }
         first[q & 1][row][pr] = fi;
         // second colour of plane i-1 from the first-colour values of planes i-2, i-1, i
         const int ib = i - 1;
@@ -778,7 +821,10 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
             const float D4 = w2 * prcp(rim + Rm[o - 1]), D5 = w2 * prcp(rim + Rm[o + 1]);
             const float sb = D0 * f2 + cim * fi + D2 * first[qb][row - 1][pr] + D3 * first[qb][row + 1][pr] + D4 * n4 +
                              D5 * n5;
-            xn[off - s0] = (Xm[2 * TS_PLANE + o] + sb) * prcp(D0 + cim + D2 + D3 + D4 + D5);
+            const float rb = Xm[2 * TS_PLANE + o];
+            const float fb = (rb + sb) * prcp(D0 + cim + D2 + D3 + D4 + D5);
+            xn[off - s0] = fb;
+            if (DOT) acc = fmaf(rb, fb, acc);
         }
         f2 = f1;
         f1 = fi;
@@ -806,6 +852,12 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
             for (int q = waited + 1; q <= issued; ++q) wait_plane(q);
         }
         __syncthreads();
+    }
+    if (DOT) {
+        // every block takes part (a failed one with its partial sum), so the reduction's
+        // counter always completes
+        __syncthreads();
+        block_grid_sum(double(acc), reinterpret_cast<double *>(&first[0][0][0]), slot, dot);
     }
 }
 
@@ -2016,9 +2068,10 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM_PRO)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM_PRO)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_restrict3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_in_apply3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     if (const char *e = std::getenv("SCIHPC_SWEEP_TMA")) tma_enable = std::atoi(e) != 0;
@@ -2157,8 +2210,10 @@ int Poisson::set_density(const double *rho, cudaStream_t s) {
     return SCIHPC_OK;
 }
 
+// dot: when not null, the last level-0 sweep may also reduce <b, x> (the inner residual and the
+// preconditioned residual) into *dot; the return value says whether it did.
 template <class T>
-void Poisson::vcycle(cudaStream_t s) {
+bool Poisson::vcycle(cudaStream_t s, double *dot) {
     std::vector<Level<T>> &Ls = levs<T>();
     const bool neumann = bc_ == 0;
     const int mode0 = (density_ || neumann) ? (sizeof(T) == 8 ? 0 : 1) : 2;
@@ -2216,7 +2271,10 @@ void Poisson::vcycle(cudaStream_t s) {
     // the first post-smoothing sweep of level 0 can apply the prolongation itself
     const bool pro0 = sizeof(T) == 4 && mode0 == 1 && tma_ready && tma_pro_ready && tma_enable && fused(0) &&
                       Ls[0].ratio == 2 && !prolong_linear;
-    auto sweep = [&](int l, const T *xo, T *xn, int c0, int zero, bool pro) {
+    // dot_out: set when the last sweep reduced <b, x> of level 0 into *dot
+    bool dot_done = false;
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
+    auto sweep = [&](int l, const T *xo, T *xn, int c0, int zero, bool pro, bool want_dot) {
         Level<T> &L = Ls[l];
         const int ci = sweep_chunk(L.n);
         const dim3 grid(unsigned(((L.n[2] + SW_TK - 1) / SW_TK) * ((L.n[1] + SW_TJ - 1) / SW_TJ)),
@@ -2234,14 +2292,18 @@ void Poisson::vcycle(cudaStream_t s) {
                 const CUtensorMap &mx = xo == Ls[0].x ? tmap[0] : tmap[1];
                 int *err = &dev_state->sweep_err;
                 if (zero)
-                    k_sweep3_tma<true, false><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], tmap[4], L, xn, cf,
-                                                                                 c0, ci, err);
+                    k_sweep3_tma<true, false, false><<<grid, SW_THREADS, TS_SMEM, s>>>(
+                        mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, nullptr);
                 else if (pro)
-                    k_sweep3_tma<false, true><<<grid, SW_THREADS, TS_SMEM_PRO, s>>>(mx, tmap[2], tmap[3], tmap[4], L, xn,
-                                                                                    cf, c0, ci, err);
-                else
-                    k_sweep3_tma<false, false><<<grid, SW_THREADS, TS_SMEM, s>>>(mx, tmap[2], tmap[3], tmap[4], L, xn,
-                                                                                 cf, c0, ci, err);
+                    k_sweep3_tma<false, true, false><<<grid, SW_THREADS, TS_SMEM_PRO, s>>>(
+                        mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, nullptr);
+                else if (want_dot && (long long)grid.x * grid.y <= RED_MAX_BLOCKS) {
+                    k_sweep3_tma<false, false, true><<<grid, SW_THREADS, TS_SMEM, s>>>(
+                        mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, dot);
+                    dot_done = true;
+                } else
+                    k_sweep3_tma<false, false, false><<<grid, SW_THREADS, TS_SMEM, s>>>(
+                        mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, nullptr);
                 return;
             }
         }
@@ -2250,12 +2312,12 @@ void Poisson::vcycle(cudaStream_t s) {
         else if constexpr (sizeof(T) == 4) k_sweep3<T, 1><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
     };
     // nu is even, so an even number of out-of-place sweeps leaves the iterate in x
-    auto smooth_level = [&](int l, int c0, bool from_zero, bool pro) {
+    auto smooth_level = [&](int l, int c0, bool from_zero, bool pro, bool want_dot) {
         if (fused(l)) {
             for (int k = 0; k < nu; ++k) {
                 T *src = (k & 1) ? Ls[l].x2 : Ls[l].x;
                 T *dst = (k & 1) ? Ls[l].x : Ls[l].x2;
-                sweep(l, src, dst, c0, (k == 0 && from_zero) ? 1 : 0, k == 0 && pro);
+                sweep(l, src, dst, c0, (k == 0 && from_zero) ? 1 : 0, k == 0 && pro, want_dot && k == nu - 1);
             }
         } else {
             for (int k = 0; k < nu; ++k) {
@@ -2270,7 +2332,7 @@ void Poisson::vcycle(cudaStream_t s) {
             leg2(l, false);
             continue;
         }
-        smooth_level(l, 0, true, false);   // level 0 starts from zero; coarser levels are zeroed by restriction
+        smooth_level(l, 0, true, false, false);   // level 0 starts from zero; coarser levels are zeroed by restriction
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const long long nc = (long long)Cl.n[0] * Cl.n[1] * Cl.n[2];
         const unsigned nb = blocks_for(nc, TPB);
@@ -2311,7 +2373,7 @@ void Poisson::vcycle(cudaStream_t s) {
     for (int l = lc - 1; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         if (l == 0 && pro0) {
-            smooth_level(0, 1, false, true);
+            smooth_level(0, 1, false, true, dot != nullptr);
             continue;
         }
         if (fused2(l)) {
@@ -2325,8 +2387,9 @@ void Poisson::vcycle(cudaStream_t s) {
                                     unsigned(F.n[0])),
                                dim3(PR_BX, PR_BY), 0, s>>>(F, Cl);
         else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
-        smooth_level(l, 1, false, false);
+        smooth_level(l, 1, false, false, l == 0 && dot != nullptr);
     }
+    return dot_done;
 }
 
 void Poisson::begin(const double *rhs, double *p, int use_guess, cudaStream_t s) {
@@ -2376,8 +2439,7 @@ void Poisson::iterate_dim(cudaStream_t s) {
         for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? float(1.0 / (D.d[a] * D.d[a])) : 0.0f;
         const dim3 ib(IN_BX, IN_BY);
         const int nbi = inner_blocks(L0, DIM);
-        vcycle<float>(s);
-        k_in_dot<DIM><<<nbi, ib, 0, s>>>(L0, slot, dev_state);
+        if (!vcycle<float>(s, &dev_state->rz)) k_in_dot<DIM><<<nbi, ib, 0, s>>>(L0, slot, dev_state);
         const int aci = DIM == 3 ? apply_chunk(L0.n) : 0;
         if (DIM == 3 && mode0 == 1 && tma_ready && tma_enable && aci > 0) {
             // direction update fused: staged q = L (z + beta d_old), then axpy stores d

@@ -89,7 +89,7 @@ private:
         else return Ld;
     }
     template <class T>
-    void vcycle(cudaStream_t s);
+    bool vcycle(cudaStream_t s, double *dot = nullptr);
     template <class T>
     int alloc_levels();
     template <class T>
