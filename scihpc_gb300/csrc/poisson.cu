@@ -2104,6 +2104,15 @@ void Poisson::destroy() {
     oc = nullptr;
     if (host_state) cudaFreeHost(host_state);
     r = nullptr;
+    drop_solve_graph();
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
+}
+
+void Poisson::drop_solve_graph() {
+    if (solve_exec) cudaGraphExecDestroy(solve_exec);
+    solve_exec = nullptr;
+    solve_key = SolveKey{};
 }
 
 namespace {
@@ -2193,6 +2202,7 @@ static Outer make_outer(const Dims &D, int density, int dirichlet, const double 
 
 int Poisson::set_density(const double *rho, cudaStream_t s) {
     rho64 = rho;
+    ++density_epoch;
     if (density_) {
         const Outer O = make_outer(D, density_, bc_ == 1, oc);
         const int nb = grid_blocks(D.interior());
@@ -2483,34 +2493,108 @@ void Poisson::finish_dim(double *p, cudaStream_t s) {
     k_relres<<<1, 1, 0, s>>>(dev_state);
 }
 
+// Capture of a whole solve on the private stream: [begin] -> while (not done) { iterate }
+// -> [finish].  The while-node's condition starts at 1 and is written by the convergence
+// kernels at the end of every iteration (0 once the solve is done, which the iteration cap
+// guarantees).
+int Poisson::capture_solve(const double *rhs, double *p, int use_guess) {
+    drop_solve_graph();
+    if (!cap_stream) SCIHPC_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr, pre_g = nullptr, post_g = nullptr;
+    auto fail = [&](cudaError_t e) {
+        cudaStreamCaptureStatus st;
+        if (cudaStreamIsCapturing(cap_stream, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(cap_stream, &junk);
+            if (junk) cudaGraphDestroy(junk);
+        }
+        for (cudaGraph_t x : {g, pre_g, post_g})
+            if (x) cudaGraphDestroy(x);
+        use_conditional = false;
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "capture of the pressure solve: %s", cudaGetErrorString(e));
+        set_last_error(msg);
+        return SCIHPC_ERR_CUDA;
+    };
+#define SCIHPC_CAP(call)                  \
+    do {                                  \
+        const cudaError_t e_ = (call);    \
+        if (e_ != cudaSuccess) return fail(e_); \
+    } while (0)
+    SCIHPC_CAP(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle handle;
+    SCIHPC_CAP(cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault));
+    use_conditional = true;
+    conditional = (unsigned long long)handle;
+    SCIHPC_CAP(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+    begin(rhs, p, use_guess, cap_stream);
+    SCIHPC_CAP(cudaStreamEndCapture(cap_stream, &pre_g));
+    cudaGraphNode_t pre_node, cond_node, post_node;
+    SCIHPC_CAP(cudaGraphAddChildGraphNode(&pre_node, g, nullptr, 0, pre_g));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    SCIHPC_CAP(cudaGraphAddNode(&cond_node, g, &pre_node, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    SCIHPC_CAP(cudaStreamBeginCaptureToGraph(cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    iterate(cap_stream);
+    SCIHPC_CAP(cudaStreamEndCapture(cap_stream, &body));
+    SCIHPC_CAP(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+    finish(p, cap_stream);
+    SCIHPC_CAP(cudaStreamEndCapture(cap_stream, &post_g));
+    SCIHPC_CAP(cudaGraphAddChildGraphNode(&post_node, g, &cond_node, 1, post_g));
+    SCIHPC_CAP(cudaGraphInstantiate(&solve_exec, g, 0));
+#undef SCIHPC_CAP
+    cudaGraphDestroy(pre_g);
+    cudaGraphDestroy(post_g);
+    cudaGraphDestroy(g);
+    use_conditional = false;
+    return SCIHPC_OK;
+}
+
 int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int maxit, int *iters, double *relres,
                    cudaStream_t s) {
     rel_tol = tol;
     max_iter = maxit;
     use_conditional = false;
-    begin(rhs, p, use_guess, s);
-    SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
-    SCIHPC_CUDA(cudaStreamSynchronize(s));
     const bool trace = std::getenv("SCIHPC_PPE_TRACE") != nullptr;
-    if (trace) std::fprintf(stderr, "ppe it %d relres %.3e\n", host_state->it, host_state->relres);
-    while (!host_state->done) {
-        iterate(s);
+    const char *ge = std::getenv("SCIHPC_PPE_GRAPH");
+    if (!trace && !(ge && ge[0] == '0')) {
+        SolveKey key;
+        key.rhs = rhs, key.p = p, key.use_guess = use_guess, key.max_iter = maxit, key.inner_max = inner_max;
+        key.prolong_linear = prolong_linear, key.rel_tol = tol, key.inner_tol = inner_tol, key.epoch = density_epoch;
+        if (!solve_exec || !(key == solve_key)) {
+            const int rc = capture_solve(rhs, p, use_guess);
+            if (rc) return rc;
+            solve_key = key;
+        }
+        SCIHPC_CUDA(cudaGraphLaunch(solve_exec, s));
+    } else {
+        begin(rhs, p, use_guess, s);
         SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         SCIHPC_CUDA(cudaStreamSynchronize(s));
-        if (trace)
-            std::fprintf(stderr, "ppe it %d relres %.3e rz %.3e dq %.3e in_it %d rr_in %.3e rr_in0 %.3e target %.3e\n",
-                         host_state->it, host_state->relres, host_state->rz, host_state->dq, host_state->in_it,
-                         host_state->rr_in, host_state->rr_in0, host_state->in_target);
+        if (trace) std::fprintf(stderr, "ppe it %d relres %.3e\n", host_state->it, host_state->relres);
+        while (!host_state->done) {
+            iterate(s);
+            SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+            SCIHPC_CUDA(cudaStreamSynchronize(s));
+            if (trace)
+                std::fprintf(stderr, "ppe it %d relres %.3e rz %.3e dq %.3e in_it %d rr_in %.3e rr_in0 %.3e target %.3e\n",
+                             host_state->it, host_state->relres, host_state->rz, host_state->dq, host_state->in_it,
+                             host_state->rr_in, host_state->rr_in0, host_state->in_target);
+        }
+        finish(p, s);
     }
-    const int it = host_state->it;
-    const bool div = host_state->diverged;
-    finish(p, s);
     SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
     SCIHPC_CUDA(cudaStreamSynchronize(s));
     SCIHPC_CUDA(cudaGetLastError());
+    // finish leaves the iteration count and the divergence flag as the loop left them
+    const int it = host_state->it;
     if (iters) *iters = it;
     if (relres) *relres = host_state->relres;
-    if (div) {
+    if (host_state->diverged) {
         set_last_error("pressure solve produced a non-finite residual");
         return SCIHPC_ERR_NONFINITE;
     }

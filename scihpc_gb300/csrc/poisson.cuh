@@ -60,7 +60,10 @@ public:
     void begin(const double *rhs, double *p, int use_guess, cudaStream_t s);
     void iterate(cudaStream_t s);   // one outer iteration incl. convergence test
     void finish(double *p, cudaStream_t s);
-    // Host-driven solve: iterates until converged or max_iter (synchronising once per iteration).
+    // Whole solve: begin, a conditional while-node over iterate, finish, captured once into a
+    // CUDA graph (rebuilt when its inputs change) and launched; one host synchronisation at
+    // the end.  SCIHPC_PPE_GRAPH=0 or SCIHPC_PPE_TRACE selects the host loop instead
+    // (synchronising once per iteration).
     int solve(const double *rhs, double *p, int use_guess, double rel_tol, int max_iter, int *iters, double *relres,
               cudaStream_t s);
     int levels(int *out, int max_levels) const;
@@ -101,6 +104,26 @@ private:
     void iterate_dim(cudaStream_t s);
     template <int DIM>
     void finish_dim(double *p, cudaStream_t s);
+    int capture_solve(const double *rhs, double *p, int use_guess);
+    void drop_solve_graph();
+
+    // the captured solve and what it was captured for
+    struct SolveKey {
+        const double *rhs = nullptr;
+        double *p = nullptr;
+        int use_guess = 0, max_iter = 0, inner_max = 0, prolong_linear = 0;
+        double rel_tol = 0.0, inner_tol = 0.0;
+        long long epoch = -1;
+        bool operator==(const SolveKey &o) const {
+            return rhs == o.rhs && p == o.p && use_guess == o.use_guess && max_iter == o.max_iter &&
+                   inner_max == o.inner_max && prolong_linear == o.prolong_linear && rel_tol == o.rel_tol &&
+                   inner_tol == o.inner_tol && epoch == o.epoch;
+        }
+    };
+    cudaGraphExec_t solve_exec = nullptr;
+    SolveKey solve_key{};
+    cudaStream_t cap_stream = nullptr;   // private stream the solve is captured on
+    long long density_epoch = 0;         // advanced by set_density
 
     Dims D{};
     int bc_ = 0, density_ = 1, fp32_ = 0;
