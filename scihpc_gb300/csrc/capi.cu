@@ -1,5 +1,6 @@
 // capi.cu -- the extern "C" entry points declared in include/scihpc_gpu.h.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -27,6 +28,14 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
 }
 
 // structured_grid.cpp:7-134 -- d = (end - start) / n, h = min d, dv = prod d.
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char *e = std::getenv("SCIHPC_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 Dims make_dims(const scihpc_grid *g) {
     Dims D{};
     D.ndim = g->ndim;

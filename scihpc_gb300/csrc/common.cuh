@@ -85,6 +85,50 @@ void set_last_error(const char *msg);
 
 inline unsigned blocks_for(long long n, int threads) { return unsigned((n + threads - 1) / threads); }
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may be scheduled while the
+// kernel before it in the stream (or graph) is still finishing; it must call pdl_wait() before
+// it touches memory that kernel writes (all kernels here call it first).  pdl_trigger() lets
+// the next kernel be scheduled once every block of this one has started.  Both are no-ops for
+// a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void pdl_trigger() {
+#if defined(__CUDA_ARCH__)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
+// SCIHPC_PDL=0 turns the programmatic attribute off everywhere (ordinary launches of the same
+// kernels)
+bool pdl_enabled();
+
+template <class... P>
+inline void launch_pdl_args(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool on, P... a) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = on ? 1 : 0;
+    void *args[] = {(void *)&a...};
+    cudaLaunchKernelExC(&cfg, (const void *)k, args);
+}
+
+// k<<<grid, block, smem, s>>>(args...), as a programmatic dependent launch when `on`; the
+// arguments are converted to the kernel's parameter types first
+template <class... P, class... A>
+inline void launch_pdl(bool on, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A &&...args) {
+    static_assert(sizeof...(P) == sizeof...(A), "argument count");
+    launch_pdl_args<P...>(k, grid, block, smem, s, on, static_cast<P>(args)...);
+}
+
 // Interior linear index q -> (I, J, K) with K fastest, matching the reference loop nests.
 // Linear index -> (I, J, K).  Indices below 2^31 (every grid of practical size) are split
 // in 32-bit arithmetic: a 64-bit division is a long instruction sequence on the GPU.

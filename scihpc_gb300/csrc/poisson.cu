@@ -246,6 +246,8 @@ __global__ void k_init(const double *__restrict__ rhs, double *__restrict__ p, O
 template <int DIM, class T>
 __global__ void k_dot_rz(const double *__restrict__ r, const T *__restrict__ z, const T *__restrict__ zold, Outer O,
                          Level<T> L0, RedSlot slot, PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     double v[2] = {0.0, 0.0};
     for_cells<DIM>(O, [&](int I, int J, int K, long long, long long co) {
@@ -262,6 +264,8 @@ __global__ void k_dot_rz(const double *__restrict__ r, const T *__restrict__ z, 
 template <int DIM, class T>
 __global__ void k_update_d(const T *__restrict__ z, T *__restrict__ zold, double *__restrict__ d, Outer O,
                            Level<T> L0, const PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     // after a residual replacement the old direction no longer matches r: restart
     const double beta = (st->it == 0 || st->restart) ? 0.0 : (st->rz - st->r_zold) / st->rz_prev;
@@ -277,6 +281,8 @@ __global__ void k_update_d(const T *__restrict__ z, T *__restrict__ zold, double
 template <int DIM>
 __global__ void k_apply_dq(const double *__restrict__ d, double *__restrict__ qv, Outer O, RedSlot slot,
                            PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->restart = 0;   // k_update_d has consumed it
     double v[1] = {0.0};
@@ -293,6 +299,8 @@ __global__ void k_apply_dq(const double *__restrict__ d, double *__restrict__ qv
 template <int DIM, class T>
 __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const double *__restrict__ d,
                        const double *__restrict__ qv, Outer O, Level<T> L0, RedSlot slot, PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     // A step far outside (0, CG_ALPHA_MAX] means <d, L d> is round-off (the iteration has
     // reached the attainable accuracy): no update, and the check ends the solve.
@@ -318,6 +326,8 @@ __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const dou
 template <int DIM, class T>
 __global__ void k_replace(const double *__restrict__ rhs, const double *__restrict__ p, Outer O,
                           double *__restrict__ r, Level<T> L0, double tol, RedSlot slot, PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done || !(st->rr <= tol * tol * st->bb)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->restart = 1;
     const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
@@ -359,6 +369,8 @@ __device__ __forceinline__ void outer_progress(PcgScalars *st, double tol, int m
 
 __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
                         int use_handle) {
+    pdl_wait();
+    pdl_trigger();
     if (advance) {
         if (st->done) {
             set_cond(handle, use_handle, 0);
@@ -489,6 +501,8 @@ __device__ __forceinline__ void smooth_one(const Level<T> &L, const T *__restric
 
 template <class T, int MODE, int DIM>
 __global__ void k_smooth(Level<T> L, const T *__restrict__ rho, Id2<T> id2, int color) {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= smooth_count<T, DIM>(L)) return;
     smooth_one<T, MODE, DIM>(L, rho, id2.v, t, color);
@@ -559,6 +573,8 @@ template <class T, int MODE>
 __global__ void __launch_bounds__(SW_THREADS, 2) k_sweep3(Level<T> L, const T *__restrict__ xo, T *__restrict__ xn,
                                                           const T *__restrict__ rho, SweepCoef<T> cf, int c0,
                                                           int zero, int ci) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ T first[2][SW_ROWS][SW_PAIRS];
     const int tid = threadIdx.x;
     const int row = tid / SW_PAIRS, pr = tid - row * SW_PAIRS;
@@ -703,6 +719,8 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
                  const __grid_constant__ CUtensorMap map_b, const __grid_constant__ CUtensorMap map_e,
                  Level<float> L, float *__restrict__ xn, SweepCoef<float> cf, int c0, int ci, int *err,
                  RedSlot slot, double *dot) {
+    pdl_wait();
+    pdl_trigger();
     static_assert(!(ZERO && PRO), "a prolongated iterate is not zero");
     static_assert(!(DOT && (ZERO || PRO)), "the dot product belongs to the last sweep of a cycle");
     constexpr int NS = PRO ? TS_STAGES_PRO : TS_STAGES;
@@ -874,6 +892,8 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
     k_restrict3_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_rho,
                     const __grid_constant__ CUtensorMap map_b, Level<float> F, Level<float> Cl, Id2<float> id2, int ci,
                     int *err) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ unsigned char ts_raw[];
     __shared__ uint64_t bar[TS_STAGES];
     __shared__ float part[SW_TJ / 2][SW_TK / 2];   // sums of the odd rows
@@ -980,6 +1000,8 @@ constexpr int V2_T = 16, V2_H = 5, V2_R = V2_T + 2 * V2_H, V2_THREADS = 256;
 
 template <class T, int MODE, bool UP>
 __global__ void __launch_bounds__(V2_THREADS) k_vcycle2(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ T X[V2_R][V2_R], Bs[V2_R][V2_R];
     __shared__ T C0[MODE == 0 ? V2_R : 1][V2_R], C1[MODE == 0 ? V2_R : 1][V2_R], G[V2_R][V2_R];
     // MODE 1: G = density; MODE 0: C0 = cx, C1 = cy, G = 1 / diagonal
@@ -1086,6 +1108,8 @@ __global__ void __launch_bounds__(AP_THREADS)
     k_in_apply3_tma(const __grid_constant__ CUtensorMap map_z, const __grid_constant__ CUtensorMap map_rho,
                     const __grid_constant__ CUtensorMap map_d, Level<float> L, float *__restrict__ q, Id2<float> id2,
                     int ci, RedSlot slot, PcgScalars *st, int *err) {
+    pdl_wait();
+    pdl_trigger();
     static_assert(AP_THREADS == TPB, "grid_sum needs TPB threads");
     extern __shared__ unsigned char ts_raw[];
     __shared__ uint64_t bar[TS_STAGES];
@@ -1248,6 +1272,8 @@ __device__ __forceinline__ void restrict_one(const Level<T> &F, const Level<T> &
 
 template <class T, int MODE, int DIM>
 __global__ void k_restrict(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2) {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
     if (t >= nc) return;
@@ -1302,6 +1328,8 @@ __device__ __forceinline__ void prolong_one(const Level<T> &F, const Level<T> &C
 
 template <class T, int DIM>
 __global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long nf = (long long)F.n[0] * F.n[1] * (DIM == 3 ? F.n[2] : 1);
     if (t >= nf) return;
@@ -1314,6 +1342,8 @@ __global__ void k_prolong(Level<T> F, Level<T> Cl, int neumann, int linear) {
 constexpr int PR_BX = 64, PR_BY = 4;
 template <class T>
 __global__ void __launch_bounds__(PR_BX *PR_BY) k_prolong3_pc(Level<T> F, Level<T> Cl) {
+    pdl_wait();
+    pdl_trigger();
     const int k = blockIdx.x * PR_BX + threadIdx.x, j = blockIdx.y * PR_BY + threadIdx.y, i = blockIdx.z;
     if (k >= F.n[2] || j >= F.n[1]) return;
     const long long Pf = (long long)(i + 1) * F.s[0] + (long long)(j + 1) * F.s[1] + k + 1;
@@ -1554,6 +1584,8 @@ __device__ __forceinline__ void dense_apply(const Level<T> &L, const double *__r
 
 template <class T, int DIM>
 __global__ void k_dense_solve(Level<T> L, const double *__restrict__ Minv, int n, int neumann) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double b[1024];
     __shared__ double mean;
     dense_apply<T, DIM>(L, Minv, n, neumann, b, &mean);
@@ -1604,6 +1636,8 @@ inline int inner_blocks(const Level<float> &L, int ndim) {
 // rz = <r, z>
 template <int DIM>
 __global__ void __launch_bounds__(TPB) k_in_dot(Level<float> L, RedSlot slot, PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     float acc = 0.0f;   // per-thread partial in FP32 (FP64 arithmetic is 1/64 rate here)
     for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
@@ -1626,6 +1660,8 @@ __global__ void __launch_bounds__(TPB) k_in_dot(Level<float> L, RedSlot slot, Pc
 // d = z + beta d, beta = rz / rz_prev (0 on the first inner iteration)
 template <int DIM>
 __global__ void __launch_bounds__(TPB) k_in_update_d(Level<float> L, float *__restrict__ d, const PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     const float beta = (st->in_it == 0 || !(st->rz_prev > 0.0)) ? 0.0f : float(st->rz / st->rz_prev);
     for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
@@ -1650,6 +1686,8 @@ template <int DIM, int MODE>
 __global__ void __launch_bounds__(TPB) k_in_apply(Level<float> L, const float *__restrict__ rho, Id2<float> id2,
                                                   const float *__restrict__ d, float *__restrict__ q, RedSlot slot,
                                                   PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     float acc = 0.0f;
     const int s0 = int(L.s[0]), s1 = int(L.s[1]);   // padded level 0 has fewer than 2^31 cells
@@ -1685,6 +1723,8 @@ template <int DIM, bool UPD>
 __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, float *__restrict__ d,
                                                  const float *__restrict__ q, float *__restrict__ e, RedSlot slot,
                                                  PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     // UPD: the direction of this iteration is d = z + beta d_old (formed, not stored, by the
     // staged k_in_apply3_tma); it is stored here, where each cell reads only itself
@@ -1729,6 +1769,8 @@ __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, float *__restri
 
 // inner progress; marks the refinement step as due
 __global__ void k_in_check(PcgScalars *st, int inner_max, int max_iter) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) return;
     st->rz_prev = st->rz;
     st->it += 1;
@@ -1744,6 +1786,8 @@ __global__ void k_in_check(PcgScalars *st, int inner_max, int max_iter) {
 template <int DIM>
 __global__ void k_out_add(double *__restrict__ p, const float *__restrict__ e, Outer O, Level<float> L0,
                           const PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done || !st->pending) return;
     for_cells<DIM>(O, [&](int I, int J, int K, long long go, long long) { p[go] += double(e[p0_of<DIM>(L0, I, J, K)]); });
 }
@@ -1753,6 +1797,8 @@ __global__ void k_out_add(double *__restrict__ p, const float *__restrict__ e, O
 template <int DIM>
 __global__ void k_out_res(const double *__restrict__ rhs, const double *__restrict__ p, Outer O, Level<float> L0,
                           float *__restrict__ e, RedSlot slot, PcgScalars *st) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done || !st->pending) return;
     const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
     double v[1] = {0.0};
@@ -1770,6 +1816,8 @@ __global__ void k_out_res(const double *__restrict__ rhs, const double *__restri
 
 // refinement, part 3: convergence on the FP64 residual; drives the conditional while-node
 __global__ void k_out_check(PcgScalars *st, double tol, int max_iter, unsigned long long handle, int use_handle) {
+    pdl_wait();
+    pdl_trigger();
     if (st->done) {
         set_cond(handle, use_handle, 0);
         return;
@@ -1808,6 +1856,8 @@ inline size_t coarse_smem_bytes(const std::vector<Level<T>> &Ls, int lc, int ndi
 template <class T, int DIM>
 __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, int nlev, const double *__restrict__ Minv,
                                                         int n, int neumann, int linear, int smem_on) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(16) unsigned char coarse_dsm[];
     __shared__ Level<T> SL[16];
     __shared__ double b[1024];
@@ -2109,6 +2159,17 @@ void Poisson::destroy() {
     cap_stream = nullptr;
 }
 
+// Programmatic dependent launches for the kernels of an iteration.  Measured on GB300: they
+// shorten a 3D V-cycle launched kernel by kernel (0.600 -> 0.566 ms at 256^3) and the captured
+// 2D two-phase step (405 -> 414 steps/s), but lengthen the captured 3D solve (10.9 -> 11.5 ms
+// to 1e-10 at 256^3), so a 3D iteration being captured into a graph uses ordinary launches.
+bool Poisson::use_pdl(cudaStream_t s) const {
+    if (!pdl_enabled()) return false;
+    if (D.ndim == 2) return true;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &st) == cudaSuccess && st == cudaStreamCaptureStatusNone;
+}
+
 void Poisson::drop_solve_graph() {
     if (solve_exec) cudaGraphExecDestroy(solve_exec);
     solve_exec = nullptr;
@@ -2224,6 +2285,7 @@ int Poisson::set_density(const double *rho, cudaStream_t s) {
 // preconditioned residual) into *dot; the return value says whether it did.
 template <class T>
 bool Poisson::vcycle(cudaStream_t s, double *dot) {
+    const bool pdl = use_pdl(s);
     std::vector<Level<T>> &Ls = levs<T>();
     const bool neumann = bc_ == 0;
     const int mode0 = (density_ || neumann) ? (sizeof(T) == 8 ? 0 : 1) : 2;
@@ -2238,13 +2300,13 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         const unsigned nb = blocks_for(rows * nh, TPB);
         const int m = l == 0 ? mode0 : 0;
         if (D.ndim == 2) {
-            if (m == 0) k_smooth<T, 0, 2><<<nb, TPB, 0, s>>>(L, rp, id2, color);
-            else if (m == 1) k_smooth<T, 1, 2><<<nb, TPB, 0, s>>>(L, rp, id2, color);
-            else k_smooth<T, 2, 2><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+            if (m == 0) launch_pdl(pdl, k_smooth<T, 0, 2>, nb, TPB, 0, s, L, rp, id2, color);
+            else if (m == 1) launch_pdl(pdl, k_smooth<T, 1, 2>, nb, TPB, 0, s, L, rp, id2, color);
+            else launch_pdl(pdl, k_smooth<T, 2, 2>, nb, TPB, 0, s, L, rp, id2, color);
         } else {
-            if (m == 0) k_smooth<T, 0, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
-            else if (m == 1) k_smooth<T, 1, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
-            else k_smooth<T, 2, 3><<<nb, TPB, 0, s>>>(L, rp, id2, color);
+            if (m == 0) launch_pdl(pdl, k_smooth<T, 0, 3>, nb, TPB, 0, s, L, rp, id2, color);
+            else if (m == 1) launch_pdl(pdl, k_smooth<T, 1, 3>, nb, TPB, 0, s, L, rp, id2, color);
+            else launch_pdl(pdl, k_smooth<T, 2, 3>, nb, TPB, 0, s, L, rp, id2, color);
         }
     };
     // levels from lc on (small enough for one block) run inside one thread block
@@ -2271,11 +2333,11 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         const dim3 grid(unsigned((F.n[1] + V2_T - 1) / V2_T), unsigned((F.n[0] + V2_T - 1) / V2_T));
         const bool m1 = l == 0 && mode0 == 1;
         if (up) {
-            if (m1) k_vcycle2<T, 1, true><<<grid, V2_THREADS, 0, s>>>(F, Cl, rp, id2);
-            else k_vcycle2<T, 0, true><<<grid, V2_THREADS, 0, s>>>(F, Cl, rp, id2);
+            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
+            else launch_pdl(pdl, k_vcycle2<T, 0, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
         } else {
-            if (m1) k_vcycle2<T, 1, false><<<grid, V2_THREADS, 0, s>>>(F, Cl, rp, id2);
-            else k_vcycle2<T, 0, false><<<grid, V2_THREADS, 0, s>>>(F, Cl, rp, id2);
+            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, false>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
+            else launch_pdl(pdl, k_vcycle2<T, 0, false>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
         }
     };
     // the first post-smoothing sweep of level 0 can apply the prolongation itself
@@ -2302,24 +2364,24 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
                 const CUtensorMap &mx = xo == Ls[0].x ? tmap[0] : tmap[1];
                 int *err = &dev_state->sweep_err;
                 if (zero)
-                    k_sweep3_tma<true, false, false><<<grid, SW_THREADS, TS_SMEM, s>>>(
+                    launch_pdl(pdl, k_sweep3_tma<true, false, false>, grid, SW_THREADS, TS_SMEM, s, 
                         mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, nullptr);
                 else if (pro)
-                    k_sweep3_tma<false, true, false><<<grid, SW_THREADS, TS_SMEM_PRO, s>>>(
+                    launch_pdl(pdl, k_sweep3_tma<false, true, false>, grid, SW_THREADS, TS_SMEM_PRO, s, 
                         mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, nullptr);
                 else if (want_dot && (long long)grid.x * grid.y <= RED_MAX_BLOCKS) {
-                    k_sweep3_tma<false, false, true><<<grid, SW_THREADS, TS_SMEM, s>>>(
+                    launch_pdl(pdl, k_sweep3_tma<false, false, true>, grid, SW_THREADS, TS_SMEM, s, 
                         mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, dot);
                     dot_done = true;
                 } else
-                    k_sweep3_tma<false, false, false><<<grid, SW_THREADS, TS_SMEM, s>>>(
+                    launch_pdl(pdl, k_sweep3_tma<false, false, false>, grid, SW_THREADS, TS_SMEM, s, 
                         mx, tmap[2], tmap[3], tmap[4], L, xn, cf, c0, ci, err, slot, nullptr);
                 return;
             }
         }
-        if (m == 0) k_sweep3<T, 0><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
-        else if (m == 2) k_sweep3<T, 2><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
-        else if constexpr (sizeof(T) == 4) k_sweep3<T, 1><<<grid, SW_THREADS, 0, s>>>(L, xo, xn, rp, cf, c0, zero, ci);
+        if (m == 0) launch_pdl(pdl, k_sweep3<T, 0>, grid, SW_THREADS, 0, s, L, xo, xn, rp, cf, c0, zero, ci);
+        else if (m == 2) launch_pdl(pdl, k_sweep3<T, 2>, grid, SW_THREADS, 0, s, L, xo, xn, rp, cf, c0, zero, ci);
+        else if constexpr (sizeof(T) == 4) launch_pdl(pdl, k_sweep3<T, 1>, grid, SW_THREADS, 0, s, L, xo, xn, rp, cf, c0, zero, ci);
     };
     // nu is even, so an even number of out-of-place sweeps leaves the iterate in x
     auto smooth_level = [&](int l, int c0, bool from_zero, bool pro, bool want_dot) {
@@ -2352,19 +2414,19 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
                 const int ci = restrict_chunk(F.n);
                 const dim3 grid(unsigned(((F.n[2] + SW_TK - 1) / SW_TK) * ((F.n[1] + SW_TJ - 1) / SW_TJ)),
                                 unsigned((F.n[0] + ci - 1) / ci));
-                k_restrict3_tma<<<grid, RT_THREADS, TS_SMEM, s>>>(tmap[0], tmap[2], tmap[3], F, Cl, id2, ci,
+                launch_pdl(pdl, k_restrict3_tma, grid, RT_THREADS, TS_SMEM, s, tmap[0], tmap[2], tmap[3], F, Cl, id2, ci,
                                                                   &dev_state->sweep_err);
                 continue;
             }
         }
         if (D.ndim == 2) {
-            if (m == 0) k_restrict<T, 0, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
-            else if (m == 1) k_restrict<T, 1, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
-            else k_restrict<T, 2, 2><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+            if (m == 0) launch_pdl(pdl, k_restrict<T, 0, 2>, nb, TPB, 0, s, F, Cl, rp, id2);
+            else if (m == 1) launch_pdl(pdl, k_restrict<T, 1, 2>, nb, TPB, 0, s, F, Cl, rp, id2);
+            else launch_pdl(pdl, k_restrict<T, 2, 2>, nb, TPB, 0, s, F, Cl, rp, id2);
         } else {
-            if (m == 0) k_restrict<T, 0, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
-            else if (m == 1) k_restrict<T, 1, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
-            else k_restrict<T, 2, 3><<<nb, TPB, 0, s>>>(F, Cl, rp, id2);
+            if (m == 0) launch_pdl(pdl, k_restrict<T, 0, 3>, nb, TPB, 0, s, F, Cl, rp, id2);
+            else if (m == 1) launch_pdl(pdl, k_restrict<T, 1, 3>, nb, TPB, 0, s, F, Cl, rp, id2);
+            else launch_pdl(pdl, k_restrict<T, 2, 3>, nb, TPB, 0, s, F, Cl, rp, id2);
         }
     }
     if (packed && lc >= 1) {
@@ -2373,12 +2435,12 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         const size_t sm = coarse_smem_bytes(Ls, lc, D.ndim);
         const int on = sm <= COARSE_SMEM_MAX ? 1 : 0;
         const size_t dyn = on ? sm : 0;
-        if (D.ndim == 2) k_coarse_cycle<T, 2><<<1, 1024, dyn, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear, on);
-        else k_coarse_cycle<T, 3><<<1, 1024, dyn, s>>>(LP, lc, nlev, dense, ncoarse, neumann, prolong_linear, on);
+        if (D.ndim == 2) launch_pdl(pdl, k_coarse_cycle<T, 2>, 1, 1024, dyn, s, LP, lc, nlev, dense, ncoarse, neumann, prolong_linear, on);
+        else launch_pdl(pdl, k_coarse_cycle<T, 3>, 1, 1024, dyn, s, LP, lc, nlev, dense, ncoarse, neumann, prolong_linear, on);
     } else {
         Level<T> &C = Ls[nlev - 1];
-        if (D.ndim == 2) k_dense_solve<T, 2><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
-        else k_dense_solve<T, 3><<<1, 1024, 0, s>>>(C, dense, ncoarse, neumann);
+        if (D.ndim == 2) launch_pdl(pdl, k_dense_solve<T, 2>, 1, 1024, 0, s, C, dense, ncoarse, neumann);
+        else launch_pdl(pdl, k_dense_solve<T, 3>, 1, 1024, 0, s, C, dense, ncoarse, neumann);
     }
     for (int l = lc - 1; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
@@ -2391,12 +2453,11 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
             continue;
         }
         const long long nf = (long long)F.n[0] * F.n[1] * F.n[2];
-        if (D.ndim == 2) k_prolong<T, 2><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
+        if (D.ndim == 2) launch_pdl(pdl, k_prolong<T, 2>, blocks_for(nf, TPB), TPB, 0, s, F, Cl, neumann, prolong_linear);
         else if (F.ratio == 2 && !prolong_linear && F.n[0] <= 65535 && F.n[1] <= 65535 * PR_BY)
-            k_prolong3_pc<T><<<dim3(unsigned((F.n[2] + PR_BX - 1) / PR_BX), unsigned((F.n[1] + PR_BY - 1) / PR_BY),
-                                    unsigned(F.n[0])),
-                               dim3(PR_BX, PR_BY), 0, s>>>(F, Cl);
-        else k_prolong<T, 3><<<blocks_for(nf, TPB), TPB, 0, s>>>(F, Cl, neumann, prolong_linear);
+            launch_pdl(pdl, k_prolong3_pc<T>, dim3(unsigned((F.n[2] + PR_BX - 1) / PR_BX), unsigned((F.n[1] + PR_BY - 1) / PR_BY),
+                                    unsigned(F.n[0])), dim3(PR_BX, PR_BY), 0, s, F, Cl);
+        else launch_pdl(pdl, k_prolong<T, 3>, blocks_for(nf, TPB), TPB, 0, s, F, Cl, neumann, prolong_linear);
         smooth_level(l, 1, false, false, l == 0 && dot != nullptr);
     }
     return dot_done;
@@ -2438,6 +2499,7 @@ void Poisson::begin_dim(const double *rhs, double *p, int use_guess, cudaStream_
 
 template <int DIM>
 void Poisson::iterate_dim(cudaStream_t s) {
+    const bool pdl = use_pdl(s);
     const Outer O = make_outer(D, density_, bc_ == 1, oc);
     RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     const int nb = grid_blocks(D.interior());
@@ -2449,35 +2511,35 @@ void Poisson::iterate_dim(cudaStream_t s) {
         for (int a = 0; a < 3; ++a) id2.v[a] = a < D.ndim ? float(1.0 / (D.d[a] * D.d[a])) : 0.0f;
         const dim3 ib(IN_BX, IN_BY);
         const int nbi = inner_blocks(L0, DIM);
-        if (!vcycle<float>(s, &dev_state->rz)) k_in_dot<DIM><<<nbi, ib, 0, s>>>(L0, slot, dev_state);
+        if (!vcycle<float>(s, &dev_state->rz)) launch_pdl(pdl, k_in_dot<DIM>, nbi, ib, 0, s, L0, slot, dev_state);
         const int aci = DIM == 3 ? apply_chunk(L0.n) : 0;
         if (DIM == 3 && mode0 == 1 && tma_ready && tma_enable && aci > 0) {
             // direction update fused: staged q = L (z + beta d_old), then axpy stores d
             const int tiles = ((L0.n[2] + SW_TK - 1) / SW_TK) * ((L0.n[1] + SW_TJ - 1) / SW_TJ);
             const unsigned blocks = unsigned(tiles * ((L0.n[0] + aci - 1) / aci));
-            k_in_apply3_tma<<<blocks, AP_THREADS, TS_SMEM, s>>>(tmap[0], tmap[2], tmap[5], L0, q32, id2, aci, slot,
+            launch_pdl(pdl, k_in_apply3_tma, blocks, AP_THREADS, TS_SMEM, s, tmap[0], tmap[2], tmap[5], L0, q32, id2, aci, slot,
                                                                dev_state, &dev_state->sweep_err);
-            k_in_axpy<DIM, true><<<nbi, ib, 0, s>>>(L0, d32, q32, e32, slot, dev_state);
+            launch_pdl(pdl, k_in_axpy<DIM, true>, nbi, ib, 0, s, L0, d32, q32, e32, slot, dev_state);
         } else {
-            k_in_update_d<DIM><<<nbi, ib, 0, s>>>(L0, d32, dev_state);
-            if (mode0 == 1) k_in_apply<DIM, 1><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
-            else k_in_apply<DIM, 2><<<nbi, ib, 0, s>>>(L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
-            k_in_axpy<DIM, false><<<nbi, ib, 0, s>>>(L0, d32, q32, e32, slot, dev_state);
+            launch_pdl(pdl, k_in_update_d<DIM>, nbi, ib, 0, s, L0, d32, dev_state);
+            if (mode0 == 1) launch_pdl(pdl, k_in_apply<DIM, 1>, nbi, ib, 0, s, L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
+            else launch_pdl(pdl, k_in_apply<DIM, 2>, nbi, ib, 0, s, L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
+            launch_pdl(pdl, k_in_axpy<DIM, false>, nbi, ib, 0, s, L0, d32, q32, e32, slot, dev_state);
         }
-        k_in_check<<<1, 1, 0, s>>>(dev_state, inner_max, max_iter);
-        k_out_add<DIM><<<nb, TPB, 0, s>>>(p_, e32, O, L0, dev_state);
-        k_out_res<DIM><<<nb, TPB, 0, s>>>(rhs_, p_, O, L0, e32, slot, dev_state);
-        k_out_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, conditional, uc);
+        launch_pdl(pdl, k_in_check, 1, 1, 0, s, dev_state, inner_max, max_iter);
+        launch_pdl(pdl, k_out_add<DIM>, nb, TPB, 0, s, p_, e32, O, L0, dev_state);
+        launch_pdl(pdl, k_out_res<DIM>, nb, TPB, 0, s, rhs_, p_, O, L0, e32, slot, dev_state);
+        launch_pdl(pdl, k_out_check, 1, 1, 0, s, dev_state, rel_tol, max_iter, conditional, uc);
         return;
     }
     Level<double> &L0 = Ld[0];
     vcycle<double>(s);
-    k_dot_rz<DIM, double><<<nb, TPB, 0, s>>>(r, L0.x, (const double *)zold, O, L0, slot, dev_state);
-    k_update_d<DIM, double><<<nb, TPB, 0, s>>>(L0.x, (double *)zold, dvec, O, L0, dev_state);
-    k_apply_dq<DIM><<<nb, TPB, 0, s>>>(dvec, q, O, slot, dev_state);
-    k_axpy<DIM, double><<<nb, TPB, 0, s>>>(p_, r, dvec, q, O, L0, slot, dev_state);
-    k_replace<DIM, double><<<nb, TPB, 0, s>>>(rhs_, p_, O, r, L0, rel_tol, slot, dev_state);
-    k_check<<<1, 1, 0, s>>>(dev_state, rel_tol, max_iter, 1, conditional, uc);
+    launch_pdl(pdl, k_dot_rz<DIM, double>, nb, TPB, 0, s, r, L0.x, (const double *)zold, O, L0, slot, dev_state);
+    launch_pdl(pdl, k_update_d<DIM, double>, nb, TPB, 0, s, L0.x, (double *)zold, dvec, O, L0, dev_state);
+    launch_pdl(pdl, k_apply_dq<DIM>, nb, TPB, 0, s, dvec, q, O, slot, dev_state);
+    launch_pdl(pdl, k_axpy<DIM, double>, nb, TPB, 0, s, p_, r, dvec, q, O, L0, slot, dev_state);
+    launch_pdl(pdl, k_replace<DIM, double>, nb, TPB, 0, s, rhs_, p_, O, r, L0, rel_tol, slot, dev_state);
+    launch_pdl(pdl, k_check, 1, 1, 0, s, dev_state, rel_tol, max_iter, 1, conditional, uc);
 }
 
 template <int DIM>

@@ -105,6 +105,7 @@ private:
     template <int DIM>
     void finish_dim(double *p, cudaStream_t s);
     int capture_solve(const double *rhs, double *p, int use_guess);
+    bool use_pdl(cudaStream_t s) const;
     void drop_solve_graph();
 
     // the captured solve and what it was captured for
