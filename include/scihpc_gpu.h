@@ -155,6 +155,11 @@ int scihpc_poisson_solve(scihpc_poisson *ps, const double *rhs, double *p, int u
  * solver's operator, on the GPU in FP64; synchronises `stream`.  The residual() of
  * multigrid_base (multigrid_base.cpp:69-72) for the finest level. */
 int scihpc_poisson_residual(scihpc_poisson *ps, const double *rhs, const double *p, double *norm, void *stream);
+/* FP32 mode (fp32 = 1): each inner FP32 conjugate-gradient solve stops once its residual has
+ * dropped by inner_tol (0 < inner_tol < 1) or after inner_max (>= 1) iterations, and the FP64
+ * refinement step follows.  Defaults 1e-4 and 12.  No reference counterpart (the reference
+ * solves in FP64 only). */
+int scihpc_poisson_set_inner(scihpc_poisson *ps, double inner_tol, int inner_max);
 /* Times `ncycles` V-cycles (the preconditioner alone, on the residual of p = 0 for rhs)
  * with CUDA events on `stream`; *ms receives the total.  p is overwritten with zeros.
  * Synchronises `stream`.  Measurement hook with no reference counterpart. */

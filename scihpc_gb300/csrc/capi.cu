@@ -294,6 +294,13 @@ int scihpc_poisson_residual(scihpc_poisson *ps, const double *rhs, const double 
     return ps->ps.residual(rhs, p, norm, S(stream));
 }
 
+int scihpc_poisson_set_inner(scihpc_poisson *ps, double inner_tol, int inner_max) {
+    REQUIRE(ps && inner_tol > 0.0 && inner_tol < 1.0 && inner_max >= 1, "poisson_set_inner: bad argument");
+    ps->ps.inner_tol = inner_tol;
+    ps->ps.inner_max = inner_max;
+    return SCIHPC_OK;
+}
+
 int scihpc_poisson_time_vcycles(scihpc_poisson *ps, const double *rhs, double *p, int ncycles, float *ms,
                                 void *stream) {
     REQUIRE(ps && rhs && p && ms && ncycles > 0, "poisson_time_vcycles: bad argument");

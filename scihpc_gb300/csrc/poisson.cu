@@ -2263,7 +2263,6 @@ static Outer make_outer(const Dims &D, int density, int dirichlet, const double 
 
 int Poisson::set_density(const double *rho, cudaStream_t s) {
     rho64 = rho;
-    ++density_epoch;
     if (density_) {
         const Outer O = make_outer(D, density_, bc_ == 1, oc);
         const int nb = grid_blocks(D.interior());
@@ -2623,17 +2622,26 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
     use_conditional = false;
     const bool trace = std::getenv("SCIHPC_PPE_TRACE") != nullptr;
     const char *ge = std::getenv("SCIHPC_PPE_GRAPH");
-    if (!trace && !(ge && ge[0] == '0')) {
+    bool graph = !trace && !(ge && ge[0] == '0');
+    if (graph) {
         SolveKey key;
         key.rhs = rhs, key.p = p, key.use_guess = use_guess, key.max_iter = maxit, key.inner_max = inner_max;
-        key.prolong_linear = prolong_linear, key.rel_tol = tol, key.inner_tol = inner_tol, key.epoch = density_epoch;
-        if (!solve_exec || !(key == solve_key)) {
+        key.prolong_linear = prolong_linear, key.rel_tol = tol, key.inner_tol = inner_tol;
+        // a solve whose inputs were seen on the previous call is captured (and then replayed
+        // while they stay the same); a one-off solve runs the host loop and pays no capture
+        if (solve_exec && key == solve_key) {
+            SCIHPC_CUDA(cudaGraphLaunch(solve_exec, s));
+        } else if (key == last_key) {
             const int rc = capture_solve(rhs, p, use_guess);
             if (rc) return rc;
             solve_key = key;
+            SCIHPC_CUDA(cudaGraphLaunch(solve_exec, s));
+        } else {
+            graph = false;
         }
-        SCIHPC_CUDA(cudaGraphLaunch(solve_exec, s));
-    } else {
+        last_key = key;
+    }
+    if (!graph) {
         begin(rhs, p, use_guess, s);
         SCIHPC_CUDA(cudaMemcpyAsync(host_state, dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         SCIHPC_CUDA(cudaStreamSynchronize(s));

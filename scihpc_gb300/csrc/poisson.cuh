@@ -60,9 +60,10 @@ public:
     void begin(const double *rhs, double *p, int use_guess, cudaStream_t s);
     void iterate(cudaStream_t s);   // one outer iteration incl. convergence test
     void finish(double *p, cudaStream_t s);
-    // Whole solve: begin, a conditional while-node over iterate, finish, captured once into a
-    // CUDA graph (rebuilt when its inputs change) and launched; one host synchronisation at
-    // the end.  SCIHPC_PPE_GRAPH=0 or SCIHPC_PPE_TRACE selects the host loop instead
+    // Whole solve.  When the same inputs come back (repeated solves of a time loop or a
+    // benchmark) it runs as one CUDA graph: begin, a conditional while-node over iterate,
+    // finish, captured once and replayed, with one host synchronisation at the end.  A solve
+    // with new inputs, SCIHPC_PPE_GRAPH=0 or SCIHPC_PPE_TRACE runs the host loop instead
     // (synchronising once per iteration).
     int solve(const double *rhs, double *p, int use_guess, double rel_tol, int max_iter, int *iters, double *relres,
               cudaStream_t s);
@@ -108,23 +109,23 @@ private:
     bool use_pdl(cudaStream_t s) const;
     void drop_solve_graph();
 
-    // the captured solve and what it was captured for
+    // the captured solve and what it was captured for (set_density rewrites the coefficient
+    // arrays in place, so a new density needs no new capture)
     struct SolveKey {
         const double *rhs = nullptr;
         double *p = nullptr;
         int use_guess = 0, max_iter = 0, inner_max = 0, prolong_linear = 0;
         double rel_tol = 0.0, inner_tol = 0.0;
-        long long epoch = -1;
         bool operator==(const SolveKey &o) const {
             return rhs == o.rhs && p == o.p && use_guess == o.use_guess && max_iter == o.max_iter &&
                    inner_max == o.inner_max && prolong_linear == o.prolong_linear && rel_tol == o.rel_tol &&
-                   inner_tol == o.inner_tol && epoch == o.epoch;
+                   inner_tol == o.inner_tol;
         }
     };
     cudaGraphExec_t solve_exec = nullptr;
     SolveKey solve_key{};
+    SolveKey last_key{};   // inputs of the previous solve call
     cudaStream_t cap_stream = nullptr;   // private stream the solve is captured on
-    long long density_epoch = 0;         // advanced by set_density
 
     Dims D{};
     int bc_ = 0, density_ = 1, fp32_ = 0;

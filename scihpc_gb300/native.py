@@ -96,6 +96,7 @@ _SIGS = {
                                     ctypes.c_int),
     "scihpc_poisson_levels": ([_vp, _ip, ctypes.c_int], ctypes.c_int),
     "scihpc_poisson_residual": ([_vp, _vp, _vp, _dp, _vp], ctypes.c_int),
+    "scihpc_poisson_set_inner": ([_vp, ctypes.c_double, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_create": ([ctypes.POINTER(_GridC), _ip, _ip, _dp, _ip, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_destroy": ([_vp], ctypes.c_int),
     "scihpc_twophase_upload": ([_vp, ctypes.c_char_p, _dp], ctypes.c_int),
@@ -283,6 +284,10 @@ class Poisson:
         ms = ctypes.c_float(0.0)
         self.L.check(self.L.scihpc_poisson_time_vcycles(self.h, _ptr(rhs), _ptr(p), ncycles, ctypes.byref(ms), stream))
         return ms.value
+
+    def set_inner(self, inner_tol: float, inner_max: int) -> None:
+        """FP32 mode: residual reduction and iteration cap of each inner FP32 solve."""
+        self.L.check(self.L.scihpc_poisson_set_inner(self.h, float(inner_tol), int(inner_max)))
 
     def residual(self, rhs, p, stream=0) -> float:
         """||rhs - A p|| over the interior cells (FP64, on the GPU)."""

@@ -208,3 +208,41 @@ def test_levels_follow_reference_rule(port):
         g = O.Grid(nd, n, (0,) * nd, (1,) * nd)
         ps = Poisson(native(g), bc=0, density=True, fp32=False)
         assert [tuple(l[:nd]) for l in ps.levels()] == [tuple(l[:nd]) for l in port.mg_levels(nd, n)]
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+@pytest.mark.parametrize("case", ["2d", "3d_fused"])
+def test_repeated_solve_graph_replay(fp32, case):
+    """A solve repeated with the same inputs runs as a captured CUDA graph (second call: capture
+    and launch; third: replay); it gives bit for bit the answer of the host-driven loop, also
+    after set_density changes the coefficients between replays."""
+    from scihpc_gb300 import Poisson
+    n, hi = DENSITY_GRIDS[case]
+    g = O.Grid(len(n), n, (0.0,) * len(n), hi)
+    rho, rhs = _density_case(g, 11)
+    rho2, _ = _density_case(g, 12)
+    rho_d, rhs_d = dev(rho), dev(rhs)
+    ps = Poisson(native(g), bc=0, density=True, fp32=fp32)
+    ps.set_density(rho_d)
+    p = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    runs = []
+    for _ in range(3):
+        p.zero_()
+        it, rr = ps.solve(rhs_d, p, rel_tol=1e-11, max_iter=200)
+        runs.append((p.cpu().numpy(), it, rr))
+    for out, it, rr in runs[1:]:
+        assert it == runs[0][1] and rr == runs[0][2], (it, rr, runs[0][1:])
+        assert np.array_equal(out, runs[0][0])
+    # new coefficients, same buffers: the replay uses them
+    rho_d.copy_(dev(rho2))
+    ps.set_density(rho_d)
+    p.zero_()
+    it2, rr2 = ps.solve(rhs_d, p, rel_tol=1e-11, max_iter=200)
+    fresh = Poisson(native(g), bc=0, density=True, fp32=fp32)
+    fresh.set_density(rho_d)
+    q = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    it3, rr3 = fresh.solve(rhs_d, q, rel_tol=1e-11, max_iter=200)   # first call: host loop
+    assert it2 == it3 and rr2 == rr3 and rr2 <= 1e-11, (it2, rr2, it3, rr3)
+    assert torch.equal(p, q)
+    ps.close()
+    fresh.close()
