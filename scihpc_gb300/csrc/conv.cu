@@ -1,15 +1,22 @@
-// conv.cu -- 3x3 convolution (stride 1, zero padding 1) as implicit GEMM on the 5th-generation
-// tensor cores: BF16 operands in shared memory, FP32 accumulators in TMEM (tcgen05.mma issued
-// by one thread, completion tracked by mbarriers), plus the weight-gradient GEMM.
+// conv.cu -- 3x3 (2D) and 3x3x3 (3D) convolutions (stride 1, zero padding 1) as implicit GEMM on
+// the 5th-generation tensor cores: BF16 operands in shared memory, FP32 accumulators in TMEM
+// (tcgen05.mma issued by one thread, completion tracked by mbarriers), plus the weight-gradient
+// GEMM.
 //
 // Activations are [pixels][channels] (channels fastest, a multiple of 16), pixels row-major
-// over an H x W image.  Tap t = 3 * (dy + 1) + (dx + 1) reads pixel (y + dy, x + dx).
+// over a D x H x W grid (D = 1 in 2D).  Tap t reads pixel (z + dz, y + dy, x + dx): in 2D
+// t = 3 (dy + 1) + (dx + 1) (9 taps), in 3D t = 9 (dz + 1) + 3 (dy + 1) + (dx + 1) (27 taps).
 //   forward:   Y[p][co] = b[co] + sum_{t, ci} X[p + off(t)][ci] * W[co][t][ci]   (GEMM M = pixels,
-//              N = Co, K = 9 Ci; optional ReLU; BF16 or FP32 output)
+//              N = Co, K = taps Ci; optional ReLU; BF16 or FP32 output)
 //   data grad: dX[p][ci] = sum_{t, co} dZ[p + off(t)][co] * Wt[ci][t][co] with
-//              Wt[ci][t][co] = W[co][8 - t][ci] -- the forward kernel on transposed weights
-//   weights:   dW[co][t][ci] = sum_p X[p + off(t)][ci] * dZ[p][co]   (GEMM M = 9 Ci rows
+//              Wt[ci][t][co] = W[co][taps - 1 - t][ci] -- the forward kernel on transposed weights
+//   weights:   dW[co][t][ci] = sum_p X[p + off(t)][ci] * dZ[p][co]   (GEMM M = taps Ci rows
 //              (t, ci), N = Co, K = pixels, split over blocks and reduced in fixed order)
+//
+// Pipeline: a K-step is 16 K-elements (one tap x 16 channels forward, 16 pixels for the
+// weights); a stage holds as many K-steps as fit in CONV_STAGE_BYTES, the threads fill one
+// stage while the MMAs of the other run, and one thread issues the stage's MMAs back to back,
+// so a copy round trip and a block barrier are paid once per stage rather than per MMA.
 #include "conv.cuh"
 #include "tc.cuh"
 
@@ -19,6 +26,7 @@ namespace {
 
 constexpr int TILE_M = 128;   // pixels (forward) or (tap, ci) rows (weight gradient) per block
 constexpr int THREADS = 128;  // four warps: one per 32-lane quarter of TMEM in the epilogue
+constexpr int CONV_STAGE_BYTES = 32 * 1024;   // per stage, two stages per block: three blocks per SM
 
 __host__ __device__ inline uint32_t tmem_cols(int n) {
     uint32_t c = 32;
@@ -26,24 +34,42 @@ __host__ __device__ inline uint32_t tmem_cols(int n) {
     return c;
 }
 
+// bytes of one K-step's operands (A: 128 rows x 16 K, B: N rows x 16 K) and K-steps per stage
+// (no more than the nk steps of the whole reduction)
+__host__ __device__ inline int step_bytes(int n) { return TILE_M * 32 + n * 32; }
+inline int steps_per_stage(int n, int nk) {
+    int s = CONV_STAGE_BYTES / step_bytes(n);
+    if (s > nk) s = nk;
+    return s < 1 ? 1 : s;
+}
+
 // byte offset of the 16-byte chunk (row r, K half kb) of an operand tile with 16 K-elements
 __device__ __forceinline__ uint32_t chunk_off(int r, int kb) { return uint32_t(((r >> 3) * 2 + kb) * 128 + (r & 7) * 16); }
 
+// tap t -> (dz, dy, dx)
+__device__ __forceinline__ void tap_shift(int t, bool three, int &dz, int &dy, int &dx) {
+    dz = 0;
+    if (three) {
+        dz = t / 9 - 1;
+        t -= (dz + 1) * 9;
+    }
+    dy = t / 3 - 1;
+    dx = t - (dy + 1) * 3 - 1;
+}
+
 // ------------------------------------------------------------------ forward / data gradient
-// X [HW][Ci] bf16, Wk [N][9][Ci] bf16 (N output channels), bias [N] or null, out [HW][N]
+// X [DHW][Ci] bf16, Wk [N][taps][Ci] bf16 (N output channels), bias [N] or null, out [DHW][N]
 template <bool OUT_BF16>
-__global__ void __launch_bounds__(THREADS) k_conv3x3(const __nv_bfloat16 *__restrict__ X,
-                                                     const __nv_bfloat16 *__restrict__ Wk,
-                                                     const float *__restrict__ bias, void *__restrict__ out, int H,
-                                                     int W, int Ci, int N, int relu, int *err) {
+__global__ void __launch_bounds__(THREADS) k_conv(const __nv_bfloat16 *__restrict__ X,
+                                                  const __nv_bfloat16 *__restrict__ Wk,
+                                                  const float *__restrict__ bias, void *__restrict__ out, int D,
+                                                  int H, int W, int Ci, int N, int relu, int sk, int *err) {
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int stage_a = TILE_M * 32, stage_b = N * 32;   // bytes per stage
-    unsigned char *sA[2] = {sm, sm + stage_a + stage_b};
-    unsigned char *sB[2] = {sm + stage_a, sm + 2 * stage_a + stage_b};
-    const long long HW = (long long)H * W;
+    const int per = step_bytes(N);
+    const long long HW = (long long)H * W, P = HW * D;
     const long long p0 = (long long)blockIdx.x * TILE_M;
     const uint32_t ncols = tmem_cols(N);
     if (tid == 0) {
@@ -58,29 +84,45 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3(const __nv_bfloat16 *__rest
     const uint32_t idesc = tc::idesc_bf16(TILE_M, N);
     // this thread's pixel for the A operand
     const long long p = p0 + tid;
-    const int py = p < HW ? int(p / W) : 0, px = p < HW ? int(p % W) : 0;
-    const int nch = Ci / 16, nk = 9 * nch;
+    int pz = 0, py = 0, px = 0;
+    if (p < P) {
+        pz = int(p / HW);
+        const long long r = p - (long long)pz * HW;
+        py = int(r / W);
+        px = int(r - (long long)py * W);
+    }
+    const bool three = D > 1;
+    const int taps = three ? 27 : 9;
+    const int nch = Ci / 16, nk = taps * nch;
+    const int ng = (nk + sk - 1) / sk;
     bool ok = true;
-    for (int ks = 0; ks < nk; ++ks) {
-        const int s = ks & 1;
-        // the MMA two steps back read this stage; every thread must agree before reuse
-        const bool freed = ks < 2 || tc::mbar_wait(&mbar[s], uint32_t(((ks >> 1) - 1) & 1));
+    for (int g = 0; g < ng; ++g) {
+        const int s = g & 1;
+        // the MMAs two stages back read this buffer; every thread must agree before reuse
+        const bool freed = g < 2 || tc::mbar_wait(&mbar[s], uint32_t(((g >> 1) - 1) & 1));
         if (!__syncthreads_and(freed)) {
             ok = false;
             break;
         }
-        const int tap = ks / nch, cc = ks - tap * nch;
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-        {   // A: 16 channels of the shifted pixel, zero outside the image
-            const int ys = py + dy, xs = px + dx;
-            const bool in = p < HW && ys >= 0 && ys < H && xs >= 0 && xs < W;
-            const __nv_bfloat16 *src = in ? X + ((long long)ys * W + xs) * Ci + cc * 16 : X;
-            tc::cp16(sA[s] + chunk_off(tid, 0), src, in ? 16u : 0u);
-            tc::cp16(sA[s] + chunk_off(tid, 1), in ? src + 8 : X, in ? 16u : 0u);
-        }
-        for (int j = tid; j < 2 * N; j += THREADS) {   // B: 16 K-elements of each output channel
-            const int n = j >> 1, kb = j & 1;
-            tc::cp16(sB[s] + chunk_off(n, kb), Wk + ((long long)n * 9 + tap) * Ci + cc * 16 + kb * 8, 16u);
+        unsigned char *base = sm + size_t(s) * sk * per;
+        const int k0 = g * sk, kn = min(sk, nk - k0);
+        for (int j = 0; j < kn; ++j) {
+            const int ks = k0 + j;
+            const int tap = ks / nch, cc = ks - tap * nch;
+            int dz, dy, dx;
+            tap_shift(tap, three, dz, dy, dx);
+            unsigned char *a = base + j * per, *bt = a + TILE_M * 32;
+            {   // A: 16 channels of the shifted pixel, zero outside the grid
+                const int zs = pz + dz, ys = py + dy, xs = px + dx;
+                const bool in = p < P && zs >= 0 && zs < D && ys >= 0 && ys < H && xs >= 0 && xs < W;
+                const __nv_bfloat16 *src = in ? X + (((long long)zs * H + ys) * W + xs) * Ci + cc * 16 : X;
+                tc::cp16(a + chunk_off(tid, 0), src, in ? 16u : 0u);
+                tc::cp16(a + chunk_off(tid, 1), in ? src + 8 : X, in ? 16u : 0u);
+            }
+            for (int q = tid; q < 2 * N; q += THREADS) {   // B: 16 K-elements of each output channel
+                const int n = q >> 1, kb = q & 1;
+                tc::cp16(bt + chunk_off(n, kb), Wk + ((long long)n * taps + tap) * Ci + cc * 16 + kb * 8, 16u);
+            }
         }
         tc::cp_commit();
         tc::cp_wait_all();
@@ -89,13 +131,16 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3(const __nv_bfloat16 *__rest
         __syncthreads();
         if (tid == 0) {
             tc::fence_after();
-            const uint64_t ad = tc::sdesc(tc::smem_u32(sA[s]), 128, 256);
-            const uint64_t bd = tc::sdesc(tc::smem_u32(sB[s]), 128, 256);
-            tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            for (int j = 0; j < kn; ++j) {
+                unsigned char *a = base + j * per;
+                const uint64_t ad = tc::sdesc(tc::smem_u32(a), 128, 256);
+                const uint64_t bd = tc::sdesc(tc::smem_u32(a + TILE_M * 32), 128, 256);
+                tc::mma_bf16(tmem, ad, bd, idesc, (k0 + j) > 0 ? 1u : 0u);
+            }
             tc::commit(&mbar[s]);
         }
     }
-    if (ok) ok = __syncthreads_and(tc::mbar_wait(&mbar[(nk - 1) & 1], uint32_t(((nk - 1) >> 1) & 1)));
+    if (ok) ok = __syncthreads_and(tc::mbar_wait(&mbar[(ng - 1) & 1], uint32_t(((ng - 1) >> 1) & 1)));
     if (!ok) {
         if (lane == 0) atomicExch(err, 1);
     } else {
@@ -104,7 +149,7 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3(const __nv_bfloat16 *__rest
         for (int c = 0; c < N; c += 8) {
             float v[8];
             tc::tmem_ld8(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
-            if (pr < HW) {
+            if (pr < P) {
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     if (bias) v[q] += bias[c + q];
@@ -132,25 +177,27 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3(const __nv_bfloat16 *__rest
 // ------------------------------------------------------------------ weight gradient
 // partial[split][r][co] = sum over the split's pixels of X[p + off(t_r)][ci_r] * dZ[p][co],
 // r = t * Ci + ci over the rows of this block's M tile
-__global__ void __launch_bounds__(THREADS) k_conv3x3_wgrad(const __nv_bfloat16 *__restrict__ X,
-                                                           const __nv_bfloat16 *__restrict__ dZ,
-                                                           float *__restrict__ partial, int H, int W, int Ci, int N,
-                                                           int pix_per_split, int *err) {
+__global__ void __launch_bounds__(THREADS) k_conv_wgrad(const __nv_bfloat16 *__restrict__ X,
+                                                        const __nv_bfloat16 *__restrict__ dZ,
+                                                        float *__restrict__ partial, int D, int H, int W, int Ci,
+                                                        int N, int pix_per_split, int sk, int *err) {
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int stage_a = TILE_M * 32, stage_b = N * 32;
-    unsigned char *sA[2] = {sm, sm + stage_a + stage_b};
-    unsigned char *sB[2] = {sm + stage_a, sm + 2 * stage_a + stage_b};
-    const long long HW = (long long)H * W;
-    const int rows = 9 * Ci;
+    const int per = step_bytes(N);
+    const long long HW = (long long)H * W, P = HW * D;
+    const bool three = D > 1;
+    const int taps = three ? 27 : 9;
+    const int rows = taps * Ci;
     const int r = blockIdx.x * TILE_M + tid;   // this thread's (tap, ci) row of A
     const int tap = r < rows ? r / Ci : 0, ci = r < rows ? r % Ci : 0;
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    int dz, dy, dx;
+    tap_shift(tap, three, dz, dy, dx);
     const long long k0 = (long long)blockIdx.y * pix_per_split;
-    const long long k1 = k0 + pix_per_split < HW ? k0 + pix_per_split : HW;
-    const int nk = int((k1 - k0 + 15) / 16);
+    const long long k1 = k0 + pix_per_split < P ? k0 + pix_per_split : P;
+    const int nk = k1 > k0 ? int((k1 - k0 + 15) / 16) : 0;
+    const int ng = (nk + sk - 1) / sk;
     const uint32_t ncols = tmem_cols(N);
     if (tid == 0) {
         tc::mbar_init(&mbar[0], 1);
@@ -163,51 +210,64 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3_wgrad(const __nv_bfloat16 *
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = tc::idesc_bf16(TILE_M, N);
     bool ok = true;
-    for (int ks = 0; ks < nk; ++ks) {
-        const int s = ks & 1;
-        const bool freed = ks < 2 || tc::mbar_wait(&mbar[s], uint32_t(((ks >> 1) - 1) & 1));
+    for (int g = 0; g < ng; ++g) {
+        const int s = g & 1;
+        const bool freed = g < 2 || tc::mbar_wait(&mbar[s], uint32_t(((g >> 1) - 1) & 1));
         if (!__syncthreads_and(freed)) {
             ok = false;
             break;
         }
-        const long long kp = k0 + 16LL * ks;
-        {   // A row: X[p + off][ci] for 16 pixels, transposed into K order
-            __align__(16) __nv_bfloat16 v[16];
+        unsigned char *base = sm + size_t(s) * sk * per;
+        const int kn = min(sk, nk - g * sk);
+        for (int j = 0; j < kn; ++j) {
+            const long long kp = k0 + 16LL * (g * sk + j);
+            unsigned char *a = base + j * per, *bt = a + TILE_M * 32;
+            {   // A row: X[p + off][ci] for 16 pixels, transposed into K order
+                __align__(16) __nv_bfloat16 v[16];
+                int z = int(kp / HW);
+                const long long rem = kp - (long long)z * HW;
+                int y = int(rem / W), x = int(rem - (long long)y * W);
 #pragma unroll
-            for (int kk = 0; kk < 16; ++kk) {
-                const long long pp = kp + kk;
-                __nv_bfloat16 x = __float2bfloat16(0.0f);
-                if (r < rows && pp < k1) {
-                    const int y = int(pp / W) + dy, xx = int(pp % W) + dx;
-                    if (y >= 0 && y < H && xx >= 0 && xx < W) x = X[((long long)y * W + xx) * Ci + ci];
+                for (int kk = 0; kk < 16; ++kk) {
+                    __nv_bfloat16 xv = __float2bfloat16(0.0f);
+                    const int zs = z + dz, ys = y + dy, xs = x + dx;
+                    if (r < rows && kp + kk < k1 && zs >= 0 && zs < D && ys >= 0 && ys < H && xs >= 0 && xs < W)
+                        xv = X[(((long long)zs * H + ys) * W + xs) * Ci + ci];
+                    v[kk] = xv;
+                    if (++x == W) {
+                        x = 0;
+                        if (++y == H) y = 0, ++z;
+                    }
                 }
-                v[kk] = x;
+                *reinterpret_cast<uint4 *>(a + chunk_off(tid, 0)) = reinterpret_cast<uint4 *>(v)[0];
+                *reinterpret_cast<uint4 *>(a + chunk_off(tid, 1)) = reinterpret_cast<uint4 *>(v)[1];
             }
-            *reinterpret_cast<uint4 *>(sA[s] + chunk_off(tid, 0)) = reinterpret_cast<uint4 *>(v)[0];
-            *reinterpret_cast<uint4 *>(sA[s] + chunk_off(tid, 1)) = reinterpret_cast<uint4 *>(v)[1];
-        }
-        for (int n = tid; n < N; n += THREADS) {   // B row: dZ[p][n] for 16 pixels
-            __align__(16) __nv_bfloat16 v[16];
+            for (int n = tid; n < N; n += THREADS) {   // B row: dZ[p][n] for 16 pixels
+                __align__(16) __nv_bfloat16 v[16];
 #pragma unroll
-            for (int kk = 0; kk < 16; ++kk) {
-                const long long pp = kp + kk;
-                v[kk] = pp < k1 ? dZ[pp * N + n] : __float2bfloat16(0.0f);
+                for (int kk = 0; kk < 16; ++kk) {
+                    const long long pp = kp + kk;
+                    v[kk] = pp < k1 ? dZ[pp * N + n] : __float2bfloat16(0.0f);
+                }
+                *reinterpret_cast<uint4 *>(bt + chunk_off(n, 0)) = reinterpret_cast<uint4 *>(v)[0];
+                *reinterpret_cast<uint4 *>(bt + chunk_off(n, 1)) = reinterpret_cast<uint4 *>(v)[1];
             }
-            *reinterpret_cast<uint4 *>(sB[s] + chunk_off(n, 0)) = reinterpret_cast<uint4 *>(v)[0];
-            *reinterpret_cast<uint4 *>(sB[s] + chunk_off(n, 1)) = reinterpret_cast<uint4 *>(v)[1];
         }
         tc::fence_async_smem();
         tc::fence_before();
         __syncthreads();
         if (tid == 0) {
             tc::fence_after();
-            const uint64_t ad = tc::sdesc(tc::smem_u32(sA[s]), 128, 256);
-            const uint64_t bd = tc::sdesc(tc::smem_u32(sB[s]), 128, 256);
-            tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            for (int j = 0; j < kn; ++j) {
+                unsigned char *a = base + j * per;
+                const uint64_t ad = tc::sdesc(tc::smem_u32(a), 128, 256);
+                const uint64_t bd = tc::sdesc(tc::smem_u32(a + TILE_M * 32), 128, 256);
+                tc::mma_bf16(tmem, ad, bd, idesc, (g * sk + j) > 0 ? 1u : 0u);
+            }
             tc::commit(&mbar[s]);
         }
     }
-    if (ok && nk > 0) ok = __syncthreads_and(tc::mbar_wait(&mbar[(nk - 1) & 1], uint32_t(((nk - 1) >> 1) & 1)));
+    if (ok && ng > 0) ok = __syncthreads_and(tc::mbar_wait(&mbar[(ng - 1) & 1], uint32_t(((ng - 1) >> 1) & 1)));
     if (!ok) {
         if (lane == 0) atomicExch(err, 1);
     } else {
@@ -216,7 +276,7 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3_wgrad(const __nv_bfloat16 *
         float *dst = partial + ((long long)blockIdx.y * rows + rr) * N;
         for (int c = 0; c < N; c += 8) {
             float v[8];
-            if (nk > 0) tc::tmem_ld8(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+            if (ng > 0) tc::tmem_ld8(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
             else
                 for (int q = 0; q < 8; ++q) v[q] = 0.0f;
             if (rr < rows)
@@ -230,52 +290,76 @@ __global__ void __launch_bounds__(THREADS) k_conv3x3_wgrad(const __nv_bfloat16 *
 }
 
 // dW[co][t][ci] = sum over splits (fixed order) of partial[split][t * Ci + ci][co]
-__global__ void k_wgrad_reduce(const float *__restrict__ partial, float *__restrict__ dW, int Ci, int N, int splits) {
-    const int rows = 9 * Ci;
+__global__ void k_wgrad_reduce(const float *__restrict__ partial, float *__restrict__ dW, int rows, int N,
+                               int splits) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)rows * N) return;
     const int co = int(i / rows), r = int(i % rows);
     float s = 0.0f;
     for (int k = 0; k < splits; ++k) s += partial[((long long)k * rows + r) * N + co];
-    dW[i] = s;   // i = co * 9 Ci + t * Ci + ci
+    dW[i] = s;   // i = co * taps Ci + t * Ci + ci
+}
+
+int forward_impl(const __nv_bfloat16 *X, const __nv_bfloat16 *Wk, const float *bias, void *out, bool out_bf16, int D,
+                 int H, int W, int Ci, int N, bool relu, int *err, cudaStream_t s) {
+    if (Ci % 16 || N % 16 || N < 16 || N > 256 || D < 1 || H < 1 || W < 1) return SCIHPC_ERR_ARG;
+    const long long P = (long long)D * H * W;
+    const unsigned blocks = unsigned((P + TILE_M - 1) / TILE_M);
+    const int sk = steps_per_stage(N, (D > 1 ? 27 : 9) * (Ci / 16));
+    const size_t smem = size_t(2) * sk * step_bytes(N);
+    if (out_bf16)
+        k_conv<true><<<blocks, THREADS, smem, s>>>(X, Wk, bias, out, D, H, W, Ci, N, relu ? 1 : 0, sk, err);
+    else
+        k_conv<false><<<blocks, THREADS, smem, s>>>(X, Wk, bias, out, D, H, W, Ci, N, relu ? 1 : 0, sk, err);
+    return SCIHPC_OK;
+}
+
+int wgrad_impl(const __nv_bfloat16 *X, const __nv_bfloat16 *dZ, float *partial, float *dW, int D, int H, int W,
+               int Ci, int N, int splits, int *err, cudaStream_t s) {
+    if (Ci % 16 || N % 16 || N < 16 || N > 256 || splits < 1 || D < 1 || H < 1 || W < 1) return SCIHPC_ERR_ARG;
+    const long long P = (long long)D * H * W;
+    const int rows = (D > 1 ? 27 : 9) * Ci;
+    long long per = (P + splits - 1) / splits;
+    per = (per + 15) / 16 * 16;
+    const int used = int((P + per - 1) / per);
+    const dim3 grid(unsigned((rows + TILE_M - 1) / TILE_M), unsigned(used));
+    const int sk = steps_per_stage(N, int((per + 15) / 16));
+    k_conv_wgrad<<<grid, THREADS, size_t(2) * sk * step_bytes(N), s>>>(X, dZ, partial, D, H, W, Ci, N, int(per), sk,
+                                                                        err);
+    const long long tot = (long long)rows * N;
+    k_wgrad_reduce<<<unsigned((tot + 255) / 256), 256, 0, s>>>(partial, dW, rows, N, used);
+    return SCIHPC_OK;
 }
 
 }  // namespace
 
-size_t conv3x3_smem(int n) { return size_t(2) * (TILE_M * 32 + n * 32); }
+size_t conv_smem(int n) { return size_t(2) * steps_per_stage(n, 1 << 20) * step_bytes(n); }
 
 int conv3x3_forward(const __nv_bfloat16 *X, const __nv_bfloat16 *Wk, const float *bias, void *out, bool out_bf16,
                     int H, int W, int Ci, int N, bool relu, int *err, cudaStream_t s) {
-    if (Ci % 16 || N % 16 || N < 16 || N > 256) return SCIHPC_ERR_ARG;
-    const long long HW = (long long)H * W;
-    const unsigned blocks = unsigned((HW + TILE_M - 1) / TILE_M);
-    const size_t smem = conv3x3_smem(N);
-    if (out_bf16)
-        k_conv3x3<true><<<blocks, THREADS, smem, s>>>(X, Wk, bias, out, H, W, Ci, N, relu ? 1 : 0, err);
-    else
-        k_conv3x3<false><<<blocks, THREADS, smem, s>>>(X, Wk, bias, out, H, W, Ci, N, relu ? 1 : 0, err);
-    return SCIHPC_OK;
+    return forward_impl(X, Wk, bias, out, out_bf16, 1, H, W, Ci, N, relu, err, s);
+}
+
+int conv3x3x3_forward(const __nv_bfloat16 *X, const __nv_bfloat16 *Wk, const float *bias, void *out, bool out_bf16,
+                      int D, int H, int W, int Ci, int N, bool relu, int *err, cudaStream_t s) {
+    return forward_impl(X, Wk, bias, out, out_bf16, D, H, W, Ci, N, relu, err, s);
 }
 
 int conv3x3_wgrad(const __nv_bfloat16 *X, const __nv_bfloat16 *dZ, float *partial, float *dW, int H, int W, int Ci,
                   int N, int splits, int *err, cudaStream_t s) {
-    if (Ci % 16 || N % 16 || N < 16 || N > 256 || splits < 1) return SCIHPC_ERR_ARG;
-    const long long HW = (long long)H * W;
-    long long per = (HW + splits - 1) / splits;
-    per = (per + 15) / 16 * 16;
-    const int used = int((HW + per - 1) / per);
-    const dim3 grid(unsigned((9 * Ci + TILE_M - 1) / TILE_M), unsigned(used));
-    k_conv3x3_wgrad<<<grid, THREADS, conv3x3_smem(N), s>>>(X, dZ, partial, H, W, Ci, N, int(per), err);
-    const long long tot = 9LL * Ci * N;
-    k_wgrad_reduce<<<unsigned((tot + 255) / 256), 256, 0, s>>>(partial, dW, Ci, N, used);
-    return SCIHPC_OK;
+    return wgrad_impl(X, dZ, partial, dW, 1, H, W, Ci, N, splits, err, s);
 }
 
-int conv3x3_init(int max_n) {
-    const int smem = int(conv3x3_smem(max_n));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv3x3<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv3x3<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv3x3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+int conv3x3x3_wgrad(const __nv_bfloat16 *X, const __nv_bfloat16 *dZ, float *partial, float *dW, int D, int H, int W,
+                    int Ci, int N, int splits, int *err, cudaStream_t s) {
+    return wgrad_impl(X, dZ, partial, dW, D, H, W, Ci, N, splits, err, s);
+}
+
+int conv3x3_init(int) {
+    const int smem = 2 * CONV_STAGE_BYTES;
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     return SCIHPC_OK;
 }
 
