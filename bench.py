@@ -395,6 +395,7 @@ def run_ours(args) -> None:
         line["poisson_256^2_dirichlet"] = dirichlet_block(torch, Poisson, Grid, cpu=not args.no_cpu)
         line["dambreak_3d"] = dambreak_block(torch, TwoPhase, Grid)
         line["learned_guess"] = learned_block(torch)
+        line["learned_guess_3d"] = learned3_block(torch)
     if rank == 0 and not args.no_cpu:
         rate, n = cpu_reference_rate(20, 2, budget_s=20.0, threads=os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
@@ -569,6 +570,85 @@ def learned_block(torch, n: int = 256, ntrain: int = 96, ntest: int = 12, steps:
                     "network runs before each solve and the multigrid iterates to 1e-10 either way"}
 
 
+def learned3_block(torch, n: int = 256, ntrain: int = 16, ntest: int = 3, steps: int = 400) -> dict:
+    """Learned initial guess in 3D (tensor-core U-Net, 3 levels, 16-64 channels, at half the
+    grid's resolution): pairs of consecutive steps of the n^3 spheres problem (density
+    1 + 999 H, smooth random divergent right-hand side) solved to 1e-10, Adam training on the
+    GPU, then time to 1e-10 on held-out pairs: FP64 multigrid and FP32-refined multigrid from
+    the previous pressure, and FP32-refined from the network's guess (inference included)."""
+    import time as _t
+    import numpy as np
+    from scihpc_gb300 import Grid, Poisson, UNet
+    from scihpc_gb300.learned import make_snapshots3, train
+    dev = torch.device("cuda")
+    t0 = _t.perf_counter()
+    tr = make_snapshots3(n, range(ntrain), torch, dev)
+    te = make_snapshots3(n, range(10 ** 6, 10 ** 6 + ntest), torch, dev)
+    torch.cuda.synchronize()
+    t_snap = _t.perf_counter() - t0
+    g = Grid(3, (n, n, n), (0.0,) * 3, (1.0,) * 3)
+    net = UNet(n, n, n, seed=0)
+
+    def test_loss():
+        return float(np.mean([net.loss_grad(g, *s) for s in te]))
+
+    loss_before = test_loss()
+    torch.cuda.synchronize()
+    t0 = _t.perf_counter()
+    losses = train(net, tr, steps, 1e-3, torch, cosine=True)
+    torch.cuda.synchronize()
+    t_train = _t.perf_counter() - t0
+    loss_after = test_loss()
+    # convolution work of one inference: 2 * 27 * ci * co per voxel of each layer's level
+    layers = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1), (32, 32, 1),
+              (48, 16, 0), (16, 16, 0), (16, 16, 0)]
+    vox = (n // 2) ** 3
+    flops = sum(2.0 * 27 * ci * co * vox / 8 ** lv for ci, co, lv in layers)
+    rho, rhs, pprev, _ = te[0]
+    guess = pprev.clone()
+    for _ in range(2):
+        net.infer(g, rho, rhs, pprev, guess)
+    torch.cuda.synchronize()
+    t0 = _t.perf_counter()
+    for _ in range(5):
+        net.infer(g, rho, rhs, pprev, guess)
+    torch.cuda.synchronize()
+    t_inf = (_t.perf_counter() - t0) / 5
+    out = {"grid": f"{n}^3", "network_grid": f"{n // 2}^3", "train_pairs": ntrain, "test_pairs": ntest,
+           "train_steps": steps, "snapshot_s": t_snap, "train_ms_per_step": 1e3 * t_train / steps,
+           "lr": "1e-3, half-cosine decay to 0", "test_loss_before": loss_before, "test_loss_after": loss_after,
+           "train_loss_first20": float(np.mean(losses[:20])), "train_loss_last20": float(np.mean(losses[-20:])),
+           "infer_ms": 1e3 * t_inf, "infer_conv_tflops": flops / t_inf / 1e12}
+    p = torch.zeros_like(pprev)
+    for name, fp32, use_net in (("fp64_from_pprev", False, False), ("fp32_refined_from_pprev", True, False),
+                                ("fp32_refined_from_net", True, True)):
+        ps = Poisson(g, bc=0, density=True, fp32=fp32)
+        times, its, rrs = [], [], []
+        for rho, rhs, pprev, _ in te:
+            ps.set_density(rho)
+            for timed in (False, True):   # the untimed solve warms up and captures the solve graph
+                p.copy_(pprev)
+                torch.cuda.synchronize()
+                t0 = _t.perf_counter()
+                if use_net:
+                    net.infer(g, rho, rhs, pprev, p)
+                it, rr = ps.solve(rhs, p, rel_tol=1e-10, max_iter=200, use_guess=True)
+                torch.cuda.synchronize()
+                if timed:
+                    times.append(_t.perf_counter() - t0)
+                    its.append(it)
+                    rrs.append(rr)
+        ps.close()
+        out[name] = {"ms_to_tol": 1e3 * float(np.mean(times)), "iterations": float(np.mean(its)),
+                     "max_relres": float(max(rrs))}
+    net.close()
+    out["fp32_learned_speedup_vs_fp64"] = out["fp64_from_pprev"]["ms_to_tol"] / out["fp32_refined_from_net"]["ms_to_tol"]
+    out["fp32_speedup_vs_fp64"] = out["fp64_from_pprev"]["ms_to_tol"] / out["fp32_refined_from_pprev"]["ms_to_tol"]
+    out["note"] = ("host-timed per solve (inference included for the network's guess); every solve iterates to "
+                   "1e-10, so the network can only change the iteration count")
+    return out
+
+
 def profile_poisson(precision: str) -> None:
     """One density update and three solver iterations of the 256^3 pressure equation: the
     small case the profiles of the pressure kernels are captured on."""
@@ -598,6 +678,8 @@ def main():
                     help="pressure V-cycles in FP32 inside FP64 refinement (default) or all FP64")
     ap.add_argument("--profile-unet", action="store_true",
                     help="only a few training steps of the 256^2 learned guess (profiling case)")
+    ap.add_argument("--profile-unet3", action="store_true",
+                    help="only a few training steps of the 3D learned guess on a 128^3 grid (profiling case)")
     ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
                     help="only three iterations of the 256^3 pressure solve (profiling case)")
     args = ap.parse_args()
@@ -610,6 +692,15 @@ def main():
         net = UNet(256, 256, seed=0)
         losses = train(net, snaps, 4, 1e-3, torch)
         print(json.dumps({"profile": "unet 256^2 training steps", "loss": losses}))
+    elif args.profile_unet3:
+        import torch
+        from scihpc_gb300 import UNet, lib
+        from scihpc_gb300.learned import make_snapshots3, train
+        lib()
+        snaps = make_snapshots3(128, range(2), torch, torch.device("cuda"))
+        net = UNet(128, 128, 128, seed=0)
+        losses = train(net, snaps, 3, 1e-3, torch)
+        print(json.dumps({"profile": "unet3 128^3 training steps", "loss": losses}))
     elif args.profile_poisson:
         profile_poisson(args.profile_poisson)
     elif args.impl == "reference":

@@ -263,6 +263,12 @@ int scihpc_conv3x3(const void *x, const void *w, const float *bias, float *out, 
                    void *stream);
 int scihpc_conv3x3_wgrad(const void *x, const void *dz, float *dw, float *partial, int splits, int h, int w_, int ci,
                          int co, void *stream);
+/* The same in 3D: x BF16 [d*h*w][ci], w BF16 [co][27][ci] (tap t = 9 (dz+1) + 3 (dy+1) +
+ * (dx+1)), out FP32 [d*h*w][co]; wgrad: dw[co][27][ci], partial: splits * 27 * ci * co floats. */
+int scihpc_conv3x3x3(const void *x, const void *w, const float *bias, float *out, int d, int h, int w_, int ci, int co,
+                     int relu, void *stream);
+int scihpc_conv3x3x3_wgrad(const void *x, const void *dz, float *dw, float *partial, int splits, int d, int h, int w_,
+                           int ci, int co, void *stream);
 
 /* ------------------------------------------------------------------ learned pressure guess
  * A 4-level 2D U-Net (16-32-64-128 channels) predicting the pressure of the variable-density
@@ -278,6 +284,12 @@ int scihpc_conv3x3_wgrad(const void *x, const void *dz, float *dw, float *partia
  * scihpc_unet_num_params entries. */
 typedef struct scihpc_unet scihpc_unet;
 int scihpc_unet_create(int h, int w, unsigned seed, scihpc_unet **out);
+/* The 3D network for an n0 x n1 x n2 pressure grid (each a multiple of 8): a 3-level U-Net
+ * (16-32-64 channels, 3x3x3 convolutions on the tensor cores) at half the grid's resolution
+ * (inputs averaged over 2 x 2 x 2 cells, the correction prolonged piecewise-constant).  The
+ * other scihpc_unet_* functions take the same arguments for either network; fields are FP64
+ * ghosted 3D arrays of the pressure grid. */
+int scihpc_unet_create3(int n0, int n1, int n2, unsigned seed, scihpc_unet **out);
 int scihpc_unet_destroy(scihpc_unet *u);
 int scihpc_unet_num_params(scihpc_unet *u, long long *n);
 int scihpc_unet_set_weights(scihpc_unet *u, const float *host, long long n);

@@ -6,4 +6,4 @@ Python callers (tests, benchmarks); it raises if the library is missing rather t
 back to any CPU path.
 """
 from .native import (BC, Grid, Lib, LibraryNotBuilt, Poisson, ScihpcError, TwoPhase, UNet, Workspace, conv3x3,  # noqa: F401
-                     conv3x3_wgrad, lib)
+                     conv3x3_wgrad, conv3x3x3, conv3x3x3_wgrad, lib)

@@ -564,9 +564,64 @@ int scihpc_conv3x3_wgrad(const void *x, const void *dz, float *dw, float *partia
     return SCIHPC_OK;
 }
 
+// the 3x3x3 convolution and its weight gradient (same conventions, 27 taps, d x h x w voxels)
+int scihpc_conv3x3x3(const void *x, const void *w, const float *bias, float *out, int d, int h, int w_, int ci, int co,
+                     int relu, void *stream) {
+    REQUIRE(x && w && out && d > 0 && h > 0 && w_ > 0, "conv3x3x3: bad argument");
+    REQUIRE(ci % 16 == 0 && co % 16 == 0 && co >= 16 && co <= 256, "conv3x3x3: channels must be multiples of 16, co <= 256");
+    static int *err = nullptr;
+    if (!err) {
+        SCIHPC_CUDA(cudaMalloc(&err, sizeof(int)));
+        SCIHPC_CUDA(cudaMemset(err, 0, sizeof(int)));
+        int rc = conv3x3_init(256);
+        if (rc) return rc;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc = conv3x3x3_forward(static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(w), bias, out,
+                               false, d, h, w_, ci, co, relu != 0, err, s);
+    if (rc) return rc;
+    CHECK_LAUNCH();
+    int herr = 0;
+    SCIHPC_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SCIHPC_CUDA(cudaStreamSynchronize(s));
+    if (herr) {
+        set_last_error("conv3x3x3: a tensor-core barrier wait timed out");
+        return SCIHPC_ERR_CUDA;
+    }
+    return SCIHPC_OK;
+}
+
+int scihpc_conv3x3x3_wgrad(const void *x, const void *dz, float *dw, float *partial, int splits, int d, int h, int w_,
+                           int ci, int co, void *stream) {
+    REQUIRE(x && dz && dw && partial && splits > 0 && d > 0 && h > 0 && w_ > 0, "conv3x3x3_wgrad: bad argument");
+    REQUIRE(ci % 16 == 0 && co % 16 == 0 && co >= 16 && co <= 256, "conv3x3x3_wgrad: channels must be multiples of 16");
+    static int *err = nullptr;
+    if (!err) {
+        SCIHPC_CUDA(cudaMalloc(&err, sizeof(int)));
+        SCIHPC_CUDA(cudaMemset(err, 0, sizeof(int)));
+        int rc = conv3x3_init(256);
+        if (rc) return rc;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc = conv3x3x3_wgrad(static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(dz), partial, dw,
+                             d, h, w_, ci, co, splits, err, s);
+    if (rc) return rc;
+    CHECK_LAUNCH();
+    int herr = 0;
+    SCIHPC_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SCIHPC_CUDA(cudaStreamSynchronize(s));
+    if (herr) {
+        set_last_error("conv3x3x3_wgrad: a tensor-core barrier wait timed out");
+        return SCIHPC_ERR_CUDA;
+    }
+    return SCIHPC_OK;
+}
+
 // ------------------------------------------------------------------ learned pressure guess
+// one handle for both networks: the 2D UNet, or the 3D UNet3 when net3 is set
 struct scihpc_unet {
     UNet net;
+    UNet3 *net3 = nullptr;
 };
 
 int scihpc_unet_create(int h, int w, unsigned seed, scihpc_unet **out) {
@@ -583,9 +638,34 @@ int scihpc_unet_create(int h, int w, unsigned seed, scihpc_unet **out) {
     return SCIHPC_OK;
 }
 
+int scihpc_unet_create3(int n0, int n1, int n2, unsigned seed, scihpc_unet **out) {
+    REQUIRE(out, "unet_create3: out is NULL");
+    auto *u = new (std::nothrow) scihpc_unet;
+    if (!u) return SCIHPC_ERR_NOMEM;
+    u->net3 = new (std::nothrow) UNet3;
+    if (!u->net3) {
+        delete u;
+        return SCIHPC_ERR_NOMEM;
+    }
+    int rc = u->net3->create(n0, n1, n2, seed);
+    if (rc) {
+        u->net3->destroy();
+        delete u->net3;
+        delete u;
+        return rc;
+    }
+    *out = u;
+    return SCIHPC_OK;
+}
+
 int scihpc_unet_destroy(scihpc_unet *u) {
     if (u) {
-        u->net.destroy();
+        if (u->net3) {
+            u->net3->destroy();
+            delete u->net3;
+        } else {
+            u->net.destroy();
+        }
         delete u;
     }
     return SCIHPC_OK;
@@ -593,46 +673,50 @@ int scihpc_unet_destroy(scihpc_unet *u) {
 
 int scihpc_unet_num_params(scihpc_unet *u, long long *n) {
     REQUIRE(u && n, "unet_num_params: NULL argument");
-    *n = u->net.num_params();
+    *n = u->net3 ? u->net3->num_params() : u->net.num_params();
     return SCIHPC_OK;
 }
 
 int scihpc_unet_set_weights(scihpc_unet *u, const float *host, long long n) {
     REQUIRE(u && host, "unet_set_weights: NULL argument");
-    return u->net.set_weights(host, n);
+    return u->net3 ? u->net3->set_weights(host, n) : u->net.set_weights(host, n);
 }
 
 int scihpc_unet_get_weights(scihpc_unet *u, float *host, long long n) {
     REQUIRE(u && host, "unet_get_weights: NULL argument");
-    return u->net.get(host, n, false);
+    return u->net3 ? u->net3->get(host, n, false) : u->net.get(host, n, false);
 }
 
 int scihpc_unet_get_gradient(scihpc_unet *u, float *host, long long n) {
     REQUIRE(u && host, "unet_get_gradient: NULL argument");
-    return u->net.get(host, n, true);
+    return u->net3 ? u->net3->get(host, n, true) : u->net.get(host, n, true);
 }
 
 int scihpc_unet_infer(scihpc_unet *u, const scihpc_grid *grid, const double *rho, const double *rhs,
                       const double *pprev, double *guess) {
     REQUIRE(u && grid && rho && rhs && guess, "unet_infer: NULL argument");
-    return u->net.infer(make_dims(grid), rho, rhs, pprev, guess);
+    const Dims D = make_dims(grid);
+    return u->net3 ? u->net3->infer(D, rho, rhs, pprev, guess) : u->net.infer(D, rho, rhs, pprev, guess);
 }
 
 int scihpc_unet_loss_grad(scihpc_unet *u, const scihpc_grid *grid, const double *rho, const double *rhs,
                           const double *pprev, const double *p, double *loss) {
     REQUIRE(u && grid && rho && rhs && p && loss, "unet_loss_grad: NULL argument");
-    return u->net.loss_grad(make_dims(grid), rho, rhs, pprev, p, loss);
+    const Dims D = make_dims(grid);
+    return u->net3 ? u->net3->loss_grad(D, rho, rhs, pprev, p, loss) : u->net.loss_grad(D, rho, rhs, pprev, p, loss);
 }
 
 int scihpc_unet_train_step(scihpc_unet *u, const scihpc_grid *grid, const double *rho, const double *rhs,
                            const double *pprev, const double *p, float lr, double *loss) {
     REQUIRE(u && grid && rho && rhs && p && loss && lr > 0.0f, "unet_train_step: bad argument");
-    return u->net.train_step(make_dims(grid), rho, rhs, pprev, p, lr, loss);
+    const Dims D = make_dims(grid);
+    return u->net3 ? u->net3->train_step(D, rho, rhs, pprev, p, lr, loss)
+                   : u->net.train_step(D, rho, rhs, pprev, p, lr, loss);
 }
 
 int scihpc_unet_stream(scihpc_unet *u, void **stream) {
     REQUIRE(u && stream, "unet_stream: NULL argument");
-    *stream = u->net.stream;
+    *stream = u->net3 ? u->net3->stream : u->net.stream;
     return SCIHPC_OK;
 }
 

@@ -2,12 +2,14 @@
 solver, training of the tensor-core U-Net (scihpc_unet_*), and the comparison of solver
 iterations with and without the guess.
 
-The workload is the Rayleigh-Taylor-type variable-density Poisson equation (density
+The 2D workload is the Rayleigh-Taylor-type variable-density Poisson equation (density
 1 + 2 H(phi), interface y = 0.5 + sum of 8 seeded sinusoids of amplitude <= 0.02, Neumann walls,
 zero-mean right-hand side).  Consecutive time steps are imitated by pairs of problems whose
 interface phases and right-hand-side modes differ slightly: the solution of the first is the
 "previous pressure" of the second, as in a time loop.  The multigrid solve always iterates to
-the same relative residual; the network only changes where it starts.
+the same relative residual; the network only changes where it starts.  The 3D workload
+(sphere_problem) is the spheres problem of the 256^3 pressure benchmark with a smooth
+right-hand side, in the same pairs of consecutive steps.
 """
 from __future__ import annotations
 
@@ -17,7 +19,15 @@ import numpy as np
 
 from .native import Grid, Poisson, UNet
 
-__all__ = ["rt_problem", "make_snapshots", "train", "solve_iterations"]
+__all__ = ["rt_problem", "make_snapshots", "sphere_problem", "make_snapshots3", "train", "solve_iterations"]
+
+
+def _grid_of(rho):
+    """The unit-square (2D) or unit-cube (3D) grid of a ghosted field."""
+    n0, n1, n2 = rho.shape[0] - 6, rho.shape[1] - 6, rho.shape[2]
+    if n2 == 1:
+        return Grid(2, (n0, n1), (0.0, 0.0), (1.0, 1.0))
+    return Grid(3, (n0, n1, n2 - 6), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
 
 
 def rt_problem(n: int, seed: int, drift: float, torch, device):
@@ -73,11 +83,74 @@ def make_snapshots(n: int, seeds, torch, device, rel_tol: float = 1e-10, fp32: b
     return out
 
 
+def sphere_problem(n: int, seed: int, drift: float, torch, device):
+    """Density and right-hand side (ghosted FP64 fields on an n^3 grid of [0,1]^3) of 3D sample
+    `seed` advanced by `drift` (0 = the previous step, 1 = the current one): density
+    1 + 999 H(phi) with phi the union of 1-12 seeded spheres (radius 0.05-0.2) that move by up
+    to one cell per step, and a zero-mean right-hand side -- the divergence of a smooth random
+    velocity with no flux through the walls -- made of six Neumann cosine modes that change
+    slightly from step to step."""
+    rng = np.random.default_rng(seed)
+    ns = 1 + seed % 12
+    r = rng.uniform(0.05, 0.2, ns)
+    cen = [rng.uniform(r[k], 1 - r[k], 3) for k in range(ns)]
+    move = [rng.standard_normal(3) for _ in range(ns)]
+    ks = rng.integers(1, 5, (6, 3))
+    amp = rng.standard_normal(6)
+    h = 1.0 / n
+    c = (torch.arange(n, dtype=torch.float64, device=device) + 0.5) * h
+    X, Y, Z = torch.meshgrid(c, c, c, indexing="ij")
+    phi = torch.full((n, n, n), -1e9, dtype=torch.float64, device=device)
+    for k in range(ns):
+        m = move[k] / np.linalg.norm(move[k]) * h * drift
+        cx, cy, cz = (float(cen[k][a] + m[a]) for a in range(3))
+        phi = torch.maximum(phi, float(r[k]) - torch.sqrt((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2))
+    w = 1.5 * h
+    H = torch.where(phi < -w, torch.zeros_like(phi), torch.where(phi > w, torch.ones_like(phi),
+                    0.5 * (1 + phi / w + torch.sin(math.pi * phi / w) / math.pi)))
+    del phi
+    rho = torch.ones((n + 6, n + 6, n + 6), dtype=torch.float64, device=device)
+    rho[3:-3, 3:-3, 3:-3] = 1.0 + 999.0 * H
+    del H
+    rho[:3], rho[-3:] = rho[3:4].clone(), rho[-4:-3].clone()
+    rho[:, :3], rho[:, -3:] = rho[:, 3:4].clone(), rho[:, -4:-3].clone()
+    rho[:, :, :3], rho[:, :, -3:] = rho[:, :, 3:4].clone(), rho[:, :, -4:-3].clone()
+    f = torch.zeros_like(X)
+    for j in range(6):
+        f += float(amp[j]) * (1 + 0.02 * drift) * torch.cos(math.pi * float(ks[j, 0]) * X + 0.03 * drift * j) * \
+             torch.cos(math.pi * float(ks[j, 1]) * Y) * torch.cos(math.pi * float(ks[j, 2]) * Z)
+    del X, Y, Z
+    rhs = torch.zeros_like(rho)
+    rhs[3:-3, 3:-3, 3:-3] = f - f.mean()
+    return rho, rhs
+
+
+def make_snapshots3(n: int, seeds, torch, device, rel_tol: float = 1e-10, fp32: bool = True):
+    """[(rho, rhs, pprev, p)] of sphere_problem for the given seeds: pprev solves the drift-0
+    problem, p the drift-1 problem (both to rel_tol)."""
+    g = Grid(3, (n, n, n), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    ps = Poisson(g, bc=0, density=True, fp32=fp32)
+    out = []
+    for s in seeds:
+        rho0, rhs0 = sphere_problem(n, s, 0.0, torch, device)
+        p0 = torch.zeros_like(rho0)
+        ps.set_density(rho0)
+        ps.solve(rhs0, p0, rel_tol=rel_tol, max_iter=200)
+        del rho0, rhs0
+        rho1, rhs1 = sphere_problem(n, s, 1.0, torch, device)
+        p1 = p0.clone()
+        ps.set_density(rho1)
+        ps.solve(rhs1, p1, rel_tol=rel_tol, max_iter=200, use_guess=True)
+        torch.cuda.synchronize()
+        out.append((rho1, rhs1, p0, p1))
+    ps.close()
+    return out
+
+
 def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0, cosine: bool = False):
     """Adam steps over the snapshots in a seeded random order; returns the loss history.
     cosine: the learning rate decays from lr to 0 along a half cosine over the steps."""
-    n = snaps[0][0].shape[0] - 6
-    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    g = _grid_of(snaps[0][0])
     rng = np.random.default_rng(seed)
     losses = []
     torch.cuda.synchronize()
@@ -91,8 +164,7 @@ def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0, cosine:
 def solve_iterations(snaps, torch, net: UNet | None = None, rel_tol: float = 1e-10, fp32: bool = True):
     """Solver iterations (V-cycles) and final residuals for each snapshot, starting from the
     previous pressure (net None) or from the network's guess."""
-    n = snaps[0][0].shape[0] - 6
-    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    g = _grid_of(snaps[0][0])
     its, res = [], []
     for rho, rhs, pprev, _ in snaps:
         ps = Poisson(g, bc=0, density=True, fp32=fp32)

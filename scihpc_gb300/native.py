@@ -120,6 +120,9 @@ _SIGS = {
     "scihpc_conv3x3_wgrad": ([_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                               ctypes.c_int, _vp], ctypes.c_int),
     "scihpc_unet_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)], ctypes.c_int),
+    "scihpc_unet_create3": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)], ctypes.c_int),
+    "scihpc_conv3x3x3": ([_vp, _vp, _vp, _vp] + [ctypes.c_int] * 6 + [_vp], ctypes.c_int),
+    "scihpc_conv3x3x3_wgrad": ([_vp, _vp, _vp, _vp] + [ctypes.c_int] * 6 + [_vp], ctypes.c_int),
     "scihpc_unet_destroy": ([_vp], ctypes.c_int),
     "scihpc_unet_num_params": ([_vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "scihpc_unet_set_weights": ([_vp, _vp, ctypes.c_longlong], ctypes.c_int),
@@ -440,13 +443,29 @@ def conv3x3_wgrad(x, dz, dw, partial, splits: int, h: int, wd: int, ci: int, co:
     lib().check(lib().scihpc_conv3x3_wgrad(_ptr(x), _ptr(dz), _ptr(dw), _ptr(partial), splits, h, wd, ci, co, None))
 
 
-class UNet:
-    """scihpc_unet: the learned initial guess of the pressure solve (tensor-core U-Net)."""
+def conv3x3x3(x, w, bias, out, d: int, h: int, wd: int, ci: int, co: int, relu: bool = False):
+    """scihpc_conv3x3x3 on device tensors: x BF16 [d*h*w][ci], w BF16 [co][27][ci], out FP32."""
+    lib().check(lib().scihpc_conv3x3x3(_ptr(x), _ptr(w), _ptr(bias), _ptr(out), d, h, wd, ci, co, int(relu), None))
 
-    def __init__(self, h: int, w: int, seed: int = 0):
+
+def conv3x3x3_wgrad(x, dz, dw, partial, splits: int, d: int, h: int, wd: int, ci: int, co: int):
+    """scihpc_conv3x3x3_wgrad on device tensors: dw FP32 [co][27][ci]."""
+    lib().check(lib().scihpc_conv3x3x3_wgrad(_ptr(x), _ptr(dz), _ptr(dw), _ptr(partial), splits, d, h, wd, ci, co,
+                                             None))
+
+
+class UNet:
+    """scihpc_unet: the learned initial guess of the pressure solve (tensor-core U-Net).
+    UNet(h, w) is the 2D network of an h x w grid; UNet(n0, n1, n2) the 3D network of an
+    n0 x n1 x n2 grid (run at half resolution)."""
+
+    def __init__(self, h: int, w: int, d: int | None = None, seed: int = 0):
         self.L = lib()
         self.h = _vp()
-        self.L.check(self.L.scihpc_unet_create(h, w, seed, ctypes.byref(self.h)))
+        if d is None:
+            self.L.check(self.L.scihpc_unet_create(h, w, seed, ctypes.byref(self.h)))
+        else:
+            self.L.check(self.L.scihpc_unet_create3(h, w, d, seed, ctypes.byref(self.h)))
         n = ctypes.c_longlong(0)
         self.L.check(self.L.scihpc_unet_num_params(self.h, ctypes.byref(n)))
         self.nparam = n.value

@@ -147,3 +147,143 @@ def test_learned_guess_trains_and_keeps_the_solve_exact():
     its, res = solve_iterations(te, torch, net)
     assert max(res) <= 1e-10, res
     assert max(its) <= max(base) + 2, (its, base)
+
+
+# ------------------------------------------------------------------ 3D network (27 taps)
+CONV3_CASES = [(4, 6, 8, 16, 16), (5, 5, 5, 32, 64), (3, 7, 4, 48, 16), (6, 4, 4, 96, 32)]
+
+
+@pytest.mark.parametrize("d,h,w,ci,co", CONV3_CASES)
+def test_conv3_forward(d, h, w, ci, co):
+    from oracle import unet3_ref as R3
+    from scihpc_gb300 import conv3x3x3
+    rng = np.random.default_rng(d * 100 + co)
+    x = R.bf16(rng.standard_normal((d * h * w, ci)))
+    wt = R.bf16(rng.standard_normal((co, 27, ci)) * 0.1)
+    b = rng.standard_normal(co).astype(np.float32)
+    out = torch.zeros((d * h * w, co), dtype=torch.float32, device="cuda")
+    for relu in (False, True):
+        conv3x3x3(bf16_tensor(x), bf16_tensor(wt), torch.from_numpy(b).cuda(), out, d, h, w, ci, co, relu)
+        ref = R3.conv(x, wt, b.astype(np.float64), (d, h, w), relu)
+        assert rel(out.cpu().numpy(), ref) <= FP32_SUM, (relu, rel(out.cpu().numpy(), ref))
+
+
+@pytest.mark.parametrize("d,h,w,ci,co", CONV3_CASES)
+def test_conv3_data_gradient(d, h, w, ci, co):
+    """Data gradient = the forward kernel on [ci][26 - t][co] weights."""
+    from oracle import unet3_ref as R3
+    from scihpc_gb300 import conv3x3x3
+    rng = np.random.default_rng(5 + d + co)
+    dz = R.bf16(rng.standard_normal((d * h * w, co)))
+    wt = R.bf16(rng.standard_normal((co, 27, ci)) * 0.1)
+    wflip = np.ascontiguousarray(wt[:, ::-1, :].transpose(2, 1, 0))
+    out = torch.zeros((d * h * w, ci), dtype=torch.float32, device="cuda")
+    conv3x3x3(bf16_tensor(dz), bf16_tensor(wflip), None, out, d, h, w, co, ci, False)
+    ref = R3.conv_dgrad(dz, wt, (d, h, w))
+    assert rel(out.cpu().numpy(), ref) <= FP32_SUM
+
+
+@pytest.mark.parametrize("d,h,w,ci,co", CONV3_CASES)
+@pytest.mark.parametrize("splits", [1, 5])
+def test_conv3_weight_gradient(d, h, w, ci, co, splits):
+    from oracle import unet3_ref as R3
+    from scihpc_gb300 import conv3x3x3_wgrad
+    rng = np.random.default_rng(13 + w + ci)
+    x = R.bf16(rng.standard_normal((d * h * w, ci)))
+    dz = R.bf16(rng.standard_normal((d * h * w, co)))
+    dw = torch.zeros((co, 27, ci), dtype=torch.float32, device="cuda")
+    part = torch.zeros(splits * 27 * ci * co, dtype=torch.float32, device="cuda")
+    conv3x3x3_wgrad(bf16_tensor(x), bf16_tensor(dz), dw, part, splits, d, h, w, ci, co)
+    ref = R3.conv_wgrad(x, dz, (d, h, w))
+    assert rel(dw.cpu().numpy(), ref) <= FP32_SUM
+
+
+def _fields3(n, rng):
+    """Ghosted 3D fields on an n^3 grid: density with a jump, rhs, previous and new pressure."""
+    N = n + 6
+    c = (np.arange(n) + 0.5) / n
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    rho = np.ones((N, N, N))
+    rho[3:-3, 3:-3, 3:-3] = np.where((X - 0.5) ** 2 + (Y - 0.4) ** 2 + (Z - 0.6) ** 2 < 0.09, 1000.0, 1.0)
+    rhs = np.zeros((N, N, N))
+    rhs[3:-3, 3:-3, 3:-3] = rng.standard_normal((n, n, n))
+    pprev = np.zeros((N, N, N))
+    pprev[3:-3, 3:-3, 3:-3] = np.cos(np.pi * X) * np.cos(np.pi * Y) + 0.1 * rng.standard_normal((n, n, n))
+    pnew = pprev.copy()
+    pnew[3:-3, 3:-3, 3:-3] += 0.05 * np.sin(np.pi * Z) * rng.standard_normal((n, n, n))
+    return rho, rhs, pprev, pnew
+
+
+def test_unet3_loss_and_gradient_match_oracle():
+    from oracle import unet3_ref as R3
+    from scihpc_gb300 import Grid, UNet
+    n = 16
+    rng = np.random.default_rng(3)
+    rho, rhs, pprev, pnew = _fields3(n, rng)
+    net = UNet(n, n, n, seed=0)
+    params = R3.init_params(5)
+    params[-16:] = rng.standard_normal(16).astype(np.float32) * 0.1
+    net.set_weights(params)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    torch.cuda.synchronize()
+    g = Grid(3, (n, n, n), (0.0,) * 3, (1.0,) * 3)
+    loss = net.loss_grad(g, d(rho), d(rhs), d(pprev), d(pnew))
+    grad = net.gradient()
+    I = (slice(3, -3),) * 3
+    x0, target, _, g0 = R3.pack(rho[I], rhs[I], pprev[I], pnew[I])
+    ref_loss, ref_grad, _ = R3.loss_and_gradient(params.astype(np.float64), x0, target, g0)
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss, (loss, ref_loss)
+    lay, _ = R3.param_layout()
+    for k, (wo, bo) in enumerate(lay):
+        co = R3.LAYERS[k][3]
+        ew = rel(grad[wo:bo], ref_grad[wo:bo])
+        eb = rel(grad[bo:bo + co], ref_grad[bo:bo + co])
+        assert ew <= 3e-2 and eb <= 3e-2, (k, ew, eb)
+    net.close()
+
+
+def test_unet3_guess_matches_oracle_and_zero_correction_is_previous_pressure():
+    from oracle import unet3_ref as R3
+    from scihpc_gb300 import Grid, UNet
+    n = 16
+    rho, rhs, pprev, _ = _fields3(n, np.random.default_rng(1))
+    net = UNet(n, n, n, seed=2)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    g = Grid(3, (n, n, n), (0.0,) * 3, (1.0,) * 3)
+    guess = torch.zeros(rho.shape, dtype=torch.float64, device="cuda")
+    params = net.weights()
+    params[-16:] = 0.2   # a visible correction
+    net.set_weights(params)
+    torch.cuda.synchronize()
+    net.infer(g, d(rho), d(rhs), d(pprev), guess)
+    I = (slice(3, -3),) * 3
+    x0, _, sp, g0 = R3.pack(rho[I], rhs[I], pprev[I])
+    a = R3.forward(params.astype(np.float64), x0, g0)
+    ref = R3.unpack(a["OUT"][:, 0], pprev[I], sp)
+    out = guess.cpu().numpy()
+    assert rel(out[I] - pprev[I], ref - pprev[I]) <= 1e-2
+    lay, _ = R3.param_layout()
+    params[lay[-1][0]:] = 0.0
+    net.set_weights(params)
+    net.infer(g, d(rho), d(rhs), d(pprev), guess)
+    assert np.array_equal(guess.cpu().numpy(), pprev)
+    net.close()
+
+
+def test_learned_guess3_trains_and_keeps_the_solve_exact():
+    """3D: training on solver snapshots lowers the loss, and a solve started from the
+    network's guess still reaches the same tolerance."""
+    from scihpc_gb300 import UNet
+    from scihpc_gb300.learned import make_snapshots3, solve_iterations, train
+    dev = torch.device("cuda")
+    tr = make_snapshots3(32, range(12), torch, dev)
+    te = make_snapshots3(32, range(1000, 1003), torch, dev)
+    net = UNet(32, 32, 32, seed=0)
+    losses = train(net, tr, 200, 1e-3, torch)
+    # a clear decrease (about 0.55x over 200 steps on 12 snapshots)
+    assert np.mean(losses[-20:]) < 0.7 * np.mean(losses[:20]), (np.mean(losses[:20]), np.mean(losses[-20:]))
+    base, _ = solve_iterations(te, torch)
+    its, res = solve_iterations(te, torch, net)
+    assert max(res) <= 1e-10, res
+    assert max(its) <= max(base) + 2, (its, base)
+    net.close()
