@@ -174,6 +174,128 @@ __global__ void __launch_bounds__(THREADS) k_conv(const __nv_bfloat16 *__restric
     if (warp == 0) tc::tmem_free(tmem, ncols);
 }
 
+// ------------------------------------------------------------------ forward, halo-tile form
+// A block computes a 1 x HT_Y x HT_X tile of output pixels (z, y, x) = 128 rows of the GEMM.
+// For each 16-channel chunk of the input it copies the tile's halo (HZ x (HT_Y + 2) x
+// (HT_X + 2) pixels) once into shared memory, laid out [z][y][K half][x] x 16 bytes, so that
+// the 8 pixels of a tile row are one 8 x 16-byte core matrix.  The A operand of tap
+// (dz, dy, dx) is then the halo seen through a shared-memory descriptor that starts at the
+// shifted row and column (core matrices 16 bytes apart along x, 160 bytes along K, one halo
+// row along M): the taps' MMAs read the same halo and no per-tap copy is made.  The weights of
+// all taps of the chunk are staged beside it.  Chunks are double-buffered.
+constexpr int HT_X = 8, HT_Y = 16;                 // 8 x 16 = TILE_M pixels
+constexpr int HX = HT_X + 2, HY = HT_Y + 2;        // halo extents in x and y
+constexpr int HROW = 2 * HX * 16;                  // bytes of one halo row: two K halves of HX pixels
+constexpr size_t HALO_SMEM_MAX = 200 * 1024;       // largest two-stage halo launch
+static_assert(HT_X * HT_Y == TILE_M, "tile");
+
+__host__ __device__ inline int halo_bytes(bool three) { return (three ? 3 : 1) * HY * HROW; }
+__host__ __device__ inline int halo_stage_bytes(bool three, int n) { return halo_bytes(three) + (three ? 27 : 9) * n * 32; }
+
+template <bool OUT_BF16, bool THREE>
+__global__ void __launch_bounds__(THREADS) k_conv_halo(const __nv_bfloat16 *__restrict__ X,
+                                                       const __nv_bfloat16 *__restrict__ Wk,
+                                                       const float *__restrict__ bias, void *__restrict__ out, int D,
+                                                       int H, int W, int Ci, int N, int relu, int *err) {
+    constexpr int TAPS = THREE ? 27 : 9, HZ = THREE ? 3 : 1;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int abytes = halo_bytes(THREE), per = halo_stage_bytes(THREE, N);
+    const int tiles_x = (W + HT_X - 1) / HT_X, tiles_y = (H + HT_Y - 1) / HT_Y;
+    const int tx = blockIdx.x % tiles_x, ty = (blockIdx.x / tiles_x) % tiles_y, z0 = blockIdx.x / (tiles_x * tiles_y);
+    const int x0 = tx * HT_X, y0 = ty * HT_Y;
+    const uint32_t ncols = tmem_cols(N);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = tc::idesc_bf16(TILE_M, N);
+    const int nch = Ci / 16;
+    bool ok = true;
+    for (int g = 0; g < nch; ++g) {
+        const int s = g & 1;
+        const bool freed = g < 2 || tc::mbar_wait(&mbar[s], uint32_t(((g >> 1) - 1) & 1));
+        if (!__syncthreads_and(freed)) {
+            ok = false;
+            break;
+        }
+        unsigned char *a = sm + size_t(s) * per, *bt = a + abytes;
+        // halo of channels g*16 .. g*16+15: entry e = ((z * HY + y) * HX + x) * 2 + kb
+        for (int e = tid; e < HZ * HY * HX * 2; e += THREADS) {
+            const int kb = e & 1, v = e >> 1;
+            const int x = v % HX, t2 = v / HX, y = t2 % HY, z = t2 / HY;
+            const int gz = THREE ? z0 + z - 1 : z0, gy = y0 + y - 1, gx = x0 + x - 1;
+            const bool in = gz >= 0 && gz < D && gy >= 0 && gy < H && gx >= 0 && gx < W;
+            const __nv_bfloat16 *src = in ? X + (((long long)gz * H + gy) * W + gx) * Ci + g * 16 + kb * 8 : X;
+            tc::cp16(a + (z * HY + y) * HROW + kb * (HX * 16) + x * 16, src, in ? 16u : 0u);
+        }
+        // weights of every tap of the chunk: tap t at t * N * 32, rows n, K halves kb
+        for (int q = tid; q < TAPS * N * 2; q += THREADS) {
+            const int t = q / (2 * N), r = q - t * 2 * N, n = r >> 1, kb = r & 1;
+            tc::cp16(bt + t * N * 32 + chunk_off(n, kb), Wk + ((long long)n * TAPS + t) * Ci + g * 16 + kb * 8, 16u);
+        }
+        tc::cp_commit();
+        tc::cp_wait_all();
+        tc::fence_async_smem();
+        tc::fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after();
+            for (int t = 0; t < TAPS; ++t) {
+                int dz, dy, dx;
+                tap_shift(t, THREE, dz, dy, dx);
+                const int row = THREE ? (1 + dz) * HY + (1 + dy) : 1 + dy;
+                const uint64_t ad = tc::sdesc(tc::smem_u32(a + row * HROW + (1 + dx) * 16), HX * 16, HROW);
+                const uint64_t bd = tc::sdesc(tc::smem_u32(bt + t * N * 32), 128, 256);
+                tc::mma_bf16(tmem, ad, bd, idesc, (g > 0 || t > 0) ? 1u : 0u);
+            }
+            tc::commit(&mbar[s]);
+        }
+    }
+    if (ok) ok = __syncthreads_and(tc::mbar_wait(&mbar[(nch - 1) & 1], uint32_t(((nch - 1) >> 1) & 1)));
+    if (!ok) {
+        if (lane == 0) atomicExch(err, 1);
+    } else {
+        tc::fence_after();
+        const int m = warp * 32 + lane;   // this thread's row of D: tile pixel (m / HT_X, m % HT_X)
+        const int gy = y0 + m / HT_X, gx = x0 + m % HT_X;
+        const bool inside = gy < H && gx < W;
+        const long long pr = ((long long)z0 * H + gy) * W + gx;
+        for (int c = 0; c < N; c += 8) {
+            float v[8];
+            tc::tmem_ld8(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+            if (inside) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    if (bias) v[q] += bias[c + q];
+                    if (relu) v[q] = fmaxf(v[q], 0.0f);
+                }
+                if (OUT_BF16) {
+                    __nv_bfloat162 h[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+                    *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + pr * N + c) =
+                        *reinterpret_cast<uint4 *>(h);
+                } else {
+                    float4 *o = reinterpret_cast<float4 *>(static_cast<float *>(out) + pr * N + c);
+                    o[0] = make_float4(v[0], v[1], v[2], v[3]);
+                    o[1] = make_float4(v[4], v[5], v[6], v[7]);
+                }
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
 // ------------------------------------------------------------------ weight gradient
 // partial[split][r][co] = sum over the split's pixels of X[p + off(t_r)][ci_r] * dZ[p][co],
 // r = t * Ci + ci over the rows of this block's M tile
@@ -303,6 +425,22 @@ __global__ void k_wgrad_reduce(const float *__restrict__ partial, float *__restr
 int forward_impl(const __nv_bfloat16 *X, const __nv_bfloat16 *Wk, const float *bias, void *out, bool out_bf16, int D,
                  int H, int W, int Ci, int N, bool relu, int *err, cudaStream_t s) {
     if (Ci % 16 || N % 16 || N < 16 || N > 256 || D < 1 || H < 1 || W < 1) return SCIHPC_ERR_ARG;
+    const bool three = D > 1;
+    const int stages = Ci / 16 >= 2 ? 2 : 1;
+    const size_t hsm = size_t(stages) * halo_stage_bytes(three, N);
+    if (hsm <= HALO_SMEM_MAX) {
+        const unsigned tiles = unsigned((W + HT_X - 1) / HT_X) * unsigned((H + HT_Y - 1) / HT_Y) * unsigned(D);
+        const int rl = relu ? 1 : 0;
+        if (three) {
+            if (out_bf16) k_conv_halo<true, true><<<tiles, THREADS, hsm, s>>>(X, Wk, bias, out, D, H, W, Ci, N, rl, err);
+            else k_conv_halo<false, true><<<tiles, THREADS, hsm, s>>>(X, Wk, bias, out, D, H, W, Ci, N, rl, err);
+        } else {
+            if (out_bf16) k_conv_halo<true, false><<<tiles, THREADS, hsm, s>>>(X, Wk, bias, out, D, H, W, Ci, N, rl, err);
+            else k_conv_halo<false, false><<<tiles, THREADS, hsm, s>>>(X, Wk, bias, out, D, H, W, Ci, N, rl, err);
+        }
+        return SCIHPC_OK;
+    }
+    // the halo and all taps' weights do not fit: one tap per K-step
     const long long P = (long long)D * H * W;
     const unsigned blocks = unsigned((P + TILE_M - 1) / TILE_M);
     const int sk = steps_per_stage(N, (D > 1 ? 27 : 9) * (Ci / 16));
@@ -356,6 +494,11 @@ int conv3x3x3_wgrad(const __nv_bfloat16 *X, const __nv_bfloat16 *dZ, float *part
 }
 
 int conv3x3_init(int) {
+    const int hs = int(HALO_SMEM_MAX);
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv_halo<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, hs));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv_halo<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, hs));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv_halo<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, hs));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_conv_halo<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, hs));
     const int smem = 2 * CONV_STAGE_BYTES;
     SCIHPC_CUDA(cudaFuncSetAttribute(k_conv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_conv<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
