@@ -78,6 +78,17 @@ int scihpc_zero_order_extrapolation(scihpc_ctx *ctx, double *f, void *stream);
 int scihpc_uccd(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *f1, double *f2,
                 void *stream);
 
+/* Transport of a scalar by a velocity, one TVD-RK3 stage at a time (runge_kutta.cpp:13-63):
+ * scihpc_flux_fill writes flux = phi (kind 0, identity_flux, flux.cpp:7-20) or phi^2 / 2
+ * (kind 1, burgers_flux, flux.cpp:86-96) on every cell; after the caller's scihpc_uccd on
+ * each axis (first derivatives d[a], upwinded by vel[a]), scihpc_rk3_stage forms the
+ * right-hand side s = -sum_a vel[a] d[a] (rhs_kind 0, convection, source.cpp:8-40) or
+ * -sum_a d[a] (rhs_kind 1, Hamilton_Jacobi, source.cpp:75-107) on every cell and applies the
+ * stage: 1: phi += dt s (s -> s1); 2: phi += dt (s - 3 s1) / 4 (s -> s2); 3: phi += dt (-s1 - s2
+ * + 8 s) / 12; 0: euler's phi += dt s.  The caller then refills phi's ghosts (scihpc_bc_fill). */
+int scihpc_flux_fill(scihpc_ctx *ctx, int kind, const double *phi, double *flux, void *stream);
+int scihpc_rk3_stage(scihpc_ctx *ctx, int stage, int rhs_kind, double dt, double *phi, const double *const d[3],
+                     const double *const vel[3], double *s1, double *s2, void *stream);
 /* Central CCD first/second derivative along `axis`: ccd_solver::find_fx / find_fy /
  * find_fz (ccd_solver.cpp:14-141). */
 int scihpc_ccd(scihpc_ctx *ctx, int axis, const double *flux, double *f1, double *f2, void *stream);

@@ -123,6 +123,19 @@ class Checker:
         self.fn("uccd")(g.ndim, n, lo, hi, *[_p(a) for a in arrs], _p(out))
         return out
 
+    def transport_rk3(self, g: Grid, types, values, flux_kind: int, rhs_kind: int, dt: float, nsteps: int, phi, u,
+                      v, w, vel_from_phi: bool = False) -> np.ndarray:
+        """runge_kutta::tvd_rk3 for nsteps steps with (identity_flux, convection) (kinds 0, 0) or
+        (burgers_flux, Hamilton_Jacobi) (kinds 1, 1); returns the new phi."""
+        out = np.ascontiguousarray(phi, dtype=np.float64).copy()
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, w)]
+        t = (ctypes.c_int * 6)(*types)
+        vals = (ctypes.c_double * 6)(*values)
+        n, lo, hi = g.c_args()
+        self.fn("transport_rk3")(g.ndim, n, lo, hi, t, vals, flux_kind, rhs_kind, ctypes.c_double(dt), nsteps,
+                                 int(vel_from_phi), _p(out), *[_p(a) for a in arrs])
+        return out
+
     def ccd(self, g: Grid, flux, mixed: bool = True) -> np.ndarray:
         flux = np.ascontiguousarray(flux, dtype=np.float64)
         out = np.zeros((9,) + g.shape)

@@ -3,6 +3,7 @@
 // reference shim (oracle/ref_shim.cpp) so that tests can call either through ctypes.
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "mg.h"
 #include "port.h"
@@ -278,6 +279,45 @@ int port_tp_diagnostics(void *h, double *out) {
     out[0] = tp->mass();
     out[1] = tp->volume();
     out[2] = tp->divergence();
+    return 0;
+}
+
+// runge_kutta::tvd_rk3 (runge_kutta.cpp:13-49), nsteps steps, with the flux / right-hand side
+// pair (identity_flux, convection) (flux_kind 0, rhs_kind 0; flux.cpp:7-20, source.cpp:8-40) or
+// (burgers_flux, Hamilton_Jacobi) (flux_kind 1, rhs_kind 1; flux.cpp:86-96, source.cpp:75-107):
+// each stage fills the flux on every cell, takes the UCCD first derivatives of every active
+// axis upwinded by the velocity, forms s on every cell (x term, then minus the y and z terms),
+// updates phi by the stage formula and refills phi's ghosts.  vel_from_phi: u is a copy of phi
+// before every step (benchmarks_1d_IBE.cpp).
+int port_transport_rk3(int ndim, const int *n, const double *lo, const double *hi, const int *t, const double *v,
+                       int flux_kind, int rhs_kind, double dt, int nsteps, int vel_from_phi, double *phi,
+                       const double *u, const double *vv, const double *w) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const size_t N = g.size();
+    Compact c(g);
+    std::vector<double> flux(N), s1(N), s2(N), s3(N), uu(u, u + N);
+    std::vector<double> d1[3], d2[3];
+    for (int a = 0; a < 3; ++a) d1[a].assign(N, 0.0), d2[a].assign(N, 0.0);
+    const double *vel[3] = {uu.data(), vv, w};
+    auto rhs = [&](double *s) {
+        for (size_t i = 0; i < N; ++i) flux[i] = flux_kind ? phi[i] * phi[i] * 0.5 : phi[i];
+        for (int a = 0; a < ndim; ++a) c.uccd_axis(a, flux.data(), vel[a], d1[a].data(), d2[a].data());
+        for (size_t i = 0; i < N; ++i) s[i] = rhs_kind ? -d1[0][i] : -vel[0][i] * d1[0][i];
+        for (int a = 1; a < ndim; ++a)
+            for (size_t i = 0; i < N; ++i) s[i] -= rhs_kind ? d1[a][i] : vel[a][i] * d1[a][i];
+    };
+    for (int step = 0; step < nsteps; ++step) {
+        if (vel_from_phi) std::memcpy(uu.data(), phi, N * sizeof(double));
+        rhs(s1.data());
+        for (size_t i = 0; i < N; ++i) phi[i] += dt * s1[i];
+        bc_fill(g, LOC_NODE, t, v, phi);
+        rhs(s2.data());
+        for (size_t i = 0; i < N; ++i) phi[i] += dt * (s2[i] - 3.0 * s1[i]) / 4.0;
+        bc_fill(g, LOC_NODE, t, v, phi);
+        rhs(s3.data());
+        for (size_t i = 0; i < N; ++i) phi[i] += dt * (-s1[i] - s2[i] + 8.0 * s3[i]) / 12.0;
+        bc_fill(g, LOC_NODE, t, v, phi);
+    }
     return 0;
 }
 

@@ -593,4 +593,39 @@ int ref_tp_diagnostics(void *h, double *out) {
     return 0;
 }
 
+// runge_kutta::tvd_rk3 (runge_kutta.cpp:13-49), nsteps steps, with (identity_flux, convection)
+// (flux_kind 0, rhs_kind 0; flux.cpp:7-20, source.cpp:8-40) or (burgers_flux, Hamilton_Jacobi)
+// (flux_kind 1, rhs_kind 1; flux.cpp:86-96, source.cpp:75-107); t/v: the scalar's boundary
+// types and values; u/vv/w: the velocity (whole arrays).  vel_from_phi: the velocity's x
+// component is a copy of phi before every step, as benchmarks_1d_IBE.cpp does.
+int ref_transport_rk3(int ndim, const int *n, const double *lo, const double *hi, const int *t, const double *v,
+                      int flux_kind, int rhs_kind, double dt, int nsteps, int vel_from_phi, double *phi,
+                      const double *u, const double *vv, const double *w) {
+    typedef void (*rhs_fn)(wrapper *, wrapper *, DataType ***, flux_fn);
+    Dims d = dims_of(ndim, n);
+    structured_grid *geo = make_grid(ndim, n, lo, hi);
+    wrapper *f = make_wrapper(true, geo, ndim, t, v);
+    wrapper *vel = make_wrapper(false, geo, ndim, t, v);
+    auto *param = new problem_parameters{};
+    param->dt = dt;
+    f->link_params(param);
+    f->link_solvers(SharedSolvers_alloc(f->scalar, geo));
+    load(f->scalar->data, phi, d);
+    load(vel->vector->x.data, u, d);
+    load(vel->vector->y.data, vv, d);
+    load(vel->vector->z.data, w, d);
+    runge_kutta rk(d.Nx, d.Ny, d.Nz);
+    const flux_fn flux = flux_kind ? static_cast<flux_fn>(&burgers_flux) : IDENTITY;
+    const rhs_fn rhs = rhs_kind ? static_cast<rhs_fn>(&Hamilton_Jacobi) : static_cast<rhs_fn>(&convection);
+    for (int step = 0; step < nsteps; ++step) {
+        if (vel_from_phi)
+            for (int i = 0; i < d.Nx; ++i)
+                for (int j = 0; j < d.Ny; ++j)
+                    for (int k = 0; k < d.Nz; ++k) vel->vector->x.data[i][j][k] = f->scalar->data[i][j][k];
+        rk.tvd_rk3(f, vel, flux, rhs);
+    }
+    save(phi, f->scalar->data, d);
+    return 0;
+}
+
 }  // extern "C"

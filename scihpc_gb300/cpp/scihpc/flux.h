@@ -22,6 +22,10 @@ void identity_old_flux(vector_data *vel);
 
 void guess_from_history(scalar_data *f);
 
+// burgers_flux (flux.cpp:86-96): flux = data^2 / 2 on every cell.  Passed to runge_kutta it
+// selects the GPU transport stages; called directly it runs on host arrays (scihpc_flux_fill).
+void burgers_flux(scalar_data *f, vector_data *vel);
+
 void identity_with_extrapolation(scalar_data *f, vector_data *vel);
 void identity_with_extrapolation(scalar_data *f);
 void identity_with_extrapolation(vector_data *vel);

@@ -859,6 +859,13 @@ void identity_old_flux(vector_data *v) {
 }
 void guess_from_history(scalar_data *) { unsupported("guess_from_history", "no GPU stage (2 old - old2)"); }
 
+void burgers_flux(scalar_data *f, vector_data *) {
+    HostCall c(grid_of_sizes(f), f);
+    double *d = c.in(f->data), *fl = c.out(f->flux);
+    if (c.ok) c.run(scihpc_flux_fill(c.ctx, 1, d, fl, nullptr), "flux_fill");
+    c.finish();
+}
+
 void identity_with_extrapolation(scalar_data *f, vector_data *) { extrapolate(f, f->data, 0); }
 void identity_with_extrapolation(scalar_data *f) { extrapolate(f, f->data, 0); }
 void identity_with_extrapolation(vector_data *v) {
@@ -999,6 +1006,9 @@ void convection(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vect
 void convection_weno(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) {
     direct_call("convection_weno");
 }
+void Hamilton_Jacobi(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) {
+    direct_call("Hamilton_Jacobi");
+}
 void mpls(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) { direct_call("mpls"); }
 void lsf_redistance_no_lambda(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) {
     direct_call("lsf_redistance_no_lambda");
@@ -1026,7 +1036,82 @@ bool stage_begin(Session *&s, wrapper *f, wrapper *vel, flux_fn flux) {
 }
 }  // namespace
 
+// Transport of a scalar that no two-phase session owns (the 1D drivers, Hamilton-Jacobi /
+// Burgers): the stages of runge_kutta.cpp:13-63 on device buffers kept per field between calls.
+// Each stage: the flux on every cell (identity or Burgers), the UCCD first derivatives of every
+// active axis upwinded by the velocity, the right-hand side (convection or Hamilton-Jacobi) with
+// the stage's update of phi, and the fill of phi's ghosts with the field's boundary conditions.
+namespace {
+struct TransportBufs {
+    scihpc_ctx *ctx = nullptr;
+    size_t n = 0;
+    double *phi = nullptr, *flux = nullptr, *s1 = nullptr, *s2 = nullptr;
+    double *d1[3] = {}, *d2[3] = {}, *vel[3] = {};
+};
+std::map<const scalar_data *, TransportBufs> g_transport;
+
+bool transport_case(wrapper *f, flux_fn flux, rhs_fn rhs) {
+    const bool known_flux = flux == static_cast<flux_fn>(&identity_flux) || flux == &burgers_flux;
+    const bool known_rhs = rhs == &convection || rhs == &Hamilton_Jacobi;
+    if (!known_flux || !known_rhs || !f->is_scalar || session_of(f)) return false;
+    if (f->scalar->ndim == 1 || rhs == &Hamilton_Jacobi || flux == &burgers_flux) return true;
+    // a two-phase session serves scalars with Neumann walls; any other boundary goes here
+    int types[6];
+    double vals[6];
+    f->bcFactory->codes(types, vals);
+    for (int face = 0; face < 2 * f->scalar->ndim; ++face)
+        if (types[face] != 1) return true;
+    return false;
+}
+
+bool transport_run(wrapper *f, wrapper *vel, flux_fn flux, rhs_fn rhs, int first_stage, int last_stage) {
+    if (!f->params) return fail(SCIHPC_ERR_ARG, "tvd_rk3: link_params first (dt)"), false;
+    scalar_data *sc = f->scalar;
+    TransportBufs &b = g_transport[sc];
+    const size_t n = cells_of(sc);
+    if (!b.ctx) {
+        b.ctx = ctx_for(grid_of(f->geo));   // the derivatives need the grid's spacing
+        if (!b.ctx) return false;
+        b.n = n;
+        double **all[] = {&b.phi, &b.flux, &b.s1, &b.s2, &b.d1[0], &b.d1[1], &b.d1[2], &b.d2[0], &b.d2[1], &b.d2[2],
+                          &b.vel[0], &b.vel[1], &b.vel[2]};
+        for (double **p : all) {
+            if (!check_cuda(cudaMalloc(p, n * sizeof(double)), "cudaMalloc")) return false;
+            if (!check_cuda(cudaMemset(*p, 0, n * sizeof(double)), "cudaMemset")) return false;
+        }
+    }
+    const int ndim = sc->ndim;
+    sync_array(sc->data);
+    if (!check_cuda(cudaMemcpy(b.phi, base_of(sc->data), n * sizeof(double), cudaMemcpyHostToDevice), "upload"))
+        return false;
+    DataType ***vc[3] = {vel->vector->x.data, vel->vector->y.data, vel->vector->z.data};
+    for (int a = 0; a < ndim; ++a) {
+        sync_array(vc[a]);
+        if (!check_cuda(cudaMemcpy(b.vel[a], base_of(vc[a]), n * sizeof(double), cudaMemcpyHostToDevice), "upload"))
+            return false;
+    }
+    int types[6];
+    double vals[6];
+    f->bcFactory->codes(types, vals);
+    const int fk = flux == &burgers_flux ? 1 : 0, rk = rhs == &Hamilton_Jacobi ? 1 : 0;
+    const double *d1[3] = {b.d1[0], b.d1[1], b.d1[2]}, *vl[3] = {b.vel[0], b.vel[1], b.vel[2]};
+    for (int st = first_stage; st <= last_stage; ++st) {
+        if (!check(scihpc_flux_fill(b.ctx, fk, b.phi, b.flux, nullptr), "flux_fill")) return false;
+        for (int a = 0; a < ndim; ++a)
+            if (!check(scihpc_uccd(b.ctx, a, b.flux, b.vel[a], b.d1[a], b.d2[a], nullptr), "uccd")) return false;
+        if (!check(scihpc_rk3_stage(b.ctx, st, rk, f->params->dt, b.phi, d1, vl, b.s1, b.s2, nullptr), "rk3_stage"))
+            return false;
+        if (!check(scihpc_bc_fill(b.ctx, 0, types, vals, b.phi, nullptr), "bc_fill")) return false;
+    }
+    return check_cuda(cudaMemcpy(base_of(sc->data), b.phi, n * sizeof(double), cudaMemcpyDeviceToHost), "download");
+}
+}  // namespace
+
 void runge_kutta::tvd_rk3(wrapper *f, wrapper *vel, flux_fn flux, rhs_fn rhs) const {
+    if (transport_case(f, flux, rhs)) {
+        transport_run(f, vel, flux, rhs, 1, 3);
+        return;
+    }
     Session *s = nullptr;
     if (!stage_begin(s, f, vel, flux)) return;
     if (rhs == &convection || rhs == &convection_weno) {
@@ -1044,6 +1129,10 @@ void runge_kutta::tvd_rk3(wrapper *f, wrapper *vel, flux_fn flux, rhs_fn rhs) co
 }
 
 void runge_kutta::euler(wrapper *f, wrapper *vel, flux_fn flux, rhs_fn rhs) const {
+    if (transport_case(f, flux, rhs)) {
+        transport_run(f, vel, flux, rhs, 0, 0);
+        return;
+    }
     Session *s = nullptr;
     if (!stage_begin(s, f, vel, flux)) return;
     if (rhs != &mpls) {

@@ -10,6 +10,7 @@
 #include "levelset.cuh"
 #include "poisson.cuh"
 #include "reduce.cuh"
+#include "transport.cuh"
 #include "twophase.cuh"
 #include "conv.cuh"
 #include "unet.cuh"
@@ -184,6 +185,30 @@ int scihpc_uccd(scihpc_ctx *ctx, int axis, const double *flux, const double *vel
     REQUIRE(ctx && flux && vel_axis && f1 && f2, "uccd: NULL argument");
     REQUIRE(axis >= 0 && axis < ctx->D.ndim, "uccd: axis out of range");
     launch_uccd(ctx->D, ctx->ops, axis, flux, vel_axis, f1, f2, ctx->t1, ctx->t2, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_flux_fill(scihpc_ctx *ctx, int kind, const double *phi, double *flux, void *stream) {
+    REQUIRE(ctx && phi && flux, "flux_fill: NULL argument");
+    REQUIRE(kind == 0 || kind == 1, "flux_fill: kind must be 0 (identity) or 1 (Burgers)");
+    launch_flux_fill(ctx->D, kind, phi, flux, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_rk3_stage(scihpc_ctx *ctx, int stage, int rhs_kind, double dt, double *phi, const double *const d[3],
+                     const double *const vel[3], double *s1, double *s2, void *stream) {
+    REQUIRE(ctx && phi && d, "rk3_stage: NULL argument");
+    REQUIRE(stage >= 0 && stage <= 3, "rk3_stage: stage must be 0 (Euler) or 1..3");
+    REQUIRE(rhs_kind == 0 || rhs_kind == 1, "rk3_stage: rhs_kind must be 0 (convection) or 1 (Hamilton-Jacobi)");
+    for (int a = 0; a < ctx->D.ndim; ++a) {
+        REQUIRE(d[a], "rk3_stage: NULL derivative");
+        REQUIRE(rhs_kind == 1 || (vel && vel[a]), "rk3_stage: convection needs the velocity");
+    }
+    REQUIRE(stage == 0 || s1, "rk3_stage: stages 1-3 need s1");
+    REQUIRE(stage <= 1 || s2, "rk3_stage: stages 2-3 need s2");
+    launch_rk3_stage(ctx->D, stage, rhs_kind, dt, phi, d, rhs_kind == 0 ? vel : nullptr, s1, s2, S(stream));
     CHECK_LAUNCH();
     return SCIHPC_OK;
 }
