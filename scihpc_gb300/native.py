@@ -79,6 +79,9 @@ _SIGS = {
     "scihpc_zero_order_extrapolation": ([_vp, _vp, _vp], ctypes.c_int),
     "scihpc_uccd": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_ccd": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_flux_fill": ([_vp, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_rk3_stage": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp],
+                         ctypes.c_int),
     "scihpc_ccd_mixed": ([_vp, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_weno5": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_godunov_gradient": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
