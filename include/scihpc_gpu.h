@@ -86,6 +86,16 @@ int scihpc_uccd(scihpc_ctx *ctx, int axis, const double *flux, const double *vel
  * -sum_a d[a] (rhs_kind 1, Hamilton_Jacobi, source.cpp:75-107) on every cell and applies the
  * stage: 1: phi += dt s (s -> s1); 2: phi += dt (s - 3 s1) / 4 (s -> s2); 3: phi += dt (-s1 - s2
  * + 8 s) / 12; 0: euler's phi += dt s.  The caller then refills phi's ghosts (scihpc_bc_fill). */
+/* The second-order finite differences of second_order_solver (second_order_solver.cpp:7-241):
+ * vel_axis NULL: find_fx/fy/fz(f) -- central first (f1) and second (f2) derivatives of flux
+ * along axis on every cell, second-order one-sided at the ends of the ghosted array; vel_axis
+ * given: find_fx/fy/fz(f, vel) -- the one-sided second-order first derivative on the side the
+ * velocity comes from and the central second derivative, at the interior points of the axis
+ * only (the axis's ghost points keep their values).  scihpc_sec_mixed: mixed_xy / mixed_yz /
+ * mixed_zx, the derivative of src along axis with the central / one-sided stencils. */
+int scihpc_sec_derivative(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *f1,
+                          double *f2, void *stream);
+int scihpc_sec_mixed(scihpc_ctx *ctx, int axis, const double *src, double *out, void *stream);
 int scihpc_flux_fill(scihpc_ctx *ctx, int kind, const double *phi, double *flux, void *stream);
 int scihpc_rk3_stage(scihpc_ctx *ctx, int stage, int rhs_kind, double dt, double *phi, const double *const d[3],
                      const double *const vel[3], double *s1, double *s2, void *stream);
@@ -246,6 +256,10 @@ int scihpc_twophase_node_from_face(scihpc_twophase *tp);
 int scihpc_twophase_find_sign(scihpc_twophase *tp);
 int scihpc_twophase_reinit_step(scihpc_twophase *tp, int lambda);
 int scihpc_twophase_set_scheme(scihpc_twophase *tp, int scheme);
+/* find_source's derivatives (and so ab_solve's): 0 the compact CCD / UCCD schemes (default,
+ * projection_method.cpp:244-312), 1 second_order_solver -- find_source_sec / ab_solve_sec
+ * (projection_method.cpp:314-382, 779-801; source.cpp:42-73). */
+int scihpc_twophase_set_source_scheme(scihpc_twophase *tp, int scheme);
 /* nsteps time steps of the drivers' loop (benchmarks_2d_bubble_rising.cpp:100-130):
  * find_dt, advection, mass correction, ab_solve, reinitialisation.  use_graph = 1 replays
  * a captured CUDA graph per step (the pressure solve iterates inside it under a device-side

@@ -136,6 +136,16 @@ class Checker:
                                  int(vel_from_phi), _p(out), *[_p(a) for a in arrs])
         return out
 
+    def sec(self, g: Grid, flux, u=None, v=None, w=None) -> np.ndarray:
+        """second_order_solver: central derivatives and mixed ones (u None) or the upwind-biased
+        derivatives; out: fx, fy, fz, fxx, fyy, fzz, fxy, fyz, fzx."""
+        z = np.zeros(g.shape)
+        arrs = [np.ascontiguousarray(a if a is not None else z, dtype=np.float64) for a in (flux, u, v, w)]
+        out = np.zeros((9,) + g.shape)
+        n, lo, hi = g.c_args()
+        self.fn("sec")(g.ndim, n, lo, hi, int(u is not None), *[_p(a) for a in arrs], _p(out))
+        return out
+
     def ccd(self, g: Grid, flux, mixed: bool = True) -> np.ndarray:
         flux = np.ascontiguousarray(flux, dtype=np.float64)
         out = np.zeros((9,) + g.shape)

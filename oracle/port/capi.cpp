@@ -256,6 +256,10 @@ int port_tp_mpls(void *h, int count) {
     return 0;
 }
 int port_tp_reinit(void *h) { return static_cast<TwoPhase *>(h)->reinit(); }
+int port_tp_set_source_scheme(void *h, int scheme) {
+    static_cast<TwoPhase *>(h)->source_scheme = scheme;
+    return 0;
+}
 int port_tp_find_source(void *h) {
     static_cast<TwoPhase *>(h)->find_source();
     return 0;
@@ -317,6 +321,27 @@ int port_transport_rk3(int ndim, const int *n, const double *lo, const double *h
         rhs(s3.data());
         for (size_t i = 0; i < N; ++i) phi[i] += dt * (-s1[i] - s2[i] + 8.0 * s3[i]) / 12.0;
         bc_fill(g, LOC_NODE, t, v, phi);
+    }
+    return 0;
+}
+
+// second_order_solver on flux (second_order_solver.cpp:7-241): upwind 0 -- find_derivatives_all;
+// upwind 1 -- find_derivatives(f, vel).  out: fx, fy, fz, fxx, fyy, fzz, fxy, fyz, fzx, zero
+// where the call writes nothing.
+int port_sec(int ndim, const int *n, const double *lo, const double *hi, int upwind, const double *flux,
+             const double *u, const double *v, const double *w, double *out) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const size_t N = g.size();
+    std::memset(out, 0, 9 * N * sizeof(double));
+    const double *vel[3] = {u, v, w};
+    for (int a = 0; a < ndim; ++a) {
+        if (upwind) sec_upwind(g, a, flux, vel[a], out + a * N, out + (3 + a) * N);
+        else sec_central(g, a, flux, out + a * N, out + (3 + a) * N);
+    }
+    if (!upwind && ndim > 1) sec_mixed(g, 1, out + 0 * N, out + 6 * N);
+    if (!upwind && ndim > 2) {
+        sec_mixed(g, 2, out + 1 * N, out + 7 * N);
+        sec_mixed(g, 0, out + 2 * N, out + 8 * N);
     }
     return 0;
 }

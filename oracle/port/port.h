@@ -76,6 +76,11 @@ struct Compact {
     void ccd_mixed(int b, double *src, double *out) const;
 };
 
+// ---- second-order finite differences (second_order_solver.cpp:7-241, secorder.cpp)
+void sec_central(const Grid &g, int a, const double *flux, double *f1, double *f2);
+void sec_upwind(const Grid &g, int a, const double *flux, const double *vel_a, double *f1, double *f2);
+void sec_mixed(const Grid &g, int b, const double *src, double *out);
+
 // ---- WENO5 and Godunov (weno_solver.cpp, godunov_gradient.cpp)
 void weno5_axis(const Grid &g, int a, const double *flux, const double *vel_a, double *fa, double *scratch_fh);
 double weno5_for_godunov(double a, double b, double c, double d);

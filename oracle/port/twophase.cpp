@@ -330,7 +330,11 @@ void TwoPhase::momentum_convection(int a) {
     ScalarField &f = vel[a];
     flux_extrapolate(g, LOC_FACE_X + a, f.data.data(), f.flux.data());
     Field *d1[3] = {&f.fx, &f.fy, &f.fz}, *d2[3] = {&f.fxx, &f.fyy, &f.fzz};
-    for (int b = 0; b < g.ndim; ++b) cmp.uccd_axis(b, f.flux.data(), nvel[b].data.data(), d1[b]->data(), d2[b]->data());
+    for (int b = 0; b < g.ndim; ++b) {
+        // convection_sec (source.cpp:42-73) with second_order_solver's upwind-biased derivative
+        if (source_scheme == 1) sec_upwind(g, b, f.flux.data(), nvel[b].data.data(), d1[b]->data(), d2[b]->data());
+        else cmp.uccd_axis(b, f.flux.data(), nvel[b].data.data(), d1[b]->data(), d2[b]->data());
+    }
     Field &s = src[a];
 #pragma omp parallel for
     for (size_t q = 0; q < N; ++q) s[q] = -nvel[0].data[q] * f.fx[q];
@@ -433,11 +437,20 @@ void TwoPhase::find_source() {
     flux_extrapolate(g, LOC_NODE, phi.data.data(), phi.flux.data());
     {
         Field *d1[3] = {&phi.fx, &phi.fy, &phi.fz}, *d2[3] = {&phi.fxx, &phi.fyy, &phi.fzz};
-        for (int a = 0; a < g.ndim; ++a) cmp.ccd_axis(a, phi.flux.data(), d1[a]->data(), d2[a]->data());
-        if (g.ndim > 1) cmp.ccd_mixed(1, phi.fx.data(), phi.fxy.data());
-        if (g.ndim > 2) {
-            cmp.ccd_mixed(2, phi.fy.data(), phi.fyz.data());
-            cmp.ccd_mixed(0, phi.fz.data(), phi.fzx.data());
+        if (source_scheme == 1) {   // secSol->find_derivatives_all (second_order_solver.cpp:229-238)
+            for (int a = 0; a < g.ndim; ++a) sec_central(g, a, phi.flux.data(), d1[a]->data(), d2[a]->data());
+            if (g.ndim > 1) sec_mixed(g, 1, phi.fx.data(), phi.fxy.data());
+            if (g.ndim > 2) {
+                sec_mixed(g, 2, phi.fy.data(), phi.fyz.data());
+                sec_mixed(g, 0, phi.fz.data(), phi.fzx.data());
+            }
+        } else {
+            for (int a = 0; a < g.ndim; ++a) cmp.ccd_axis(a, phi.flux.data(), d1[a]->data(), d2[a]->data());
+            if (g.ndim > 1) cmp.ccd_mixed(1, phi.fx.data(), phi.fxy.data());
+            if (g.ndim > 2) {
+                cmp.ccd_mixed(2, phi.fy.data(), phi.fyz.data());
+                cmp.ccd_mixed(0, phi.fz.data(), phi.fzx.data());
+            }
         }
     }
     for (int a = 0; a < g.ndim; ++a) {
@@ -452,7 +465,8 @@ void TwoPhase::find_source() {
             if (c == a) continue;
             d1[c] = a == 0 ? &nvel[c].fx : (a == 1 ? &nvel[c].fy : &nvel[c].fz);
             d2[c] = a == 0 ? &nvel[c].fxx : (a == 1 ? &nvel[c].fyy : &nvel[c].fzz);
-            cmp.uccd_axis(a, nvel[c].flux.data(), nvel[a].data.data(), d1[c]->data(), d2[c]->data());
+            if (source_scheme == 1) sec_upwind(g, a, nvel[c].flux.data(), nvel[a].data.data(), d1[c]->data(), d2[c]->data());
+            else cmp.uccd_axis(a, nvel[c].flux.data(), nvel[a].data.data(), d1[c]->data(), d2[c]->data());
         }
         add_stress(a);
     }

@@ -30,6 +30,7 @@ struct TwoPhase {
     int vel_types[3][6];
     int scalar_types[6];
     int scheme = 0, n_mpls = 0, reinit_every = 0, ppe_mode = 0, reinit_lambda = 1;
+    int source_scheme = 0;   // 1: find_source_sec / ab_solve_sec (projection_method.cpp:314-382, 779-801)
     int step_count = 0, last_ppe_iters = 0;
     double exact_tol = 1e-13, last_relres = 0.0;
 

@@ -30,6 +30,7 @@
 #include "simple_bc.h"
 #include "godunov_gradient.h"
 #include "multigrid.h"
+#include "second_order_solver.h"
 
 namespace {
 
@@ -382,6 +383,7 @@ struct RefTP {
     shared_solvers *solvers;
     dummy_data *dummy;
     int scheme, n_mpls, reinit_every, ppe_mode, reinit_lambda, step;
+    int source_scheme;   // 1: find_source_sec / ab_solve_sec
 };
 
 void *ref_tp_create(int ndim, const int *n, const double *lo, const double *hi, const int *vel_bc,
@@ -540,22 +542,25 @@ int ref_tp_reinit(void *h) {
     return instep;
 }
 
+int ref_tp_set_source_scheme(void *h, int scheme) {
+    static_cast<RefTP *>(h)->source_scheme = scheme;
+    return 0;
+}
+
 int ref_tp_find_source(void *h) {
     auto *tp = static_cast<RefTP *>(h);
-    tp->flow->find_source(tp->vel, tp->nvel, tp->phi);
+    if (tp->source_scheme == 1) tp->flow->find_source_sec(tp->vel, tp->nvel, tp->phi);
+    else tp->flow->find_source(tp->vel, tp->nvel, tp->phi);
     return 0;
 }
 
 int ref_tp_ab_solve(void *h) {
     auto *tp = static_cast<RefTP *>(h);
-    if (tp->ppe_mode == 1) {
-        int saved = tp->param->iter;
-        tp->param->iter = 0;
-        tp->flow->ab_solve(tp->vel, tp->nvel, tp->pressure, tp->phi);
-        tp->param->iter = saved;
-    } else {
-        tp->flow->ab_solve(tp->vel, tp->nvel, tp->pressure, tp->phi);
-    }
+    const int saved = tp->param->iter;
+    if (tp->ppe_mode == 1) tp->param->iter = 0;
+    if (tp->source_scheme == 1) tp->flow->ab_solve_sec(tp->vel, tp->nvel, tp->pressure, tp->phi);
+    else tp->flow->ab_solve(tp->vel, tp->nvel, tp->pressure, tp->phi);
+    if (tp->ppe_mode == 1) tp->param->iter = saved;
     return 0;
 }
 
@@ -625,6 +630,28 @@ int ref_transport_rk3(int ndim, const int *n, const double *lo, const double *hi
         rk.tvd_rk3(f, vel, flux, rhs);
     }
     save(phi, f->scalar->data, d);
+    return 0;
+}
+
+// second_order_solver (second_order_solver.cpp:7-241) on flux: upwind 0 -- find_derivatives_all
+// (central fx.., fxx.. and the mixed fxy, fyz, fzx); upwind 1 -- find_derivatives(f, vel).
+// out: fx, fy, fz, fxx, fyy, fzz, fxy, fyz, fzx (entries a call does not write stay zero).
+int ref_sec(int ndim, const int *n, const double *lo, const double *hi, int upwind, const double *flux,
+            const double *u, const double *v, const double *w, double *out) {
+    Dims d = dims_of(ndim, n);
+    size_t N = size_t(d.Nx) * d.Ny * d.Nz;
+    structured_grid *geo = make_grid(ndim, n, lo, hi);
+    scalar_data *f = make_scalar(d);
+    vector_data *vel = make_vector(d);
+    load(f->flux, flux, d);
+    load(vel->x.data, u, d);
+    load(vel->y.data, v, d);
+    load(vel->z.data, w, d);
+    second_order_solver sec(geo->dx, geo->dy, geo->dz);
+    if (upwind) sec.find_derivatives(f, vel);
+    else sec.find_derivatives_all(f);
+    DataType ***o[9] = {f->fx, f->fy, f->fz, f->fxx, f->fyy, f->fzz, f->fxy, f->fyz, f->fzx};
+    for (int m = 0; m < 9; ++m) save(out + m * N, o[m], d);
     return 0;
 }
 

@@ -31,7 +31,7 @@ FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path
 
 # Per-file flags: the boundary fills must round exactly like the reference's separate
 # multiply and add, so contraction into fused multiply-adds is off there.
-FILE_FLAGS = {"bc.cu": ["-fmad=false"], "transport.cu": ["-fmad=false"]}
+FILE_FLAGS = {"bc.cu": ["-fmad=false"], "transport.cu": ["-fmad=false"], "secorder.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

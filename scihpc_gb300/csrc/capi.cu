@@ -10,6 +10,7 @@
 #include "levelset.cuh"
 #include "poisson.cuh"
 #include "reduce.cuh"
+#include "secorder.cuh"
 #include "transport.cuh"
 #include "twophase.cuh"
 #include "conv.cuh"
@@ -209,6 +210,24 @@ int scihpc_rk3_stage(scihpc_ctx *ctx, int stage, int rhs_kind, double dt, double
     REQUIRE(stage == 0 || s1, "rk3_stage: stages 1-3 need s1");
     REQUIRE(stage <= 1 || s2, "rk3_stage: stages 2-3 need s2");
     launch_rk3_stage(ctx->D, stage, rhs_kind, dt, phi, d, rhs_kind == 0 ? vel : nullptr, s1, s2, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_sec_derivative(scihpc_ctx *ctx, int axis, const double *flux, const double *vel_axis, double *f1,
+                          double *f2, void *stream) {
+    REQUIRE(ctx && flux && f1 && f2, "sec_derivative: NULL argument");
+    REQUIRE(axis >= 0 && axis < ctx->D.ndim, "sec_derivative: axis out of range");
+    if (vel_axis) launch_sec_upwind(ctx->D, axis, flux, vel_axis, f1, f2, S(stream));
+    else launch_sec_central(ctx->D, axis, flux, f1, f2, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_sec_mixed(scihpc_ctx *ctx, int axis, const double *src, double *out, void *stream) {
+    REQUIRE(ctx && src && out, "sec_mixed: NULL argument");
+    REQUIRE(axis >= 0 && axis < ctx->D.ndim, "sec_mixed: axis out of range");
+    launch_sec_mixed(ctx->D, axis, src, out, S(stream));
     CHECK_LAUNCH();
     return SCIHPC_OK;
 }
@@ -474,6 +493,13 @@ int scihpc_twophase_reinit_step(scihpc_twophase *tp, int lambda) {
 int scihpc_twophase_set_scheme(scihpc_twophase *tp, int scheme) {
     REQUIRE(tp && (scheme == 0 || scheme == 1), "twophase_set_scheme: scheme must be 0 (UCCD) or 1 (WENO5)");
     tp->tp.set_scheme(scheme);
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_set_source_scheme(scihpc_twophase *tp, int scheme) {
+    REQUIRE(tp && (scheme == 0 || scheme == 1),
+            "twophase_set_source_scheme: scheme must be 0 (compact) or 1 (second order)");
+    tp->tp.set_source_scheme(scheme);
     return SCIHPC_OK;
 }
 

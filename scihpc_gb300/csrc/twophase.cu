@@ -22,6 +22,7 @@
 #include "lsm_device.cuh"
 #include "reduce.cuh"
 #include "twophase.cuh"
+#include "secorder.cuh"
 
 namespace scihpc {
 
@@ -1015,6 +1016,15 @@ void TwoPhaseGpu::reinit_step(int lambda) {
     reinit_lambda = keep;
 }
 
+void TwoPhaseGpu::set_source_scheme(int s) {
+    if (s == source_scheme) return;
+    source_scheme = s;
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+}
+
 void TwoPhaseGpu::set_scheme(int s) {
     if (s == scheme) return;
     scheme = s;
@@ -1045,11 +1055,20 @@ void TwoPhaseGpu::find_source() {
     {
         cudaStream_t s = side[0];
         launch_extrapolate(D, 0, phi.data, phi.flux, s);
-        for (int a = 0; a < nd; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], s);
-        launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
-        if (nd > 2) {
-            launch_ccd_mixed(D, ops, 2, phi.d1[1], phi.mixed[1], work, s);
-            launch_ccd_mixed(D, ops, 0, phi.d1[2], phi.mixed[2], work, s);
+        if (source_scheme == 1) {   // secSol->find_derivatives_all (second_order_solver.cpp:229-238)
+            for (int a = 0; a < nd; ++a) launch_sec_central(D, a, phi.flux, phi.d1[a], phi.d2[a], s);
+            launch_sec_mixed(D, 1, phi.d1[0], phi.mixed[0], s);
+            if (nd > 2) {
+                launch_sec_mixed(D, 2, phi.d1[1], phi.mixed[1], s);
+                launch_sec_mixed(D, 0, phi.d1[2], phi.mixed[2], s);
+            }
+        } else {
+            for (int a = 0; a < nd; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], s);
+            launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
+            if (nd > 2) {
+                launch_ccd_mixed(D, ops, 2, phi.d1[1], phi.mixed[1], work, s);
+                launch_ccd_mixed(D, ops, 0, phi.d1[2], phi.mixed[2], work, s);
+            }
         }
         if (P.We > 0.0) {
             const double *d[9] = {phi.d1[0], phi.d1[1], phi.d1[2], phi.d2[0], phi.d2[1], phi.d2[2],
@@ -1071,13 +1090,18 @@ void TwoPhaseGpu::find_source() {
         // identity_with_extrapolation_face_*)
         DevScalar &U = vel[a];
         launch_extrapolate(D, 1 + a, U.data, U.flux, s);
-        for (int b = 0; b < nd; ++b) launch_uccd(D, ops, b, U.flux, nv[b], U.d1[b], U.d2[b], tb1[a], tb2[a], s);
+        // (find_source_sec: convection_sec with secSol's upwind-biased derivative, source.cpp:42-73)
+        for (int b = 0; b < nd; ++b) {
+            if (source_scheme == 1) launch_sec_upwind(D, b, U.flux, nv[b], U.d1[b], U.d2[b], s);
+            else launch_uccd(D, ops, b, U.flux, nv[b], U.d1[b], U.d2[b], tb1[a], tb2[a], s);
+        }
         k_convection_s<<<nbi, TPB, 0, s>>>(src[a], nv[0], nv[1], nv[2], U.d1[0], U.d1[1], U.d1[2], D);
         // cross derivatives of the other face-averaged components along a
         for (int c = 0; c < nd; ++c) {
             if (c == a) continue;
             launch_extrapolate(D, 1 + a, nv[c], fv_flux[a], s);
-            launch_uccd(D, ops, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], tb1[a], tb2[a], s);
+            if (source_scheme == 1) launch_sec_upwind(D, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], s);
+            else launch_uccd(D, ops, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], tb1[a], tb2[a], s);
         }
     }
     join(nd);

@@ -50,6 +50,9 @@ public:
     void find_sign();        // find_sign (wrapper_func.cpp:387-402) into the sign field
     void reinit_step(int lambda);   // one TVD-RK3 step of the redistance equation
     void set_scheme(int s);  // convection: 0 UCCD (source.cpp:8-40), 1 WENO5
+    // find_source's derivatives: 0 the compact schemes (projection_method.cpp:244-312),
+    // 1 second_order_solver (find_source_sec, projection_method.cpp:314-382)
+    void set_source_scheme(int s);
     void find_source();
     void ab_solve_pre();     // store, find_source, AB2, PPE right-hand side, solver begin
     void ab_solve_post();    // solver finish, pressure BC, velocity correction, node velocity
@@ -93,6 +96,7 @@ private:
 
     HostParams P{};
     int scheme = 1, n_mpls = 5, reinit_every = 1, fp32 = 0, reinit_lambda = 1;
+    int source_scheme = 0;
     int step_count = 0;
     int vel_types[3][6];
     int scalar_types[6];

@@ -80,6 +80,8 @@ _SIGS = {
     "scihpc_uccd": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_ccd": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_flux_fill": ([_vp, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_sec_derivative": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_sec_mixed": ([_vp, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_rk3_stage": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp],
                          ctypes.c_int),
     "scihpc_ccd_mixed": ([_vp, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
@@ -118,6 +120,7 @@ _SIGS = {
     "scihpc_twophase_find_sign": ([_vp], ctypes.c_int),
     "scihpc_twophase_reinit_step": ([_vp, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_set_scheme": ([_vp, ctypes.c_int], ctypes.c_int),
+    "scihpc_twophase_set_source_scheme": ([_vp, ctypes.c_int], ctypes.c_int),
     "scihpc_conv3x3": ([_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp],
                        ctypes.c_int),
     "scihpc_conv3x3_wgrad": ([_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -223,6 +226,13 @@ class Workspace:
 
     def ccd_mixed(self, axis, src, out, stream=0):
         self.L.check(self.L.scihpc_ccd_mixed(self.h, axis, _ptr(src), _ptr(out), stream))
+
+    def sec_derivative(self, axis, flux, vel, f1, f2, stream=0):
+        """second_order_solver::find_fx/fy/fz: central (vel None) or upwind-biased."""
+        self.L.check(self.L.scihpc_sec_derivative(self.h, axis, _ptr(flux), _ptr(vel), _ptr(f1), _ptr(f2), stream))
+
+    def sec_mixed(self, axis, src, out, stream=0):
+        self.L.check(self.L.scihpc_sec_mixed(self.h, axis, _ptr(src), _ptr(out), stream))
 
     def weno5(self, axis, flux, vel, fa, stream=0):
         self.L.check(self.L.scihpc_weno5(self.h, axis, _ptr(flux), _ptr(vel), _ptr(fa), stream))
@@ -399,6 +409,10 @@ class TwoPhase:
 
     def set_scheme(self, scheme: int):
         self.L.check(self.L.scihpc_twophase_set_scheme(self.h, scheme))
+
+    def set_source_scheme(self, scheme: int):
+        """find_source's derivatives: 0 compact (CCD/UCCD), 1 second order (find_source_sec)."""
+        self.L.check(self.L.scihpc_twophase_set_source_scheme(self.h, scheme))
 
     def ab_solve(self):
         it = ctypes.c_int(0)

@@ -196,3 +196,31 @@ def test_lsf_fields_and_integrals(port, ndim):
     rmass, rvol = port.lsf_integrals(g, prm, phi)
     assert abs(mass - rmass) <= 1e-13 * abs(rmass)
     assert abs(vol - rvol) <= 1e-13 * abs(rvol)
+
+
+@pytest.mark.parametrize("gi", range(len(GRIDS)))
+def test_second_order_solver(port, gi):
+    """second_order_solver's stencils (second_order_solver.cpp:7-241): the same arithmetic in
+    the same order, so bit for bit -- central with the mixed derivatives, and upwind-biased
+    (which leaves the ghost points of its axis as they were)."""
+    g = GRIDS[gi]
+    w = ws(g)
+    rng = np.random.default_rng(700 + gi)
+    flux = smooth_field(g, rng) + 0.01 * rng.standard_normal(g.shape)
+    vel = [rng.standard_normal(g.shape) for _ in range(3)]
+    central, upwind = port.sec(g, flux), port.sec(g, flux, *vel)
+    z = lambda: torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    d1 = []
+    for a in range(g.ndim):
+        f1, f2 = z(), z()
+        w.sec_derivative(a, dev(flux), None, f1, f2)
+        assert np.array_equal(host(f1), central[a]) and np.array_equal(host(f2), central[3 + a]), a
+        d1.append(f1)
+        u1, u2 = z(), z()
+        w.sec_derivative(a, dev(flux), dev(vel[a]), u1, u2)
+        assert np.array_equal(host(u1), upwind[a]) and np.array_equal(host(u2), upwind[3 + a]), a
+    pairs = [(1, 0, 6)] + ([(2, 1, 7), (0, 2, 8)] if g.ndim > 2 else [])
+    for b, src, k in pairs:
+        out = z()
+        w.sec_mixed(b, d1[src], out)
+        assert np.array_equal(host(out), central[k]), (b, k)

@@ -176,3 +176,32 @@ def test_checkpoint_restart_continues_bit_for_bit(tmp_path):
         other.restore(ck)
     for s in (a, b, other):
         s.close()
+
+
+def test_find_source_second_order():
+    """find_source_sec (projection_method.cpp:314-382): the level set's derivatives and the
+    momentum convection by second_order_solver."""
+    port, gpu = make_pair(G)
+    port.call("init")
+    gpu.init()
+    port.call("set_source_scheme", 1)
+    gpu.set_source_scheme(1)
+    port.call("find_source")
+    gpu.find_source()
+    compare(G, port, gpu, ["u_src", "v_src"], 1e-11)
+    compare(G, port, gpu, ["curvature"], 1e-10)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_full_steps_second_order(graph):
+    """Two steps with ab_solve_sec (projection_method.cpp:779-801), host-driven and captured."""
+    port, gpu = make_pair(G)
+    port.call("init")
+    gpu.init()
+    port.call("set_source_scheme", 1)
+    gpu.set_source_scheme(1)
+    for k in range(2):
+        port.call("step", 1)
+        gpu.step(1, graph=graph)
+    compare(G, port, gpu, ["phi"], LS_TOL)
+    compare(G, port, gpu, ["p", "u", "v"], FLOW_TOL)

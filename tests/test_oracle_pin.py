@@ -88,3 +88,42 @@ def test_two_phase_steps_bitexact(both):
         for nm in ("phi", "p", "u", "v", "nu", "nv", "rho", "curvature"):
             assert np.array_equal(s[0].get(nm), s[1].get(nm)), (k, nm)
         assert s[0].scalars() == s[1].scalars()
+
+
+@pytest.mark.parametrize("gi", range(len(GRIDS)))
+def test_second_order_solver_bitexact(both, gi):
+    """second_order_solver (second_order_solver.cpp:7-241): central + mixed and upwind-biased."""
+    P, R = both
+    g = GRIDS[gi]
+    rng = np.random.default_rng(40 + gi)
+    f = smooth_field(g, rng) + 0.01 * rng.standard_normal(g.shape)
+    u, v, w = (rng.standard_normal(g.shape) for _ in range(3))
+    assert np.array_equal(P.sec(g, f), R.sec(g, f))
+    assert np.array_equal(P.sec(g, f, u, v, w), R.sec(g, f, u, v, w))
+
+
+def test_two_phase_steps_second_order_bitexact(both):
+    """Time steps with ab_solve_sec (find_source_sec: second_order_solver for the level set's
+    derivatives, convection_sec for the momentum, projection_method.cpp:314-382, 779-801)."""
+    P, R = both
+    g = O.Grid(2, (16, 32), (0.0, 0.0), (1.0, 2.0))
+    prm = bubble_params(g, 1e-12)
+    prm.update(ppe_tol=1e-30, ppe_tol2=0.0, ppe_max_iter=500)
+    opt = dict(scheme=0, n_mpls=5, reinit_every=1, ppe_mode=1, reinit_lambda=1)
+    s = [C.twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm, opt) for C in (P, R)]
+    phi = bubble_phi(g, (0.43, 0.57), 0.23)
+    for x in s:
+        x.set("phi", phi)
+        x.call("init")
+        x.call("set_source_scheme", 1)
+    I = g.interior()
+    for k in range(2):
+        for x in s:
+            x.call("step", 1)
+        for nm in ("phi", "p", "u", "v", "nu", "nv", "rho", "curvature"):
+            # the upwind-biased derivatives never write the ghost points of their axis, so a
+            # few ghost cells of the velocities hold the same non-finite values on both sides
+            a, b = s[0].get(nm), s[1].get(nm)
+            assert np.array_equal(a, b, equal_nan=True), (k, nm)
+            assert np.isfinite(a[I]).all(), (k, nm)
+        assert s[0].scalars() == s[1].scalars()
