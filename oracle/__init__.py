@@ -125,8 +125,9 @@ class Checker:
 
     def transport_rk3(self, g: Grid, types, values, flux_kind: int, rhs_kind: int, dt: float, nsteps: int, phi, u,
                       v, w, vel_from_phi: bool = False) -> np.ndarray:
-        """runge_kutta::tvd_rk3 for nsteps steps with (identity_flux, convection) (kinds 0, 0) or
-        (burgers_flux, Hamilton_Jacobi) (kinds 1, 1); returns the new phi."""
+        """runge_kutta::tvd_rk3 for nsteps steps with (identity_flux, convection) (kinds 0, 0),
+        (burgers_flux, Hamilton_Jacobi) (kinds 1, 1) or convection_sec (rhs kind 2); returns the
+        new phi."""
         out = np.ascontiguousarray(phi, dtype=np.float64).copy()
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, w)]
         t = (ctypes.c_int * 6)(*types)

@@ -288,7 +288,8 @@ int port_tp_diagnostics(void *h, double *out) {
 
 // runge_kutta::tvd_rk3 (runge_kutta.cpp:13-49), nsteps steps, with the flux / right-hand side
 // pair (identity_flux, convection) (flux_kind 0, rhs_kind 0; flux.cpp:7-20, source.cpp:8-40) or
-// (burgers_flux, Hamilton_Jacobi) (flux_kind 1, rhs_kind 1; flux.cpp:86-96, source.cpp:75-107):
+// (burgers_flux, Hamilton_Jacobi) (flux_kind 1, rhs_kind 1; flux.cpp:86-96, source.cpp:75-107),
+// or convection_sec (rhs_kind 2, source.cpp:42-73: second_order_solver's derivative):
 // each stage fills the flux on every cell, takes the UCCD first derivatives of every active
 // axis upwinded by the velocity, forms s on every cell (x term, then minus the y and z terms),
 // updates phi by the stage formula and refills phi's ghosts.  vel_from_phi: u is a copy of phi
@@ -305,10 +306,14 @@ int port_transport_rk3(int ndim, const int *n, const double *lo, const double *h
     const double *vel[3] = {uu.data(), vv, w};
     auto rhs = [&](double *s) {
         for (size_t i = 0; i < N; ++i) flux[i] = flux_kind ? phi[i] * phi[i] * 0.5 : phi[i];
-        for (int a = 0; a < ndim; ++a) c.uccd_axis(a, flux.data(), vel[a], d1[a].data(), d2[a].data());
-        for (size_t i = 0; i < N; ++i) s[i] = rhs_kind ? -d1[0][i] : -vel[0][i] * d1[0][i];
+        for (int a = 0; a < ndim; ++a) {
+            if (rhs_kind == 2) sec_upwind(g, a, flux.data(), vel[a], d1[a].data(), d2[a].data());
+            else c.uccd_axis(a, flux.data(), vel[a], d1[a].data(), d2[a].data());
+        }
+        const bool hj = rhs_kind == 1;
+        for (size_t i = 0; i < N; ++i) s[i] = hj ? -d1[0][i] : -vel[0][i] * d1[0][i];
         for (int a = 1; a < ndim; ++a)
-            for (size_t i = 0; i < N; ++i) s[i] -= rhs_kind ? d1[a][i] : vel[a][i] * d1[a][i];
+            for (size_t i = 0; i < N; ++i) s[i] -= hj ? d1[a][i] : vel[a][i] * d1[a][i];
     };
     for (int step = 0; step < nsteps; ++step) {
         if (vel_from_phi) std::memcpy(uu.data(), phi, N * sizeof(double));

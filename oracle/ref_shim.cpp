@@ -600,7 +600,8 @@ int ref_tp_diagnostics(void *h, double *out) {
 
 // runge_kutta::tvd_rk3 (runge_kutta.cpp:13-49), nsteps steps, with (identity_flux, convection)
 // (flux_kind 0, rhs_kind 0; flux.cpp:7-20, source.cpp:8-40) or (burgers_flux, Hamilton_Jacobi)
-// (flux_kind 1, rhs_kind 1; flux.cpp:86-96, source.cpp:75-107); t/v: the scalar's boundary
+// (flux_kind 1, rhs_kind 1; flux.cpp:86-96, source.cpp:75-107), or convection_sec (rhs_kind 2,
+// source.cpp:42-73); t/v: the scalar's boundary
 // types and values; u/vv/w: the velocity (whole arrays).  vel_from_phi: the velocity's x
 // component is a copy of phi before every step, as benchmarks_1d_IBE.cpp does.
 int ref_transport_rk3(int ndim, const int *n, const double *lo, const double *hi, const int *t, const double *v,
@@ -621,7 +622,9 @@ int ref_transport_rk3(int ndim, const int *n, const double *lo, const double *hi
     load(vel->vector->z.data, w, d);
     runge_kutta rk(d.Nx, d.Ny, d.Nz);
     const flux_fn flux = flux_kind ? static_cast<flux_fn>(&burgers_flux) : IDENTITY;
-    const rhs_fn rhs = rhs_kind ? static_cast<rhs_fn>(&Hamilton_Jacobi) : static_cast<rhs_fn>(&convection);
+    const rhs_fn rhs = rhs_kind == 1   ? static_cast<rhs_fn>(&Hamilton_Jacobi)
+                       : rhs_kind == 2 ? static_cast<rhs_fn>(&convection_sec)
+                                       : static_cast<rhs_fn>(&convection);
     for (int step = 0; step < nsteps; ++step) {
         if (vel_from_phi)
             for (int i = 0; i < d.Nx; ++i)

@@ -8,6 +8,7 @@
 #include "ccd_solver.h"
 #include "multigrid.h"
 #include "scalar_data.h"
+#include "second_order_solver.h"
 #include "structured_grid.h"
 #include "uccd_solver.h"
 #include "weno_solver.h"
@@ -16,6 +17,7 @@ struct shared_solvers {
     ccd_solver *ccd = nullptr;     // GPU line solves on host arrays (ccd_solver.h)
     uccd_solver *uccd = nullptr;
     weno_solver *weno = nullptr;
+    second_order_solver *secSol = nullptr;   // second-order stencils on host arrays (second_order_solver.h)
     multigrid *mg = nullptr;       // GPU-backed (multigrid.h)
     structured_grid *geo = nullptr;
     int mg_bc = -1;                // -1 none, 0 Neumann, 1 Dirichlet

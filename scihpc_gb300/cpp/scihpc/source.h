@@ -3,7 +3,8 @@
 // convection (source.cpp:8-40, UCCD), mpls (source.cpp:109-154), lsf_redistance_lambda /
 // lsf_redistance_no_lambda (source.cpp:156-241), Hamilton_Jacobi (source.cpp:75-107: s = -sum
 // of the UCCD derivatives of the flux, upwinded by the velocity).  convection_weno is the WENO5
-// (weno_solver.cpp:270-278) variant of convection.  Called directly they report
+// (weno_solver.cpp:270-278) variant of convection, convection_sec (source.cpp:42-73) the
+// second_order_solver one.  Called directly they report
 // SCIHPC_ERR_UNSUPPORTED through scihpc_cpp_last_status(): the GPU path evaluates them only
 // inside the time integrator.
 #ifndef SCIHPC_GB300_SOURCE_H
@@ -17,6 +18,7 @@ typedef void (*scihpc_flux_fn)(scalar_data *, vector_data *);
 
 void convection(wrapper *f, wrapper *vel, DataType ***s, void (*flux)(scalar_data *, vector_data *));
 void convection_weno(wrapper *f, wrapper *vel, DataType ***s, void (*flux)(scalar_data *, vector_data *));
+void convection_sec(wrapper *f, wrapper *vel, DataType ***s, void (*flux)(scalar_data *, vector_data *));
 void Hamilton_Jacobi(wrapper *f, wrapper *vel, DataType ***s, void (*flux)(scalar_data *, vector_data *));
 void mpls(wrapper *phi, wrapper *vel, DataType ***s, void (*flux)(scalar_data *, vector_data *));
 void lsf_redistance_no_lambda(wrapper *phi, wrapper *vel, DataType ***s, void (*flux)(scalar_data *, vector_data *));

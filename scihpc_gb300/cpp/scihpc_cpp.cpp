@@ -747,6 +747,7 @@ shared_solvers *SharedSolvers_alloc(scalar_data *f, structured_grid *geo) {
     s->ccd = new ccd_solver(f, geo);
     s->uccd = new uccd_solver(f, geo);
     s->weno = new weno_solver(f, geo);
+    s->secSol = new second_order_solver(geo->dx, geo->dy, geo->dz);
     s->mg = new multigrid(f, geo);
     return s;
 }
@@ -1009,6 +1010,67 @@ void convection_weno(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *,
 void Hamilton_Jacobi(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) {
     direct_call("Hamilton_Jacobi");
 }
+void convection_sec(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) {
+    direct_call("convection_sec");
+}
+
+// ---------------------------------------------------------------- second_order_solver
+second_order_solver::second_order_solver(DataType _dx, DataType _dy, DataType _dz) : dx(_dx), dy(_dy), dz(_dz) {}
+
+namespace {
+// the scalar's grid with the solver's spacing (the stencils divide by it)
+scihpc_grid sec_grid(const scalar_data *f, const second_order_solver *so) {
+    scihpc_grid c = grid_of_sizes(f);
+    const double d[3] = {so->dx, so->dy, so->dz};
+    for (int a = 0; a < f->ndim; ++a) c.hi[a] = c.lo[a] + d[a] * c.n[a];
+    return c;
+}
+
+void sec_axis(const second_order_solver *so, scalar_data *f, int a, DataType ***vel_a) {
+    if (a >= f->ndim) return;
+    DataType ***d1[3] = {f->fx, f->fy, f->fz}, ***d2[3] = {f->fxx, f->fyy, f->fzz};
+    HostCall c(sec_grid(f, so), f);
+    double *fl = c.in(f->flux), *v = vel_a ? c.in(vel_a) : nullptr, *o1 = c.out(d1[a]), *o2 = c.out(d2[a]);
+    if (c.ok) c.run(scihpc_sec_derivative(c.ctx, a, fl, v, o1, o2, nullptr), "sec_derivative");
+    c.finish();
+}
+
+void sec_mix(const second_order_solver *so, scalar_data *f, int b, DataType ***src, DataType ***dst) {
+    if (b >= f->ndim) return;
+    HostCall c(sec_grid(f, so), f);
+    double *in = c.in(src), *out = c.out(dst);
+    if (c.ok) c.run(scihpc_sec_mixed(c.ctx, b, in, out, nullptr), "sec_mixed");
+    c.finish();
+}
+}  // namespace
+
+void second_order_solver::find_fx(scalar_data *f) const { sec_axis(this, f, 0, nullptr); }
+void second_order_solver::find_fy(scalar_data *f) const { sec_axis(this, f, 1, nullptr); }
+void second_order_solver::find_fz(scalar_data *f) const { sec_axis(this, f, 2, nullptr); }
+void second_order_solver::find_fx(scalar_data *f, vector_data *vel) const { sec_axis(this, f, 0, vel->x.data); }
+void second_order_solver::find_fy(scalar_data *f, vector_data *vel) const { sec_axis(this, f, 1, vel->y.data); }
+void second_order_solver::find_fz(scalar_data *f, vector_data *vel) const { sec_axis(this, f, 2, vel->z.data); }
+void second_order_solver::mixed_xy(scalar_data *f) const { sec_mix(this, f, 1, f->fx, f->fxy); }
+void second_order_solver::mixed_yz(scalar_data *f) const { sec_mix(this, f, 2, f->fy, f->fyz); }
+void second_order_solver::mixed_zx(scalar_data *f) const { sec_mix(this, f, 0, f->fz, f->fzx); }
+void second_order_solver::find_derivatives(scalar_data *f) const {
+    find_fx(f);
+    if (f->ndim > 1) find_fy(f);
+    if (f->ndim > 2) find_fz(f);
+}
+void second_order_solver::find_derivatives(scalar_data *f, vector_data *vel) const {
+    find_fx(f, vel);
+    if (f->ndim > 1) find_fy(f, vel);
+    if (f->ndim > 2) find_fz(f, vel);
+}
+void second_order_solver::find_derivatives_all(scalar_data *f) const {
+    find_derivatives(f);
+    if (f->ndim > 1) mixed_xy(f);
+    if (f->ndim > 2) {
+        mixed_yz(f);
+        mixed_zx(f);
+    }
+}
 void mpls(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) { direct_call("mpls"); }
 void lsf_redistance_no_lambda(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) {
     direct_call("lsf_redistance_no_lambda");
@@ -1052,9 +1114,10 @@ std::map<const scalar_data *, TransportBufs> g_transport;
 
 bool transport_case(wrapper *f, flux_fn flux, rhs_fn rhs) {
     const bool known_flux = flux == static_cast<flux_fn>(&identity_flux) || flux == &burgers_flux;
-    const bool known_rhs = rhs == &convection || rhs == &Hamilton_Jacobi;
+    const bool known_rhs = rhs == &convection || rhs == &Hamilton_Jacobi || rhs == &convection_sec;
     if (!known_flux || !known_rhs || !f->is_scalar || session_of(f)) return false;
-    if (f->scalar->ndim == 1 || rhs == &Hamilton_Jacobi || flux == &burgers_flux) return true;
+    if (f->scalar->ndim == 1 || rhs == &Hamilton_Jacobi || rhs == &convection_sec || flux == &burgers_flux)
+        return true;
     // a two-phase session serves scalars with Neumann walls; any other boundary goes here
     int types[6];
     double vals[6];
@@ -1097,8 +1160,13 @@ bool transport_run(wrapper *f, wrapper *vel, flux_fn flux, rhs_fn rhs, int first
     const double *d1[3] = {b.d1[0], b.d1[1], b.d1[2]}, *vl[3] = {b.vel[0], b.vel[1], b.vel[2]};
     for (int st = first_stage; st <= last_stage; ++st) {
         if (!check(scihpc_flux_fill(b.ctx, fk, b.phi, b.flux, nullptr), "flux_fill")) return false;
-        for (int a = 0; a < ndim; ++a)
-            if (!check(scihpc_uccd(b.ctx, a, b.flux, b.vel[a], b.d1[a], b.d2[a], nullptr), "uccd")) return false;
+        for (int a = 0; a < ndim; ++a) {
+            // convection_sec: second_order_solver's upwind-biased derivative (source.cpp:42-73)
+            const int rc = rhs == &convection_sec
+                               ? scihpc_sec_derivative(b.ctx, a, b.flux, b.vel[a], b.d1[a], b.d2[a], nullptr)
+                               : scihpc_uccd(b.ctx, a, b.flux, b.vel[a], b.d1[a], b.d2[a], nullptr);
+            if (!check(rc, "derivative")) return false;
+        }
         if (!check(scihpc_rk3_stage(b.ctx, st, rk, f->params->dt, b.phi, d1, vl, b.s1, b.s2, nullptr), "rk3_stage"))
             return false;
         if (!check(scihpc_bc_fill(b.ctx, 0, types, vals, b.phi, nullptr), "bc_fill")) return false;
@@ -1148,12 +1216,14 @@ projection_method::projection_method(scalar_data *) {}
 void projection_method::find_source(wrapper *vel, wrapper *nvel, wrapper *lsf) const {
     Session *s = session_for(lsf, vel, nvel, nullptr);
     if (!s || !push_scalars(s)) return;
+    if (!check(scihpc_twophase_set_source_scheme(s->tp, 0), "set_source_scheme")) return;
     if (check(scihpc_twophase_find_source(s->tp), "find_source")) pull_scalars(s);
 }
 
 void projection_method::ab_solve(wrapper *vel, wrapper *nvel, wrapper *pressure, wrapper *lsf) {
     Session *s = session_for(lsf, vel, nvel, pressure);
     if (!s || !push_scalars(s)) return;
+    if (!check(scihpc_twophase_set_source_scheme(s->tp, 0), "set_source_scheme")) return;
     const int rc = scihpc_twophase_ab_solve(s->tp, &last_iterations, &last_relres);
     if (rc == SCIHPC_ERR_MAXITER) {
         fail(rc, "ab_solve: pressure solve stopped at ppe_max_iter above ppe_tol");
@@ -1216,11 +1286,24 @@ void projection_method::add_body_force(wrapper *) const {
 void projection_method::add_surface_force(wrapper *) const {
     unsupported("add_surface_force", "a stage inside the GPU find_source");
 }
-void projection_method::find_source_sec(wrapper *, wrapper *, wrapper *) const {
-    unsupported("find_source_sec", "the second-order discretisation is not on the GPU path");
+void projection_method::find_source_sec(wrapper *vel, wrapper *nvel, wrapper *lsf) const {
+    Session *s = session_for(lsf, vel, nvel, nullptr);
+    if (!s || !push_scalars(s)) return;
+    if (!check(scihpc_twophase_set_source_scheme(s->tp, 1), "set_source_scheme")) return;
+    if (check(scihpc_twophase_find_source(s->tp), "find_source_sec")) pull_scalars(s);
 }
-void projection_method::ab_solve_sec(wrapper *, wrapper *, wrapper *, wrapper *) {
-    unsupported("ab_solve_sec", "the second-order discretisation is not on the GPU path");
+
+void projection_method::ab_solve_sec(wrapper *vel, wrapper *nvel, wrapper *pressure, wrapper *lsf) {
+    Session *s = session_for(lsf, vel, nvel, pressure);
+    if (!s || !push_scalars(s)) return;
+    if (!check(scihpc_twophase_set_source_scheme(s->tp, 1), "set_source_scheme")) return;
+    const int rc = scihpc_twophase_ab_solve(s->tp, &last_iterations, &last_relres);
+    if (rc == SCIHPC_ERR_MAXITER) {
+        fail(rc, "ab_solve_sec: pressure solve stopped at ppe_max_iter above ppe_tol");
+    } else if (!check(rc, "ab_solve_sec")) {
+        return;
+    }
+    pull_scalars(s);
 }
 
 // ---------------------------------------------------------------- wrapper_func

@@ -99,7 +99,9 @@ int main(int argc, char **argv) {
         param->iter++;
         solver.tvd_rk3(&phi, &nvel, &identity_flux, P["weno"] != 0.0 ? &convection_weno : &convection);
         for (int c = 0; c < 5; ++c) solver.euler(&phi, &nvel, &identity_flux, &mpls);
-        flow_solver.ab_solve(&vel, &nvel, &pressure, &phi);
+        // second_order: the projection step of benchmarks_2d_dambreak.cpp (ab_solve_sec)
+        if (P.count("second_order") && P["second_order"] != 0.0) flow_solver.ab_solve_sec(&vel, &nvel, &pressure, &phi);
+        else flow_solver.ab_solve(&vel, &nvel, &pressure, &phi);
         int instep = 0;
         while (instep * param->rdt < 2.0 * param->ls_width) {
             if (instep == 0) find_sign(&phi);

@@ -75,7 +75,7 @@ int field_mode(int argc, char **argv) {
     runge_kutta solver(f->Nx, f->Ny, f->Nz);
     void (*flux)(scalar_data *, vector_data *) = fk ? &burgers_flux : static_cast<void (*)(scalar_data *, vector_data *)>(&identity_flux);
     void (*rhs)(wrapper *, wrapper *, DataType ***, void (*)(scalar_data *, vector_data *)) =
-        rk ? &Hamilton_Jacobi : &convection;
+        rk == 1 ? &Hamilton_Jacobi : (rk == 2 ? &convection_sec : &convection);
     for (int s = 0; s < nsteps; ++s) {
         if (vel_from_phi) std::memcpy(vel->vector->x.data[0][0], f->data[0][0], N * sizeof(double));
         solver.tvd_rk3(phi, vel, flux, rhs);

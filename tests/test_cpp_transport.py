@@ -23,6 +23,8 @@ CASES = [
     (2, (16, 12), 0.0, 1.0, 0, 0, 0, 5e-4, 10, False),   # 2D convection, periodic
     (2, (12, 16), 0.0, 1.0, 1, 1, 1, 5e-4, 10, False),   # 2D Hamilton-Jacobi (Burgers flux), Neumann
     (3, (8, 10, 12), 0.0, 1.0, 0, 0, 1, 5e-4, 4, False),  # 3D Hamilton-Jacobi (identity flux), periodic
+    (1, (32,), -1.0, 1.0, 0, 0, 2, 6e-4, 40, False),     # 1D convection_sec, periodic
+    (2, (16, 12), 0.0, 1.0, 1, 0, 2, 5e-4, 10, False),   # 2D convection_sec, Neumann
 ]
 
 
