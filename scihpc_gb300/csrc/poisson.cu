@@ -998,8 +998,13 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
 // The V-cycle of a 128 x 256 grid drops from about 21 launches to 5.
 constexpr int V2_T = 16, V2_H = 5, V2_R = V2_T + 2 * V2_H, V2_THREADS = 256;
 
-template <class T, int MODE, bool UP>
-__global__ void __launch_bounds__(V2_THREADS) k_vcycle2(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2) {
+// DOT (up leg of level 0 inside the FP32 inner conjugate gradients): the leg's output is z and
+// its right-hand side the inner residual r, so <r, z> over the written cells is reduced into
+// *dot (every block takes part).
+template <class T, int MODE, bool UP, bool DOT = false>
+__global__ void __launch_bounds__(V2_THREADS) k_vcycle2(Level<T> F, Level<T> Cl, const T *__restrict__ rho, Id2<T> id2,
+                                                        RedSlot slot = RedSlot{}, double *dot = nullptr) {
+    static_assert(!DOT || UP, "the dot product belongs to the up leg");
     pdl_wait();
     pdl_trigger();
     __shared__ T X[V2_R][V2_R], Bs[V2_R][V2_R];
@@ -1064,10 +1069,18 @@ __global__ void __launch_bounds__(V2_THREADS) k_vcycle2(Level<T> F, Level<T> Cl,
         __syncthreads();
     }
     // the tile's iterate
+    float acc = 0.0f;   // DOT: this thread's part of <r, z>
     for (int e = tid; e < V2_T * V2_T; e += V2_THREADS) {
         const int r = e / V2_T + V2_H, c = e % V2_T + V2_H;
         const int I = I0 + r, J = J0 + c;
-        if (I < F.n[0] && J < F.n[1]) (UP ? F.x : F.x2)[(I + 1) * s0 + (J + 1)] = X[r][c];
+        if (I < F.n[0] && J < F.n[1]) {
+            (UP ? F.x : F.x2)[(I + 1) * s0 + (J + 1)] = X[r][c];
+            if (DOT) acc = fmaf(float(Bs[r][c]), float(X[r][c]), acc);
+        }
+    }
+    if constexpr (DOT) {
+        __shared__ double red[V2_THREADS];
+        block_grid_sum(double(acc), red, slot, dot);
     }
     if (UP) return;
     // residual of the tile, restricted: coarse cell (ci, cj) of the tile sums four residuals
@@ -2327,24 +2340,28 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
     auto fused2 = [&](int l) {
         return D.ndim == 2 && l < lc && Ls[l].ratio == 2 && !prolong_linear && (l > 0 || mode0 != 2);
     };
+    // set when the last level-0 pass reduced <b, x> into *dot
+    bool dot_done = false;
+    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     auto leg2 = [&](int l, bool up) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         const dim3 grid(unsigned((F.n[1] + V2_T - 1) / V2_T), unsigned((F.n[0] + V2_T - 1) / V2_T));
         const bool m1 = l == 0 && mode0 == 1;
-        if (up) {
-            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
-            else launch_pdl(pdl, k_vcycle2<T, 0, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
+        if (up && l == 0 && dot && (long long)grid.x * grid.y <= RED_MAX_BLOCKS) {
+            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, true, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2, slot, dot);
+            else launch_pdl(pdl, k_vcycle2<T, 0, true, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2, slot, dot);
+            dot_done = true;
+        } else if (up) {
+            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2, slot, nullptr);
+            else launch_pdl(pdl, k_vcycle2<T, 0, true>, grid, V2_THREADS, 0, s, F, Cl, rp, id2, slot, nullptr);
         } else {
-            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, false>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
-            else launch_pdl(pdl, k_vcycle2<T, 0, false>, grid, V2_THREADS, 0, s, F, Cl, rp, id2);
+            if (m1) launch_pdl(pdl, k_vcycle2<T, 1, false>, grid, V2_THREADS, 0, s, F, Cl, rp, id2, slot, nullptr);
+            else launch_pdl(pdl, k_vcycle2<T, 0, false>, grid, V2_THREADS, 0, s, F, Cl, rp, id2, slot, nullptr);
         }
     };
     // the first post-smoothing sweep of level 0 can apply the prolongation itself
     const bool pro0 = sizeof(T) == 4 && mode0 == 1 && tma_ready && tma_pro_ready && tma_enable && fused(0) &&
                       Ls[0].ratio == 2 && !prolong_linear;
-    // dot_out: set when the last sweep reduced <b, x> of level 0 into *dot
-    bool dot_done = false;
-    RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     auto sweep = [&](int l, const T *xo, T *xn, int c0, int zero, bool pro, bool want_dot) {
         Level<T> &L = Ls[l];
         const int ci = sweep_chunk(L.n);
