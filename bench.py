@@ -458,13 +458,8 @@ def dirichlet_block(torch, Poisson, Grid, cpu: bool) -> dict:
     return out
 
 
-def dambreak_block(torch, TwoPhase, Grid, steps: int = 40, warmup: int = 3) -> dict:
-    """3D dam break, 128 x 64 x 64 cells on [0,4] x [0,2] x [0,2]: water column [0,1] x [0,2] x
-    [0,1] (signed distance to its free surfaces), air/water 1000/1.2 density and 1e-3/1.8e-5
-    viscosity, gravity 9.81 along -z, L = 1, no surface tension, slip walls on all faces, UCCD
-    transport, reinitialisation every 20 steps (the reference's dam-break driver), pressure to
-    relative residual 1e-10 each step with FP64 V-cycles and with FP32 V-cycles in FP64
-    refinement.  Graph replay; the working set (~60 fields of 0.6 M cells) exceeds L2."""
+def dambreak_setup(Grid):
+    """Grid, parameters and initial level set of the 128 x 64 x 64 dam break (dambreak_block)."""
     import numpy as np
     n = (128, 64, 64)
     g = Grid(3, n, (0.0, 0.0, 0.0), (4.0, 2.0, 2.0))
@@ -478,6 +473,17 @@ def dambreak_block(torch, TwoPhase, Grid, steps: int = 40, warmup: int = 3) -> d
     phi = np.zeros(g.shape)
     phi[3:-3, 3:-3, 3:-3] = np.where((X < 1.0) & (Z < 1.0), np.minimum(1.0 - X, 1.0 - Z),
                                      -np.sqrt(np.maximum(X - 1.0, 0.0) ** 2 + np.maximum(Z - 1.0, 0.0) ** 2))
+    return g, prm, phi
+
+
+def dambreak_block(torch, TwoPhase, Grid, steps: int = 40, warmup: int = 3) -> dict:
+    """3D dam break, 128 x 64 x 64 cells on [0,4] x [0,2] x [0,2]: water column [0,1] x [0,2] x
+    [0,1] (signed distance to its free surfaces), air/water 1000/1.2 density and 1e-3/1.8e-5
+    viscosity, gravity 9.81 along -z, L = 1, no surface tension, slip walls on all faces, UCCD
+    transport, reinitialisation every 20 steps (the reference's dam-break driver), pressure to
+    relative residual 1e-10 each step with FP64 V-cycles and with FP32 V-cycles in FP64
+    refinement.  Graph replay; the working set (~60 fields of 0.6 M cells) exceeds L2."""
+    g, prm, phi = dambreak_setup(Grid)
     out = {"grid": "128x64x64 on [0,4]x[0,2]x[0,2]", "steps_timed": steps,
            "physics": "rho 1000/1.2, mu 1e-3/1.8e-5, g 9.81 (-z), L 1, no surface tension, slip walls",
            "step": "find_dt + UCCD/TVD-RK3 transport + ab_solve (pressure to rel. residual 1e-10); "
@@ -680,6 +686,8 @@ def main():
                     help="only a few training steps of the 256^2 learned guess (profiling case)")
     ap.add_argument("--profile-unet3", action="store_true",
                     help="only a few training steps of the 3D learned guess on a 128^3 grid (profiling case)")
+    ap.add_argument("--profile-dambreak", action="store_true",
+                    help="init and two steps of the 128x64x64 dam break, kernel by kernel (profiling case)")
     ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
                     help="only three iterations of the 256^3 pressure solve (profiling case)")
     args = ap.parse_args()
@@ -701,6 +709,16 @@ def main():
         net = UNet(128, 128, 128, seed=0)
         losses = train(net, snaps, 3, 1e-3, torch)
         print(json.dumps({"profile": "unet3 128^3 training steps", "loss": losses}))
+    elif args.profile_dambreak:
+        import torch
+        from scihpc_gb300 import Grid, TwoPhase, lib
+        lib()
+        g, prm, phi = dambreak_setup(Grid)
+        tp = TwoPhase(g, ["slip"] * 6, ["neumann"] * 6, prm, scheme=0, n_mpls=0, reinit_every=20, fp32=True)
+        tp.set("phi", phi)
+        tp.init()
+        tp.step(2, graph=False, sync=True)
+        print(json.dumps({"profile": "dambreak 128x64x64, init + 2 steps", "scalars": tp.scalars()}))
     elif args.profile_poisson:
         profile_poisson(args.profile_poisson)
     elif args.impl == "reference":

@@ -10,6 +10,8 @@
 // system, a scratch pair), then the backward sweep finishes the line holding only the i+1
 // values in registers.  This sequential form serves lines longer than the warp-cooperative
 // solver of linescan.cu handles (more than 512 points).
+#include <algorithm>
+#include <array>
 #include <cmath>
 #include <vector>
 
@@ -136,6 +138,81 @@ std::vector<double> pack_scan(const HostLineOp &op) {
         r[8] = a, r[9] = b, r[10] = c, r[11] = d;
     }
     return t;
+}
+
+// Tables of the warp-cooperative solve (linescan.cu) for one launch shape: lines of n points,
+// T = 32 * wpl threads per line, thread t holding points t*C .. t*C+C-1.  Thread index fastest,
+// so that a warp's loads are coalesced:
+//   [C][12][T]  the per-point factors {L (4), K (4), Dinv (4)} of point t*C+k (zero past n);
+//   [48][T]     the matrix halves of the scan maps.  A lane's chunk map and every partial map of
+//               the shuffle scans are affine maps x -> M x + c whose matrices depend only on the
+//               factorisation and the shape, so they are formed here once per axis and the kernel
+//               carries the 2-vectors c alone: [0,20) the forward partial matrix of t before each
+//               of the five shuffle steps, [20,24) the final forward matrix of thread t-1 of the
+//               same warp, [24,44) and [44,48) the same for the backward scan (thread t+1);
+//   [wpl][8]    per warp, the final forward matrix of its lane 31 and the final backward matrix
+//               of its lane 0.
+namespace {
+using Mat2 = std::array<double, 4>;
+
+// b a (row-major 2x2)
+Mat2 mat_mul(const Mat2 &b, const Mat2 &a) {
+    return {b[0] * a[0] + b[1] * a[2], b[0] * a[1] + b[1] * a[3], b[2] * a[0] + b[3] * a[2],
+            b[2] * a[1] + b[3] * a[3]};
+}
+}  // namespace
+
+std::vector<double> lane_table(const std::vector<double> &tab, int n, int wpl, int C) {
+    const int T = 32 * wpl;
+    const size_t pts = size_t(C) * 12 * T;
+    std::vector<double> out(pts + size_t(T) * 48 + size_t(wpl) * 8, 0.0);
+    for (int t = 0; t < T; ++t)
+        for (int k = 0; k < C && t * C + k < n; ++k)
+            for (int q = 0; q < 12; ++q) out[(size_t(k) * 12 + q) * T + t] = tab[size_t(t * C + k) * 12 + q];
+    const Mat2 I = {1.0, 0.0, 0.0, 1.0}, Z = {0.0, 0.0, 0.0, 0.0};
+    std::vector<Mat2> F(T), G(T);
+    for (int t = 0; t < T; ++t) {
+        const int lo = t * C, cnt = lo >= n ? 0 : std::min(C, n - lo);
+        Mat2 f = I, g = I;
+        for (int k = 0; k < cnt; ++k) {
+            const double *r = &tab[size_t(lo + k) * 12];
+            f = lo + k == 0 ? Z : mat_mul({-r[0], -r[1], -r[2], -r[3]}, f);
+        }
+        for (int k = cnt - 1; k >= 0; --k) {
+            const double *r = &tab[size_t(lo + k) * 12];
+            g = lo + k == n - 1 ? Z : mat_mul({r[4], r[5], r[6], r[7]}, g);
+        }
+        F[t] = f;
+        G[t] = g;
+    }
+    for (int w = 0; w < wpl; ++w) {
+        Mat2 *f = &F[size_t(w) * 32], *g = &G[size_t(w) * 32];
+        for (int st = 0, d = 1; d < 32; ++st, d <<= 1) {
+            const std::vector<Mat2> f0(f, f + 32), g0(g, g + 32);
+            for (int l = 0; l < 32; ++l) {
+                double *e = &out[pts + size_t(w) * 32 + l];
+                for (int q = 0; q < 4; ++q) {
+                    e[size_t(4 * st + q) * T] = f0[l][q];
+                    e[size_t(24 + 4 * st + q) * T] = g0[l][q];
+                }
+                if (l >= d) f[l] = mat_mul(f0[l], f0[l - d]);
+                if (l + d < 32) g[l] = mat_mul(g0[l], g0[l + d]);
+            }
+        }
+        for (int l = 0; l < 32; ++l) {
+            double *e = &out[pts + size_t(w) * 32 + l];
+            for (int q = 0; q < 4; ++q) {
+                e[size_t(20 + q) * T] = l > 0 ? f[l - 1][q] : 0.0;
+                e[size_t(44 + q) * T] = l < 31 ? g[l + 1][q] : 0.0;
+            }
+        }
+        double *wt = &out[pts + size_t(T) * 48 + size_t(w) * 8];
+        for (int q = 0; q < 4; ++q) {
+            wt[q] = f[31][q];
+            wt[4 + q] = g[0][q];
+        }
+    }
+    return out;
 }
 
 // Right-hand sides: one-sided three-point closures at both ends and the interior formulas
@@ -327,18 +404,25 @@ int CompactOps::build(const Dims &D) {
         std::vector<double> tc = pack(c), tu = pack(u), td = pack(dn);
         std::vector<double> sc = pack_scan(c), su = pack_scan(u), sd = pack_scan(dn);
         const size_t bytes = tc.size() * sizeof(double);
-        SCIHPC_CUDA(cudaMalloc(&ccd[a], 6 * bytes));
+        SCIHPC_CUDA(cudaMalloc(&ccd[a], 3 * bytes));
         up[a] = ccd[a] + tc.size();
         down[a] = up[a] + tc.size();
-        scan_ccd[a] = down[a] + tc.size();
-        scan_up[a] = scan_ccd[a] + tc.size();
-        scan_down[a] = scan_up[a] + tc.size();
         SCIHPC_CUDA(cudaMemcpy(ccd[a], tc.data(), bytes, cudaMemcpyHostToDevice));
         SCIHPC_CUDA(cudaMemcpy(up[a], tu.data(), bytes, cudaMemcpyHostToDevice));
         SCIHPC_CUDA(cudaMemcpy(down[a], td.data(), bytes, cudaMemcpyHostToDevice));
-        SCIHPC_CUDA(cudaMemcpy(scan_ccd[a], sc.data(), bytes, cudaMemcpyHostToDevice));
-        SCIHPC_CUDA(cudaMemcpy(scan_up[a], su.data(), bytes, cudaMemcpyHostToDevice));
-        SCIHPC_CUDA(cudaMemcpy(scan_down[a], sd.data(), bytes, cudaMemcpyHostToDevice));
+        int wpl, C;
+        if (scan_shape(D, a, wpl, C)) {
+            std::vector<double> lc = lane_table(sc, n, wpl, C), lu = lane_table(su, n, wpl, C),
+                                ld = lane_table(sd, n, wpl, C);
+            const size_t lb = lc.size() * sizeof(double);
+            SCIHPC_CUDA(cudaMalloc(&lane_ccd[a], 3 * lb));
+            lane_up[a] = lane_ccd[a] + lc.size();
+            lane_down[a] = lane_up[a] + lc.size();
+            SCIHPC_CUDA(cudaMemcpy(lane_ccd[a], lc.data(), lb, cudaMemcpyHostToDevice));
+            SCIHPC_CUDA(cudaMemcpy(lane_up[a], lu.data(), lb, cudaMemcpyHostToDevice));
+            SCIHPC_CUDA(cudaMemcpy(lane_down[a], ld.data(), lb, cudaMemcpyHostToDevice));
+            lane_wpl[a] = wpl, lane_c[a] = C, lane_n[a] = n;
+        }
     }
     return SCIHPC_OK;
 }
@@ -347,7 +431,9 @@ void CompactOps::release() {
     for (int a = 0; a < 3; ++a) {
         if (ccd[a]) cudaFree(ccd[a]);
         ccd[a] = up[a] = down[a] = nullptr;
-        scan_ccd[a] = scan_up[a] = scan_down[a] = nullptr;
+        if (lane_ccd[a]) cudaFree(lane_ccd[a]);
+        lane_ccd[a] = lane_up[a] = lane_down[a] = nullptr;
+        lane_wpl[a] = lane_c[a] = lane_n[a] = 0;
     }
 }
 

@@ -9,13 +9,30 @@ struct CompactOps {
     double *ccd[3] = {nullptr, nullptr, nullptr};
     double *up[3] = {nullptr, nullptr, nullptr};
     double *down[3] = {nullptr, nullptr, nullptr};
-    // scan form for linescan.cu: per point {L (4), K = -Dinv U (4), Dinv (4)}
-    double *scan_ccd[3] = {nullptr, nullptr, nullptr};
-    double *scan_up[3] = {nullptr, nullptr, nullptr};
-    double *scan_down[3] = {nullptr, nullptr, nullptr};
+    // Tables of the warp-cooperative solves (linescan.cu; lane_table in compact.cu): per point
+    // {L (4), K = -Dinv U (4), Dinv (4)} and the matrix halves of the scan maps, laid out for
+    // the launch shape scan_shape chose when they were built: lane_wpl warps per line, lane_c
+    // points per lane, lines of lane_n points.
+    double *lane_ccd[3] = {nullptr, nullptr, nullptr};
+    double *lane_up[3] = {nullptr, nullptr, nullptr};
+    double *lane_down[3] = {nullptr, nullptr, nullptr};
+    int lane_wpl[3] = {0, 0, 0}, lane_c[3] = {0, 0, 0}, lane_n[3] = {0, 0, 0};
     int build(const Dims &D);
     void release();
 };
+
+// Launch shape of the warp-cooperative solves along axis a: each lane holds a contiguous chunk
+// of C points; when there are few lines (fewer than four per SM) two or four warps share one
+// line, for shorter FP64 dependency chains and more warps in flight.  False for lines longer
+// than 16 points per lane.
+inline bool scan_shape(const Dims &D, int a, int &wpl, int &C) {
+    const long long lines = (long long)D.N[(a + 1) % 3] * D.N[(a + 2) % 3];
+    const int n = D.N[a];
+    wpl = 1;
+    if (lines < 4LL * NUM_SMS) wpl = n >= 192 ? 4 : (n >= 96 ? 2 : 1);
+    C = (n + 32 * wpl - 1) / (32 * wpl);
+    return C <= 16;
+}
 
 // uccd_solver::find_f{x,y,z}: t1/t2 are scratch fields for the down-wind system.
 void launch_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,

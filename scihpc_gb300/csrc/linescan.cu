@@ -8,8 +8,12 @@
 // reduced diagonal block (all fixed per axis, computed once on the host).  Affine maps
 // x -> M x + c compose associatively, so one warp solves one line: each lane composes the
 // maps of its contiguous chunk, a 5-step shuffle scan combines the 32 chunk maps, and each
-// lane then replays its chunk from the value entering it.  The line lives in registers;
-// nothing but the input and the outputs touches memory.  Lines up to 32 * CM points.
+// lane then replays its chunk from the value entering it.  Every matrix M met on the way
+// (chunk products, scan partials) depends on the factorisation and the launch shape only and
+// is precomputed per axis, so the kernel forms the vector halves c alone: about a third of the
+// FP64 work of composing full maps, on a GPU whose FP64 rate bounds these solves.  The line
+// lives in registers; nothing but the input and the outputs touches memory.  Lines up to
+// 32 * 16 points with one warp, 128 * 16 with four.
 #include "common.cuh"
 #include "compact.cuh"
 
@@ -17,77 +21,66 @@ namespace scihpc {
 
 namespace {
 
-struct Aff {
-    double m00, m01, m10, m11, c0, c1;
-};
-
-__device__ __forceinline__ Aff aff_identity() { return {1.0, 0.0, 0.0, 1.0, 0.0, 0.0}; }
-
-// b o a : x -> b(a(x))
-__device__ __forceinline__ Aff compose(const Aff &b, const Aff &a) {
-    Aff r;
-    r.m00 = b.m00 * a.m00 + b.m01 * a.m10;
-    r.m01 = b.m00 * a.m01 + b.m01 * a.m11;
-    r.m10 = b.m10 * a.m00 + b.m11 * a.m10;
-    r.m11 = b.m10 * a.m01 + b.m11 * a.m11;
-    r.c0 = b.m00 * a.c0 + b.m01 * a.c1 + b.c0;
-    r.c1 = b.m10 * a.c0 + b.m11 * a.c1 + b.c1;
-    return r;
-}
-
-__device__ __forceinline__ Aff shfl_up(const Aff &a, int d) {
-    return {__shfl_up_sync(0xffffffffu, a.m00, d), __shfl_up_sync(0xffffffffu, a.m01, d),
-            __shfl_up_sync(0xffffffffu, a.m10, d), __shfl_up_sync(0xffffffffu, a.m11, d),
-            __shfl_up_sync(0xffffffffu, a.c0, d), __shfl_up_sync(0xffffffffu, a.c1, d)};
-}
-
-__device__ __forceinline__ Aff shfl_down(const Aff &a, int d) {
-    return {__shfl_down_sync(0xffffffffu, a.m00, d), __shfl_down_sync(0xffffffffu, a.m01, d),
-            __shfl_down_sync(0xffffffffu, a.m10, d), __shfl_down_sync(0xffffffffu, a.m11, d),
-            __shfl_down_sync(0xffffffffu, a.c0, d), __shfl_down_sync(0xffffffffu, a.c1, d)};
-}
-
 // One system: rhs r[k] (2-vectors) of the lane's points lo .. lo+cnt-1 in, solution out
-// (in place).  tab: per point {L00 L01 L10 L11, K00 K01 K10 K11, D00 D01 D10 D11}.
+// (in place).  lt: the line's tables for this launch shape (lane_table in compact.cu), thread
+// index fastest so that every load of a warp is coalesced: per point of the chunk {L00 L01 L10
+// L11, K00 K01 K10 K11, D00 D01 D10 D11}, then the matrix halves of the chunk and scan maps, so
+// that only the vector halves are formed here; tid: the thread's index within its line.
 template <int CM, int WPL>
-__device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM], const double *__restrict__ tab,
-                                             int lo, int cnt, int n, int lane, int warp, Aff *sh) {
-    // forward: chunk map, warp inclusive scan, replay
-    Aff F = aff_identity();
+__device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM], const double *__restrict__ lt, int tid,
+                                             int lo, int cnt, int n, int C, int lane, int warp, double2 *sh) {
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int T = 32 * WPL;
+    const double *pt = lt + tid;                                 // [k][12][T]
+    const double *me = lt + (size_t)C * 12 * T + tid;            // [48][T]
+    const double *wt = lt + (size_t)C * 12 * T + (size_t)48 * T;  // [WPL][8]
+    // forward: the chunk's map applied to a zero entry vector, inclusive warp scan, replay
+    double c0 = 0.0, c1 = 0.0;
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
             const int i = lo + k;
             if (i == 0) {
-                F = {0.0, 0.0, 0.0, 0.0, r0[k], r1[k]};
+                c0 = r0[k], c1 = r1[k];
             } else {
-                const double *t = tab + (size_t)i * 12;
-                const Aff f = {-t[0], -t[1], -t[2], -t[3], r0[k], r1[k]};
-                F = compose(f, F);
+                const double *t = pt + (size_t)k * 12 * T;
+                const double a = r0[k] - (t[0 * T] * c0 + t[1 * T] * c1);
+                const double b = r1[k] - (t[2 * T] * c0 + t[3 * T] * c1);
+                c0 = a, c1 = b;
             }
         }
     }
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const Aff o = shfl_up(F, d);
-        if (lane >= d) F = compose(F, o);
+    for (int st = 0; st < 5; ++st) {
+        const int d = 1 << st;
+        const double o0 = __shfl_up_sync(FULL, c0, d), o1 = __shfl_up_sync(FULL, c1, d);
+        if (lane >= d) {
+            const double *ml = me + 4 * st * T;
+            const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + c0;
+            const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + c1;
+            c0 = a, c1 = b;
+        }
     }
-    // with several warps per line, warp w enters with the composition of warps 0 .. w-1
-    Aff Pw = aff_identity();
+    double v0 = __shfl_up_sync(FULL, c0, 1), v1 = __shfl_up_sync(FULL, c1, 1);   // v at lo-1
     if (WPL > 1) {
-        if (lane == 31) sh[warp] = F;
+        // warp w enters with the composition of warps 0 .. w-1
+        if (lane == 31) sh[warp] = make_double2(c0, c1);
         __syncthreads();
-        for (int v = 0; v < warp; ++v) Pw = compose(sh[v], Pw);
+        double p0 = 0.0, p1 = 0.0;
+        for (int w = 0; w < warp; ++w) {
+            const double *m = wt + 8 * w;
+            const double a = m[0] * p0 + m[1] * p1 + sh[w].x;
+            const double b = m[2] * p0 + m[3] * p1 + sh[w].y;
+            p0 = a, p1 = b;
+        }
         __syncthreads();
-    }
-    const Aff P = shfl_up(F, 1);
-    double v0 = P.c0, v1 = P.c1;   // v at lo-1 (unused by the lane holding point 0)
-    if (WPL > 1) {
         if (lane == 0) {
-            v0 = Pw.c0, v1 = Pw.c1;
+            v0 = p0, v1 = p1;
         } else {
-            v0 = P.m00 * Pw.c0 + P.m01 * Pw.c1 + P.c0;
-            v1 = P.m10 * Pw.c0 + P.m11 * Pw.c1 + P.c1;
+            const double *ml = me + 20 * T;
+            const double a = ml[0 * T] * p0 + ml[1 * T] * p1 + v0;
+            const double b = ml[2 * T] * p0 + ml[3 * T] * p1 + v1;
+            v0 = a, v1 = b;
         }
     }
 #pragma unroll
@@ -97,63 +90,76 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
             if (i == 0) {
                 v0 = r0[k], v1 = r1[k];
             } else {
-                const double *t = tab + (size_t)i * 12;
-                const double a = r0[k] - (t[0] * v0 + t[1] * v1);
-                const double b = r1[k] - (t[2] * v0 + t[3] * v1);
+                const double *t = pt + (size_t)k * 12 * T;
+                const double a = r0[k] - (t[0 * T] * v0 + t[1 * T] * v1);
+                const double b = r1[k] - (t[2 * T] * v0 + t[3 * T] * v1);
                 v0 = a, v1 = b;
             }
             r0[k] = v0, r1[k] = v1;
         }
     }
-    // backward: chunk map (applied from the chunk end down), reverse warp scan, replay
-    Aff G = aff_identity();
+    // backward: e_i = Dinv_i v_i (kept in r), the chunk's map applied to a zero exit vector,
+    // reverse warp scan, replay
+    double g0 = 0.0, g1 = 0.0;
 #pragma unroll
     for (int k = CM - 1; k >= 0; --k) {
         if (k < cnt) {
             const int i = lo + k;
-            const double *t = tab + (size_t)i * 12;
-            const double e0 = t[8] * r0[k] + t[9] * r1[k], e1 = t[10] * r0[k] + t[11] * r1[k];
+            const double *t = pt + (size_t)k * 12 * T;
+            const double e0 = t[8 * T] * r0[k] + t[9 * T] * r1[k], e1 = t[10 * T] * r0[k] + t[11 * T] * r1[k];
+            r0[k] = e0, r1[k] = e1;
             if (i == n - 1) {
-                G = {0.0, 0.0, 0.0, 0.0, e0, e1};
+                g0 = e0, g1 = e1;
             } else {
-                const Aff g = {t[4], t[5], t[6], t[7], e0, e1};
-                G = compose(g, G);
+                const double a = t[4 * T] * g0 + t[5 * T] * g1 + e0;
+                const double b = t[6 * T] * g0 + t[7 * T] * g1 + e1;
+                g0 = a, g1 = b;
             }
         }
     }
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const Aff o = shfl_down(G, d);
-        if (lane + d < 32) G = compose(G, o);
+    for (int st = 0; st < 5; ++st) {
+        const int d = 1 << st;
+        const double o0 = __shfl_down_sync(FULL, g0, d), o1 = __shfl_down_sync(FULL, g1, d);
+        if (lane + d < 32) {
+            const double *ml = me + (24 + 4 * st) * T;
+            const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + g0;
+            const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + g1;
+            g0 = a, g1 = b;
+        }
     }
-    Aff Sw = aff_identity();   // composition of the warps after this one
+    double x0 = __shfl_down_sync(FULL, g0, 1), x1 = __shfl_down_sync(FULL, g1, 1);   // x at lo+cnt
     if (WPL > 1) {
-        if (lane == 0) sh[warp] = G;
+        // composition of the warps after this one
+        if (lane == 0) sh[warp] = make_double2(g0, g1);
         __syncthreads();
-        for (int v = WPL - 1; v > warp; --v) Sw = compose(sh[v], Sw);
+        double q0 = 0.0, q1 = 0.0;
+        for (int w = WPL - 1; w > warp; --w) {
+            const double *m = wt + 8 * w + 4;
+            const double a = m[0] * q0 + m[1] * q1 + sh[w].x;
+            const double b = m[2] * q0 + m[3] * q1 + sh[w].y;
+            q0 = a, q1 = b;
+        }
         __syncthreads();
-    }
-    const Aff Q = shfl_down(G, 1);
-    double x0 = Q.c0, x1 = Q.c1;   // x at lo+cnt (unused by the lane holding n-1)
-    if (WPL > 1) {
         if (lane == 31) {
-            x0 = Sw.c0, x1 = Sw.c1;
+            x0 = q0, x1 = q1;
         } else {
-            x0 = Q.m00 * Sw.c0 + Q.m01 * Sw.c1 + Q.c0;
-            x1 = Q.m10 * Sw.c0 + Q.m11 * Sw.c1 + Q.c1;
+            const double *ml = me + 44 * T;
+            const double a = ml[0 * T] * q0 + ml[1 * T] * q1 + x0;
+            const double b = ml[2 * T] * q0 + ml[3 * T] * q1 + x1;
+            x0 = a, x1 = b;
         }
     }
 #pragma unroll
     for (int k = CM - 1; k >= 0; --k) {
         if (k < cnt) {
             const int i = lo + k;
-            const double *t = tab + (size_t)i * 12;
-            const double e0 = t[8] * r0[k] + t[9] * r1[k], e1 = t[10] * r0[k] + t[11] * r1[k];
             if (i == n - 1) {
-                x0 = e0, x1 = e1;
+                x0 = r0[k], x1 = r1[k];
             } else {
-                const double a = t[4] * x0 + t[5] * x1 + e0;
-                const double b = t[6] * x0 + t[7] * x1 + e1;
+                const double *t = pt + (size_t)k * 12 * T;
+                const double a = t[4 * T] * x0 + t[5 * T] * x1 + r0[k];
+                const double b = t[6 * T] * x0 + t[7 * T] * x1 + r1[k];
                 x0 = a, x1 = b;
             }
             r0[k] = x0, r1[k] = x1;
@@ -169,9 +175,9 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
 template <int MODE, int CM, int WPL>
 __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, const double *__restrict__ vel,
                                                    double *__restrict__ f1, double *__restrict__ f2,
-                                                   const double *__restrict__ tabA, const double *__restrict__ tabB,
+                                                   const double *__restrict__ ltA, const double *__restrict__ ltB,
                                                    Dims D, int a, int fast, int slow) {
-    __shared__ Aff sh[WPL > 1 ? WPL : 1];
+    __shared__ double2 sh[WPL > 1 ? WPL : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long line = WPL > 1 ? (long long)blockIdx.x : (long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const long long nf = D.N[fast], ns = D.N[slow];
@@ -240,8 +246,9 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
             if (k < cnt && (i < GHC || i > n - 1 - GHC)) f[(long long)i * st] = F(i);
         }
     }
-    solve_system<CM, WPL>(r0, r1, tabA, lo, cnt, n, lane, warp, sh);
-    if (MODE == 1) solve_system<CM, WPL>(q0, q1, tabB, lo, cnt, n, lane, warp, sh);
+    const int tid = WPL > 1 ? int(threadIdx.x) : lane;
+    solve_system<CM, WPL>(r0, r1, ltA, tid, lo, cnt, n, C, lane, warp, sh);
+    if (MODE == 1) solve_system<CM, WPL>(q0, q1, ltB, tid, lo, cnt, n, C, lane, warp, sh);
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
@@ -260,25 +267,25 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
 }
 
 template <int MODE>
-bool launch_scan(const Dims &D, int a, double *io, const double *vel, double *f1, double *f2, const double *tA,
-                 const double *tB, cudaStream_t s) {
+bool launch_scan(const Dims &D, const CompactOps &ops, int a, double *io, const double *vel, double *f1, double *f2,
+                 const double *ltA, const double *ltB, cudaStream_t s) {
+    // the shape the matrix tables were built for (scan_shape); none for lines that are too long
+    if (!ltA || ops.lane_n[a] != D.N[a]) return false;
     const int b = (a + 1) % 3, c = (a + 2) % 3;
     const int fast = b > c ? b : c, slow = b > c ? c : b;
     const long long lines = (long long)D.N[b] * D.N[c];
-    const int n = D.N[a];
-    // Each lane's chunk is an FP64 dependency chain.  When there are few lines (fewer than a
-    // few per SM) several warps share a line: shorter chains and more warps in flight.
-    int wpl = 1;
-    if (lines < 4LL * NUM_SMS) wpl = n >= 192 ? 4 : (n >= 96 ? 2 : 1);
-    const int C = (n + 32 * wpl - 1) / (32 * wpl);
+    const int wpl = ops.lane_wpl[a], C = ops.lane_c[a];
     if (wpl > 1) {
         const unsigned blocks = unsigned(lines);
         const int tpb = 32 * wpl;
 #define SCAN_WPL(W)                                                                                              \
-    if (C <= 2) scan_kernel<MODE, 2, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);        \
-    else if (C <= 4) scan_kernel<MODE, 4, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);   \
-    else if (C <= 8) scan_kernel<MODE, 8, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);   \
-    else if (C <= 16) scan_kernel<MODE, 16, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow); \
+    if (C <= 2) scan_kernel<MODE, 2, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow); \
+    else if (C <= 4) scan_kernel<MODE, 4, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast,   \
+                                                                      slow);                                        \
+    else if (C <= 8) scan_kernel<MODE, 8, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast,   \
+                                                                      slow);                                        \
+    else if (C <= 16) scan_kernel<MODE, 16, W><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, \
+                                                                        slow);                                      \
     else return false;
         if (wpl == 2) {
             SCAN_WPL(2)
@@ -293,9 +300,10 @@ bool launch_scan(const Dims &D, int a, double *io, const double *vel, double *f1
     while (wpb < 8 && lines >= (long long)wpb * 2 * 4 * NUM_SMS) wpb *= 2;
     const unsigned blocks = unsigned((lines + wpb - 1) / wpb);
     const int tpb = 32 * wpb;
-    if (C <= 4) scan_kernel<MODE, 4, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
-    else if (C <= 8) scan_kernel<MODE, 8, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
-    else if (C <= 16) scan_kernel<MODE, 16, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, tA, tB, D, a, fast, slow);
+    if (C <= 4) scan_kernel<MODE, 4, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow);
+    else if (C <= 8) scan_kernel<MODE, 8, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow);
+    else if (C <= 16)
+        scan_kernel<MODE, 16, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow);
     else return false;
     return true;
 }
@@ -304,16 +312,16 @@ bool launch_scan(const Dims &D, int a, double *io, const double *vel, double *f1
 
 bool scan_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
                double *f2, cudaStream_t s) {
-    return launch_scan<1>(D, a, const_cast<double *>(flux), vel, f1, f2, ops.scan_up[a], ops.scan_down[a], s);
+    return launch_scan<1>(D, ops, a, const_cast<double *>(flux), vel, f1, f2, ops.lane_up[a], ops.lane_down[a], s);
 }
 
 bool scan_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux, double *f1, double *f2,
               cudaStream_t s) {
-    return launch_scan<0>(D, a, const_cast<double *>(flux), nullptr, f1, f2, ops.scan_ccd[a], nullptr, s);
+    return launch_scan<0>(D, ops, a, const_cast<double *>(flux), nullptr, f1, f2, ops.lane_ccd[a], nullptr, s);
 }
 
 bool scan_mixed(const Dims &D, const CompactOps &ops, int a, double *src, double *out, cudaStream_t s) {
-    return launch_scan<2>(D, a, src, nullptr, out, nullptr, ops.scan_ccd[a], nullptr, s);
+    return launch_scan<2>(D, ops, a, src, nullptr, out, nullptr, ops.lane_ccd[a], nullptr, s);
 }
 
 }  // namespace scihpc

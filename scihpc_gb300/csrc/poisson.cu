@@ -18,6 +18,7 @@
 //     density update, applied as a matrix-vector product).
 // Level hierarchy: the reference's coarsening rule (multigrid.cpp:8-41), so level counts
 // match the reference's multigrid.
+#include <cooperative_groups.h>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -1507,41 +1508,75 @@ __global__ void k_dense_build(Level<T> L, double *__restrict__ M, int n, int neu
     }
 }
 
-__global__ void k_dense_pin_and_invert(double *__restrict__ M, double *__restrict__ W, int n, int neumann) {
-    // W: n x 2n work matrix [M | I]; result inverse written back into M.
+// Gauss-Jordan inverse of the coarsest-level matrix (every entry shifted by mean(diag)/n for
+// Neumann walls, which pins the constant null space).  W is the n x 2n work matrix [M | I]; the
+// inverse is written back into M.  Step k touches only the live columns k+1 .. n+k: the columns
+// left of them are eliminated and no longer read, those right of them are still unit vectors
+// that the step leaves unchanged, so every entry that is read later sees the same operations as
+// in a full-width elimination.  The live columns are split evenly over the launch's blocks (one
+// block, or one cluster for large n): a column is scaled and eliminated by one block within a
+// step, and the cluster barrier between steps publishes column k+1 and the next pivot.
+__global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restrict__ M, double *__restrict__ W, int n,
+                                                               int neumann) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
     __shared__ double piv, scale;
     __shared__ double fac[1024];
     const int t = threadIdx.x, nt = blockDim.x;
-    if (neumann) {
-        if (t == 0) {
-            double s = 0.0;
-            for (int c = 0; c < n; ++c) s += M[(size_t)c * n + c];
-            scale = s / n / n;
+    const int r = int(cluster.block_rank()), nb = int(cluster.num_blocks());   // the grid is one cluster
+    if (t == 0) {
+        double sd = 0.0;
+        if (neumann) {
+            for (int c = 0; c < n; ++c) sd += M[(size_t)c * n + c];
+            sd = sd / n / n;
         }
-        __syncthreads();
-        for (int e = t; e < n * n; e += nt) M[e] += scale;
-        __syncthreads();
-    }
-    const int w = 2 * n;
-    for (int e = t; e < n * w; e += nt) {
-        const int rr = e / w, cc = e % w;
-        W[e] = cc < n ? M[(size_t)rr * n + cc] : (cc - n == rr ? 1.0 : 0.0);
+        scale = sd;
     }
     __syncthreads();
+    const int w = 2 * n;
+    for (long long e = (long long)r * nt + t; e < (long long)n * w; e += (long long)nb * nt) {
+        const int rr = int(e / w), cc = int(e % w);
+        W[e] = cc < n ? (neumann ? M[(size_t)rr * n + cc] + scale : M[(size_t)rr * n + cc]) : (cc - n == rr ? 1.0 : 0.0);
+    }
+    cluster.sync();
+    const int per = (n + nb - 1) / nb;
     for (int k = 0; k < n; ++k) {
+        const int c0 = k + 1 + r * per, c1 = min(c0 + per, n + k + 1), ncol = c1 - c0;
         if (t == 0) piv = 1.0 / W[(size_t)k * w + k];
-        __syncthreads();
-        for (int cc = t; cc < w; cc += nt) W[(size_t)k * w + cc] *= piv;
-        __syncthreads();
         for (int rr = t; rr < n; rr += nt) fac[rr] = W[(size_t)rr * w + k];
         __syncthreads();
-        for (int e = t; e < n * w; e += nt) {
-            const int rr = e / w, cc = e % w;
-            if (rr != k) W[e] -= fac[rr] * W[(size_t)k * w + cc];
+        if (ncol > 0) {
+            for (int cc = c0 + t; cc < c1; cc += nt) W[(size_t)k * w + cc] *= piv;
+            __syncthreads();
+            for (int e = t; e < n * ncol; e += nt) {
+                const int rr = e / ncol, cc = c0 + e % ncol;
+                if (rr != k) W[(size_t)rr * w + cc] -= fac[rr] * W[(size_t)k * w + cc];
+            }
         }
-        __syncthreads();
+        cluster.sync();
     }
-    for (int e = t; e < n * n; e += nt) M[e] = W[(size_t)(e / n) * w + n + e % n];
+    for (long long e = (long long)r * nt + t; e < (long long)n * n; e += (long long)nb * nt)
+        M[e] = W[(size_t)(e / n) * w + n + e % n];
+}
+
+// One block for small coarsest levels; for n >= 128 a cluster of eight blocks (the one-block
+// elimination there is bound by the FP64 rate of a single SM).
+static void launch_dense_invert(double *M, double *W, int n, int neumann, cudaStream_t s) {
+    const unsigned nb = n >= 128 ? 8u : 1u;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nb);
+    cfg.blockDim = dim3(1024);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = nb;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    // a launch error stays the thread's last runtime error, which the caller's check reports
+    (void)cudaLaunchKernelEx(&cfg, k_dense_pin_and_invert, M, W, n, neumann);
 }
 
 // Coarsest-level direct solve x = Minv (b - mean b) in FP64 (mean removed for Neumann walls),
@@ -2255,7 +2290,7 @@ void Poisson::build_coarse(cudaStream_t s) {
     double *M = dense, *W = dense + size_t(ncoarse) * ncoarse;
     if (D.ndim == 2) k_dense_build<T, 2><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, M, ncoarse, neumann);
     else k_dense_build<T, 3><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, M, ncoarse, neumann);
-    k_dense_pin_and_invert<<<1, 1024, 0, s>>>(M, W, ncoarse, neumann);
+    launch_dense_invert(M, W, ncoarse, neumann, s);
 }
 
 static Outer make_outer(const Dims &D, int density, int dirichlet, const double *oc) {

@@ -602,10 +602,20 @@ __global__ void k_dt_part(const double *__restrict__ u, const double *__restrict
 
 __global__ void k_dt_finish(const double *__restrict__ partial, int nb, StepScalars *sc, Dims D, HostParams P,
                             int advance_time) {
-    if (threadIdx.x != 0) return;
+    // Each of the 32 lanes folds a contiguous run of the block partials (independent loads in
+    // flight together), then lane 0 folds the 32 runs in order.
+    __shared__ DtPart runs[32];
     const DtPart *pp = reinterpret_cast<const DtPart *>(partial);
+    const int lane = threadIdx.x;
+    const int per = (nb + 31) / 32;
+    const int q0 = lane * per, q1 = q0 + per < nb ? q0 + per : nb;
+    DtPart run{0.0, 0.0, 0.0, 1.0, 0.0};
+    for (int q = q0; q < q1; ++q) run = dt_combine(run, pp[q]);
+    runs[lane] = run;
+    __syncwarp();
+    if (lane != 0) return;
     DtPart acc{0.0, 0.0, 0.0, 1.0, 0.0};
-    for (int q = 0; q < nb; ++q) acc = dt_combine(acc, pp[q]);
+    for (int l = 0; l < 32; ++l) acc = dt_combine(acc, runs[l]);
     const double mc = fmax(acc.a * 0.0, acc.b);
     const double dx = D.d[0], dy = D.d[1], dz = D.d[2];
     double conv = acc.mu / dx + acc.mv / dy;
