@@ -143,7 +143,7 @@ std::vector<double> pack_scan(const HostLineOp &op) {
 // Tables of the warp-cooperative solve (linescan.cu) for one launch shape: lines of n points,
 // T = 32 * wpl threads per line, thread t holding points t*C .. t*C+C-1.  Thread index fastest,
 // so that a warp's loads are coalesced:
-//   [C][12][T]  the per-point factors {L (4), K (4), Dinv (4)} of point t*C+k (zero past n);
+//   [C][12][T]  the per-point factors {-L (4), K (4), Dinv (4)} of point t*C+k (zero past n);
 //   [48][T]     the matrix halves of the scan maps.  A lane's chunk map and every partial map of
 //               the shuffle scans are affine maps x -> M x + c whose matrices depend only on the
 //               factorisation and the shape, so they are formed here once per axis and the kernel
@@ -168,7 +168,10 @@ std::vector<double> lane_table(const std::vector<double> &tab, int n, int wpl, i
     std::vector<double> out(pts + size_t(T) * 48 + size_t(wpl) * 8, 0.0);
     for (int t = 0; t < T; ++t)
         for (int k = 0; k < C && t * C + k < n; ++k)
-            for (int q = 0; q < 12; ++q) out[(size_t(k) * 12 + q) * T + t] = tab[size_t(t * C + k) * 12 + q];
+            for (int q = 0; q < 12; ++q) {
+                const double x = tab[size_t(t * C + k) * 12 + q];
+                out[(size_t(k) * 12 + q) * T + t] = q < 4 ? -x : x;
+            }
     const Mat2 I = {1.0, 0.0, 0.0, 1.0}, Z = {0.0, 0.0, 0.0, 0.0};
     std::vector<Mat2> F(T), G(T);
     for (int t = 0; t < T; ++t) {

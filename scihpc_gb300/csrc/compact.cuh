@@ -10,7 +10,7 @@ struct CompactOps {
     double *up[3] = {nullptr, nullptr, nullptr};
     double *down[3] = {nullptr, nullptr, nullptr};
     // Tables of the warp-cooperative solves (linescan.cu; lane_table in compact.cu): per point
-    // {L (4), K = -Dinv U (4), Dinv (4)} and the matrix halves of the scan maps, laid out for
+    // {-L (4), K = -Dinv U (4), Dinv (4)} and the matrix halves of the scan maps, laid out for
     // the launch shape scan_shape chose when they were built: lane_wpl warps per line, lane_c
     // points per lane, lines of lane_n points.
     double *lane_ccd[3] = {nullptr, nullptr, nullptr};

@@ -23,8 +23,9 @@ namespace {
 
 // One system: rhs r[k] (2-vectors) of the lane's points lo .. lo+cnt-1 in, solution out
 // (in place).  lt: the line's tables for this launch shape (lane_table in compact.cu), thread
-// index fastest so that every load of a warp is coalesced: per point of the chunk {L00 L01 L10
-// L11, K00 K01 K10 K11, D00 D01 D10 D11}, then the matrix halves of the chunk and scan maps, so
+// index fastest so that every load of a warp is coalesced: per point of the chunk {-L00 -L01
+// -L10 -L11, K00 K01 K10 K11, D00 D01 D10 D11} (L negated: each row of the forward step is two
+// FMAs), then the matrix halves of the chunk and scan maps, so
 // that only the vector halves are formed here; tid: the thread's index within its line.
 template <int CM, int WPL>
 __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM], const double *__restrict__ lt, int tid,
@@ -44,8 +45,8 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
                 c0 = r0[k], c1 = r1[k];
             } else {
                 const double *t = pt + (size_t)k * 12 * T;
-                const double a = r0[k] - (t[0 * T] * c0 + t[1 * T] * c1);
-                const double b = r1[k] - (t[2 * T] * c0 + t[3 * T] * c1);
+                const double a = fma(t[0 * T], c0, fma(t[1 * T], c1, r0[k]));   // t[0..3] = -L
+                const double b = fma(t[2 * T], c0, fma(t[3 * T], c1, r1[k]));
                 c0 = a, c1 = b;
             }
         }
@@ -91,8 +92,8 @@ __device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM],
                 v0 = r0[k], v1 = r1[k];
             } else {
                 const double *t = pt + (size_t)k * 12 * T;
-                const double a = r0[k] - (t[0 * T] * v0 + t[1 * T] * v1);
-                const double b = r1[k] - (t[2 * T] * v0 + t[3 * T] * v1);
+                const double a = fma(t[0 * T], v0, fma(t[1 * T], v1, r0[k]));
+                const double b = fma(t[2 * T], v0, fma(t[3 * T], v1, r1[k]));
                 v0 = a, v1 = b;
             }
             r0[k] = v0, r1[k] = v1;
