@@ -1516,14 +1516,16 @@ __global__ void k_dense_build(Level<T> L, double *__restrict__ M, int n, int neu
 // in a full-width elimination.  The live columns are split evenly over the launch's blocks (one
 // block, or one cluster for large n): a column is scaled and eliminated by one block within a
 // step, and the cluster barrier between steps publishes column k+1 and the next pivot.
-__global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restrict__ M, double *__restrict__ W, int n,
-                                                               int neumann) {
+__global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restrict__ M, double *__restrict__ Wg, int n,
+                                                               int neumann, int in_smem) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ double piv, scale;
     __shared__ double fac[1024];
     const int t = threadIdx.x, nt = blockDim.x;
     const int r = int(cluster.block_rank()), nb = int(cluster.num_blocks());   // the grid is one cluster
+    extern __shared__ double w_smem[];
+    double *W = in_smem ? w_smem : Wg;   // one block and a small level: [M | I] in shared memory
     if (t == 0) {
         double sd = 0.0;
         if (neumann) {
@@ -1538,7 +1540,13 @@ __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restric
         const int rr = int(e / w), cc = int(e % w);
         W[e] = cc < n ? (neumann ? M[(size_t)rr * n + cc] + scale : M[(size_t)rr * n + cc]) : (cc - n == rr ? 1.0 : 0.0);
     }
-    cluster.sync();
+    // one block: a block barrier orders its global writes (the cluster barrier's release /
+    // acquire costs about a microsecond a step)
+    auto step_barrier = [&]() {
+        if (nb > 1) cluster.sync();
+        else __syncthreads();
+    };
+    step_barrier();
     const int per = (n + nb - 1) / nb;
     for (int k = 0; k < n; ++k) {
         const int c0 = k + 1 + r * per, c1 = min(c0 + per, n + k + 1), ncol = c1 - c0;
@@ -1553,20 +1561,24 @@ __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restric
                 if (rr != k) W[(size_t)rr * w + cc] -= fac[rr] * W[(size_t)k * w + cc];
             }
         }
-        cluster.sync();
+        step_barrier();
     }
     for (long long e = (long long)r * nt + t; e < (long long)n * n; e += (long long)nb * nt)
         M[e] = W[(size_t)(e / n) * w + n + e % n];
 }
 
-// One block for small coarsest levels; for n >= 128 a cluster of eight blocks (the one-block
-// elimination there is bound by the FP64 rate of a single SM).
+// One block for small coarsest levels (its work matrix in shared memory when n <= 50); for n >= 128 a cluster
+// of eight blocks (the one-block elimination there is bound by the FP64 rate of a single SM).
 static void launch_dense_invert(double *M, double *W, int n, int neumann, cudaStream_t s) {
     const unsigned nb = n >= 128 ? 8u : 1u;
+    const size_t smem = size_t(n) * 2 * n * sizeof(double);
+    // within the default 48 KB with the 8 KB of static shared memory (n <= 50): no opt-in
+    // attribute, which could otherwise fall inside a stream capture
+    const int in_smem = nb == 1 && smem <= 40 * 1024;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
     cfg.blockDim = dim3(1024);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = in_smem ? smem : 0;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1576,7 +1588,7 @@ static void launch_dense_invert(double *M, double *W, int n, int neumann, cudaSt
     cfg.attrs = at;
     cfg.numAttrs = 1;
     // a launch error stays the thread's last runtime error, which the caller's check reports
-    (void)cudaLaunchKernelEx(&cfg, k_dense_pin_and_invert, M, W, n, neumann);
+    (void)cudaLaunchKernelEx(&cfg, k_dense_pin_and_invert, M, W, n, neumann, in_smem);
 }
 
 // Coarsest-level direct solve x = Minv (b - mean b) in FP64 (mean removed for Neumann walls),
