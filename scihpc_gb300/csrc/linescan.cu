@@ -21,149 +21,192 @@ namespace scihpc {
 
 namespace {
 
-// One system: rhs r[k] (2-vectors) of the lane's points lo .. lo+cnt-1 in, solution out
-// (in place).  lt: the line's tables for this launch shape (lane_table in compact.cu), thread
-// index fastest so that every load of a warp is coalesced: per point of the chunk {-L00 -L01
-// -L10 -L11, K00 K01 K10 K11, D00 D01 D10 D11} (L negated: each row of the forward step is two
-// FMAs), then the matrix halves of the chunk and scan maps, so
-// that only the vector halves are formed here; tid: the thread's index within its line.
-template <int CM, int WPL>
-__device__ __forceinline__ void solve_system(double (&r0)[CM], double (&r1)[CM], const double *__restrict__ lt, int tid,
-                                             int lo, int cnt, int n, int C, int lane, int warp, double2 *sh) {
+// NS independent systems (UCCD's upwind and downwind pair, or one): rhs r[q][k] (2-vectors) of
+// the lane's points lo .. lo+cnt-1 in, solutions out (in place), every phase run for all
+// systems together (independent FP64 chains in flight, one barrier and one shuffle round for
+// both).  lt[q]: the tables of system q for this launch shape (lane_table in compact.cu),
+// thread index fastest so that every load of a warp is coalesced: per point of the chunk
+// {-L00 -L01 -L10 -L11, K00 K01 K10 K11, D00 D01 D10 D11} (L negated: each row of the forward
+// step is two FMAs), then the matrix halves of the chunk and scan maps, so that only the vector
+// halves are formed here; tid: the thread's index within its line.
+template <int NS, int CM, int WPL>
+__device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[2][CM], const double *__restrict__ ltA,
+                                              const double *__restrict__ ltB, int tid, int lo, int cnt, int n, int C,
+                                              int lane, int warp, double2 (*sh)[WPL > 1 ? WPL : 1]) {
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int T = 32 * WPL;
-    const double *pt = lt + tid;                                 // [k][12][T]
-    const double *me = lt + (size_t)C * 12 * T + tid;            // [48][T]
-    const double *wt = lt + (size_t)C * 12 * T + (size_t)48 * T;  // [WPL][8]
+    const double *pt[2], *me[2], *wt[2];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+        const double *lt = q == 0 ? ltA : ltB;
+        pt[q] = lt + tid;                                       // [k][12][T]
+        me[q] = lt + (size_t)C * 12 * T + tid;                  // [48][T]
+        wt[q] = lt + (size_t)C * 12 * T + (size_t)48 * T;       // [WPL][8]
+    }
     // forward: the chunk's map applied to a zero entry vector, inclusive warp scan, replay
-    double c0 = 0.0, c1 = 0.0;
+    double c0[2] = {0.0, 0.0}, c1[2] = {0.0, 0.0};
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
             const int i = lo + k;
-            if (i == 0) {
-                c0 = r0[k], c1 = r1[k];
-            } else {
-                const double *t = pt + (size_t)k * 12 * T;
-                const double a = fma(t[0 * T], c0, fma(t[1 * T], c1, r0[k]));   // t[0..3] = -L
-                const double b = fma(t[2 * T], c0, fma(t[3 * T], c1, r1[k]));
-                c0 = a, c1 = b;
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                if (i == 0) {
+                    c0[q] = r0[q][k], c1[q] = r1[q][k];
+                } else {
+                    const double *t = pt[q] + (size_t)k * 12 * T;
+                    const double a = fma(t[0 * T], c0[q], fma(t[1 * T], c1[q], r0[q][k]));
+                    const double b = fma(t[2 * T], c0[q], fma(t[3 * T], c1[q], r1[q][k]));
+                    c0[q] = a, c1[q] = b;
+                }
             }
         }
     }
 #pragma unroll
     for (int st = 0; st < 5; ++st) {
         const int d = 1 << st;
-        const double o0 = __shfl_up_sync(FULL, c0, d), o1 = __shfl_up_sync(FULL, c1, d);
-        if (lane >= d) {
-            const double *ml = me + 4 * st * T;
-            const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + c0;
-            const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + c1;
-            c0 = a, c1 = b;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            const double o0 = __shfl_up_sync(FULL, c0[q], d), o1 = __shfl_up_sync(FULL, c1[q], d);
+            if (lane >= d) {
+                const double *ml = me[q] + 4 * st * T;
+                const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + c0[q];
+                const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + c1[q];
+                c0[q] = a, c1[q] = b;
+            }
         }
     }
-    double v0 = __shfl_up_sync(FULL, c0, 1), v1 = __shfl_up_sync(FULL, c1, 1);   // v at lo-1
+    double v0[2], v1[2];   // v at lo-1
+#pragma unroll
+    for (int q = 0; q < NS; ++q) v0[q] = __shfl_up_sync(FULL, c0[q], 1), v1[q] = __shfl_up_sync(FULL, c1[q], 1);
     if (WPL > 1) {
         // warp w enters with the composition of warps 0 .. w-1
-        if (lane == 31) sh[warp] = make_double2(c0, c1);
-        __syncthreads();
-        double p0 = 0.0, p1 = 0.0;
-        for (int w = 0; w < warp; ++w) {
-            const double *m = wt + 8 * w;
-            const double a = m[0] * p0 + m[1] * p1 + sh[w].x;
-            const double b = m[2] * p0 + m[3] * p1 + sh[w].y;
-            p0 = a, p1 = b;
+        if (lane == 31) {
+#pragma unroll
+            for (int q = 0; q < NS; ++q) sh[q][warp] = make_double2(c0[q], c1[q]);
         }
         __syncthreads();
-        if (lane == 0) {
-            v0 = p0, v1 = p1;
-        } else {
-            const double *ml = me + 20 * T;
-            const double a = ml[0 * T] * p0 + ml[1 * T] * p1 + v0;
-            const double b = ml[2 * T] * p0 + ml[3 * T] * p1 + v1;
-            v0 = a, v1 = b;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            double p0 = 0.0, p1 = 0.0;
+            for (int w = 0; w < warp; ++w) {
+                const double *m = wt[q] + 8 * w;
+                const double a = m[0] * p0 + m[1] * p1 + sh[q][w].x;
+                const double b = m[2] * p0 + m[3] * p1 + sh[q][w].y;
+                p0 = a, p1 = b;
+            }
+            if (lane == 0) {
+                v0[q] = p0, v1[q] = p1;
+            } else {
+                const double *ml = me[q] + 20 * T;
+                const double a = ml[0 * T] * p0 + ml[1 * T] * p1 + v0[q];
+                const double b = ml[2 * T] * p0 + ml[3 * T] * p1 + v1[q];
+                v0[q] = a, v1[q] = b;
+            }
         }
+        __syncthreads();
     }
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
             const int i = lo + k;
-            if (i == 0) {
-                v0 = r0[k], v1 = r1[k];
-            } else {
-                const double *t = pt + (size_t)k * 12 * T;
-                const double a = fma(t[0 * T], v0, fma(t[1 * T], v1, r0[k]));
-                const double b = fma(t[2 * T], v0, fma(t[3 * T], v1, r1[k]));
-                v0 = a, v1 = b;
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                if (i == 0) {
+                    v0[q] = r0[q][k], v1[q] = r1[q][k];
+                } else {
+                    const double *t = pt[q] + (size_t)k * 12 * T;
+                    const double a = fma(t[0 * T], v0[q], fma(t[1 * T], v1[q], r0[q][k]));
+                    const double b = fma(t[2 * T], v0[q], fma(t[3 * T], v1[q], r1[q][k]));
+                    v0[q] = a, v1[q] = b;
+                }
+                r0[q][k] = v0[q], r1[q][k] = v1[q];
             }
-            r0[k] = v0, r1[k] = v1;
         }
     }
     // backward: e_i = Dinv_i v_i (kept in r), the chunk's map applied to a zero exit vector,
     // reverse warp scan, replay
-    double g0 = 0.0, g1 = 0.0;
+    double g0[2] = {0.0, 0.0}, g1[2] = {0.0, 0.0};
 #pragma unroll
     for (int k = CM - 1; k >= 0; --k) {
         if (k < cnt) {
             const int i = lo + k;
-            const double *t = pt + (size_t)k * 12 * T;
-            const double e0 = t[8 * T] * r0[k] + t[9 * T] * r1[k], e1 = t[10 * T] * r0[k] + t[11 * T] * r1[k];
-            r0[k] = e0, r1[k] = e1;
-            if (i == n - 1) {
-                g0 = e0, g1 = e1;
-            } else {
-                const double a = t[4 * T] * g0 + t[5 * T] * g1 + e0;
-                const double b = t[6 * T] * g0 + t[7 * T] * g1 + e1;
-                g0 = a, g1 = b;
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                const double *t = pt[q] + (size_t)k * 12 * T;
+                const double e0 = t[8 * T] * r0[q][k] + t[9 * T] * r1[q][k];
+                const double e1 = t[10 * T] * r0[q][k] + t[11 * T] * r1[q][k];
+                r0[q][k] = e0, r1[q][k] = e1;
+                if (i == n - 1) {
+                    g0[q] = e0, g1[q] = e1;
+                } else {
+                    const double a = t[4 * T] * g0[q] + t[5 * T] * g1[q] + e0;
+                    const double b = t[6 * T] * g0[q] + t[7 * T] * g1[q] + e1;
+                    g0[q] = a, g1[q] = b;
+                }
             }
         }
     }
 #pragma unroll
     for (int st = 0; st < 5; ++st) {
         const int d = 1 << st;
-        const double o0 = __shfl_down_sync(FULL, g0, d), o1 = __shfl_down_sync(FULL, g1, d);
-        if (lane + d < 32) {
-            const double *ml = me + (24 + 4 * st) * T;
-            const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + g0;
-            const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + g1;
-            g0 = a, g1 = b;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            const double o0 = __shfl_down_sync(FULL, g0[q], d), o1 = __shfl_down_sync(FULL, g1[q], d);
+            if (lane + d < 32) {
+                const double *ml = me[q] + (24 + 4 * st) * T;
+                const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + g0[q];
+                const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + g1[q];
+                g0[q] = a, g1[q] = b;
+            }
         }
     }
-    double x0 = __shfl_down_sync(FULL, g0, 1), x1 = __shfl_down_sync(FULL, g1, 1);   // x at lo+cnt
+    double x0[2], x1[2];   // x at lo+cnt
+#pragma unroll
+    for (int q = 0; q < NS; ++q) x0[q] = __shfl_down_sync(FULL, g0[q], 1), x1[q] = __shfl_down_sync(FULL, g1[q], 1);
     if (WPL > 1) {
         // composition of the warps after this one
-        if (lane == 0) sh[warp] = make_double2(g0, g1);
-        __syncthreads();
-        double q0 = 0.0, q1 = 0.0;
-        for (int w = WPL - 1; w > warp; --w) {
-            const double *m = wt + 8 * w + 4;
-            const double a = m[0] * q0 + m[1] * q1 + sh[w].x;
-            const double b = m[2] * q0 + m[3] * q1 + sh[w].y;
-            q0 = a, q1 = b;
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NS; ++q) sh[q][warp] = make_double2(g0[q], g1[q]);
         }
         __syncthreads();
-        if (lane == 31) {
-            x0 = q0, x1 = q1;
-        } else {
-            const double *ml = me + 44 * T;
-            const double a = ml[0 * T] * q0 + ml[1 * T] * q1 + x0;
-            const double b = ml[2 * T] * q0 + ml[3 * T] * q1 + x1;
-            x0 = a, x1 = b;
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            double p0 = 0.0, p1 = 0.0;
+            for (int w = WPL - 1; w > warp; --w) {
+                const double *m = wt[q] + 8 * w + 4;
+                const double a = m[0] * p0 + m[1] * p1 + sh[q][w].x;
+                const double b = m[2] * p0 + m[3] * p1 + sh[q][w].y;
+                p0 = a, p1 = b;
+            }
+            if (lane == 31) {
+                x0[q] = p0, x1[q] = p1;
+            } else {
+                const double *ml = me[q] + 44 * T;
+                const double a = ml[0 * T] * p0 + ml[1 * T] * p1 + x0[q];
+                const double b = ml[2 * T] * p0 + ml[3 * T] * p1 + x1[q];
+                x0[q] = a, x1[q] = b;
+            }
         }
+        __syncthreads();
     }
 #pragma unroll
     for (int k = CM - 1; k >= 0; --k) {
         if (k < cnt) {
             const int i = lo + k;
-            if (i == n - 1) {
-                x0 = r0[k], x1 = r1[k];
-            } else {
-                const double *t = pt + (size_t)k * 12 * T;
-                const double a = t[4 * T] * x0 + t[5 * T] * x1 + r0[k];
-                const double b = t[6 * T] * x0 + t[7 * T] * x1 + r1[k];
-                x0 = a, x1 = b;
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                if (i == n - 1) {
+                    x0[q] = r0[q][k], x1[q] = r1[q][k];
+                } else {
+                    const double *t = pt[q] + (size_t)k * 12 * T;
+                    const double a = t[4 * T] * x0[q] + t[5 * T] * x1[q] + r0[q][k];
+                    const double b = t[6 * T] * x0[q] + t[7 * T] * x1[q] + r1[q][k];
+                    x0[q] = a, x1[q] = b;
+                }
+                r0[q][k] = x0[q], r1[q][k] = x1[q];
             }
-            r0[k] = x0, r1[k] = x1;
         }
     }
 }
@@ -178,7 +221,7 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
                                                    double *__restrict__ f1, double *__restrict__ f2,
                                                    const double *__restrict__ ltA, const double *__restrict__ ltB,
                                                    Dims D, int a, int fast, int slow) {
-    __shared__ double2 sh[WPL > 1 ? WPL : 1];
+    __shared__ double2 sh[2][WPL > 1 ? WPL : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long line = WPL > 1 ? (long long)blockIdx.x : (long long)blockIdx.x * (blockDim.x >> 5) + warp;
     const long long nf = D.N[fast], ns = D.N[slow];
@@ -200,7 +243,7 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
         return i < GHC ? GHC : (i > n - 1 - GHC ? n - 1 - GHC : i);
     };
     auto F = [&](int i) { return f[(long long)src(i) * st]; };
-    double r0[CM], r1[CM], q0[CM], q1[CM];
+    double r0[2][CM], r1[2][CM];   // [0]: the (upwind) system, [1]: UCCD's downwind system
     const double c3 = -0.06096119008109, c2 = 1.99692238016218, c1 = -1.93596119008109;
     double fm = cnt > 0 && lo > 0 ? F(lo - 1) : 0.0;
     double fc = cnt > 0 ? F(lo) : 0.0;
@@ -221,18 +264,18 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
                     s = -(-3.5 * g0 + 4.0 * g1 - 0.5 * g2) * ih;
                     ss = (9.0 * g0 - 12.0 * g1 + 3.0 * g2) * ih * ih;
                 }
-                r0[k] = s, r1[k] = ss;
-                q0[k] = s, q1[k] = ss;
+                r0[0][k] = s, r1[0][k] = ss;
+                r0[1][k] = s, r1[1][k] = ss;
             } else {
                 const double ss = (3.0 * fm - 6.0 * fc + 3.0 * fp) * ih * ih;
                 if (MODE == 1) {
-                    r0[k] = (c1 * fm + c2 * fc + c3 * fp) * ih;
-                    q0[k] = -(c3 * fm + c2 * fc + c1 * fp) * ih;
-                    q1[k] = ss;
+                    r0[0][k] = (c1 * fm + c2 * fc + c3 * fp) * ih;
+                    r0[1][k] = -(c3 * fm + c2 * fc + c1 * fp) * ih;
+                    r1[1][k] = ss;
                 } else {
-                    r0[k] = 15.0 / 16.0 * (fp - fm) * ih;
+                    r0[0][k] = 15.0 / 16.0 * (fp - fm) * ih;
                 }
-                r1[k] = ss;
+                r1[0][k] = ss;
             }
             fm = fc;
             fc = fp;
@@ -248,20 +291,19 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
         }
     }
     const int tid = WPL > 1 ? int(threadIdx.x) : lane;
-    solve_system<CM, WPL>(r0, r1, ltA, tid, lo, cnt, n, C, lane, warp, sh);
-    if (MODE == 1) solve_system<CM, WPL>(q0, q1, ltB, tid, lo, cnt, n, C, lane, warp, sh);
+    solve_systems<MODE == 1 ? 2 : 1, CM, WPL>(r0, r1, ltA, ltB, tid, lo, cnt, n, C, lane, warp, sh);
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
             const long long o = base + (long long)(lo + k) * st;
             if (MODE == 1) {
-                f1[o] = vel[o] > 0 ? r0[k] : q0[k];
-                f2[o] = 0.5 * (r1[k] + q1[k]);
+                f1[o] = vel[o] > 0 ? r0[0][k] : r0[1][k];
+                f2[o] = 0.5 * (r1[0][k] + r1[1][k]);
             } else if (MODE == 0) {
-                f1[o] = r0[k];
-                f2[o] = r1[k];
+                f1[o] = r0[0][k];
+                f2[o] = r1[0][k];
             } else {
-                f1[o] = r0[k];
+                f1[o] = r0[0][k];
             }
         }
     }
