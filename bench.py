@@ -17,6 +17,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import tempfile
 import statistics
 import subprocess
 import sys
@@ -89,7 +90,7 @@ class Clocks:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f".clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"scihpc_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)

@@ -132,9 +132,10 @@ int scihpc_curvature(scihpc_ctx *ctx, const double *phi, const double *const d[9
  * (synchronises `stream`).  out[0] = mass, out[1] = volume. */
 int scihpc_lsf_integrals(scihpc_ctx *ctx, const double prm[4], const double *phi, double out[2], void *stream);
 
-/* The same integrals for callers that cannot allocate device memory (code running while
- * someone else captures a CUDA graph, plugins whose host owns all device memory, loops that
- * must not touch the allocator).  No context: its scratch lives in a static device array
+/* The same integrals for callers that cannot allocate device memory: plugins whose host
+ * application owns all device memory through its own pool, and real-time loops that must
+ * not touch the allocator (cudaMalloc / cudaFree can synchronise the device).  No context:
+ * its scratch lives in a static device array
  * of 1048576 ghosted cells (8 MiB, held by every GPU that loads the library until exit);
  * larger grids are rejected with SCIHPC_ERR_ARG.  All calls share that array: calls that
  * overlap on the GPU race and must be serialised by the caller.  The first call on each

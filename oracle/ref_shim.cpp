@@ -31,6 +31,7 @@
 #include "godunov_gradient.h"
 #include "multigrid.h"
 #include "second_order_solver.h"
+#include "vtkWriter.h"
 
 namespace {
 
@@ -655,6 +656,30 @@ int ref_sec(int ndim, const int *n, const double *lo, const double *hi, int upwi
     else sec.find_derivatives_all(f);
     DataType ***o[9] = {f->fx, f->fy, f->fz, f->fxx, f->fyy, f->fzz, f->fxy, f->fyz, f->fzx};
     for (int m = 0; m < 9; ++m) save(out + m * N, o[m], d);
+    return 0;
+}
+
+// vtkWriter (vtkWriter.cpp:13-111): <prefix>0.vtk with a scalar, a raw array as a scalar, a
+// vector and three raw arrays as a vector, on the grid [-0.5, 1.5] x [0.25, 2.0] (x [0, 1]);
+// f, u, v, w: ghosted [Nx][Ny][Nz] arrays.
+int ref_vtk_write(int ndim, const int *n, const double *f_in, const double *u, const double *v, const double *w,
+                  const char *prefix) {
+    Dims d = dims_of(ndim, n);
+    const double lo[3] = {-0.5, 0.25, 0.0}, hi[3] = {1.5, 2.0, 1.0};
+    structured_grid *geo = make_grid(ndim, n, lo, hi);
+    scalar_data *f = make_scalar(d);
+    vector_data *vel = make_vector(d);
+    load(f->data, f_in, d);
+    load(vel->x.data, u, d);
+    load(vel->y.data, v, d);
+    load(vel->z.data, w, d);
+    vtkWriter vtk(geo, prefix);
+    vtk.create(0);
+    vtk.add_scalar(f, "phi");
+    vtk.add_scalar(vel->x.data, f, "u_as_scalar");
+    vtk.add_vector(vel, "vel");
+    vtk.add_vector(vel->z.data, vel->y.data, vel->x.data, vel, "vel_swapped");
+    vtk.close();
     return 0;
 }
 

@@ -29,7 +29,7 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
     return e == cudaErrorMemoryAllocation ? SCIHPC_ERR_NOMEM : SCIHPC_ERR_CUDA;
 }
 
-// structured_grid.cpp:7-134 -- d = (end - start) / n, h = min d, dv = prod d.
+// Programmatic dependent launch for the multigrid kernels (on unless SCIHPC_PDL=0).
 bool pdl_enabled() {
     static const bool on = [] {
         const char *e = std::getenv("SCIHPC_PDL");
@@ -38,6 +38,7 @@ bool pdl_enabled() {
     return on;
 }
 
+// structured_grid.cpp:7-134 -- d = (end - start) / n, h = min d, dv = prod d.
 Dims make_dims(const scihpc_grid *g) {
     Dims D{};
     D.ndim = g->ndim;

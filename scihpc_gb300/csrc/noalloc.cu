@@ -1,8 +1,10 @@
 // noalloc.cu -- enclosed mass / volume of a level set without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is being captured
-// by someone else, plugins inside a host application that owns all device memory through
-// its own pool, or real-time loops that must not touch the allocator.  For them this file
+// Some callers cannot call cudaMalloc: plugins inside a host application that owns all
+// device memory through its own pool (a stray cudaMalloc there can exceed the host's
+// memory budget or fragment its pool), and real-time loops that must not touch the
+// allocator (cudaMalloc and cudaFree can synchronise the device and take milliseconds).
+// For them this file
 // offers scihpc_lsf_integrals_noalloc, the same kernels as scihpc_lsf_integrals with their
 // scratch (one product field plus the block partial sums) in a file-scope __device__
 // array instead of a context allocation.

@@ -1516,12 +1516,20 @@ __global__ void k_dense_build(Level<T> L, double *__restrict__ M, int n, int neu
 // in a full-width elimination.  The live columns are split evenly over the launch's blocks (one
 // block, or one cluster for large n): a column is scaled and eliminated by one block within a
 // step, and the cluster barrier between steps publishes column k+1 and the next pivot.
+// static shared memory of k_dense_pin_and_invert: fac[DENSE_FAC] plus piv and scale
+constexpr int DENSE_FAC = 1024;
+constexpr size_t DENSE_STATIC_SMEM = sizeof(double) * (DENSE_FAC + 2);
+// the work matrix goes to dynamic shared memory only while static + dynamic stays within the
+// 48 KB every launch may use without an opt-in attribute
+constexpr size_t DENSE_SMEM_LIMIT = 48 * 1024;
+static_assert(DENSE_STATIC_SMEM < DENSE_SMEM_LIMIT, "dense inverse: static shared memory too large");
+
 __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restrict__ M, double *__restrict__ Wg, int n,
                                                                int neumann, int in_smem) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ double piv, scale;
-    __shared__ double fac[1024];
+    __shared__ double fac[DENSE_FAC];
     const int t = threadIdx.x, nt = blockDim.x;
     const int r = int(cluster.block_rank()), nb = int(cluster.num_blocks());   // the grid is one cluster
     extern __shared__ double w_smem[];
@@ -1572,9 +1580,9 @@ __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restric
 static void launch_dense_invert(double *M, double *W, int n, int neumann, cudaStream_t s) {
     const unsigned nb = n >= 128 ? 8u : 1u;
     const size_t smem = size_t(n) * 2 * n * sizeof(double);
-    // within the default 48 KB with the 8 KB of static shared memory (n <= 50): no opt-in
-    // attribute, which could otherwise fall inside a stream capture
-    const int in_smem = nb == 1 && smem <= 40 * 1024;
+    // within the default 48 KB together with the kernel's static shared memory (n <= 50): no
+    // opt-in attribute, which could otherwise fall inside a stream capture
+    const int in_smem = nb == 1 && smem + DENSE_STATIC_SMEM <= DENSE_SMEM_LIMIT;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nb);
     cfg.blockDim = dim3(1024);

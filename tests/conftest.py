@@ -14,3 +14,6 @@ os.environ.setdefault("OMP_NUM_THREADS", "1")
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: long-running CPU oracle case")
+    # the CPU checkers: the restatement always, the reference where its sources are
+    import oracle
+    oracle.build(ref=True)

@@ -67,8 +67,7 @@ def test_transport_driver_compiles_and_links(driver):
     assert os.path.exists(driver)
 
 
-@pytest.mark.skipif(not O.ref_available() and not os.path.isdir(os.path.join(O.REF_DIR, "scihpc")),
-                    reason="reference sources not present")
+@pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
 @pytest.mark.parametrize("case", CASES)
 def test_oracle_transport_matches_reference_bit_for_bit(case):
     """The restatement of tvd_rk3 with both flux / right-hand-side pairs is the reference's

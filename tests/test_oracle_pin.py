@@ -9,8 +9,7 @@ import pytest
 import oracle as O
 from tests.helpers import bubble_params, bubble_phi, grid2, grid3, smooth_field
 
-pytestmark = pytest.mark.skipif(not (O.ref_available() or O.os.path.isdir(O.os.path.join(O.REF_DIR, "scihpc"))),
-                                reason="reference sources not present")
+pytestmark = pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
 
 
 @pytest.fixture(scope="module")
