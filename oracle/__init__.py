@@ -264,6 +264,10 @@ class TwoPhaseState:
     def set_exact_tol(self, tol: float) -> None:
         self.chk.lib.port_tp_set_exact_tol(self.h, ctypes.c_double(tol))
 
+    def set_fpc_cycles(self, n: int) -> None:
+        """Cycle cap of the restatement's fast pressure correction (the reference's is 100)."""
+        self.chk.lib.port_tp_set_fpc_cycles(self.h, int(n))
+
     def call(self, name: str, *args) -> int:
         return self.chk.fn(f"tp_{name}")(self.h, *args)
 

@@ -239,6 +239,11 @@ int port_tp_set_exact_tol(void *h, double tol) {
     return 0;
 }
 
+int port_tp_set_fpc_cycles(void *h, int n) {
+    static_cast<TwoPhase *>(h)->fpc_max_cycles = n;
+    return 0;
+}
+
 int port_tp_init(void *h) {
     static_cast<TwoPhase *>(h)->init();
     return 0;
@@ -272,7 +277,7 @@ int port_tp_ab_solve(void *h) {
 int port_tp_projection(void *h) {
     auto *tp = static_cast<TwoPhase *>(h);
     tp->ppe_coefficients(false);
-    return tp->projection(tp->ppe_mode == 2);
+    return tp->projection(tp->ppe_mode >= 2);
 }
 int port_tp_step(void *h, int nsteps) {
     static_cast<TwoPhase *>(h)->step(nsteps);

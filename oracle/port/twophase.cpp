@@ -633,8 +633,12 @@ void TwoPhase::pressure_guess() {
     }
 }
 
-// fast_pressure_correction (projection_method.cpp:659-753) on the reference multigrid.
-int TwoPhase::fast_pressure_correction() {
+// fast_pressure_correction (projection_method.cpp:659-753) on the reference multigrid
+// (full_cycle until the absolute residual is at most ppe_tol, at most fpc_max_cycles cycles).
+// exact: the same constant-coefficient equation solved by the CG of coef_cg_solve to
+// exact_tol instead (relative residual; zero-mean solution, as the multigrid's compatibility
+// condition keeps it), for comparisons on converged fields.
+int TwoPhase::fast_pressure_correction(bool exact) {
     const size_t sx = g.stride(0), sy = g.stride(1), sz = g.stride(2);
     const double dt = p.dt, r12 = p.density_ratio;
     MGLevel &L0 = mg.at[0];
@@ -649,17 +653,43 @@ int TwoPhase::fast_pressure_correction() {
                 r += RHS[o];
                 L0.rhs[pos] = r;
             }
-    double err = L0.residual();
-    int it = 0;
-    while (err > p.ppe_tol && it < 100) {
-        ++it;
-        mg.full_cycle();
-        err = L0.residual();
-    }
     Field &pp = pres.data;
-    for (int I = 0; I < g.n[0]; ++I)
-        for (int J = 0; J < g.n[1]; ++J)
-            for (int K = 0; K < g.n[2]; ++K) pp[g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K))] = L0.sol[L0.of(I, J, K)];
+    int it = 0;
+    if (exact) {
+        // the multigrid's Neumann operator (multigrid_base.cpp:236-291) as face coefficients
+        const size_t N = g.size();
+        Field KC(N, 0.0), KR(N, 0.0), KL(N, 0.0), KU(N, 0.0), KD(N, 0.0), KF(N, 0.0), KB(N, 0.0), rhs(N, 0.0);
+        for (int I = 0; I < g.n[0]; ++I)
+            for (int J = 0; J < g.n[1]; ++J)
+                for (int K = 0; K < g.n[2]; ++K) {
+                    const size_t o = g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K));
+                    KR[o] = I < g.n[0] - 1 ? 1.0 / g.d[0] / g.d[0] : 0.0;
+                    KL[o] = I > 0 ? 1.0 / g.d[0] / g.d[0] : 0.0;
+                    KU[o] = J < g.n[1] - 1 ? 1.0 / g.d[1] / g.d[1] : 0.0;
+                    KD[o] = J > 0 ? 1.0 / g.d[1] / g.d[1] : 0.0;
+                    if (g.ndim > 2) {
+                        KF[o] = K < g.n[2] - 1 ? 1.0 / g.d[2] / g.d[2] : 0.0;
+                        KB[o] = K > 0 ? 1.0 / g.d[2] / g.d[2] : 0.0;
+                    }
+                    KC[o] = -(KR[o] + KL[o] + KU[o] + KD[o] + KF[o] + KB[o]);
+                    rhs[o] = L0.rhs[L0.of(I, J, K)];
+                }
+        double rel = 0.0;
+        it = coef_cg_solve(g, KC.data(), KR.data(), KL.data(), KU.data(), KD.data(), KF.data(), KB.data(), rhs.data(),
+                           pp.data(), exact_tol, 200000, &rel);
+        last_relres = rel;
+    } else {
+        double err = L0.residual();
+        while (err > p.ppe_tol && it < fpc_max_cycles) {
+            ++it;
+            mg.full_cycle();
+            err = L0.residual();
+        }
+        for (int I = 0; I < g.n[0]; ++I)
+            for (int J = 0; J < g.n[1]; ++J)
+                for (int K = 0; K < g.n[2]; ++K) pp[g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K))] = L0.sol[L0.of(I, J, K)];
+        last_relres = err;
+    }
     scalar_bc(pp);
     const Field &ph = pres.flux;
     for (int i = 0; i < g.N[0] - 1; ++i)
@@ -690,17 +720,21 @@ void TwoPhase::ab_solve() {
     pres.old = pres.data;
     find_source();
     intermediate_velocity();
+    // ppe_mode 0: the reference's schedule (SOR projection while iter < 5, then the fast
+    // pressure correction); 2: the exact projection every step; 3: the reference's schedule
+    // with both equations solved exactly
+    const bool stock = ppe_mode == 0 || ppe_mode == 3;
     for (int cnt = 0; cnt < p.ppe_initer; ++cnt) {
-        const bool proj = ppe_mode != 0 || p.iter < 5;
+        const bool proj = !stock || p.iter < 5;
         if (proj) {
             if (cnt == 0) ppe_coefficients(false);
-            last_ppe_iters = projection(ppe_mode == 2);
+            last_ppe_iters = projection(ppe_mode >= 2);
         } else {
             if (cnt == 0) {
                 pressure_guess();
                 ppe_coefficients(true);
             }
-            last_ppe_iters = fast_pressure_correction();
+            last_ppe_iters = fast_pressure_correction(ppe_mode == 3);
         }
     }
     node_from_face();

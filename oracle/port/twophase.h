@@ -33,6 +33,9 @@ struct TwoPhase {
     int source_scheme = 0;   // 1: find_source_sec / ab_solve_sec (projection_method.cpp:314-382, 779-801)
     int step_count = 0, last_ppe_iters = 0;
     double exact_tol = 1e-13, last_relres = 0.0;
+    // full_cycle cap of fast_pressure_correction (the reference's loop stops at 100,
+    // projection_method.cpp:697); settable so that the restatement can run it to convergence
+    int fpc_max_cycles = 100;
 
     TwoPhase(const Grid &g, const int *vel_bc, const int *scalar_bc, const Params &p, const int *opt);
 
@@ -72,7 +75,7 @@ struct TwoPhase {
     int projection(bool exact);
     double linfinity() const;
     void pressure_guess();
-    int fast_pressure_correction();
+    int fast_pressure_correction(bool exact = false);
     void ab_solve();
     void init();
     void step(int nsteps);
