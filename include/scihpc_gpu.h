@@ -118,6 +118,14 @@ int scihpc_weno5(scihpc_ctx *ctx, int axis, const double *flux, const double *ve
  * Godunov |grad phi| on interior cells, 0 on ghosts (godunov_gradient.cpp:7-157). */
 int scihpc_godunov_gradient(scihpc_ctx *ctx, const double *phi, const double *sign, double *grad, void *stream);
 
+/* stabilized_upon_gradient (godunov_gradient.cpp:159-181): grad = Godunov |grad phi| as
+ * above, then phi /= max(grad) over every cell, in place.  The maximum is found on the
+ * device (no host synchronisation). */
+int scihpc_stabilized_upon_gradient(scihpc_ctx *ctx, double *phi, const double *sign, double *grad, void *stream);
+
+/* guess_from_history (flux.cpp:653-662): flux = 2 old - old2 on every cell. */
+int scihpc_guess_from_history(scihpc_ctx *ctx, const double *old, const double *old2, double *flux, void *stream);
+
 /* Smoothed Heaviside, delta, sign, density and viscosity of phi on every cell
  * (lsm.cpp:8-43; wrapper_func.cpp:9-40,387-418).  prm = {ls_width, density_ratio,
  * viscosity_ratio, positive_ref}.  Any output may be NULL. */
@@ -207,7 +215,8 @@ int scihpc_twophase_destroy(scihpc_twophase *tp);
 /* Copy one named field between HOST memory and the device state (synchronous).  Names:
  * phi, p, p_old, p_old2, u, v, w (staggered velocity), nu, nv, nw (node velocity), rho,
  * mu, delta, heaviside, curvature, sign, grad, u_src, v_src, w_src, u_src_old, v_src_old,
- * w_src_old, rhs. */
+ * w_src_old, rhs, p_flux (the pressure's flux array: pressure_guess_solution's output),
+ * rhs_fpc (init_ppe_fpc_coefficients' right-hand-side term). */
 int scihpc_twophase_upload(scihpc_twophase *tp, const char *name, const double *host);
 int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host);
 /* Device pointer of a named field (for zero-copy use by callers). */
@@ -248,6 +257,28 @@ int scihpc_twophase_ab_solve(scihpc_twophase *tp, int *iters, double *relres);
 int scihpc_twophase_intermediate_velocity(scihpc_twophase *tp);
 int scihpc_twophase_projection(scihpc_twophase *tp, int *iters, double *relres);
 int scihpc_twophase_node_from_face(scihpc_twophase *tp);
+/* Pressure schedule of ab_solve and of the time step.  schedule 0 (default): the projection
+ * equation above every step.  schedule 1: the reference's schedule (projection_method.cpp:
+ * 755-777): the projection equation while iter < 5, then pressure_guess_solution,
+ * init_ppe_fpc_coefficients and fast_pressure_correction, each solve repeated ppe_initer
+ * times.  tol_mode 0: ppe_tol is a relative residual; 1: the absolute residual 2-norm, as the
+ * reference's loops test it.  The fast correction is capped at 100 iterations as the
+ * reference's loop is (:697); its solver is allocated here (not during capture). */
+int scihpc_twophase_set_ppe_schedule(scihpc_twophase *tp, int schedule, int tol_mode);
+/* The stages of the fast pressure correction one at a time:
+ * pressure_guess_solution (projection_method.cpp:803-815): the pressure's flux array =
+ * old + dt_old (old - old2) / dt_old2 on every cell;
+ * init_ppe_fpc_coefficients (:467-541): the right-hand-side term sum_f C_f (ph_nb - ph_c),
+ * C_f = (1 - density_ratio / rho_f) / d^2, from that flux array and the density;
+ * fast_pressure_correction (:659-753): the constant-coefficient equation (the multigrid's
+ * Neumann operator, multigrid_base.cpp:236-291) with right-hand side density_ratio / dt
+ * div(u*) + that term, solved to ppe_tol (tol_mode of set_ppe_schedule) in at most 100
+ * iterations, the pressure boundary fill and the velocity correction
+ * u -= dt ((dp - dph) / density_ratio + dph / rho_f).  Each synchronises the session's
+ * stream. */
+int scihpc_twophase_pressure_guess(scihpc_twophase *tp);
+int scihpc_twophase_fpc_coefficients(scihpc_twophase *tp);
+int scihpc_twophase_fast_pressure_correction(scihpc_twophase *tp, int *iters, double *relres);
 /* Finer-grained stages for callers that drive the reinitialisation loop themselves, as the
  * reference drivers do (benchmarks_2d_bubble_rising.cpp:122-129): find_sign
  * (wrapper_func.cpp:387-402); one runge_kutta::tvd_rk3 step (runge_kutta.cpp:13-49) with

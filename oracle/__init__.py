@@ -169,6 +169,23 @@ class Checker:
         self.fn("godunov")(g.ndim, n, lo, hi, _p(phi), _p(sign), _p(out))
         return out
 
+    def stabilize(self, g: Grid, phi, sign):
+        """stabilized_upon_gradient: returns (phi / max grad, grad)."""
+        out = np.ascontiguousarray(phi, dtype=np.float64).copy()
+        sign = np.ascontiguousarray(sign, dtype=np.float64)
+        grad = np.zeros(g.shape)
+        n, lo, hi = g.c_args()
+        self.fn("stabilize")(g.ndim, n, lo, hi, _p(out), _p(sign), _p(grad))
+        return out, grad
+
+    def guess_from_history(self, g: Grid, old, old2) -> np.ndarray:
+        old = np.ascontiguousarray(old, dtype=np.float64)
+        old2 = np.ascontiguousarray(old2, dtype=np.float64)
+        out = np.zeros(g.shape)
+        n, _, _ = g.c_args()
+        self.fn("guess_from_history")(g.ndim, n, _p(old), _p(old2), _p(out))
+        return out
+
     def lsf_fields(self, g: Grid, prm, phi) -> np.ndarray:
         phi = np.ascontiguousarray(phi, dtype=np.float64)
         p = np.asarray(prm, dtype=np.float64)

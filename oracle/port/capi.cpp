@@ -1,6 +1,7 @@
 // capi.cpp -- TEST INFRASTRUCTURE (CPU restatement, see port.h).
 // extern "C" entry points of the restatement, with the same argument conventions as the
 // reference shim (oracle/ref_shim.cpp) so that tests can call either through ctypes.
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -76,6 +77,27 @@ int port_godunov(int ndim, const int *n, const double *lo, const double *hi, con
                  double *grad) {
     Grid g = make_grid(ndim, n, lo, hi);
     godunov_gradient(g, phi, sign, grad);
+    return 0;
+}
+
+// stabilized_upon_gradient (godunov_gradient.cpp:159-181): the Godunov gradient, its maximum
+// over every cell (from 0), then phi divided by it on every cell
+int port_stabilize(int ndim, const int *n, const double *lo, const double *hi, double *phi, const double *sign,
+                   double *grad) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    godunov_gradient(g, phi, sign, grad);
+    const size_t N = g.size();
+    double mx = 0.0;
+    for (size_t q = 0; q < N; ++q) mx = std::fmax(mx, grad[q]);
+    for (size_t q = 0; q < N; ++q) phi[q] /= mx;
+    return 0;
+}
+
+// guess_from_history (flux.cpp:653-662): flux = 2 old - old2 on every cell
+int port_guess_from_history(int ndim, const int *n, const double *old, const double *old2, double *flux) {
+    size_t N = 1;
+    for (int a = 0; a < ndim; ++a) N *= size_t(n[a] + 2 * GHC);
+    for (size_t q = 0; q < N; ++q) flux[q] = 2.0 * old[q] - old2[q];
     return 0;
 }
 
@@ -278,6 +300,20 @@ int port_tp_projection(void *h) {
     auto *tp = static_cast<TwoPhase *>(h);
     tp->ppe_coefficients(false);
     return tp->projection(tp->ppe_mode >= 2);
+}
+// the stages of the fast pressure correction one at a time (projection_method.cpp:467-541,
+// 659-753, 803-815); the coefficient stage leaves its right-hand-side term in "rhs"
+int port_tp_pressure_guess(void *h) {
+    static_cast<TwoPhase *>(h)->pressure_guess();
+    return 0;
+}
+int port_tp_fpc_coefficients(void *h) {
+    static_cast<TwoPhase *>(h)->ppe_coefficients(true);
+    return 0;
+}
+int port_tp_fast_pressure_correction(void *h) {
+    auto *tp = static_cast<TwoPhase *>(h);
+    return tp->fast_pressure_correction(tp->ppe_mode == 3);
 }
 int port_tp_step(void *h, int nsteps) {
     static_cast<TwoPhase *>(h)->step(nsteps);

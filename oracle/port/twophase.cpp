@@ -765,6 +765,7 @@ Field *TwoPhase::field(const std::string &s) {
     if (s == "p") return &pres.data;
     if (s == "p_old") return &pres.old;
     if (s == "p_old2") return &pres.old2;
+    if (s == "p_flux") return &pres.flux;
     if (s == "u") return &vel[0].data;
     if (s == "v") return &vel[1].data;
     if (s == "w") return &vel[2].data;

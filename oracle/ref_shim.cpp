@@ -245,6 +245,34 @@ int ref_godunov(int ndim, const int *n, const double *lo, const double *hi, cons
     return 0;
 }
 
+// stabilized_upon_gradient (godunov_gradient.cpp:159-181): grad, then phi /= max(grad), in place.
+int ref_stabilize(int ndim, const int *n, const double *lo, const double *hi, double *phi, const double *sign,
+                  double *grad) {
+    Dims d = dims_of(ndim, n);
+    structured_grid *geo = make_grid(ndim, n, lo, hi);
+    int t[6] = {1, 1, 1, 1, 1, 1};
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    wrapper *w = make_wrapper(true, geo, ndim, t, v);
+    w->link_dummy(dummy_data_alloc(w->scalar));
+    load(w->scalar->data, phi, d);
+    load(w->dummy->sign, sign, d);
+    stabilized_upon_gradient(w);
+    save(grad, w->dummy->grad, d);
+    save(phi, w->scalar->data, d);
+    return 0;
+}
+
+// guess_from_history (flux.cpp:653-662): flux from old and old2.
+int ref_guess_from_history(int ndim, const int *n, const double *old, const double *old2, double *flux) {
+    Dims d = dims_of(ndim, n);
+    scalar_data *f = make_scalar(d);
+    load(f->old, old, d);
+    load(f->old2, old2, d);
+    guess_from_history(f);
+    save(flux, f->flux, d);
+    return 0;
+}
+
 // Level-set property fields (wrapper_func.cpp:9-58,387-418) and the curvature of
 // find_source (projection_method.cpp:258-263 then wrapper_func.cpp:115-174).
 // prm: ls_width, density_ratio, viscosity_ratio, positive_ref.

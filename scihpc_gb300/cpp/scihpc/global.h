@@ -45,8 +45,11 @@ struct problem_parameters {
     DataType Froude_number = -1.0;
     DataType Weber_number = -1.0;
 
-    // ppe_tol is the relative residual the GPU pressure solve iterates to (the reference
-    // uses it as an SOR / multigrid stopping threshold); ppe_max_iter caps its iterations.
+    // ppe_tol: the residual target of the GPU pressure solves -- by default the absolute
+    // residual 2-norm, the reference's multigrid test (projection_method.cpp:697); relative
+    // after scihpc_cpp_set_pressure_schedule(.., 0) (gpu_session.h).  ppe_max_iter caps the
+    // projection solve's iterations (the reference's SOR sweeps), the fast correction stops at
+    // 100 as the reference's does.  ppe_tol2 (SOR's update test) has no GPU counterpart.
     DataType ppe_tol = 1e-4;
     DataType ppe_tol2 = 1e-7;
     int ppe_max_iter = 100;

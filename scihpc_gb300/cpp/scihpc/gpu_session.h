@@ -22,4 +22,14 @@ const char *scihpc_cpp_last_message();
 // (default), 0 = FP64 V-cycles
 void scihpc_cpp_set_pressure_precision(int fp32);
 
+// pressure schedule of sessions created from now on.  schedule 1 (default): ab_solve runs the
+// reference's schedule -- projection() while iter < 5, then pressure_guess_solution,
+// init_ppe_fpc_coefficients and fast_pressure_correction, ppe_initer times each
+// (projection_method.cpp:755-777); schedule 0: projection()'s equation every step.
+// tol_mode 1 (default): ppe_tol is an absolute residual 2-norm, as the reference's multigrid
+// loop tests it (projection_method.cpp:697); tol_mode 0: a relative residual.  Either way the
+// GPU solves run multigrid-preconditioned CG, not SOR sweeps or full_cycle iterations, so
+// their iterates differ from the reference's; at convergence the fields agree.
+void scihpc_cpp_set_pressure_schedule(int schedule, int tol_mode);
+
 #endif

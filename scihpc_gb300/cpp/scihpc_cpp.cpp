@@ -52,6 +52,9 @@ namespace {
 int g_status = 0;
 std::string g_message;
 int g_pressure_fp32 = 1;
+// pressure schedule and tolerance of sessions (scihpc_cpp_set_pressure_schedule): the
+// reference's ab_solve schedule with its absolute residual test by default
+int g_schedule = 1, g_tol_mode = 1;
 
 void fail(int code, const std::string &msg) {
     g_status = code;
@@ -78,6 +81,10 @@ DataType *base_of(DataType ***a) { return a[0][0]; }   // init_array storage is 
 int scihpc_cpp_last_status() { return g_status; }
 const char *scihpc_cpp_last_message() { return g_message.c_str(); }
 void scihpc_cpp_set_pressure_precision(int fp32) { g_pressure_fp32 = fp32 ? 1 : 0; }
+void scihpc_cpp_set_pressure_schedule(int schedule, int tol_mode) {
+    g_schedule = schedule ? 1 : 0;
+    g_tol_mode = tol_mode ? 1 : 0;
+}
 
 // ---------------------------------------------------------------- global.h
 DataType ***init_array(int Nx, int Ny, int Nz) {
@@ -208,7 +215,14 @@ indices scalar_data::index_mapping(int i, int j, int k) {
     return r;
 }
 
+namespace {
+bool session_store(const scalar_data *f);
+}
+
+// old2 <- old <- data (scalar_data.cpp:125-135); a pressure held by a GPU session moves its
+// history on the device too (pressure_guess_solution reads it there)
 void scalar_data::store() const {
+    if (session_store(this)) return;
     const size_t n = cells_of(this);
     std::memcpy(base_of(old2), base_of(old), n * sizeof(DataType));
     std::memcpy(base_of(old), base_of(data), n * sizeof(DataType));
@@ -288,6 +302,20 @@ bool attach_pressure(Session *s, wrapper *p) {
     return upload(s, "p", p->scalar->data);
 }
 
+// scalar_data::store of a pressure held by a session: the shift old2 <- old <- data on the
+// device arrays, and the host arrays brought up to date with them
+bool session_store(const scalar_data *f) {
+    auto it = g_mirrors.find(f->data);
+    if (it == g_mirrors.end() || it->second.name != "p") return false;
+    Session *s = it->second.s;
+    const size_t n = cells_of(f);
+    if (!download(s, "p", f->data) || !download(s, "p_old", f->old)) return true;
+    std::memcpy(base_of(f->old2), base_of(f->old), n * sizeof(DataType));
+    std::memcpy(base_of(f->old), base_of(f->data), n * sizeof(DataType));
+    upload(s, "p_old", f->old) && upload(s, "p_old2", f->old2);
+    return true;
+}
+
 // host scalars -> device (the drivers advance t and iter and set lsf_mass0 on the host)
 bool push_scalars(Session *s) {
     const problem_parameters *p = s->params;
@@ -342,6 +370,11 @@ Session *session_for(wrapper *phi, wrapper *vel, wrapper *nvel, wrapper *pressur
                             double(p->ppe_max_iter), p->ppe_omega, double(p->ppe_initer), p->dt};
     const int opt[5] = {0, 0, 0, g_pressure_fp32, 1};
     if (!check(scihpc_twophase_create(&g, vbc, sbc, prm, opt, &s->tp), "twophase_create")) {
+        delete s;
+        return nullptr;
+    }
+    if (!check(scihpc_twophase_set_ppe_schedule(s->tp, g_schedule, g_tol_mode), "set_ppe_schedule")) {
+        scihpc_twophase_destroy(s->tp);
         delete s;
         return nullptr;
     }
@@ -858,7 +891,12 @@ void identity_old_flux(scalar_data *f) { host_copy(f->flux, f->old, f); }
 void identity_old_flux(vector_data *v) {
     for (scalar_data *c : {&v->x, &v->y, &v->z}) host_copy(c->flux, c->old, c);
 }
-void guess_from_history(scalar_data *) { unsupported("guess_from_history", "no GPU stage (2 old - old2)"); }
+void guess_from_history(scalar_data *f) {
+    HostCall c(grid_of_sizes(f), f);
+    double *o = c.in(f->old), *o2 = c.in(f->old2), *fl = c.out(f->flux);
+    if (c.ok) c.run(scihpc_guess_from_history(c.ctx, o, o2, fl, nullptr), "guess_from_history");
+    c.finish();
+}
 
 void burgers_flux(scalar_data *f, vector_data *) {
     HostCall c(grid_of_sizes(f), f);
@@ -1258,18 +1296,33 @@ void projection_method::projection(wrapper *pressure, wrapper *lsf, wrapper *) c
     pull_scalars(s);
 }
 
-// The reference's fast pressure correction iterates a constant-coefficient equation; the GPU
-// solves the variable-coefficient equation of projection() to ppe_tol instead.
-void projection_method::fast_pressure_correction(wrapper *pressure, wrapper *lsf, wrapper *vel) {
-    projection(pressure, lsf, vel);
+// the constant-coefficient equation with the extrapolated pressure's variable-density term
+// on its right-hand side (projection_method.cpp:659-753), on the GPU multigrid
+void projection_method::fast_pressure_correction(wrapper *pressure, wrapper *lsf, wrapper *) {
+    Session *s = stage_session(lsf, "fast_pressure_correction");
+    if (!s || !attach_pressure(s, pressure)) return;
+    const int rc = scihpc_twophase_fast_pressure_correction(s->tp, &last_iterations, &last_relres);
+    if (rc == SCIHPC_ERR_MAXITER) fail(rc, "fast_pressure_correction: stopped at 100 iterations above ppe_tol");
+    else if (!check(rc, "fast_pressure_correction")) return;
+    pull_scalars(s);
 }
 
-// the GPU builds the coefficients from the density inside projection()
+// the GPU builds projection()'s coefficients from the density inside projection()
 void projection_method::init_ppe_proj_coefficients(wrapper *) {}
-void projection_method::init_ppe_fpc_coefficients(wrapper *) {}
 
-void projection_method::pressure_guess_solution(wrapper *) {
-    unsupported("pressure_guess_solution", "the GPU pressure solve starts from the previous pressure");
+// the right-hand-side term of the fast correction from the extrapolated pressure and the
+// density (projection_method.cpp:467-541)
+void projection_method::init_ppe_fpc_coefficients(wrapper *pressure) {
+    Session *s = stage_session(pressure, "init_ppe_fpc_coefficients");
+    if (!s || !attach_pressure(s, pressure)) return;
+    check(scihpc_twophase_fpc_coefficients(s->tp), "init_ppe_fpc_coefficients");
+}
+
+// flux = old + dt_old (old - old2) / dt_old2 (projection_method.cpp:803-815)
+void projection_method::pressure_guess_solution(wrapper *pressure) {
+    Session *s = stage_session(pressure, "pressure_guess_solution");
+    if (!s || !attach_pressure(s, pressure)) return;
+    check(scihpc_twophase_pressure_guess(s->tp), "pressure_guess_solution");
 }
 void projection_method::add_stress_x(wrapper *, wrapper *, wrapper *) const {
     unsupported("add_stress_x", "a stage inside the GPU find_source");
@@ -1382,9 +1435,16 @@ void godunov_gradient(wrapper *f) {
     c.finish();
 }
 
+// godunov_gradient, then phi /= max |grad phi| (godunov_gradient.cpp:159-181)
 void stabilized_upon_gradient(wrapper *f) {
-    godunov_gradient(f);
-    unsupported("stabilized_upon_gradient", "the rescale by max |grad phi| has no GPU stage");
+    if (!f->dummy) {
+        fail(SCIHPC_ERR_ARG, "stabilized_upon_gradient: wrapper not linked to dummy_data");
+        return;
+    }
+    HostCall c(grid_of(f->geo), f->scalar);
+    double *phi = c.out(f->scalar->data), *sg = c.in(f->dummy->sign), *g = c.out(f->dummy->grad);
+    if (c.ok) c.run(scihpc_stabilized_upon_gradient(c.ctx, phi, sg, g, nullptr), "stabilized_upon_gradient");
+    c.finish();
 }
 
 void find_sign(wrapper *lsf) {

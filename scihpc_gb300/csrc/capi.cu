@@ -264,6 +264,20 @@ int scihpc_godunov_gradient(scihpc_ctx *ctx, const double *phi, const double *si
     return SCIHPC_OK;
 }
 
+int scihpc_stabilized_upon_gradient(scihpc_ctx *ctx, double *phi, const double *sign, double *grad, void *stream) {
+    REQUIRE(ctx && phi && sign && grad, "stabilized_upon_gradient: NULL argument");
+    launch_stabilize(ctx->D, phi, sign, grad, ctx->partial, ctx->red + 2, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
+int scihpc_guess_from_history(scihpc_ctx *ctx, const double *old, const double *old2, double *flux, void *stream) {
+    REQUIRE(ctx && old && old2 && flux, "guess_from_history: NULL argument");
+    launch_guess_from_history(ctx->D, old, old2, flux, S(stream));
+    CHECK_LAUNCH();
+    return SCIHPC_OK;
+}
+
 int scihpc_lsf_fields(scihpc_ctx *ctx, const double prm[4], const double *phi, double *heaviside, double *delta,
                       double *sign, double *density, double *viscosity, void *stream) {
     REQUIRE(ctx && prm && phi, "lsf_fields: NULL argument");
@@ -529,6 +543,28 @@ int scihpc_twophase_projection(scihpc_twophase *tp, int *iters, double *relres) 
 int scihpc_twophase_node_from_face(scihpc_twophase *tp) {
     REQUIRE(tp, "twophase_node_from_face: NULL argument");
     return tp->tp.node_from_face();
+}
+
+int scihpc_twophase_set_ppe_schedule(scihpc_twophase *tp, int schedule, int tol_mode) {
+    REQUIRE(tp, "twophase_set_ppe_schedule: NULL argument");
+    REQUIRE(schedule == 0 || schedule == 1, "twophase_set_ppe_schedule: schedule must be 0 (projection) or 1 (stock)");
+    REQUIRE(tol_mode == 0 || tol_mode == 1, "twophase_set_ppe_schedule: tol_mode must be 0 (relative) or 1 (absolute)");
+    return tp->tp.set_ppe_schedule(schedule, tol_mode);
+}
+
+int scihpc_twophase_pressure_guess(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_pressure_guess: NULL argument");
+    return tp->tp.pressure_guess();
+}
+
+int scihpc_twophase_fpc_coefficients(scihpc_twophase *tp) {
+    REQUIRE(tp, "twophase_fpc_coefficients: NULL argument");
+    return tp->tp.fpc_coefficients();
+}
+
+int scihpc_twophase_fast_pressure_correction(scihpc_twophase *tp, int *iters, double *relres) {
+    REQUIRE(tp, "twophase_fast_pressure_correction: NULL argument");
+    return tp->tp.fast_pressure_correction(iters, relres);
 }
 
 int scihpc_twophase_step(scihpc_twophase *tp, int nsteps, int use_graph, int sync) {

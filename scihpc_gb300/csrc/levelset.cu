@@ -163,7 +163,48 @@ __global__ void integral_kernel(const double *__restrict__ w, Dims D, int which,
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
+// max over every cell of grad (>= 0; ghosts hold 0), block partials for finish_reduce<MaxOp>
+// (godunov_gradient.cpp:161-170: fmax from 0.0, in any order the same value)
+__global__ void max_kernel(const double *__restrict__ g, long long n, double *__restrict__ partial) {
+    __shared__ double sh[RED_THREADS];
+    const long long per_block = (n + gridDim.x - 1) / gridDim.x;
+    const long long b0 = blockIdx.x * per_block;
+    const long long b1 = b0 + per_block < n ? b0 + per_block : n;
+    double m = 0.0;
+    for (long long q = b0 + threadIdx.x; q < b1; q += blockDim.x) m = fmax(m, g[q]);
+    m = block_reduce<MaxOp>(m, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+}
+
+// phi /= max |grad phi| on every cell (godunov_gradient.cpp:172-180)
+__global__ void rescale_kernel(double *__restrict__ phi, long long n, const double *__restrict__ mx) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    phi[q] = __ddiv_rn(phi[q], *mx);
+}
+
+// guess_from_history (flux.cpp:653-662): flux = 2 old - old2 on every cell
+__global__ void history_kernel(const double *__restrict__ old, const double *__restrict__ old2,
+                               double *__restrict__ flux, long long n) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    flux[q] = __dsub_rn(__dmul_rn(2.0, old[q]), old2[q]);
+}
+
 }  // namespace
+
+void launch_stabilize(const Dims &D, double *phi, const double *sign, double *grad, double *partial, double *mx,
+                      cudaStream_t s) {
+    launch_godunov(D, phi, sign, grad, s);
+    const int nb = red_blocks(D.size());
+    max_kernel<<<nb, RED_THREADS, 0, s>>>(grad, D.size(), partial);
+    finish_reduce<MaxOp><<<1, 1024, 0, s>>>(partial, nb, mx);
+    rescale_kernel<<<blocks_for(D.size(), 256), 256, 0, s>>>(phi, D.size(), mx);
+}
+
+void launch_guess_from_history(const Dims &D, const double *old, const double *old2, double *flux, cudaStream_t s) {
+    history_kernel<<<blocks_for(D.size(), 256), 256, 0, s>>>(old, old2, flux, D.size());
+}
 
 void launch_weno5(const Dims &D, int a, const double *flux, const double *vel, double *out, cudaStream_t s) {
     weno_kernel<<<blocks_for(D.interior(), 128), 128, 0, s>>>(flux, vel, out, D, a);

@@ -327,10 +327,10 @@ __global__ void k_axpy(double *__restrict__ p, double *__restrict__ r, const dou
 // declared on the true residual.
 template <int DIM, class T>
 __global__ void k_replace(const double *__restrict__ rhs, const double *__restrict__ p, Outer O,
-                          double *__restrict__ r, Level<T> L0, double tol, RedSlot slot, PcgScalars *st) {
+                          double *__restrict__ r, Level<T> L0, RedSlot slot, PcgScalars *st) {
     pdl_wait();
     pdl_trigger();
-    if (st->done || !(st->rr <= tol * tol * st->bb)) return;
+    if (st->done || !(st->rr <= st->tol * st->tol * st->bb)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->restart = 1;
     const double mean = O.dirichlet ? 0.0 : st->mean / double(O.n);
     double v[1] = {0.0};
@@ -356,7 +356,8 @@ __device__ __forceinline__ void set_cond(unsigned long long handle, int use_hand
 #endif
 }
 
-__device__ __forceinline__ void outer_progress(PcgScalars *st, double tol, int max_iter, int first) {
+__device__ __forceinline__ void outer_progress(PcgScalars *st, int max_iter, int first) {
+    const double tol = st->tol;
     const double rel = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0;
     st->relres = rel;
     if (first || rel < st->best) {
@@ -369,10 +370,15 @@ __device__ __forceinline__ void outer_progress(PcgScalars *st, double tol, int m
     st->done = (rel <= tol || st->it >= max_iter || st->diverged || st->since_best >= 3) ? 1 : 0;
 }
 
-__global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, unsigned long long handle,
+// advance = 0 (the check after begin) also fixes the relative target of the solve:
+// max(rel_tol, abs_tol / ||g||) once ||g|| is known.
+__global__ void k_check(PcgScalars *st, double rel_tol, int max_iter, int advance, unsigned long long handle,
                         int use_handle) {
     pdl_wait();
     pdl_trigger();
+    if (!advance)
+        st->tol = (st->abs_tol > 0.0 && st->bb > 0.0) ? fmax(rel_tol, st->abs_tol / sqrt(st->bb)) : rel_tol;
+    const double tol = st->tol;
     if (advance) {
         if (st->done) {
             set_cond(handle, use_handle, 0);
@@ -381,7 +387,7 @@ __global__ void k_check(PcgScalars *st, double tol, int max_iter, int advance, u
         st->rz_prev = st->rz;
         st->it += 1;
     }
-    outer_progress(st, tol, max_iter, !advance);
+    outer_progress(st, max_iter, !advance);
     if (advance && st->in_break) st->done = 1;   // breakdown of the FP64 recurrence (k_axpy)
     st->rr_in0 = st->rr;
     st->in_target = fmax(st->in_tol, 0.25 * tol / fmax(st->relres, 1e-300));
@@ -417,7 +423,10 @@ __global__ void k_true_res(const double *__restrict__ rhs, const double *__restr
     grid_sum<1>(v, slot, o);
 }
 
-__global__ void k_set_inner(PcgScalars *st, double in_tol) { st->in_tol = in_tol; }
+__global__ void k_set_inner(PcgScalars *st, double in_tol, double abs_tol) {
+    st->in_tol = in_tol;
+    st->abs_tol = abs_tol;
+}
 
 __global__ void k_relres(PcgScalars *st) { st->relres = st->bb > 0.0 ? sqrt(st->rr / st->bb) : 0.0; }
 
@@ -1884,15 +1893,16 @@ __global__ void k_out_res(const double *__restrict__ rhs, const double *__restri
 }
 
 // refinement, part 3: convergence on the FP64 residual; drives the conditional while-node
-__global__ void k_out_check(PcgScalars *st, double tol, int max_iter, unsigned long long handle, int use_handle) {
+__global__ void k_out_check(PcgScalars *st, int max_iter, unsigned long long handle, int use_handle) {
     pdl_wait();
     pdl_trigger();
+    const double tol = st->tol;
     if (st->done) {
         set_cond(handle, use_handle, 0);
         return;
     }
     if (st->pending) {
-        outer_progress(st, tol, max_iter, 0);
+        outer_progress(st, max_iter, 0);
         st->in_it = 0;
         st->in_break = 0;
         st->rr_in0 = st->rr;
@@ -2558,7 +2568,7 @@ void Poisson::begin_dim(const double *rhs, double *p, int use_guess, cudaStream_
     RedSlot slot{partial, reinterpret_cast<unsigned *>(partial + 2 * RED_MAX_BLOCKS)};
     const int nb = grid_blocks(D.interior());
     cudaMemsetAsync(dev_state, 0, sizeof(PcgScalars), s);
-    k_set_inner<<<1, 1, 0, s>>>(dev_state, inner_tol);
+    k_set_inner<<<1, 1, 0, s>>>(dev_state, inner_tol, abs_tol);
     if (bc_ == 0) k_rhs_sum<DIM><<<nb, TPB, 0, s>>>(rhs, O, slot, &dev_state->mean);
     if (fp32_) {
         cudaMemsetAsync(e32, 0, size_t(Lf[0].cells) * sizeof(float), s);
@@ -2601,7 +2611,7 @@ void Poisson::iterate_dim(cudaStream_t s) {
         launch_pdl(pdl, k_in_check, 1, 1, 0, s, dev_state, inner_max, max_iter);
         launch_pdl(pdl, k_out_add<DIM>, nb, TPB, 0, s, p_, e32, O, L0, dev_state);
         launch_pdl(pdl, k_out_res<DIM>, nb, TPB, 0, s, rhs_, p_, O, L0, e32, slot, dev_state);
-        launch_pdl(pdl, k_out_check, 1, 1, 0, s, dev_state, rel_tol, max_iter, conditional, uc);
+        launch_pdl(pdl, k_out_check, 1, 1, 0, s, dev_state, max_iter, conditional, uc);
         return;
     }
     Level<double> &L0 = Ld[0];
@@ -2610,7 +2620,7 @@ void Poisson::iterate_dim(cudaStream_t s) {
     launch_pdl(pdl, k_update_d<DIM, double>, nb, TPB, 0, s, L0.x, (double *)zold, dvec, O, L0, dev_state);
     launch_pdl(pdl, k_apply_dq<DIM>, nb, TPB, 0, s, dvec, q, O, slot, dev_state);
     launch_pdl(pdl, k_axpy<DIM, double>, nb, TPB, 0, s, p_, r, dvec, q, O, L0, slot, dev_state);
-    launch_pdl(pdl, k_replace<DIM, double>, nb, TPB, 0, s, rhs_, p_, O, r, L0, rel_tol, slot, dev_state);
+    launch_pdl(pdl, k_replace<DIM, double>, nb, TPB, 0, s, rhs_, p_, O, r, L0, slot, dev_state);
     launch_pdl(pdl, k_check, 1, 1, 0, s, dev_state, rel_tol, max_iter, 1, conditional, uc);
 }
 
@@ -2699,7 +2709,7 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
     if (graph) {
         SolveKey key;
         key.rhs = rhs, key.p = p, key.use_guess = use_guess, key.max_iter = maxit, key.inner_max = inner_max;
-        key.prolong_linear = prolong_linear, key.rel_tol = tol, key.inner_tol = inner_tol;
+        key.prolong_linear = prolong_linear, key.rel_tol = tol, key.inner_tol = inner_tol, key.abs_tol = abs_tol;
         // a solve whose inputs were seen on the previous call is captured (and then replayed
         // while they stay the same); a one-off solve runs the host loop and pays no capture
         if (solve_exec && key == solve_key) {
@@ -2741,7 +2751,7 @@ int Poisson::solve(const double *rhs, double *p, int use_guess, double tol, int 
         set_last_error("pressure solve produced a non-finite residual");
         return SCIHPC_ERR_NONFINITE;
     }
-    if (host_state->relres > tol && it >= maxit) return SCIHPC_ERR_MAXITER;
+    if (host_state->relres > host_state->tol && it >= maxit) return SCIHPC_ERR_MAXITER;
     return SCIHPC_OK;
 }
 

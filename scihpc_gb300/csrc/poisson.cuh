@@ -46,6 +46,8 @@ struct PcgScalars {
     int in_break;           // the inner recurrence broke down (FP32 round-off)
     int restart;            // FP64 CG: the residual was replaced, next direction restarts
     int sweep_err;          // a staged sweep timed out waiting for its planes
+    double abs_tol;         // absolute residual target (0: none)
+    double tol;             // relative target in force: max(rel_tol, abs_tol / ||g||), set at begin
 };
 
 class Poisson {
@@ -75,6 +77,10 @@ public:
     int fp32() const { return fp32_; }
 
     double rel_tol = 1e-10;
+    // absolute target: the solve also stops once ||g - L p|| <= abs_tol (2-norm over the
+    // interior; 0 = relative target only).  The reference's multigrid loops stop on this
+    // absolute residual (projection_method.cpp:695-697).
+    double abs_tol = 0.0;
     int max_iter = 200;
     PcgScalars *dev_state = nullptr;    // device
     PcgScalars *host_state = nullptr;   // pinned mirror
@@ -115,11 +121,11 @@ private:
         const double *rhs = nullptr;
         double *p = nullptr;
         int use_guess = 0, max_iter = 0, inner_max = 0, prolong_linear = 0;
-        double rel_tol = 0.0, inner_tol = 0.0;
+        double rel_tol = 0.0, inner_tol = 0.0, abs_tol = 0.0;
         bool operator==(const SolveKey &o) const {
             return rhs == o.rhs && p == o.p && use_guess == o.use_guess && max_iter == o.max_iter &&
                    inner_max == o.inner_max && prolong_linear == o.prolong_linear && rel_tol == o.rel_tol &&
-                   inner_tol == o.inner_tol;
+                   inner_tol == o.inner_tol && abs_tol == o.abs_tol;
         }
     };
     cudaGraphExec_t solve_exec = nullptr;

@@ -542,6 +542,90 @@ __global__ void k_correct(double *__restrict__ u, double *__restrict__ v, double
     }
 }
 
+// ---------------------------------------------------------------- fast pressure correction
+// The reference's schedule from the fifth step on (projection_method.cpp:755-777): the
+// pressure is extrapolated in time (pressure_guess_solution), the variable-density term is
+// moved to the right-hand side with that extrapolation (init_ppe_fpc_coefficients), and a
+// constant-coefficient equation is solved (fast_pressure_correction).  Products and sums are
+// rounded separately (no fused multiply-add), as the reference's CPU build rounds them.
+
+// pressure_guess_solution (projection_method.cpp:803-815), every cell:
+// flux = old + dt_old (old - old2) / dt_old2
+__global__ void k_pressure_guess(double *__restrict__ fl, const double *__restrict__ old,
+                                 const double *__restrict__ old2, long long n, const StepScalars *sc) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double dpdt = __ddiv_rn(__dsub_rn(old[q], old2[q]), sc->dt_old2);
+    fl[q] = __dadd_rn(old[q], __dmul_rn(sc->dt_old, dpdt));
+}
+
+// init_ppe_fpc_coefficients (projection_method.cpp:467-541), interior cells:
+// C_f = (1 - rho12 / rho_f) / d^2 (0 on wall faces), CC = -sum C_f,
+// RHS = CC ph_c + C_R ph_R + C_L ph_L + C_U ph_U + C_D ph_D [+ (C_F ph_F + C_B ph_B)]
+__global__ void k_fpc_coefficients(double *__restrict__ out, const double *__restrict__ ph,
+                                   const double *__restrict__ Rho, Dims D, double r12) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.interior()) return;
+    int I, J, K;
+    split3(q, D, I, J, K);
+    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+    auto coef = [&](long long st, double d, bool wall) {
+        if (wall) return 0.0;
+        const double rf = __dmul_rn(0.5, __dadd_rn(Rho[o], Rho[o + st]));
+        return __ddiv_rn(__ddiv_rn(__dsub_rn(1.0, __ddiv_rn(r12, rf)), d), d);
+    };
+    const long long sx = D.s[0], sy = D.s[1];
+    const double CR = coef(sx, D.d[0], I == D.n[0] - 1), CL = coef(-sx, D.d[0], I == 0);
+    const double CU = coef(sy, D.d[1], J == D.n[1] - 1), CD = coef(-sy, D.d[1], J == 0);
+    double CF = 0.0, CB = 0.0;
+    double CC = -__dadd_rn(__dadd_rn(__dadd_rn(CR, CL), CU), CD);
+    if (D.ndim > 2) {
+        CF = coef(1, D.d[2], K == D.n[2] - 1);
+        CB = coef(-1, D.d[2], K == 0);
+        CC = __dsub_rn(CC, __dadd_rn(CF, CB));
+    }
+    double r = __dmul_rn(CC, ph[o]);
+    r = __dadd_rn(r, __dmul_rn(CR, ph[o + sx]));
+    r = __dadd_rn(r, __dmul_rn(CL, ph[o - sx]));
+    r = __dadd_rn(r, __dmul_rn(CU, ph[o + sy]));
+    r = __dadd_rn(r, __dmul_rn(CD, ph[o - sy]));
+    if (D.ndim > 2) r = __dadd_rn(r, __dadd_rn(__dmul_rn(CF, ph[o + 1]), __dmul_rn(CB, ph[o - 1])));
+    out[o] = r;
+}
+
+// right-hand side of fast_pressure_correction (projection_method.cpp:667-690), interior cells:
+// div(u*) rho12 / dt + RHS
+__global__ void k_fpc_rhs(double *__restrict__ rhs, const double *__restrict__ u, const double *__restrict__ v,
+                          const double *__restrict__ w, const double *__restrict__ fpc, Dims D, double r12,
+                          const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    double d = __dadd_rn(__ddiv_rn(__dsub_rn(u[o], u[o - D.s[0]]), D.d[0]),
+                         __ddiv_rn(__dsub_rn(v[o], v[o - D.s[1]]), D.d[1]));
+    if (D.ndim > 2) d = __dadd_rn(d, __ddiv_rn(__dsub_rn(w[o], w[o - 1]), D.d[2]));
+    d = __dmul_rn(d, __ddiv_rn(r12, sc->dt));
+    rhs[o] = __dadd_rn(d, fpc[o]);
+}
+
+// velocity correction of fast_pressure_correction (projection_method.cpp:716-750), interior
+// cells: u -= dt ((dp - dph) / rho12 + dph / rho_f)
+__global__ void k_correct_fpc(double *__restrict__ u, double *__restrict__ v, double *__restrict__ w,
+                              const double *__restrict__ p, const double *__restrict__ ph,
+                              const double *__restrict__ Rho, Dims D, double r12, const StepScalars *sc) {
+    long long o;
+    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
+    const double dt = sc->dt;
+    double *vel[3] = {u, v, w};
+    for (int a = 0; a < D.ndim; ++a) {
+        const long long st = D.s[a];
+        const double g1 = __ddiv_rn(__dsub_rn(p[o + st], p[o]), D.d[a]);
+        const double g2 = __ddiv_rn(__dsub_rn(ph[o + st], ph[o]), D.d[a]);
+        const double rf = __dmul_rn(0.5, __dadd_rn(Rho[o], Rho[o + st]));
+        const double c = __dadd_rn(__ddiv_rn(__dsub_rn(g1, g2), r12), __ddiv_rn(g2, rf));
+        vel[a][o] = __dsub_rn(vel[a][o], __dmul_rn(dt, c));
+    }
+}
+
 // node_from_face (wrapper_func.cpp:267-293), interior cells (the node BC fills the rest)
 __global__ void k_node_from_face(double *__restrict__ n0, double *__restrict__ n1, double *__restrict__ n2,
                                  const double *__restrict__ u, const double *__restrict__ v,
@@ -675,6 +759,7 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
     P.positive_ref = prm[9] != 0.0;
     P.ppe_tol = prm[10];
     P.ppe_max_iter = int(prm[12]);
+    P.ppe_initer = prm[14] >= 1.0 ? int(prm[14]) : 1;
     scheme = opt[0];
     n_mpls = opt[1];
     reinit_every = opt[2];
@@ -731,7 +816,8 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
         ALLOC(src[c]);
         ALLOC(src_old[c]);
     }
-    for (double **p : {&H, &delta, &sign, &grad, &curv, &a_f, &b_f, &rho, &mu, &RHS, &s1, &s2, &s3, &t1, &t2, &work})
+    for (double **p : {&H, &delta, &sign, &grad, &curv, &a_f, &b_f, &rho, &mu, &RHS, &RHS_fpc, &s1, &s2, &s3, &t1, &t2,
+                       &work})
         ALLOC(*p);
     for (int a = 0; a < D.ndim; ++a) {
         ALLOC(fv_flux[a]);
@@ -765,12 +851,20 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
     return SCIHPC_OK;
 }
 
+void TwoPhaseGpu::drop_graphs() {
+    for (int k = 0; k < 2; ++k) {
+        if (graph_exec[k]) cudaGraphExecDestroy(graph_exec[k]);
+        if (graph[k]) cudaGraphDestroy(graph[k]);
+        graph_exec[k] = nullptr;
+        graph[k] = nullptr;
+    }
+}
+
 void TwoPhaseGpu::destroy() {
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
-    graph_exec = nullptr;
-    graph = nullptr;
+    drop_graphs();
     ppe.destroy();
+    if (fpc_ready) fpc.destroy();
+    fpc_ready = false;
     ops.release();
     for (void *p : allocs) cudaFree(p);
     allocs.clear();
@@ -805,6 +899,8 @@ double *TwoPhaseGpu::field(const std::string &s) {
     if (s == "p") return pres.data;
     if (s == "p_old") return pres.old;
     if (s == "p_old2") return pres.old2;
+    if (s == "p_flux") return pres.flux;
+    if (s == "rhs_fpc") return RHS_fpc;
     if (s == "u") return vel[0].data;
     if (s == "v") return vel[1].data;
     if (s == "w") return vel[2].data;
@@ -910,6 +1006,7 @@ int TwoPhaseGpu::restore(const char *path) {
         return SCIHPC_ERR_ARG;
     }
     SCIHPC_CUDA(cudaMemcpy(sc, sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice));
+    iter_host = sc_host->iter;
     return SCIHPC_OK;
 }
 
@@ -936,6 +1033,7 @@ int TwoPhaseGpu::set_scalars(const double *in) {
     sc_host->iter = in[4];
     sc_host->stable_CFL = in[5];
     sc_host->lsf_mass0 = in[6];
+    iter_host = in[4];
     SCIHPC_CUDA(cudaMemcpyAsync(sc, sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice, stream));
     SCIHPC_CUDA(cudaStreamSynchronize(stream));
     return SCIHPC_OK;
@@ -1029,20 +1127,14 @@ void TwoPhaseGpu::reinit_step(int lambda) {
 void TwoPhaseGpu::set_source_scheme(int s) {
     if (s == source_scheme) return;
     source_scheme = s;
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
-    graph_exec = nullptr;
-    graph = nullptr;
+    drop_graphs();
 }
 
 void TwoPhaseGpu::set_scheme(int s) {
     if (s == scheme) return;
     scheme = s;
     // a captured step graph holds the old scheme's kernels
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
-    graph_exec = nullptr;
-    graph = nullptr;
+    drop_graphs();
 }
 
 int TwoPhaseGpu::reinit() {
@@ -1141,13 +1233,71 @@ void TwoPhaseGpu::ab2_part() {
     vel_bc(vel, -1);
 }
 
+// stopping rule of one pressure solve: ppe_tol as a relative or absolute residual target
+// (ppe_tol_mode), at most `cap` iterations
+void TwoPhaseGpu::set_solver_tol(Poisson &ps, int cap) {
+    ps.rel_tol = ppe_tol_mode == 1 ? 0.0 : P.ppe_tol;
+    ps.abs_tol = ppe_tol_mode == 1 ? P.ppe_tol : 0.0;
+    ps.max_iter = cap;
+}
+
 void TwoPhaseGpu::projection_begin() {
     const unsigned nbi = blocks_for(D.interior(), TPB);
     k_div_rhs<<<nbi, TPB, 0, stream>>>(RHS, vel[0].data, vel[1].data, vel[2].data, D, sc);
     ppe.set_density(rho, stream);
-    ppe.rel_tol = P.ppe_tol;
-    ppe.max_iter = P.ppe_max_iter;
+    set_solver_tol(ppe, P.ppe_max_iter);
     ppe.begin(RHS, pres.data, 1, stream);
+}
+
+// the reference's correction loop runs at most 100 multigrid cycles (projection_method.cpp:697)
+constexpr int FPC_MAX_ITER = 100;
+
+int TwoPhaseGpu::ensure_fpc() {
+    if (fpc_ready) return SCIHPC_OK;
+    scihpc_grid g{};
+    g.ndim = D.ndim;
+    for (int a = 0; a < 3; ++a) {
+        g.n[a] = D.n[a];
+        g.lo[a] = D.lo[a];
+        g.hi[a] = D.lo[a] + D.n[a] * (a < D.ndim ? D.d[a] : 1.0);
+    }
+    // Neumann walls, constant coefficients 1 / d^2: the multigrid operator the reference builds
+    // with shared_solvers_mg_init_Neumann (multigrid_base.cpp:236-291)
+    int rc = fpc.create(&g, 0, 0, fp32);
+    if (rc) return rc;
+    fpc_ready = true;
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::set_ppe_schedule(int schedule, int tol_mode) {
+    if (schedule == 1) {
+        int rc = ensure_fpc();
+        if (rc) return rc;
+    }
+    if (schedule != ppe_schedule) drop_graphs();
+    ppe_schedule = schedule;
+    ppe_tol_mode = tol_mode;
+    drop_graphs();   // the stopping rule is captured in the step graphs
+    return SCIHPC_OK;
+}
+
+// fast_pressure_correction's right-hand side and the solve's start (projection_method.cpp:
+// 659-697); the multigrid's previous solution is its initial guess in the reference, the
+// previous pressure here (the converged zero-mean solution does not depend on it)
+void TwoPhaseGpu::fpc_begin() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    k_fpc_rhs<<<nbi, TPB, 0, stream>>>(RHS, vel[0].data, vel[1].data, vel[2].data, RHS_fpc, D, P.density_ratio, sc);
+    set_solver_tol(fpc, FPC_MAX_ITER);
+    fpc.begin(RHS, pres.data, 1, stream);
+}
+
+void TwoPhaseGpu::fpc_end() {
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    fpc.finish(pres.data, stream);
+    scalar_bc(pres.data);
+    k_correct_fpc<<<nbi, TPB, 0, stream>>>(vel[0].data, vel[1].data, vel[2].data, pres.data, pres.flux, rho, D,
+                                           P.density_ratio, sc);
+    vel_bc(vel, -1);
 }
 
 void TwoPhaseGpu::projection_end() {
@@ -1165,52 +1315,110 @@ void TwoPhaseGpu::node_part() {
     vel_bc(nvel, 0);
 }
 
-void TwoPhaseGpu::ab_solve_pre() {
+// scalar_data::store (scalar_data.cpp:125-135), find_source, find_intermediate_velocity, then
+// the first pressure solve's start; with the fast correction also pressure_guess_solution and
+// init_ppe_fpc_coefficients (computed once per step, at cnt == 0 of projection_method.cpp:762)
+void TwoPhaseGpu::ab_solve_pre(bool use_fpc) {
     const long long N = D.size();
     const unsigned nbf = blocks_for(N, TPB);
-    // scalar_data::store (scalar_data.cpp:125-135)
     k_copy<<<nbf, TPB, 0, stream>>>(pres.old2, pres.old, N);
     k_copy<<<nbf, TPB, 0, stream>>>(pres.old, pres.data, N);
     find_source();
     ab2_part();
-    projection_begin();
+    if (use_fpc) {
+        k_pressure_guess<<<nbf, TPB, 0, stream>>>(pres.flux, pres.old, pres.old2, N, sc);
+        k_fpc_coefficients<<<blocks_for(D.interior(), TPB), TPB, 0, stream>>>(RHS_fpc, pres.flux, rho, D,
+                                                                             P.density_ratio);
+        fpc_begin();
+    } else {
+        projection_begin();
+    }
 }
 
-void TwoPhaseGpu::ab_solve_post() {
-    projection_end();
+void TwoPhaseGpu::ab_solve_post(bool use_fpc) {
+    if (use_fpc) fpc_end();
+    else projection_end();
     node_part();
 }
 
-// the pressure iteration after projection_begin, one host synchronisation per iteration
-int TwoPhaseGpu::run_ppe(int *iters, double *relres) {
-    SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
+// the pressure iteration after a solver's begin, one host synchronisation per iteration
+int TwoPhaseGpu::run_ppe(Poisson &ps, int *iters, double *relres) {
+    ps.use_conditional = false;
+    SCIHPC_CUDA(cudaMemcpyAsync(ps.host_state, ps.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
     SCIHPC_CUDA(cudaStreamSynchronize(stream));
-    while (!ppe.host_state->done) {
-        ppe.iterate(stream);
-        SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
+    while (!ps.host_state->done) {
+        ps.iterate(stream);
+        SCIHPC_CUDA(cudaMemcpyAsync(ps.host_state, ps.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
         SCIHPC_CUDA(cudaStreamSynchronize(stream));
     }
-    last_iters = ppe.host_state->it;
+    last_iters = ps.host_state->it;
     if (iters) *iters = last_iters;
+    (void)relres;
     return SCIHPC_OK;
 }
 
-int TwoPhaseGpu::ab_solve(int *iters, double *relres) {
-    ppe.use_conditional = false;
-    ab_solve_pre();
-    int rc = run_ppe(iters, relres);
-    if (rc) return rc;
-    ab_solve_post();
-    SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
-    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+namespace {
+// final state of a finished pressure solve (after its finish kernels)
+int solve_status(Poisson &ps, cudaStream_t s, double *last_relres, double *relres) {
+    SCIHPC_CUDA(cudaMemcpyAsync(ps.host_state, ps.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    SCIHPC_CUDA(cudaStreamSynchronize(s));
     SCIHPC_CUDA(cudaGetLastError());
-    last_relres = ppe.host_state->relres;
-    if (relres) *relres = ppe.host_state->relres;
-    if (ppe.host_state->diverged) {
+    *last_relres = ps.host_state->relres;
+    if (relres) *relres = ps.host_state->relres;
+    if (ps.host_state->diverged) {
         set_last_error("pressure solve produced a non-finite residual");
         return SCIHPC_ERR_NONFINITE;
     }
     return SCIHPC_OK;
+}
+}  // namespace
+
+int TwoPhaseGpu::ab_solve(int *iters, double *relres) {
+    const bool use_fpc = fpc_step();
+    Poisson &ps = use_fpc ? fpc : ppe;
+    // the stock schedule repeats the solve ppe_initer times (projection_method.cpp:761-774)
+    const int reps = ppe_schedule == 1 ? P.ppe_initer : 1;
+    ab_solve_pre(use_fpc);
+    for (int r = 0; r < reps; ++r) {
+        if (r > 0) {
+            if (use_fpc) {
+                fpc_end();
+                fpc_begin();
+            } else {
+                projection_end();
+                projection_begin();
+            }
+        }
+        int rc = run_ppe(ps, iters, relres);
+        if (rc) return rc;
+    }
+    ab_solve_post(use_fpc);
+    return solve_status(ps, stream, &last_relres, relres);
+}
+
+int TwoPhaseGpu::pressure_guess() {
+    const long long N = D.size();
+    k_pressure_guess<<<blocks_for(N, TPB), TPB, 0, stream>>>(pres.flux, pres.old, pres.old2, N, sc);
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::fpc_coefficients() {
+    k_fpc_coefficients<<<blocks_for(D.interior(), TPB), TPB, 0, stream>>>(RHS_fpc, pres.flux, rho, D, P.density_ratio);
+    SCIHPC_CUDA(cudaStreamSynchronize(stream));
+    SCIHPC_CUDA(cudaGetLastError());
+    return SCIHPC_OK;
+}
+
+int TwoPhaseGpu::fast_pressure_correction(int *iters, double *relres) {
+    int rc = ensure_fpc();
+    if (rc) return rc;
+    fpc_begin();
+    rc = run_ppe(fpc, iters, relres);
+    if (rc) return rc;
+    fpc_end();
+    return solve_status(fpc, stream, &last_relres, relres);
 }
 
 int TwoPhaseGpu::intermediate_velocity() {
@@ -1221,21 +1429,11 @@ int TwoPhaseGpu::intermediate_velocity() {
 }
 
 int TwoPhaseGpu::projection(int *iters, double *relres) {
-    ppe.use_conditional = false;
     projection_begin();
-    int rc = run_ppe(iters, relres);
+    int rc = run_ppe(ppe, iters, relres);
     if (rc) return rc;
     projection_end();
-    SCIHPC_CUDA(cudaMemcpyAsync(ppe.host_state, ppe.dev_state, sizeof(PcgScalars), cudaMemcpyDeviceToHost, stream));
-    SCIHPC_CUDA(cudaStreamSynchronize(stream));
-    SCIHPC_CUDA(cudaGetLastError());
-    last_relres = ppe.host_state->relres;
-    if (relres) *relres = ppe.host_state->relres;
-    if (ppe.host_state->diverged) {
-        set_last_error("pressure solve produced a non-finite residual");
-        return SCIHPC_ERR_NONFINITE;
-    }
-    return SCIHPC_OK;
+    return solve_status(ppe, stream, &last_relres, relres);
 }
 
 int TwoPhaseGpu::node_from_face() {
@@ -1287,66 +1485,91 @@ long long count_kernels(cudaGraph_t g) {
 }
 }  // namespace
 
-int TwoPhaseGpu::capture_step() {
+int TwoPhaseGpu::capture_step(int use_fpc) {
     // Graph of one time step: [pre-solve kernels] -> while(not converged){ one pressure
-    // iteration } -> [post-solve kernels, reinitialisation].
+    // iteration } -> [post-solve kernels, reinitialisation].  The stock schedule's repeated
+    // solves (ppe_initer > 1) chain further [finish, begin] -> while pairs before the post part.
+    Poisson &ps = use_fpc ? fpc : ppe;
+    const int reps = ppe_schedule == 1 ? P.ppe_initer : 1;
     cudaGraph_t g;
     SCIHPC_CUDA(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle handle;
-    SCIHPC_CUDA(cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault));
-    ppe.use_conditional = true;
-    ppe.conditional = (unsigned long long)handle;
+    ps.use_conditional = true;
 
-    cudaGraph_t pre_g, body_g_dummy, post_g;
-    (void)body_g_dummy;
+    cudaGraph_t seg_g;
     SCIHPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     find_dt();
     k_advance_time<<<1, 1, 0, stream>>>(sc);
     advect();
     mpls(n_mpls);
-    ab_solve_pre();
-    SCIHPC_CUDA(cudaStreamEndCapture(stream, &pre_g));
-
-    cudaGraphNode_t pre_node, cond_node, post_node;
-    SCIHPC_CUDA(cudaGraphAddChildGraphNode(&pre_node, g, nullptr, 0, pre_g));
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = handle;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    SCIHPC_CUDA(cudaGraphAddNode(&cond_node, g, &pre_node, nullptr, 1, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    SCIHPC_CUDA(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    ppe.iterate(stream);
-    SCIHPC_CUDA(cudaStreamEndCapture(stream, &body));
-
-    nodes_body = count_kernels(body);
+    ab_solve_pre(use_fpc != 0);
+    SCIHPC_CUDA(cudaStreamEndCapture(stream, &seg_g));
+    cudaGraphNode_t last;
+    SCIHPC_CUDA(cudaGraphAddChildGraphNode(&last, g, nullptr, 0, seg_g));
+    nodes_pre = count_kernels(seg_g);
+    cudaGraphDestroy(seg_g);
+    for (int r = 0; r < reps; ++r) {
+        if (r > 0) {
+            SCIHPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            if (use_fpc) {
+                fpc_end();
+                fpc_begin();
+            } else {
+                projection_end();
+                projection_begin();
+            }
+            SCIHPC_CUDA(cudaStreamEndCapture(stream, &seg_g));
+            cudaGraphNode_t mid;
+            SCIHPC_CUDA(cudaGraphAddChildGraphNode(&mid, g, &last, 1, seg_g));
+            cudaGraphDestroy(seg_g);
+            last = mid;
+        }
+        // one conditional handle per while node: the solver's check kernels set it
+        cudaGraphConditionalHandle handle;
+        SCIHPC_CUDA(cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault));
+        ps.conditional = (unsigned long long)handle;
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cond_node;
+        SCIHPC_CUDA(cudaGraphAddNode(&cond_node, g, &last, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        SCIHPC_CUDA(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        ps.iterate(stream);
+        SCIHPC_CUDA(cudaStreamEndCapture(stream, &body));
+        nodes_body = count_kernels(body);
+        last = cond_node;
+    }
     SCIHPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    k_count_ppe<<<1, 1, 0, stream>>>(sc, ppe.dev_state);
-    ab_solve_post();
+    k_count_ppe<<<1, 1, 0, stream>>>(sc, ps.dev_state);
+    ab_solve_post(use_fpc != 0);
     // step counter handled on the host: reinit runs every `reinit_every` steps; the graph
     // is captured for the common case reinit_every == 1 (otherwise the host calls reinit)
     if (reinit_every == 1) reinit();
-    SCIHPC_CUDA(cudaStreamEndCapture(stream, &post_g));
-    SCIHPC_CUDA(cudaGraphAddChildGraphNode(&post_node, g, &cond_node, 1, post_g));
-    nodes_pre = count_kernels(pre_g);
-    nodes_post = count_kernels(post_g);
-    SCIHPC_CUDA(cudaGraphInstantiate(&graph_exec, g, 0));
-    graph = g;
-    cudaGraphDestroy(pre_g);
-    cudaGraphDestroy(post_g);
-    ppe.use_conditional = false;
+    SCIHPC_CUDA(cudaStreamEndCapture(stream, &seg_g));
+    cudaGraphNode_t post_node;
+    SCIHPC_CUDA(cudaGraphAddChildGraphNode(&post_node, g, &last, 1, seg_g));
+    nodes_post = count_kernels(seg_g);
+    cudaGraphDestroy(seg_g);
+    SCIHPC_CUDA(cudaGraphInstantiate(&graph_exec[use_fpc], g, 0));
+    graph[use_fpc] = g;
+    ps.use_conditional = false;
     return SCIHPC_OK;
 }
 
 int TwoPhaseGpu::step(int nsteps, bool use_graph) {
-    if (use_graph && !graph_exec) {
-        int rc = capture_step();
-        if (rc) return rc;
-    }
     for (int s = 0; s < nsteps; ++s) {
+        // the step advances iter before ab_solve (benchmarks_2d_bubble_rising.cpp:104-106),
+        // which picks the pressure stage from it
+        iter_host += 1.0;
+        const int use_fpc = fpc_step() ? 1 : 0;
         if (use_graph) {
-            SCIHPC_CUDA(cudaGraphLaunch(graph_exec, stream));
+            if (!graph_exec[use_fpc]) {
+                int rc = capture_step(use_fpc);
+                if (rc) return rc;
+            }
+            SCIHPC_CUDA(cudaGraphLaunch(graph_exec[use_fpc], stream));
             ++step_count;
             if (reinit_every > 1 && step_count % reinit_every == 0) reinit();
         } else {
@@ -1358,7 +1581,7 @@ int TwoPhaseGpu::step(int nsteps, bool use_graph) {
             double rr;
             int rc = ab_solve(&it, &rr);
             if (rc) return rc;
-            k_count_ppe<<<1, 1, 0, stream>>>(sc, ppe.dev_state);
+            k_count_ppe<<<1, 1, 0, stream>>>(sc, use_fpc ? fpc.dev_state : ppe.dev_state);
             ++step_count;
             if (reinit_every > 0 && step_count % reinit_every == 0) reinit();
         }

@@ -29,6 +29,7 @@ struct HostParams {
     int positive_ref;
     double ppe_tol;
     int ppe_max_iter;
+    int ppe_initer;
 };
 
 class TwoPhaseGpu {
@@ -54,19 +55,34 @@ public:
     // 1 second_order_solver (find_source_sec, projection_method.cpp:314-382)
     void set_source_scheme(int s);
     void find_source();
-    void ab_solve_pre();     // store, find_source, AB2, PPE right-hand side, solver begin
-    void ab_solve_post();    // solver finish, pressure BC, velocity correction, node velocity
+    // pressure schedule: 0 the projection equation solved every step (default); 1 the
+    // reference's ab_solve schedule (projection_method.cpp:755-777): the projection equation
+    // while iter < 5, then pressure_guess_solution, init_ppe_fpc_coefficients and
+    // fast_pressure_correction, each repeated ppe_initer times.  tol_mode 0: ppe_tol is the
+    // relative residual; 1: the absolute residual 2-norm, as the reference's loops test it.
+    int set_ppe_schedule(int schedule, int tol_mode);
+    bool fpc_step() const { return ppe_schedule == 1 && iter_host >= 5.0; }
+    void ab_solve_pre(bool fpc);    // store, find_source, AB2, PPE right-hand side, solver begin
+    void ab_solve_post(bool fpc);   // solver finish, pressure BC, velocity correction, node velocity
     int ab_solve(int *iters, double *relres);   // host-driven pressure iteration
     // the stages of ab_solve one at a time (projection_method.cpp:384-402, 544-657; the
     // node velocity of wrapper_func.cpp:177-293)
     int intermediate_velocity();
     int projection(int *iters, double *relres);
     int node_from_face();
+    // the stages of the fast pressure correction (projection_method.cpp:467-541, 659-753,
+    // 803-815): pressure_guess_solution into the pressure's flux array, the right-hand side
+    // term of init_ppe_fpc_coefficients from it, and the correction itself
+    int pressure_guess();
+    int fpc_coefficients();
+    int fast_pressure_correction(int *iters, double *relres);
     void ab2_part();
     void projection_begin();
     void projection_end();
+    void fpc_begin();
+    void fpc_end();
     void node_part();
-    int run_ppe(int *iters, double *relres);
+    int run_ppe(Poisson &ps, int *iters, double *relres);
     int init();
     int step(int nsteps, bool graph);
     int diagnostics(double *out);
@@ -75,6 +91,7 @@ public:
     cudaStream_t stream = nullptr;
     Dims D{};
     double last_iters = 0, last_relres = 0, last_ms = 0;
+    double iter_host = 0.0;   // host copy of StepScalars::iter (selects the pressure stage)
 
 private:
     void scalar_bc(double *f);
@@ -82,7 +99,10 @@ private:
     void rk_stage_update(int stage);
     void convection_rhs(double *s);
     void reinit_stage(int stage);
-    int capture_step();
+    int capture_step(int fpc);
+    void drop_graphs();
+    int ensure_fpc();
+    void set_solver_tol(Poisson &ps, int cap);
 
     // independent work of one stage runs as parallel branches on side streams (fork/join by
     // events; the branches become parallel nodes when the step is captured as a graph)
@@ -102,6 +122,10 @@ private:
     int scalar_types[6];
     CompactOps ops;
     Poisson ppe;
+    Poisson fpc;               // constant-coefficient solver of the fast pressure correction
+    bool fpc_ready = false;
+    int ppe_schedule = 0, ppe_tol_mode = 0;
+    double *RHS_fpc = nullptr;   // init_ppe_fpc_coefficients' RHS array
     DevScalar phi, pres, vel[3], nvel[3];
     double *H = nullptr, *delta = nullptr, *sign = nullptr, *grad = nullptr, *curv = nullptr, *a_f = nullptr,
            *b_f = nullptr, *rho = nullptr, *mu = nullptr;
@@ -112,8 +136,8 @@ private:
     StepScalars *sc_host = nullptr;   // pinned
     std::vector<void *> allocs;
     size_t nfield_allocs = 0;   // allocs[0 .. nfield_allocs) are whole ghosted fields
-    cudaGraphExec_t graph_exec = nullptr;
-    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // step graphs: projection, fast correction
+    cudaGraph_t graph[2] = {nullptr, nullptr};
     int reinit_steps = 0;
     GhostFill phi_fill{};
     long long nodes_pre = 0, nodes_body = 0, nodes_post = 0;

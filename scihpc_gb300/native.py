@@ -87,6 +87,8 @@ _SIGS = {
     "scihpc_ccd_mixed": ([_vp, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_weno5": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_godunov_gradient": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_stabilized_upon_gradient": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "scihpc_guess_from_history": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_lsf_fields": ([_vp, _dp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "scihpc_curvature": ([_vp, _vp, ctypes.POINTER(_vp), _vp, _vp], ctypes.c_int),
     "scihpc_lsf_integrals": ([_vp, _dp, _vp, _dp, _vp], ctypes.c_int),
@@ -142,6 +144,10 @@ _SIGS = {
     "scihpc_twophase_intermediate_velocity": ([_vp], ctypes.c_int),
     "scihpc_twophase_projection": ([_vp, _ip, _dp], ctypes.c_int),
     "scihpc_twophase_node_from_face": ([_vp], ctypes.c_int),
+    "scihpc_twophase_set_ppe_schedule": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "scihpc_twophase_pressure_guess": ([_vp], ctypes.c_int),
+    "scihpc_twophase_fpc_coefficients": ([_vp], ctypes.c_int),
+    "scihpc_twophase_fast_pressure_correction": ([_vp, _ip, _dp], ctypes.c_int),
     "scihpc_twophase_step": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "scihpc_twophase_diagnostics": ([_vp, _dp], ctypes.c_int),
     "scihpc_twophase_stream": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
@@ -239,6 +245,14 @@ class Workspace:
 
     def godunov_gradient(self, phi, sign, grad, stream=0):
         self.L.check(self.L.scihpc_godunov_gradient(self.h, _ptr(phi), _ptr(sign), _ptr(grad), stream))
+
+    def stabilized_upon_gradient(self, phi, sign, grad, stream=0):
+        """grad = Godunov |grad phi|, then phi /= max(grad) in place (godunov_gradient.cpp:159-181)."""
+        self.L.check(self.L.scihpc_stabilized_upon_gradient(self.h, _ptr(phi), _ptr(sign), _ptr(grad), stream))
+
+    def guess_from_history(self, old, old2, flux, stream=0):
+        """flux = 2 old - old2 on every cell (flux.cpp:653-662)."""
+        self.L.check(self.L.scihpc_guess_from_history(self.h, _ptr(old), _ptr(old2), _ptr(flux), stream))
 
     def lsf_fields(self, prm, phi, H=None, delta=None, sign=None, rho=None, mu=None, stream=0):
         p = (ctypes.c_double * 4)(*prm)
@@ -418,6 +432,23 @@ class TwoPhase:
         it = ctypes.c_int(0)
         rr = ctypes.c_double(0.0)
         self.L.check(self.L.scihpc_twophase_ab_solve(self.h, ctypes.byref(it), ctypes.byref(rr)))
+        return it.value, rr.value
+
+    def set_ppe_schedule(self, schedule: int, tol_mode: int = 0):
+        """0: the projection equation every step; 1: the reference's schedule (projection while
+        iter < 5, then the fast pressure correction).  tol_mode 1: ppe_tol is absolute."""
+        self.L.check(self.L.scihpc_twophase_set_ppe_schedule(self.h, schedule, tol_mode))
+
+    def pressure_guess(self):
+        self.L.check(self.L.scihpc_twophase_pressure_guess(self.h))
+
+    def fpc_coefficients(self):
+        self.L.check(self.L.scihpc_twophase_fpc_coefficients(self.h))
+
+    def fast_pressure_correction(self):
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        self.L.check(self.L.scihpc_twophase_fast_pressure_correction(self.h, ctypes.byref(it), ctypes.byref(rr)))
         return it.value, rr.value
 
     def step(self, nsteps=1, graph=False, sync=True):

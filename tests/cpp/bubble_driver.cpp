@@ -47,6 +47,9 @@ int main(int argc, char **argv) {
             std::fprintf(stderr, "parameter %s missing from %s\n", k, argv[1]);
             return 2;
         }
+    // pressure schedule (gpu_session.h): the reference's by default; "exact" = 1 selects the
+    // projection equation every step with a relative ppe_tol
+    if (P.count("exact") && P["exact"] != 0.0) scihpc_cpp_set_pressure_schedule(0, 0);
     auto geo = structured_grid(axis{P["x0"], P["x1"], int(P["nx"])}, axis{P["y0"], P["y1"], int(P["ny"])});
 
     auto phi = wrapper(true, &geo, bc_info{NEUMANN}, bc_info{NEUMANN}, bc_info{NEUMANN}, bc_info{NEUMANN});
@@ -87,6 +90,7 @@ int main(int argc, char **argv) {
     param->min_CFL = P["min_CFL"];
     param->ppe_tol = P["ppe_tol"];
     param->ppe_max_iter = int(P["ppe_max_iter"]);
+    param->ppe_initer = P.count("ppe_initer") ? int(P["ppe_initer"]) : 1;   // as benchmarks_2d_bubble_rising.cpp:79
     param->positive_ref = P["positive_ref"] != 0.0;
 
     flow_solver.find_source(&vel, &nvel, &phi);
@@ -100,8 +104,31 @@ int main(int argc, char **argv) {
         solver.tvd_rk3(&phi, &nvel, &identity_flux, P["weno"] != 0.0 ? &convection_weno : &convection);
         for (int c = 0; c < 5; ++c) solver.euler(&phi, &nvel, &identity_flux, &mpls);
         // second_order: the projection step of benchmarks_2d_dambreak.cpp (ab_solve_sec)
-        if (P.count("second_order") && P["second_order"] != 0.0) flow_solver.ab_solve_sec(&vel, &nvel, &pressure, &phi);
-        else flow_solver.ab_solve(&vel, &nvel, &pressure, &phi);
+        if (P.count("second_order") && P["second_order"] != 0.0) {
+            flow_solver.ab_solve_sec(&vel, &nvel, &pressure, &phi);
+        } else if (P.count("compose") && P["compose"] != 0.0) {
+            // ab_solve's stages called one by one, as projection_method::ab_solve composes them
+            // (projection_method.cpp:755-777)
+            pressure.scalar->store();
+            flow_solver.find_source(&vel, &nvel, &phi);
+            flow_solver.find_intermediate_velocity(&vel);
+            for (int cnt = 0; cnt < param->ppe_initer; ++cnt) {
+                if (param->iter < 5) {
+                    if (cnt == 0) flow_solver.init_ppe_proj_coefficients(&pressure);
+                    flow_solver.projection(&pressure, &phi, &vel);
+                } else {
+                    if (cnt == 0) {
+                        flow_solver.pressure_guess_solution(&pressure);
+                        flow_solver.init_ppe_fpc_coefficients(&pressure);
+                    }
+                    flow_solver.fast_pressure_correction(&pressure, &phi, &vel);
+                }
+            }
+            node_from_face(&vel, &nvel);
+            nvel.apply_nvel_bc();
+        } else {
+            flow_solver.ab_solve(&vel, &nvel, &pressure, &phi);
+        }
         int instep = 0;
         while (instep * param->rdt < 2.0 * param->ls_width) {
             if (instep == 0) find_sign(&phi);

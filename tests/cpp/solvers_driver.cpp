@@ -6,7 +6,8 @@
 //        viscosity_ratio
 // in.bin holds five ghosted fields: flux, u, v, phi, sign.  out.bin receives, in order:
 // ccd fx fy fxx fyy fxy, uccd fx fy fxx fyy, weno fx fy, heaviside delta density viscosity,
-// godunov grad, extrapolated flux, curvature.
+// godunov grad, extrapolated flux, curvature, guess_from_history's flux (2 phi - flux), and
+// stabilized_upon_gradient's phi and grad.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -81,6 +82,15 @@ int main(int argc, char **argv) {
     identity_with_extrapolation(f);
     emit(out, f->flux, n);
     std::fwrite(curv.data(), sizeof(double), n, out);
+    // guess_from_history with old = phi, old2 = the extrapolated flux
+    put(f->old, f->data[0][0], n);
+    put(f->old2, f->flux[0][0], n);
+    guess_from_history(f);
+    emit(out, f->flux, n);
+    // phi / max |grad phi| (the reference's dam-break drivers call it before their time loop)
+    stabilized_upon_gradient(&phi);
+    emit(out, f->data, n);
+    emit(out, dummy->grad, n);
     std::fclose(out);
     std::printf("status %d\n", scihpc_cpp_last_status());
     return scihpc_cpp_last_status() == 0 ? 0 : 1;

@@ -32,13 +32,14 @@ def test_driver_compiles_and_links(driver):
     assert os.path.exists(driver)
 
 
-def run_driver(driver, tmp_path, steps, weno, vtk=False, second_order=False):
+def run_driver(driver, tmp_path, steps, weno, vtk=False, second_order=False, compose=False, exact=False):
     prm = bubble_params(G, ppe_tol=1e-12)
     vals = dict(nx=G.n[0], ny=G.n[1], x0=G.lo[0], x1=G.hi[0], y0=G.lo[1], y1=G.hi[1], cx=CENTER[0], cy=CENTER[1],
                 r=RADIUS, density_ratio=prm["density_ratio"], viscosity_ratio=prm["viscosity_ratio"], Re=prm["Re"],
                 Fr=prm["Fr"], We=prm["We"], ls_width=prm["ls_width"], rdt=prm["rdt"], max_CFL=prm["max_CFL"],
                 min_CFL=prm["min_CFL"], ppe_tol=prm["ppe_tol"], ppe_max_iter=prm["ppe_max_iter"],
-                positive_ref=prm["positive_ref"], steps=steps, weno=int(weno), second_order=int(second_order))
+                positive_ref=prm["positive_ref"], steps=steps, weno=int(weno), second_order=int(second_order),
+                compose=int(compose), exact=int(exact))
     pf = tmp_path / "params.txt"
     pf.write_text("".join(f"{k} = {float(v)!r}\n" for k, v in vals.items()))
     out = tmp_path / "out.bin"
@@ -51,9 +52,10 @@ def run_driver(driver, tmp_path, steps, weno, vtk=False, second_order=False):
     return fields, r.stdout, prm
 
 
-def port_state(prm, steps, weno, second_order=False):
+def port_state(prm, steps, weno, second_order=False, ppe_mode=2):
     port = O.Checker("port").twophase(G, ["no_slip"] * 6, ["neumann"] * 6, prm,
-                                      dict(scheme=int(weno), n_mpls=5, reinit_every=1, ppe_mode=2, reinit_lambda=1))
+                                      dict(scheme=int(weno), n_mpls=5, reinit_every=1, ppe_mode=ppe_mode,
+                                           reinit_lambda=1))
     port.set_exact_tol(1e-14)
     port.set("phi", bubble_phi(G, CENTER, RADIUS))
     port.call("init")
@@ -74,6 +76,34 @@ def test_driver_matches_oracle(driver, tmp_path, weno):
         assert rel_l2(fields[nm][I], port.get(nm)[I]) <= 1e-9, (nm, log)
     t_line = [ln for ln in log.splitlines() if ln.startswith("t ")][-1].split()
     assert abs(float(t_line[1]) - port.scalars()["t"]) <= 1e-15
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("compose", [False, True], ids=["ab_solve", "stages"])
+def test_driver_stock_schedule_matches_oracle(driver, tmp_path, compose):
+    """Seven steps through the drop-in with its default pressure schedule -- the reference's:
+    projection() for iter < 5, then pressure_guess_solution, init_ppe_fpc_coefficients and
+    fast_pressure_correction -- either inside projection_method::ab_solve or composed stage by
+    stage by the driver (store, find_source, find_intermediate_velocity, ..., node_from_face),
+    against the restatement of that schedule with both equations solved exactly (ppe_mode 3)."""
+    fields, log, prm = run_driver(driver, tmp_path, 7, True, compose=compose)
+    port = port_state(prm, 7, True, ppe_mode=3)
+    I = G.interior()
+    assert rel_l2(fields["phi"][I], port.get("phi")[I]) <= 1e-10, log
+    for nm in ("p", "u", "v"):
+        assert rel_l2(fields[nm][I], port.get(nm)[I]) <= 1e-9, (nm, log)
+
+
+@pytest.mark.gpu
+def test_driver_exact_schedule_matches_oracle(driver, tmp_path):
+    """The projection equation every step (scihpc_cpp_set_pressure_schedule(0, 0)) over seven
+    steps against ppe_mode 2."""
+    fields, log, prm = run_driver(driver, tmp_path, 7, True, exact=True)
+    port = port_state(prm, 7, True, ppe_mode=2)
+    I = G.interior()
+    assert rel_l2(fields["phi"][I], port.get("phi")[I]) <= 1e-10, log
+    for nm in ("p", "u", "v"):
+        assert rel_l2(fields[nm][I], port.get(nm)[I]) <= 1e-9, (nm, log)
 
 
 @pytest.mark.gpu

@@ -56,7 +56,7 @@ def test_solver_classes_match_oracle(driver, tmp_path):
     raw = np.fromfile(fout, dtype=np.float64)
     n = int(np.prod(g.shape))
     out = [raw[q * n:(q + 1) * n].reshape(g.shape) for q in range(raw.size // n)]
-    assert len(out) == 18
+    assert len(out) == 21
     port = O.Checker("port")
     zeros = np.zeros(g.shape)
     ccd = port.ccd(g, flux, mixed=True)
@@ -83,6 +83,11 @@ def test_solver_classes_match_oracle(driver, tmp_path):
     w.curvature(d(phi), derivs, curv)
     torch.cuda.synchronize()
     assert np.array_equal(out[17], curv.cpu().numpy())
+    ext = port.flux_extrapolate(g, 0, phi)
+    assert np.array_equal(out[18], port.guess_from_history(g, phi, ext)), "guess_from_history"
+    st_phi, st_grad = port.stabilize(g, phi, sign)
+    assert near(out[19], st_phi, TOL), "stabilized_upon_gradient phi"
+    assert near(out[20], st_grad, TOL), "stabilized_upon_gradient grad"
 
 
 @pytest.mark.gpu

@@ -172,6 +172,35 @@ def test_godunov(port, gi):
     assert np.abs(host(out) - ref).max() <= TOL * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("gi", range(len(GRIDS)))
+def test_stabilized_upon_gradient(port, gi):
+    """stabilized_upon_gradient (godunov_gradient.cpp:159-181): the Godunov gradient, its
+    device-side maximum over every cell and the division of phi by it."""
+    g = GRIDS[gi]
+    w = ws(g)
+    rng = np.random.default_rng(820 + gi)
+    phi = 0.2 * smooth_field(g, rng)
+    sign = np.sign(rng.standard_normal(g.shape))
+    ref_phi, ref_grad = port.stabilize(g, phi, sign)
+    d_phi = dev(phi)
+    grad = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    w.stabilized_upon_gradient(d_phi, dev(sign), grad)
+    assert np.abs(host(grad) - ref_grad).max() <= TOL * np.abs(ref_grad).max()
+    assert np.abs(host(d_phi) - ref_phi).max() <= TOL * np.abs(ref_phi).max()
+
+
+@pytest.mark.parametrize("gi", range(len(GRIDS)))
+def test_guess_from_history_bitexact(port, gi):
+    """guess_from_history (flux.cpp:653-662): 2 old - old2 on every cell, bit for bit."""
+    g = GRIDS[gi]
+    w = ws(g)
+    rng = np.random.default_rng(840 + gi)
+    old, old2 = rng.standard_normal(g.shape), rng.standard_normal(g.shape)
+    out = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    w.guess_from_history(dev(old), dev(old2), out)
+    assert np.array_equal(host(out), port.guess_from_history(g, old, old2))
+
+
 @pytest.mark.parametrize("ndim", [2, 3])
 def test_lsf_fields_and_integrals(port, ndim):
     if ndim == 2:

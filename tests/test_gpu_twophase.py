@@ -26,14 +26,15 @@ def native(g):
     return Grid(g.ndim, tuple(g.n), tuple(g.lo), tuple(g.hi))
 
 
-def make_pair(g, scheme=1, fp32=False):
+def make_pair(g, scheme=1, fp32=False, reinit_lambda=1, ppe_mode=2):
     from scihpc_gb300 import TwoPhase
     prm = bubble_params(g, ppe_tol=1e-12)
     port = O.Checker("port").twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm,
-                                      dict(scheme=scheme, n_mpls=5, reinit_every=1, ppe_mode=2, reinit_lambda=1))
+                                      dict(scheme=scheme, n_mpls=5, reinit_every=1, ppe_mode=ppe_mode,
+                                           reinit_lambda=reinit_lambda))
     port.set_exact_tol(1e-14)
     gpu = TwoPhase(native(g), ["no_slip"] * 6, ["neumann"] * 6, prm, scheme=scheme, n_mpls=5, reinit_every=1,
-                   fp32=fp32)
+                   fp32=fp32, reinit_lambda=bool(reinit_lambda))
     phi = bubble_phi(g, (0.43, 0.57), 0.23)
     port.set("phi", phi)
     gpu.set("phi", phi)
@@ -204,4 +205,83 @@ def test_full_steps_second_order(graph):
         port.call("step", 1)
         gpu.step(1, graph=graph)
     compare(G, port, gpu, ["phi"], LS_TOL)
+    compare(G, port, gpu, ["p", "u", "v"], FLOW_TOL)
+
+
+@pytest.mark.parametrize("graph", [False, True], ids=["eager", "graph"])
+def test_full_steps_reinit_without_lambda(graph):
+    """Whole steps whose reinitialisation uses lsf_redistance_no_lambda (source.cpp:157-169:
+    the redistance right-hand side without the volume-constraint correction)."""
+    port, gpu = make_pair(G, reinit_lambda=0)
+    port.call("init")
+    gpu.init()
+    for k in range(2):
+        port.call("step", 1)
+        gpu.step(1, graph=graph)
+    compare(G, port, gpu, ["phi"], LS_TOL)
+    compare(G, port, gpu, ["p", "u", "v"], FLOW_TOL)
+
+
+def test_reinit_step_without_lambda():
+    """One runge_kutta::tvd_rk3 step with lsf_redistance_no_lambda on a distorted level set."""
+    port, gpu = make_pair(G, reinit_lambda=0)
+    port.call("init")
+    gpu.init()
+    phi = port.get("phi")
+    phi[3:-3, 3:-3] *= 1.0 + 0.3 * np.sin(7.0 * np.arange(phi.shape[1] - 6))[None, :, None]
+    for s in (port, gpu):
+        s.set("phi", phi)
+    port.call("reinit")
+    gpu.reinit()
+    compare(G, port, gpu, ["phi"], LS_TOL)
+
+
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32_refined"])
+@pytest.mark.parametrize("graph", [False, True], ids=["eager", "graph"])
+def test_stock_schedule_steps(graph, fp32):
+    """The reference's own ab_solve schedule (projection_method.cpp:755-777) on the GPU: the
+    projection equation for steps 1-4, then pressure_guess_solution, init_ppe_fpc_coefficients
+    and fast_pressure_correction (the constant-coefficient multigrid equation and its
+    two-density velocity correction) from step 5 on, against the restatement of the same
+    schedule with both equations solved exactly (ppe_mode 3, itself pinned to the reference's
+    converged schedule in test_oracle_pin.py).  Seven steps."""
+    port, gpu = make_pair(G, fp32=fp32, ppe_mode=3)
+    gpu.set_ppe_schedule(1, 0)
+    port.call("init")
+    gpu.init()
+    for k in range(7):
+        port.call("step", 1)
+        gpu.step(1, graph=graph)
+        compare(G, port, gpu, ["phi"], LS_TOL)
+        compare(G, port, gpu, ["p", "u", "v"], FLOW_TOL)
+
+
+def test_fast_pressure_correction_stages():
+    """The stages one at a time, as the reference's projection_method exposes them, on the
+    state after five steps of the stock schedule: pressure_guess_solution (every cell, bit for
+    bit), init_ppe_fpc_coefficients' right-hand-side term, and fast_pressure_correction (the
+    constant-coefficient solve, the pressure fill and the velocity correction)."""
+    port, gpu = make_pair(G, ppe_mode=3)
+    gpu.set_ppe_schedule(1, 0)
+    port.call("init")
+    gpu.init()
+    for k in range(5):   # iter 1..5: the fifth step is the first with the fast correction
+        port.call("step", 1)
+        gpu.step(1)
+    rng = np.random.default_rng(5)
+    p_old = port.get("p")
+    p_old2 = p_old * (1.0 + 0.01 * rng.standard_normal(G.shape))
+    for s in (port, gpu):
+        s.set("p_old", p_old)
+        s.set("p_old2", p_old2)
+        s.set_scalars(dt_old=0.011, dt_old2=0.013)
+    port.call("pressure_guess")
+    gpu.pressure_guess()
+    assert np.array_equal(gpu.get("p_flux"), port.get("p_flux"))
+    port.call("fpc_coefficients")
+    gpu.fpc_coefficients()
+    I = G.interior()
+    assert rel_l2(gpu.get("rhs_fpc")[I], port.get("rhs")[I]) <= 1e-12
+    port.call("fast_pressure_correction")
+    it, rr = gpu.fast_pressure_correction()
     compare(G, port, gpu, ["p", "u", "v"], FLOW_TOL)

@@ -49,6 +49,10 @@ def test_stencils_bitexact(both, gi):
     phi = 0.2 * smooth_field(g, rng)
     sign = np.sign(rng.standard_normal(g.shape))
     assert np.array_equal(P.godunov(g, phi, sign), R.godunov(g, phi, sign))
+    a, b = P.stabilize(g, phi, sign), R.stabilize(g, phi, sign)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    old, old2 = rng.standard_normal(g.shape), rng.standard_normal(g.shape)
+    assert np.array_equal(P.guess_from_history(g, old, old2), R.guess_from_history(g, old, old2))
     prm = [0.15, 0.001, 0.01, 0.0]
     assert np.array_equal(P.lsf_fields(g, prm, phi), R.lsf_fields(g, prm, phi))
     assert np.array_equal(P.lsf_integrals(g, prm, phi), R.lsf_integrals(g, prm, phi))
