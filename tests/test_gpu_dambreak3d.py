@@ -69,11 +69,12 @@ def test_dambreak_steps_match_oracle(fp32):
     assert e1["phi"] <= 1e-10 and all(e1[nm] <= 1e-9 for nm in ("p", "u", "v", "w")), e1
     # step 2 starts from velocities that agree to ~1e-13; its right-hand side div(u*)/dt is a
     # small difference of O(1) face velocities and amplifies that by ~1e5 here (measured:
-    # rhs 2.8e-8, p 1.8e-9 with every stage's own error at round-off), so the bound widens
-    # by the same factor
+    # rhs 2.8e-8, p 1.8e-9 with every stage's own error at round-off).  The restatement
+    # itself, its velocities perturbed in the last bit after step 1, moves by p 2.5e-9 and
+    # u, v, w 8e-9 at this step (test_oracle_sensitivity.py), so the bound is 5e-8
     port.call("step", 1)
     gpu.step(1, graph=True)
     e2 = errors()
-    assert e2["phi"] <= 1e-10 and all(e2[nm] <= 1e-7 for nm in ("p", "u", "v", "w")), e2
+    assert e2["phi"] <= 1e-10 and all(e2[nm] <= 5e-8 for nm in ("p", "u", "v", "w")), e2
     sp, sg = port.scalars(), gpu.scalars()
     assert abs(sp["dt"] - sg["dt"]) <= 1e-14 * sp["dt"]
