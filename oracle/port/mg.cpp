@@ -324,10 +324,25 @@ int coef_cg_solve(const Grid &g, const double *CC, const double *CR, const doubl
     if (bnorm == 0.0) bnorm = 1.0;
     applyM(x, Md);
     for (size_t t = 0; t < n; ++t) r[t] = b[t] - Md[t];
-    // Jacobi preconditioner.  z is not projected: D^-1 stays symmetric, the constant
-    // component it adds to x is removed once at the end.
+    // Jacobi preconditioner on small grids, a multigrid V-cycle on large ones.  z is not
+    // projected: either stays symmetric, the constant component it adds to x is removed once
+    // at the end.
+    MGPrecond *mgp = nullptr;
+    if (n >= 8192) {
+        std::vector<double> cf[3];
+        const size_t st[3] = {sx, sy, sz};
+        const double *C[3] = {CR, CU, CF};
+        for (int a = 0; a < g.ndim; ++a) {
+            cf[a].resize(n);
+            for (size_t t = 0; t < n; ++t) cf[a][t] = C[a][idx[t]];
+        }
+        (void)st;
+        mgp = new MGPrecond(g.ndim, g.n, cf);
+    }
     auto precond = [&]() {
-        for (size_t t = 0; t < n; ++t) z[t] = r[t] / (-CC[idx[t]]);
+        if (mgp) mgp->apply(r, z);
+        else
+            for (size_t t = 0; t < n; ++t) z[t] = r[t] / (-CC[idx[t]]);
     };
     precond();
     d = z;
@@ -368,6 +383,7 @@ int coef_cg_solve(const Grid &g, const double *CC, const double *CR, const doubl
         rz = rz2;
         for (size_t t = 0; t < n; ++t) d[t] = z[t] + beta * d[t];
     }
+    delete mgp;
     x = xbest;
     remove_mean(x);
     for (size_t t = 0; t < n; ++t) p[idx[t]] = x[t];

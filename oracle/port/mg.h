@@ -38,10 +38,23 @@ struct RefMG {
     void full_cycle();                                                       // multigrid.cpp:85-107
 };
 
+// Multigrid V(1,1) preconditioner of the face-coefficient operator (mgcg.cpp): cf[a] holds
+// the +a face coefficient of every interior cell (compact, K fastest; 0 on the wall).
+struct MGPrecond {
+    struct Impl;
+    Impl *impl;
+    MGPrecond(int ndim, const int *n, const std::vector<double> *cf);
+    ~MGPrecond();
+    MGPrecond(const MGPrecond &) = delete;
+    MGPrecond &operator=(const MGPrecond &) = delete;
+    void apply(const std::vector<double> &r, std::vector<double> &z);
+};
+
 // Exact solve of the variable-coefficient equation of projection() with its seven
 // coefficient arrays (projection_method.cpp:404-465): sum C_nb p_nb + CC p = rhs on the
-// interior cells, solution normalised to zero interior mean.  Jacobi-preconditioned CG on
-// the negated (positive semidefinite) operator.  Returns the iterations taken.
+// interior cells, solution normalised to zero interior mean.  CG on the negated (positive
+// semidefinite) operator, preconditioned by Jacobi on small grids and by MGPrecond on grids
+// of 8192 cells and more.  Returns the iterations taken.
 int coef_cg_solve(const Grid &g, const double *CC, const double *CR, const double *CL, const double *CU,
                   const double *CD, const double *CF, const double *CB, const double *rhs, double *p,
                   double rel_tol, int max_iter, double *relres);
