@@ -360,7 +360,7 @@ int coef_cg_solve(const Grid &g, const double *CC, const double *CR, const doubl
             best = rel;
             xbest = x;
             since_best = 0;
-        } else if (++since_best > 2000) {
+        } else if (++since_best > (mgp ? 30 : 2000)) {
             break;   // stagnated at the attainable accuracy
         }
         if (rel <= rel_tol) break;
