@@ -31,6 +31,23 @@ DOMAIN = ((0.0, 0.0), (1.0, 2.0))
 BUBBLE = ((0.5, 0.5), 0.25)
 PPE_TOL = 1e-10
 
+# Algorithmic FP64 operations per interior cell of the reinitialisation's gradient kernel in
+# 2D, counted from the reference formulas (one flop per add, subtract, multiply, divide or
+# square root; max/min not counted): per axis the fourth-order central difference (10), the
+# five distinct second differences (15), two WENO-JS corrections (47 each: three indicators
+# 23, three weights 9, two normalised weights 4, the correction 11), the two one-sided
+# derivatives (6) and the square (1) -- 126; both axes, their sum and its root (254); the
+# redistance source -sign (g - 1) rdt / dt (4) and the lambda fields a, b (4) -- 262
+# (godunov_gradient.cpp:19-198, source.cpp:157-198).
+REINIT_FLOPS_2D = 262
+# DRAM traffic per launch and share of the step from the committed ncu summaries (None when
+# not captured); the command that made each is in the summary file.
+REINIT_TRAFFIC_BYTES = None
+REINIT_TRAFFIC_SRC = None
+REINIT_SHARE = 0.244   # profiles/twophase_step_128x256_launches.md
+VCYCLE_256_TRAFFIC_BYTES = None
+VCYCLE_256_TRAFFIC_SRC = None
+
 
 PPE_DESC = {"fp32": "FP32 V-cycles and conjugate gradients inside FP64 iterative refinement "
                     "(FP64 residual and pressure)",
@@ -156,31 +173,206 @@ def max_over_ranks(ws, v: float, device) -> float:
 
 
 # ----------------------------------------------------------------------------- CPU legs
-def cpu_reference_rate(steps: int, warmup: int, budget_s: float, threads: int):
-    """The reference algorithm on the host cores: the restatement's stock ab_solve (SOR for
-    the first 5 steps, then fast pressure correction with the reference multigrid), WENO5
-    advection, as the reference drivers run it.  Returns (steps/s, steps timed)."""
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+# The reference algorithm on the host cores (oracle/port: the restatement, pinned bit for bit
+# to the reference compiled from its sources where those are present; the GPU machine has only
+# the restatement).  Every figure is the median of three fixed windows, with all host cores
+# (the reference's OpenMP loops, SOR's racy in-place sweep included) and with one thread.
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=20).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def _port(threads: int):
     import oracle as O
+    P = O.Checker("port")
+    P.lib.port_set_threads(threads)
+    return O, P
+
+
+def _windows(step, nwin: int, nsteps: int) -> list:
+    rates = []
+    for _ in range(nwin):
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            step()
+        rates.append(nsteps / (time.perf_counter() - t0))
+    return rates
+
+
+def cpu_bubble(threads: int, win_all: int = 50, win_one: int = 10) -> dict:
+    """The bench's workload (128 x 256 rising bubble, TC1 fluid, WENO5, 5 mpls steps, reinit
+    every step) under the reference's stock ab_solve schedule and its drivers' solver
+    settings (ppe_tol 1e-8, ppe_tol2 1e-7, 100 SOR sweeps at most, ppe_initer 1;
+    benchmarks_2d_bubble_rising.cpp:78-79, global.h:49-53), after the five start-up steps
+    (SOR while iter < 5, then the first fast pressure correction): steps/s of three windows
+    of win_all steps on all cores, then three of win_one steps on one thread (same run)."""
+    import numpy as np
+    O, P = _port(threads)
     g = O.Grid(2, (NX, NY), DOMAIN[0], DOMAIN[1])
     prm = physics(min((DOMAIN[1][0] - DOMAIN[0][0]) / NX, (DOMAIN[1][1] - DOMAIN[0][1]) / NY))
-    # the reference drivers' solver settings (benchmarks_2d_bubble_rising.cpp:78-79, global.h:49-53)
     prm.update(ppe_tol=1e-8, ppe_tol2=1e-7, ppe_max_iter=100, ppe_initer=1)
-    s = O.Checker("port").twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm,
-                                   dict(scheme=1, n_mpls=5, reinit_every=1, ppe_mode=0, reinit_lambda=1))
+    s = P.twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm,
+                   dict(scheme=1, n_mpls=5, reinit_every=1, ppe_mode=0, reinit_lambda=1))
     s.set("phi", initial_phi(g.shape))
     s.call("init")
-    for _ in range(warmup):
+    for _ in range(5):
         s.call("step", 1)
+    step = lambda: s.call("step", 1)
+    r_all = _windows(step, 3, win_all)
+    P.lib.port_set_threads(1)
+    r_one = _windows(step, 3, win_one)
+    P.lib.port_set_threads(threads)
+    return {"all_cores": {"value": float(np.median(r_all)), "windows": r_all, "steps_per_window": win_all,
+                          "cores": threads},
+            "one_thread": {"value": float(np.median(r_one)), "windows": r_one, "steps_per_window": win_one,
+                           "cores": 1},
+            "startup_steps": 5}
+
+
+def cpu_dambreak(threads: int, win: int = 5) -> dict:
+    """The 128 x 64 x 64 dam break as the reference's driver runs it
+    (benchmarks_3d_dambreak.cpp:74-146): UCCD transport, no mass correction, ppe_tol 1e-4,
+    ppe_tol2 1e-10, ppe_max_iter 100, and iter never advanced, so ab_solve runs SOR every
+    step; reinitialisation (30 TVD-RK3 steps) every 20 steps, timed once on its own."""
+    import numpy as np
+    O, P = _port(threads)
+    g, prm, phi = dambreak_setup(O.Grid)
+    prm.update(ppe_tol=1e-4, ppe_tol2=1e-10, ppe_max_iter=100, ppe_initer=1)
+    s = P.twophase(g, ["slip"] * 6, ["neumann"] * 6, prm,
+                   dict(scheme=0, n_mpls=0, reinit_every=0, ppe_mode=0, reinit_lambda=1))
+    s.set("phi", phi)
+    s.call("init")
+
+    def step():
+        s.set_scalars(iter=0.0)
+        s.call("step", 1)
+
+    step()
+    r_all = _windows(step, 3, win)
     t0 = time.perf_counter()
-    n = 0
-    while n < steps:
-        s.call("step", 1)
-        n += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return n / dt, n
+    s.call("reinit")
+    reinit_s = time.perf_counter() - t0
+    P.lib.port_set_threads(1)
+    r_one = _windows(step, 3, 1)
+    P.lib.port_set_threads(threads)
+    med = float(np.median(r_all))
+    return {"all_cores": {"value": med, "windows": r_all, "steps_per_window": win, "cores": threads},
+            "one_thread": {"value": float(np.median(r_one)), "windows": r_one, "steps_per_window": 1, "cores": 1},
+            "reinit_s_all_cores": reinit_s,
+            "with_reinit_every_20": 1.0 / (1.0 / med + reinit_s / 20.0),
+            "unit": "steps/s",
+            "note": "windows exclude the reinitialisation; with_reinit_every_20 adds it at the driver's rate "
+                    "(the GPU figure includes it)"}
+
+
+def spheres_field(n: int):
+    """The construction of poisson_problem on the host (same seeded generator, same draws) on an
+    n^3 grid: (density, right-hand side = div of the random wall-tight face velocity, mean
+    removed) as ghosted float64 arrays."""
+    import numpy as np
+    import torch
+    gen = torch.Generator(device="cpu").manual_seed(20261203)
+    h = 1.0 / n
+    c = (np.arange(n) + 0.5) * h
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    phi = np.full((n, n, n), -1e9)
+    for _ in range(12):
+        r = 0.05 + 0.15 * torch.rand(1, generator=gen).item()
+        cen = [r + (1 - 2 * r) * torch.rand(1, generator=gen).item() for _ in range(3)]
+        phi = np.maximum(phi, r - np.sqrt((X - cen[0]) ** 2 + (Y - cen[1]) ** 2 + (Z - cen[2]) ** 2))
+    del X, Y, Z
+    w = 1.5 * h
+    H = np.where(phi < -w, 0.0, np.where(phi > w, 1.0, 0.5 * (1 + phi / w + np.sin(np.pi * phi / w) / np.pi)))
+    rho = np.ones((n + 6,) * 3)
+    rho[3:-3, 3:-3, 3:-3] = 1.0 + 999.0 * H
+    del H, phi
+    div = np.zeros((n, n, n))
+    shapes = ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))
+    for a in range(3):
+        u = torch.rand(shapes[a], generator=gen, dtype=torch.float64).numpy() - 0.5
+        sl = [slice(None)] * 3
+        for e in (0, -1):
+            sl[a] = e
+            u[tuple(sl)] = 0.0
+        div += np.diff(u, axis=a) / h
+    rhs = np.zeros((n + 6,) * 3)
+    rhs[3:-3, 3:-3, 3:-3] = div - div.mean()
+    return rho, rhs
+
+
+def cpu_sor(threads: int) -> dict:
+    """projection()'s SOR (omega 1.5, in-place sweeps, per-sweep mean removal; the reference's
+    pressure solve for this equation, projection_method.cpp:576-627) on the spheres problem:
+    ms per sweep at 256^3 (mean of 3 sweeps all cores, 2 sweeps one thread), and the sweeps
+    and time to relative residual 1e-10 at 64^3, measured on all cores (residual formed every
+    100 sweeps).  The one-thread 64^3 time and the 256^3 time to 1e-10 are extrapolations,
+    labelled as such: SOR's sweep count grows as h^-2."""
+    O, P = _port(threads)
+    out = {}
+    g = O.Grid(3, (256,) * 3, (0.0,) * 3, (1.0,) * 3)
+    rho, rhs = spheres_field(256)
+    _, n3, _, sec = P.sor_solve(g, rho, rhs, max_sweeps=3)
+    ms_all = 1e3 * sec / n3
+    P.lib.port_set_threads(1)
+    _, n1, _, sec = P.sor_solve(g, rho, rhs, max_sweeps=2, parallel=False)
+    ms_one = 1e3 * sec / n1
+    P.lib.port_set_threads(threads)
+    del rho, rhs
+    g64 = O.Grid(3, (64,) * 3, (0.0,) * 3, (1.0,) * 3)
+    rho, rhs = spheres_field(64)
+    _, sweeps, rel, sec64 = P.sor_solve(g64, rho, rhs, rel_tol=1e-10, max_sweeps=200000, check_every=100)
+    P.lib.port_set_threads(1)
+    _, nn, _, sec1 = P.sor_solve(g64, rho, rhs, max_sweeps=200, parallel=False)
+    P.lib.port_set_threads(threads)
+    ms64_one = 1e3 * sec1 / nn
+    out["sor_ms_per_sweep_256^3"] = {"all_cores": ms_all, "one_thread": ms_one, "cores": threads}
+    out["sor_to_1e-10_64^3"] = {"sweeps": sweeps, "final_relres": rel, "all_cores_s": sec64,
+                                "one_thread_s_extrapolated": sweeps * ms64_one / 1e3,
+                                "one_thread_ms_per_sweep": ms64_one}
+    out["sor_to_1e-10_256^3_s_extrapolated"] = {
+        "all_cores": sweeps * 16 * ms_all / 1e3, "one_thread": sweeps * 16 * ms_one / 1e3,
+        "how": "sweeps at 64^3 x 16 (h^-2) x measured ms per sweep at 256^3"}
+    return out
+
+
+def cpu_multigrid_256(threads: int) -> dict:
+    """The reference multigrid (v_cycle with its steepest-descent relax, restated) on the
+    256^2 Dirichlet problem to relative residual 1e-10: median of 3 solves, all cores and
+    one thread."""
+    import numpy as np
+    O, P = _port(threads)
+    n = 256
+    g = O.Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    xc = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(xc, xc, indexing="ij")
+    rhs = -(2 * np.pi ** 2 * np.sin(np.pi * X) * np.sin(np.pi * Y)).T.ravel()
+    out = {}
+    for key, th in (("all_cores", threads), ("one_thread", 1)):
+        P.lib.port_set_threads(th)
+        P.mg_poisson(g, rhs, True, 1e-10, 400)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            _, cyc, hist = P.mg_poisson(g, rhs, True, 1e-10, 400)
+            ts.append(time.perf_counter() - t0)
+        out[key] = {"ms_to_tol": 1e3 * float(np.median(ts)), "cycles": cyc, "final_relres": float(hist[-1]),
+                    "cores": th}
+    P.lib.port_set_threads(threads)
+    return out
 
 
 def run_reference(args) -> None:
@@ -188,15 +380,19 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    rate, n = cpu_reference_rate(args.steps, min(args.warmup, 3), budget_s=120.0, threads=threads)
+    b = cpu_bubble(threads)
+    rate = b["all_cores"]["value"]
+    n = 3 * b["all_cores"]["steps_per_window"]
     line = {"metric": "time steps/s", "value": rate, "unit": "steps/s", "n_gpus": args.gpus, "steps": n,
-            "warmup": min(args.warmup, 3), "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak",
+            "warmup": b["startup_steps"], "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic bubble)",
             "config": config_block({"parallelism": "host OpenMP", "pressure_solver": "reference schedule: SOR "
                                     "for 5 steps, then fast pressure correction on the reference multigrid"}),
             "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{n} time steps after warm-up (bounded to 120 s)"},
+                             "model": cpu_model(),
+                             "sample": f"median of 3 windows of {b['all_cores']['steps_per_window']} steps after "
+                                       "the 5 start-up steps", "one_thread": b["one_thread"]},
             "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -366,8 +562,22 @@ def run_ours(args) -> None:
            "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
            "api": "scihpc_twophase_upload x4 + scihpc_twophase_step + scihpc_twophase_download x4"}
 
-    # roofline of the dominant kernel group: one V(2,2) pressure V-cycle on this grid
+    # roofline of the step's dominant kernel: the reinitialisation's gradient kernel
+    # (k_reinit_a2d, the largest share of the step's launch list), FP64-bound on
+    # L2-resident data, against the FP64 roof measured here; the pressure V-cycle (the
+    # HBM-bound kernel group at 256^3) beside it
+    from scihpc_gb300.native import measure_fp64_peak
     hbm = peaks()
+    fp64_peak = measure_fp64_peak()
+    ra_ms = tp.time_reinit_gradient(200)
+    ra_flops = REINIT_FLOPS_2D * NX * NY
+    roof = {"bound": "fp64", "kernel": "k_reinit_a2d (Godunov |grad phi| + redistance source + lambda fields)",
+            "achieved": ra_flops / (ra_ms * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": ra_flops / (ra_ms * 1e-3) / 1e12 / fp64_peak,
+            "peak_src": "measured in this run (chains of FP64 fused multiply-adds on every SM, CUDA events)",
+            "traffic": REINIT_TRAFFIC_BYTES, "alg_flops_per_launch": ra_flops, "launch_ms": ra_ms,
+            "flops_per_cell": REINIT_FLOPS_2D, "share_of_step": REINIT_SHARE,
+            "traffic_src": REINIT_TRAFFIC_SRC}
     fp32 = args.ppe == "fp32"
     ps = Poisson(g, bc=0, density=True, fp32=fp32)
     ps.set_density(tp.device_ptr("rho"))
@@ -375,12 +585,11 @@ def run_ours(args) -> None:
     ncyc = 200
     vms = ps.time_vcycles(tp.device_ptr("rhs"), ptmp, ncyc) / ncyc
     vb = vcycle_bytes(ps.levels(), 2, 4 if fp32 else 8)
-    roof = {"bound": "hbm", "kernel": f"pressure V(2,2) cycle, all levels ({'FP32' if fp32 else 'FP64'})",
-            "achieved": vb / vms / 1e6,
-            "peak": hbm["hbm_gbs"], "unit": "GB/s", "frac": vb / vms / 1e6 / hbm["hbm_gbs"],
-            "peak_src": hbm["src"], "traffic": None, "alg_bytes_per_launch": vb, "launch_ms": vms,
-            "note": "128x256 working set is L2-resident and the cycle is latency bound; achieved "
-                    "counts model bytes (the 256^3 block below is the HBM-bound case)"}
+    roof["vcycle_128x256"] = {"bound": "hbm", "kernel": f"pressure V(2,2) cycle, all levels ({'FP32' if fp32 else 'FP64'})",
+                              "achieved": vb / vms / 1e6, "peak": hbm["hbm_gbs"], "unit": "GB/s",
+                              "frac": vb / vms / 1e6 / hbm["hbm_gbs"], "peak_src": hbm["src"], "traffic": None,
+                              "alg_bytes_per_launch": vb, "launch_ms": vms,
+                              "note": "L2-resident working set: latency bound, model bytes"}
     ps.close()
 
     line = {"metric": "time steps/s", "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
@@ -393,15 +602,31 @@ def run_ours(args) -> None:
             "diagnostics": diag}
     if rank == 0 and not args.no_poisson:
         line["poisson_256^3"] = poisson_block(torch, Poisson, Grid, hbm)
-        line["poisson_256^2_dirichlet"] = dirichlet_block(torch, Poisson, Grid, cpu=not args.no_cpu)
+        v = line["poisson_256^3"]["fp32_refined"]
+        roof["vcycle_256^3"] = {"bound": "hbm", "kernel": "pressure V(2,2) cycle, all levels (FP32), 256^3",
+                                "achieved": v["vcycle_gbs"], "peak": hbm["hbm_gbs"], "unit": "GB/s",
+                                "frac": v["vcycle_frac_of_hbm"], "peak_src": hbm["src"],
+                                "alg_bytes_per_launch": v["vcycle_alg_bytes"], "launch_ms": v["vcycle_ms"],
+                                "traffic": VCYCLE_256_TRAFFIC_BYTES, "traffic_src": VCYCLE_256_TRAFFIC_SRC}
+        line["poisson_256^2_dirichlet"] = dirichlet_block(torch, Poisson, Grid, cpu=False)
         line["dambreak_3d"] = dambreak_block(torch, TwoPhase, Grid)
         line["learned_guess"] = learned_block(torch)
         line["learned_guess_3d"] = learned3_block(torch)
     if rank == 0 and not args.no_cpu:
-        rate, n = cpu_reference_rate(20, 2, budget_s=20.0, threads=os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{n} time steps of the same workload (reference algorithm, "
-                                          "restatement in oracle/port, all host cores)"}
+        threads = os.cpu_count() or 1
+        b = cpu_bubble(threads)
+        model = cpu_model()
+        line["cpu_baseline"] = {"value": b["all_cores"]["value"], "unit": "steps/s", "cores": threads, "kind": "port",
+                                "model": model,
+                                "sample": f"median of 3 windows of {b['all_cores']['steps_per_window']} time steps of "
+                                          "the same workload after the reference schedule's 5 start-up steps "
+                                          "(reference algorithm restated in oracle/port, all host cores)",
+                                "one_thread": b["one_thread"]}
+        line["cpu_baselines"] = {"model": model, "cores": threads,
+                                 "rising_bubble_128x256": b,
+                                 "dambreak_3d_128x64x64": cpu_dambreak(threads),
+                                 "poisson_spheres_sor": cpu_sor(threads),
+                                 "poisson_256^2_dirichlet_reference_mg": cpu_multigrid_256(threads)}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

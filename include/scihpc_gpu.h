@@ -308,6 +308,14 @@ int scihpc_twophase_stream(scihpc_twophase *tp, void **stream);
 int scihpc_twophase_graph_stats(scihpc_twophase *tp, long long out[4]);
 /* Statistics of the last pressure solve: {iterations, relative residual, ms}. */
 int scihpc_twophase_ppe_stats(scihpc_twophase *tp, double out[3]);
+/* Measurement hooks with no reference counterpart.  time_reinit_gradient: ms per launch of
+ * the reinitialisation's gradient kernel (Godunov |grad phi|, the redistance source and the
+ * lambda fields, godunov_gradient.cpp:7-157 and source.cpp:157-198), n back-to-back launches
+ * timed with CUDA events on the session's stream (synchronises).  measure_fp64_peak: FP64
+ * TFLOP/s of chains of fused multiply-adds over all SMs (best of 5 launches; allocates and
+ * synchronises the device). */
+int scihpc_twophase_time_reinit_gradient(scihpc_twophase *tp, int n, float *ms);
+int scihpc_measure_fp64_peak(double *tflops);
 
 /* ------------------------------------------------------------------ tensor-core convolutions
  * 3x3 convolution, stride 1, zero padding 1, as implicit GEMM on the tcgen05 tensor cores

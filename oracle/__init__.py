@@ -229,6 +229,22 @@ class Checker:
                                       max_iter, ctypes.byref(rel))
         return p, it, rel.value
 
+    def sor_solve(self, g: Grid, rho, rhs, p0=None, omega=1.5, parallel=True, rel_tol=0.0, max_sweeps=1,
+                  check_every=0):
+        """projection()'s SOR sweeps (port_sor_solve); returns (p, sweeps, relative residual,
+        seconds spent in the sweep loop)."""
+        assert self.which == "port"
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        p = np.zeros(g.shape) if p0 is None else np.ascontiguousarray(p0, dtype=np.float64).copy()
+        rel = ctypes.c_double(1.0)
+        sec = ctypes.c_double(0.0)
+        n, lo, hi = g.c_args()
+        it = self.lib.port_sor_solve(g.ndim, n, lo, hi, _p(rho), _p(rhs), _p(p), ctypes.c_double(omega),
+                                     int(parallel), ctypes.c_double(rel_tol), int(max_sweeps), int(check_every),
+                                     ctypes.byref(rel), ctypes.byref(sec))
+        return p, it, rel.value, sec.value
+
     def twophase(self, g: Grid, vel_bc, scalar_bc, prm: dict, opt: dict) -> "TwoPhaseState":
         return TwoPhaseState(self, g, vel_bc, scalar_bc, prm, opt)
 

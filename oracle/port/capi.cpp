@@ -1,10 +1,13 @@
 // capi.cpp -- TEST INFRASTRUCTURE (CPU restatement, see port.h).
 // extern "C" entry points of the restatement, with the same argument conventions as the
 // reference shim (oracle/ref_shim.cpp) so that tests can call either through ctypes.
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <omp.h>
 
 #include "mg.h"
 #include "port.h"
@@ -190,6 +193,108 @@ int port_coef_solve(int ndim, const int *n, const double *lo, const double *hi, 
                          tp.CB.data(), rhs, p, rel_tol, max_iter, relres);
 }
 
+// The SOR sweeps of projection() (projection_method.cpp:576-627) on the equation of
+// init_ppe_proj_coefficients for a given density, for CPU timing: in-place over-relaxed
+// Gauss-Seidel with omega, per-sweep mean removal and the Neumann fill of p.  parallel = 1
+// runs the sweep as the reference does under OpenMP (one parallel loop over the cells with
+// in-place updates, racy like the reference's); 0 in lexicographic order.  Every check_every
+// sweeps (0: never) the relative residual ||rhs - A p|| / ||rhs|| (rhs mean removed) is
+// formed, and the loop stops once it is at most rel_tol or after max_sweeps.
+int port_sor_solve(int ndim, const int *n, const double *lo, const double *hi, const double *rho, const double *rhs,
+                   double *p, double omega, int parallel, double rel_tol, int max_sweeps, int check_every,
+                   double *relres, double *seconds) {
+    Grid g = make_grid(ndim, n, lo, hi);
+    const int sb[6] = {1, 1, 1, 1, 1, 1};
+    const size_t sx = g.stride(0), sy = g.stride(1), sz = g.stride(2);
+    const long long cells = (long long)g.n[0] * g.n[1] * g.n[2];
+    // init_ppe_proj_coefficients (projection_method.cpp:404-465)
+    std::vector<double> C7[7];
+    for (auto &c : C7) c.assign(g.size(), 0.0);
+    double *CC = C7[0].data(), *CR = C7[1].data(), *CL = C7[2].data(), *CU = C7[3].data(), *CD = C7[4].data(),
+           *CF = C7[5].data(), *CB = C7[6].data();
+#pragma omp parallel for collapse(3)
+    for (int I = 0; I < g.n[0]; ++I)
+        for (int J = 0; J < g.n[1]; ++J)
+            for (int K = 0; K < g.n[2]; ++K) {
+                const size_t o = g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K));
+                auto c = [&](size_t st, double d, bool wall) {
+                    return wall ? 0.0 : 1.0 / (0.5 * (rho[o] + rho[o + st])) / d / d;
+                };
+                CR[o] = c(sx, g.d[0], I == g.n[0] - 1);
+                CL[o] = c(-sx, g.d[0], I == 0);
+                CU[o] = c(sy, g.d[1], J == g.n[1] - 1);
+                CD[o] = c(-sy, g.d[1], J == 0);
+                if (g.ndim > 2) {
+                    CF[o] = c(sz, g.d[2], K == g.n[2] - 1);
+                    CB[o] = c(-sz, g.d[2], K == 0);
+                }
+                CC[o] = -(CR[o] + CL[o] + CU[o] + CD[o]) - (CF[o] + CB[o]);
+            }
+    double mean = 0.0, bn = 0.0;
+    for (int I = 0; I < g.n[0]; ++I)
+        for (int J = 0; J < g.n[1]; ++J)
+            for (int K = 0; K < g.n[2]; ++K) mean += rhs[g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K))];
+    mean /= double(cells);
+    for (int I = 0; I < g.n[0]; ++I)
+        for (int J = 0; J < g.n[1]; ++J)
+            for (int K = 0; K < g.n[2]; ++K) {
+                const double b = rhs[g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K))] - mean;
+                bn += b * b;
+            }
+    bn = std::sqrt(bn);
+    auto cell = [&](int I, int J, int K, double &sump) {
+        const size_t o = g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K));
+        double pn = rhs[o] - (CL[o] * p[o - sx] + CR[o] * p[o + sx] + CD[o] * p[o - sy] + CU[o] * p[o + sy]);
+        if (g.ndim > 2) pn -= CB[o] * p[o - sz] + CF[o] * p[o + sz];
+        pn /= CC[o];
+        p[o] = omega * pn + (1.0 - omega) * p[o];
+        sump += p[o];
+    };
+    static const double zero[6] = {0, 0, 0, 0, 0, 0};
+    int it = 0;
+    double rel = 1.0;
+    const auto t0 = std::chrono::steady_clock::now();
+    while (it < max_sweeps) {
+        double sump = 0.0;
+        if (parallel) {
+#pragma omp parallel for collapse(3) reduction(+ : sump)
+            for (int I = 0; I < g.n[0]; ++I)
+                for (int J = 0; J < g.n[1]; ++J)
+                    for (int K = 0; K < g.n[2]; ++K) cell(I, J, K, sump);
+        } else {
+            for (int I = 0; I < g.n[0]; ++I)
+                for (int J = 0; J < g.n[1]; ++J)
+                    for (int K = 0; K < g.n[2]; ++K) cell(I, J, K, sump);
+        }
+        sump /= double(cells);
+#pragma omp parallel for collapse(3)
+        for (int I = 0; I < g.n[0]; ++I)
+            for (int J = 0; J < g.n[1]; ++J)
+                for (int K = 0; K < g.n[2]; ++K) p[g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K))] -= sump;
+        bc_fill(g, LOC_NODE, sb, zero, p);
+        ++it;
+        if (check_every > 0 && it % check_every == 0) {
+            double rr = 0.0;
+#pragma omp parallel for collapse(3) reduction(+ : rr)
+            for (int I = 0; I < g.n[0]; ++I)
+                for (int J = 0; J < g.n[1]; ++J)
+                    for (int K = 0; K < g.n[2]; ++K) {
+                        const size_t o = g.at(g.ix(0, I), g.ix(1, J), g.ix(2, K));
+                        double a = CC[o] * p[o] + CL[o] * p[o - sx] + CR[o] * p[o + sx] + CD[o] * p[o - sy] +
+                                   CU[o] * p[o + sy];
+                        if (g.ndim > 2) a += CB[o] * p[o - sz] + CF[o] * p[o + sz];
+                        const double r = rhs[o] - mean - a;
+                        rr += r * r;
+                    }
+            rel = std::sqrt(rr) / bn;
+            if (rel <= rel_tol) break;
+        }
+    }
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (relres) *relres = rel;
+    return it;
+}
+
 // ---------------------------------------------------------------- two-phase state
 void *port_tp_create(int ndim, const int *n, const double *lo, const double *hi, const int *vel_bc,
                      const int *scalar_bc, const double *prm, const int *opt) {
@@ -259,6 +364,12 @@ int port_tp_set_scalars(void *h, const double *in) {
 int port_tp_set_exact_tol(void *h, double tol) {
     static_cast<TwoPhase *>(h)->exact_tol = tol;
     return 0;
+}
+
+// OpenMP threads of the restatement's parallel loops from now on (CPU timing)
+int port_set_threads(int n) {
+    omp_set_num_threads(n > 0 ? n : 1);
+    return n;
 }
 
 int port_tp_set_fpc_cycles(void *h, int n) {

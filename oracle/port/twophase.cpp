@@ -592,6 +592,9 @@ int TwoPhase::projection(bool exact) {
             std::memcpy(tmp.data(), pp.data(), N * sizeof(double));   // store_tmp
             sump = 0.0;
             error = 0.0;
+            // the reference's loop (projection_method.cpp:578-606): one OpenMP loop over the
+            // cells updating p in place -- lexicographic with one thread, racy with more
+#pragma omp parallel for collapse(3) reduction(+ : sump, error)
             for (int I = 0; I < g.n[0]; ++I)
                 for (int J = 0; J < g.n[1]; ++J)
                     for (int K = 0; K < g.n[2]; ++K) {

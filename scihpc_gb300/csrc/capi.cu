@@ -586,6 +586,57 @@ int scihpc_twophase_stream(scihpc_twophase *tp, void **stream) {
     return SCIHPC_OK;
 }
 
+int scihpc_twophase_time_reinit_gradient(scihpc_twophase *tp, int n, float *ms) {
+    REQUIRE(tp && ms && n > 0, "twophase_time_reinit_gradient: bad argument");
+    return tp->tp.time_reinit_gradient(n, ms);
+}
+
+// FP64 roof of this GPU: independent chains of fused multiply-adds per thread, enough
+// blocks for every SM; 2 flops per FMA.
+namespace {
+constexpr int FP64_CHAINS = 8;
+__global__ void k_fp64_fma_chains(double *out, int iters, double b, double c) {
+    double a[FP64_CHAINS];
+    for (int k = 0; k < FP64_CHAINS; ++k) a[k] = double(threadIdx.x + k);
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int k = 0; k < FP64_CHAINS; ++k) a[k] = fma(a[k], b, c);
+    double s = 0.0;
+    for (int k = 0; k < FP64_CHAINS; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+int scihpc_measure_fp64_peak(double *tflops) {
+    REQUIRE(tflops, "measure_fp64_peak: NULL argument");
+    const int blocks = NUM_SMS * 8, threads = 256, iters = 4096;
+    double *out = nullptr;
+    SCIHPC_CUDA(cudaMalloc(&out, size_t(blocks) * threads * sizeof(double)));
+    cudaEvent_t e0, e1;
+    SCIHPC_CUDA(cudaEventCreate(&e0));
+    SCIHPC_CUDA(cudaEventCreate(&e1));
+    // b slightly below 1 keeps the chains finite; c breaks any algebraic shortcut
+    for (int w = 0; w < 2; ++w) k_fp64_fma_chains<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    float best = 1e30f;
+    for (int r = 0; r < 5; ++r) {
+        cudaEventRecord(e0);
+        k_fp64_fma_chains<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, e0, e1);
+        best = t < best ? t : best;
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) return cuda_fail(err, "fp64 peak kernel", __FILE__, __LINE__);
+    const double flops = 2.0 * double(blocks) * threads * iters * FP64_CHAINS;
+    *tflops = flops / (double(best) * 1e-3) / 1e12;
+    return SCIHPC_OK;
+}
+
 int scihpc_twophase_graph_stats(scihpc_twophase *tp, long long out[4]) {
     REQUIRE(tp && out, "twophase_graph_stats: NULL argument");
     return tp->tp.graph_stats(out);

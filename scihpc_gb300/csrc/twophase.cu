@@ -1590,6 +1590,36 @@ int TwoPhaseGpu::step(int nsteps, bool use_graph) {
     return SCIHPC_OK;
 }
 
+// Measurement hook: n back-to-back launches of the reinitialisation's gradient kernel (the
+// Godunov gradient, the redistance source and the lambda fields of stage 1: k_reinit_a2d in
+// 2D, k_reinit_a in 3D) between CUDA events on the session's stream.  The kernel reads phi,
+// sign and delta and rewrites the same outputs each time, so the launches are identical.
+int TwoPhaseGpu::time_reinit_gradient(int n, float *ms) {
+    cudaEvent_t e0, e1;
+    SCIHPC_CUDA(cudaEventCreate(&e0));
+    SCIHPC_CUDA(cudaEventCreate(&e1));
+    const unsigned nbi = blocks_for(D.interior(), TPB);
+    auto launch = [&]() {
+        if (D.ndim == 2)
+            k_reinit_a2d<<<dim3(unsigned((D.n[1] + RA_TJ - 1) / RA_TJ), unsigned((D.n[0] + RA_TI - 1) / RA_TI)), RA_NT,
+                           0, stream>>>(phi.data, sign, delta, grad, s1, a_f, b_f, D, P.rdt, sc);
+        else
+            k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, s1, a_f, b_f, D, P.rdt, sc);
+    };
+    for (int k = 0; k < 3; ++k) launch();
+    SCIHPC_CUDA(cudaEventRecord(e0, stream));
+    for (int k = 0; k < n; ++k) launch();
+    SCIHPC_CUDA(cudaEventRecord(e1, stream));
+    SCIHPC_CUDA(cudaEventSynchronize(e1));
+    SCIHPC_CUDA(cudaGetLastError());
+    float t = 0.0f;
+    SCIHPC_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / float(n);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return SCIHPC_OK;
+}
+
 int TwoPhaseGpu::graph_stats(long long *out) {
     SCIHPC_CUDA(cudaMemcpyAsync(sc_host, sc, sizeof(StepScalars), cudaMemcpyDeviceToHost, stream));
     SCIHPC_CUDA(cudaStreamSynchronize(stream));

@@ -87,6 +87,7 @@ public:
     int step(int nsteps, bool graph);
     int diagnostics(double *out);
     int graph_stats(long long *out);   // kernel nodes {pre, body, post}, PPE iterations summed over steps
+    int time_reinit_gradient(int n, float *ms);   // ms per launch of the reinit gradient kernel
 
     cudaStream_t stream = nullptr;
     Dims D{};

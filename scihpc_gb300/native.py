@@ -145,6 +145,8 @@ _SIGS = {
     "scihpc_twophase_projection": ([_vp, _ip, _dp], ctypes.c_int),
     "scihpc_twophase_node_from_face": ([_vp], ctypes.c_int),
     "scihpc_twophase_set_ppe_schedule": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "scihpc_twophase_time_reinit_gradient": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "scihpc_measure_fp64_peak": ([_dp], ctypes.c_int),
     "scihpc_twophase_pressure_guess": ([_vp], ctypes.c_int),
     "scihpc_twophase_fpc_coefficients": ([_vp], ctypes.c_int),
     "scihpc_twophase_fast_pressure_correction": ([_vp, _ip, _dp], ctypes.c_int),
@@ -475,10 +477,24 @@ class TwoPhase:
     def download_ptr(self, name: str, host_ptr: int) -> None:
         self.L.check(self.L.scihpc_twophase_download(self.h, name.encode(), ctypes.cast(host_ptr, _dp)))
 
+    def time_reinit_gradient(self, n: int = 100) -> float:
+        """ms per launch of the reinitialisation's gradient kernel (measurement hook)."""
+        ms = ctypes.c_float(0.0)
+        self.L.check(self.L.scihpc_twophase_time_reinit_gradient(self.h, n, ctypes.byref(ms)))
+        return ms.value
+
     def ppe_stats(self) -> dict:
         out = (ctypes.c_double * 3)()
         self.L.check(self.L.scihpc_twophase_ppe_stats(self.h, out))
         return dict(iters=out[0], relres=out[1], ms=out[2])
+
+
+def measure_fp64_peak() -> float:
+    """FP64 TFLOP/s of fused multiply-add chains on the current device (measurement hook)."""
+    L = lib()
+    t = ctypes.c_double(0.0)
+    L.check(L.scihpc_measure_fp64_peak(ctypes.byref(t)))
+    return t.value
 
 
 def conv3x3(x, w, bias, out, h: int, wd: int, ci: int, co: int, relu: bool = False):
