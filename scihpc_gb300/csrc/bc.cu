@@ -111,6 +111,32 @@ __global__ void bc_axis_kernel(double *__restrict__ f, Dims D, AxisFill P) {
     fill_line(l, sa, D.n[P.a], false, P.face, P.tl, P.vl, dh);
 }
 
+// The same fill for up to three independent fields in one launch per axis: thread t fills
+// line t % lines of field t / lines (the fields are different arrays, so their lines never
+// touch one another; the axes still go x, y, z, one launch each).
+struct AxisFillMany {
+    double *f[3];
+    AxisFill P[3];
+};
+
+__global__ void bc_axis_many_kernel(AxisFillMany M, int nf, Dims D, int a, int fast, int slow) {
+    const long long nfa = D.n[fast], ns = D.n[slow], lines = nfa * ns;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lines * nf) return;
+    const int fi = int(t / lines);
+    const long long u = t - fi * lines;
+    const AxisFill &P = M.P[fi];
+    int idx[3];
+    idx[a] = 0;
+    idx[fast] = D.ix(fast, int(u % nfa));
+    idx[slow] = D.ix(slow, int(u / nfa));
+    double *l = M.f[fi] + D.at(idx[0], idx[1], idx[2]);
+    const long long sa = D.s[a];
+    const double dh = D.d[a];
+    fill_line(l, sa, D.n[a], true, P.face, P.tr, P.vr, dh);
+    fill_line(l, sa, D.n[a], false, P.face, P.tl, P.vl, dh);
+}
+
 // Clamp of an array index to the extrapolation source along one axis (flux.cpp:98-330,
 // simple_bc.cpp:7-43): ghosts copy the boundary cell; on a staggered axis the left ghosts
 // copy the wall face at index GHC-1.
@@ -161,6 +187,28 @@ void launch_bc_fill(const Dims &D, int location, const int *types, const double 
         P.vr = values[2 * a + 1];
         const long long lines = (long long)D.n[b] * D.n[c];
         bc_axis_kernel<<<blocks_for(lines, 128), 128, 0, s>>>(f, D, P);
+    }
+}
+
+void launch_bc_fill_many(const Dims &D, int nf, const int *locations, const int *const *types, const double *values,
+                         double *const *f, cudaStream_t s) {
+    for (int a = 0; a < D.ndim; ++a) {
+        AxisFillMany M{};
+        const int b = (a + 1) % 3, c = (a + 2) % 3;
+        for (int q = 0; q < nf; ++q) {
+            AxisFill &P = M.P[q];
+            P.a = a;
+            P.fast = b > c ? b : c;
+            P.slow = b > c ? c : b;
+            P.face = locations[q] == a + 1;
+            P.tl = types[q][2 * a];
+            P.tr = types[q][2 * a + 1];
+            P.vl = values[2 * a];
+            P.vr = values[2 * a + 1];
+            M.f[q] = f[q];
+        }
+        const long long lines = (long long)D.n[b] * D.n[c];
+        bc_axis_many_kernel<<<blocks_for(lines * nf, 128), 128, 0, s>>>(M, nf, D, a, b > c ? b : c, b > c ? c : b);
     }
 }
 

@@ -162,6 +162,10 @@ __host__ __device__ inline void split3_full(long long q, const Dims &D, int &i, 
 
 // ---------------------------------------------------------------- kernels used across files
 void launch_bc_fill(const Dims &D, int location, const int *types, const double *values, double *f, cudaStream_t s);
+// nf (<= 3) independent fields filled together, one launch per axis: field q at location
+// locations[q] with face types types[q][6]; `values` (the faces' bc values) are shared
+void launch_bc_fill_many(const Dims &D, int nf, const int *locations, const int *const *types, const double *values,
+                         double *const *f, cudaStream_t s);
 void launch_extrapolate(const Dims &D, int location, const double *data, double *flux, cudaStream_t s);
 void launch_zero_order(const Dims &D, double *f, cudaStream_t s);
 

@@ -1584,6 +1584,117 @@ __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restric
         M[e] = W[(size_t)(e / n) * w + n + e % n];
 }
 
+// Inverse of the coarsest-level matrix from its band.  In the coarsest level's ordering (k
+// fastest) the 5/7-point operator is banded with half-bandwidth bw = n1 (2D) or n1 n2 (3D).
+// For Neumann walls the last unknown is pinned (its row and column replaced by those of the
+// identity), which leaves the matrix SPD; the inverse applied to a right-hand side with zero
+// mean then gives a solution that differs from the zero-mean one by a constant, so the
+// matrix stored is P A_pin^-1 E: column n-1 zeroed (E) and every column's mean subtracted (P).
+// Applied to b - mean(b) it gives the same zero-mean solution as the inverse of the
+// rank-one-pinned matrix (the rows of A sum to zero).  Every block factors the band
+// (Cholesky, right-looking, in shared memory: ~n bw^2 / 2 FMAs) and then each warp solves for
+// its own columns (forward and backward substitution, the bw-term sums split over the lanes
+// and reduced in a fixed order), so the blocks never wait on one another.  src holds the
+// assembled n x n matrix, dst receives the inverse (different buffers: blocks read src while
+// others write dst).
+constexpr int BAND_THREADS = 256;
+constexpr int BAND_WARPS = BAND_THREADS / 32;
+constexpr size_t BAND_SMEM_LIMIT = 44 * 1024;   // dynamic shared memory without an opt-in attribute
+
+inline size_t band_smem(int n, int bw) { return sizeof(double) * size_t(n) * size_t(bw + 2 + BAND_WARPS); }
+
+__global__ void __launch_bounds__(BAND_THREADS) k_band_inverse(const double *__restrict__ src, double *__restrict__ dst,
+                                                               int n, int bw, int neumann) {
+    extern __shared__ double band_smem_raw[];
+    double *Lb = band_smem_raw;                        // Lb[i * (bw + 1) + d] = A[i][i - d]
+    double *invd = Lb + size_t(n) * (bw + 1);          // 1 / L[i][i]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double *y = invd + n + size_t(warp) * n;           // this warp's solution vector
+    const int W = bw + 1;
+    const int m = n - 1;                               // pinned unknown (Neumann)
+    for (int e = tid; e < n * W; e += BAND_THREADS) {
+        const int i = e / W, d = e - i * W;
+        double v = i - d >= 0 ? src[size_t(i) * n + (i - d)] : 0.0;
+        if (neumann && i == m) v = d == 0 ? 1.0 : 0.0;
+        Lb[e] = v;
+    }
+    __syncthreads();
+    __shared__ double dj;
+    for (int j = 0; j < n; ++j) {
+        if (tid == 0) {
+            const double d = sqrt(Lb[j * W]);
+            Lb[j * W] = d;
+            invd[j] = 1.0 / d;
+            dj = 1.0 / d;
+        }
+        __syncthreads();
+        const int iend = min(n - 1, j + bw);
+        for (int i = j + 1 + tid; i <= iend; i += BAND_THREADS) Lb[i * W + (i - j)] *= dj;
+        __syncthreads();
+        // trailing update: A[i][k] -= L[i][j] L[k][j] for j < k <= i <= j + bw
+        const int t = iend - j;   // rows below the diagonal in this column
+        for (int e = tid; e < t * (t + 1) / 2; e += BAND_THREADS) {
+            // e -> (a, c), 0 <= c <= a < t, i = j + 1 + a, k = j + 1 + c
+            int a = int((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+            while (a * (a + 1) / 2 > e) --a;
+            while ((a + 1) * (a + 2) / 2 <= e) ++a;
+            const int c = e - a * (a + 1) / 2;
+            const int i = j + 1 + a, k = j + 1 + c;
+            Lb[i * W + (i - k)] -= Lb[i * W + (i - j)] * Lb[k * W + (k - j)];
+        }
+        __syncthreads();
+    }
+    // columns of the inverse, one warp per column
+    const int nwarps = gridDim.x * BAND_WARPS;
+    for (int c = blockIdx.x * BAND_WARPS + warp; c < n; c += nwarps) {
+        const bool zero_col = neumann && c == m;
+        for (int i = lane; i < n; i += 32) y[i] = 0.0;
+        __syncwarp();
+        if (!zero_col) {
+            for (int i = c; i < n; ++i) {   // L y = e_c
+                double s = 0.0;
+                for (int d = 1 + lane; d <= bw; d += 32) {
+                    const int k = i - d;
+                    if (k >= c) s += Lb[i * W + d] * y[k];
+                }
+                for (int w = 16; w > 0; w >>= 1) s += __shfl_down_sync(0xffffffffu, s, w);
+                if (lane == 0) y[i] = ((i == c ? 1.0 : 0.0) - s) * invd[i];
+                __syncwarp();
+            }
+            for (int i = n - 1; i >= 0; --i) {   // L^T x = y, in place
+                double s = 0.0;
+                for (int d = 1 + lane; d <= bw; d += 32) {
+                    const int k = i + d;
+                    if (k < n) s += Lb[k * W + d] * y[k];
+                }
+                for (int w = 16; w > 0; w >>= 1) s += __shfl_down_sync(0xffffffffu, s, w);
+                if (lane == 0) y[i] = (y[i] - s) * invd[i];
+                __syncwarp();
+            }
+        }
+        double mean = 0.0;
+        if (neumann && !zero_col) {
+            double a = 0.0;
+            for (int i = lane; i < n; i += 32) a += y[i];
+            for (int w = 16; w > 0; w >>= 1) a += __shfl_down_sync(0xffffffffu, a, w);
+            mean = __shfl_sync(0xffffffffu, a, 0) / n;   // lane 0's sum, the same value in every lane
+        }
+        for (int i = lane; i < n; i += 32) dst[size_t(i) * n + c] = zero_col ? 0.0 : y[i] - mean;
+        __syncwarp();
+    }
+}
+
+// half-bandwidth of the coarsest level's matrix in its ordering
+static int coarse_bandwidth(const int *cn, int ndim) { return ndim == 3 ? cn[1] * cn[2] : cn[1]; }
+
+static bool band_fits(int n, int bw) { return band_smem(n, bw) <= BAND_SMEM_LIMIT; }
+
+static void launch_band_invert(const double *A, double *Minv, int n, int bw, int neumann, cudaStream_t s) {
+    const int want = (n + BAND_WARPS - 1) / BAND_WARPS;
+    const int blocks = want < NUM_SMS ? want : NUM_SMS;
+    k_band_inverse<<<blocks, BAND_THREADS, band_smem(n, bw), s>>>(A, Minv, n, bw, neumann);
+}
+
 // One block for small coarsest levels (its work matrix in shared memory when n <= 50); for n >= 128 a cluster
 // of eight blocks (the one-block elimination there is bound by the FP64 rate of a single SM).
 static void launch_dense_invert(double *M, double *W, int n, int neumann, cudaStream_t s) {
@@ -2318,9 +2429,15 @@ void Poisson::build_coarse(cudaStream_t s) {
     }
     Level<T> &C = Ls[nlev - 1];
     double *M = dense, *W = dense + size_t(ncoarse) * ncoarse;
-    if (D.ndim == 2) k_dense_build<T, 2><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, M, ncoarse, neumann);
-    else k_dense_build<T, 3><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, M, ncoarse, neumann);
-    launch_dense_invert(M, W, ncoarse, neumann, s);
+    const int bw = coarse_bandwidth(C.n, D.ndim);
+    // banded inverse where the band fits in shared memory (assembled into W, inverse into M);
+    // otherwise Gauss-Jordan on the dense matrix in place
+    const bool band = band_fits(ncoarse, bw) && std::getenv("SCIHPC_DENSE_GJ") == nullptr;
+    double *A = band ? W : M;
+    if (D.ndim == 2) k_dense_build<T, 2><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, A, ncoarse, neumann);
+    else k_dense_build<T, 3><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, A, ncoarse, neumann);
+    if (band) launch_band_invert(A, M, ncoarse, bw, neumann, s);
+    else launch_dense_invert(M, W, ncoarse, neumann, s);
 }
 
 static Outer make_outer(const Dims &D, int density, int dirichlet, const double *oc) {

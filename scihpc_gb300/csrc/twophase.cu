@@ -1044,12 +1044,18 @@ void TwoPhaseGpu::scalar_bc(double *f) {
     launch_bc_fill(D, 0, scalar_types, zero, f, stream);
 }
 
+// the components' fills are independent: one launch per axis for all of them
 void TwoPhaseGpu::vel_bc(DevScalar *v, int location_for_all) {
     static const double zero[6] = {0, 0, 0, 0, 0, 0};
+    int loc[3];
+    const int *types[3];
+    double *f[3];
     for (int c = 0; c < D.ndim; ++c) {
-        const int loc = location_for_all >= 0 ? location_for_all : 1 + c;
-        launch_bc_fill(D, loc, vel_types[c], zero, v[c].data, stream);
+        loc[c] = location_for_all >= 0 ? location_for_all : 1 + c;
+        types[c] = vel_types[c];
+        f[c] = v[c].data;
     }
+    launch_bc_fill_many(D, D.ndim, loc, types, zero, f, stream);
 }
 
 void TwoPhaseGpu::find_dt() {
@@ -1187,7 +1193,11 @@ void TwoPhaseGpu::find_source() {
         for (int c = 0; c < 3; ++c) nv[c] = a == nd - 1 || c >= nd ? nvel[c].data : fv[a][c];
         k_to_face<<<blocks_for(nface, TPB), TPB, 0, s>>>(nv[0], nv[1], nv[2], vel[0].data, vel[1].data, vel[2].data, D,
                                                          a);
-        for (int c = 0; c < nd; ++c) launch_bc_fill(D, 1 + a, vel_types[c], zero, nv[c], s);
+        {
+            const int loc[3] = {1 + a, 1 + a, 1 + a};
+            const int *types[3] = {vel_types[0], vel_types[1], vel_types[2]};
+            launch_bc_fill_many(D, nd, loc, types, zero, nv, s);
+        }
         // convection of the a-component by the face-averaged velocity (source.cpp:8-40 with
         // identity_with_extrapolation_face_*)
         DevScalar &U = vel[a];
