@@ -600,7 +600,8 @@ def run_ours(args) -> None:
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches),
             "ppe_iters_per_step": ppe_iters / args.steps, "wall_s": t_wall, "roofline": roof,
             "diagnostics": diag}
-    if rank == 0 and not args.no_poisson:
+    blocks = set(args.blocks.split(","))
+    if rank == 0 and not args.no_poisson and "poisson" in blocks:
         line["poisson_256^3"] = poisson_block(torch, Poisson, Grid, hbm)
         v = line["poisson_256^3"]["fp32_refined"]
         roof["vcycle_256^3"] = {"bound": "hbm", "kernel": "pressure V(2,2) cycle, all levels (FP32), 256^3",
@@ -608,10 +609,15 @@ def run_ours(args) -> None:
                                 "frac": v["vcycle_frac_of_hbm"], "peak_src": hbm["src"],
                                 "alg_bytes_per_launch": v["vcycle_alg_bytes"], "launch_ms": v["vcycle_ms"],
                                 "traffic": VCYCLE_256_TRAFFIC_BYTES, "traffic_src": VCYCLE_256_TRAFFIC_SRC}
-        line["poisson_256^2_dirichlet"] = dirichlet_block(torch, Poisson, Grid, cpu=False)
-        line["dambreak_3d"] = dambreak_block(torch, TwoPhase, Grid)
-        line["learned_guess"] = learned_block(torch)
-        line["learned_guess_3d"] = learned3_block(torch)
+    if rank == 0 and not args.no_poisson:
+        if "dirichlet" in blocks:
+            line["poisson_256^2_dirichlet"] = dirichlet_block(torch, Poisson, Grid, cpu=False)
+        if "dambreak" in blocks:
+            line["dambreak_3d"] = dambreak_block(torch, TwoPhase, Grid)
+        if "learned" in blocks:
+            line["learned_guess"] = learned_block(torch)
+        if "learned3" in blocks:
+            line["learned_guess_3d"] = learned3_block(torch)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         b = cpu_bubble(threads)
@@ -881,13 +887,13 @@ def learned3_block(torch, n: int = 256, ntrain: int = 16, ntest: int = 3, steps:
     return out
 
 
-def profile_poisson(precision: str) -> None:
-    """One density update and three solver iterations of the 256^3 pressure equation: the
-    small case the profiles of the pressure kernels are captured on."""
+def profile_poisson(precision: str, n: int = 256) -> None:
+    """One density update and three solver iterations of the n^3 pressure equation (the
+    spheres problem): the case the profiles of the pressure kernels are captured on."""
     import torch
     from scihpc_gb300 import Grid, Poisson, lib
     lib()
-    g, rho, rhs = poisson_problem(torch, Grid)
+    g, rho, rhs = poisson_problem(torch, Grid, n)
     ps = Poisson(g, bc=0, density=True, fp32=precision == "fp32")
     ps.set_density(rho)
     p = torch.zeros(g.shape, dtype=torch.float64, device=rho.device)
@@ -915,7 +921,10 @@ def main():
     ap.add_argument("--profile-dambreak", action="store_true",
                     help="init and two steps of the 128x64x64 dam break, kernel by kernel (profiling case)")
     ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
-                    help="only three iterations of the 256^3 pressure solve (profiling case)")
+                    help="only three iterations of the n^3 pressure solve (profiling case)")
+    ap.add_argument("--poisson-n", type=int, default=256, help="grid of --profile-poisson")
+    ap.add_argument("--blocks", default="poisson,dirichlet,dambreak,learned,learned3",
+                    help="comma-separated extra blocks of the bench line")
     args = ap.parse_args()
     if args.profile_unet:
         import torch
@@ -946,7 +955,7 @@ def main():
         tp.step(2, graph=False, sync=True)
         print(json.dumps({"profile": "dambreak 128x64x64, init + 2 steps", "scalars": tp.scalars()}))
     elif args.profile_poisson:
-        profile_poisson(args.profile_poisson)
+        profile_poisson(args.profile_poisson, args.poisson_n)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -569,9 +569,14 @@ __device__ __forceinline__ T gs_update(const Level<T> &L, int off, int s0, int s
         const T sx = C0 * nb[0] + C1 * nb[1] + C2 * nb[2] + C3 * nb[3] + C4 * nb[4] + C5 * nb[5];
         return (b + sx) * prcp(C0 + C1 + C2 + C3 + C4 + C5);
     } else if constexpr (MODE == 0) {
-        const T sx = L.cx[off - s0] * nb[0] + L.cx[off] * nb[1] + L.cy[off - s1] * nb[2] + L.cy[off] * nb[3] +
-                     L.cz[off - 1] * nb[4] + L.cz[off] * nb[5];
-        return (b + sx) * L.idg[off];
+        const T c0 = L.cx[off - s0], c1 = L.cx[off], c2 = L.cy[off - s1], c3 = L.cy[off], c4 = L.cz[off - 1],
+                c5 = L.cz[off];
+        const T sx = c0 * nb[0] + c1 * nb[1] + c2 * nb[2] + c3 * nb[3] + c4 * nb[4] + c5 * nb[5];
+        // FP32: the reciprocal of the six coefficients just read, instead of streaming the
+        // stored inverse diagonal (one array fewer per sweep); FP64 keeps the stored one
+        // (an FP64 division costs more than the load)
+        if constexpr (sizeof(T) == 4) return (b + sx) * prcp(((c0 + c1) + (c2 + c3)) + (c4 + c5));
+        else return (b + sx) * L.idg[off];
     } else {
         const T sx = cf.w[0] * (nb[0] + nb[1]) + cf.w[1] * (nb[2] + nb[3]) + cf.w[2] * (nb[4] + nb[5]);
         return (b + sx) * cf.dinv;
@@ -1597,9 +1602,13 @@ __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restric
 // and reduced in a fixed order), so the blocks never wait on one another.  src holds the
 // assembled n x n matrix, dst receives the inverse (different buffers: blocks read src while
 // others write dst).
-constexpr int BAND_THREADS = 256;
+// GB300 issues FP64 at a small fraction of its FP32 rate, shared by the warps of an SM, so
+// the kernel keeps FP64 work per SM low: two warps per block (one column each at a time),
+// as many blocks as columns need, and no FP64 arithmetic in index calculations.
+constexpr int BAND_THREADS = 64;
 constexpr int BAND_WARPS = BAND_THREADS / 32;
 constexpr size_t BAND_SMEM_LIMIT = 44 * 1024;   // dynamic shared memory without an opt-in attribute
+constexpr int BAND_MAX_BW = 64;
 
 inline size_t band_smem(int n, int bw) { return sizeof(double) * size_t(n) * size_t(bw + 2 + BAND_WARPS); }
 
@@ -1618,32 +1627,45 @@ __global__ void __launch_bounds__(BAND_THREADS) k_band_inverse(const double *__r
         if (neumann && i == m) v = d == 0 ? 1.0 : 0.0;
         Lb[e] = v;
     }
+    // pairs (a, c), c <= a < bw, of the trailing update: thread tid takes the pairs
+    // a * B + c = tid, tid + BAND_THREADS, ... with B = bw rounded up to a power of two
+    int B = 1, lb = 0;
+    while (B < bw) B <<= 1, ++lb;
+    __shared__ double rpiv;
     __syncthreads();
-    __shared__ double dj;
+    // Right-looking Cholesky.  Step j: thread 0 forms 1 / sqrt(a_jj); the update of the
+    // trailing band uses the unscaled column, a_ik -= a_ij a_kj / a_jj, so column j itself is
+    // scaled one step later, when nothing reads it any more.
     for (int j = 0; j < n; ++j) {
         if (tid == 0) {
             const double d = sqrt(Lb[j * W]);
+            const double r = 1.0 / d;
             Lb[j * W] = d;
-            invd[j] = 1.0 / d;
-            dj = 1.0 / d;
+            invd[j] = r;
+            rpiv = r;
         }
         __syncthreads();
-        const int iend = min(n - 1, j + bw);
-        for (int i = j + 1 + tid; i <= iend; i += BAND_THREADS) Lb[i * W + (i - j)] *= dj;
-        __syncthreads();
-        // trailing update: A[i][k] -= L[i][j] L[k][j] for j < k <= i <= j + bw
-        const int t = iend - j;   // rows below the diagonal in this column
-        for (int e = tid; e < t * (t + 1) / 2; e += BAND_THREADS) {
-            // e -> (a, c), 0 <= c <= a < t, i = j + 1 + a, k = j + 1 + c
-            int a = int((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
-            while (a * (a + 1) / 2 > e) --a;
-            while ((a + 1) * (a + 2) / 2 <= e) ++a;
-            const int c = e - a * (a + 1) / 2;
-            const int i = j + 1 + a, k = j + 1 + c;
-            Lb[i * W + (i - k)] -= Lb[i * W + (i - j)] * Lb[k * W + (k - j)];
+        const double r = rpiv, r2 = r * r;
+        const int t = min(n - 1, j + bw) - j;   // rows below the diagonal in column j
+        for (int e = tid; e < B * B; e += BAND_THREADS) {
+            const int a = e >> lb, c = e & (B - 1);
+            if (a < t && c <= a) {
+                const int i = j + 1 + a, k = j + 1 + c;
+                Lb[i * W + (i - k)] -= Lb[i * W + (i - j)] * Lb[k * W + (k - j)] * r2;
+            }
+        }
+        if (j > 0) {   // scale column j - 1 (no longer read)
+            const int jp = j - 1, tp = min(n - 1, jp + bw) - jp;
+            const double rp = invd[jp];
+            for (int a = tid; a < tp; a += BAND_THREADS) Lb[(jp + 1 + a) * W + (1 + a)] *= rp;
         }
         __syncthreads();
     }
+    {
+        const int jp = n - 1, tp = min(n - 1, jp + bw) - jp;
+        for (int a = tid; a < tp; a += BAND_THREADS) Lb[(jp + 1 + a) * W + (1 + a)] *= invd[jp];
+    }
+    __syncthreads();
     // columns of the inverse, one warp per column
     const int nwarps = gridDim.x * BAND_WARPS;
     for (int c = blockIdx.x * BAND_WARPS + warp; c < n; c += nwarps) {
@@ -1687,7 +1709,7 @@ __global__ void __launch_bounds__(BAND_THREADS) k_band_inverse(const double *__r
 // half-bandwidth of the coarsest level's matrix in its ordering
 static int coarse_bandwidth(const int *cn, int ndim) { return ndim == 3 ? cn[1] * cn[2] : cn[1]; }
 
-static bool band_fits(int n, int bw) { return band_smem(n, bw) <= BAND_SMEM_LIMIT; }
+static bool band_fits(int n, int bw) { return bw <= BAND_MAX_BW && band_smem(n, bw) <= BAND_SMEM_LIMIT; }
 
 static void launch_band_invert(const double *A, double *Minv, int n, int bw, int neumann, cudaStream_t s) {
     const int want = (n + BAND_WARPS - 1) / BAND_WARPS;
