@@ -1596,29 +1596,31 @@ __global__ void __launch_bounds__(1024) k_dense_pin_and_invert(double *__restric
 // mean then gives a solution that differs from the zero-mean one by a constant, so the
 // matrix stored is P A_pin^-1 E: column n-1 zeroed (E) and every column's mean subtracted (P).
 // Applied to b - mean(b) it gives the same zero-mean solution as the inverse of the
-// rank-one-pinned matrix (the rows of A sum to zero).  Every block factors the band
-// (Cholesky, right-looking, in shared memory: ~n bw^2 / 2 FMAs) and then each warp solves for
-// its own columns (forward and backward substitution, the bw-term sums split over the lanes
-// and reduced in a fixed order), so the blocks never wait on one another.  src holds the
-// assembled n x n matrix, dst receives the inverse (different buffers: blocks read src while
-// others write dst).
-// GB300 issues FP64 at a small fraction of its FP32 rate, shared by the warps of an SM, so
-// the kernel keeps FP64 work per SM low: two warps per block (one column each at a time),
-// as many blocks as columns need, and no FP64 arithmetic in index calculations.
+// rank-one-pinned matrix (the rows of A sum to zero).
+//
+// Two kernels.  k_band_factor: every block factors the band (Cholesky A_pin = L L^T,
+// right-looking, in shared memory, ~n bw^2 / 2 FMAs; no block waits for another) and each
+// warp forms columns of Y = L^-1 by forward substitution, the bw-term sums split over the
+// lanes and reduced in a fixed order.  k_band_gram: A_pin^-1 = Y^T Y, one block per column,
+// with E and P applied there.  GB300's FP64 pipe is shared by an SM's warps and its latency
+// sets the pace of the sequential parts (n pivots, n substitution rows), so the factor kernel
+// runs two warps per block on as many SMs as the columns need, forms each pivot with one
+// reciprocal square root, and keeps FP64 out of its index arithmetic.
 constexpr int BAND_THREADS = 64;
 constexpr int BAND_WARPS = BAND_THREADS / 32;
 constexpr size_t BAND_SMEM_LIMIT = 44 * 1024;   // dynamic shared memory without an opt-in attribute
 constexpr int BAND_MAX_BW = 64;
+constexpr int BAND_MAX_N = 1024;                // k_band_gram: one thread per row
 
 inline size_t band_smem(int n, int bw) { return sizeof(double) * size_t(n) * size_t(bw + 2 + BAND_WARPS); }
 
-__global__ void __launch_bounds__(BAND_THREADS) k_band_inverse(const double *__restrict__ src, double *__restrict__ dst,
-                                                               int n, int bw, int neumann) {
+__global__ void __launch_bounds__(BAND_THREADS) k_band_factor(const double *__restrict__ src, double *__restrict__ Y,
+                                                              int n, int bw, int neumann) {
     extern __shared__ double band_smem_raw[];
     double *Lb = band_smem_raw;                        // Lb[i * (bw + 1) + d] = A[i][i - d]
     double *invd = Lb + size_t(n) * (bw + 1);          // 1 / L[i][i]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    double *y = invd + n + size_t(warp) * n;           // this warp's solution vector
+    double *y = invd + n + size_t(warp) * n;           // this warp's column of Y
     const int W = bw + 1;
     const int m = n - 1;                               // pinned unknown (Neumann)
     for (int e = tid; e < n * W; e += BAND_THREADS) {
@@ -1633,14 +1635,14 @@ __global__ void __launch_bounds__(BAND_THREADS) k_band_inverse(const double *__r
     while (B < bw) B <<= 1, ++lb;
     __shared__ double rpiv;
     __syncthreads();
-    // Right-looking Cholesky.  Step j: thread 0 forms 1 / sqrt(a_jj); the update of the
-    // trailing band uses the unscaled column, a_ik -= a_ij a_kj / a_jj, so column j itself is
-    // scaled one step later, when nothing reads it any more.
+    // Step j: thread 0 forms r = 1 / sqrt(a_jj); the update of the trailing band uses the
+    // unscaled column, a_ik -= a_ij a_kj r^2, so column j is scaled one step later, when
+    // nothing reads it any more.
     for (int j = 0; j < n; ++j) {
         if (tid == 0) {
-            const double d = sqrt(Lb[j * W]);
-            const double r = 1.0 / d;
-            Lb[j * W] = d;
+            const double a = Lb[j * W];
+            const double r = rsqrt(a);
+            Lb[j * W] = a * r;
             invd[j] = r;
             rpiv = r;
         }
@@ -1661,61 +1663,72 @@ __global__ void __launch_bounds__(BAND_THREADS) k_band_inverse(const double *__r
         }
         __syncthreads();
     }
-    {
-        const int jp = n - 1, tp = min(n - 1, jp + bw) - jp;
-        for (int a = tid; a < tp; a += BAND_THREADS) Lb[(jp + 1 + a) * W + (1 + a)] *= invd[jp];
-    }
-    __syncthreads();
-    // columns of the inverse, one warp per column
+    // (column n - 1 has no entries below its diagonal)
+    // columns of Y = L^-1 (lower triangular), one warp per column
     const int nwarps = gridDim.x * BAND_WARPS;
     for (int c = blockIdx.x * BAND_WARPS + warp; c < n; c += nwarps) {
-        const bool zero_col = neumann && c == m;
-        for (int i = lane; i < n; i += 32) y[i] = 0.0;
+        for (int i = lane; i < c; i += 32) y[i] = 0.0;
         __syncwarp();
-        if (!zero_col) {
-            for (int i = c; i < n; ++i) {   // L y = e_c
-                double s = 0.0;
-                for (int d = 1 + lane; d <= bw; d += 32) {
-                    const int k = i - d;
-                    if (k >= c) s += Lb[i * W + d] * y[k];
-                }
-                for (int w = 16; w > 0; w >>= 1) s += __shfl_down_sync(0xffffffffu, s, w);
-                if (lane == 0) y[i] = ((i == c ? 1.0 : 0.0) - s) * invd[i];
-                __syncwarp();
+        for (int i = c; i < n; ++i) {   // L y = e_c
+            double s = 0.0;
+            for (int d = 1 + lane; d <= bw; d += 32) {
+                const int k = i - d;
+                if (k >= c) s += Lb[i * W + d] * y[k];
             }
-            for (int i = n - 1; i >= 0; --i) {   // L^T x = y, in place
-                double s = 0.0;
-                for (int d = 1 + lane; d <= bw; d += 32) {
-                    const int k = i + d;
-                    if (k < n) s += Lb[k * W + d] * y[k];
-                }
-                for (int w = 16; w > 0; w >>= 1) s += __shfl_down_sync(0xffffffffu, s, w);
-                if (lane == 0) y[i] = (y[i] - s) * invd[i];
-                __syncwarp();
-            }
+            for (int w = 16; w > 0; w >>= 1) s += __shfl_down_sync(0xffffffffu, s, w);
+            if (lane == 0) y[i] = ((i == c ? 1.0 : 0.0) - s) * invd[i];
+            __syncwarp();
         }
-        double mean = 0.0;
-        if (neumann && !zero_col) {
-            double a = 0.0;
-            for (int i = lane; i < n; i += 32) a += y[i];
-            for (int w = 16; w > 0; w >>= 1) a += __shfl_down_sync(0xffffffffu, a, w);
-            mean = __shfl_sync(0xffffffffu, a, 0) / n;   // lane 0's sum, the same value in every lane
-        }
-        for (int i = lane; i < n; i += 32) dst[size_t(i) * n + c] = zero_col ? 0.0 : y[i] - mean;
+        for (int i = lane; i < n; i += 32) Y[size_t(i) * n + c] = y[i];
         __syncwarp();
     }
+}
+
+// dst[r][c] = (Y^T Y)[r][c] = sum_{i >= max(r, c)} Y[i][r] Y[i][c]; Neumann: column n - 1
+// zeroed and each column's mean over r subtracted (fixed-order block sum)
+__global__ void k_band_gram(const double *__restrict__ Y, double *__restrict__ dst, int n, int neumann) {
+    __shared__ double sh[BAND_MAX_N];
+    const int c = blockIdx.x, r = threadIdx.x;
+    double x = 0.0;
+    if (r < n) {
+        double a0 = 0.0, a1 = 0.0;
+        int i = r > c ? r : c;
+        for (; i + 1 < n; i += 2) {
+            a0 += Y[size_t(i) * n + r] * Y[size_t(i) * n + c];
+            a1 += Y[size_t(i + 1) * n + r] * Y[size_t(i + 1) * n + c];
+        }
+        if (i < n) a0 += Y[size_t(i) * n + r] * Y[size_t(i) * n + c];
+        x = a0 + a1;
+    }
+    if (neumann) {
+        if (c == n - 1) x = 0.0;
+        sh[r] = r < n ? x : 0.0;
+        __syncthreads();
+        if (r == 0) {
+            double s = 0.0;
+            for (int q = 0; q < n; ++q) s += sh[q];
+            sh[0] = s / n;
+        }
+        __syncthreads();
+        x -= sh[0];
+    }
+    if (r < n) dst[size_t(r) * n + c] = x;
+}
+
+static bool band_fits(int n, int bw) {
+    return bw <= BAND_MAX_BW && n <= BAND_MAX_N && band_smem(n, bw) <= BAND_SMEM_LIMIT;
+}
+
+// A: the assembled matrix, Yw: n x n scratch, Minv: the inverse
+static void launch_band_invert(const double *A, double *Yw, double *Minv, int n, int bw, int neumann, cudaStream_t s) {
+    const int want = (n + BAND_WARPS - 1) / BAND_WARPS;
+    const int blocks = want < NUM_SMS ? want : NUM_SMS;
+    k_band_factor<<<blocks, BAND_THREADS, band_smem(n, bw), s>>>(A, Yw, n, bw, neumann);
+    k_band_gram<<<n, (n + 31) / 32 * 32, 0, s>>>(Yw, Minv, n, neumann);
 }
 
 // half-bandwidth of the coarsest level's matrix in its ordering
 static int coarse_bandwidth(const int *cn, int ndim) { return ndim == 3 ? cn[1] * cn[2] : cn[1]; }
-
-static bool band_fits(int n, int bw) { return bw <= BAND_MAX_BW && band_smem(n, bw) <= BAND_SMEM_LIMIT; }
-
-static void launch_band_invert(const double *A, double *Minv, int n, int bw, int neumann, cudaStream_t s) {
-    const int want = (n + BAND_WARPS - 1) / BAND_WARPS;
-    const int blocks = want < NUM_SMS ? want : NUM_SMS;
-    k_band_inverse<<<blocks, BAND_THREADS, band_smem(n, bw), s>>>(A, Minv, n, bw, neumann);
-}
 
 // One block for small coarsest levels (its work matrix in shared memory when n <= 50); for n >= 128 a cluster
 // of eight blocks (the one-block elimination there is bound by the FP64 rate of a single SM).
@@ -2065,15 +2078,14 @@ inline size_t coarse_smem_bytes(const std::vector<Level<T>> &Ls, int lc, int ndi
     return cells * size_t(3 + ndim) * sizeof(T);
 }
 
+// The body of the one-block coarse cycle (k_coarse_cycle), also run by block 0 of the
+// cooperative cycle (k_coop_cycle): SL, b, mean and coarse_dsm are the calling block's
+// shared memory.
 template <class T, int DIM>
-__global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, int nlev, const double *__restrict__ Minv,
-                                                        int n, int neumann, int linear, int smem_on) {
-    pdl_wait();
-    pdl_trigger();
-    extern __shared__ __align__(16) unsigned char coarse_dsm[];
-    __shared__ Level<T> SL[16];
-    __shared__ double b[1024];
-    __shared__ double mean;
+__device__ void coarse_block(const LevelPack<T> &LP, int lc, int nlev, const double *__restrict__ Minv, int n,
+                             int neumann, int linear, int smem_on, unsigned char *coarse_dsm, Level<T> *SL, double *b,
+                             double *mean_p) {
+    double &mean = *mean_p;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int nu = 2;
     // the coarsest inverse's rows, fetched now so that the dense solve does not wait for them
@@ -2160,6 +2172,70 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
     if (smem_on) {
         const long long c = LP.L[lc].cells;
         for (long long i = tid; i < c; i += nt) LP.L[lc].x[i] = SL[lc].x[i];
+    }
+}
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, int nlev, const double *__restrict__ Minv,
+                                                        int n, int neumann, int linear, int smem_on) {
+    pdl_wait();
+    pdl_trigger();
+    extern __shared__ __align__(16) unsigned char coarse_dsm[];
+    __shared__ Level<T> SL[16];
+    __shared__ double b[1024];
+    __shared__ double mean;
+    coarse_block<T, DIM>(LP, lc, nlev, Minv, n, neumann, linear, smem_on, coarse_dsm, SL, b, &mean);
+}
+
+// The V-cycle's levels l2 .. lc-1 (each at most COOP_MAX_CELLS cells) and the coarse end,
+// down and up, in one cooperative launch: every red-black colour, restriction and
+// prolongation is a grid-stride pass over the level's cells (the per-cell updates of the
+// separate kernels), with a grid-wide barrier between passes instead of a kernel boundary;
+// block 0 runs the coarse end (levels lc .. nlev-1 and the dense solve) while the others
+// wait.  The small levels' launches cost more than their work, which this removes.
+constexpr long long COOP_MAX_CELLS = 262144;
+constexpr int COOP_THREADS = 1024;
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(COOP_THREADS) k_coop_cycle(LevelPack<T> LP, int l2, int lc, int nlev,
+                                                             const double *__restrict__ Minv, int n, int neumann,
+                                                             int linear, int smem_on) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char coarse_dsm[];
+    __shared__ Level<T> SL[16];
+    __shared__ double b[1024];
+    __shared__ double mean;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long gs = (long long)gridDim.x * blockDim.x;
+    const int nu = 2;
+    for (int l = l2; l < lc; ++l) {
+        const Level<T> &L = LP.L[l];
+        const long long cnt = smooth_count<T, DIM>(L);
+        for (int k = 0; k < nu; ++k)
+            for (int color = 0; color < 2; ++color) {
+                for (long long t = gt; t < cnt; t += gs) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
+                grid.sync();
+            }
+        const Level<T> &Cl = LP.L[l + 1];
+        const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
+        for (long long t = gt; t < nc; t += gs) restrict_one<T, 0, DIM>(L, Cl, nullptr, nullptr, t);
+        grid.sync();
+    }
+    if (blockIdx.x == 0)
+        coarse_block<T, DIM>(LP, lc, nlev, Minv, n, neumann, linear, smem_on, coarse_dsm, SL, b, &mean);
+    grid.sync();
+    for (int l = lc - 1; l >= l2; --l) {
+        const Level<T> &L = LP.L[l];
+        const long long nf = (long long)L.n[0] * L.n[1] * (DIM == 3 ? L.n[2] : 1);
+        for (long long t = gt; t < nf; t += gs) prolong_one<T, DIM>(L, LP.L[l + 1], neumann, linear, t);
+        grid.sync();
+        const long long cnt = smooth_count<T, DIM>(L);
+        for (int k = 0; k < nu; ++k)
+            for (int color = 1; color >= 0; --color) {
+                for (long long t = gt; t < cnt; t += gs) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
+                grid.sync();
+            }
     }
 }
 
@@ -2330,12 +2406,16 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_coop_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_coop_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM_PRO)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_restrict3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_in_apply3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
+    rc = fp32 ? plan_coop<float>() : plan_coop<double>();
+    if (rc) return rc;
     if (const char *e = std::getenv("SCIHPC_SWEEP_TMA")) tma_enable = std::atoi(e) != 0;
     if (!density) {
         // constant coefficients: build the hierarchy once (rho unused)
@@ -2458,7 +2538,7 @@ void Poisson::build_coarse(cudaStream_t s) {
     double *A = band ? W : M;
     if (D.ndim == 2) k_dense_build<T, 2><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, A, ncoarse, neumann);
     else k_dense_build<T, 3><<<blocks_for(ncoarse, 128), 128, 0, s>>>(C, A, ncoarse, neumann);
-    if (band) launch_band_invert(A, M, ncoarse, bw, neumann, s);
+    if (band) launch_band_invert(A, W + size_t(ncoarse) * ncoarse, M, ncoarse, bw, neumann, s);
     else launch_dense_invert(M, W, ncoarse, neumann, s);
 }
 
@@ -2500,6 +2580,54 @@ int Poisson::set_density(const double *rho, cudaStream_t s) {
 
 // dot: when not null, the last level-0 sweep may also reduce <b, x> (the inner residual and the
 // preconditioned residual) into *dot; the return value says whether it did.
+// levels from this one on run inside one thread block (k_coarse_cycle)
+template <class T>
+static int coarse_start(const std::vector<Level<T>> &Ls, int nlev) {
+    int lc = nlev - 1;
+    for (int l = 1; l < nlev; ++l) {
+        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= (sizeof(T) == 4 ? COARSE_CELLS_FP32 : COARSE_CELLS_FP64)) {
+            lc = l;
+            break;
+        }
+    }
+    if (lc < 1 || nlev > 16) lc = nlev - 1 > 0 ? nlev - 1 : 0;
+    return lc;
+}
+
+// The cooperative small-level cycle is used in 3D when at least one level between the
+// coarse block's levels and COOP_MAX_CELLS exists and one block per SM fits (grid sized from
+// the occupancy, here at set-up, outside any capture).  SCIHPC_COOP=0 keeps one launch per
+// pass instead.
+template <class T>
+int Poisson::plan_coop() {
+    coop_blocks = 0;
+    coop_l2 = -1;
+    const char *e = std::getenv("SCIHPC_COOP");
+    if (D.ndim != 3 || (e && e[0] == '0')) return SCIHPC_OK;
+    std::vector<Level<T>> &Ls = levs<T>();
+    const int lc = coarse_start<T>(Ls, nlev);
+    int l2 = -1;
+    for (int l = 1; l < lc; ++l)
+        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= COOP_MAX_CELLS) {
+            l2 = l;
+            break;
+        }
+    if (l2 < 1 || nlev > 16) return SCIHPC_OK;
+    const size_t sm = coarse_smem_bytes(Ls, lc, D.ndim);
+    coop_dyn = sm <= COARSE_SMEM_MAX ? sm : 0;
+    int dev = 0, coop = 0, per_sm = 0;
+    SCIHPC_CUDA(cudaGetDevice(&dev));
+    SCIHPC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return SCIHPC_OK;
+    SCIHPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coop_cycle<T, 3>, COOP_THREADS, coop_dyn));
+    if (per_sm < 1) return SCIHPC_OK;
+    int sms = 0;
+    SCIHPC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    coop_blocks = sms;   // one block per SM: enough threads for the largest level's colour
+    coop_l2 = l2;
+    return SCIHPC_OK;
+}
+
 template <class T>
 bool Poisson::vcycle(cudaStream_t s, double *dot) {
     const bool pdl = use_pdl(s);
@@ -2527,15 +2655,11 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         }
     };
     // levels from lc on (small enough for one block) run inside one thread block
-    int lc = nlev - 1;
-    for (int l = 1; l < nlev; ++l) {
-        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= (sizeof(T) == 4 ? COARSE_CELLS_FP32 : COARSE_CELLS_FP64)) {
-            lc = l;
-            break;
-        }
-    }
+    const int lc = coarse_start<T>(Ls, nlev);
     const bool packed = nlev <= 16;   // LevelPack capacity
-    if (lc < 1 || !packed) lc = nlev - 1 > 0 ? nlev - 1 : 0;
+    // levels l2 .. lc-1 and the coarse block in one cooperative launch (3D)
+    const bool coop = coop_blocks > 0 && coop_l2 >= 1 && coop_l2 < lc && packed;
+    const int ldown = coop ? coop_l2 : lc;
     // 3D levels of at least FUSED_MIN_CELLS cells use the one-pass out-of-place sweep
     auto fused = [&](int l) {
         return D.ndim == 3 && (long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] >= FUSED_MIN_CELLS &&
@@ -2620,7 +2744,7 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         }
     };
     if (!fused(0) && !fused2(0)) cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
-    for (int l = 0; l < lc; ++l) {
+    for (int l = 0; l < ldown; ++l) {
         if (fused2(l)) {
             leg2(l, false);
             continue;
@@ -2650,7 +2774,16 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
             else launch_pdl(pdl, k_restrict<T, 2, 3>, nb, TPB, 0, s, F, Cl, rp, id2);
         }
     }
-    if (packed && lc >= 1) {
+    if (coop) {
+        LevelPack<T> LP;
+        for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
+        int on = coop_dyn > 0 ? 1 : 0;
+        int l2v = coop_l2, lcv = lc, nlv = nlev, ncv = ncoarse, nmv = neumann ? 1 : 0, lin = prolong_linear;
+        const double *mv = dense;
+        void *args[] = {&LP, &l2v, &lcv, &nlv, &mv, &ncv, &nmv, &lin, &on};
+        cudaLaunchCooperativeKernel((const void *)k_coop_cycle<T, 3>, dim3(unsigned(coop_blocks)), dim3(COOP_THREADS),
+                                    args, coop_dyn, s);
+    } else if (packed && lc >= 1) {
         LevelPack<T> LP;
         for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
         const size_t sm = coarse_smem_bytes(Ls, lc, D.ndim);
@@ -2663,7 +2796,7 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         if (D.ndim == 2) launch_pdl(pdl, k_dense_solve<T, 2>, 1, 1024, 0, s, C, dense, ncoarse, neumann);
         else launch_pdl(pdl, k_dense_solve<T, 3>, 1, 1024, 0, s, C, dense, ncoarse, neumann);
     }
-    for (int l = lc - 1; l >= 0; --l) {
+    for (int l = ldown - 1; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         if (l == 0 && pro0) {
             smooth_level(0, 1, false, true, dot != nullptr);
