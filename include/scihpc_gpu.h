@@ -349,6 +349,14 @@ int scihpc_conv3x3x3_wgrad(const void *x, const void *dz, float *dw, float *part
  * scihpc_unet_num_params entries. */
 typedef struct scihpc_unet scihpc_unet;
 int scihpc_unet_create(int h, int w, unsigned seed, scihpc_unet **out);
+/* The same 2D network run on the h x w pressure grid coarsened factor x factor (h / factor
+ * and w / factor multiples of 8): its inputs are, per coarse pixel, the mean density, the
+ * mean residual of pprev in the pressure equation (face coefficients 2 / (rho_c + rho_nb) /
+ * d^2) and the mean pprev; it predicts the mean error p - pprev per coarse pixel (training
+ * target and loss on the coarse grid, in units of a tenth of the residual's rms), and infer
+ * adds that prediction, interpolated bilinearly to the cells, to pprev.  The other
+ * scihpc_unet_* calls are unchanged. */
+int scihpc_unet_create_coarse(int h, int w, int factor, unsigned seed, scihpc_unet **out);
 /* The 3D network for an n0 x n1 x n2 pressure grid (each a multiple of 8): a 3-level U-Net
  * (16-32-64 channels, 3x3x3 convolutions on the tensor cores) at half the grid's resolution
  * (inputs averaged over 2 x 2 x 2 cells, the correction prolonged piecewise-constant).  The

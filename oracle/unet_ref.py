@@ -119,6 +119,64 @@ def pack(rho, rhs, pprev, pnew=None):
     return bf16(x0), target, sp
 
 
+def pack_coarse(rho, rhs, pprev, d, fac, pnew=None):
+    """The coarse-correction mode (scihpc_unet_create_coarse): interior 2D fields [n0][n1] and
+    the spacing d -> x0 of the (n0/fac) x (n1/fac) network image, the normalised coarse target,
+    and the output scale s_e.  Per coarse pixel: mean density, mean residual of pprev in the
+    pressure equation (face coefficient 2 / (rho_c + rho_nb) / d^2 on interior faces), mean
+    pprev; target = mean of (pnew - pprev) / s_e, s_e = 0.1 rms(r - mean r)."""
+    n0, n1 = rho.shape
+    lap = np.zeros_like(pprev)
+    for a, dd in ((0, d[0]), (1, d[1])):
+        w = 2.0 / (dd * dd)
+        lo = [slice(None)] * 2
+        hi = [slice(None)] * 2
+        lo[a], hi[a] = slice(0, -1), slice(1, None)
+        lo, hi = tuple(lo), tuple(hi)
+        flux = w / (rho[lo] + rho[hi]) * (pprev[hi] - pprev[lo])   # face between lo and hi
+        lap[lo] += flux
+        lap[hi] -= flux
+    r = rhs - lap
+    hc, wc = n0 // fac, n1 // fac
+    mean = lambda f: f.reshape(hc, fac, wc, fac).mean(axis=(1, 3))
+    cin = [f32(mean(rho)), f32(mean(r)), f32(mean(pprev))]
+    P = hc * wc
+    mr = cin[0].sum() / P
+    sd = np.sqrt(max((cin[0] * cin[0]).sum() / P - mr * mr, 0.0)) + 1e-12
+    m1 = cin[1].sum() / P
+    rr = np.sqrt(max((cin[1] * cin[1]).sum() / P - m1 * m1, 0.0)) + 1e-300
+    sp = np.sqrt((cin[2] * cin[2]).sum() / P)
+    sp = sp if sp > 0 else 1.0
+    se = 0.1 * rr
+    x0 = np.zeros((P, 16))
+    x0[:, 0] = f32((cin[0] - mr) / sd).ravel()
+    x0[:, 1] = f32((cin[1] - m1) / rr).ravel()
+    x0[:, 2] = f32(cin[2] / sp).ravel()
+    target = None if pnew is None else f32((mean(pnew - pprev) / se).ravel())
+    return bf16(x0), target, se
+
+
+def unpack_coarse(out0, pprev, se, fac):
+    """guess = pprev + se * bilinear interpolation of the coarse output (pixel centres,
+    clamped at the walls) on the interior cells."""
+    n0, n1 = pprev.shape
+    hc, wc = n0 // fac, n1 // fac
+    o = np.asarray(out0, dtype=np.float64).reshape(hc, wc)
+
+    def axis(n, nc):
+        x = np.clip((np.arange(n) + 0.5) / fac - 0.5, 0.0, nc - 1)
+        k0 = x.astype(int)
+        k1 = np.minimum(k0 + 1, nc - 1)
+        return k0, k1, x - k0
+
+    i0, i1, wi = axis(n0, hc)
+    j0, j1, wj = axis(n1, wc)
+    W_ = wi[:, None]
+    V_ = wj[None, :]
+    v = (1 - W_) * ((1 - V_) * o[i0][:, j0] + V_ * o[i0][:, j1]) + W_ * ((1 - V_) * o[i1][:, j0] + V_ * o[i1][:, j1])
+    return pprev + se * v
+
+
 def forward(params, x0, h, w):
     """All activations (BF16-rounded where the GPU stores BF16; OUT is float32)."""
     lay, _ = param_layout()

@@ -777,6 +777,21 @@ int scihpc_unet_create(int h, int w, unsigned seed, scihpc_unet **out) {
     return SCIHPC_OK;
 }
 
+int scihpc_unet_create_coarse(int h, int w, int factor, unsigned seed, scihpc_unet **out) {
+    REQUIRE(out, "unet_create_coarse: out is NULL");
+    REQUIRE(factor >= 1 && factor <= 16, "unet_create_coarse: factor must be 1 .. 16");
+    auto *u = new (std::nothrow) scihpc_unet;
+    if (!u) return SCIHPC_ERR_NOMEM;
+    int rc = u->net.create(h, w, seed, factor);
+    if (rc) {
+        u->net.destroy();
+        delete u;
+        return rc;
+    }
+    *out = u;
+    return SCIHPC_OK;
+}
+
 int scihpc_unet_create3(int n0, int n1, int n2, unsigned seed, scihpc_unet **out) {
     REQUIRE(out, "unet_create3: out is NULL");
     auto *u = new (std::nothrow) scihpc_unet;

@@ -2078,9 +2078,8 @@ inline size_t coarse_smem_bytes(const std::vector<Level<T>> &Ls, int lc, int ndi
     return cells * size_t(3 + ndim) * sizeof(T);
 }
 
-// The body of the one-block coarse cycle (k_coarse_cycle), also run by block 0 of the
-// cooperative cycle (k_coop_cycle): SL, b, mean and coarse_dsm are the calling block's
-// shared memory.
+// The body of the one-block coarse cycle (k_coarse_cycle): SL, b, mean and coarse_dsm are
+// the block's shared memory.
 template <class T, int DIM>
 __device__ void coarse_block(const LevelPack<T> &LP, int lc, int nlev, const double *__restrict__ Minv, int n,
                              int neumann, int linear, int smem_on, unsigned char *coarse_dsm, Level<T> *SL, double *b,
@@ -2185,58 +2184,6 @@ __global__ void __launch_bounds__(1024) k_coarse_cycle(LevelPack<T> LP, int lc, 
     __shared__ double b[1024];
     __shared__ double mean;
     coarse_block<T, DIM>(LP, lc, nlev, Minv, n, neumann, linear, smem_on, coarse_dsm, SL, b, &mean);
-}
-
-// The V-cycle's levels l2 .. lc-1 (each at most COOP_MAX_CELLS cells) and the coarse end,
-// down and up, in one cooperative launch: every red-black colour, restriction and
-// prolongation is a grid-stride pass over the level's cells (the per-cell updates of the
-// separate kernels), with a grid-wide barrier between passes instead of a kernel boundary;
-// block 0 runs the coarse end (levels lc .. nlev-1 and the dense solve) while the others
-// wait.  The small levels' launches cost more than their work, which this removes.
-constexpr long long COOP_MAX_CELLS = 262144;
-constexpr int COOP_THREADS = 1024;
-
-template <class T, int DIM>
-__global__ void __launch_bounds__(COOP_THREADS) k_coop_cycle(LevelPack<T> LP, int l2, int lc, int nlev,
-                                                             const double *__restrict__ Minv, int n, int neumann,
-                                                             int linear, int smem_on) {
-    namespace cg = cooperative_groups;
-    cg::grid_group grid = cg::this_grid();
-    extern __shared__ __align__(16) unsigned char coarse_dsm[];
-    __shared__ Level<T> SL[16];
-    __shared__ double b[1024];
-    __shared__ double mean;
-    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long gs = (long long)gridDim.x * blockDim.x;
-    const int nu = 2;
-    for (int l = l2; l < lc; ++l) {
-        const Level<T> &L = LP.L[l];
-        const long long cnt = smooth_count<T, DIM>(L);
-        for (int k = 0; k < nu; ++k)
-            for (int color = 0; color < 2; ++color) {
-                for (long long t = gt; t < cnt; t += gs) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
-                grid.sync();
-            }
-        const Level<T> &Cl = LP.L[l + 1];
-        const long long nc = (long long)Cl.n[0] * Cl.n[1] * (DIM == 3 ? Cl.n[2] : 1);
-        for (long long t = gt; t < nc; t += gs) restrict_one<T, 0, DIM>(L, Cl, nullptr, nullptr, t);
-        grid.sync();
-    }
-    if (blockIdx.x == 0)
-        coarse_block<T, DIM>(LP, lc, nlev, Minv, n, neumann, linear, smem_on, coarse_dsm, SL, b, &mean);
-    grid.sync();
-    for (int l = lc - 1; l >= l2; --l) {
-        const Level<T> &L = LP.L[l];
-        const long long nf = (long long)L.n[0] * L.n[1] * (DIM == 3 ? L.n[2] : 1);
-        for (long long t = gt; t < nf; t += gs) prolong_one<T, DIM>(L, LP.L[l + 1], neumann, linear, t);
-        grid.sync();
-        const long long cnt = smooth_count<T, DIM>(L);
-        for (int k = 0; k < nu; ++k)
-            for (int color = 1; color >= 0; --color) {
-                for (long long t = gt; t < cnt; t += gs) smooth_one<T, 0, DIM>(L, nullptr, nullptr, t, color);
-                grid.sync();
-            }
-    }
 }
 
 }  // namespace
@@ -2406,16 +2353,12 @@ int Poisson::create(const scihpc_grid *g, int bc, int density, int fp32) {
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_coarse_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_coop_cycle<float, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
-    SCIHPC_CUDA(cudaFuncSetAttribute(k_coop_cycle<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(COARSE_SMEM_MAX)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_sweep3_tma<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM_PRO)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_restrict3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_in_apply3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TS_SMEM)));
-    rc = fp32 ? plan_coop<float>() : plan_coop<double>();
-    if (rc) return rc;
     if (const char *e = std::getenv("SCIHPC_SWEEP_TMA")) tma_enable = std::atoi(e) != 0;
     if (!density) {
         // constant coefficients: build the hierarchy once (rho unused)
@@ -2594,40 +2537,6 @@ static int coarse_start(const std::vector<Level<T>> &Ls, int nlev) {
     return lc;
 }
 
-// The cooperative small-level cycle is used in 3D when at least one level between the
-// coarse block's levels and COOP_MAX_CELLS exists and one block per SM fits (grid sized from
-// the occupancy, here at set-up, outside any capture).  SCIHPC_COOP=0 keeps one launch per
-// pass instead.
-template <class T>
-int Poisson::plan_coop() {
-    coop_blocks = 0;
-    coop_l2 = -1;
-    const char *e = std::getenv("SCIHPC_COOP");
-    if (D.ndim != 3 || (e && e[0] == '0')) return SCIHPC_OK;
-    std::vector<Level<T>> &Ls = levs<T>();
-    const int lc = coarse_start<T>(Ls, nlev);
-    int l2 = -1;
-    for (int l = 1; l < lc; ++l)
-        if ((long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] <= COOP_MAX_CELLS) {
-            l2 = l;
-            break;
-        }
-    if (l2 < 1 || nlev > 16) return SCIHPC_OK;
-    const size_t sm = coarse_smem_bytes(Ls, lc, D.ndim);
-    coop_dyn = sm <= COARSE_SMEM_MAX ? sm : 0;
-    int dev = 0, coop = 0, per_sm = 0;
-    SCIHPC_CUDA(cudaGetDevice(&dev));
-    SCIHPC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    if (!coop) return SCIHPC_OK;
-    SCIHPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coop_cycle<T, 3>, COOP_THREADS, coop_dyn));
-    if (per_sm < 1) return SCIHPC_OK;
-    int sms = 0;
-    SCIHPC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    coop_blocks = sms;   // one block per SM: enough threads for the largest level's colour
-    coop_l2 = l2;
-    return SCIHPC_OK;
-}
-
 template <class T>
 bool Poisson::vcycle(cudaStream_t s, double *dot) {
     const bool pdl = use_pdl(s);
@@ -2657,9 +2566,6 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
     // levels from lc on (small enough for one block) run inside one thread block
     const int lc = coarse_start<T>(Ls, nlev);
     const bool packed = nlev <= 16;   // LevelPack capacity
-    // levels l2 .. lc-1 and the coarse block in one cooperative launch (3D)
-    const bool coop = coop_blocks > 0 && coop_l2 >= 1 && coop_l2 < lc && packed;
-    const int ldown = coop ? coop_l2 : lc;
     // 3D levels of at least FUSED_MIN_CELLS cells use the one-pass out-of-place sweep
     auto fused = [&](int l) {
         return D.ndim == 3 && (long long)Ls[l].n[0] * Ls[l].n[1] * Ls[l].n[2] >= FUSED_MIN_CELLS &&
@@ -2744,7 +2650,7 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         }
     };
     if (!fused(0) && !fused2(0)) cudaMemsetAsync(Ls[0].x, 0, size_t(Ls[0].cells) * sizeof(T), s);
-    for (int l = 0; l < ldown; ++l) {
+    for (int l = 0; l < lc; ++l) {
         if (fused2(l)) {
             leg2(l, false);
             continue;
@@ -2774,16 +2680,7 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
             else launch_pdl(pdl, k_restrict<T, 2, 3>, nb, TPB, 0, s, F, Cl, rp, id2);
         }
     }
-    if (coop) {
-        LevelPack<T> LP;
-        for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
-        int on = coop_dyn > 0 ? 1 : 0;
-        int l2v = coop_l2, lcv = lc, nlv = nlev, ncv = ncoarse, nmv = neumann ? 1 : 0, lin = prolong_linear;
-        const double *mv = dense;
-        void *args[] = {&LP, &l2v, &lcv, &nlv, &mv, &ncv, &nmv, &lin, &on};
-        cudaLaunchCooperativeKernel((const void *)k_coop_cycle<T, 3>, dim3(unsigned(coop_blocks)), dim3(COOP_THREADS),
-                                    args, coop_dyn, s);
-    } else if (packed && lc >= 1) {
+    if (packed && lc >= 1) {
         LevelPack<T> LP;
         for (int l = 0; l < nlev && l < 16; ++l) LP.L[l] = Ls[l];
         const size_t sm = coarse_smem_bytes(Ls, lc, D.ndim);
@@ -2796,7 +2693,7 @@ bool Poisson::vcycle(cudaStream_t s, double *dot) {
         if (D.ndim == 2) launch_pdl(pdl, k_dense_solve<T, 2>, 1, 1024, 0, s, C, dense, ncoarse, neumann);
         else launch_pdl(pdl, k_dense_solve<T, 3>, 1, 1024, 0, s, C, dense, ncoarse, neumann);
     }
-    for (int l = ldown - 1; l >= 0; --l) {
+    for (int l = lc - 1; l >= 0; --l) {
         Level<T> &F = Ls[l], &Cl = Ls[l + 1];
         if (l == 0 && pro0) {
             smooth_level(0, 1, false, true, dot != nullptr);

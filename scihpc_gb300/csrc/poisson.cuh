@@ -153,12 +153,6 @@ private:
     bool tma_ready = false, tma_pro_ready = false;
     int tma_enable = 1;
     int ncoarse = 0;
-    // cooperative small-level cycle (k_coop_cycle, 3D): its first level, grid and shared memory;
-    // coop_blocks 0 = not used
-    int coop_l2 = -1, coop_blocks = 0;
-    size_t coop_dyn = 0;
-    template <class T>
-    int plan_coop();
     const double *rhs_ = nullptr;
     double *p_ = nullptr;
 };

@@ -190,6 +190,122 @@ __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ 
     if (threadIdx.x == 0) *loss = a / double(P);
 }
 
+// ------------------------------------------------------------------ coarse-correction mode
+// With factor F > 1 the network sees the pressure grid coarsened F x F: per coarse pixel the
+// mean density, the mean residual of the previous pressure r = rhs - sum_f C_f (pprev_nb -
+// pprev_c) (C_f = 2 / (rho_c + rho_nb) / d^2 on interior faces, the pressure equation's
+// operator) and the mean previous pressure.  It predicts the mean of the error p - pprev over
+// each coarse pixel, in units of s_e = 0.1 rms(r - mean r) (the error of a residual r on the
+// unit square with density ~1-3 is about that size: e ~ rho r / k^2, k^2 >= 2 pi^2), and the
+// guess is pprev + s_e times the prediction interpolated bilinearly to the cells.  The loss is
+// on the coarse error -- the part of the error the multigrid cycle's coarse levels remove --
+// and the interpolated correction is smooth, so it adds little high-frequency residual.
+constexpr double COARSE_OUT_SCALE = 0.1;
+
+__global__ void k_coarse_inputs(const double *__restrict__ rho, const double *__restrict__ rhs,
+                                const double *__restrict__ pprev, Dims D, int fac, int Hc, int Wc,
+                                float *__restrict__ cin) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (long long)Hc * Wc) return;
+    const int I = int(p / Wc), J = int(p - (long long)I * Wc);
+    const double w0 = 2.0 / (D.d[0] * D.d[0]), w1 = 2.0 / (D.d[1] * D.d[1]);
+    double sr = 0.0, sres = 0.0, sp = 0.0;
+    for (int a = 0; a < fac; ++a)
+        for (int b = 0; b < fac; ++b) {
+            const int i = I * fac + a, j = J * fac + b;
+            const long long g = D.at(i + GHC, j + GHC, 0);
+            const double rc = rho[g];
+            sr += rc;
+            double r = rhs[g];
+            if (pprev) {
+                const double pc = pprev[g];
+                sp += pc;
+                double lap = 0.0;
+                if (i > 0) lap += w0 / (rc + rho[g - D.s[0]]) * (pprev[g - D.s[0]] - pc);
+                if (i < D.n[0] - 1) lap += w0 / (rc + rho[g + D.s[0]]) * (pprev[g + D.s[0]] - pc);
+                if (j > 0) lap += w1 / (rc + rho[g - D.s[1]]) * (pprev[g - D.s[1]] - pc);
+                if (j < D.n[1] - 1) lap += w1 / (rc + rho[g + D.s[1]]) * (pprev[g + D.s[1]] - pc);
+                r -= lap;
+            }
+            sres += r;
+        }
+    const double inv = 1.0 / double(fac * fac);
+    cin[p * 3 + 0] = float(sr * inv);
+    cin[p * 3 + 1] = float(sres * inv);
+    cin[p * 3 + 2] = float(sp * inv);
+}
+
+// st = {mean rho, std rho, mean r, rms(r - mean r), rms pprev, s_e} over the coarse pixels
+__global__ void k_stats_coarse(const float *__restrict__ cin, long long P, double *__restrict__ st) {
+    __shared__ double sh[1024];
+    double a[5] = {0, 0, 0, 0, 0};
+    for (long long p = threadIdx.x; p < P; p += blockDim.x) {
+        const double r0 = cin[p * 3], r1 = cin[p * 3 + 1], r2 = cin[p * 3 + 2];
+        a[0] += r0, a[1] += r0 * r0, a[2] += r1, a[3] += r1 * r1, a[4] += r2 * r2;
+    }
+    double t[5];
+    for (int m = 0; m < 5; ++m) t[m] = block_reduce<SumOp>(a[m], sh);
+    if (threadIdx.x == 0) {
+        const double mr = t[0] / P, m1 = t[2] / P;
+        st[0] = mr;
+        st[1] = sqrt(fmax(t[1] / P - mr * mr, 0.0)) + 1e-12;
+        st[2] = m1;
+        st[3] = sqrt(fmax(t[3] / P - m1 * m1, 0.0)) + 1e-300;
+        st[4] = sqrt(t[4] / P);
+        st[5] = COARSE_OUT_SCALE * st[3];
+    }
+}
+
+// x0 from the coarse inputs; target: the mean of (pnew - pprev) over each coarse pixel / s_e
+__global__ void k_pack_coarse(const float *__restrict__ cin, const double *__restrict__ st,
+                              const double *__restrict__ pprev, const double *__restrict__ pnew, Dims D, int fac,
+                              int Hc, int Wc, __nv_bfloat16 *__restrict__ x0, float *__restrict__ target) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (long long)Hc * Wc) return;
+    const double sp = st[4] > 0.0 ? st[4] : 1.0;
+    __nv_bfloat16 v[C_IN];
+    for (int c = 0; c < C_IN; ++c) v[c] = __float2bfloat16(0.0f);
+    v[0] = __float2bfloat16(float((double(cin[p * 3]) - st[0]) / st[1]));
+    v[1] = __float2bfloat16(float((double(cin[p * 3 + 1]) - st[2]) / st[3]));
+    v[2] = __float2bfloat16(float(double(cin[p * 3 + 2]) / sp));
+    for (int c = 0; c < C_IN; ++c) x0[p * C_IN + c] = v[c];
+    if (target) {
+        const int I = int(p / Wc), J = int(p - (long long)I * Wc);
+        double s = 0.0;
+        for (int a = 0; a < fac; ++a)
+            for (int b = 0; b < fac; ++b) {
+                const long long g = D.at(I * fac + a + GHC, J * fac + b + GHC, 0);
+                s += pnew[g] - (pprev ? pprev[g] : 0.0);
+            }
+        target[p] = float(s / double(fac * fac) / st[5]);
+    }
+}
+
+// guess = pprev + s_e * (bilinear interpolation of out[.][0] from the coarse pixel centres),
+// clamped at the walls; ghost cells copy pprev
+__global__ void k_unpack_coarse(const float *__restrict__ out, const double *__restrict__ pprev, Dims D,
+                                const double *__restrict__ st, int fac, int Hc, int Wc, double *__restrict__ guess) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= D.size()) return;
+    guess[q] = pprev ? pprev[q] : 0.0;
+    const int i = int(q / D.s[0]) - GHC, j = int((q % D.s[0]) / D.s[1]) - GHC;
+    if (i < 0 || i >= D.n[0] || j < 0 || j >= D.n[1]) return;
+    auto axis = [&](int k, int nc, int &k0, int &k1, double &w) {
+        double x = (k + 0.5) / fac - 0.5;
+        x = x < 0.0 ? 0.0 : (x > nc - 1 ? double(nc - 1) : x);
+        k0 = int(x);
+        k1 = k0 + 1 < nc ? k0 + 1 : k0;
+        w = x - k0;
+    };
+    int i0, i1, j0, j1;
+    double wi, wj;
+    axis(i, Hc, i0, i1, wi);
+    axis(j, Wc, j0, j1, wj);
+    auto O = [&](int a, int b) { return double(out[((long long)a * Wc + b) * 16]); };
+    const double v = (1.0 - wi) * ((1.0 - wj) * O(i0, j0) + wj * O(i0, j1)) + wi * ((1.0 - wj) * O(i1, j0) + wj * O(i1, j1));
+    guess[q] += st[5] * v;
+}
+
 // BF16 copies of one layer's weights: forward [co][t][ci] and data-gradient [ci][t][co] with
 // the taps flipped (t -> 8 - t)
 __global__ void k_weights_bf16(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb,
@@ -217,9 +333,17 @@ inline unsigned nblk(long long n, int t = TPB) { return unsigned((n + t - 1) / t
 
 }  // namespace
 
-int UNet::create(int h, int w, unsigned seed) {
+int UNet::create(int h, int w, unsigned seed, int factor) {
+    if (factor < 1 || h % factor || w % factor) {
+        set_last_error("unet: the coarsening factor must divide the grid");
+        return SCIHPC_ERR_ARG;
+    }
+    fac = factor;
+    PH = h, PW = w;
+    h /= factor;
+    w /= factor;
     if (h % 8 || w % 8 || h < 8 || w < 8) {
-        set_last_error("unet: image sides must be multiples of 8");
+        set_last_error("unet: image sides (after coarsening) must be multiples of 8");
         return SCIHPC_ERR_ARG;
     }
     for (int l = 0; l < 4; ++l) H[l] = h >> l, W[l] = w >> l;
@@ -260,7 +384,7 @@ int UNet::create(int h, int w, unsigned seed) {
     if ((rc = alloc_skip())) return rc;
     if ((rc = dalloc((void **)&dz, maxact * 2)) || (rc = dalloc((void **)&partial, maxpart * 4)) ||
         (rc = dalloc((void **)&target, (long long)H[0] * W[0] * 4)) || (rc = dalloc((void **)&stats, 8 * 8)) ||
-        (rc = dalloc((void **)&err, 16)))
+        (rc = dalloc((void **)&err, 16)) || (rc = dalloc((void **)&cin, (long long)H[0] * W[0] * 3 * 4)))
         return rc;
     // He-normal weights, zero biases; the last layer starts near zero (guess = previous pressure)
     std::vector<float> hw(size_t(nparam), 0.0f);
@@ -407,9 +531,17 @@ float *UNet::gconcat(int skip) {
 }
 
 int UNet::prepare(const Dims &D, const double *rho, const double *rhs, const double *pprev, const double *pnew) {
-    if (D.ndim != 2 || D.n[0] != H[0] || D.n[1] != W[0]) {
+    if (D.ndim != 2 || D.n[0] != PH || D.n[1] != PW) {
         set_last_error("unet: grid does not match the network's image size");
         return SCIHPC_ERR_ARG;
+    }
+    if (fac > 1) {
+        const long long P = (long long)H[0] * W[0];
+        k_coarse_inputs<<<nblk(P), TPB, 0, stream>>>(rho, rhs, pprev, D, fac, H[0], W[0], cin);
+        k_stats_coarse<<<1, 1024, 0, stream>>>(cin, P, stats);
+        k_pack_coarse<<<nblk(P), TPB, 0, stream>>>(cin, stats, pprev, pnew, D, fac, H[0], W[0],
+                                                   (__nv_bfloat16 *)act[X0], pnew ? target : nullptr);
+        return SCIHPC_OK;
     }
     k_stats<<<1, 1024, 0, stream>>>(rho, rhs, pprev, D, stats);
     const long long P = (long long)H[0] * W[0];
@@ -432,7 +564,11 @@ int UNet::check_err() {
 int UNet::infer(const Dims &D, const double *rho, const double *rhs, const double *pprev, double *guess) {
     int rc = prepare(D, rho, rhs, pprev, nullptr);
     if (rc || (rc = forward())) return rc;
-    k_unpack<<<nblk(D.size()), TPB, 0, stream>>>((const float *)act[OUT], pprev, D, stats, guess);
+    if (fac > 1)
+        k_unpack_coarse<<<nblk(D.size()), TPB, 0, stream>>>((const float *)act[OUT], pprev, D, stats, fac, H[0], W[0],
+                                                            guess);
+    else
+        k_unpack<<<nblk(D.size()), TPB, 0, stream>>>((const float *)act[OUT], pprev, D, stats, guess);
     SCIHPC_CUDA(cudaGetLastError());
     return check_err();
 }

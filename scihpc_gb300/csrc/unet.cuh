@@ -15,7 +15,9 @@ public:
     static constexpr int NT = 22;            // activation tensors
     static constexpr int WGRAD_SPLITS = 64;  // pixel ranges of the weight-gradient GEMMs
 
-    int create(int h, int w, unsigned seed);
+    // h, w: the pressure grid; factor 1: the network runs on it; factor F > 1: the network
+    // runs on the grid coarsened F x F (the coarse-correction mode of unet.cu)
+    int create(int h, int w, unsigned seed, int factor = 1);
     void destroy();
     long long num_params() const { return nparam; }
     int set_weights(const float *host, long long n);
@@ -41,6 +43,8 @@ private:
     float *gconcat(int skip);
 
     int H[4] = {0, 0, 0, 0}, W[4] = {0, 0, 0, 0};
+    int fac = 1, PH = 0, PW = 0;   // coarsening factor and the pressure grid it applies to
+    float *cin = nullptr;          // coarse inputs (density, residual, previous pressure) per pixel
     long long nparam = 0, woff[NL] = {}, boff[NL] = {}, wb_off[NL] = {};
     float *wmaster = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
     __nv_bfloat16 *wb = nullptr, *wt = nullptr, *dz = nullptr;

@@ -19,7 +19,7 @@ import numpy as np
 
 from .native import Grid, Poisson, UNet
 
-__all__ = ["rt_problem", "make_snapshots", "sphere_problem", "make_snapshots3", "train", "solve_iterations"]
+__all__ = ["rt_problem", "make_snapshots", "cfg4_problem", "make_snapshots_cfg4", "sphere_problem", "make_snapshots3", "train", "solve_iterations"]
 
 
 def _grid_of(rho):
@@ -60,6 +60,72 @@ def rt_problem(n: int, seed: int, drift: float, torch, device):
     rhs = torch.zeros_like(rho)
     rhs[3:-3, 3:-3, 0] = f - f.mean()
     return rho, rhs
+
+
+def cfg4_problem(n: int, seed: int, drift: float, torch, device, modes: int = 24):
+    """The learned-guess workload of the 512^2 benchmark configuration on an n x n grid of
+    [0,1]^2 (ghosted FP64 fields), sample `seed` advanced by `drift` (0 = the previous step,
+    1 = the current one): density 1 + 2 H(phi) (ratio 3, heavy above) across the interface
+    y = 0.5 + sum_{k=1..8} a_k sin(2 pi m_k x + theta_k), a_k ~ U[0, 0.02], m_k ~ U{1..8},
+    theta_k ~ U[0, 2 pi) (numpy's default generator seeded with `seed`; the phases advance by
+    0.05 per step), and a right-hand side that is the discrete divergence of a seeded random
+    face velocity with no flux through the walls: `modes` Fourier modes
+    u = A sin(pi p x) cos(pi q y), v = B cos(pi p' x) sin(pi q' y) with p, q ~ U{1..16} and
+    amplitudes ~ N(0, 1) / (p + q), perturbed by 5 % of a second draw per step."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(0.0, 0.02, 8)
+    m = rng.integers(1, 9, 8)
+    th = rng.uniform(0.0, 2 * math.pi, 8)
+    pu, qu, pv, qv = (rng.integers(1, 17, modes) for _ in range(4))
+    A = rng.standard_normal(modes) / (pu + qu) + 0.05 * drift * rng.standard_normal(modes) / (pu + qu)
+    B = rng.standard_normal(modes) / (pv + qv) + 0.05 * drift * rng.standard_normal(modes) / (pv + qv)
+    h = 1.0 / n
+    c = (torch.arange(n, dtype=torch.float64, device=device) + 0.5) * h
+    f = torch.arange(n + 1, dtype=torch.float64, device=device) * h    # face coordinates
+    X, Y = torch.meshgrid(c, c, indexing="ij")
+    iface = 0.5 + sum(float(a[k]) * torch.sin(2 * math.pi * float(m[k]) * X + float(th[k]) + 0.05 * drift)
+                      for k in range(8))
+    phi = Y - iface
+    w = 1.5 * h
+    H = torch.where(phi < -w, torch.zeros_like(phi), torch.where(phi > w, torch.ones_like(phi),
+                    0.5 * (1 + phi / w + torch.sin(math.pi * phi / w) / math.pi)))
+    rho = torch.ones((n + 6, n + 6, 1), dtype=torch.float64, device=device)
+    rho[3:-3, 3:-3, 0] = 1.0 + 2.0 * H   # the heavy fluid above the interface
+    rho[:3], rho[-3:] = rho[3:4].clone(), rho[-4:-3].clone()
+    rho[:, :3], rho[:, -3:] = rho[:, 3:4].clone(), rho[:, -4:-3].clone()
+    Xu, Yu = torch.meshgrid(f, c, indexing="ij")    # x-faces: (n + 1) x n
+    Xv, Yv = torch.meshgrid(c, f, indexing="ij")    # y-faces: n x (n + 1)
+    u = sum(float(A[k]) * torch.sin(math.pi * float(pu[k]) * Xu) * torch.cos(math.pi * float(qu[k]) * Yu)
+            for k in range(modes))
+    v = sum(float(B[k]) * torch.cos(math.pi * float(pv[k]) * Xv) * torch.sin(math.pi * float(qv[k]) * Yv)
+            for k in range(modes))
+    u[0], u[-1] = 0.0, 0.0
+    v[:, 0], v[:, -1] = 0.0, 0.0
+    div = (u[1:] - u[:-1]) / h + (v[:, 1:] - v[:, :-1]) / h
+    rhs = torch.zeros_like(rho)
+    rhs[3:-3, 3:-3, 0] = div - div.mean()
+    return rho, rhs
+
+
+def make_snapshots_cfg4(n: int, seeds, torch, device, rel_tol: float = 1e-10, fp32: bool = True):
+    """[(rho, rhs, pprev, p)] of cfg4_problem for the given seeds: pprev solves the drift-0
+    problem from zero, p the drift-1 problem from pprev (both to rel_tol, one solver)."""
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    ps = Poisson(g, bc=0, density=True, fp32=fp32)
+    out = []
+    for s in seeds:
+        rho0, rhs0 = cfg4_problem(n, s, 0.0, torch, device)
+        rho1, rhs1 = cfg4_problem(n, s, 1.0, torch, device)
+        p0 = torch.zeros_like(rho0)
+        ps.set_density(rho0)
+        ps.solve(rhs0, p0, rel_tol=rel_tol, max_iter=200)
+        p1 = p0.clone()
+        ps.set_density(rho1)
+        ps.solve(rhs1, p1, rel_tol=rel_tol, max_iter=200, use_guess=True)
+        torch.cuda.synchronize()
+        out.append((rho1, rhs1, p0, p1))
+    ps.close()
+    return out
 
 
 def make_snapshots(n: int, seeds, torch, device, rel_tol: float = 1e-10, fp32: bool = True):

@@ -129,6 +129,8 @@ _SIGS = {
                               ctypes.c_int, _vp], ctypes.c_int),
     "scihpc_unet_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_unet_create3": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)], ctypes.c_int),
+    "scihpc_unet_create_coarse": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)],
+                                  ctypes.c_int),
     "scihpc_conv3x3x3": ([_vp, _vp, _vp, _vp] + [ctypes.c_int] * 6 + [_vp], ctypes.c_int),
     "scihpc_conv3x3x3_wgrad": ([_vp, _vp, _vp, _vp] + [ctypes.c_int] * 6 + [_vp], ctypes.c_int),
     "scihpc_unet_destroy": ([_vp], ctypes.c_int),
@@ -520,13 +522,16 @@ def conv3x3x3_wgrad(x, dz, dw, partial, splits: int, d: int, h: int, wd: int, ci
 
 class UNet:
     """scihpc_unet: the learned initial guess of the pressure solve (tensor-core U-Net).
-    UNet(h, w) is the 2D network of an h x w grid; UNet(n0, n1, n2) the 3D network of an
-    n0 x n1 x n2 grid (run at half resolution)."""
+    UNet(h, w) is the 2D network of an h x w grid; UNet(h, w, factor=F) the same network on
+    the grid coarsened F x F predicting a coarse correction; UNet(n0, n1, n2) the 3D network
+    of an n0 x n1 x n2 grid (run at half resolution)."""
 
-    def __init__(self, h: int, w: int, d: int | None = None, seed: int = 0):
+    def __init__(self, h: int, w: int, d: int | None = None, seed: int = 0, factor: int = 1):
         self.L = lib()
         self.h = _vp()
-        if d is None:
+        if d is None and factor > 1:
+            self.L.check(self.L.scihpc_unet_create_coarse(h, w, factor, seed, ctypes.byref(self.h)))
+        elif d is None:
             self.L.check(self.L.scihpc_unet_create(h, w, seed, ctypes.byref(self.h)))
         else:
             self.L.check(self.L.scihpc_unet_create3(h, w, d, seed, ctypes.byref(self.h)))

@@ -114,6 +114,44 @@ def test_unet_loss_and_gradient_match_oracle():
         assert ew <= 3e-2 and eb <= 3e-2, (k, ew, eb)
 
 
+def test_unet_coarse_mode_matches_oracle():
+    """Coarse-correction mode (factor 4 on a 64 x 64 grid: a 16 x 16 network image): the
+    inputs (restricted density, residual of pprev and pprev), the loss on the restricted error
+    and every parameter gradient, and the guess (bilinear interpolation of the coarse output
+    added to pprev) against the oracle's restatement."""
+    from scihpc_gb300 import Grid, UNet
+    import oracle as O
+    n, fac = 64, 4
+    g = O.Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    rng = np.random.default_rng(9)
+    rho, rhs, pprev, pnew = _fields(g, rng)
+    net = UNet(n, n, seed=0, factor=fac)
+    params = R.init_params(6)
+    params[-16:] = rng.standard_normal(16).astype(np.float32) * 0.1
+    net.set_weights(params)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    G = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    torch.cuda.synchronize()
+    loss = net.loss_grad(G, d(rho), d(rhs), d(pprev), d(pnew))
+    grad = net.gradient()
+    I = (slice(3, -3), slice(3, -3), 0)
+    x0, target, se = R.pack_coarse(rho[I], rhs[I], pprev[I], g.spacing(), fac, pnew[I])
+    hc = n // fac
+    ref_loss, ref_grad, _ = R.loss_and_gradient(params.astype(np.float64), x0, target, hc, hc)
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss, (loss, ref_loss)
+    lay, _ = R.param_layout()
+    for k, (wo, bo) in enumerate(lay):
+        co = R.LAYERS[k][3]
+        assert rel(grad[wo:bo], ref_grad[wo:bo]) <= 3e-2 and rel(grad[bo:bo + co], ref_grad[bo:bo + co]) <= 3e-2, k
+    guess = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+    net.infer(G, d(rho), d(rhs), d(pprev), guess)
+    out = R.forward(params.astype(np.float64), x0, hc, hc)["OUT"][:, 0]
+    ref = R.unpack_coarse(out, pprev[I], se, fac)
+    gi = guess.cpu().numpy()[I]
+    assert rel(gi - pprev[I], ref - pprev[I]) <= 3e-2, rel(gi - pprev[I], ref - pprev[I])
+    net.close()
+
+
 def test_unet_guess_is_previous_pressure_when_correction_is_zero():
     """With the last layer's weights and bias at zero the guess is exactly pprev."""
     from scihpc_gb300 import Grid, UNet
