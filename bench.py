@@ -615,7 +615,7 @@ def run_ours(args) -> None:
         if "dambreak" in blocks:
             line["dambreak_3d"] = dambreak_block(torch, TwoPhase, Grid)
         if "learned" in blocks:
-            line["learned_guess"] = learned_block(torch)
+            line["learned_guess"] = learned_block(torch, ntrain=args.learned_train)
         if "learned3" in blocks:
             line["learned_guess_3d"] = learned3_block(torch)
     if rank == 0 and not args.no_cpu:
@@ -744,12 +744,13 @@ def dambreak_block(torch, TwoPhase, Grid, steps: int = 40, warmup: int = 3) -> d
 
 
 def learned_block(torch, n: int = 512, factor: int = 4, ntrain: int = 2048, ntest: int = 16,
-                  steps: int = 3000) -> dict:
+                  steps: int = 3000, chunk: int = 2048) -> dict:
     """Learned initial guess, 2D benchmark configuration: 512^2 Rayleigh-Taylor-type fields
     (density ratio 3, interface from 8 seeded sinusoids, right-hand side the divergence of a
     seeded random wall-tight velocity; learned.cfg4_problem), pairs of consecutive steps
     solved by the FP32-refined multigrid to 1e-10 on the GPU (2048 training pairs, 16 held-out
-    pairs from seeds >= 10^6).  The tensor-core U-Net (4 levels, 16-128 channels) runs on the
+    pairs from seeds >= 10^6; above `chunk` training pairs they are generated chunk by chunk
+    and visited once each).  The tensor-core U-Net (4 levels, 16-128 channels) runs on the
     grid coarsened factor x factor and predicts the coarse error of the previous pressure
     (scihpc_unet_create_coarse); Adam training on the GPU.  Time to 1e-10 on the held-out
     pairs from the previous pressure and from the network's guess (inference included), with
@@ -757,10 +758,11 @@ def learned_block(torch, n: int = 512, factor: int = 4, ntrain: int = 2048, ntes
     import time as _t
     import numpy as np
     from scihpc_gb300 import Grid, Poisson, UNet
-    from scihpc_gb300.learned import make_snapshots_cfg4, train
+    from scihpc_gb300.learned import guess_errors, make_snapshots_cfg4, train, train_cfg4_stream
     dev = torch.device("cuda")
+    stream = ntrain > chunk
     t0 = _t.perf_counter()
-    tr = make_snapshots_cfg4(n, range(ntrain), torch, dev)
+    tr = None if stream else make_snapshots_cfg4(n, range(ntrain), torch, dev)
     te = make_snapshots_cfg4(n, range(10 ** 6, 10 ** 6 + ntest), torch, dev)
     t_snap = _t.perf_counter() - t0
     net = UNet(n, n, seed=0, factor=factor)
@@ -772,10 +774,15 @@ def learned_block(torch, n: int = 512, factor: int = 4, ntrain: int = 2048, ntes
     loss_before = test_loss()
     torch.cuda.synchronize()
     t0 = _t.perf_counter()
-    losses = train(net, tr, steps, 1e-3, torch, cosine=True)
+    if stream:   # snapshot generation included in the training time
+        losses = train_cfg4_stream(net, n, range(ntrain), chunk, 1e-3, torch, dev)
+        steps = len(losses)
+    else:
+        losses = train(net, tr, steps, 1e-3, torch, cosine=True)
     torch.cuda.synchronize()
     t_train = _t.perf_counter() - t0
     loss_after = test_loss()
+    err_ratio = guess_errors(te, torch, net)
     del tr
     hc = n // factor
     layers = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (64, 128, 3),
@@ -791,10 +798,13 @@ def learned_block(torch, n: int = 512, factor: int = 4, ntrain: int = 2048, ntes
         ps.set_density(rho_b)
         torch.cuda.synchronize()
 
-    def run(use_net):
+    def run(use_net, zero=False):
         torch.cuda.synchronize()
         t1 = _t.perf_counter()
-        p_b.copy_(pp_b)
+        if zero:
+            p_b.zero_()
+        else:
+            p_b.copy_(pp_b)
         if use_net:
             net.infer(g, rho_b, rhs_b, pp_b, p_b)
         it, rr = ps.solve(rhs_b, p_b, rel_tol=1e-10, max_iter=200, use_guess=True)
@@ -806,10 +816,12 @@ def learned_block(torch, n: int = 512, factor: int = 4, ntrain: int = 2048, ntes
         run(False)
         run(True)
     res = {False: [], True: []}
+    it_zero = []
     for snap in te:
         load(snap)
         for use_net in (False, True):
             res[use_net].append(run(use_net))
+        it_zero.append(run(False, zero=True)[1])
     t_inf = []
     for _ in range(20):
         torch.cuda.synchronize()
@@ -823,9 +835,12 @@ def learned_block(torch, n: int = 512, factor: int = 4, ntrain: int = 2048, ntes
     it1 = [r[1] for r in res[True]]
     return {"grid": f"{n}x{n}", "network_grid": f"{hc}x{hc}", "train_snapshots": ntrain, "test_snapshots": ntest,
             "train_steps": steps, "snapshot_s": t_snap, "train_ms_per_step": 1e3 * t_train / steps,
+            "train_streamed": stream,
             "lr": "1e-3, half-cosine decay to 0", "test_loss_before": loss_before, "test_loss_after": loss_after,
             "train_loss_first150": float(np.mean(losses[:150])), "train_loss_last150": float(np.mean(losses[-150:])),
             "infer_ms": 1e3 * float(np.median(t_inf)), "infer_conv_tflops": flops / float(np.median(t_inf)) / 1e12,
+            "guess_error_ratio_mean": float(np.mean(err_ratio)), "guess_error_ratio_max": float(np.max(err_ratio)),
+            "vcycles_from_zero": float(np.mean(it_zero)),
             "vcycles_from_pprev": float(np.mean(it0)), "vcycles_from_net": float(np.mean(it1)),
             "pairs_fewer_iterations_with_net": int(sum(b < a for a, b in zip(it0, it1))),
             "pairs_more_iterations_with_net": int(sum(b > a for a, b in zip(it0, it1))),
@@ -845,7 +860,7 @@ def learned3_block(torch, n: int = 256, ntrain: int = 16, ntest: int = 3, steps:
     import time as _t
     import numpy as np
     from scihpc_gb300 import Grid, Poisson, UNet
-    from scihpc_gb300.learned import make_snapshots3, train
+    from scihpc_gb300.learned import guess_errors, make_snapshots3, train
     dev = torch.device("cuda")
     t0 = _t.perf_counter()
     tr = make_snapshots3(n, range(ntrain), torch, dev)
@@ -861,10 +876,15 @@ def learned3_block(torch, n: int = 256, ntrain: int = 16, ntest: int = 3, steps:
     loss_before = test_loss()
     torch.cuda.synchronize()
     t0 = _t.perf_counter()
-    losses = train(net, tr, steps, 1e-3, torch, cosine=True)
+    if stream:   # snapshot generation included in the training time
+        losses = train_cfg4_stream(net, n, range(ntrain), chunk, 1e-3, torch, dev)
+        steps = len(losses)
+    else:
+        losses = train(net, tr, steps, 1e-3, torch, cosine=True)
     torch.cuda.synchronize()
     t_train = _t.perf_counter() - t0
     loss_after = test_loss()
+    err_ratio = guess_errors(te, torch, net)
     # convolution work of one inference: 2 * 27 * ci * co per voxel of each layer's level
     layers = [(16, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (96, 32, 1), (32, 32, 1),
               (48, 16, 0), (16, 16, 0), (16, 16, 0)]
@@ -884,16 +904,20 @@ def learned3_block(torch, n: int = 256, ntrain: int = 16, ntest: int = 3, steps:
            "train_steps": steps, "snapshot_s": t_snap, "train_ms_per_step": 1e3 * t_train / steps,
            "lr": "1e-3, half-cosine decay to 0", "test_loss_before": loss_before, "test_loss_after": loss_after,
            "train_loss_first20": float(np.mean(losses[:20])), "train_loss_last20": float(np.mean(losses[-20:])),
-           "infer_ms": 1e3 * t_inf, "infer_conv_tflops": flops / t_inf / 1e12}
+           "infer_ms": 1e3 * t_inf, "infer_conv_tflops": flops / t_inf / 1e12,
+           "guess_error_ratio_mean": float(np.mean(err_ratio)), "guess_error_ratio_max": float(np.max(err_ratio))}
     p = torch.zeros_like(pprev)
     for name, fp32, use_net in (("fp64_from_pprev", False, False), ("fp32_refined_from_pprev", True, False),
-                                ("fp32_refined_from_net", True, True)):
+                                ("fp32_refined_from_net", True, True), ("fp32_refined_from_zero", True, None)):
         ps = Poisson(g, bc=0, density=True, fp32=fp32)
         times, its, rrs = [], [], []
         for rho, rhs, pprev, _ in te:
             ps.set_density(rho)
             for timed in (False, True):   # the untimed solve warms up and captures the solve graph
-                p.copy_(pprev)
+                if use_net is None:
+                    p.zero_()
+                else:
+                    p.copy_(pprev)
                 torch.cuda.synchronize()
                 t0 = _t.perf_counter()
                 if use_net:
@@ -953,6 +977,9 @@ def main():
     ap.add_argument("--poisson-n", type=int, default=256, help="grid of --profile-poisson")
     ap.add_argument("--blocks", default="poisson,dirichlet,dambreak,learned,learned3",
                     help="comma-separated extra blocks of the bench line")
+    ap.add_argument("--learned-train", type=int, default=2048,
+                    help="training pairs of the 512^2 learned-guess block (above 2048 they are "
+                         "generated in chunks of 2048 and visited once each)")
     args = ap.parse_args()
     if args.profile_unet:
         import torch

@@ -19,7 +19,7 @@ import numpy as np
 
 from .native import Grid, Poisson, UNet
 
-__all__ = ["rt_problem", "make_snapshots", "cfg4_problem", "make_snapshots_cfg4", "sphere_problem", "make_snapshots3", "train", "solve_iterations"]
+__all__ = ["rt_problem", "make_snapshots", "cfg4_problem", "make_snapshots_cfg4", "sphere_problem", "make_snapshots3", "train", "train_cfg4_stream", "solve_iterations", "guess_errors"]
 
 
 def _grid_of(rho):
@@ -227,6 +227,28 @@ def train(net: UNet, snaps, steps: int, lr: float, torch, seed: int = 0, cosine:
     return losses
 
 
+def train_cfg4_stream(net: UNet, n: int, seeds, chunk: int, lr: float, torch, device, visits: int = 1,
+                      seed: int = 0):
+    """Adam training on cfg4_problem snapshots generated chunk by chunk: each chunk of seeds is
+    solved (make_snapshots_cfg4), every snapshot of it visited `visits` times in a seeded
+    random order, and the chunk dropped, so the number of snapshots is not bounded by device
+    memory.  The learning rate decays from lr to 0 along a half cosine over all steps.
+    Returns the loss history."""
+    seeds = list(seeds)
+    steps = len(seeds) * visits
+    g = Grid(2, (n, n), (0.0, 0.0), (1.0, 1.0))
+    rng = np.random.default_rng(seed)
+    losses = []
+    for c0 in range(0, len(seeds), chunk):
+        snaps = make_snapshots_cfg4(n, seeds[c0:c0 + chunk], torch, device)
+        for i in rng.permutation(np.repeat(np.arange(len(snaps)), visits)):
+            k = len(losses)
+            rho, rhs, pprev, p = snaps[int(i)]
+            losses.append(net.train_step(g, rho, rhs, pprev, p, lr * 0.5 * (1.0 + math.cos(math.pi * k / steps))))
+        del snaps
+    return losses
+
+
 def solve_iterations(snaps, torch, net: UNet | None = None, rel_tol: float = 1e-10, fp32: bool = True):
     """Solver iterations (V-cycles) and final residuals for each snapshot, starting from the
     previous pressure (net None) or from the network's guess."""
@@ -245,3 +267,27 @@ def solve_iterations(snaps, torch, net: UNet | None = None, rel_tol: float = 1e-
         its.append(it)
         res.append(rr)
     return its, res
+
+
+def guess_errors(snaps, torch, net: UNet):
+    """For each snapshot, the interior L2 distance of the network's guess to the converged
+    pressure over that of the previous pressure, both with their means removed (the Neumann
+    problem fixes the pressure up to a constant): below 1 where the network moves the start
+    of the solve towards the answer."""
+    g = _grid_of(snaps[0][0])
+    out = []
+    for rho, rhs, pprev, p in snaps:
+        guess = pprev.clone()
+        torch.cuda.synchronize()
+        net.infer(g, rho, rhs, pprev, guess)
+        torch.cuda.synchronize()
+        if rho.shape[2] == 1:
+            I = (slice(3, -3), slice(3, -3), 0)
+        else:
+            I = (slice(3, -3),) * 3
+        e_net = guess[I] - p[I]
+        e_prev = pprev[I] - p[I]
+        e_net = e_net - e_net.mean()
+        e_prev = e_prev - e_prev.mean()
+        out.append(float(torch.linalg.vector_norm(e_net) / torch.linalg.vector_norm(e_prev)))
+    return out

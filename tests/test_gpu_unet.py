@@ -171,20 +171,28 @@ def test_unet_guess_is_previous_pressure_when_correction_is_zero():
 
 
 def test_learned_guess_trains_and_keeps_the_solve_exact():
-    """Training on solver snapshots lowers the loss, and a solve started from the network's
-    guess still reaches the same tolerance (multigrid stays the judge of the result)."""
+    """The 512^2 workload's problem family at 128^2 with the coarse-correction network
+    (factor 4, a 32 x 32 network image): training on 64 solver snapshots lowers the loss, the
+    trained network moves the start of every held-out solve towards the converged pressure
+    (the distance shrinks to about half; 0.91 at worst over the 8 pairs), and the solve from
+    its guess still reaches 1e-10.  What that gain buys is measured, not asserted: the V-cycle
+    counts are printed on failure only, because a guess error halved saves ~0.3 of a V-cycle
+    that reduces the error ~12x, so the counts from the previous pressure and from the
+    network are equal here (8 and 8 for every pair)."""
     from scihpc_gb300 import UNet
-    from scihpc_gb300.learned import make_snapshots, solve_iterations, train
+    from scihpc_gb300.learned import guess_errors, make_snapshots_cfg4, solve_iterations, train
     dev = torch.device("cuda")
-    tr = make_snapshots(64, range(32), torch, dev)
-    te = make_snapshots(64, range(1000, 1006), torch, dev)
-    net = UNet(64, 64, seed=0)
-    losses = train(net, tr, 300, 1e-3, torch)
+    tr = make_snapshots_cfg4(128, range(64), torch, dev)
+    te = make_snapshots_cfg4(128, range(1000, 1008), torch, dev)
+    net = UNet(128, 128, seed=0, factor=4)
+    losses = train(net, tr, 400, 1e-3, torch, cosine=True)
     assert np.mean(losses[-30:]) < 0.5 * np.mean(losses[:30]), (np.mean(losses[:30]), np.mean(losses[-30:]))
+    ratio = guess_errors(te, torch, net)
     base, _ = solve_iterations(te, torch)
     its, res = solve_iterations(te, torch, net)
+    assert max(ratio) < 1.0 and np.mean(ratio) < 0.75, (ratio, its, base)
     assert max(res) <= 1e-10, res
-    assert max(its) <= max(base) + 2, (its, base)
+    net.close()
 
 
 # ------------------------------------------------------------------ 3D network (27 taps)
@@ -310,7 +318,10 @@ def test_unet3_guess_matches_oracle_and_zero_correction_is_previous_pressure():
 
 def test_learned_guess3_trains_and_keeps_the_solve_exact():
     """3D: training on solver snapshots lowers the loss, and a solve started from the
-    network's guess still reaches the same tolerance."""
+    network's guess still reaches the same tolerance.  No gain is asserted: this network does
+    not move the start towards the answer consistently (distance to the converged pressure
+    0.73-1.12 times the previous pressure's over held-out pairs at 32^3 and 64^3, 0.97 on
+    average at 256^3), and the V-cycle counts stay those from the previous pressure."""
     from scihpc_gb300 import UNet
     from scihpc_gb300.learned import make_snapshots3, solve_iterations, train
     dev = torch.device("cuda")
@@ -320,8 +331,6 @@ def test_learned_guess3_trains_and_keeps_the_solve_exact():
     losses = train(net, tr, 200, 1e-3, torch)
     # a clear decrease (about 0.55x over 200 steps on 12 snapshots)
     assert np.mean(losses[-20:]) < 0.7 * np.mean(losses[:20]), (np.mean(losses[:20]), np.mean(losses[-20:]))
-    base, _ = solve_iterations(te, torch)
     its, res = solve_iterations(te, torch, net)
-    assert max(res) <= 1e-10, res
-    assert max(its) <= max(base) + 2, (its, base)
+    assert max(res) <= 1e-10, (res, its)
     net.close()
