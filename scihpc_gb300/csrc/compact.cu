@@ -449,7 +449,7 @@ static void line_layout(const Dims &D, int a, int &fast, int &slow, long long &l
 
 void launch_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
                  double *f2, double *t1, double *t2, cudaStream_t s) {
-    if (scan_uccd(D, ops, a, flux, vel, f1, f2, s)) return;
+    if (seq_uccd(D, ops, a, flux, vel, f1, f2, s) || scan_uccd(D, ops, a, flux, vel, f1, f2, s)) return;
     int fast, slow;
     long long lines;
     line_layout(D, a, fast, slow, lines);
@@ -459,7 +459,7 @@ void launch_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux
 
 void launch_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux, double *f1, double *f2,
                 cudaStream_t s) {
-    if (scan_ccd(D, ops, a, flux, f1, f2, s)) return;
+    if (seq_ccd(D, ops, a, flux, f1, f2, s) || scan_ccd(D, ops, a, flux, f1, f2, s)) return;
     int fast, slow;
     long long lines;
     line_layout(D, a, fast, slow, lines);
@@ -469,7 +469,7 @@ void launch_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux,
 
 void launch_ccd_mixed(const Dims &D, const CompactOps &ops, int a, double *src, double *out, double *tmp,
                       cudaStream_t s) {
-    if (scan_mixed(D, ops, a, src, out, s)) return;
+    if (seq_mixed(D, ops, a, src, out, s) || scan_mixed(D, ops, a, src, out, s)) return;
     int fast, slow;
     long long lines;
     line_layout(D, a, fast, slow, lines);

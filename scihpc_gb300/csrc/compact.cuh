@@ -44,6 +44,13 @@ void launch_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux,
 void launch_ccd_mixed(const Dims &D, const CompactOps &ops, int a, double *src, double *out, double *tmp,
                       cudaStream_t s);
 
+// Sequential solves staged in shared memory, one thread per line and system (linescan.cu):
+// 3D grids whose lines leave room for four warps per SM; false (nothing launched) otherwise.
+bool seq_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
+              double *f2, cudaStream_t s);
+bool seq_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux, double *f1, double *f2,
+             cudaStream_t s);
+bool seq_mixed(const Dims &D, const CompactOps &ops, int a, double *src, double *out, cudaStream_t s);
 // Warp-cooperative solves (linescan.cu); false when the line is too long for them.
 bool scan_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
                double *f2, cudaStream_t s);

@@ -16,6 +16,7 @@
 // 32 * 16 points with one warp, 128 * 16 with four.
 #include "common.cuh"
 #include "compact.cuh"
+#include "tc.cuh"
 
 namespace scihpc {
 
@@ -351,7 +352,211 @@ bool launch_scan(const Dims &D, const CompactOps &ops, int a, double *io, const 
     return true;
 }
 
+// ------------------------------------------------------------ sequential solves (3D)
+// One thread per line and system, in the order of the factored solve (forward elimination,
+// then back substitution: matrix_solver.cpp:56-83), with the lines staged in shared memory.
+// A scan composes and replays each chunk's maps and combines 32 of them: about 150 FP64
+// operations per point for UCCD's two systems, where the recurrences themselves need 42.
+// Which one is faster depends on the line count: a 3D grid has thousands of lines per axis
+// (one warp per SM sub-partition at 128 x 64 x 64), enough to keep the FP64 pipes busy with
+// one thread per line; a 2D grid has a few hundred, and keeps the scan.
+// Block: LPB consecutive lines x NS systems (thread t: line t % LPB, system t / LPB).  Shared
+// memory: the lines' values F[LPB][pf] (MODE 2: already extrapolated), for UCCD the upwinding
+// velocity W[LPB][pf], then per system and line the forward values, overwritten by the
+// solution, V[NS][LPB][pv] as (value, second) pairs; odd pitches keep a half-warp's 8-byte
+// accesses on distinct banks.  The block copies its lines in with asynchronous copies, all in
+// flight at once, in the order that is contiguous in memory (along the line when it is the
+// fastest axis, across lines otherwise), and stores the results in the same order.
+// op: per point {L (4), U (4), Dinv (4)} of the factored system, read through L1 (every
+// thread of a warp reads the same point).
+constexpr int SEQ_MAX_LPB = 32;
+
+template <int MODE, int NS>
+__global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict__ io, const double *__restrict__ vel,
+                                                              double *__restrict__ f1, double *__restrict__ f2,
+                                                              const double *__restrict__ opA,
+                                                              const double *__restrict__ opB, Dims D, int a, int fast,
+                                                              int slow, int lpb, int pf, int pv) {
+    extern __shared__ __align__(16) double seq_sm[];
+    __shared__ long long bse[SEQ_MAX_LPB];
+    double *F = seq_sm;
+    double *W = F + (size_t)lpb * pf;   // UCCD only
+    double *V = W + (MODE == 1 ? (size_t)lpb * pf : 0);
+    const int n = D.N[a];
+    const long long nf = D.N[fast], lines = nf * D.N[slow];
+    const long long line0 = (long long)blockIdx.x * lpb;
+    const int nl = int(lines - line0 < lpb ? lines - line0 : lpb);   // lines of this block
+    const long long st = D.s[a];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid < nl) {
+        const long long line = line0 + tid;
+        int idx[3];
+        idx[a] = 0;
+        idx[fast] = int(line % nf);
+        idx[slow] = int(line / nf);
+        bse[tid] = D.at(idx[0], idx[1], idx[2]);
+    }
+    __syncthreads();
+    const int total = nl * n;
+    auto src = [&](int i) -> int {
+        if (MODE != 2) return i;
+        return i < GHC ? GHC : (i > n - 1 - GHC ? n - 1 - GHC : i);
+    };
+    auto fetch = [&](int l, int i) {
+        tc::cp8(&F[l * pf + i], &io[bse[l] + (long long)src(i) * st]);
+        if (MODE == 1) tc::cp8(&W[l * pf + i], &vel[bse[l] + (long long)i * st]);
+    };
+    if (st == 1) {
+        for (int e = tid; e < total; e += nt) {
+            const int l = e / n;
+            fetch(l, e - l * n);
+        }
+    } else {
+        for (int e = tid; e < total; e += nt) {
+            const int i = e / nl;
+            fetch(e - i * nl, i);
+        }
+    }
+    tc::cp_commit();
+    tc::cp_wait_all();
+    __syncthreads();
+    const int l = tid % lpb, q = tid / lpb;
+    if (l < nl && q < NS) {
+        const double *f = F + l * pf;
+        double *v = V + ((size_t)q * lpb + l) * pv;
+        const double *op = q == 0 ? opA : opB;
+        const double ih = D.rd[a];
+        const double c3 = -0.06096119008109, c2 = 1.99692238016218, c1 = -1.93596119008109;
+        // forward elimination; one-sided closures at both ends (uccd_solver.cpp:29-51,
+        // ccd_solver.cpp:31-40), interior right-hand sides (uccd_solver.cpp:17-19,:33-41,
+        // ccd_solver.cpp:22-28)
+        double u_p = (-3.5 * f[0] + 4.0 * f[1] - 0.5 * f[2]) * ih;
+        double uu_p = (9.0 * f[0] - 12.0 * f[1] + 3.0 * f[2]) * ih * ih;
+        v[0] = u_p;
+        v[1] = uu_p;
+        double fm = f[0], f0 = f[1];
+#pragma unroll 2
+        for (int i = 1; i < n - 1; ++i) {
+            const double fp = f[i + 1];
+            double ssu = (3.0 * fm - 6.0 * f0 + 3.0 * fp) * ih * ih;
+            double su;
+            if (MODE == 1) su = q == 0 ? (c1 * fm + c2 * f0 + c3 * fp) * ih : -(c3 * fm + c2 * f0 + c1 * fp) * ih;
+            else su = 15.0 / 16.0 * (fp - fm) * ih;
+            fm = f0;
+            f0 = fp;
+            const double *r = op + (size_t)i * 12;
+            su = su - (r[0] * u_p + r[1] * uu_p);
+            ssu = ssu - (r[2] * u_p + r[3] * uu_p);
+            u_p = su, uu_p = ssu;
+            v[2 * i] = su;
+            v[2 * i + 1] = ssu;
+        }
+        {
+            const int i = n - 1;
+            double su = -(-3.5 * f[n - 1] + 4.0 * f[n - 2] - 0.5 * f[n - 3]) * ih;
+            double ssu = (9.0 * f[n - 1] - 12.0 * f[n - 2] + 3.0 * f[n - 3]) * ih * ih;
+            const double *r = op + (size_t)i * 12;
+            su = su - (r[0] * u_p + r[1] * uu_p);
+            ssu = ssu - (r[2] * u_p + r[3] * uu_p);
+            // back substitution starts here
+            double xu = r[8] * su + r[9] * ssu;
+            double yu = r[10] * su + r[11] * ssu;
+            v[2 * i] = xu;
+            v[2 * i + 1] = yu;
+#pragma unroll 2
+            for (int k = n - 2; k >= 0; --k) {
+                const double *rk = op + (size_t)k * 12;
+                double sk = v[2 * k], ssk = v[2 * k + 1];
+                sk = sk - (rk[4] * xu + rk[5] * yu);
+                ssk = ssk - (rk[6] * xu + rk[7] * yu);
+                xu = rk[8] * sk + rk[9] * ssk;
+                yu = rk[10] * sk + rk[11] * ssk;
+                v[2 * k] = xu;
+                v[2 * k + 1] = yu;
+            }
+        }
+    }
+    __syncthreads();
+    auto put = [&](int l2, int i) {
+        const long long o = bse[l2] + (long long)i * st;
+        const double *x0 = V + (size_t)l2 * pv + 2 * i;
+        if (MODE == 1) {
+            const double *x1 = V + ((size_t)lpb + l2) * pv + 2 * i;
+            f1[o] = W[l2 * pf + i] > 0 ? x0[0] : x1[0];
+            f2[o] = 0.5 * (x0[1] + x1[1]);
+        } else if (MODE == 0) {
+            f1[o] = x0[0];
+            f2[o] = x0[1];
+        } else {
+            f1[o] = x0[0];
+            // the reference extrapolates the source in place (ccd_solver.cpp:151-155)
+            if (i < GHC || i > n - 1 - GHC) io[o] = F[l2 * pf + i];
+        }
+    };
+    if (st == 1) {
+        for (int e = tid; e < total; e += nt) {
+            const int l2 = e / n;
+            put(l2, e - l2 * n);
+        }
+    } else {
+        for (int e = tid; e < total; e += nt) {
+            const int i = e / nl;
+            put(e - i * nl, i);
+        }
+    }
+}
+
+// Sequential solves for 3D grids with lines short enough; false (nothing launched) otherwise,
+// and the scans run.
+template <int MODE>
+bool launch_seq(const Dims &D, int a, double *io, const double *vel, double *f1, double *f2, const double *opA,
+                const double *opB, cudaStream_t s) {
+    if (D.ndim != 3 || !opA) return false;
+    constexpr int NS = MODE == 1 ? 2 : 1;
+    const int n = D.N[a];
+    const int pf = n | 1, pv = 2 * n + 1;
+    auto bytes = [&](int lpb) {
+        return size_t(lpb) * ((MODE == 1 ? 2 : 1) * size_t(pf) + size_t(NS) * pv) * sizeof(double);
+    };
+    // One thread per line keeps about a sixth of an SM's FP64 pipe busy per warp (the
+    // recurrence is a dependency chain), so the sequential solve pays only with at least four
+    // warps per SM; longer lines, whose blocks fill an SM's shared memory with fewer threads,
+    // keep the scan (at 128 x 64 x 64: 88 us sequential against 185 us scanned along y and z,
+    // 317 us against 167 us along x).
+    const int lpb = SEQ_MAX_LPB;
+    const size_t smem_sm = 228 * 1024, per_block = bytes(lpb) + 1024;
+    if ((int)(smem_sm / per_block) * NS < 4) return false;
+    static bool attr_set = false;   // one instantiation per MODE
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(seq_kernel<MODE, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess)
+            return false;
+        attr_set = true;
+    }
+    const int b = (a + 1) % 3, c = (a + 2) % 3;
+    const int fast = b > c ? b : c, slow = b > c ? c : b;
+    const long long lines = (long long)D.N[b] * D.N[c];
+    const unsigned blocks = unsigned((lines + lpb - 1) / lpb);
+    seq_kernel<MODE, NS><<<blocks, lpb * NS, bytes(lpb), s>>>(io, vel, f1, f2, opA, opB, D, a, fast, slow, lpb, pf,
+                                                               pv);
+    return true;
+}
+
 }  // namespace
+
+bool seq_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
+              double *f2, cudaStream_t s) {
+    return launch_seq<1>(D, a, const_cast<double *>(flux), vel, f1, f2, ops.up[a], ops.down[a], s);
+}
+
+bool seq_ccd(const Dims &D, const CompactOps &ops, int a, const double *flux, double *f1, double *f2,
+             cudaStream_t s) {
+    return launch_seq<0>(D, a, const_cast<double *>(flux), nullptr, f1, f2, ops.ccd[a], nullptr, s);
+}
+
+bool seq_mixed(const Dims &D, const CompactOps &ops, int a, double *src, double *out, cudaStream_t s) {
+    return launch_seq<2>(D, a, src, nullptr, out, nullptr, ops.ccd[a], nullptr, s);
+}
 
 bool scan_uccd(const Dims &D, const CompactOps &ops, int a, const double *flux, const double *vel, double *f1,
                double *f2, cudaStream_t s) {

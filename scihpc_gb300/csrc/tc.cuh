@@ -120,6 +120,10 @@ __device__ __forceinline__ void cp16(void *smem, const void *gmem, uint32_t src_
 __device__ __forceinline__ void cp4(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
 }
+// 8-byte asynchronous copy global -> shared (both 8-byte aligned)
+__device__ __forceinline__ void cp8(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 

@@ -833,6 +833,8 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
         SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
     }
     SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    SCIHPC_CUDA(cudaStreamCreateWithFlags(&dens_stream, cudaStreamNonBlocking));
+    SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_dens, cudaEventDisableTiming));
     SCIHPC_CUDA(cudaMalloc(&partial, 8 * RED_MAX_BLOCKS * sizeof(double)));
     allocs.push_back(partial);
     SCIHPC_CUDA(cudaMalloc(&sc, sizeof(StepScalars)));
@@ -878,6 +880,11 @@ void TwoPhaseGpu::destroy() {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     ev_fork = nullptr;
+    if (dens_stream) cudaStreamDestroy(dens_stream);
+    if (ev_dens) cudaEventDestroy(ev_dens);
+    dens_stream = nullptr;
+    ev_dens = nullptr;
+    dens_pending = false;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
 }
@@ -1160,6 +1167,12 @@ void TwoPhaseGpu::find_source() {
     // direction each (the last direction on the main stream, in nvel)
     const int nd = D.ndim;
     fork(nd);
+    if (dens_async) {   // nothing below changes the density
+        cudaStreamWaitEvent(dens_stream, ev_fork, 0);
+        ppe.set_density(rho, dens_stream);
+        cudaEventRecord(ev_dens, dens_stream);
+        dens_pending = true;
+    }
     {
         cudaStream_t s = side[0];
         launch_extrapolate(D, 0, phi.data, phi.flux, s);
@@ -1254,7 +1267,12 @@ void TwoPhaseGpu::set_solver_tol(Poisson &ps, int cap) {
 void TwoPhaseGpu::projection_begin() {
     const unsigned nbi = blocks_for(D.interior(), TPB);
     k_div_rhs<<<nbi, TPB, 0, stream>>>(RHS, vel[0].data, vel[1].data, vel[2].data, D, sc);
-    ppe.set_density(rho, stream);
+    if (dens_pending) {
+        cudaStreamWaitEvent(stream, ev_dens, 0);
+        dens_pending = false;
+    } else {
+        ppe.set_density(rho, stream);
+    }
     set_solver_tol(ppe, P.ppe_max_iter);
     ppe.begin(RHS, pres.data, 1, stream);
 }
@@ -1333,7 +1351,9 @@ void TwoPhaseGpu::ab_solve_pre(bool use_fpc) {
     const unsigned nbf = blocks_for(N, TPB);
     k_copy<<<nbf, TPB, 0, stream>>>(pres.old2, pres.old, N);
     k_copy<<<nbf, TPB, 0, stream>>>(pres.old, pres.data, N);
+    dens_async = !use_fpc;
     find_source();
+    dens_async = false;
     ab2_part();
     if (use_fpc) {
         k_pressure_guess<<<nbf, TPB, 0, stream>>>(pres.flux, pres.old, pres.old2, N, sc);

@@ -111,6 +111,13 @@ private:
     void join(int n);
     cudaStream_t side[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
+    // the pressure operator's density setup (Poisson::set_density: coefficients of every level
+    // and the coarsest level's inverse) runs on its own stream from the density's computation
+    // in find_source to the start of the pressure solve, beside the source terms' line solves;
+    // dens_async asks find_source for it, dens_pending says that projection_begin must join it
+    cudaStream_t dens_stream = nullptr;
+    cudaEvent_t ev_dens = nullptr;
+    bool dens_async = false, dens_pending = false;
     // per-direction face-averaged velocities of find_source for the directions other than the
     // last (that one uses nvel, as before), their extrapolation scratch and line-solve scratch
     double *fv[3][3] = {}, *fv_flux[3] = {}, *tb1[3] = {}, *tb2[3] = {};

@@ -46,8 +46,9 @@ def ws(g):
 
 GRIDS = [grid2(), grid2(9, 14, (-1.0, 0.5), (2.0, 3.0)), grid3(), grid3(6, 5, 7)]
 # line lengths for every register tier of the warp-cooperative solver (<= 128, 256, 512
-# points) and one longer line for the sequential fallback
-LONG = [grid2(120, 9), grid2(7, 250), grid2(500, 5), grid2(5, 600), grid3(40, 6, 260)]
+# points) and one longer line for the sequential fallback; in 3D the shared-memory sequential
+# solves run (one to 32 lines per block, blocks with fewer lines than the others)
+LONG = [grid2(120, 9), grid2(7, 250), grid2(500, 5), grid2(5, 600), grid3(40, 6, 260), grid3(70, 33, 37)]
 
 
 @pytest.mark.parametrize("gi", range(len(GRIDS)))
