@@ -103,6 +103,8 @@ __global__ void k_mpls_fields(const double *__restrict__ phi, const double *__re
                               const double *__restrict__ fy, const double *__restrict__ fz, double *__restrict__ w,
                               double *__restrict__ H, double *__restrict__ De, double *__restrict__ G,
                               double *__restrict__ Rho, Dims D, double lw, double dr, int pos) {
+    pdl_wait();
+    pdl_trigger();
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= D.size()) return;
     const double x = phi[q];
@@ -121,6 +123,8 @@ __global__ void k_mpls_fields(const double *__restrict__ phi, const double *__re
 // pass 2: sums of the lsf_mass contributions and of g delta |grad phi| over interior cells
 __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restrict__ H, const double *__restrict__ De,
                             const double *__restrict__ G, Dims D, double dr, int pos, double *__restrict__ partial) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sh[RED_THREADS];
     const long long n = D.interior();
     const long long per_block = (n + gridDim.x - 1) / gridDim.x;
@@ -170,6 +174,8 @@ __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restri
 }
 
 __global__ void k_mpls_finish(const double *__restrict__ partial, int nb, StepScalars *sc, double dv) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sh[1024];
     double v[2];
     for (int m = 0; m < 2; ++m) {
@@ -189,6 +195,8 @@ __global__ void k_mpls_finish(const double *__restrict__ partial, int nb, StepSc
 // s = eta delta |grad phi|, then the Euler update (runge_kutta.cpp:51-63), interior cells
 __global__ void k_mpls_update(double *__restrict__ phi, const double *__restrict__ De, const double *__restrict__ G,
                               Dims D, const StepScalars *sc, GhostFill GF) {
+    pdl_wait();
+    pdl_trigger();
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= D.interior()) return;
     int I, J, K;
@@ -210,6 +218,8 @@ __global__ void k_sign(const double *__restrict__ phi, double *__restrict__ sg, 
 __global__ void k_reinit_a(const double *__restrict__ phi, const double *__restrict__ sg,
                            const double *__restrict__ De, double *__restrict__ G, double *__restrict__ s,
                            double *__restrict__ A, double *__restrict__ B, Dims D, double rdt, const StepScalars *sc) {
+    pdl_wait();
+    pdl_trigger();
     long long o;
     if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
     const double g = godunov_at(phi, o, sg[o], D);
@@ -241,6 +251,8 @@ __global__ void __launch_bounds__(RA_NT)
     k_reinit_a2d(const double *__restrict__ phi, const double *__restrict__ sg, const double *__restrict__ De,
                  double *__restrict__ G, double *__restrict__ s, double *__restrict__ A, double *__restrict__ B, Dims D,
                  double rdt, const StepScalars *sc) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int PI = RA_TI + 6, PJ = RA_TJ + 6;   // phi with three ghost layers
     constexpr int DI = RA_TI + 4, DJ = RA_TJ + 4;   // second differences at -2 .. T+1
     constexpr int QI = RA_TI + 3, QJ = RA_TJ + 3;   // pairs at -2 .. T
@@ -345,6 +357,8 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
                            double *__restrict__ sk, const double *__restrict__ s1, const double *__restrict__ s2,
                            const double *__restrict__ A, const double *__restrict__ B, Dims D, double rdt,
                            int lambda, int stage, const StepScalars *sc, GhostFill GF) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double fsrc;   // rdt / dt, one division per block
     if (threadIdx.x == 0) fsrc = rdt / sc->dt;
     __syncthreads();
@@ -1104,11 +1118,13 @@ void TwoPhaseGpu::mpls(int count) {
         for (int a = 0; a < D.ndim; ++a)
             launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], a == D.ndim - 1 ? stream : side[a]);
         join(D.ndim - 1);
-        k_mpls_fields<<<nbf, TPB, 0, stream>>>(phi.data, phi.d1[0], phi.d1[1], phi.d1[2], work, H, delta, grad, rho, D,
-                                               P.ls_width, P.density_ratio, P.positive_ref);
-        k_mpls_sums<<<nb, RED_THREADS, 0, stream>>>(work, H, delta, grad, D, P.density_ratio, P.positive_ref, partial);
-        k_mpls_finish<<<1, 1024, 0, stream>>>(partial, nb, sc, D.dv);
-        k_mpls_update<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, D, sc, phi_fill);
+        const bool pdl = pdl_step();
+        launch_pdl(pdl, k_mpls_fields, nbf, TPB, 0, stream, phi.data, phi.d1[0], phi.d1[1], phi.d1[2], work, H, delta,
+                   grad, rho, D, P.ls_width, P.density_ratio, P.positive_ref);
+        launch_pdl(pdl, k_mpls_sums, nb, RED_THREADS, 0, stream, work, H, delta, grad, D, P.density_ratio,
+                   P.positive_ref, partial);
+        launch_pdl(pdl, k_mpls_finish, 1, 1024, 0, stream, partial, nb, sc, D.dv);
+        launch_pdl(pdl, k_mpls_update, nbi, TPB, 0, stream, phi.data, delta, grad, D, sc, phi_fill);
         if (!phi_fill.on) scalar_bc(phi.data);
     }
 }
@@ -1116,13 +1132,16 @@ void TwoPhaseGpu::mpls(int count) {
 void TwoPhaseGpu::reinit_stage(int stage) {
     const unsigned nbi = blocks_for(D.interior(), TPB);
     double *S[3] = {s1, s2, s3};
+    const bool pdl = pdl_step();
     if (D.ndim == 2)
-        k_reinit_a2d<<<dim3(unsigned((D.n[1] + RA_TJ - 1) / RA_TJ), unsigned((D.n[0] + RA_TI - 1) / RA_TI)), RA_NT, 0,
-                       stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
+        launch_pdl(pdl, k_reinit_a2d,
+                   dim3(unsigned((D.n[1] + RA_TJ - 1) / RA_TJ), unsigned((D.n[0] + RA_TI - 1) / RA_TI)), RA_NT, 0,
+                   stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
     else
-        k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
-    k_reinit_b<<<nbi, TPB, 0, stream>>>(phi.data, delta, grad, S[stage - 1], s1, s2, a_f, b_f, D, P.rdt, reinit_lambda,
-                                        stage, sc, phi_fill);
+        launch_pdl(pdl, k_reinit_a, nbi, TPB, 0, stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt,
+                   sc);
+    launch_pdl(pdl, k_reinit_b, nbi, TPB, 0, stream, phi.data, delta, grad, S[stage - 1], s1, s2, a_f, b_f, D, P.rdt,
+               reinit_lambda, stage, sc, phi_fill);
     if (!phi_fill.on) scalar_bc(phi.data);
 }
 
