@@ -298,7 +298,18 @@ __global__ void __launch_bounds__(THREADS) k_conv_halo(const __nv_bfloat16 *__re
 
 // ------------------------------------------------------------------ weight gradient
 // partial[split][r][co] = sum over the split's pixels of X[p + off(t_r)][ci_r] * dZ[p][co],
-// r = t * Ci + ci over the rows of this block's M tile
+// r = t * Ci + ci over the rows of this block's M tile.
+// K runs over pixels, and both operands are stored channels-fastest, so both are MN-major
+// tiles for the MMA (transpose bits of the instruction descriptor): every 16-byte chunk of a
+// tile is 8 consecutive channels of one pixel, copied straight from X (shifted by the row's
+// tap, zero outside the grid) or dZ with cp.async -- no gather, no transpose.  MN-major
+// layout without swizzle: a core matrix is 8 K-rows of 16 bytes (8 MN elements); the two core
+// matrices along K of one 8-element MN group sit side by side, the MN groups 256 B apart.  As
+// for the K-major tiles, the descriptor's leading byte offset is the K step between core
+// matrices (128 B) and the stride byte offset the MN step (256 B) (checked against the CPU
+// restatement by the weight-gradient tests).
+__device__ __forceinline__ uint32_t mn_off(int m0, int k) { return uint32_t((m0 >> 3) * 256 + (k >> 3) * 128 + (k & 7) * 16); }
+
 __global__ void __launch_bounds__(THREADS) k_conv_wgrad(const __nv_bfloat16 *__restrict__ X,
                                                         const __nv_bfloat16 *__restrict__ dZ,
                                                         float *__restrict__ partial, int D, int H, int W, int Ci,
@@ -312,10 +323,18 @@ __global__ void __launch_bounds__(THREADS) k_conv_wgrad(const __nv_bfloat16 *__r
     const bool three = D > 1;
     const int taps = three ? 27 : 9;
     const int rows = taps * Ci;
-    const int r = blockIdx.x * TILE_M + tid;   // this thread's (tap, ci) row of A
-    const int tap = r < rows ? r / Ci : 0, ci = r < rows ? r % Ci : 0;
-    int dz, dy, dx;
-    tap_shift(tap, three, dz, dy, dx);
+    // this thread's two A chunks: pixel k_a of the K-step, MN groups g_a and g_a + 1 (8 rows each)
+    const int k_a = tid >> 3, g_a = (tid & 7) * 2;
+    int dzs[2], dys[2], dxs[2], ci0[2];
+    bool rv[2];
+    for (int u = 0; u < 2; ++u) {
+        const int r0 = blockIdx.x * TILE_M + (g_a + u) * 8;
+        rv[u] = r0 < rows;
+        const int tap = rv[u] ? r0 / Ci : 0;
+        ci0[u] = rv[u] ? r0 - tap * Ci : 0;
+        tap_shift(tap, three, dzs[u], dys[u], dxs[u]);
+    }
+    const int ng8 = N >> 3;   // B chunks per K-row
     const long long k0 = (long long)blockIdx.y * pix_per_split;
     const long long k1 = k0 + pix_per_split < P ? k0 + pix_per_split : P;
     const int nk = k1 > k0 ? int((k1 - k0 + 15) / 16) : 0;
@@ -330,7 +349,7 @@ __global__ void __launch_bounds__(THREADS) k_conv_wgrad(const __nv_bfloat16 *__r
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = tmem_base;
-    const uint32_t idesc = tc::idesc_bf16(TILE_M, N);
+    const uint32_t idesc = tc::idesc_bf16(TILE_M, N) | (1u << 15) | (1u << 16);   // A and B MN-major
     bool ok = true;
     for (int g = 0; g < ng; ++g) {
         const int s = g & 1;
@@ -344,37 +363,33 @@ __global__ void __launch_bounds__(THREADS) k_conv_wgrad(const __nv_bfloat16 *__r
         for (int j = 0; j < kn; ++j) {
             const long long kp = k0 + 16LL * (g * sk + j);
             unsigned char *a = base + j * per, *bt = a + TILE_M * 32;
-            {   // A row: X[p + off][ci] for 16 pixels, transposed into K order
-                __align__(16) __nv_bfloat16 v[16];
-                int z = int(kp / HW);
-                const long long rem = kp - (long long)z * HW;
-                int y = int(rem / W), x = int(rem - (long long)y * W);
-#pragma unroll
-                for (int kk = 0; kk < 16; ++kk) {
-                    __nv_bfloat16 xv = __float2bfloat16(0.0f);
-                    const int zs = z + dz, ys = y + dy, xs = x + dx;
-                    if (r < rows && kp + kk < k1 && zs >= 0 && zs < D && ys >= 0 && ys < H && xs >= 0 && xs < W)
-                        xv = X[(((long long)zs * H + ys) * W + xs) * Ci + ci];
-                    v[kk] = xv;
-                    if (++x == W) {
-                        x = 0;
-                        if (++y == H) y = 0, ++z;
-                    }
+            {   // A: X at the row's shifted pixel, 8 channels per chunk
+                const long long p = kp + k_a;
+                int z = 0, y = 0, x = 0;
+                const bool pin = p < k1;
+                if (pin) {
+                    z = int(p / HW);
+                    const long long rem = p - (long long)z * HW;
+                    y = int(rem / W);
+                    x = int(rem - (long long)y * W);
                 }
-                *reinterpret_cast<uint4 *>(a + chunk_off(tid, 0)) = reinterpret_cast<uint4 *>(v)[0];
-                *reinterpret_cast<uint4 *>(a + chunk_off(tid, 1)) = reinterpret_cast<uint4 *>(v)[1];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int zs = z + dzs[u], ys = y + dys[u], xs = x + dxs[u];
+                    const bool in = pin && rv[u] && zs >= 0 && zs < D && ys >= 0 && ys < H && xs >= 0 && xs < W;
+                    const __nv_bfloat16 *src = in ? X + (((long long)zs * H + ys) * W + xs) * Ci + ci0[u] : X;
+                    tc::cp16(a + mn_off((g_a + u) * 8, k_a), src, in ? 16u : 0u);
+                }
             }
-            for (int n = tid; n < N; n += THREADS) {   // B row: dZ[p][n] for 16 pixels
-                __align__(16) __nv_bfloat16 v[16];
-#pragma unroll
-                for (int kk = 0; kk < 16; ++kk) {
-                    const long long pp = kp + kk;
-                    v[kk] = pp < k1 ? dZ[pp * N + n] : __float2bfloat16(0.0f);
-                }
-                *reinterpret_cast<uint4 *>(bt + chunk_off(n, 0)) = reinterpret_cast<uint4 *>(v)[0];
-                *reinterpret_cast<uint4 *>(bt + chunk_off(n, 1)) = reinterpret_cast<uint4 *>(v)[1];
+            for (int c = tid; c < 16 * ng8; c += THREADS) {   // B: dZ, 8 output channels per chunk
+                const int k = c / ng8, n0 = (c - k * ng8) * 8;
+                const long long p = kp + k;
+                const bool in = p < k1;
+                tc::cp16(bt + mn_off(n0, k), in ? dZ + p * N + n0 : dZ, in ? 16u : 0u);
             }
         }
+        tc::cp_commit();
+        tc::cp_wait_all();
         tc::fence_async_smem();
         tc::fence_before();
         __syncthreads();

@@ -26,6 +26,7 @@ namespace {
 
 constexpr int C_IN = 16;   // packed input channels (3 used)
 constexpr int TPB = 256;
+constexpr int RED_NB = 256;   // blocks of the two-pass (block sums, then in block order) reductions
 
 struct LayerDef {
     int in, out, ci, co, relu, level;
@@ -118,13 +119,14 @@ __global__ void k_bias_grad(const __nv_bfloat16 *__restrict__ dz, float *__restr
     if (threadIdx.x == 0) db[c] = float(s);
 }
 
-// per-sample statistics over the interior: mean rho, std rho, rms rhs, rms pprev
-__global__ void k_stats(const double *__restrict__ rho, const double *__restrict__ rhs,
-                        const double *__restrict__ pprev, Dims D, double *__restrict__ st) {
-    __shared__ double sh[1024];
+// per-sample statistics over the interior: mean rho, std rho, rms rhs, rms pprev; block sums
+// (pixels strided over the grid), then the sums in block order
+__global__ void k_stats_part(const double *__restrict__ rho, const double *__restrict__ rhs,
+                             const double *__restrict__ pprev, Dims D, double *__restrict__ part) {
+    __shared__ double sh[TPB];
     const long long n = (long long)D.n[0] * D.n[1];
     double a[4] = {0, 0, 0, 0};
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+    for (long long q = (long long)blockIdx.x * TPB + threadIdx.x; q < n; q += (long long)RED_NB * TPB) {
         const int i = int(q / D.n[1]), j = int(q % D.n[1]);
         const long long g = D.at(i + GHC, j + GHC, 0);
         a[0] += rho[g];
@@ -132,15 +134,23 @@ __global__ void k_stats(const double *__restrict__ rho, const double *__restrict
         a[2] += rhs[g] * rhs[g];
         a[3] += pprev ? pprev[g] * pprev[g] : 0.0;
     }
-    double r[4];
-    for (int m = 0; m < 4; ++m) r[m] = block_reduce<SumOp>(a[m], sh);
-    if (threadIdx.x == 0) {
-        const double mean = r[0] / n;
-        st[0] = mean;
-        st[1] = sqrt(fmax(r[1] / n - mean * mean, 0.0)) + 1e-12;
-        st[2] = sqrt(r[2] / n) + 1e-300;
-        st[3] = sqrt(r[3] / n);
+    for (int m = 0; m < 4; ++m) {
+        const double r = block_reduce<SumOp>(a[m], sh);
+        if (threadIdx.x == 0) part[m * RED_NB + blockIdx.x] = r;
+        __syncthreads();
     }
+}
+
+__global__ void k_stats_fin(const double *__restrict__ part, long long n, double *__restrict__ st) {
+    if (threadIdx.x != 0) return;
+    double r[4] = {0, 0, 0, 0};
+    for (int m = 0; m < 4; ++m)
+        for (int b = 0; b < RED_NB; ++b) r[m] += part[m * RED_NB + b];
+    const double mean = r[0] / n;
+    st[0] = mean;
+    st[1] = sqrt(fmax(r[1] / n - mean * mean, 0.0)) + 1e-12;
+    st[2] = sqrt(r[2] / n) + 1e-300;
+    st[3] = sqrt(r[3] / n);
 }
 
 // x0[p] = (rho', rhs', pprev', 0 ...) for pixel p = i * ny + j; target t[p] if p_new given
@@ -175,19 +185,26 @@ __global__ void k_unpack(const float *__restrict__ out, const double *__restrict
     guess[q] += sp * double(out[((long long)i * D.n[1] + j) * 16]);
 }
 
-// loss = mean (out[p][0] - t[p])^2; gout[p][c] = d loss / d out[p][c]
-__global__ void k_loss(const float *__restrict__ out, const float *__restrict__ t, float *__restrict__ gout, long long P,
-                       double *__restrict__ loss) {
-    __shared__ double sh[1024];
+// loss = mean (out[p][0] - t[p])^2; gout[p][c] = d loss / d out[p][c]; block sums, then in order
+__global__ void k_loss_part(const float *__restrict__ out, const float *__restrict__ t, float *__restrict__ gout,
+                            long long P, double *__restrict__ part) {
+    __shared__ double sh[TPB];
     double a = 0.0;
-    for (long long p = threadIdx.x; p < P; p += blockDim.x) {
+    for (long long p = (long long)blockIdx.x * TPB + threadIdx.x; p < P; p += (long long)RED_NB * TPB) {
         const float d = out[p * 16] - t[p];
         a += double(d) * d;
         gout[p * 16] = 2.0f * d / float(P);
         for (int c = 1; c < 16; ++c) gout[p * 16 + c] = 0.0f;
     }
     a = block_reduce<SumOp>(a, sh);
-    if (threadIdx.x == 0) *loss = a / double(P);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+__global__ void k_loss_fin(const double *__restrict__ part, long long P, double *__restrict__ loss) {
+    if (threadIdx.x != 0) return;
+    double s = 0.0;
+    for (int b = 0; b < RED_NB; ++b) s += part[b];
+    *loss = s / double(P);
 }
 
 // ------------------------------------------------------------------ coarse-correction mode
@@ -236,24 +253,32 @@ __global__ void k_coarse_inputs(const double *__restrict__ rho, const double *__
 }
 
 // st = {mean rho, std rho, mean r, rms(r - mean r), rms pprev, s_e} over the coarse pixels
-__global__ void k_stats_coarse(const float *__restrict__ cin, long long P, double *__restrict__ st) {
-    __shared__ double sh[1024];
+__global__ void k_stats_coarse_part(const float *__restrict__ cin, long long P, double *__restrict__ part) {
+    __shared__ double sh[TPB];
     double a[5] = {0, 0, 0, 0, 0};
-    for (long long p = threadIdx.x; p < P; p += blockDim.x) {
+    for (long long p = (long long)blockIdx.x * TPB + threadIdx.x; p < P; p += (long long)RED_NB * TPB) {
         const double r0 = cin[p * 3], r1 = cin[p * 3 + 1], r2 = cin[p * 3 + 2];
         a[0] += r0, a[1] += r0 * r0, a[2] += r1, a[3] += r1 * r1, a[4] += r2 * r2;
     }
-    double t[5];
-    for (int m = 0; m < 5; ++m) t[m] = block_reduce<SumOp>(a[m], sh);
-    if (threadIdx.x == 0) {
-        const double mr = t[0] / P, m1 = t[2] / P;
-        st[0] = mr;
-        st[1] = sqrt(fmax(t[1] / P - mr * mr, 0.0)) + 1e-12;
-        st[2] = m1;
-        st[3] = sqrt(fmax(t[3] / P - m1 * m1, 0.0)) + 1e-300;
-        st[4] = sqrt(t[4] / P);
-        st[5] = COARSE_OUT_SCALE * st[3];
+    for (int m = 0; m < 5; ++m) {
+        const double r = block_reduce<SumOp>(a[m], sh);
+        if (threadIdx.x == 0) part[m * RED_NB + blockIdx.x] = r;
+        __syncthreads();
     }
+}
+
+__global__ void k_stats_coarse_fin(const double *__restrict__ part, long long P, double *__restrict__ st) {
+    if (threadIdx.x != 0) return;
+    double t[5] = {0, 0, 0, 0, 0};
+    for (int m = 0; m < 5; ++m)
+        for (int b = 0; b < RED_NB; ++b) t[m] += part[m * RED_NB + b];
+    const double mr = t[0] / P, m1 = t[2] / P;
+    st[0] = mr;
+    st[1] = sqrt(fmax(t[1] / P - mr * mr, 0.0)) + 1e-12;
+    st[2] = m1;
+    st[3] = sqrt(fmax(t[3] / P - m1 * m1, 0.0)) + 1e-300;
+    st[4] = sqrt(t[4] / P);
+    st[5] = COARSE_OUT_SCALE * st[3];
 }
 
 // x0 from the coarse inputs; target: the mean of (pnew - pprev) over each coarse pixel / s_e
@@ -384,6 +409,7 @@ int UNet::create(int h, int w, unsigned seed, int factor) {
     if ((rc = alloc_skip())) return rc;
     if ((rc = dalloc((void **)&dz, maxact * 2)) || (rc = dalloc((void **)&partial, maxpart * 4)) ||
         (rc = dalloc((void **)&target, (long long)H[0] * W[0] * 4)) || (rc = dalloc((void **)&stats, 8 * 8)) ||
+        (rc = dalloc((void **)&dred, 5 * RED_NB * sizeof(double))) ||
         (rc = dalloc((void **)&err, 16)) || (rc = dalloc((void **)&cin, (long long)H[0] * W[0] * 3 * 4)))
         return rc;
     // He-normal weights, zero biases; the last layer starts near zero (guess = previous pressure)
@@ -538,12 +564,14 @@ int UNet::prepare(const Dims &D, const double *rho, const double *rhs, const dou
     if (fac > 1) {
         const long long P = (long long)H[0] * W[0];
         k_coarse_inputs<<<nblk(P), TPB, 0, stream>>>(rho, rhs, pprev, D, fac, H[0], W[0], cin);
-        k_stats_coarse<<<1, 1024, 0, stream>>>(cin, P, stats);
+        k_stats_coarse_part<<<RED_NB, TPB, 0, stream>>>(cin, P, dred);
+        k_stats_coarse_fin<<<1, 32, 0, stream>>>(dred, P, stats);
         k_pack_coarse<<<nblk(P), TPB, 0, stream>>>(cin, stats, pprev, pnew, D, fac, H[0], W[0],
                                                    (__nv_bfloat16 *)act[X0], pnew ? target : nullptr);
         return SCIHPC_OK;
     }
-    k_stats<<<1, 1024, 0, stream>>>(rho, rhs, pprev, D, stats);
+    k_stats_part<<<RED_NB, TPB, 0, stream>>>(rho, rhs, pprev, D, dred);
+    k_stats_fin<<<1, 32, 0, stream>>>(dred, (long long)D.n[0] * D.n[1], stats);
     const long long P = (long long)H[0] * W[0];
     k_pack<<<nblk(P), TPB, 0, stream>>>(rho, rhs, pprev, pnew, D, stats, (__nv_bfloat16 *)act[X0],
                                        pnew ? target : nullptr);
@@ -578,7 +606,8 @@ int UNet::loss_grad(const Dims &D, const double *rho, const double *rhs, const d
     int rc = prepare(D, rho, rhs, pprev, pnew);
     if (rc || (rc = forward())) return rc;
     const long long P = (long long)H[0] * W[0];
-    k_loss<<<1, 1024, 0, stream>>>((const float *)act[OUT], target, gact[OUT], P, stats + 4);
+    k_loss_part<<<RED_NB, TPB, 0, stream>>>((const float *)act[OUT], target, gact[OUT], P, dred);
+    k_loss_fin<<<1, 32, 0, stream>>>(dred, P, stats + 4);
     if ((rc = backward())) return rc;
     SCIHPC_CUDA(cudaMemcpyAsync(loss, stats + 4, sizeof(double), cudaMemcpyDeviceToHost, stream));
     return check_err();

@@ -52,7 +52,7 @@ private:
     float *gact[NT] = {};
     float *gskip[3] = {nullptr, nullptr, nullptr};
     float *partial = nullptr, *target = nullptr;
-    double *stats = nullptr;
+    double *stats = nullptr, *dred = nullptr;   // dred: partial sums of the two-pass reductions
     int *err = nullptr;
     long long adam_t = 0;
     std::vector<void *> allocs;
