@@ -44,7 +44,7 @@ REINIT_FLOPS_2D = 262
 # not captured); the command that made each is in the summary file.
 REINIT_TRAFFIC_BYTES = 841387   # read 841,387 B, write 0 B (mean of three launches)
 REINIT_TRAFFIC_SRC = "profiles/reinit_2d_128x256_traffic.md"
-REINIT_SHARE = 0.244   # profiles/twophase_step_128x256_launches.md
+REINIT_SHARE = 0.252   # profiles/twophase_step_128x256_launches.md
 VCYCLE_256_TRAFFIC_BYTES = 1436369067   # read 1.088 GB + write 0.348 GB, mean of three V-cycles
 VCYCLE_256_TRAFFIC_SRC = "profiles/poisson_256cubed_vcycle_traffic.md"
 
@@ -876,11 +876,7 @@ def learned3_block(torch, n: int = 256, ntrain: int = 16, ntest: int = 3, steps:
     loss_before = test_loss()
     torch.cuda.synchronize()
     t0 = _t.perf_counter()
-    if stream:   # snapshot generation included in the training time
-        losses = train_cfg4_stream(net, n, range(ntrain), chunk, 1e-3, torch, dev)
-        steps = len(losses)
-    else:
-        losses = train(net, tr, steps, 1e-3, torch, cosine=True)
+    losses = train(net, tr, steps, 1e-3, torch, cosine=True)
     torch.cuda.synchronize()
     t_train = _t.perf_counter() - t0
     loss_after = test_loss()
