@@ -492,6 +492,71 @@ def poisson_block(torch, Poisson, Grid, hbm):
     return out
 
 
+def stock_block(torch, args, flush, clocks_cls) -> dict:
+    """The same bubble step under the reference's own pressure schedule, the one the reference
+    arm runs (projection_method.cpp:755-777: the projection equation while iter < 5, then
+    pressure_guess_solution + init_ppe_fpc_coefficients + fast_pressure_correction on the
+    constant-coefficient multigrid, ppe_tol 1e-8 absolute, at most 100 cycles, ppe_initer 1),
+    which is the C++ drop-in's default.  Timed like the headline (graph replay, L2 flushed
+    before each step, CUDA events), after the five projection steps and the warm-up, over at
+    most 50 steps and e2e over the next 50 through the C ABI with the same four fields up and
+    down: windows inside the first ~110 steps, where the reference arm's windows (steps 6-155)
+    are."""
+    from scihpc_gb300 import Grid, TwoPhase
+    g = Grid(2, (NX, NY), DOMAIN[0], DOMAIN[1])
+    h = min(g.spacing())
+    prm = physics(h)
+    prm.update(ppe_tol=1e-8, ppe_max_iter=100, ppe_initer=1)
+    tp = TwoPhase(g, ["no_slip"] * 6, ["neumann"] * 6, prm, scheme=1, n_mpls=5, reinit_every=1,
+                  fp32=args.ppe == "fp32")
+    tp.set_ppe_schedule(1, 1)
+    tp.set("phi", initial_phi(g.shape))
+    tp.init()
+    stream = torch.cuda.ExternalStream(tp.stream())
+    tp.step(5 + args.warmup, graph=True, sync=True)
+    it0 = tp.graph_stats()["ppe_iters_total"]
+    torch.cuda.synchronize()
+    nt = max(1, min(args.steps, 50))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nt)]
+    clocks = clocks_cls(torch.cuda.current_device())
+    with clocks:
+        for k in range(nt):
+            flush.fill_(float(k))
+            torch.cuda.current_stream().synchronize()
+            ev[k][0].record(stream)
+            tp.step(1, graph=True, sync=False)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    iters = tp.graph_stats()["ppe_iters_total"] - it0
+    names = ["phi", "u", "v", "p"]
+    hb = {nm: torch.empty(g.shape, dtype=torch.float64).pin_memory() for nm in names}
+    for nm in names:
+        tp.download_ptr(nm, hb[nm].data_ptr())
+    n_e2e = nt
+    torch.cuda.synchronize()
+    it1 = tp.graph_stats()["ppe_iters_total"]
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        for nm in names:
+            tp.upload_ptr(nm, hb[nm].data_ptr())
+        tp.step(1, graph=True, sync=True)
+        for nm in names:
+            tp.download_ptr(nm, hb[nm].data_ptr())
+    e2e = n_e2e / (time.perf_counter() - t0)
+    it_e2e = (tp.graph_stats()["ppe_iters_total"] - it1) / n_e2e
+    diag = tp.diagnostics()
+    tp.close()
+    return {"schedule": "reference: projection while iter < 5, then fast pressure correction (constant-coefficient "
+                        "multigrid, ppe_tol 1e-8 absolute, at most 100 cycles)",
+            "steps_timed": nt, "steps_per_s": nt / (ms / 1e3), "ms_per_step": ms / nt,
+            "e2e_steps_per_s": e2e, "fpc_cycles_per_step": iters / nt,
+            "e2e_fpc_cycles_per_step": it_e2e, "clocks": clocks.summary(),
+            "diagnostics": diag,
+            "note": "same schedule and tolerances as the reference arm (--impl reference); the headline solves the "
+                    "variable-density projection equation to a relative residual of 1e-10 every step"}
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -601,6 +666,8 @@ def run_ours(args) -> None:
             "ppe_iters_per_step": ppe_iters / args.steps, "wall_s": t_wall, "roofline": roof,
             "diagnostics": diag}
     blocks = set(args.blocks.split(","))
+    if rank == 0 and "stock" in blocks:
+        line["stock_schedule"] = stock_block(torch, args, flush, Clocks)
     if rank == 0 and not args.no_poisson and "poisson" in blocks:
         line["poisson_256^3"] = poisson_block(torch, Poisson, Grid, hbm)
         v = line["poisson_256^3"]["fp32_refined"]
@@ -971,7 +1038,7 @@ def main():
     ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
                     help="only three iterations of the n^3 pressure solve (profiling case)")
     ap.add_argument("--poisson-n", type=int, default=256, help="grid of --profile-poisson")
-    ap.add_argument("--blocks", default="poisson,dirichlet,dambreak,learned,learned3",
+    ap.add_argument("--blocks", default="stock,poisson,dirichlet,dambreak,learned,learned3",
                     help="comma-separated extra blocks of the bench line")
     ap.add_argument("--learned-train", type=int, default=2048,
                     help="training pairs of the 512^2 learned-guess block (above 2048 they are "
