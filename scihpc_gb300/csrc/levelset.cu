@@ -35,20 +35,21 @@ __device__ __forceinline__ double weno_face(double a, double b, double c, double
         q2 = (-a + 5.0 * b + 2.0 * c) * sixth;
     }
     // WENO-Z weights a_k = d_k (1 + tau / g_k), g_k = eps + beta_k, multiplied through by
-    // g0 g1 g2 so that one division remains
+    // g0 g1 g2 so that one reciprocal remains (the refined hardware reciprocal: within ~1 ulp
+    // of the reference's division)
     const double tau = fabs(b0 - b2);
     const double g0 = WENO_EPS + b0, g1 = WENO_EPS + b1, g2 = WENO_EPS + b2;
     const double a0 = (g0 + tau) * g1 * g2;
     const double a1 = 6.0 * (g1 + tau) * g0 * g2;
     const double a2 = 3.0 * (g2 + tau) * g0 * g1;
-    return (a0 * q0 + a1 * q1 + a2 * q2) / (a0 + a1 + a2);
+    return (a0 * q0 + a1 * q1 + a2 * q2) * rcp_refined(a0 + a1 + a2);
 }
 
-// Upwinded face value between cells i and i+1 (weno_solver.cpp:185-199).
+// Upwinded face value between cells i and i+1 (weno_solver.cpp:185-199): only the
+// reconstruction the face velocity selects is formed.
 __device__ __forceinline__ double weno_upwind_face(const double *f, long long o, long long st, const double *vel) {
-    const double fm = weno_face(f[o - 2 * st], f[o - st], f[o], f[o + st], f[o + 2 * st], true);
-    const double fp = weno_face(f[o - st], f[o], f[o + st], f[o + 2 * st], f[o + 3 * st], false);
-    return vel[o] + vel[o + st] > 0.0 ? fm : fp;
+    if (vel[o] + vel[o + st] > 0.0) return weno_face(f[o - 2 * st], f[o - st], f[o], f[o + st], f[o + 2 * st], true);
+    return weno_face(f[o - st], f[o], f[o + st], f[o + 2 * st], f[o + 3 * st], false);
 }
 
 __global__ void weno_kernel(const double *__restrict__ f, const double *__restrict__ vel, double *__restrict__ out,

@@ -8,6 +8,32 @@ namespace scihpc {
 
 constexpr double WENO_EPS = 1e-8;   // global.h:14
 
+// GB300 runs FP64 at about two operations per SM per clock, and FP64 comparisons and min/max
+// take that pipe too; these do the same on the integer pipe, from the IEEE bit patterns.
+// max(x, +0) (a negative x, or -0, gives +0)
+__device__ __forceinline__ double pos_part(double x) {
+    const long long b = __double_as_longlong(x);
+    return __longlong_as_double(b & ~(b >> 63));
+}
+__device__ __forceinline__ double flip_sign(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+// max(a, b) of two non-negative doubles: their bit patterns order as integers
+__device__ __forceinline__ double nonneg_max(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x > y ? x : y);
+}
+// x > 0 for a non-NaN x
+__device__ __forceinline__ bool sign_bits_positive(double x) { return __double_as_longlong(x) > 0; }
+// 1 / x for a normal, finite x: the hardware's approximate reciprocal and one Newton-Raphson
+// step y (2 - x y) (the error squares: the weights' normalisation needs far less than FP64's
+// last bits; the reference's correctly rounded division and this differ by ~1 ulp)
+__device__ __forceinline__ double rcp_refined(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return fma(y, fma(-x, y, 1.0), y);
+}
+
 __device__ __forceinline__ double heaviside_d(double x, double w) {
     if (x < -w) return 0.0;
     if (x > w) return 1.0;
@@ -31,10 +57,10 @@ __device__ __forceinline__ double weno_godunov(double a, double b, double c, dou
     const double is2 = 13.0 * (c - d) * (c - d) + 3.0 * (3.0 * c - d) * (3.0 * c - d);
     const double e0 = WENO_EPS + is0, e1 = WENO_EPS + is1, e2 = WENO_EPS + is2;
     // weights alpha_k = d_k / e_k^2 normalised; multiplied through by (e0 e1 e2)^2 so that a
-    // single division remains (FP64 division is the costly operation on this GPU)
+    // single reciprocal remains (FP64 division is the costly operation on this GPU)
     const double q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
     const double p12 = q1 * q2, p02 = q0 * q2, p01 = q0 * q1;
-    const double inv = 1.0 / (p12 + 6.0 * p02 + 3.0 * p01);
+    const double inv = rcp_refined(p12 + 6.0 * p02 + 3.0 * p01);
     const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
     return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
 }
@@ -52,9 +78,8 @@ __device__ __forceinline__ double godunov_at(const double *__restrict__ phi, lon
                                                 c0 - 2.0 * m1 + m2);
         const double dm = v - ih * weno_godunov(m3 - 2.0 * m2 + m1, m2 - 2.0 * m1 + c0, m1 - 2.0 * c0 + p1,
                                                 c0 - 2.0 * p1 + p2);
-        double g;
-        if (sgn > 0.0) g = fmax(-fmin(dp, 0.0), fmax(dm, 0.0));
-        else g = fmax(fmax(dp, 0.0), -fmin(dm, 0.0));
+        const double g = sign_bits_positive(sgn) ? nonneg_max(pos_part(flip_sign(dp)), pos_part(dm))
+                                                 : nonneg_max(pos_part(dp), pos_part(flip_sign(dm)));
         g2 += g * g;
     }
     return sqrt(g2);

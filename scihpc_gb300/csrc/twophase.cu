@@ -245,6 +245,7 @@ __global__ void k_reinit_a(const double *__restrict__ phi, const double *__restr
 // Tiles of RA_TI (axis 0) x RA_TJ (axis 1) cells: 256 tiles for the 128 x 256 bubble, so
 // that every SM has FP64 work.
 constexpr int RA_TI = 8, RA_TJ = 16;
+
 constexpr int RA_NT = 2 * RA_TI * RA_TJ;   // two threads per cell: one per axis
 
 __global__ void __launch_bounds__(RA_NT)
@@ -331,11 +332,14 @@ __global__ void __launch_bounds__(RA_NT)
     // forward: (q0, q1, q2) = (X(i+1), B(i), Y(i-1)); backward: (Y(i-2), B(i-1), X(i))
     const double Sp = qB1 * qY1 + 6.0 * qX1 * qY1 + 3.0 * qX1 * qB1;
     const double Sm = qB0 * qX0 + 6.0 * qY0 * qX0 + 3.0 * qY0 * qB0;
-    const double r = 1.0 / (Sp * Sm);
+    const double r = rcp_refined(Sp * Sm);
     const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
     const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
     const double dp = v + ih * wp, dm = v - ih * wm;
-    const double ga = sgn > 0.0 ? fmax(-fmin(dp, 0.0), fmax(dm, 0.0)) : fmax(fmax(dp, 0.0), -fmin(dm, 0.0));
+    // Godunov's upwind choice, max(-min(dp, 0), max(dm, 0)) for sgn > 0 and max(max(dp, 0),
+    // -min(dm, 0)) otherwise, on the integer pipe (nonneg_max, pos_part: lsm_device.cuh)
+    const double ga = sign_bits_positive(sgn) ? nonneg_max(pos_part(flip_sign(dp)), pos_part(dm))
+                                              : nonneg_max(pos_part(dp), pos_part(flip_sign(dm)));
     const double gg = ga * ga;
     const double g2 = gg + __shfl_xor_sync(0xffffffffu, gg, 1);   // the same sum in both threads
     if (!live) return;
