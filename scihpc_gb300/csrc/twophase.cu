@@ -397,7 +397,9 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
                         b += B[p];
                     }
         }
-        if (fabs(b) > 1e-8) s += a / b * De[o] * G[o] * fsrc;
+        // a / b by the refined hardware reciprocal (b > 1e-8 here): the division is the longest
+        // dependency chain of this short kernel
+        if (fabs(b) > 1e-8) s += a * rcp_refined(b) * De[o] * G[o] * fsrc;
         sk[o] = s;
     }
     double f = phi[o];
