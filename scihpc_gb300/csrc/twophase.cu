@@ -495,7 +495,7 @@ __global__ void k_stress(StressArgs S, Dims D, int a) {
     }
     p1 *= m;
     p2 *= S.ref * de * (1.0 - S.vr);
-    S.src[o] += (p1 + p2) / S.Re / r;
+    S.src[o] += (p1 + p2) * rcp_refined(S.Re * r);
 }
 
 // add_body_force + add_surface_force (projection_method.cpp:184-242) on interior cells.
@@ -506,8 +506,8 @@ __global__ void k_forces(double *__restrict__ su, double *__restrict__ sv, doubl
     long long o;
     if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
     if (Fr > 0.0) {
-        if (D.ndim == 2) sv[o] += -1.0 / Fr;
-        else if (D.ndim == 3) sw[o] += -1.0 / Fr;
+        if (D.ndim == 2) sv[o] += -rcp_refined(Fr);
+        else if (D.ndim == 3) sw[o] += -rcp_refined(Fr);
     }
     if (We > 0.0) {
         double *dst[3] = {su, sv, sw};
@@ -518,7 +518,7 @@ __global__ void k_forces(double *__restrict__ su, double *__restrict__ sv, doubl
             const double de = 0.5 * (De[o] + De[o + st]);
             const double pp = 0.5 * (pf[a][o] + pf[a][o + st]);
             const double r = 0.5 * (Rho[o] + Rho[o + st]);
-            dst[a][o] -= c * de * pp / (We * r);
+            dst[a][o] -= c * de * pp * rcp_refined(We * r);
         }
     }
 }
@@ -536,14 +536,18 @@ __global__ void k_ab2(double *__restrict__ u, double *__restrict__ v, double *__
     if (D.ndim == 3) w[o] += dt * (1.5 * sw[o] - 0.5 * ow[o]);
 }
 
+// Divisions in the per-cell kernels of the projection step (divergence, correction, stress,
+// forces) go through the refined hardware reciprocal or the rounded 1 / d: an FP64 division
+// is a sequence of about ten FP64 operations, which bounded these kernels on GB300 (results
+// within an ulp or two of the reference's divisions).
 // divergence / dt into RHS (projection_method.cpp:546-568)
 __global__ void k_div_rhs(double *__restrict__ rhs, const double *__restrict__ u, const double *__restrict__ v,
                           const double *__restrict__ w, Dims D, const StepScalars *sc) {
     long long o;
     if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
-    double d = (u[o] - u[o - D.s[0]]) / D.d[0] + (v[o] - v[o - D.s[1]]) / D.d[1];
-    if (D.ndim > 2) d += (w[o] - w[o - 1]) / D.d[2];
-    rhs[o] = d / sc->dt;
+    double d = (u[o] - u[o - D.s[0]]) * D.rd[0] + (v[o] - v[o - D.s[1]]) * D.rd[1];
+    if (D.ndim > 2) d += (w[o] - w[o - 1]) * D.rd[2];
+    rhs[o] = d * rcp_refined(sc->dt);
 }
 
 // velocity correction of projection() (projection_method.cpp:630-654), interior cells
@@ -553,12 +557,12 @@ __global__ void k_correct(double *__restrict__ u, double *__restrict__ v, double
     if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
     const double dt = sc->dt;
     double r = 0.5 * (Rho[o] + Rho[o + D.s[0]]);
-    u[o] -= dt / D.d[0] / r * (p[o + D.s[0]] - p[o]);
+    u[o] -= dt * D.rd[0] * rcp_refined(r) * (p[o + D.s[0]] - p[o]);
     r = 0.5 * (Rho[o] + Rho[o + D.s[1]]);
-    v[o] -= dt / D.d[1] / r * (p[o + D.s[1]] - p[o]);
+    v[o] -= dt * D.rd[1] * rcp_refined(r) * (p[o + D.s[1]] - p[o]);
     if (D.ndim > 2) {
         r = 0.5 * (Rho[o] + Rho[o + 1]);
-        w[o] -= dt / D.d[2] / r * (p[o + 1] - p[o]);
+        w[o] -= dt * D.rd[2] * rcp_refined(r) * (p[o + 1] - p[o]);
     }
 }
 
