@@ -120,9 +120,12 @@ __global__ void k_mpls_fields(const double *__restrict__ phi, const double *__re
     G[q] = sqrt(g);
 }
 
-// pass 2: sums of the lsf_mass contributions and of g delta |grad phi| over interior cells
+// pass 2: sums of the lsf_mass contributions and of g delta |grad phi| over interior cells;
+// the last block to finish adds the block sums in block order (32 lanes, a fixed shuffle tree)
+// and sets mass and eta (one launch fewer per correction than a separate final pass)
 __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restrict__ H, const double *__restrict__ De,
-                            const double *__restrict__ G, Dims D, double dr, int pos, double *__restrict__ partial) {
+                            const double *__restrict__ G, Dims D, double dr, int pos, double *__restrict__ partial,
+                            unsigned *__restrict__ counter, StepScalars *sc) {
     pdl_wait();
     pdl_trigger();
     __shared__ double sh[RED_THREADS];
@@ -167,28 +170,29 @@ __global__ void k_mpls_sums(const double *__restrict__ w, const double *__restri
     const double a = block_reduce<SumOp>(sm, sh);
     __syncthreads();
     const double b = block_reduce<SumOp>(se, sh);
+    __shared__ bool last;
     if (threadIdx.x == 0) {
         partial[blockIdx.x] = a;
         partial[RED_MAX_BLOCKS + blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
-}
-
-__global__ void k_mpls_finish(const double *__restrict__ partial, int nb, StepScalars *sc, double dv) {
-    pdl_wait();
-    pdl_trigger();
-    __shared__ double sh[1024];
+    __syncthreads();
+    if (!last || threadIdx.x >= 32) return;
+    __threadfence();
+    const int nb = int(gridDim.x), lane = int(threadIdx.x);
     double v[2];
     for (int m = 0; m < 2; ++m) {
-        const int per = (nb + blockDim.x - 1) / blockDim.x;
-        double a = 0.0;
-        for (int q = threadIdx.x * per; q < (threadIdx.x + 1) * per && q < nb; ++q) a += partial[m * RED_MAX_BLOCKS + q];
-        v[m] = block_reduce<SumOp>(a, sh);
-        __syncthreads();
+        double t = 0.0;
+        for (int q = lane; q < nb; q += 32) t += __ldcg(&partial[m * RED_MAX_BLOCKS + q]);
+        for (int d = 16; d > 0; d >>= 1) t += __shfl_down_sync(0xffffffffu, t, d);
+        v[m] = t;
     }
-    if (threadIdx.x == 0) {
-        const double mass = v[0] * dv;
+    if (lane == 0) {
+        const double mass = v[0] * D.dv;
         sc->mass = mass;
-        sc->eta = (sc->lsf_mass0 - mass) / (v[1] * dv * sc->dt);
+        sc->eta = (sc->lsf_mass0 - mass) / (v[1] * D.dv * sc->dt);
+        *counter = 0u;
     }
 }
 
@@ -861,6 +865,9 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
     SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_dens, cudaEventDisableTiming));
     SCIHPC_CUDA(cudaMalloc(&partial, 8 * RED_MAX_BLOCKS * sizeof(double)));
     allocs.push_back(partial);
+    SCIHPC_CUDA(cudaMalloc(&mpls_counter, sizeof(unsigned)));
+    SCIHPC_CUDA(cudaMemset(mpls_counter, 0, sizeof(unsigned)));
+    allocs.push_back(mpls_counter);
     SCIHPC_CUDA(cudaMalloc(&sc, sizeof(StepScalars)));
     allocs.push_back(sc);
     SCIHPC_CUDA(cudaMallocHost(&sc_host, sizeof(StepScalars)));
@@ -1132,8 +1139,7 @@ void TwoPhaseGpu::mpls(int count) {
         launch_pdl(pdl, k_mpls_fields, nbf, TPB, 0, stream, phi.data, phi.d1[0], phi.d1[1], phi.d1[2], work, H, delta,
                    grad, rho, D, P.ls_width, P.density_ratio, P.positive_ref);
         launch_pdl(pdl, k_mpls_sums, nb, RED_THREADS, 0, stream, work, H, delta, grad, D, P.density_ratio,
-                   P.positive_ref, partial);
-        launch_pdl(pdl, k_mpls_finish, 1, 1024, 0, stream, partial, nb, sc, D.dv);
+                   P.positive_ref, partial, mpls_counter, sc);
         launch_pdl(pdl, k_mpls_update, nbi, TPB, 0, stream, phi.data, delta, grad, D, sc, phi_fill);
         if (!phi_fill.on) scalar_bc(phi.data);
     }

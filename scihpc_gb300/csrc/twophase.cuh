@@ -146,6 +146,7 @@ private:
     double *src[3] = {nullptr, nullptr, nullptr}, *src_old[3] = {nullptr, nullptr, nullptr};
     double *RHS = nullptr, *s1 = nullptr, *s2 = nullptr, *s3 = nullptr, *t1 = nullptr, *t2 = nullptr, *work = nullptr;
     double *partial = nullptr;
+    unsigned *mpls_counter = nullptr;   // blocks of k_mpls_sums done (the last one resets it)
     StepScalars *sc = nullptr;        // device
     StepScalars *sc_host = nullptr;   // pinned
     std::vector<void *> allocs;
