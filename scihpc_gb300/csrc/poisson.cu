@@ -59,9 +59,10 @@ struct RedSlot {
     unsigned *counter;      // zero-initialised, reset by the last block
 };
 
-// Blocks of exactly TPB threads (1D, or 2D with blockDim.x * blockDim.y == TPB).
+// Blocks of exactly TPB threads (1D, or 2D with blockDim.x * blockDim.y == TPB).  Returns
+// true in the one thread that wrote the sums (thread 0 of the last block).
 template <int NV>
-__device__ void grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
+__device__ bool grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
     __shared__ double sh[NV][TPB];
     __shared__ bool last;
     const int t = threadIdx.x + threadIdx.y * blockDim.x;
@@ -79,7 +80,7 @@ __device__ void grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
         last = ticket == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last) return;
+    if (!last) return false;
     __threadfence();
     const int nb = gridDim.x;
     const int per = (nb + TPB - 1) / TPB;
@@ -98,6 +99,7 @@ __device__ void grid_sum(double (&v)[NV], RedSlot slot, double *out[NV]) {
         for (int m = 0; m < NV; ++m) *out[m] = sh[m][0];
         *slot.counter = 0u;
     }
+    return t == 0;
 }
 
 inline int grid_blocks(long long n) {
@@ -1128,8 +1130,8 @@ __global__ void __launch_bounds__(V2_THREADS) k_vcycle2(Level<T> F, Level<T> Cl,
 // staged by TMA in the boxes of k_sweep3_tma, and every neighbour's d is z + beta d_old read
 // from shared memory.  The new direction itself is stored by k_in_axpy<true>, which reads the
 // same operands cell by cell (a stencil kernel cannot overwrite d in place: neighbouring
-// blocks still read the old values).  The arithmetic is that of k_in_update_d and
-// k_in_apply.  A block owns SW_TJ x SW_TK columns and a chunk of planes; a thread a 2 x 2
+// blocks still read the old values).  The arithmetic is that of k_in_apply<DIM, 1, true>.
+// A block owns SW_TJ x SW_TK columns and a chunk of planes; a thread a 2 x 2
 // group of columns.  The grid is one-dimensional (grid_sum indexes blocks by blockIdx.x).
 constexpr int AP_THREADS = (SW_TJ / 2) * (SW_TK / 2);   // 256 == TPB
 
@@ -1881,38 +1883,20 @@ __global__ void __launch_bounds__(TPB) k_in_dot(Level<float> L, RedSlot slot, Pc
     grid_sum<1>(v, slot, o);
 }
 
-// d = z + beta d, beta = rz / rz_prev (0 on the first inner iteration)
-template <int DIM>
-__global__ void __launch_bounds__(TPB) k_in_update_d(Level<float> L, float *__restrict__ d, const PcgScalars *st) {
-    pdl_wait();
-    pdl_trigger();
-    if (st->done) return;
-    const float beta = (st->in_it == 0 || !(st->rz_prev > 0.0)) ? 0.0f : float(st->rz / st->rz_prev);
-    for_level0<DIM>(L, [&](long long base, int fs, int nf, int k0) {
-        float z[IN_RU], dv[IN_RU];
-#pragma unroll
-        for (int u = 0; u < IN_RU; ++u) {
-            const int k = k0 + u * IN_BX;
-            const long long P = base + (long long)k * fs;
-            z[u] = k < nf ? L.x[P] : 0.0f;
-            dv[u] = k < nf ? d[P] : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < IN_RU; ++u) {
-            const int k = k0 + u * IN_BX;
-            if (k < nf) d[base + (long long)k * fs] = z[u] + beta * dv[u];
-        }
-    });
-}
 
-// q = L d (the level-0 operator of the V-cycle) and <d, q>
-template <int DIM, int MODE>
+// q = L d (the level-0 operator of the V-cycle) and <d, q>.  UPD: d is the new direction
+// z + beta d_old (beta = rz / rz_prev, 0 on the first inner iteration), formed here from z
+// (L.x) and the old direction at every stencil point and stored by k_in_axpy<DIM, true>
+// afterwards, when no block reads the old one any more.
+template <int DIM, int MODE, bool UPD>
 __global__ void __launch_bounds__(TPB) k_in_apply(Level<float> L, const float *__restrict__ rho, Id2<float> id2,
                                                   const float *__restrict__ d, float *__restrict__ q, RedSlot slot,
                                                   PcgScalars *st) {
     pdl_wait();
     pdl_trigger();
     if (st->done) return;
+    const float beta = UPD ? ((st->in_it == 0 || !(st->rz_prev > 0.0)) ? 0.0f : float(st->rz / st->rz_prev)) : 0.0f;
+    auto D_ = [&](int P) { return UPD ? L.x[P] + beta * d[P] : d[P]; };
     float acc = 0.0f;
     const int s0 = int(L.s[0]), s1 = int(L.s[1]);   // padded level 0 has fewer than 2^31 cells
     const float w0 = 2.0f * id2.v[0], w1 = 2.0f * id2.v[1], w2 = 2.0f * id2.v[2];
@@ -1922,16 +1906,18 @@ __global__ void __launch_bounds__(TPB) k_in_apply(Level<float> L, const float *_
             const int k = k0 + u * IN_BX;
             if (k >= nf) continue;
             const int P = int(base) + k * fs;
-            const float dc = d[P];
+            const float dc = D_(P);
             float sq;
             if (MODE == 1) {
                 const float rc = rho[P];
-                sq = w0 * prcp(rc + rho[P - s0]) * (dc - d[P - s0]) + w0 * prcp(rc + rho[P + s0]) * (dc - d[P + s0]) +
-                     w1 * prcp(rc + rho[P - s1]) * (dc - d[P - s1]) + w1 * prcp(rc + rho[P + s1]) * (dc - d[P + s1]);
-                if (DIM == 3) sq += w2 * prcp(rc + rho[P - 1]) * (dc - d[P - 1]) + w2 * prcp(rc + rho[P + 1]) * (dc - d[P + 1]);
+                sq = w0 * prcp(rc + rho[P - s0]) * (dc - D_(P - s0)) + w0 * prcp(rc + rho[P + s0]) * (dc - D_(P + s0)) +
+                     w1 * prcp(rc + rho[P - s1]) * (dc - D_(P - s1)) + w1 * prcp(rc + rho[P + s1]) * (dc - D_(P + s1));
+                if (DIM == 3)
+                    sq += w2 * prcp(rc + rho[P - 1]) * (dc - D_(P - 1)) + w2 * prcp(rc + rho[P + 1]) * (dc - D_(P + 1));
             } else {
-                sq = id2.v[0] * ((dc - d[P - s0]) + (dc - d[P + s0])) + id2.v[1] * ((dc - d[P - s1]) + (dc - d[P + s1]));
-                if (DIM == 3) sq += id2.v[2] * ((dc - d[P - 1]) + (dc - d[P + 1]));
+                sq = id2.v[0] * ((dc - D_(P - s0)) + (dc - D_(P + s0))) +
+                     id2.v[1] * ((dc - D_(P - s1)) + (dc - D_(P + s1)));
+                if (DIM == 3) sq += id2.v[2] * ((dc - D_(P - 1)) + (dc - D_(P + 1)));
             }
             q[P] = sq;
             acc += dc * sq;
@@ -1942,11 +1928,24 @@ __global__ void __launch_bounds__(TPB) k_in_apply(Level<float> L, const float *_
     grid_sum<1>(v, slot, o);
 }
 
+// inner progress; marks the refinement step as due (run by the thread that finished the
+// axpy's residual sum)
+__device__ __forceinline__ void in_check(PcgScalars *st, int inner_max, int max_iter) {
+    st->rz_prev = st->rz;
+    st->it += 1;
+    st->in_it += 1;
+    const double rel = st->rr_in0 > 0.0 ? sqrt(st->rr_in / st->rr_in0) : 0.0;
+    // a residual four times above the best one so far also means FP32 round-off has taken over
+    const bool bad = !(rel == rel) || isinf(rel) || st->in_break || (st->in_it > 1 && st->rr_in > 16.0 * st->rr_in_min);
+    if (st->in_it == 1 || st->rr_in < st->rr_in_min) st->rr_in_min = st->rr_in;
+    st->pending = (bad || rel <= st->in_target || st->in_it >= inner_max || st->it >= max_iter) ? 1 : 0;
+}
+
 // e += alpha d, r -= alpha q, ||r||^2
 template <int DIM, bool UPD>
 __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, float *__restrict__ d,
                                                  const float *__restrict__ q, float *__restrict__ e, RedSlot slot,
-                                                 PcgScalars *st) {
+                                                 PcgScalars *st, int inner_max, int max_iter) {
     pdl_wait();
     pdl_trigger();
     if (st->done) return;
@@ -1988,23 +1987,11 @@ __global__ void __launch_bounds__(TPB) k_in_axpy(Level<float> L, float *__restri
     });
     double v[1] = {double(acc)};
     double *o[1] = {&st->rr_in};
-    grid_sum<1>(v, slot, o);
+    // every other block has read st (alpha, beta) before it added its sum, so the finishing
+    // thread may advance the inner state
+    if (grid_sum<1>(v, slot, o)) in_check(st, inner_max, max_iter);
 }
 
-// inner progress; marks the refinement step as due
-__global__ void k_in_check(PcgScalars *st, int inner_max, int max_iter) {
-    pdl_wait();
-    pdl_trigger();
-    if (st->done) return;
-    st->rz_prev = st->rz;
-    st->it += 1;
-    st->in_it += 1;
-    const double rel = st->rr_in0 > 0.0 ? sqrt(st->rr_in / st->rr_in0) : 0.0;
-    // a residual four times above the best one so far also means FP32 round-off has taken over
-    const bool bad = !(rel == rel) || isinf(rel) || st->in_break || (st->in_it > 1 && st->rr_in > 16.0 * st->rr_in_min);
-    if (st->in_it == 1 || st->rr_in < st->rr_in_min) st->rr_in_min = st->rr_in;
-    st->pending = (bad || rel <= st->in_target || st->in_it >= inner_max || st->it >= max_iter) ? 1 : 0;
-}
 
 // refinement, part 1: p += e
 template <int DIM>
@@ -2770,14 +2757,19 @@ void Poisson::iterate_dim(cudaStream_t s) {
             const unsigned blocks = unsigned(tiles * ((L0.n[0] + aci - 1) / aci));
             launch_pdl(pdl, k_in_apply3_tma, blocks, AP_THREADS, TS_SMEM, s, tmap[0], tmap[2], tmap[5], L0, q32, id2, aci, slot,
                                                                dev_state, &dev_state->sweep_err);
-            launch_pdl(pdl, k_in_axpy<DIM, true>, nbi, ib, 0, s, L0, d32, q32, e32, slot, dev_state);
+            launch_pdl(pdl, k_in_axpy<DIM, true>, nbi, ib, 0, s, L0, d32, q32, e32, slot, dev_state, inner_max,
+                       max_iter);
         } else {
-            launch_pdl(pdl, k_in_update_d<DIM>, nbi, ib, 0, s, L0, d32, dev_state);
-            if (mode0 == 1) launch_pdl(pdl, k_in_apply<DIM, 1>, nbi, ib, 0, s, L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
-            else launch_pdl(pdl, k_in_apply<DIM, 2>, nbi, ib, 0, s, L0, (const float *)rho_pad, id2, d32, q32, slot, dev_state);
-            launch_pdl(pdl, k_in_axpy<DIM, false>, nbi, ib, 0, s, L0, d32, q32, e32, slot, dev_state);
+            // direction update fused into the apply; axpy stores d and runs the inner check
+            if (mode0 == 1)
+                launch_pdl(pdl, k_in_apply<DIM, 1, true>, nbi, ib, 0, s, L0, (const float *)rho_pad, id2, d32, q32, slot,
+                           dev_state);
+            else
+                launch_pdl(pdl, k_in_apply<DIM, 2, true>, nbi, ib, 0, s, L0, (const float *)rho_pad, id2, d32, q32, slot,
+                           dev_state);
+            launch_pdl(pdl, k_in_axpy<DIM, true>, nbi, ib, 0, s, L0, d32, q32, e32, slot, dev_state, inner_max,
+                       max_iter);
         }
-        launch_pdl(pdl, k_in_check, 1, 1, 0, s, dev_state, inner_max, max_iter);
         launch_pdl(pdl, k_out_add<DIM>, nb, TPB, 0, s, p_, e32, O, L0, dev_state);
         launch_pdl(pdl, k_out_res<DIM>, nb, TPB, 0, s, rhs_, p_, O, L0, e32, slot, dev_state);
         launch_pdl(pdl, k_out_check, 1, 1, 0, s, dev_state, max_iter, conditional, uc);
