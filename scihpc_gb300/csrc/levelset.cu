@@ -35,8 +35,8 @@ __device__ __forceinline__ double weno_face(double a, double b, double c, double
         q2 = (-a + 5.0 * b + 2.0 * c) * sixth;
     }
     // WENO-Z weights a_k = d_k (1 + tau / g_k), g_k = eps + beta_k, multiplied through by
-    // g0 g1 g2 so that one reciprocal remains (the refined hardware reciprocal: within ~1 ulp
-    // of the reference's division)
+    // g0 g1 g2 so that one reciprocal remains (the refined hardware reciprocal: within about
+    // an ulp of the reference's division)
     const double tau = fabs(b0 - b2);
     const double g0 = WENO_EPS + b0, g1 = WENO_EPS + b1, g2 = WENO_EPS + b2;
     const double a0 = (g0 + tau) * g1 * g2;

@@ -25,12 +25,14 @@ __device__ __forceinline__ double nonneg_max(double a, double b) {
 }
 // x > 0 for a non-NaN x
 __device__ __forceinline__ bool sign_bits_positive(double x) { return __double_as_longlong(x) > 0; }
-// 1 / x for a normal, finite x: the hardware's approximate reciprocal and one Newton-Raphson
-// step y (2 - x y) (the error squares: the weights' normalisation needs far less than FP64's
-// last bits; the reference's correctly rounded division and this differ by ~1 ulp)
+// 1 / x for a normal, finite x: the hardware's approximate reciprocal and two Newton-Raphson
+// steps y += y (1 - x y), each squaring the relative error, so that the result is within
+// about an ulp of the correctly rounded division (with one step the WENO derivatives of the
+// solver-class test ended 1e-12 away from the reference's where differences cancel)
 __device__ __forceinline__ double rcp_refined(double x) {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    y = fma(y, fma(-x, y, 1.0), y);
     return fma(y, fma(-x, y, 1.0), y);
 }
 
