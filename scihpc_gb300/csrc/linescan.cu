@@ -71,8 +71,8 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
             const double o0 = __shfl_up_sync(FULL, c0[q], d), o1 = __shfl_up_sync(FULL, c1[q], d);
             if (lane >= d) {
                 const double *ml = me[q] + 4 * st * T;
-                const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + c0[q];
-                const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + c1[q];
+                const double a = fma(ml[0 * T], o0, fma(ml[1 * T], o1, c0[q]));
+                const double b = fma(ml[2 * T], o0, fma(ml[3 * T], o1, c1[q]));
                 c0[q] = a, c1[q] = b;
             }
         }
@@ -92,16 +92,16 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
             double p0 = 0.0, p1 = 0.0;
             for (int w = 0; w < warp; ++w) {
                 const double *m = wt[q] + 8 * w;
-                const double a = m[0] * p0 + m[1] * p1 + sh[q][w].x;
-                const double b = m[2] * p0 + m[3] * p1 + sh[q][w].y;
+                const double a = fma(m[0], p0, fma(m[1], p1, sh[q][w].x));
+                const double b = fma(m[2], p0, fma(m[3], p1, sh[q][w].y));
                 p0 = a, p1 = b;
             }
             if (lane == 0) {
                 v0[q] = p0, v1[q] = p1;
             } else {
                 const double *ml = me[q] + 20 * T;
-                const double a = ml[0 * T] * p0 + ml[1 * T] * p1 + v0[q];
-                const double b = ml[2 * T] * p0 + ml[3 * T] * p1 + v1[q];
+                const double a = fma(ml[0 * T], p0, fma(ml[1 * T], p1, v0[q]));
+                const double b = fma(ml[2 * T], p0, fma(ml[3 * T], p1, v1[q]));
                 v0[q] = a, v1[q] = b;
             }
         }
@@ -135,14 +135,14 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
 #pragma unroll
             for (int q = 0; q < NS; ++q) {
                 const double *t = pt[q] + (size_t)k * 12 * T;
-                const double e0 = t[8 * T] * r0[q][k] + t[9 * T] * r1[q][k];
-                const double e1 = t[10 * T] * r0[q][k] + t[11 * T] * r1[q][k];
+                const double e0 = fma(t[8 * T], r0[q][k], t[9 * T] * r1[q][k]);
+                const double e1 = fma(t[10 * T], r0[q][k], t[11 * T] * r1[q][k]);
                 r0[q][k] = e0, r1[q][k] = e1;
                 if (i == n - 1) {
                     g0[q] = e0, g1[q] = e1;
                 } else {
-                    const double a = t[4 * T] * g0[q] + t[5 * T] * g1[q] + e0;
-                    const double b = t[6 * T] * g0[q] + t[7 * T] * g1[q] + e1;
+                    const double a = fma(t[4 * T], g0[q], fma(t[5 * T], g1[q], e0));
+                    const double b = fma(t[6 * T], g0[q], fma(t[7 * T], g1[q], e1));
                     g0[q] = a, g1[q] = b;
                 }
             }
@@ -156,8 +156,8 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
             const double o0 = __shfl_down_sync(FULL, g0[q], d), o1 = __shfl_down_sync(FULL, g1[q], d);
             if (lane + d < 32) {
                 const double *ml = me[q] + (24 + 4 * st) * T;
-                const double a = ml[0 * T] * o0 + ml[1 * T] * o1 + g0[q];
-                const double b = ml[2 * T] * o0 + ml[3 * T] * o1 + g1[q];
+                const double a = fma(ml[0 * T], o0, fma(ml[1 * T], o1, g0[q]));
+                const double b = fma(ml[2 * T], o0, fma(ml[3 * T], o1, g1[q]));
                 g0[q] = a, g1[q] = b;
             }
         }
@@ -177,16 +177,16 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
             double p0 = 0.0, p1 = 0.0;
             for (int w = WPL - 1; w > warp; --w) {
                 const double *m = wt[q] + 8 * w + 4;
-                const double a = m[0] * p0 + m[1] * p1 + sh[q][w].x;
-                const double b = m[2] * p0 + m[3] * p1 + sh[q][w].y;
+                const double a = fma(m[0], p0, fma(m[1], p1, sh[q][w].x));
+                const double b = fma(m[2], p0, fma(m[3], p1, sh[q][w].y));
                 p0 = a, p1 = b;
             }
             if (lane == 31) {
                 x0[q] = p0, x1[q] = p1;
             } else {
                 const double *ml = me[q] + 44 * T;
-                const double a = ml[0 * T] * p0 + ml[1 * T] * p1 + x0[q];
-                const double b = ml[2 * T] * p0 + ml[3 * T] * p1 + x1[q];
+                const double a = fma(ml[0 * T], p0, fma(ml[1 * T], p1, x0[q]));
+                const double b = fma(ml[2 * T], p0, fma(ml[3 * T], p1, x1[q]));
                 x0[q] = a, x1[q] = b;
             }
         }
@@ -202,8 +202,8 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
                     x0[q] = r0[q][k], x1[q] = r1[q][k];
                 } else {
                     const double *t = pt[q] + (size_t)k * 12 * T;
-                    const double a = t[4 * T] * x0[q] + t[5 * T] * x1[q] + r0[q][k];
-                    const double b = t[6 * T] * x0[q] + t[7 * T] * x1[q] + r1[q][k];
+                    const double a = fma(t[4 * T], x0[q], fma(t[5 * T], x1[q], r0[q][k]));
+                    const double b = fma(t[6 * T], x0[q], fma(t[7 * T], x1[q], r1[q][k]));
                     x0[q] = a, x1[q] = b;
                 }
                 r0[q][k] = x0[q], r1[q][k] = x1[q];
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
     const long long base = D.at(idx[0], idx[1], idx[2]);
     const long long st = D.s[a];
     const int n = D.N[a];
-    const double ih = D.rd[a];
+    const double ih = D.rd[a], ih2 = ih * ih;
     const int C = (n + 32 * WPL - 1) / (32 * WPL);
     const int lo = (WPL > 1 ? int(threadIdx.x) : lane) * C;
     const int cnt = lo >= n ? 0 : (lo + C <= n ? C : n - lo);
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
                 r0[0][k] = s, r1[0][k] = ss;
                 r0[1][k] = s, r1[1][k] = ss;
             } else {
-                const double ss = (3.0 * fm - 6.0 * fc + 3.0 * fp) * ih * ih;
+                const double ss = fma(3.0, fm, fma(-6.0, fc, 3.0 * fp)) * ih2;
                 if (MODE == 1) {
                     r0[0][k] = (c1 * fm + c2 * fc + c3 * fp) * ih;
                     r0[1][k] = -(c3 * fm + c2 * fc + c1 * fp) * ih;
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict
         const double *f = F + l * pf;
         double *v = V + ((size_t)q * lpb + l) * pv;
         const double *op = q == 0 ? opA : opB;
-        const double ih = D.rd[a];
+        const double ih = D.rd[a], ih2 = ih * ih;
         const double c3 = -0.06096119008109, c2 = 1.99692238016218, c1 = -1.93596119008109;
         // forward elimination; one-sided closures at both ends (uccd_solver.cpp:29-51,
         // ccd_solver.cpp:31-40), interior right-hand sides (uccd_solver.cpp:17-19,:33-41,
@@ -438,15 +438,15 @@ __global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict
 #pragma unroll 2
         for (int i = 1; i < n - 1; ++i) {
             const double fp = f[i + 1];
-            double ssu = (3.0 * fm - 6.0 * f0 + 3.0 * fp) * ih * ih;
+            double ssu = fma(3.0, fm, fma(-6.0, f0, 3.0 * fp)) * ih2;
             double su;
             if (MODE == 1) su = q == 0 ? (c1 * fm + c2 * f0 + c3 * fp) * ih : -(c3 * fm + c2 * f0 + c1 * fp) * ih;
             else su = 15.0 / 16.0 * (fp - fm) * ih;
             fm = f0;
             f0 = fp;
             const double *r = op + (size_t)i * 12;
-            su = su - (r[0] * u_p + r[1] * uu_p);
-            ssu = ssu - (r[2] * u_p + r[3] * uu_p);
+            su = fma(-r[0], u_p, fma(-r[1], uu_p, su));
+            ssu = fma(-r[2], u_p, fma(-r[3], uu_p, ssu));
             u_p = su, uu_p = ssu;
             v[2 * i] = su;
             v[2 * i + 1] = ssu;
@@ -456,8 +456,8 @@ __global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict
             double su = -(-3.5 * f[n - 1] + 4.0 * f[n - 2] - 0.5 * f[n - 3]) * ih;
             double ssu = (9.0 * f[n - 1] - 12.0 * f[n - 2] + 3.0 * f[n - 3]) * ih * ih;
             const double *r = op + (size_t)i * 12;
-            su = su - (r[0] * u_p + r[1] * uu_p);
-            ssu = ssu - (r[2] * u_p + r[3] * uu_p);
+            su = fma(-r[0], u_p, fma(-r[1], uu_p, su));
+            ssu = fma(-r[2], u_p, fma(-r[3], uu_p, ssu));
             // back substitution starts here
             double xu = r[8] * su + r[9] * ssu;
             double yu = r[10] * su + r[11] * ssu;
@@ -467,10 +467,10 @@ __global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict
             for (int k = n - 2; k >= 0; --k) {
                 const double *rk = op + (size_t)k * 12;
                 double sk = v[2 * k], ssk = v[2 * k + 1];
-                sk = sk - (rk[4] * xu + rk[5] * yu);
-                ssk = ssk - (rk[6] * xu + rk[7] * yu);
-                xu = rk[8] * sk + rk[9] * ssk;
-                yu = rk[10] * sk + rk[11] * ssk;
+                sk = fma(-rk[4], xu, fma(-rk[5], yu, sk));
+                ssk = fma(-rk[6], xu, fma(-rk[7], yu, ssk));
+                xu = fma(rk[8], sk, rk[9] * ssk);
+                yu = fma(rk[10], sk, rk[11] * ssk);
                 v[2 * k] = xu;
                 v[2 * k + 1] = yu;
             }

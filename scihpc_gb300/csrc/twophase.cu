@@ -288,10 +288,10 @@ __global__ void __launch_bounds__(RA_NT)
     }
     __syncthreads();
     auto pair_q = [](double u, double w, double &qx, double &qy, double &qb) {
-        const double d = w - u, t = 13.0 * d * d;
-        const double x = w - 3.0 * u, y = 3.0 * w - u, z = w + u;
-        const double ex = WENO_EPS + (t + 3.0 * x * x), ey = WENO_EPS + (t + 3.0 * y * y),
-                     eb = WENO_EPS + (t + 3.0 * z * z);
+        // eps + 13 d^2 + 3 x^2 (and y, z) with the common part formed once, as FMAs
+        const double d = w - u, te = fma(13.0 * d, d, WENO_EPS);
+        const double x = fma(-3.0, u, w), y = fma(3.0, w, -u), z = w + u;
+        const double ex = fma(3.0 * x, x, te), ey = fma(3.0 * y, y, te), eb = fma(3.0 * z, z, te);
         qx = ex * ex, qy = ey * ey, qb = eb * eb;
     };
     for (int e = tid; e < QI * RA_TJ + RA_TI * QJ; e += RA_NT) {
