@@ -332,10 +332,12 @@ __global__ void __launch_bounds__(RA_NT)
     const double p1 = ax == 0 ? P[ti + 4][tj + 3] : P[ti + 3][tj + 4];
     const double p2 = ax == 0 ? P[ti + 5][tj + 3] : P[ti + 3][tj + 5];
     const double ih = D.rd[ax];
-    const double v = ih * (1.0 / 12.0) * (-(m1 - m2) + 7.0 * (c0 - m1) + 7.0 * (p1 - c0) - (p2 - p1));
+    // the fourth-order central difference (-(m1 - m2) + 7 (c0 - m1) + 7 (p1 - c0) - (p2 - p1)) / 12,
+    // its 7 c0 terms cancelled: ((m2 - p2) + 8 (p1 - m1)) / 12
+    const double v = ih * (1.0 / 12.0) * fma(8.0, p1 - m1, m2 - p2);
     // forward: (q0, q1, q2) = (X(i+1), B(i), Y(i-1)); backward: (Y(i-2), B(i-1), X(i))
-    const double Sp = qB1 * qY1 + 6.0 * qX1 * qY1 + 3.0 * qX1 * qB1;
-    const double Sm = qB0 * qX0 + 6.0 * qY0 * qX0 + 3.0 * qY0 * qB0;
+    const double Sp = fma(qY1, fma(6.0, qX1, qB1), 3.0 * qX1 * qB1);   // qB1 qY1 + 6 qX1 qY1 + 3 qX1 qB1
+    const double Sm = fma(qX0, fma(6.0, qY0, qB0), 3.0 * qY0 * qB0);   // qB0 qX0 + 6 qY0 qX0 + 3 qY0 qB0
     const double r = rcp_refined(Sp * Sm);
     const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
     const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
