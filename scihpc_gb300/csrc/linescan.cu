@@ -246,6 +246,8 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
     auto F = [&](int i) { return f[(long long)src(i) * st]; };
     double r0[2][CM], r1[2][CM];   // [0]: the (upwind) system, [1]: UCCD's downwind system
     const double c3 = -0.06096119008109, c2 = 1.99692238016218, c1 = -1.93596119008109;
+    const double k3 = 3.0 * ih2, k6 = -6.0 * ih2, k15 = 15.0 / 16.0 * ih;
+    const double u1 = c1 * ih, u2 = c2 * ih, u3 = c3 * ih, w1 = -c3 * ih, w2 = -c2 * ih, w3 = -c1 * ih;
     double fm = cnt > 0 && lo > 0 ? F(lo - 1) : 0.0;
     double fc = cnt > 0 ? F(lo) : 0.0;
 #pragma unroll
@@ -268,13 +270,14 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
                 r0[0][k] = s, r1[0][k] = ss;
                 r0[1][k] = s, r1[1][k] = ss;
             } else {
-                const double ss = fma(3.0, fm, fma(-6.0, fc, 3.0 * fp)) * ih2;
+                // interior stencils with the 1 / h factors folded into the coefficients
+                const double ss = fma(k3, fm + fp, k6 * fc);
                 if (MODE == 1) {
-                    r0[0][k] = (c1 * fm + c2 * fc + c3 * fp) * ih;
-                    r0[1][k] = -(c3 * fm + c2 * fc + c1 * fp) * ih;
+                    r0[0][k] = fma(u1, fm, fma(u2, fc, u3 * fp));
+                    r0[1][k] = fma(w1, fm, fma(w2, fc, w3 * fp));
                     r1[1][k] = ss;
                 } else {
-                    r0[0][k] = 15.0 / 16.0 * (fp - fm) * ih;
+                    r0[0][k] = k15 * (fp - fm);
                 }
                 r1[0][k] = ss;
             }
@@ -427,6 +430,10 @@ __global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict
         const double *op = q == 0 ? opA : opB;
         const double ih = D.rd[a], ih2 = ih * ih;
         const double c3 = -0.06096119008109, c2 = 1.99692238016218, c1 = -1.93596119008109;
+        // interior stencils with the 1 / h factors folded into the coefficients; UCCD's
+        // downwind system has the mirrored first-derivative stencil
+        const double k3 = 3.0 * ih2, k6 = -6.0 * ih2, k15 = 15.0 / 16.0 * ih;
+        const double s1c = (q == 0 ? c1 : -c3) * ih, s2c = (q == 0 ? c2 : -c2) * ih, s3c = (q == 0 ? c3 : -c1) * ih;
         // forward elimination; one-sided closures at both ends (uccd_solver.cpp:29-51,
         // ccd_solver.cpp:31-40), interior right-hand sides (uccd_solver.cpp:17-19,:33-41,
         // ccd_solver.cpp:22-28)
@@ -438,10 +445,10 @@ __global__ void __launch_bounds__(SEQ_MAX_LPB * 2) seq_kernel(double *__restrict
 #pragma unroll 2
         for (int i = 1; i < n - 1; ++i) {
             const double fp = f[i + 1];
-            double ssu = fma(3.0, fm, fma(-6.0, f0, 3.0 * fp)) * ih2;
+            double ssu = fma(k3, fm + fp, k6 * f0);
             double su;
-            if (MODE == 1) su = q == 0 ? (c1 * fm + c2 * f0 + c3 * fp) * ih : -(c3 * fm + c2 * f0 + c1 * fp) * ih;
-            else su = 15.0 / 16.0 * (fp - fm) * ih;
+            if (MODE == 1) su = fma(s1c, fm, fma(s2c, f0, s3c * fp));
+            else su = k15 * (fp - fm);
             fm = f0;
             f0 = fp;
             const double *r = op + (size_t)i * 12;
