@@ -162,8 +162,8 @@ Mat2 mat_mul(const Mat2 &b, const Mat2 &a) {
 }
 }  // namespace
 
-std::vector<double> lane_table(const std::vector<double> &tab, int n, int wpl, int C) {
-    const int T = 32 * wpl;
+std::vector<double> lane_table(const std::vector<double> &tab, int n, int wpl, int C, int seg) {
+    const int T = seg * wpl;   // seg: lanes per line (32, or 16 with wpl 1)
     const size_t pts = size_t(C) * 12 * T;
     std::vector<double> out(pts + size_t(T) * 48 + size_t(wpl) * 8, 0.0);
     for (int t = 0; t < T; ++t)
@@ -188,30 +188,31 @@ std::vector<double> lane_table(const std::vector<double> &tab, int n, int wpl, i
         F[t] = f;
         G[t] = g;
     }
+    const int S = seg;   // lanes of one shuffle scan
     for (int w = 0; w < wpl; ++w) {
-        Mat2 *f = &F[size_t(w) * 32], *g = &G[size_t(w) * 32];
-        for (int st = 0, d = 1; d < 32; ++st, d <<= 1) {
-            const std::vector<Mat2> f0(f, f + 32), g0(g, g + 32);
-            for (int l = 0; l < 32; ++l) {
-                double *e = &out[pts + size_t(w) * 32 + l];
+        Mat2 *f = &F[size_t(w) * S], *g = &G[size_t(w) * S];
+        for (int st = 0, d = 1; d < S; ++st, d <<= 1) {
+            const std::vector<Mat2> f0(f, f + S), g0(g, g + S);
+            for (int l = 0; l < S; ++l) {
+                double *e = &out[pts + size_t(w) * S + l];
                 for (int q = 0; q < 4; ++q) {
                     e[size_t(4 * st + q) * T] = f0[l][q];
                     e[size_t(24 + 4 * st + q) * T] = g0[l][q];
                 }
                 if (l >= d) f[l] = mat_mul(f0[l], f0[l - d]);
-                if (l + d < 32) g[l] = mat_mul(g0[l], g0[l + d]);
+                if (l + d < S) g[l] = mat_mul(g0[l], g0[l + d]);
             }
         }
-        for (int l = 0; l < 32; ++l) {
-            double *e = &out[pts + size_t(w) * 32 + l];
+        for (int l = 0; l < S; ++l) {
+            double *e = &out[pts + size_t(w) * S + l];
             for (int q = 0; q < 4; ++q) {
                 e[size_t(20 + q) * T] = l > 0 ? f[l - 1][q] : 0.0;
-                e[size_t(44 + q) * T] = l < 31 ? g[l + 1][q] : 0.0;
+                e[size_t(44 + q) * T] = l < S - 1 ? g[l + 1][q] : 0.0;
             }
         }
         double *wt = &out[pts + size_t(T) * 48 + size_t(w) * 8];
         for (int q = 0; q < 4; ++q) {
-            wt[q] = f[31][q];
+            wt[q] = f[S - 1][q];
             wt[4 + q] = g[0][q];
         }
     }
@@ -413,10 +414,10 @@ int CompactOps::build(const Dims &D) {
         SCIHPC_CUDA(cudaMemcpy(ccd[a], tc.data(), bytes, cudaMemcpyHostToDevice));
         SCIHPC_CUDA(cudaMemcpy(up[a], tu.data(), bytes, cudaMemcpyHostToDevice));
         SCIHPC_CUDA(cudaMemcpy(down[a], td.data(), bytes, cudaMemcpyHostToDevice));
-        int wpl, C;
-        if (scan_shape(D, a, wpl, C)) {
-            std::vector<double> lc = lane_table(sc, n, wpl, C), lu = lane_table(su, n, wpl, C),
-                                ld = lane_table(sd, n, wpl, C);
+        int wpl, C, seg;
+        if (scan_shape(D, a, wpl, C, seg)) {
+            std::vector<double> lc = lane_table(sc, n, wpl, C, seg), lu = lane_table(su, n, wpl, C, seg),
+                                ld = lane_table(sd, n, wpl, C, seg);
             const size_t lb = lc.size() * sizeof(double);
             SCIHPC_CUDA(cudaMalloc(&lane_ccd[a], 3 * lb));
             lane_up[a] = lane_ccd[a] + lc.size();
@@ -424,7 +425,7 @@ int CompactOps::build(const Dims &D) {
             SCIHPC_CUDA(cudaMemcpy(lane_ccd[a], lc.data(), lb, cudaMemcpyHostToDevice));
             SCIHPC_CUDA(cudaMemcpy(lane_up[a], lu.data(), lb, cudaMemcpyHostToDevice));
             SCIHPC_CUDA(cudaMemcpy(lane_down[a], ld.data(), lb, cudaMemcpyHostToDevice));
-            lane_wpl[a] = wpl, lane_c[a] = C, lane_n[a] = n;
+            lane_wpl[a] = wpl, lane_c[a] = C, lane_n[a] = n, lane_seg[a] = seg;
         }
     }
     return SCIHPC_OK;
@@ -437,6 +438,7 @@ void CompactOps::release() {
         if (lane_ccd[a]) cudaFree(lane_ccd[a]);
         lane_ccd[a] = lane_up[a] = lane_down[a] = nullptr;
         lane_wpl[a] = lane_c[a] = lane_n[a] = 0;
+        lane_seg[a] = 32;
     }
 }
 

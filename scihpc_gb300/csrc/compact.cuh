@@ -17,6 +17,7 @@ struct CompactOps {
     double *lane_up[3] = {nullptr, nullptr, nullptr};
     double *lane_down[3] = {nullptr, nullptr, nullptr};
     int lane_wpl[3] = {0, 0, 0}, lane_c[3] = {0, 0, 0}, lane_n[3] = {0, 0, 0};
+    int lane_seg[3] = {32, 32, 32};   // lanes per line: 32, or 16 (two lines per warp)
     int build(const Dims &D);
     void release();
 };
@@ -25,12 +26,16 @@ struct CompactOps {
 // of C points; when there are few lines (fewer than four per SM) two or four warps share one
 // line, for shorter FP64 dependency chains and more warps in flight.  False for lines longer
 // than 16 points per lane.
-inline bool scan_shape(const Dims &D, int a, int &wpl, int &C) {
+inline bool scan_shape(const Dims &D, int a, int &wpl, int &C, int &seg) {
     const long long lines = (long long)D.N[(a + 1) % 3] * D.N[(a + 2) % 3];
     const int n = D.N[a];
     wpl = 1;
     if (lines < 4LL * NUM_SMS) wpl = n >= 192 ? 4 : (n >= 96 ? 2 : 1);
-    C = (n + 32 * wpl - 1) / (32 * wpl);
+    // many lines of 65-160 points: 16 lanes per line, two lines per warp (chunks of up to 10
+    // points: fewer idle lanes than 32 chunks of 3-5, and one shuffle step less); the FP64
+    // work per point, not the parallelism, bounds these solves
+    seg = wpl == 1 && n > 64 && n <= 160 && lines >= 8LL * NUM_SMS ? 16 : 32;
+    C = (n + seg * wpl - 1) / (seg * wpl);
     return C <= 16;
 }
 

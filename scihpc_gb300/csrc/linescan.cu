@@ -30,12 +30,16 @@ namespace {
 // {-L00 -L01 -L10 -L11, K00 K01 K10 K11, D00 D01 D10 D11} (L negated: each row of the forward
 // step is two FMAs), then the matrix halves of the chunk and scan maps, so that only the vector
 // halves are formed here; tid: the thread's index within its line.
-template <int NS, int CM, int WPL>
+// SW: lanes per line within a warp (32, or 16 for two lines per warp when lines are many and
+// moderately long: fewer idle lanes and one shuffle step less); lane is the lane within them.
+template <int NS, int CM, int WPL, int SW = 32>
 __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[2][CM], const double *__restrict__ ltA,
                                               const double *__restrict__ ltB, int tid, int lo, int cnt, int n, int C,
                                               int lane, int warp, double2 (*sh)[WPL > 1 ? WPL : 1]) {
     constexpr unsigned FULL = 0xffffffffu;
-    constexpr int T = 32 * WPL;
+    static_assert(SW == 32 || (SW == 16 && WPL == 1), "half-warp lines have one segment");
+    constexpr int T = SW * WPL;
+    constexpr int STEPS = SW == 32 ? 5 : 4;
     const double *pt[2], *me[2], *wt[2];
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
@@ -64,11 +68,11 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
         }
     }
 #pragma unroll
-    for (int st = 0; st < 5; ++st) {
+    for (int st = 0; st < STEPS; ++st) {
         const int d = 1 << st;
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
-            const double o0 = __shfl_up_sync(FULL, c0[q], d), o1 = __shfl_up_sync(FULL, c1[q], d);
+            const double o0 = __shfl_up_sync(FULL, c0[q], d, SW), o1 = __shfl_up_sync(FULL, c1[q], d, SW);
             if (lane >= d) {
                 const double *ml = me[q] + 4 * st * T;
                 const double a = fma(ml[0 * T], o0, fma(ml[1 * T], o1, c0[q]));
@@ -79,7 +83,7 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
     }
     double v0[2], v1[2];   // v at lo-1
 #pragma unroll
-    for (int q = 0; q < NS; ++q) v0[q] = __shfl_up_sync(FULL, c0[q], 1), v1[q] = __shfl_up_sync(FULL, c1[q], 1);
+    for (int q = 0; q < NS; ++q) v0[q] = __shfl_up_sync(FULL, c0[q], 1, SW), v1[q] = __shfl_up_sync(FULL, c1[q], 1, SW);
     if (WPL > 1) {
         // warp w enters with the composition of warps 0 .. w-1
         if (lane == 31) {
@@ -149,12 +153,12 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
         }
     }
 #pragma unroll
-    for (int st = 0; st < 5; ++st) {
+    for (int st = 0; st < STEPS; ++st) {
         const int d = 1 << st;
 #pragma unroll
         for (int q = 0; q < NS; ++q) {
-            const double o0 = __shfl_down_sync(FULL, g0[q], d), o1 = __shfl_down_sync(FULL, g1[q], d);
-            if (lane + d < 32) {
+            const double o0 = __shfl_down_sync(FULL, g0[q], d, SW), o1 = __shfl_down_sync(FULL, g1[q], d, SW);
+            if (lane + d < SW) {
                 const double *ml = me[q] + (24 + 4 * st) * T;
                 const double a = fma(ml[0 * T], o0, fma(ml[1 * T], o1, g0[q]));
                 const double b = fma(ml[2 * T], o0, fma(ml[3 * T], o1, g1[q]));
@@ -164,7 +168,7 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
     }
     double x0[2], x1[2];   // x at lo+cnt
 #pragma unroll
-    for (int q = 0; q < NS; ++q) x0[q] = __shfl_down_sync(FULL, g0[q], 1), x1[q] = __shfl_down_sync(FULL, g1[q], 1);
+    for (int q = 0; q < NS; ++q) x0[q] = __shfl_down_sync(FULL, g0[q], 1, SW), x1[q] = __shfl_down_sync(FULL, g1[q], 1, SW);
     if (WPL > 1) {
         // composition of the warps after this one
         if (lane == 0) {
@@ -217,16 +221,21 @@ __device__ __forceinline__ void solve_systems(double (&r0)[2][CM], double (&r1)[
 // f1 = its CCD first derivative.
 // WPL == 1: each warp of the block solves its own line.  WPL > 1: the block's WPL warps solve
 // one line together (shorter chunks per lane, and the per-warp maps combined in shared memory).
-template <int MODE, int CM, int WPL>
+template <int MODE, int CM, int WPL, int SW = 32>
 __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, const double *__restrict__ vel,
                                                    double *__restrict__ f1, double *__restrict__ f2,
                                                    const double *__restrict__ ltA, const double *__restrict__ ltB,
                                                    Dims D, int a, int fast, int slow) {
     __shared__ double2 sh[2][WPL > 1 ? WPL : 1];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long line = WPL > 1 ? (long long)blockIdx.x : (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    // lane: the thread's lane within its line's SW lanes
+    const int lane = threadIdx.x & (SW - 1), warp = threadIdx.x >> 5;
+    const long long line = WPL > 1 ? (long long)blockIdx.x : (long long)blockIdx.x * (blockDim.x / SW) + threadIdx.x / SW;
     const long long nf = D.N[fast], ns = D.N[slow];
-    if (line >= nf * ns) return;   // uniform per warp (per block when WPL > 1)
+    // SW 32: uniform per warp (per block when WPL > 1); SW 16: the second half-warp of the
+    // grid's last warp may have no line, and it still takes part in the shuffles (which stay
+    // within each half)
+    const bool has_line = line < nf * ns;
+    if (SW == 32 && !has_line) return;
     int idx[3];
     idx[a] = 0;
     idx[fast] = int(line % nf);
@@ -235,9 +244,9 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
     const long long st = D.s[a];
     const int n = D.N[a];
     const double ih = D.rd[a], ih2 = ih * ih;
-    const int C = (n + 32 * WPL - 1) / (32 * WPL);
+    const int C = (n + SW * WPL - 1) / (SW * WPL);
     const int lo = (WPL > 1 ? int(threadIdx.x) : lane) * C;
-    const int cnt = lo >= n ? 0 : (lo + C <= n ? C : n - lo);
+    const int cnt = !has_line || lo >= n ? 0 : (lo + C <= n ? C : n - lo);
     double *f = io + base;
     auto src = [&](int i) -> int {
         if (MODE != 2) return i;
@@ -295,7 +304,7 @@ __global__ void __launch_bounds__(256) scan_kernel(double *__restrict__ io, cons
         }
     }
     const int tid = WPL > 1 ? int(threadIdx.x) : lane;
-    solve_systems<MODE == 1 ? 2 : 1, CM, WPL>(r0, r1, ltA, ltB, tid, lo, cnt, n, C, lane, warp, sh);
+    solve_systems<MODE == 1 ? 2 : 1, CM, WPL, SW>(r0, r1, ltA, ltB, tid, lo, cnt, n, C, lane, warp, sh);
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
         if (k < cnt) {
@@ -342,11 +351,17 @@ bool launch_scan(const Dims &D, const CompactOps &ops, int a, double *io, const 
 #undef SCAN_WPL
         return true;
     }
-    // many lines: one warp per line, up to eight lines per block
+    // many lines: one warp per line (two with 16-lane lines), up to eight warps per block
+    const int lpw = ops.lane_seg[a] == 16 ? 2 : 1;
     int wpb = 1;
-    while (wpb < 8 && lines >= (long long)wpb * 2 * 4 * NUM_SMS) wpb *= 2;
-    const unsigned blocks = unsigned((lines + wpb - 1) / wpb);
+    while (wpb < 8 && lines >= (long long)wpb * lpw * 2 * 4 * NUM_SMS) wpb *= 2;
+    const unsigned blocks = unsigned((lines + (long long)wpb * lpw - 1) / ((long long)wpb * lpw));
     const int tpb = 32 * wpb;
+    if (lpw == 2) {
+        if (C > 10) return false;
+        scan_kernel<MODE, 10, 1, 16><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow);
+        return true;
+    }
     if (C <= 4) scan_kernel<MODE, 4, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow);
     else if (C <= 8) scan_kernel<MODE, 8, 1><<<blocks, tpb, 0, s>>>(io, vel, f1, f2, ltA, ltB, D, a, fast, slow);
     else if (C <= 16)
