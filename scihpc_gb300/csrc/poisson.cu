@@ -547,6 +547,11 @@ constexpr int SW_TJ = 16;                    // interior j rows per tile
 constexpr int SW_PAIRS = SW_TK / 2 + 2;      // with the ring
 constexpr int SW_ROWS = SW_TJ + 2;
 constexpr int SW_THREADS = SW_PAIRS * SW_ROWS;   // 612
+// row pitch (floats) of the staged sweep's first-colour exchange: rows 16 banks apart, so the
+// two rows a warp covers fall in different banks
+constexpr int SW_FROW = 48;
+static_assert(SW_TK == 64 && SW_TJ % 2 == 0 && SW_ROWS % 2 == 0, "thread layout of the staged sweep");
+static_assert(SW_THREADS - SW_TJ * (SW_PAIRS - 2) == 68 + 2 * SW_TJ, "ring threads of the staged sweep");
 
 // Per-level constants of the sweep: MODE 1 w[a] = 2 / d_a^2 (face coefficient
 // w / (rho_c + rho_nb)); MODE 2 w[a] = 1 / d_a^2 and dinv = 1 / (2 sum w).
@@ -746,21 +751,27 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
     extern __shared__ unsigned char ts_raw[];
     __shared__ uint64_t bar[NS];
     // after the plane loop, DOT reuses these SW_THREADS * 2 floats as SW_THREADS doubles
-    __shared__ __align__(16) float first[2][SW_ROWS][SW_PAIRS];
-    static_assert(2 * SW_ROWS * SW_PAIRS >= 2 * SW_THREADS, "reduction scratch");
+    __shared__ __align__(16) float first[2][SW_ROWS][SW_FROW];
+    static_assert(2 * SW_ROWS * SW_FROW >= 2 * SW_THREADS, "reduction scratch");
     float *tiles = reinterpret_cast<float *>(ts_raw + ((128 - (tc::smem_u32(ts_raw) & 127)) & 127));
     const int tid = threadIdx.x;
-    // Warps 0 .. SW_TJ-1 each own one interior row of SW_TK/2 column pairs (first and second
-    // colour); the remaining threads own the ring's pairs (first colour only), so the second-
-    // colour update never diverges inside an interior warp.
+    // Warps 0 .. SW_TJ-1 own the interior (first and second colour); the remaining threads own
+    // the ring's pairs (first colour only), so the second-colour update never diverges inside an
+    // interior warp.  Lanes 0-15 of a warp take 16 column pairs of one row and lanes 16-31 the
+    // same pairs of the next row, whose colour parity is the opposite: the half-warps read the
+    // even and the odd words of the staged boxes, so a warp's shared-memory loads (stride two
+    // words per lane) meet no bank conflict.  The ring's rows 0 and SW_ROWS - 1 (an odd distance
+    // apart) are paired the same way.
     int row, pr;
+    const int hw = (tid >> 4) & 1, hl = tid & 15;
     if (tid < SW_TJ * (SW_PAIRS - 2)) {
-        row = tid / (SW_PAIRS - 2) + 1, pr = tid % (SW_PAIRS - 2) + 1;
+        const int w = tid >> 5;
+        row = 2 * (w >> 1) + 1 + hw, pr = 16 * (w & 1) + 1 + hl;
     } else {
         const int r = tid - SW_TJ * (SW_PAIRS - 2);
-        if (r < SW_PAIRS) row = 0, pr = r;
-        else if (r < 2 * SW_PAIRS) row = SW_ROWS - 1, pr = r - SW_PAIRS;
-        else row = (r - 2 * SW_PAIRS) / 2 + 1, pr = ((r - 2 * SW_PAIRS) & 1) ? SW_PAIRS - 1 : 0;
+        if (r < 64) row = hw ? SW_ROWS - 1 : 0, pr = 16 * (r >> 5) + hl;
+        else if (r < 68) row = (r & 2) ? SW_ROWS - 1 : 0, pr = 32 + (r & 1);
+        else row = (r - 68) / 2 + 1, pr = ((r - 68) & 1) ? SW_PAIRS - 1 : 0;
     }
     const int tiles_k = (L.n[2] + SW_TK - 1) / SW_TK;
     const int tk = blockIdx.x % tiles_k, tj = blockIdx.x / tiles_k;
@@ -957,9 +968,11 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
         // planes q - 1 .. q + 1 are on chip
         const float *Xc = tiles + oc0, *Xm = tiles + om1, *Xp = tiles + op1;
         const float *Rc = Xc + TS_PLANE, *Rm = Xm + TS_PLANE, *Rp = Xp + TS_PLANE, *Bc = Xc + 2 * TS_PLANE;
+        // the upper half-warp takes its two cells in the other order, so that at each step the
+        // half-warps read the odd and the even words (no shared-memory bank conflict)
 #pragma unroll
         for (int dk = 0; dk < 2; ++dk) {
-            const int o = sc + dk;
+            const int o = sc + (dk ^ ((tid >> 4) & 1));
             const float rc = Rc[o], xc = Xc[o];
             const float C0 = pdiv(2.0f, rc + Rm[o]) * c0, C1 = pdiv(2.0f, rc + Rp[o]) * c0;
             const float C2 = pdiv(2.0f, rc + Rc[o - TS_W]) * c1, C3 = pdiv(2.0f, rc + Rc[o + TS_W]) * c1;
@@ -1190,10 +1203,13 @@ __global__ void __launch_bounds__(AP_THREADS)
         const float *Rc = Zc + TS_PLANE, *Rm = Zm + TS_PLANE, *Rp = Zp + TS_PLANE;
         const float *Dc = Zc + 2 * TS_PLANE, *Dm = Zm + 2 * TS_PLANE, *Dp = Zp + 2 * TS_PLANE;
         const int i = i0 - 1 + qq;
+        // the upper half-warp takes the two columns in the other order (no shared-memory bank
+        // conflict between the half-warps, as in k_restrict3_tma)
 #pragma unroll
         for (int dj = 0; dj < 2; ++dj)
 #pragma unroll
-            for (int dk = 0; dk < 2; ++dk) {
+            for (int dx = 0; dx < 2; ++dx) {
+                const int dk = dx ^ ((tid >> 4) & 1);
                 const int o = sc + dj * TS_W + dk;
                 const float dc = Zc[o] + beta * Dc[o];
                 const float rc = Rc[o];
