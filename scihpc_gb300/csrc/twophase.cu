@@ -246,18 +246,16 @@ __global__ void k_reinit_a(const double *__restrict__ phi, const double *__restr
 // times per cell, and the two normalisations of a cell share one division.  The arithmetic
 // is FP64 throughout (godunov_gradient.cpp:19-198); the rounding differs from godunov_at's
 // only in the order of operations.
-// Tiles of RA_TI (axis 0) x RA_TJ (axis 1) cells: 256 tiles for the 128 x 256 bubble, so
-// that every SM has FP64 work.
-constexpr int RA_TI = 8, RA_TJ = 16;
-
-constexpr int RA_NT = 2 * RA_TI * RA_TJ;   // two threads per cell: one per axis
-
-__global__ void __launch_bounds__(RA_NT)
+// Tiles of RA_TI (axis 0) x RA_TJ (axis 1) cells, two threads per cell (one per axis); the
+// tile shape is chosen per grid at launch (reinit_a2d_shape).
+template <int RA_TI, int RA_TJ>
+__global__ void __launch_bounds__(2 * RA_TI * RA_TJ)
     k_reinit_a2d(const double *__restrict__ phi, const double *__restrict__ sg, const double *__restrict__ De,
                  double *__restrict__ G, double *__restrict__ s, double *__restrict__ A, double *__restrict__ B, Dims D,
                  double rdt, const StepScalars *sc) {
     pdl_wait();
     pdl_trigger();
+    constexpr int RA_NT = 2 * RA_TI * RA_TJ;
     constexpr int PI = RA_TI + 6, PJ = RA_TJ + 6;   // phi with three ghost layers
     constexpr int DI = RA_TI + 4, DJ = RA_TJ + 4;   // second differences at -2 .. T+1
     constexpr int QI = RA_TI + 3, QJ = RA_TJ + 3;   // pairs at -2 .. T
@@ -358,6 +356,39 @@ __global__ void __launch_bounds__(RA_NT)
         A[o] = sgn * de * (g - 1.0);
         B[o] = g * de * de;
     }
+}
+
+// Tile shape of k_reinit_a2d for a 2D grid.  The kernel is bound by the FP64 pipe of each
+// SM, so its time follows the SM with the most work: the tiles that SM receives times the
+// FP64 operations of one tile (the pair terms and second differences include the tile's
+// halo, so larger tiles cost less per cell).  The 128 x 256 bubble gets 16 x 14 tiles, 152
+// tiles for 152 SMs (8 x 16 tiles, 256 of them, put two tiles on 104 SMs and one on the
+// other 48); small grids get 8 x 8 tiles, for more blocks.
+enum ReinitShape { RA_16x14 = 0, RA_8x8 = 1 };
+inline ReinitShape reinit_a2d_shape(const Dims &D) {
+    const int ti[2] = {16, 8}, tj[2] = {14, 8};
+    int best = 0;
+    double best_cost = 0.0;
+    for (int c = 0; c < 2; ++c) {
+        const long long tiles = (long long)((D.n[0] + ti[c] - 1) / ti[c]) * ((D.n[1] + tj[c] - 1) / tj[c]);
+        // FP64 operations of one tile: ~13 per indicator pair, 3 per second difference, ~80 per
+        // cell for the two corrections, the upwind choice and the outputs
+        const double pairs = double((ti[c] + 3) * tj[c] + ti[c] * (tj[c] + 3));
+        const double d2 = double((ti[c] + 4) * tj[c] + ti[c] * (tj[c] + 4));
+        const double work = 13.0 * pairs + 3.0 * d2 + 80.0 * ti[c] * tj[c];
+        const double cost = double((tiles + NUM_SMS - 1) / NUM_SMS) * work;
+        if (c == 0 || cost < best_cost) best = c, best_cost = cost;
+    }
+    return ReinitShape(best);
+}
+
+template <class... A>
+inline void launch_reinit_a2d(bool pdl, ReinitShape shape, const Dims &D, cudaStream_t s, A &&...args) {
+    auto grid = [&](int ti, int tj) {
+        return dim3(unsigned((D.n[1] + tj - 1) / tj), unsigned((D.n[0] + ti - 1) / ti));
+    };
+    if (shape == RA_16x14) launch_pdl(pdl, k_reinit_a2d<16, 14>, grid(16, 14), 2 * 16 * 14, 0, s, args...);
+    else launch_pdl(pdl, k_reinit_a2d<8, 8>, grid(8, 8), 2 * 8 * 8, 0, s, args...);
 }
 
 // lambda correction with the zero-order-extrapolated a, b (a ghost reads the nearest
@@ -1152,9 +1183,8 @@ void TwoPhaseGpu::reinit_stage(int stage) {
     double *S[3] = {s1, s2, s3};
     const bool pdl = pdl_step();
     if (D.ndim == 2)
-        launch_pdl(pdl, k_reinit_a2d,
-                   dim3(unsigned((D.n[1] + RA_TJ - 1) / RA_TJ), unsigned((D.n[0] + RA_TI - 1) / RA_TI)), RA_NT, 0,
-                   stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt, sc);
+        launch_reinit_a2d(pdl, reinit_a2d_shape(D), D, stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D,
+                          P.rdt, sc);
     else
         launch_pdl(pdl, k_reinit_a, nbi, TPB, 0, stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt,
                    sc);
@@ -1668,8 +1698,8 @@ int TwoPhaseGpu::time_reinit_gradient(int n, float *ms) {
     const unsigned nbi = blocks_for(D.interior(), TPB);
     auto launch = [&]() {
         if (D.ndim == 2)
-            k_reinit_a2d<<<dim3(unsigned((D.n[1] + RA_TJ - 1) / RA_TJ), unsigned((D.n[0] + RA_TI - 1) / RA_TI)), RA_NT,
-                           0, stream>>>(phi.data, sign, delta, grad, s1, a_f, b_f, D, P.rdt, sc);
+            launch_reinit_a2d(false, reinit_a2d_shape(D), D, stream, phi.data, sign, delta, grad, s1, a_f, b_f, D,
+                              P.rdt, sc);
         else
             k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, s1, a_f, b_f, D, P.rdt, sc);
     };
