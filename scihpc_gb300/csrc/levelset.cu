@@ -45,24 +45,72 @@ __device__ __forceinline__ double weno_face(double a, double b, double c, double
     return (a0 * q0 + a1 * q1 + a2 * q2) * rcp_refined(a0 + a1 + a2);
 }
 
-// Upwinded face value between cells i and i+1 (weno_solver.cpp:185-199): only the
-// reconstruction the face velocity selects is formed.
+// Upwinded face value between cells i and i+1 (weno_solver.cpp:185-199).  The right-biased
+// reconstruction is the left-biased one of the mirrored stencil (interpolation_p /
+// indicators_p are interpolation_m / indicators_m read from the other side), so the face
+// velocity only selects the five inputs and every thread runs the same instructions.
 __device__ __forceinline__ double weno_upwind_face(const double *f, long long o, long long st, const double *vel) {
-    if (vel[o] + vel[o + st] > 0.0) return weno_face(f[o - 2 * st], f[o - st], f[o], f[o + st], f[o + 2 * st], true);
-    return weno_face(f[o - st], f[o], f[o + st], f[o + 2 * st], f[o + 3 * st], false);
+    const bool up = vel[o] + vel[o + st] > 0.0;
+    const long long c = up ? o : o + st, dn = up ? st : -st;
+    return weno_face(f[c - 2 * dn], f[c - dn], f[c], f[c + dn], f[c + 2 * dn], true);
 }
 
-__global__ void weno_kernel(const double *__restrict__ f, const double *__restrict__ vel, double *__restrict__ out,
-                            Dims D, int a) {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= D.interior()) return;
-    int I, J, K;
-    split3(q, D, I, J, K);
-    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+// d/dx_a of the upwinded WENO flux (weno_solver.cpp:185-199): (h(i+1/2) - h(i-1/2)) / d_a.
+// Every face is computed once and shared by the two cells beside it.
+// Along the contiguous axis (a = ndim - 1): lane l of a warp computes the face between cells
+// c0 + l - 1 and c0 + l of one line, and lanes 0..30 take their cell's derivative from their
+// own face and the next lane's (31 cells per warp).
+constexpr int WZ_SEG = 31;
+__global__ void weno_kernel_lane(const double *__restrict__ f, const double *__restrict__ vel, double *__restrict__ out,
+                                 Dims D, int a) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int na = D.n[a];
+    const long long segs = (na + WZ_SEG - 1) / WZ_SEG;
+    const long long lines = D.interior() / na;
+    if (warp >= lines * segs) return;   // whole warps leave together
+    const long long line = warp / segs;
+    const int c0 = int(warp - line * segs) * WZ_SEG;
+    // the line's cells: the other interior indices (axis 0 slowest)
+    int I = 0, J = 0;
+    if (D.ndim == 3) {
+        I = int(line / D.n[1]);
+        J = int(line - (long long)I * D.n[1]);
+    } else {
+        I = int(line);
+    }
+    const int c = c0 + lane - 1;   // this lane's face lies between cells c and c + 1
     const long long st = D.s[a];
-    const double hr = weno_upwind_face(f, o, st, vel);
-    const double hl = weno_upwind_face(f, o - st, st, vel);
-    out[o] = (hr - hl) / D.d[a];
+    const long long o = D.ndim == 3 ? D.at(D.ix(0, I), D.ix(1, J), D.ix(2, c)) : D.at(D.ix(0, I), D.ix(1, c), 0);
+    const double h = c < na ? weno_upwind_face(f, o, st, vel) : 0.0;
+    const double hn = __shfl_down_sync(0xffffffffu, h, 1);
+    if (lane < WZ_SEG && c + 1 < na) out[o + st] = (hn - h) / D.d[a];
+}
+
+// Along the other axes: a block of 32 x WZ_W threads, lanes along the contiguous axis, warp w
+// computes the faces between cells a0 + w - 1 and a0 + w; warps 0 .. WZ_W - 2 then form the
+// derivatives of cells a0 .. a0 + WZ_W - 2 from shared memory.
+constexpr int WZ_W = 8;
+__global__ void __launch_bounds__(32 * WZ_W)
+    weno_kernel_tile(const double *__restrict__ f, const double *__restrict__ vel, double *__restrict__ out, Dims D,
+                     int a) {
+    __shared__ double H[WZ_W][33];
+    const int lane = threadIdx.x, w = threadIdx.y;
+    const int cl = D.ndim - 1;                  // contiguous axis
+    const int ot = D.ndim == 3 ? 3 - a - cl : -1;   // the remaining axis (3D)
+    const int q = blockIdx.x * 32 + lane;       // index along the contiguous axis
+    const int c = blockIdx.y * (WZ_W - 1) + w - 1;   // the face lies between cells c and c + 1 along a
+    const int r = blockIdx.z;                   // index along the remaining axis (3D)
+    const bool live = q < D.n[cl] && c < D.n[a];
+    int idx[3] = {0, 0, 0};
+    idx[cl] = q;
+    idx[a] = c;
+    if (ot >= 0) idx[ot] = r;
+    const long long st = D.s[a];
+    const long long o = D.at(D.ix(0, idx[0]), D.ix(1, idx[1]), D.ndim == 3 ? D.ix(2, idx[2]) : 0);
+    H[w][lane] = live ? weno_upwind_face(f, o, st, vel) : 0.0;
+    __syncthreads();
+    if (w < WZ_W - 1 && live && c + 1 < D.n[a]) out[o + st] = (H[w + 1][lane] - H[w][lane]) / D.d[a];
 }
 
 }  // namespace
@@ -208,7 +256,15 @@ void launch_guess_from_history(const Dims &D, const double *old, const double *o
 }
 
 void launch_weno5(const Dims &D, int a, const double *flux, const double *vel, double *out, cudaStream_t s) {
-    weno_kernel<<<blocks_for(D.interior(), 128), 128, 0, s>>>(flux, vel, out, D, a);
+    if (a == D.ndim - 1) {
+        const long long warps = D.interior() / D.n[a] * ((D.n[a] + WZ_SEG - 1) / WZ_SEG);
+        weno_kernel_lane<<<blocks_for(warps * 32, 128), 128, 0, s>>>(flux, vel, out, D, a);
+    } else {
+        const int cl = D.ndim - 1, ot = D.ndim == 3 ? 3 - a - cl : -1;
+        const dim3 grid(unsigned((D.n[cl] + 31) / 32), unsigned((D.n[a] + WZ_W - 2) / (WZ_W - 1)),
+                        unsigned(ot >= 0 ? D.n[ot] : 1));
+        weno_kernel_tile<<<grid, dim3(32, WZ_W), 0, s>>>(flux, vel, out, D, a);
+    }
 }
 
 void launch_godunov(const Dims &D, const double *phi, const double *sign, double *grad, cudaStream_t s) {

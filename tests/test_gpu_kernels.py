@@ -160,6 +160,26 @@ def test_weno5(port, gi):
         assert np.abs(o[I] - ref[a][I]).max() <= TOL * np.abs(ref[a][I]).max(), a
 
 
+@pytest.mark.parametrize("g", [LONG[0], LONG[1], LONG[4], LONG[5]], ids=lambda g: "x".join(map(str, g.n)))
+def test_weno5_long(port, g):
+    """Grids with several warp segments along the contiguous axis and several tiles (and
+    partial ones) along the others: every face is computed once and shared by its two cells."""
+    w = ws(g)
+    rng = np.random.default_rng(750)
+    flux = smooth_field(g, rng) + 0.3 * np.sign(smooth_field(g, rng))
+    vel = [rng.standard_normal(g.shape) for _ in range(3)]
+    ref = port.weno5(g, flux, *vel)
+    I = g.interior()
+    for a in range(g.ndim):
+        out = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
+        w.weno5(a, dev(flux), dev(vel[a]), out)
+        o = host(out)
+        assert np.abs(o[I] - ref[a][I]).max() <= TOL * np.abs(ref[a][I]).max(), a
+        ghosts = np.ones(o.shape, dtype=bool)
+        ghosts[I] = False
+        assert not np.any(o[ghosts]), a   # only interior cells are written
+
+
 @pytest.mark.parametrize("gi", range(len(GRIDS)))
 def test_godunov(port, gi):
     g = GRIDS[gi]
