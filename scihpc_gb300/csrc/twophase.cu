@@ -887,6 +887,12 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
         if (a < D.ndim - 1)
             for (int c = 0; c < D.ndim; ++c) ALLOC(fv[a][c]);
     }
+    if (D.ndim == 2)
+        for (int a = 0; a < 2; ++a)
+            for (int k = 0; k < 2; ++k) {
+                ALLOC(tbs1[a][k]);
+                ALLOC(tbs2[a][k]);
+            }
 #undef ALLOC
     nfield_allocs = allocs.size();
     for (int k = 0; k < 3; ++k) {
@@ -894,6 +900,13 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
         SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
     }
     SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    for (int a = 0; a < 3; ++a) {
+        SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_sub[a], cudaEventDisableTiming));
+        for (int k = 0; k < 2; ++k) {
+            SCIHPC_CUDA(cudaStreamCreateWithFlags(&sub[a][k], cudaStreamNonBlocking));
+            SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_subj[a][k], cudaEventDisableTiming));
+        }
+    }
     SCIHPC_CUDA(cudaStreamCreateWithFlags(&dens_stream, cudaStreamNonBlocking));
     SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_dens, cudaEventDisableTiming));
     SCIHPC_CUDA(cudaMalloc(&partial, 8 * RED_MAX_BLOCKS * sizeof(double)));
@@ -944,6 +957,16 @@ void TwoPhaseGpu::destroy() {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     ev_fork = nullptr;
+    for (int a = 0; a < 3; ++a) {
+        if (ev_sub[a]) cudaEventDestroy(ev_sub[a]);
+        ev_sub[a] = nullptr;
+        for (int k = 0; k < 2; ++k) {
+            if (sub[a][k]) cudaStreamDestroy(sub[a][k]);
+            if (ev_subj[a][k]) cudaEventDestroy(ev_subj[a][k]);
+            sub[a][k] = nullptr;
+            ev_subj[a][k] = nullptr;
+        }
+    }
     if (dens_stream) cudaStreamDestroy(dens_stream);
     if (ev_dens) cudaEventDestroy(ev_dens);
     dens_stream = nullptr;
@@ -956,6 +979,18 @@ void TwoPhaseGpu::destroy() {
 void TwoPhaseGpu::fork(int n) {
     cudaEventRecord(ev_fork, stream);
     for (int k = 0; k < n; ++k) cudaStreamWaitEvent(side[k], ev_fork, 0);
+}
+
+// sub-branches of the branch running on stream `s`: sub[g][0 .. n-1] start after the work
+// already issued on s; sub_join(g, k, s) makes s wait for sub[g][k]
+void TwoPhaseGpu::sub_fork(int g, int n, cudaStream_t s) {
+    cudaEventRecord(ev_sub[g], s);
+    for (int k = 0; k < n; ++k) cudaStreamWaitEvent(sub[g][k], ev_sub[g], 0);
+}
+
+void TwoPhaseGpu::sub_join(int g, int k, cudaStream_t s) {
+    cudaEventRecord(ev_subj[g][k], sub[g][k]);
+    cudaStreamWaitEvent(s, ev_subj[g][k], 0);
 }
 
 void TwoPhaseGpu::join(int n) {
@@ -1250,6 +1285,13 @@ void TwoPhaseGpu::find_source() {
                 launch_sec_mixed(D, 2, phi.d1[1], phi.mixed[1], s);
                 launch_sec_mixed(D, 0, phi.d1[2], phi.mixed[2], s);
             }
+        } else if (split_source()) {
+            // the y derivatives beside the x derivatives and their mixed derivative
+            sub_fork(2, 1, s);
+            launch_ccd(D, ops, 0, phi.flux, phi.d1[0], phi.d2[0], s);
+            launch_ccd(D, ops, 1, phi.flux, phi.d1[1], phi.d2[1], sub[2][0]);
+            launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
+            sub_join(2, 0, s);
         } else {
             for (int a = 0; a < nd; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], s);
             launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
@@ -1282,19 +1324,29 @@ void TwoPhaseGpu::find_source() {
         // identity_with_extrapolation_face_*)
         DevScalar &U = vel[a];
         launch_extrapolate(D, 1 + a, U.data, U.flux, s);
+        // 2D: the y derivative and the cross derivative on sub-branches beside the x derivative
+        const bool split = split_source();
+        if (split) sub_fork(a, 2, s);
         // (find_source_sec: convection_sec with secSol's upwind-biased derivative, source.cpp:42-73)
         for (int b = 0; b < nd; ++b) {
             if (source_scheme == 1) launch_sec_upwind(D, b, U.flux, nv[b], U.d1[b], U.d2[b], s);
+            else if (split && b > 0)
+                launch_uccd(D, ops, b, U.flux, nv[b], U.d1[b], U.d2[b], tbs1[a][0], tbs2[a][0], sub[a][0]);
             else launch_uccd(D, ops, b, U.flux, nv[b], U.d1[b], U.d2[b], tb1[a], tb2[a], s);
         }
+        if (split) sub_join(a, 0, s);
         k_convection_s<<<nbi, TPB, 0, s>>>(src[a], nv[0], nv[1], nv[2], U.d1[0], U.d1[1], U.d1[2], D);
         // cross derivatives of the other face-averaged components along a
         for (int c = 0; c < nd; ++c) {
             if (c == a) continue;
-            launch_extrapolate(D, 1 + a, nv[c], fv_flux[a], s);
+            cudaStream_t sx = split ? sub[a][1] : s;
+            launch_extrapolate(D, 1 + a, nv[c], fv_flux[a], sx);
             if (source_scheme == 1) launch_sec_upwind(D, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], s);
+            else if (split)
+                launch_uccd(D, ops, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], tbs1[a][1], tbs2[a][1], sx);
             else launch_uccd(D, ops, a, fv_flux[a], nv[a], nvel[c].d1[a], nvel[c].d2[a], tb1[a], tb2[a], s);
         }
+        if (split) sub_join(a, 1, s);
     }
     join(nd);
     const double ref = P.positive_ref ? 1.0 : -1.0;

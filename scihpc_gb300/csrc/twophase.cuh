@@ -109,6 +109,8 @@ private:
     // events; the branches become parallel nodes when the step is captured as a graph)
     void fork(int n);
     void join(int n);
+    void sub_fork(int g, int n, cudaStream_t s);
+    void sub_join(int g, int k, cudaStream_t s);
     // Programmatic dependent launches (in 2D, as for the multigrid) for the two chains of
     // small kernels that run back to back on the main stream: the reinitialisation stages and
     // the mass correction (451 -> 475 steps/s on the bubble step).  Measured on the same box:
@@ -127,6 +129,13 @@ private:
     // per-direction face-averaged velocities of find_source for the directions other than the
     // last (that one uses nvel, as before), their extrapolation scratch and line-solve scratch
     double *fv[3][3] = {}, *fv_flux[3] = {}, *tb1[3] = {}, *tb2[3] = {};
+    // 2D: inside find_source's branches the line solves that do not depend on one another run
+    // as parallel branches of their own (sub[a][k], a = velocity direction, 2 = the level set);
+    // each concurrent UCCD solve has its own scratch (used only by the long-line fallback)
+    bool split_source() const { return D.ndim == 2 && source_scheme != 1; }
+    cudaStream_t sub[3][2] = {};
+    cudaEvent_t ev_sub[3] = {}, ev_subj[3][2] = {};
+    double *tbs1[2][2] = {}, *tbs2[2][2] = {};
 
     HostParams P{};
     int scheme = 1, n_mpls = 5, reinit_every = 1, fp32 = 0, reinit_lambda = 1;
