@@ -218,22 +218,7 @@ __global__ void k_sign(const double *__restrict__ phi, double *__restrict__ sg, 
     if (q < n) sg[q] = sign_d(phi[q], lw);
 }
 
-// Godunov gradient, the redistance source and the lambda-correction fields a, b.
-__global__ void k_reinit_a(const double *__restrict__ phi, const double *__restrict__ sg,
-                           const double *__restrict__ De, double *__restrict__ G, double *__restrict__ s,
-                           double *__restrict__ A, double *__restrict__ B, Dims D, double rdt, const StepScalars *sc) {
-    pdl_wait();
-    pdl_trigger();
-    long long o;
-    if (!interior_cell((long long)blockIdx.x * blockDim.x + threadIdx.x, D, o)) return;
-    const double g = godunov_at(phi, o, sg[o], D);
-    G[o] = g;
-    s[o] = -sg[o] * (g - 1.0) * rdt / sc->dt;
-    A[o] = sg[o] * De[o] * (g - 1.0);
-    B[o] = g * De[o] * De[o];
-}
-
-// k_reinit_a for 2D grids, on tiles of RA_T x RA_T cells in shared memory.  The Godunov
+// The reinitialisation's gradient kernel for 2D grids, on tiles of RA_T x RA_T cells in shared memory.  The Godunov
 // gradient needs, per cell and axis, two WENO-JS corrections (forward and backward), each
 // from four second differences D2 and three smoothness indicators.  The indicators of
 // neighbouring cells are the same three functions of consecutive pairs (u, w) = (D2[p],
@@ -389,6 +374,153 @@ inline void launch_reinit_a2d(bool pdl, ReinitShape shape, const Dims &D, cudaSt
     };
     if (shape == RA_16x14) launch_pdl(pdl, k_reinit_a2d<16, 14>, grid(16, 14), 2 * 16 * 14, 0, s, args...);
     else launch_pdl(pdl, k_reinit_a2d<8, 8>, grid(8, 8), 2 * 8 * 8, 0, s, args...);
+}
+
+// The reinitialisation's gradient kernel for 3D grids: the tiled scheme of k_reinit_a2d on R3_TI x R3_TJ x R3_TK cells
+// (dynamic shared memory: phi with three ghost layers, the second differences along each axis
+// and the three (eps + indicator)^2 terms of every pair), one thread per cell and axis with
+// the axes in separate warps; the per-axis arithmetic is that of k_reinit_a2d, the squares
+// of the three one-sided choices are summed in axis order and the axis-0 threads write the
+// outputs.
+constexpr int R3_TI = 4, R3_TJ = 8, R3_TK = 8;
+constexpr int R3_NC = R3_TI * R3_TJ * R3_TK;   // cells per tile
+constexpr int R3_NT = 3 * R3_NC;
+constexpr int R3_PI = R3_TI + 6, R3_PJ = R3_TJ + 6, R3_PK = R3_TK + 6;
+// D2 along axis 0 / 1 / 2 at -2 .. T+1 of that axis, and the pairs at -2 .. T
+constexpr int R3_ND0 = (R3_TI + 4) * R3_TJ * R3_TK, R3_ND1 = R3_TI * (R3_TJ + 4) * R3_TK,
+              R3_ND2 = R3_TI * R3_TJ * (R3_TK + 4);
+constexpr int R3_NQ0 = (R3_TI + 3) * R3_TJ * R3_TK, R3_NQ1 = R3_TI * (R3_TJ + 3) * R3_TK,
+              R3_NQ2 = R3_TI * R3_TJ * (R3_TK + 3);
+constexpr size_t R3_SMEM =
+    sizeof(double) * (size_t(R3_PI) * R3_PJ * R3_PK + R3_ND0 + R3_ND1 + R3_ND2 + 3 * (R3_NQ0 + R3_NQ1 + R3_NQ2) + 3 * R3_NC);
+static_assert(R3_NC % 32 == 0, "the axes of k_reinit_a3d run in whole warps");
+
+__global__ void __launch_bounds__(R3_NT, 2)
+    k_reinit_a3d(const double *__restrict__ phi, const double *__restrict__ sg, const double *__restrict__ De,
+                 double *__restrict__ G, double *__restrict__ s, double *__restrict__ A, double *__restrict__ B, Dims D,
+                 double rdt, const StepScalars *sc) {
+    pdl_wait();
+    pdl_trigger();
+    extern __shared__ __align__(16) double r3[];
+    double *P = r3;                                      // [PI][PJ][PK]
+    double *D0 = P + R3_PI * R3_PJ * R3_PK;              // [TI+4][TJ][TK]
+    double *D1 = D0 + R3_ND0;                            // [TI][TJ+4][TK]
+    double *D2 = D1 + R3_ND1;                            // [TI][TJ][TK+4]
+    double *Q0 = D2 + R3_ND2;                            // [3][TI+3][TJ][TK]
+    double *Q1 = Q0 + 3 * R3_NQ0;                        // [3][TI][TJ+3][TK]
+    double *Q2 = Q1 + 3 * R3_NQ1;                        // [3][TI][TJ][TK+3]
+    double *GG = Q2 + 3 * R3_NQ2;                        // [3][cells]
+    __shared__ double fsrc;
+    const int tid = threadIdx.x;
+    const int K0 = blockIdx.x * R3_TK, J0 = blockIdx.y * R3_TJ, I0 = blockIdx.z * R3_TI;
+    if (tid == 0) fsrc = rdt / sc->dt;
+    auto pidx = [](int i, int j, int k) { return (i * R3_PJ + j) * R3_PK + k; };
+    for (int e = tid; e < R3_PI * R3_PJ * R3_PK; e += R3_NT) {
+        const int i = e / (R3_PJ * R3_PK), r = e - i * (R3_PJ * R3_PK), j = r / R3_PK, k = r - j * R3_PK;
+        const int I = I0 - 3 + i, J = J0 - 3 + j, K = K0 - 3 + k;
+        double v = 0.0;
+        if (I >= -GHC && I < D.n[0] + GHC && J >= -GHC && J < D.n[1] + GHC && K >= -GHC && K < D.n[2] + GHC)
+            v = phi[D.at(I + GHC, J + GHC, K + GHC)];
+        P[e] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < R3_ND0 + R3_ND1 + R3_ND2; e += R3_NT) {
+        if (e < R3_ND0) {   // along axis 0: tile rows -2 .. TI+1
+            const int a = e / (R3_TJ * R3_TK), r = e - a * (R3_TJ * R3_TK), b = r / R3_TK, c = r - b * R3_TK;
+            D0[e] = P[pidx(a + 2, b + 3, c + 3)] - 2.0 * P[pidx(a + 1, b + 3, c + 3)] + P[pidx(a, b + 3, c + 3)];
+        } else if (e < R3_ND0 + R3_ND1) {
+            const int f = e - R3_ND0;
+            const int a = f / ((R3_TJ + 4) * R3_TK), r = f - a * ((R3_TJ + 4) * R3_TK), b = r / R3_TK, c = r - b * R3_TK;
+            D1[f] = P[pidx(a + 3, b + 2, c + 3)] - 2.0 * P[pidx(a + 3, b + 1, c + 3)] + P[pidx(a + 3, b, c + 3)];
+        } else {
+            const int f = e - R3_ND0 - R3_ND1;
+            const int a = f / (R3_TJ * (R3_TK + 4)), r = f - a * (R3_TJ * (R3_TK + 4)), b = r / (R3_TK + 4),
+                      c = r - b * (R3_TK + 4);
+            D2[f] = P[pidx(a + 3, b + 3, c + 2)] - 2.0 * P[pidx(a + 3, b + 3, c + 1)] + P[pidx(a + 3, b + 3, c)];
+        }
+    }
+    __syncthreads();
+    auto pair_q = [](double u, double w, double &qx, double &qy, double &qb) {
+        const double d = w - u, te = fma(13.0 * d, d, WENO_EPS);
+        const double x = fma(-3.0, u, w), y = fma(3.0, w, -u), z = w + u;
+        const double ex = fma(3.0 * x, x, te), ey = fma(3.0 * y, y, te), eb = fma(3.0 * z, z, te);
+        qx = ex * ex, qy = ey * ey, qb = eb * eb;
+    };
+    for (int e = tid; e < R3_NQ0 + R3_NQ1 + R3_NQ2; e += R3_NT) {
+        if (e < R3_NQ0) {   // pair p = a - 2 along axis 0: D0 rows a, a + 1
+            pair_q(D0[e], D0[e + R3_TJ * R3_TK], Q0[e], Q0[R3_NQ0 + e], Q0[2 * R3_NQ0 + e]);
+        } else if (e < R3_NQ0 + R3_NQ1) {
+            const int f = e - R3_NQ0;
+            const int a = f / ((R3_TJ + 3) * R3_TK), r = f - a * ((R3_TJ + 3) * R3_TK), b = r / R3_TK, c = r - b * R3_TK;
+            const int d = (a * (R3_TJ + 4) + b) * R3_TK + c;
+            pair_q(D1[d], D1[d + R3_TK], Q1[f], Q1[R3_NQ1 + f], Q1[2 * R3_NQ1 + f]);
+        } else {
+            const int f = e - R3_NQ0 - R3_NQ1;
+            const int a = f / (R3_TJ * (R3_TK + 3)), r = f - a * (R3_TJ * (R3_TK + 3)), b = r / (R3_TK + 3),
+                      c = r - b * (R3_TK + 3);
+            const int d = (a * R3_TJ + b) * (R3_TK + 4) + c;
+            pair_q(D2[d], D2[d + 1], Q2[f], Q2[R3_NQ2 + f], Q2[2 * R3_NQ2 + f]);
+        }
+    }
+    __syncthreads();
+    // warps of axis ax; cell = (ti, tj, tk) of the tile
+    const int ax = tid / R3_NC, cell = tid - ax * R3_NC;
+    const int ti = cell / (R3_TJ * R3_TK), tr = cell - ti * (R3_TJ * R3_TK), tj = tr / R3_TK, tk = tr - tj * R3_TK;
+    const int I = I0 + ti, J = J0 + tj, K = K0 + tk;
+    const bool live = I < D.n[0] && J < D.n[1] && K < D.n[2];
+    const long long o = live ? D.at(I + GHC, J + GHC, K + GHC) : D.at(GHC, GHC, GHC);
+    const double sgn = sg[o];
+    // D2 at i-2 .. i+2 along ax, the pair terms X(i), X(i+1), Y(i-2), Y(i-1), B(i-1), B(i) and
+    // phi at i-2 .. i+2: element (m) of a run along ax starting at the cell's row -2 / pair -2
+    const double *Dl, *Ql;
+    int dstep, qstep, qn;
+    if (ax == 0) {
+        Dl = D0 + (ti * R3_TJ + tj) * R3_TK + tk, dstep = R3_TJ * R3_TK;
+        Ql = Q0 + (ti * R3_TJ + tj) * R3_TK + tk, qstep = R3_TJ * R3_TK, qn = R3_NQ0;
+    } else if (ax == 1) {
+        Dl = D1 + (ti * (R3_TJ + 4) + tj) * R3_TK + tk, dstep = R3_TK;
+        Ql = Q1 + (ti * (R3_TJ + 3) + tj) * R3_TK + tk, qstep = R3_TK, qn = R3_NQ1;
+    } else {
+        Dl = D2 + (ti * R3_TJ + tj) * (R3_TK + 4) + tk, dstep = 1;
+        Ql = Q2 + (ti * R3_TJ + tj) * (R3_TK + 3) + tk, qstep = 1, qn = R3_NQ2;
+    }
+    const int pstep = ax == 0 ? R3_PJ * R3_PK : (ax == 1 ? R3_PK : 1);
+    const double *Pc = P + pidx(ti + 3, tj + 3, tk + 3);
+    double d2[5];
+    for (int k = 0; k < 5; ++k) d2[k] = Dl[k * dstep];
+    const double qX0 = Ql[2 * qstep], qX1 = Ql[3 * qstep];                // X(i), X(i+1)
+    const double qY0 = Ql[qn], qY1 = Ql[qn + qstep];                      // Y(i-2), Y(i-1)
+    const double qB0 = Ql[2 * qn + qstep], qB1 = Ql[2 * qn + 2 * qstep];  // B(i-1), B(i)
+    const double m2 = Pc[-2 * pstep], m1 = Pc[-pstep], p1 = Pc[pstep], p2 = Pc[2 * pstep];
+    const double ih = D.rd[ax];
+    auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double d) {
+        const double p12 = q1 * q2, p01 = q0 * q1;
+        const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
+        return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
+    };
+    const double v = ih * (1.0 / 12.0) * fma(8.0, p1 - m1, m2 - p2);
+    const double Sp = fma(qY1, fma(6.0, qX1, qB1), 3.0 * qX1 * qB1);
+    const double Sm = fma(qX0, fma(6.0, qY0, qB0), 3.0 * qY0 * qB0);
+    const double r = rcp_refined(Sp * Sm);
+    const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
+    const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
+    const double dp = v + ih * wp, dm = v - ih * wm;
+    const double ga = sign_bits_positive(sgn) ? nonneg_max(pos_part(flip_sign(dp)), pos_part(dm))
+                                              : nonneg_max(pos_part(dp), pos_part(flip_sign(dm)));
+    GG[ax * R3_NC + cell] = ga * ga;
+    __syncthreads();
+    if (ax != 0 || !live) return;
+    const double g = sqrt(GG[cell] + GG[R3_NC + cell] + GG[2 * R3_NC + cell]);
+    const double de = De[o];
+    G[o] = g;
+    s[o] = -sgn * (g - 1.0) * fsrc;
+    A[o] = sgn * de * (g - 1.0);
+    B[o] = g * de * de;
+}
+
+inline dim3 reinit_a3d_grid(const Dims &D) {
+    return dim3(unsigned((D.n[2] + R3_TK - 1) / R3_TK), unsigned((D.n[1] + R3_TJ - 1) / R3_TJ),
+                unsigned((D.n[0] + R3_TI - 1) / R3_TI));
 }
 
 // lambda correction with the zero-order-extrapolated a, b (a ghost reads the nearest
@@ -900,6 +1032,7 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
         SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
     }
     SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    SCIHPC_CUDA(cudaFuncSetAttribute(k_reinit_a3d, cudaFuncAttributeMaxDynamicSharedMemorySize, int(R3_SMEM)));
     for (int a = 0; a < 3; ++a) {
         SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_sub[a], cudaEventDisableTiming));
         for (int k = 0; k < 2; ++k) {
@@ -1221,8 +1354,8 @@ void TwoPhaseGpu::reinit_stage(int stage) {
         launch_reinit_a2d(pdl, reinit_a2d_shape(D), D, stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D,
                           P.rdt, sc);
     else
-        launch_pdl(pdl, k_reinit_a, nbi, TPB, 0, stream, phi.data, sign, delta, grad, S[stage - 1], a_f, b_f, D, P.rdt,
-                   sc);
+        launch_pdl(pdl, k_reinit_a3d, reinit_a3d_grid(D), R3_NT, R3_SMEM, stream, phi.data, sign, delta, grad,
+                   S[stage - 1], a_f, b_f, D, P.rdt, sc);
     launch_pdl(pdl, k_reinit_b, nbi, TPB, 0, stream, phi.data, delta, grad, S[stage - 1], s1, s2, a_f, b_f, D, P.rdt,
                reinit_lambda, stage, sc, phi_fill);
     if (!phi_fill.on) scalar_bc(phi.data);
@@ -1741,19 +1874,19 @@ int TwoPhaseGpu::step(int nsteps, bool use_graph) {
 
 // Measurement hook: n back-to-back launches of the reinitialisation's gradient kernel (the
 // Godunov gradient, the redistance source and the lambda fields of stage 1: k_reinit_a2d in
-// 2D, k_reinit_a in 3D) between CUDA events on the session's stream.  The kernel reads phi,
+// 2D, k_reinit_a3d in 3D) between CUDA events on the session's stream.  The kernel reads phi,
 // sign and delta and rewrites the same outputs each time, so the launches are identical.
 int TwoPhaseGpu::time_reinit_gradient(int n, float *ms) {
     cudaEvent_t e0, e1;
     SCIHPC_CUDA(cudaEventCreate(&e0));
     SCIHPC_CUDA(cudaEventCreate(&e1));
-    const unsigned nbi = blocks_for(D.interior(), TPB);
     auto launch = [&]() {
         if (D.ndim == 2)
             launch_reinit_a2d(false, reinit_a2d_shape(D), D, stream, phi.data, sign, delta, grad, s1, a_f, b_f, D,
                               P.rdt, sc);
         else
-            k_reinit_a<<<nbi, TPB, 0, stream>>>(phi.data, sign, delta, grad, s1, a_f, b_f, D, P.rdt, sc);
+            k_reinit_a3d<<<reinit_a3d_grid(D), R3_NT, R3_SMEM, stream>>>(phi.data, sign, delta, grad, s1, a_f, b_f, D,
+                                                                         P.rdt, sc);
     };
     for (int k = 0; k < 3; ++k) launch();
     SCIHPC_CUDA(cudaEventRecord(e0, stream));
