@@ -1019,12 +1019,13 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
         if (a < D.ndim - 1)
             for (int c = 0; c < D.ndim; ++c) ALLOC(fv[a][c]);
     }
-    if (D.ndim == 2)
-        for (int a = 0; a < 2; ++a)
-            for (int k = 0; k < 2; ++k) {
-                ALLOC(tbs1[a][k]);
-                ALLOC(tbs2[a][k]);
-            }
+    for (int a = 0; a < D.ndim; ++a)
+        for (int k = 0; k < 2; ++k) {
+            ALLOC(tbs1[a][k]);
+            ALLOC(tbs2[a][k]);
+        }
+    if (D.ndim == 3)
+        for (int k = 0; k < 2; ++k) ALLOC(mtmp[k]);
 #undef ALLOC
     nfield_allocs = allocs.size();
     for (int k = 0; k < 3; ++k) {
@@ -1033,7 +1034,7 @@ int TwoPhaseGpu::create(const scihpc_grid *g, const int *vel_bc, const int *scal
     }
     SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     SCIHPC_CUDA(cudaFuncSetAttribute(k_reinit_a3d, cudaFuncAttributeMaxDynamicSharedMemorySize, int(R3_SMEM)));
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 4; ++a) {
         SCIHPC_CUDA(cudaEventCreateWithFlags(&ev_sub[a], cudaEventDisableTiming));
         for (int k = 0; k < 2; ++k) {
             SCIHPC_CUDA(cudaStreamCreateWithFlags(&sub[a][k], cudaStreamNonBlocking));
@@ -1090,7 +1091,7 @@ void TwoPhaseGpu::destroy() {
     }
     if (ev_fork) cudaEventDestroy(ev_fork);
     ev_fork = nullptr;
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < 4; ++a) {
         if (ev_sub[a]) cudaEventDestroy(ev_sub[a]);
         ev_sub[a] = nullptr;
         for (int k = 0; k < 2; ++k) {
@@ -1419,12 +1420,17 @@ void TwoPhaseGpu::find_source() {
                 launch_sec_mixed(D, 0, phi.d1[2], phi.mixed[2], s);
             }
         } else if (split_source()) {
-            // the y derivatives beside the x derivatives and their mixed derivative
-            sub_fork(2, 1, s);
+            // the derivatives along y (and z) and their mixed derivatives beside those along x
+            sub_fork(3, nd - 1, s);
             launch_ccd(D, ops, 0, phi.flux, phi.d1[0], phi.d2[0], s);
-            launch_ccd(D, ops, 1, phi.flux, phi.d1[1], phi.d2[1], sub[2][0]);
+            launch_ccd(D, ops, 1, phi.flux, phi.d1[1], phi.d2[1], sub[3][0]);
+            if (nd > 2) launch_ccd(D, ops, 2, phi.flux, phi.d1[2], phi.d2[2], sub[3][1]);
             launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
-            sub_join(2, 0, s);
+            if (nd > 2) {
+                launch_ccd_mixed(D, ops, 2, phi.d1[1], phi.mixed[1], mtmp[0], sub[3][0]);
+                launch_ccd_mixed(D, ops, 0, phi.d1[2], phi.mixed[2], mtmp[1], sub[3][1]);
+            }
+            for (int k = 0; k < nd - 1; ++k) sub_join(3, k, s);
         } else {
             for (int a = 0; a < nd; ++a) launch_ccd(D, ops, a, phi.flux, phi.d1[a], phi.d2[a], s);
             launch_ccd_mixed(D, ops, 1, phi.d1[0], phi.mixed[0], work, s);
