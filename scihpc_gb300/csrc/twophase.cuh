@@ -129,11 +129,11 @@ private:
     // per-direction face-averaged velocities of find_source for the directions other than the
     // last (that one uses nvel, as before), their extrapolation scratch and line-solve scratch
     double *fv[3][3] = {}, *fv_flux[3] = {}, *tb1[3] = {}, *tb2[3] = {};
-    // 2D: inside find_source's branches the line solves that do not depend on one another run
-    // as parallel branches of their own (sub[a][k], a = velocity direction, 3 = the level set);
-    // each concurrent UCCD solve has its own scratch (used only by the long-line fallback)
-    // (3D, measured: dam break 182.9 -> 187.7 steps/s with FP32 V-cycles, 150.7 -> 148.1 with
-    // FP64 ones, whose density setup on its own stream meets more concurrent work)
+    // Inside find_source's branches the line solves that do not depend on one another run as
+    // parallel branches of their own (sub[a][k], a = velocity direction, 3 = the level set);
+    // each concurrent UCCD solve has its own scratch (used only by the long-line fallback).
+    // Measured: bubble step 553 -> 559 steps/s; 3D dam break 182.9 -> 187.7 steps/s with FP32
+    // V-cycles, 150.7 -> 148.1 with FP64 ones.
     bool split_source() const { return source_scheme != 1; }
     cudaStream_t sub[4][2] = {};
     cudaEvent_t ev_sub[4] = {}, ev_subj[4][2] = {};
