@@ -1035,6 +1035,8 @@ def main():
                     help="only a few training steps of the 3D learned guess on a 128^3 grid (profiling case)")
     ap.add_argument("--profile-dambreak", action="store_true",
                     help="init and two steps of the 128x64x64 dam break, kernel by kernel (profiling case)")
+    ap.add_argument("--profile-reinit3d", action="store_true",
+                    help="the dam break's 3D reinitialisation gradient kernel, 53 launches (profiling case)")
     ap.add_argument("--profile-poisson", choices=["fp32", "fp64"],
                     help="only three iterations of the n^3 pressure solve (profiling case)")
     ap.add_argument("--poisson-n", type=int, default=256, help="grid of --profile-poisson")
@@ -1072,6 +1074,17 @@ def main():
         tp.init()
         tp.step(2, graph=False, sync=True)
         print(json.dumps({"profile": "dambreak 128x64x64, init + 2 steps", "scalars": tp.scalars()}))
+    elif args.profile_reinit3d:
+        import torch
+        from scihpc_gb300 import Grid, TwoPhase, lib
+        lib()
+        g, prm, phi = dambreak_setup(Grid)
+        tp = TwoPhase(g, ["slip"] * 6, ["neumann"] * 6, prm, scheme=0, n_mpls=0, reinit_every=20, fp32=True)
+        tp.set("phi", phi)
+        tp.init()
+        tp.step(3, graph=True, sync=True)
+        ms = tp.time_reinit_gradient(50)
+        print(json.dumps({"profile": "dambreak 128x64x64, reinitialisation gradient kernel", "launch_ms": ms}))
     elif args.profile_poisson:
         profile_poisson(args.profile_poisson, args.poisson_n)
     elif args.impl == "reference":
