@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "poisson.cuh"
@@ -728,6 +729,19 @@ __device__ void block_grid_sum(double v, double *red, RedSlot slot, double *out)
     }
 }
 
+// Steps q0 + R .. q0 + U - 1 (at most up to `last`) of a plane loop, each with its position
+// R in the group as a compile-time constant (std::integral_constant); true when a step failed.
+template <int R, int U, class F>
+__device__ __forceinline__ bool sweep_group(F &step, int q0, int last) {
+    if constexpr (R < U) {
+        if (q0 + R > last) return false;
+        if (step(q0 + R, std::integral_constant<int, R>{})) return true;
+        return sweep_group<R + 1, U>(step, q0, last);
+    } else {
+        return false;
+    }
+}
+
 // out-of-place sweep of level 0; ZERO: the old iterate is zero (not loaded).  PRO: the old
 // iterate is x + P e, with e the level-1 correction (piecewise-constant prolongation, ratio 2)
 // added on the fly from a staged coarse box: the prolongation pass and its write of x are
@@ -800,8 +814,6 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
                             &bar[st]);
     };
     auto wait_plane = [&](int q) { return tc::mbar_wait(&bar[q % NS], uint32_t((q / NS) & 1), TS_WAIT_LIMIT); };
-    // stage offsets of planes q - 1, q, q + 1, rotated once per step
-    int om1 = 0, oc0 = SST, op1 = 2 * SST;
     // coarse-box offsets of the parent of this pair's cells and of their j neighbours'
     // parents; a k neighbour's parent is the parent or the cell beside it, by the parity
     const int cpar = ((row + 1) >> 1) * TS_CW + pr + 4;
@@ -825,8 +837,15 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
     float c1h1 = 0, c1h2 = 0;
     float acc = 0.0f;   // DOT: this thread's part of <r, z> (FP32, as the inner vector kernels)
     bool fail = __syncthreads_or(!ok);
-    for (int q = 1; q <= nq - 2 && !fail; ++q) {
-        // planes q - 2 .. q + 1 are on chip
+    // One step per plane q (planes q - 2 .. q + 1 on chip).  Plane p lives in stage p % NS, so
+    // the loop runs in groups of U steps starting at q = 1 (mod U), U a multiple of NS and of 2:
+    // in the R-th step of a group every stage offset and the parity of the first-colour
+    // exchange buffers are compile-time constants.  Returns true when a plane never arrived.
+    constexpr int U = NS % 2 == 0 ? NS : 2 * NS;
+    auto step = [&](int q, auto R) -> bool {
+        constexpr int r = decltype(R)::value;
+        constexpr int om1 = (r % NS) * SST, oc0 = ((r + 1) % NS) * SST, op1 = ((r + 2) % NS) * SST;
+        constexpr int qa = (r + 1) & 1, qb = r & 1;   // parities of q and q - 1
         const int i = i0 - 2 + q;
         const int par = (i + j + c0) & 1;
         const int k = kbase + par;
@@ -856,11 +875,10 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
             xn[off] = fi;
             if (DOT) acc = fmaf(Xc[2 * TS_PLANE + o], fi, acc);
         }
-        first[q & 1][row][pr] = fi;
+        first[qa][row][pr] = fi;
         // second colour of plane i-1 from the first-colour values of planes i-2, i-1, i
         const int ib = i - 1;
         if (inner && kin && ib >= i0 && ib < i1) {
-            const int qb = (q - 1) & 1;
             const float nbm = first[qb][row][pr - 1], nbp = first[qb][row][pr + 1];
             const float n4 = par == 0 ? nbm : f1, n5 = par == 0 ? f1 : nbp;
             const float D0 = c1h2;
@@ -877,11 +895,9 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
         f1 = fi;
         c1h2 = c1h1;
         c1h1 = C1;
-        om1 = oc0, oc0 = op1;
-        op1 = op1 == (NS - 1) * SST ? 0 : op1 + SST;
         if (tid == 0 && q + 2 <= nq - 1)
             if ((ok = wait_plane(q + 2))) waited = q + 2;
-        if ((fail = __syncthreads_or(!ok))) break;
+        if (__syncthreads_or(!ok)) return true;
         // plane q - 2 is no longer needed: its stage takes plane q - 2 + NS
         if (q >= 2 && q - 2 + NS < nq) {
             issued = q - 2 + NS;
@@ -890,7 +906,9 @@ __global__ void __launch_bounds__(SW_THREADS, 2)
                 issue(q - 2 + NS);
             }
         }
-    }
+        return false;
+    };
+    for (int q0 = 1; q0 <= nq - 2 && !fail; q0 += U) fail = sweep_group<0, U>(step, q0, nq - 2);
     if (fail) {
         // a plane never arrived: report, and let the copies still in flight land (each wait
         // again bounded) before the block exits
