@@ -969,7 +969,6 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
         return tc::mbar_wait(&bar[q % TS_STAGES], uint32_t((q / TS_STAGES) & 1), TS_WAIT_LIMIT);
     };
     constexpr int SST = 3 * TS_PLANE;
-    int om1 = 0, oc0 = SST, op1 = 2 * SST;   // stage offsets of planes q - 1, q, q + 1
     const int issued_pre = min(TS_STAGES, nq) - 1;
     int issued = issued_pre, waited = -1;
     bool ok = true;
@@ -981,32 +980,53 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
     }
     const float c0 = id2.v[0], c1 = id2.v[1], c2 = id2.v[2];
     float acc = 0;
+    // The thread's two cells: a (taken first) and b; the upper half-warp takes them in the
+    // other order, so that every load of the half-warps is of words of opposite parity (no
+    // shared-memory bank conflict).  The face between a and b is formed once; each cell's
+    // (i, i+1) face is the next plane's (i-1, i) face (carried); both are the same sums as
+    // residual_at forms, so the residuals are unchanged.
+    const int hw = (tid >> 4) & 1;
+    const int oa = sc + hw, ob = sc + 1 - hw;   // box offsets of a and b
+    const int oA = hw ? sc + 2 : sc - 1, oB = hw ? sc - 1 : sc + 2;   // their other k neighbours
+    float za = 0.0f, zb = 0.0f;   // the (i, i+1) faces of a and b, carried to the next plane
     bool fail = __syncthreads_or(!ok);
-    for (int q = 1; q <= nq - 2 && !fail; ++q) {
-        // planes q - 1 .. q + 1 are on chip
+    // one step per plane q (planes q - 1 .. q + 1 on chip) in groups of TS_STAGES, as in
+    // k_sweep3_tma: stage offsets and the plane parity are compile-time constants
+    auto step = [&](int q, auto R) -> bool {
+        constexpr int r = decltype(R)::value;
+        constexpr int om1 = (r % TS_STAGES) * SST, oc0 = ((r + 1) % TS_STAGES) * SST,
+                      op1 = ((r + 2) % TS_STAGES) * SST;
+        constexpr bool odd = (r & 1) != 0;   // i = i0 - 1 + q with i0 even and q = 1 + r (mod 2)
         const float *Xc = tiles + oc0, *Xm = tiles + om1, *Xp = tiles + op1;
         const float *Rc = Xc + TS_PLANE, *Rm = Xm + TS_PLANE, *Rp = Xp + TS_PLANE, *Bc = Xc + 2 * TS_PLANE;
-        // the upper half-warp takes its two cells in the other order, so that at each step the
-        // half-warps read the odd and the even words (no shared-memory bank conflict)
-#pragma unroll
-        for (int dk = 0; dk < 2; ++dk) {
-            const int o = sc + (dk ^ ((tid >> 4) & 1));
-            const float rc = Rc[o], xc = Xc[o];
-            const float C0 = pdiv(2.0f, rc + Rm[o]) * c0, C1 = pdiv(2.0f, rc + Rp[o]) * c0;
-            const float C2 = pdiv(2.0f, rc + Rc[o - TS_W]) * c1, C3 = pdiv(2.0f, rc + Rc[o + TS_W]) * c1;
-            const float C4 = pdiv(2.0f, rc + Rc[o - 1]) * c2, C5 = pdiv(2.0f, rc + Rc[o + 1]) * c2;
-            float sres = C0 * (xc - Xm[o]) + C1 * (xc - Xp[o]) + C2 * (xc - Xc[o - TS_W]) + C3 * (xc - Xc[o + TS_W]);
-            sres += C4 * (xc - Xc[o - 1]) + C5 * (xc - Xc[o + 1]);
-            acc += Bc[o] - sres;
+        const float ra = Rc[oa], rb = Rc[ob], xa = Xc[oa], xb = Xc[ob];
+        float C0a = za, C0b = zb;
+        if (q == 1) {
+            C0a = pdiv(2.0f, ra + Rm[oa]) * c0;
+            C0b = pdiv(2.0f, rb + Rm[ob]) * c0;
         }
-        const int i = i0 - 1 + q;
-        if ((i & 1) && (jj & 1)) part[jj >> 1][kc] = acc;
-        om1 = oc0, oc0 = op1;
-        op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
+        const float C1a = pdiv(2.0f, ra + Rp[oa]) * c0, C1b = pdiv(2.0f, rb + Rp[ob]) * c0;
+        const float C2a = pdiv(2.0f, ra + Rc[oa - TS_W]) * c1, C3a = pdiv(2.0f, ra + Rc[oa + TS_W]) * c1;
+        const float C2b = pdiv(2.0f, rb + Rc[ob - TS_W]) * c1, C3b = pdiv(2.0f, rb + Rc[ob + TS_W]) * c1;
+        const float Cs = pdiv(2.0f, ra + rb) * c2;   // the face between a and b
+        const float Coa = pdiv(2.0f, ra + Rc[oA]) * c2, Cob = pdiv(2.0f, rb + Rc[oB]) * c2;
+        const float xA = Xc[oA], xB = Xc[oB];
+        // k - 1 and k + 1 faces and neighbours of a and b (a is the lower cell when hw == 0)
+        const float C4a = hw ? Cs : Coa, C5a = hw ? Coa : Cs, X4a = hw ? xb : xA, X5a = hw ? xA : xb;
+        const float C4b = hw ? Cob : Cs, C5b = hw ? Cs : Cob, X4b = hw ? xB : xa, X5b = hw ? xa : xB;
+        float sa = C0a * (xa - Xm[oa]) + C1a * (xa - Xp[oa]) + C2a * (xa - Xc[oa - TS_W]) + C3a * (xa - Xc[oa + TS_W]);
+        sa += C4a * (xa - X4a) + C5a * (xa - X5a);
+        acc += Bc[oa] - sa;
+        float sb = C0b * (xb - Xm[ob]) + C1b * (xb - Xp[ob]) + C2b * (xb - Xc[ob - TS_W]) + C3b * (xb - Xc[ob + TS_W]);
+        sb += C4b * (xb - X4b) + C5b * (xb - X5b);
+        acc += Bc[ob] - sb;
+        za = C1a, zb = C1b;
+        if (odd && (jj & 1)) part[jj >> 1][kc] = acc;
         if (tid == 0 && q + 2 <= nq - 1)
             if ((ok = wait_plane(q + 2))) waited = q + 2;
-        if ((fail = __syncthreads_or(!ok))) break;
-        if (i & 1) {
+        if (__syncthreads_or(!ok)) return true;
+        if (odd) {
+            const int i = i0 - 1 + q;
             if (!(jj & 1) && live) {
                 const long long Pc =
                     (long long)((i >> 1) + 1) * Cl.s[0] + (long long)((j >> 1) + 1) * Cl.s[1] + (k >> 1) + 1;
@@ -1023,7 +1043,10 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
                 issue(q + TS_STAGES - 1);
             }
         }
-    }
+        return false;
+    };
+    static_assert(TS_STAGES % 2 == 0, "plane parity of a restriction step");
+    for (int q0 = 1; q0 <= nq - 2 && !fail; q0 += TS_STAGES) fail = sweep_group<0, TS_STAGES>(step, q0, nq - 2);
     if (fail) {
         if (tid == 0) {
             atomicExch(err, 1);
