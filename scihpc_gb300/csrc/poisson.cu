@@ -1225,7 +1225,6 @@ __global__ void __launch_bounds__(AP_THREADS)
         return tc::mbar_wait(&bar[qq % TS_STAGES], uint32_t((qq / TS_STAGES) & 1), TS_WAIT_LIMIT);
     };
     constexpr int SST = 3 * TS_PLANE;
-    int om1 = 0, oc0 = SST, op1 = 2 * SST;   // stage offsets of planes qq - 1, qq, qq + 1
     const int issued_pre = min(TS_STAGES, nq) - 1;
     int issued = issued_pre, waited = -1;
     bool ok = true;
@@ -1238,38 +1237,83 @@ __global__ void __launch_bounds__(AP_THREADS)
     const float w0 = 2.0f * id2.v[0], w1 = 2.0f * id2.v[1], w2 = 2.0f * id2.v[2];
     const int s0 = int(L.s[0]), s1 = int(L.s[1]);
     float acc = 0.0f;
+    // Cell c = 2 dj + e of the thread's 2 x 2 group: row dj, e = 0 the column taken first (a),
+    // e = 1 the other (b); the upper half-warp takes the columns in the other order, so that the
+    // half-warps read words of opposite parity (no shared-memory bank conflict).  Each face
+    // coefficient and each neighbour's direction value is formed once per plane: the faces and
+    // values inside the group are shared by its cells, and the values and (i, i+1) faces of a
+    // plane are carried to the next one; every one is the same expression as in
+    // k_in_apply<DIM, 1, true>, so q is unchanged.
+    const int hw = (tid >> 4) & 1;
+    int oc[4], okk[4];   // box offsets of the cells and of their k neighbour outside the group
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int dj = c >> 1, e = c & 1;
+        oc[c] = sc + dj * TS_W + (e ? 1 - hw : hw);
+        okk[c] = sc + dj * TS_W + (e == 0 ? (hw ? 2 : -1) : (hw ? -1 : 2));
+    }
+    float dmv[4] = {0, 0, 0, 0}, dcv[4] = {0, 0, 0, 0}, zf[4] = {0, 0, 0, 0};   // carried per cell
     bool fail = __syncthreads_or(!ok);
-    for (int qq = 1; qq <= nq - 2 && !fail; ++qq) {
+    auto step = [&](int qq, auto R) -> bool {
+        constexpr int r = decltype(R)::value;
+        constexpr int om1 = (r % TS_STAGES) * SST, oc0 = ((r + 1) % TS_STAGES) * SST,
+                      op1 = ((r + 2) % TS_STAGES) * SST;
         const float *Zc = tiles + oc0, *Zm = tiles + om1, *Zp = tiles + op1;
         const float *Rc = Zc + TS_PLANE, *Rm = Zm + TS_PLANE, *Rp = Zp + TS_PLANE;
         const float *Dc = Zc + 2 * TS_PLANE, *Dm = Zm + 2 * TS_PLANE, *Dp = Zp + 2 * TS_PLANE;
         const int i = i0 - 1 + qq;
-        // the upper half-warp takes the two columns in the other order (no shared-memory bank
-        // conflict between the half-warps, as in k_restrict3_tma)
+        float rcv[4], dpv[4];
 #pragma unroll
-        for (int dj = 0; dj < 2; ++dj)
+        for (int c = 0; c < 4; ++c) rcv[c] = Rc[oc[c]];
+        if (qq == 1) {
 #pragma unroll
-            for (int dx = 0; dx < 2; ++dx) {
-                const int dk = dx ^ ((tid >> 4) & 1);
-                const int o = sc + dj * TS_W + dk;
-                const float dc = Zc[o] + beta * Dc[o];
-                const float rc = Rc[o];
-                float sq = w0 * prcp(rc + Rm[o]) * (dc - (Zm[o] + beta * Dm[o])) +
-                           w0 * prcp(rc + Rp[o]) * (dc - (Zp[o] + beta * Dp[o])) +
-                           w1 * prcp(rc + Rc[o - TS_W]) * (dc - (Zc[o - TS_W] + beta * Dc[o - TS_W])) +
-                           w1 * prcp(rc + Rc[o + TS_W]) * (dc - (Zc[o + TS_W] + beta * Dc[o + TS_W]));
-                sq += w2 * prcp(rc + Rc[o - 1]) * (dc - (Zc[o - 1] + beta * Dc[o - 1])) +
-                      w2 * prcp(rc + Rc[o + 1]) * (dc - (Zc[o + 1] + beta * Dc[o + 1]));
-                if (j + dj < L.n[1] && k + dk < L.n[2]) {
-                    q[(i + 1) * s0 + (j + dj + 1) * s1 + k + dk + 1] = sq;
-                    acc += dc * sq;
-                }
+            for (int c = 0; c < 4; ++c) {
+                dcv[c] = Zc[oc[c]] + beta * Dc[oc[c]];
+                dmv[c] = Zm[oc[c]] + beta * Dm[oc[c]];
+                zf[c] = w0 * prcp(rcv[c] + Rm[oc[c]]);
             }
-        om1 = oc0, oc0 = op1;
-        op1 = op1 == (TS_STAGES - 1) * SST ? 0 : op1 + SST;
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) dpv[c] = Zp[oc[c]] + beta * Dp[oc[c]];
+        // faces inside the group: between the rows (columns a, b), between the columns (rows 0, 1)
+        const float Fj[2] = {w1 * prcp(rcv[0] + rcv[2]), w1 * prcp(rcv[1] + rcv[3])};
+        const float Fk[2] = {w2 * prcp(rcv[0] + rcv[1]), w2 * prcp(rcv[2] + rcv[3])};
+        float zn[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int dj = c >> 1, e = c & 1;
+            const int o = oc[c];
+            const float rc = rcv[c], dc = dcv[c];
+            const float Fz1 = w0 * prcp(rc + Rp[o]);
+            // j: the row outside the group (j - 1 for row 0, j + 1 for row 1) and the other row
+            const int oj = dj ? o + TS_W : o - TS_W;
+            const float Fjo = w1 * prcp(rc + Rc[oj]), djo = Zc[oj] + beta * Dc[oj];
+            const float F2 = dj ? Fj[e] : Fjo, F3 = dj ? Fjo : Fj[e];
+            const float d2 = dj ? dcv[c ^ 2] : djo, d3 = dj ? djo : dcv[c ^ 2];
+            // k: the column outside the group and the other column; the outside one is at k - 1
+            // for the lower column (a when hw == 0)
+            const float Fko = w2 * prcp(rc + Rc[okk[c]]), dko = Zc[okk[c]] + beta * Dc[okk[c]];
+            const bool low = e == 0 ? !hw : hw;
+            const float F4 = low ? Fko : Fk[dj], F5 = low ? Fk[dj] : Fko;
+            const float d4 = low ? dko : dcv[c ^ 1], d5 = low ? dcv[c ^ 1] : dko;
+            float sq = zf[c] * (dc - dmv[c]) + Fz1 * (dc - dpv[c]) + F2 * (dc - d2) + F3 * (dc - d3);
+            sq += F4 * (dc - d4) + F5 * (dc - d5);
+            const int dk = e ? 1 - hw : hw;
+            if (j + dj < L.n[1] && k + dk < L.n[2]) {
+                q[(i + 1) * s0 + (j + dj + 1) * s1 + k + dk + 1] = sq;
+                acc += dc * sq;
+            }
+            zn[c] = Fz1;
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            dmv[c] = dcv[c];
+            dcv[c] = dpv[c];
+            zf[c] = zn[c];
+        }
         if (tid == 0 && qq + 2 <= nq - 1)
             if ((ok = wait_plane(qq + 2))) waited = qq + 2;
-        if ((fail = __syncthreads_or(!ok))) break;
+        if (__syncthreads_or(!ok)) return true;
         if (qq + TS_STAGES - 1 < nq) {
             issued = qq + TS_STAGES - 1;
             if (tid == 0) {
@@ -1277,7 +1321,9 @@ __global__ void __launch_bounds__(AP_THREADS)
                 issue(qq + TS_STAGES - 1);
             }
         }
-    }
+        return false;
+    };
+    for (int q0 = 1; q0 <= nq - 2 && !fail; q0 += TS_STAGES) fail = sweep_group<0, TS_STAGES>(step, q0, nq - 2);
     if (fail) {
         if (tid == 0) {
             atomicExch(err, 1);
