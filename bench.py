@@ -537,12 +537,11 @@ def stock_block(torch, args, flush, clocks_cls) -> dict:
     torch.cuda.synchronize()
     it1 = tp.graph_stats()["ppe_iters_total"]
     t0 = time.perf_counter()
+    ptrs = [hb[nm].data_ptr() for nm in names]
     for _ in range(n_e2e):
-        for nm in names:
-            tp.upload_ptr(nm, hb[nm].data_ptr())
-        tp.step(1, graph=True, sync=True)
-        for nm in names:
-            tp.download_ptr(nm, hb[nm].data_ptr())
+        tp.upload_many_ptr(names, ptrs)
+        tp.step(1, graph=True, sync=False)
+        tp.download_many_ptr(names, ptrs)
     e2e = n_e2e / (time.perf_counter() - t0)
     it_e2e = (tp.graph_stats()["ppe_iters_total"] - it1) / n_e2e
     diag = tp.diagnostics()
@@ -616,16 +615,16 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     barrier(ws)
     t0 = time.perf_counter()
+    ptrs = [hb[nm].data_ptr() for nm in names]
     for _ in range(e2e_steps):
-        for nm in names:
-            tp.upload_ptr(nm, hb[nm].data_ptr())
-        tp.step(1, graph=True, sync=True)
-        for nm in names:
-            tp.download_ptr(nm, hb[nm].data_ptr())
+        tp.upload_many_ptr(names, ptrs)
+        tp.step(1, graph=True, sync=False)
+        tp.download_many_ptr(names, ptrs)   # on the step's stream: returns once the fields are on the host
     e2e_s = max_over_ranks(ws, time.perf_counter() - t0, torch.device("cuda"))
     e2e = {"value": ws * e2e_steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes, "steps": e2e_steps,
-           "api": "scihpc_twophase_upload x4 + scihpc_twophase_step + scihpc_twophase_download x4"}
+           "api": "scihpc_twophase_upload_many (4 fields) + scihpc_twophase_step + "
+                  "scihpc_twophase_download_many (4 fields)"}
 
     # roofline of the step's dominant kernel: the reinitialisation's gradient kernel
     # (k_reinit_a2d, the largest share of the step's launch list), FP64-bound on

@@ -219,6 +219,11 @@ int scihpc_twophase_destroy(scihpc_twophase *tp);
  * rhs_fpc (init_ppe_fpc_coefficients' right-hand-side term). */
 int scihpc_twophase_upload(scihpc_twophase *tp, const char *name, const double *host);
 int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host);
+/* The same for n fields at once: one asynchronous copy per field on the session's stream and a
+ * single synchronisation before returning (the host buffers may be reused on return), instead
+ * of one round trip per field.  Every name is checked before any copy starts. */
+int scihpc_twophase_upload_many(scihpc_twophase *tp, int n, const char *const *names, const double *const *host);
+int scihpc_twophase_download_many(scihpc_twophase *tp, int n, const char *const *names, double *const *host);
 /* Device pointer of a named field (for zero-copy use by callers). */
 int scihpc_twophase_field(scihpc_twophase *tp, const char *name, double **dev);
 /* Scalars {t, dt, dt_old, dt_old2, iter, stable_CFL, lsf_mass0}. */

@@ -423,6 +423,32 @@ int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host
     return SCIHPC_OK;
 }
 
+int scihpc_twophase_upload_many(scihpc_twophase *tp, int n, const char *const *names, const double *const *host) {
+    REQUIRE(tp && n >= 0 && (n == 0 || (names && host)), "twophase_upload_many: bad argument");
+    for (int f = 0; f < n; ++f) {
+        REQUIRE(names[f] && host[f], "twophase_upload_many: NULL name or buffer");
+        REQUIRE(tp->tp.field(names[f]), "twophase_upload_many: unknown field name");
+    }
+    const size_t bytes = size_t(tp->tp.D.size()) * sizeof(double);
+    for (int f = 0; f < n; ++f)
+        SCIHPC_CUDA(cudaMemcpyAsync(tp->tp.field(names[f]), host[f], bytes, cudaMemcpyHostToDevice, tp->tp.stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(tp->tp.stream));
+    return SCIHPC_OK;
+}
+
+int scihpc_twophase_download_many(scihpc_twophase *tp, int n, const char *const *names, double *const *host) {
+    REQUIRE(tp && n >= 0 && (n == 0 || (names && host)), "twophase_download_many: bad argument");
+    for (int f = 0; f < n; ++f) {
+        REQUIRE(names[f] && host[f], "twophase_download_many: NULL name or buffer");
+        REQUIRE(tp->tp.field(names[f]), "twophase_download_many: unknown field name");
+    }
+    const size_t bytes = size_t(tp->tp.D.size()) * sizeof(double);
+    for (int f = 0; f < n; ++f)
+        SCIHPC_CUDA(cudaMemcpyAsync(host[f], tp->tp.field(names[f]), bytes, cudaMemcpyDeviceToHost, tp->tp.stream));
+    SCIHPC_CUDA(cudaStreamSynchronize(tp->tp.stream));
+    return SCIHPC_OK;
+}
+
 int scihpc_twophase_field(scihpc_twophase *tp, const char *name, double **dev) {
     REQUIRE(tp && name && dev, "twophase_field: NULL argument");
     double *d = tp->tp.field(name);

@@ -108,6 +108,10 @@ _SIGS = {
     "scihpc_twophase_destroy": ([_vp], ctypes.c_int),
     "scihpc_twophase_upload": ([_vp, ctypes.c_char_p, _dp], ctypes.c_int),
     "scihpc_twophase_download": ([_vp, ctypes.c_char_p, _dp], ctypes.c_int),
+    "scihpc_twophase_upload_many": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_dp)],
+                                    ctypes.c_int),
+    "scihpc_twophase_download_many": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_dp)],
+                                      ctypes.c_int),
     "scihpc_twophase_field": ([_vp, ctypes.c_char_p, ctypes.POINTER(_vp)], ctypes.c_int),
     "scihpc_twophase_checkpoint": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "scihpc_twophase_restore": ([_vp, ctypes.c_char_p], ctypes.c_int),
@@ -478,6 +482,24 @@ class TwoPhase:
 
     def download_ptr(self, name: str, host_ptr: int) -> None:
         self.L.check(self.L.scihpc_twophase_download(self.h, name.encode(), ctypes.cast(host_ptr, _dp)))
+
+    @staticmethod
+    def _many(names, host_ptrs):
+        n = len(names)
+        assert len(host_ptrs) == n
+        nm = (ctypes.c_char_p * n)(*[x.encode() for x in names])
+        hp = (_dp * n)(*[ctypes.cast(p, _dp) for p in host_ptrs])
+        return n, nm, hp
+
+    def upload_many_ptr(self, names, host_ptrs) -> None:
+        """Several fields from host memory in one call (one synchronisation)."""
+        n, nm, hp = self._many(names, host_ptrs)
+        self.L.check(self.L.scihpc_twophase_upload_many(self.h, n, nm, hp))
+
+    def download_many_ptr(self, names, host_ptrs) -> None:
+        """Several fields to host memory in one call (one synchronisation)."""
+        n, nm, hp = self._many(names, host_ptrs)
+        self.L.check(self.L.scihpc_twophase_download_many(self.h, n, nm, hp))
 
     def time_reinit_gradient(self, n: int = 100) -> float:
         """ms per launch of the reinitialisation's gradient kernel (measurement hook)."""

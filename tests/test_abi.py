@@ -62,6 +62,13 @@ def test_host_argument_checks(lib):
     out = (ctypes.c_double * 2)()
     assert lib.scihpc_lsf_integrals_noalloc(ctypes.byref(big), p4, ctypes.c_void_p(8), out, None) == 1
     assert b"static scratch" in lib.scihpc_last_error()
+    # the batched field copies check their arguments before any copy
+    names = (ctypes.c_char_p * 1)(b"phi")
+    bufs = (ctypes.POINTER(ctypes.c_double) * 1)()
+    assert lib.scihpc_twophase_upload_many(None, 1, names, bufs) == 1
+    assert b"upload_many" in lib.scihpc_last_error()
+    assert lib.scihpc_twophase_download_many(None, -1, names, bufs) == 1
+    assert b"download_many" in lib.scihpc_last_error()
 
 
 def test_build_recipe_targets_sm103a():

@@ -285,3 +285,26 @@ def test_fast_pressure_correction_stages():
     port.call("fast_pressure_correction")
     it, rr = gpu.fast_pressure_correction()
     compare(G, port, gpu, ["p", "u", "v"], FLOW_TOL)
+
+
+def test_batched_field_copies():
+    """scihpc_twophase_upload_many / download_many move several fields with one synchronisation
+    and give the same fields as one upload / download per field; an unknown name is refused
+    before any copy."""
+    port, gpu = make_pair(G)
+    names = ["phi", "u", "v", "p"]
+    rng = np.random.default_rng(31)
+    src = {nm: np.ascontiguousarray(rng.standard_normal(G.shape)) for nm in names}
+    ptrs = [src[nm].ctypes.data for nm in names]
+    gpu.upload_many_ptr(names, ptrs)
+    for nm in names:
+        assert np.array_equal(gpu.get(nm), src[nm]), nm
+    out = {nm: np.zeros(G.shape) for nm in names}
+    gpu.download_many_ptr(names, [out[nm].ctypes.data for nm in names])
+    for nm in names:
+        assert np.array_equal(out[nm], src[nm]), nm
+    keep = gpu.get("phi")
+    with pytest.raises(Exception):
+        gpu.upload_many_ptr(["phi", "nope"], [src["u"].ctypes.data, src["v"].ctypes.data])
+    assert np.array_equal(gpu.get("phi"), keep)   # nothing was copied
+    gpu.close()
