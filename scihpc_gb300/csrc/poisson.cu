@@ -44,7 +44,8 @@ constexpr double CG_ALPHA_MAX = 20.0;
 // Levels of at most this many cells run together in one thread block (k_coarse_cycle).  One
 // SM executes about 4 FP64 flops per clock on GB300, so FP64 cycles hand over to the single
 // block much later than FP32 ones.  (FP32: measured 4096 -> 1024 cells: 128 x 256 two-phase
-// step 420 -> 424 steps/s, 256^3 V-cycle 0.566 -> 0.562 ms; 512 is no better.)
+// step 420 -> 424 steps/s, 256^3 V-cycle 0.566 -> 0.562 ms; 512 is no better; 2048, which takes
+// the bubble's 32 x 64 level into the block too, measured 555 against 559 steps/s.)
 constexpr long long COARSE_CELLS_FP32 = 1024;
 constexpr long long COARSE_CELLS_FP64 = 128;
 // dynamic shared memory the coarse kernel may take for its levels (plus ~10 KB static)
