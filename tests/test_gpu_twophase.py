@@ -308,3 +308,40 @@ def test_batched_field_copies():
         gpu.upload_many_ptr(["phi", "nope"], [src["u"].ctypes.data, src["v"].ctypes.data])
     assert np.array_equal(gpu.get("phi"), keep)   # nothing was copied
     gpu.close()
+
+
+@pytest.mark.parametrize("n", [(162, 171), (18, 10, 12)], ids=["2d_16x14_partial", "3d_4x8x8_partial"])
+def test_reinit_partial_tiles(n):
+    """Reinitialisation (its steps x 3 stages of the Godunov gradient kernel and the lambda
+    correction) on grids where the kernel's tiles are partial along every axis: 162 x 171 takes
+    the 16 x 14 shape (the cost rule prefers it there; the sizes still coarsen to a pressure
+    grid of 18 x 19), 18 x 10 x 12 the 4 x 8 x 8 3D tiles.  A level set that is not a distance
+    function, so that reinitialisation moves it."""
+    from scihpc_gb300 import TwoPhase
+    g = O.Grid(len(n), n, (0.0,) * len(n), tuple(x / n[0] for x in n))   # square cells
+    prm = bubble_params(g, ppe_tol=1e-12)
+    opt = dict(scheme=1, n_mpls=0, reinit_every=1, ppe_mode=2, reinit_lambda=1)
+    port = O.Checker("port").twophase(g, ["no_slip"] * 6, ["neumann"] * 6, prm, opt)
+    gpu = TwoPhase(native(g), ["no_slip"] * 6, ["neumann"] * 6, prm, scheme=1, n_mpls=0, reinit_every=1,
+                   reinit_lambda=True)
+    c = g.spacing()
+    xs = [g.lo[a] + (np.arange(g.n[a]) + 0.5) * c[a] for a in range(g.ndim)]
+    M = np.meshgrid(*xs, indexing="ij")
+    r = np.sqrt(sum((M[a] - 0.45) ** 2 for a in range(g.ndim)))
+    core = (0.3 - r) * (1.0 + 0.5 * np.sin(3.0 * M[0]))
+    phi = np.zeros(g.shape)
+    if g.ndim == 2:
+        phi[3:-3, 3:-3, 0] = core
+    else:
+        phi[3:-3, 3:-3, 3:-3] = core
+    port.set("phi", phi)
+    gpu.set("phi", phi)
+    port.call("init")
+    gpu.init()
+    n1 = port.call("reinit")
+    n2 = gpu.reinit()
+    assert n1 == n2 and n1 > 0
+    moved = rel_l2(gpu.get("phi")[g.interior()], phi[g.interior()])
+    assert moved > 1e-3, moved   # the reinitialisation changed the level set
+    compare(g, port, gpu, ["phi"], LS_TOL)
+    gpu.close()
