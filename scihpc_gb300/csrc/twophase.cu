@@ -238,9 +238,17 @@ __global__ void __launch_bounds__(2 * RA_TI * RA_TJ)
     k_reinit_a2d(const double *__restrict__ phi, const double *__restrict__ sg, const double *__restrict__ De,
                  double *__restrict__ G, double *__restrict__ s, double *__restrict__ A, double *__restrict__ B, Dims D,
                  double rdt, const StepScalars *sc) {
+    constexpr int RA_NT = 2 * RA_TI * RA_TJ;
+    // this thread's cell, and the smoothed delta field, which no kernel of the
+    // reinitialisation chain writes: loaded before waiting for the previous kernel
+    const int ax = threadIdx.x & 1, cell = threadIdx.x >> 1;
+    const int ti = cell / RA_TJ, tj = cell - ti * RA_TJ;
+    const int I = blockIdx.y * RA_TI + ti, J = blockIdx.x * RA_TJ + tj;
+    const bool live = I < D.n[0] && J < D.n[1];
+    const long long o = live ? D.at(I + GHC, J + GHC, 0) : D.at(GHC, GHC, 0);
+    const double de = De[o];
     pdl_wait();
     pdl_trigger();
-    constexpr int RA_NT = 2 * RA_TI * RA_TJ;
     constexpr int PI = RA_TI + 6, PJ = RA_TJ + 6;   // phi with three ghost layers
     constexpr int DI = RA_TI + 4, DJ = RA_TJ + 4;   // second differences at -2 .. T+1
     constexpr int QI = RA_TI + 3, QJ = RA_TJ + 3;   // pairs at -2 .. T
@@ -288,11 +296,6 @@ __global__ void __launch_bounds__(2 * RA_TI * RA_TJ)
     }
     __syncthreads();
     // thread pair (2c, 2c + 1) owns cell c; the even thread takes axis 0, the odd one axis 1
-    const int ax = tid & 1, cell = tid >> 1;
-    const int ti = cell / RA_TJ, tj = cell - ti * RA_TJ;
-    const int I = I0 + ti, J = J0 + tj;
-    const bool live = I < D.n[0] && J < D.n[1];
-    const long long o = live ? D.at(I + GHC, J + GHC, 0) : D.at(GHC, GHC, 0);
     const double sgn = sg[o];
     // weights of one correction from its three squared indicator terms and D2 values a..d
     auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double d) {
@@ -333,7 +336,6 @@ __global__ void __launch_bounds__(2 * RA_TI * RA_TJ)
     const double g2 = gg + __shfl_xor_sync(0xffffffffu, gg, 1);   // the same sum in both threads
     if (!live) return;
     const double g = sqrt(g2);
-    const double de = De[o];
     if (ax == 0) {
         G[o] = g;
         s[o] = -sgn * (g - 1.0) * fsrc;
@@ -530,17 +532,21 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
                            double *__restrict__ sk, const double *__restrict__ s1, const double *__restrict__ s2,
                            const double *__restrict__ A, const double *__restrict__ B, Dims D, double rdt,
                            int lambda, int stage, const StepScalars *sc, GhostFill GF) {
+    // the cell, the time step and the smoothed delta field (none written by a kernel of the
+    // reinitialisation chain): read before waiting for the previous kernel
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = q < D.interior();
+    int I = 0, J = 0, K = 0;
+    if (in) split3(q, D, I, J, K);
+    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
+    const double dt = sc->dt;
+    const double de = in ? De[o] : 0.0;
     pdl_wait();
     pdl_trigger();
     __shared__ double fsrc;   // rdt / dt, one division per block
-    if (threadIdx.x == 0) fsrc = rdt / sc->dt;
+    if (threadIdx.x == 0) fsrc = rdt / dt;
     __syncthreads();
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= D.interior()) return;
-    int I, J, K;
-    split3(q, D, I, J, K);
-    const long long o = D.at(D.ix(0, I), D.ix(1, J), D.ix(2, K));
-    const double dt = sc->dt;
+    if (!in) return;
     double s = sk[o];
     if (lambda) {
         auto cl = [&](int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); };
@@ -568,7 +574,7 @@ __global__ void k_reinit_b(double *__restrict__ phi, const double *__restrict__ 
         }
         // a / b by the refined hardware reciprocal (b > 1e-8 here): the division is the longest
         // dependency chain of this short kernel
-        if (fabs(b) > 1e-8) s += a * rcp_refined(b) * De[o] * G[o] * fsrc;
+        if (fabs(b) > 1e-8) s += a * rcp_refined(b) * de * G[o] * fsrc;
         sk[o] = s;
     }
     double f = phi[o];
