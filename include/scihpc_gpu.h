@@ -147,8 +147,7 @@ int scihpc_lsf_integrals(scihpc_ctx *ctx, const double prm[4], const double *phi
  * of 1048576 ghosted cells (8 MiB, held by every GPU that loads the library until exit);
  * larger grids are rejected with SCIHPC_ERR_ARG.  All calls share that array: calls that
  * overlap on the GPU race and must be serialised by the caller.  The first call on each
- * device resolves the array's device address; make it before any stream capture.
- * Synchronises `stream`.  This entry point has no counterpart in the reference. */
+ * device resolves the array's device address.  Synchronises `stream`.  This entry point has no counterpart in the reference. */
 int scihpc_lsf_integrals_noalloc(const scihpc_grid *grid, const double prm[4], const double *phi, double out[2],
                                  void *stream);
 

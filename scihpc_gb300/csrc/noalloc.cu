@@ -17,8 +17,7 @@
 //     every scratch entry it reads before reading it, so leftovers of a previous call do
 //     not matter.
 //   - The first call on each device resolves the array's device address with
-//     cudaGetSymbolAddress (a host-side symbol is only a stand-in, never a device address);
-//     make that first call before any stream capture.
+//     cudaGetSymbolAddress (a host-side symbol is only a stand-in, never a device address).
 #include <mutex>
 
 #include "common.cuh"
