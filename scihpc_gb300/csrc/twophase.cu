@@ -298,10 +298,13 @@ __global__ void __launch_bounds__(2 * RA_TI * RA_TJ)
     // thread pair (2c, 2c + 1) owns cell c; the even thread takes axis 0, the odd one axis 1
     const double sgn = sg[o];
     // weights of one correction from its three squared indicator terms and D2 values a..d
-    auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double d) {
+    // one WENO-JS correction w0 / 3 (a - 2b + c) + (w2 - 1/2) / 6 t with w0 = q1 q2 inv and
+    // w2 = 3 q0 q1 inv, the constants folded into the weights: (q1 q2) (inv / 3) and
+    // (q0 q1) (inv / 2) - 1/12; t = b - 2c + d is the same for both corrections of a cell
+    auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double t) {
         const double p12 = q1 * q2, p01 = q0 * q1;
-        const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
-        return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
+        const double c0 = p12 * (inv * (1.0 / 3.0)), c2 = fma(p01, inv * 0.5, -1.0 / 12.0);
+        return fma(c0, fma(-2.0, b, a) + c, c2 * t);
     };
     // D2 at i-2 .. i+2 and the pair terms of this cell along axis ax (index i = cell)
     double d2[5];
@@ -325,8 +328,9 @@ __global__ void __launch_bounds__(2 * RA_TI * RA_TJ)
     const double Sp = fma(qY1, fma(6.0, qX1, qB1), 3.0 * qX1 * qB1);   // qB1 qY1 + 6 qX1 qY1 + 3 qX1 qB1
     const double Sm = fma(qX0, fma(6.0, qY0, qB0), 3.0 * qY0 * qB0);   // qB0 qX0 + 6 qY0 qX0 + 3 qY0 qB0
     const double r = rcp_refined(Sp * Sm);
-    const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
-    const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
+    const double t3 = fma(-2.0, d2[2], d2[1] + d2[3]);
+    const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], t3);
+    const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], t3);
     const double dp = v + ih * wp, dm = v - ih * wm;
     // Godunov's upwind choice, max(-min(dp, 0), max(dm, 0)) for sgn > 0 and max(max(dp, 0),
     // -min(dm, 0)) otherwise, on the integer pipe (nonneg_max, pos_part: lsm_device.cuh)
@@ -495,17 +499,21 @@ __global__ void __launch_bounds__(R3_NT, 2)
     const double qB0 = Ql[2 * qn + qstep], qB1 = Ql[2 * qn + 2 * qstep];  // B(i-1), B(i)
     const double m2 = Pc[-2 * pstep], m1 = Pc[-pstep], p1 = Pc[pstep], p2 = Pc[2 * pstep];
     const double ih = D.rd[ax];
-    auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double d) {
+    // one WENO-JS correction w0 / 3 (a - 2b + c) + (w2 - 1/2) / 6 t with w0 = q1 q2 inv and
+    // w2 = 3 q0 q1 inv, the constants folded into the weights: (q1 q2) (inv / 3) and
+    // (q0 q1) (inv / 2) - 1/12; t = b - 2c + d is the same for both corrections of a cell
+    auto corr = [](double q0, double q1, double q2, double inv, double a, double b, double c, double t) {
         const double p12 = q1 * q2, p01 = q0 * q1;
-        const double w0 = p12 * inv, w2 = 3.0 * p01 * inv;
-        return w0 * (1.0 / 3.0) * (a - 2.0 * b + c) + (w2 - 0.5) * (1.0 / 6.0) * (b - 2.0 * c + d);
+        const double c0 = p12 * (inv * (1.0 / 3.0)), c2 = fma(p01, inv * 0.5, -1.0 / 12.0);
+        return fma(c0, fma(-2.0, b, a) + c, c2 * t);
     };
     const double v = ih * (1.0 / 12.0) * fma(8.0, p1 - m1, m2 - p2);
     const double Sp = fma(qY1, fma(6.0, qX1, qB1), 3.0 * qX1 * qB1);
     const double Sm = fma(qX0, fma(6.0, qY0, qB0), 3.0 * qY0 * qB0);
     const double r = rcp_refined(Sp * Sm);
-    const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], d2[1]);
-    const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], d2[3]);
+    const double t3 = fma(-2.0, d2[2], d2[1] + d2[3]);
+    const double wp = corr(qX1, qB1, qY1, Sm * r, d2[4], d2[3], d2[2], t3);
+    const double wm = corr(qY0, qB0, qX0, Sp * r, d2[0], d2[1], d2[2], t3);
     const double dp = v + ih * wp, dm = v - ih * wm;
     const double ga = sign_bits_positive(sgn) ? nonneg_max(pos_part(flip_sign(dp)), pos_part(dm))
                                               : nonneg_max(pos_part(dp), pos_part(flip_sign(dm)));
