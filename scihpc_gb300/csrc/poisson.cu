@@ -3029,24 +3029,36 @@ int Poisson::residual(const double *rhs, const double *p, double *norm, cudaStre
     return SCIHPC_OK;
 }
 
+// n V-cycles captured as one CUDA graph (on the private capture stream), as a solve runs them,
+// and timed by events around its replay on `s` (after one untimed replay); *ms is the time of
+// all n.
 int Poisson::time_vcycles(const double *rhs, double *p, int n, float *ms, cudaStream_t s) {
     use_conditional = false;
     begin(rhs, p, 0, s);
+    if (!cap_stream) SCIHPC_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    SCIHPC_CUDA(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < n; ++k) {
+        if (fp32_) vcycle<float>(cap_stream);
+        else vcycle<double>(cap_stream);
+    }
+    SCIHPC_CUDA(cudaStreamEndCapture(cap_stream, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    SCIHPC_CUDA(ie);
     cudaEvent_t e0, e1;
     SCIHPC_CUDA(cudaEventCreate(&e0));
     SCIHPC_CUDA(cudaEventCreate(&e1));
-    if (fp32_) vcycle<float>(s);   // warm
-    else vcycle<double>(s);
+    SCIHPC_CUDA(cudaGraphLaunch(ge, s));   // warm
     SCIHPC_CUDA(cudaEventRecord(e0, s));
-    for (int k = 0; k < n; ++k) {
-        if (fp32_) vcycle<float>(s);
-        else vcycle<double>(s);
-    }
+    SCIHPC_CUDA(cudaGraphLaunch(ge, s));
     SCIHPC_CUDA(cudaEventRecord(e1, s));
     SCIHPC_CUDA(cudaEventSynchronize(e1));
     SCIHPC_CUDA(cudaEventElapsedTime(ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaGraphExecDestroy(ge);
     SCIHPC_CUDA(cudaGetLastError());
     return SCIHPC_OK;
 }
