@@ -1896,10 +1896,10 @@ int TwoPhaseGpu::step(int nsteps, bool use_graph) {
 // Godunov gradient, the redistance source and the lambda fields of stage 1: k_reinit_a2d in
 // 2D, k_reinit_a3d in 3D) on the session's stream, captured as one CUDA graph and timed by
 // events around its replay, as the kernel runs inside the captured step.  (Issued one by one
-// from the host, the launches of the 2D kernel took 16.4 us each whatever the kernel, against
-// 15.6 us of kernel time in a launch list with cold caches: the host's launch rate, not the
-// kernel, set that figure.)  The kernel reads phi, sign and delta and rewrites the same outputs
-// each time, so the launches are identical.
+// from the host as ordinary launches, three different versions of the 2D kernel each measured
+// 16.4 us per launch, against 15.6 us of kernel time for one of them in a launch list with
+// cold caches: a per-launch floor outside the kernel.)  The kernel reads phi, sign and delta
+// and rewrites the same outputs each time, so the launches are identical.
 int TwoPhaseGpu::time_reinit_gradient(int n, float *ms) {
     if (n < 1) return SCIHPC_ERR_ARG;
     auto launch = [&]() {
