@@ -44,7 +44,7 @@ REINIT_FLOPS_2D = 262
 # not captured); the command that made each is in the summary file.
 REINIT_TRAFFIC_BYTES = 838485   # read 838,485 B, write 0 B (mean of three launches)
 REINIT_TRAFFIC_SRC = "profiles/reinit_2d_128x256_traffic.md"
-REINIT_SHARE = 0.225   # profiles/twophase_step_128x256_launches.md
+REINIT_SHARE = 0.211   # profiles/twophase_step_128x256_launches.md
 VCYCLE_256_TRAFFIC_BYTES = 1436369067   # read 1.088 GB + write 0.348 GB, mean of three V-cycles
 VCYCLE_256_TRAFFIC_SRC = "profiles/poisson_256cubed_vcycle_traffic.md"
 
