@@ -220,7 +220,9 @@ int scihpc_twophase_upload(scihpc_twophase *tp, const char *name, const double *
 int scihpc_twophase_download(scihpc_twophase *tp, const char *name, double *host);
 /* The same for n fields at once: one asynchronous copy per field on the session's stream and a
  * single synchronisation before returning (the host buffers may be reused on return), instead
- * of one round trip per field.  Every name is checked before any copy starts. */
+ * of one round trip per field.  Every name is checked before any copy starts.  Like the
+ * single-field calls these have no counterpart in the reference, whose fields live in host
+ * memory (scalar_data.h). */
 int scihpc_twophase_upload_many(scihpc_twophase *tp, int n, const char *const *names, const double *const *host);
 int scihpc_twophase_download_many(scihpc_twophase *tp, int n, const char *const *names, double *const *host);
 /* Device pointer of a named field (for zero-copy use by callers). */
